@@ -1,0 +1,81 @@
+"""Builds libmcpm.so (the C-ABI of include/mcpm.h) in-tree for sm_103a.
+
+Each CUDA translation unit is compiled in parallel with nvcc, then linked into
+one shared library next to this file.  The particle kernels are compiled with
+``--fmad=false``: the FP64 path then rounds every multiply and add separately,
+as the reference does, and the compensated FP32 sums stay exact.
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(HERE)
+CSRC = os.path.join(HERE, "csrc")
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(HERE, "libmcpm.so")
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "--fmad=false", "-Xcompiler", "-fPIC,-O2",
+           "-Xptxas", "-warn-spills", "--expt-relaxed-constexpr"]
+SOURCES = ["mcpm_session.cu", "mcpm_kernels.cu", "mcpm_forces.cu"]
+
+
+def nvcc():
+    p = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not os.path.exists(p):
+        raise RuntimeError("nvcc not found")
+    return p
+
+
+def _run(cmd):
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("build failed: %s\n%s%s" % (" ".join(cmd), r.stdout, r.stderr))
+    return r.stdout + r.stderr
+
+
+def _deps():
+    out = [os.path.join(REPO, "include", "mcpm.h")]
+    for f in os.listdir(CSRC):
+        if f.endswith((".h", ".cuh")):
+            out.append(os.path.join(CSRC, f))
+    return out
+
+
+def build(force=False, verbose=False):
+    os.makedirs(BUILD, exist_ok=True)
+    hdrs = _deps()
+    hdr_t = max(os.path.getmtime(h) for h in hdrs)
+    objs, todo = [], []
+    for src in SOURCES:
+        s = os.path.join(CSRC, src)
+        o = os.path.join(BUILD, src.replace(".cu", ".o"))
+        objs.append(o)
+        if force or not os.path.exists(o) or os.path.getmtime(o) < max(os.path.getmtime(s), hdr_t):
+            todo.append((s, o))
+    cc = nvcc()
+    logs = []
+
+    def comp(so):
+        s, o = so
+        return _run([cc, *ARCH, *NVFLAGS, "-c", s, "-o", o])
+
+    if todo:
+        with ThreadPoolExecutor(max_workers=len(todo)) as ex:
+            logs = list(ex.map(comp, todo))
+    if todo or not os.path.exists(LIB):
+        _run([cc, *ARCH, "-shared", "-o", LIB, *objs])
+    if verbose:
+        for l in logs:
+            if l.strip():
+                print(l)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(force="--force" in sys.argv, verbose=True))

@@ -1,0 +1,161 @@
+// mcpm_device.cuh -- device helpers shared by the particle-step kernels:
+// counter-based Philox draws, the reference's scalar laws (Y(n), mu(T)),
+// compensated FP32 accumulation and warp / block reductions.
+#pragma once
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+#include "../../include/mcpm.h"
+#include "mcpm_internal.h"
+
+namespace mcpm {
+
+// ------------------------------------------------------------------ Philox
+// Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11): 10 rounds of two
+// 32x32->64 multiplies, key bumped by the Weyl constants between rounds.
+__device__ __forceinline__ uint4 philox(uint4 c, uint2 k) {
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    uint32_t hi0 = __umulhi(0xD2511F53u, c.x), lo0 = 0xD2511F53u * c.x;
+    uint32_t hi1 = __umulhi(0xCD9E8D57u, c.z), lo1 = 0xCD9E8D57u * c.z;
+    c = make_uint4(hi1 ^ c.y ^ k.x, lo1, hi0 ^ c.w ^ k.y, lo0);
+    k.x += 0x9E3779B9u;
+    k.y += 0xBB67AE85u;
+  }
+  return c;
+}
+__device__ __forceinline__ uint4 philox(uint64_t seed, uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3) {
+  return philox(make_uint4(c0, c1, c2, c3), make_uint2((uint32_t)seed, (uint32_t)(seed >> 32)));
+}
+
+__device__ __forceinline__ double u01d(uint32_t x) { return ((double)x + 0.5) * (1.0 / 4294967296.0); }
+// 24-bit uniform in (0,1), exact in float
+__device__ __forceinline__ float u01f(uint32_t x) { return ((float)(x >> 8) + 0.5f) * (1.0f / 16777216.0f); }
+__device__ __forceinline__ int pick(uint32_t r, int n) { return (int)(((uint64_t)r * (uint64_t)n) >> 32); }
+
+constexpr double kTwoPi = 6.283185307179586476925286766559;
+
+template <typename real> struct Normals3 { real z0, z1, z2; };
+
+// three standard normals (Box-Muller on the four Philox words)
+template <typename real> __device__ __forceinline__ Normals3<real> normals3(uint4 r);
+template <> __device__ __forceinline__ Normals3<double> normals3<double>(uint4 r) {
+  double a = sqrt(-2.0 * log(u01d(r.x)));
+  double b = sqrt(-2.0 * log(u01d(r.z)));
+  double s1, c1;
+  sincos(kTwoPi * u01d(r.y), &s1, &c1);
+  return {a * c1, a * s1, b * cos(kTwoPi * u01d(r.w))};
+}
+template <> __device__ __forceinline__ Normals3<float> normals3<float>(uint4 r) {
+  float a = sqrtf(-2.0f * logf(u01f(r.x)));
+  float b = sqrtf(-2.0f * logf(u01f(r.z)));
+  float s1, c1;
+  sincospif(2.0f * u01f(r.y), &s1, &c1);
+  return {a * c1, a * s1, b * cospif(2.0f * u01f(r.w))};
+}
+
+// --------------------------------------------------------------- laws
+// increase_collision_rate, src/Main_Functions.cpp:1906-1915
+__device__ __forceinline__ double ycoll(double n, double b) {
+  double nb = n * b;
+  return 1.0 + 0.625 * n * b + 0.2869 * (nb * nb) + 0.115 * pow(nb, 3.0);
+}
+// scale_mu, src/Main_Functions.cpp:1970-1973 (pow(x, 0.5) == sqrt(x) exactly)
+__device__ __forceinline__ double scale_mu(double T, const DevConsts& k) {
+  double r = T / k.T0;
+  return k.mu * (k.visp == 0.5 ? sqrt(r) : pow(r, k.visp));
+}
+
+// ---------------------------------------------------- compensated sums
+// Knuth TwoSum: s + e == a + b exactly (needs separate rounding: the kernels
+// are compiled with --fmad=false).
+struct CSum {
+  float hi, lo;
+};
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = a + b;
+  float bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+__device__ __forceinline__ void cadd(CSum& acc, float x) {
+  float s, e;
+  two_sum(acc.hi, x, s, e);
+  acc.hi = s;
+  acc.lo += e;
+}
+__device__ __forceinline__ CSum ccombine(CSum a, CSum b) {
+  float s, e;
+  two_sum(a.hi, b.hi, s, e);
+  e += a.lo + b.lo;
+  CSum r;
+  r.hi = s + e;
+  r.lo = e - (r.hi - s);
+  return r;
+}
+__device__ __forceinline__ double cvalue(CSum a) { return (double)a.hi + (double)a.lo; }
+
+// accumulator abstraction: double sums in FP64 mode, compensated float in FP32
+template <typename real> struct Acc;
+template <> struct Acc<double> {
+  double v;
+  __device__ __forceinline__ void zero() { v = 0.0; }
+  __device__ __forceinline__ void add(double x) { v += x; }
+  __device__ __forceinline__ double get() const { return v; }
+  __device__ __forceinline__ void shfl_xor(int m) { v += __shfl_xor_sync(0xffffffffu, v, m); }
+  __device__ __forceinline__ void merge(const Acc& o) { v += o.v; }
+};
+template <> struct Acc<float> {
+  CSum c;
+  __device__ __forceinline__ void zero() { c.hi = 0.f; c.lo = 0.f; }
+  __device__ __forceinline__ void add(float x) { cadd(c, x); }
+  __device__ __forceinline__ double get() const { return cvalue(c); }
+  __device__ __forceinline__ void shfl_xor(int m) {
+    CSum o;
+    o.hi = __shfl_xor_sync(0xffffffffu, c.hi, m);
+    o.lo = __shfl_xor_sync(0xffffffffu, c.lo, m);
+    c = ccombine(c, o);
+  }
+  __device__ __forceinline__ void merge(const Acc& o) { c = ccombine(c, o.c); }
+};
+
+// Reduce K accumulators over a tile of TILE threads (32 = one warp, or a
+// whole block).  Every thread of the tile gets the totals.  smem must hold
+// K * (TILE/32) Acc entries when TILE > 32.
+template <typename real, int K, int TILE>
+__device__ __forceinline__ void tile_reduce(Acc<real> (&a)[K], Acc<real>* smem) {
+#pragma unroll
+  for (int m = 16; m >= 1; m >>= 1)
+#pragma unroll
+    for (int q = 0; q < K; ++q) a[q].shfl_xor(m);
+  if constexpr (TILE > 32) {
+    constexpr int W = TILE / 32;
+    int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0)
+#pragma unroll
+      for (int q = 0; q < K; ++q) smem[q * W + warp] = a[q];
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < K; ++q) {
+      Acc<real> t = smem[q * W];
+      for (int w = 1; w < W; ++w) t.merge(smem[q * W + w]);
+      a[q] = t;
+    }
+  }
+}
+
+__device__ __forceinline__ void raise_status(uint32_t* status, uint32_t bits) {
+  if (bits) atomicOr(status, bits);
+}
+
+// warp-aggregated atomic increment of a per-cell counter
+__device__ __forceinline__ void count_key(int32_t* cnt, int key, bool active) {
+  unsigned am = __ballot_sync(0xffffffffu, active);
+  if (!active) return;
+  unsigned peers = __match_any_sync(am, key);
+  int leader = __ffs(peers) - 1;
+  if ((int)(threadIdx.x & 31) == leader) atomicAdd(&cnt[key], __popc(peers));
+}
+
+}  // namespace mcpm

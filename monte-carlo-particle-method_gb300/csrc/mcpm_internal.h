@@ -1,0 +1,137 @@
+// mcpm_internal.h -- session state and kernel launchers shared by the
+// translation units of libmcpm.
+#pragma once
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/mcpm.h"
+
+namespace mcpm {
+
+// Internal per-cell fields stored after the exported ones (enum mcpm_cell_field).
+enum {
+  CFI_Y = MCPM_CF_COUNT,  // Y(n)
+  CFI_A1,                 // exp(-dt/tau)
+  CFI_A2,                 // (1 - exp(-dt/tau)) tau
+  CFI_A3,                 // sqrt((1 - exp(-2 dt/tau)) kT/m)
+  CFI_3KT,                // 3 kb T / m
+  CF_DEV_COUNT
+};
+
+// Stages of the fused per-cell particle pass (update kernel).
+enum : uint32_t {
+  ST_RNG = 1u << 0,       // draw + whiten normals (random_generator)
+  ST_STORE_XI = 1u << 1,  // keep whitened normals in the session (split mode)
+  ST_LOAD_XI = 1u << 2,   // take whitened normals from the session (split mode)
+  ST_FP = 1u << 3,        // Velocity_FP_parallel
+  ST_LR = 1u << 4,        // long-range kick U2 += F2 dt
+  ST_DFP = 1u << 5,       // DFP_extra_streaming
+  ST_BC1 = 1u << 6,       // apply_BC before store_old_positions
+  ST_OLD = 1u << 7,       // store_old_positions
+  ST_STREAM = 1u << 8,    // free flight
+  ST_BC2 = 1u << 9,       // apply_BC after streaming
+  ST_BC3 = 1u << 10,      // the third apply_BC of the loop body
+  ST_KEY = 1u << 11       // bin the new positions for the next cell_update
+};
+
+// Counter-stream ids for the Philox draws (third counter word).
+enum : uint32_t { RNG_FP = 0, RNG_BC = 1, RNG_ESMC = 2, RNG_BIN = 3, RNG_ESMC_ACC = 4, RNG_ESMC_M = 5 };
+
+struct DevConsts {
+  int N0, N1, C;
+  int dir0, dir1;
+  int problem, model, long_range;
+  double dx, dy, dz, L0, L1;
+  double sigma, m, kb, n, Fn, T0, mu, visp, b, dt, phi, eqdist, ast, bst;
+  double Tw[4], Uw[4];
+  uint64_t seed;
+};
+
+// One set of device particle arrays (SoA).  real is float or double.
+struct PBuf {
+  void *x1, *x2, *U1, *U2, *U3, *x1o, *x2o;
+  int32_t* pid;
+};
+
+// Work-list bookkeeping written by the scan kernel.
+enum { WL_NSMALL = 0, WL_NBIG = 1, WL_MAXCNT = 2, WL_N = 3, WL_COUNT = 4 };
+// Work counters used by the persistent kernels (reset by the scan kernel).
+enum { WK_MOM_BIG = 0, WK_MOM_SMALL, WK_UPD_BIG, WK_UPD_SMALL, WK_COUNT };
+
+struct Tuning {
+  int wcap;         // cells with more particles than this go to the block path
+  int block;        // threads per block of the persistent kernels
+  int bcap;         // particles per cell staged in shared memory (block path)
+  int grid_mom;     // persistent grid sizes
+  int grid_upd;
+};
+
+struct Session {
+  mcpm_config cfg{};
+  DevConsts k{};
+  int prec = MCPM_FP64;
+  size_t rsz = 8;  // sizeof(real)
+  int64_t N = 0, cap = 0;
+  int C = 0;
+  bool need_old = false;  // diffuse walls read positions before the last flight
+  bool need_x1 = false;
+  PBuf P[2]{};
+  int cur = 0;
+  int32_t* key = nullptr;       // cell of each slot, current layout
+  int32_t* cnt = nullptr;       // [C] particles per cell, current layout
+  int32_t* cnt_next = nullptr;  // [C] counts accumulated for the next layout
+  int32_t* off = nullptr;       // [C+1]
+  int32_t* cursor = nullptr;    // [C]
+  int32_t* list_small = nullptr;
+  int32_t* list_big = nullptr;
+  int32_t* wl = nullptr;        // [WL_COUNT]
+  int32_t* work = nullptr;      // [WK_COUNT]
+  double* cell = nullptr;       // [CF_DEV_COUNT][C]
+  double* xi = nullptr;         // [3][cap] whitened normals, slot order
+  double* inj = nullptr;        // [3][cap] injected raw normals, particle-id order
+  double* stage = nullptr;      // [5][cap] host<->device staging (double)
+  double* faces = nullptr;      // [4][N1+1] long-range face scratch
+  uint32_t* status = nullptr;
+  cudaStream_t stream = nullptr;
+  int step = 0;
+  int bc_calls = 0;             // apply_BC calls in the current step (split mode)
+  int rng_mode = MCPM_RNG_PHILOX;
+  bool keys_current = false;    // key/cnt_next describe the current positions
+  bool sorted = false;          // layout is sorted by key, cnt/off/lists valid
+  bool needs_rebin = false;     // positions moved since the last binning
+  bool have_particles = false;
+  bool omega_init = false;      // ESMC majorant initialised (src/main.cpp:250-269)
+  int num_sms = 0;
+  Tuning tune{};
+  int64_t launches = 0;
+  cudaStream_t own_stream = nullptr;
+  // profiling mode: CUDA-event pairs per launch, by kernel class
+  bool prof = false;
+  struct ProfRec { cudaEvent_t a, b; int cls; int n; };
+  std::vector<ProfRec> prof_recs;
+  std::vector<cudaEvent_t> prof_pool;
+  // graph of one fused step
+  cudaGraphExec_t graph = nullptr;
+  uint64_t graph_sig = 0;
+  std::string err;
+};
+
+// ------------------------------------------------------------- launchers
+// (defined in mcpm_kernels.cu / mcpm_forces.cu; each returns the number of
+// kernels it launched)
+int launch_bin(Session& s, int bin_step);
+int launch_scan(Session& s);
+int launch_scatter(Session& s);
+int launch_moments(Session& s);
+int launch_solve(Session& s, int with_alpha);
+int launch_update(Session& s, uint32_t stages, int bc_call_base);
+int launch_esmc(Session& s);
+int launch_long_range(Session& s);
+int launch_init_omega(Session& s);
+int launch_convert_in(Session& s, int64_t n);
+int launch_convert_out(Session& s, int64_t n);
+
+}  // namespace mcpm

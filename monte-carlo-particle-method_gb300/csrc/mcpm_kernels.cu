@@ -1,0 +1,1128 @@
+// mcpm_kernels.cu -- the particle-step kernels for sm_103a.
+//
+// Layout: particle state is SoA (x1, x2, U1, U2, U3, pid [, x1_old, x2_old])
+// kept sorted by cell in HBM; a cell is the contiguous segment
+// [off[c], off[c] + cnt[c]).  Per-cell data is SoA doubles [field][C].
+//
+// Per step (mcpm_step): scan (counts -> offsets + work lists) -> scatter
+// (reorder into the new cell order) -> moments -> per-cell FP64 solves ->
+// [long-range force] -> fused update (random_generator + Velocity_FP +
+// kick + DFP_extra_streaming + BCs + free flight + re-binning).
+//
+// Cells are processed by persistent blocks fed from two prefix-sum work
+// lists: cells with more than `wcap` particles are handled by a whole block,
+// the rest by one warp each.  Compiled with --fmad=false: every multiply
+// and add rounds separately, as in the reference (x86-64 without FMA) and as
+// the compensated FP32 sums require.
+#include <cfloat>
+
+#include "mcpm_device.cuh"
+
+namespace mcpm {
+
+#define FULL 0xffffffffu
+
+template <typename real> struct PT {
+  real *x1, *x2, *U1, *U2, *U3, *x1o, *x2o;
+  int32_t* pid;
+};
+template <typename real> static PT<real> pt(const PBuf& b) {
+  return {(real*)b.x1, (real*)b.x2, (real*)b.U1, (real*)b.U2, (real*)b.U3, (real*)b.x1o, (real*)b.x2o, b.pid};
+}
+
+// ======================================================= binning (a1)
+// cell_update binning, src/Main_Functions.cpp:2231-2266, with the face
+// jitter of :2238-2247 drawn from Philox.  Particles outside [0, Len] raise
+// MCPM_ERR_OUT_OF_BOX (the reference exits); a particle on the far wall is
+// binned into the last cell.
+template <typename real>
+__device__ __forceinline__ int bin_one(real x1, real x2, int pid, int step, const DevConsts& k, uint32_t& bad) {
+  int j = 0;
+  if (k.dir0 == 1) {
+    j = (int)floor(x1 / (real)k.dx);
+    if (!(x1 >= (real)0 && x1 <= (real)k.L0)) bad |= MCPM_ERR_OUT_OF_BOX;
+  }
+  real dy = (real)k.dy;
+  int kk = (int)floor(x2 / dy);
+  if (!(x2 >= (real)0 && x2 <= (real)k.L1)) bad |= MCPM_ERR_OUT_OF_BOX;
+  if (kk > 0 && kk < k.N1 - 1) {
+    if (fabs(x2 - dy * kk) < (real)1e-15 || fabs(x2 - dy * (kk + 1)) < (real)1e-15) {
+      uint4 r = philox(k.seed, (uint32_t)pid, (uint32_t)step, RNG_BIN, 0u);
+      int sgn = (u01d(r.x) > 0.5) ? 1 : -1;
+      kk = (int)floor((x2 + (real)1e-14 * sgn) / dy);
+    }
+  }
+  j = j < 0 ? 0 : (j > k.N0 - 1 ? k.N0 - 1 : j);
+  kk = kk < 0 ? 0 : (kk > k.N1 - 1 ? k.N1 - 1 : kk);
+  return kk * k.N0 + j;
+}
+
+template <typename real>
+__global__ void k_bin(PT<real> p, int64_t n, DevConsts k, int step, int32_t* key, int32_t* cnt_next,
+                      uint32_t* status) {
+  uint32_t bad = 0;
+  for (int64_t i0 = (int64_t)blockIdx.x * blockDim.x; i0 < n; i0 += (int64_t)gridDim.x * blockDim.x) {
+    int64_t i = i0 + threadIdx.x;
+    bool act = i < n;
+    int c = 0;
+    if (act) {
+      real x1 = p.x1 ? p.x1[i] : (real)0;
+      c = bin_one<real>(x1, p.x2[i], p.pid[i], step, k, bad);
+      key[i] = c;
+    }
+    count_key(cnt_next, c, act);
+  }
+  raise_status(status, bad);
+}
+
+// ================================================ scan + work lists
+// One block: counts of the new layout -> cnt, exclusive offsets, the two
+// work lists (cells with <= wcap particles, cells with more), max count;
+// resets the accumulation counters and cursors for the next step.
+constexpr int SCAN_T = 1024;
+__global__ void __launch_bounds__(SCAN_T) k_scan(int32_t* cnt_next, int32_t* cnt, int32_t* off, int32_t* cursor,
+                                                 int32_t* list_small, int32_t* list_big, int32_t* wl,
+                                                 int32_t* work, int C, int wcap) {
+  __shared__ int sh[3][SCAN_T / 32];
+  __shared__ int shmax[SCAN_T / 32];
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  const int items = (C + SCAN_T - 1) / SCAN_T;
+  const int b = t * items, e = min(C, b + items);
+  int s_cnt = 0, s_small = 0, s_big = 0, mx = 0;
+  for (int c = b; c < e; ++c) {
+    int v = cnt_next[c];
+    s_cnt += v;
+    if (v > wcap) s_big++; else s_small++;
+    mx = max(mx, v);
+  }
+  // inclusive warp scans of the three totals
+  int v0 = s_cnt, v1 = s_small, v2 = s_big;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    int a0 = __shfl_up_sync(FULL, v0, d), a1 = __shfl_up_sync(FULL, v1, d), a2 = __shfl_up_sync(FULL, v2, d);
+    if (lane >= d) { v0 += a0; v1 += a1; v2 += a2; }
+  }
+#pragma unroll
+  for (int d = 16; d >= 1; d >>= 1) mx = max(mx, __shfl_xor_sync(FULL, mx, d));
+  if (lane == 31) { sh[0][warp] = v0; sh[1][warp] = v1; sh[2][warp] = v2; }
+  if (lane == 0) shmax[warp] = mx;
+  __syncthreads();
+  if (warp == 0) {
+    int w0 = sh[0][lane], w1 = sh[1][lane], w2 = sh[2][lane], m2 = shmax[lane];
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      int a0 = __shfl_up_sync(FULL, w0, d), a1 = __shfl_up_sync(FULL, w1, d), a2 = __shfl_up_sync(FULL, w2, d);
+      if (lane >= d) { w0 += a0; w1 += a1; w2 += a2; }
+    }
+#pragma unroll
+    for (int d = 16; d >= 1; d >>= 1) m2 = max(m2, __shfl_xor_sync(FULL, m2, d));
+    sh[0][lane] = w0; sh[1][lane] = w1; sh[2][lane] = w2;
+    if (lane == 31) {
+      wl[WL_N] = w0; wl[WL_NSMALL] = w1; wl[WL_NBIG] = w2; wl[WL_MAXCNT] = m2;
+    }
+  }
+  __syncthreads();
+  int base0 = (warp ? sh[0][warp - 1] : 0) + v0 - s_cnt;
+  int base1 = (warp ? sh[1][warp - 1] : 0) + v1 - s_small;
+  int base2 = (warp ? sh[2][warp - 1] : 0) + v2 - s_big;
+  for (int c = b; c < e; ++c) {
+    int v = cnt_next[c];
+    cnt[c] = v;
+    off[c] = base0;
+    base0 += v;
+    if (v > wcap) list_big[base2++] = c; else list_small[base1++] = c;
+    cnt_next[c] = 0;
+    cursor[c] = 0;
+  }
+  if (t == SCAN_T - 1) off[C] = base0;
+  if (t < WK_COUNT) work[t] = 0;
+}
+
+// ============================================================ scatter
+// Reorders the particle arrays into cell order: slot = off[key] + rank,
+// ranks handed out per cell by warp-aggregated atomics.
+template <typename real>
+__global__ void k_scatter(PT<real> src, PT<real> dst, const int32_t* key, const int32_t* off, int32_t* cursor,
+                          int64_t n) {
+  const int lane = threadIdx.x & 31;
+  for (int64_t i0 = (int64_t)blockIdx.x * blockDim.x; i0 < n; i0 += (int64_t)gridDim.x * blockDim.x) {
+    int64_t i = i0 + threadIdx.x;
+    bool act = i < n;
+    int c = act ? key[i] : -1;
+    unsigned am = __ballot_sync(FULL, act);
+    if (act) {
+      unsigned peers = __match_any_sync(am, c);
+      int leader = __ffs(peers) - 1;
+      int rank = __popc(peers & ((1u << lane) - 1u));
+      int bse = 0;
+      if (lane == leader) bse = atomicAdd(&cursor[c], __popc(peers));
+      bse = __shfl_sync(peers, bse, leader);
+      int64_t d = (int64_t)off[c] + bse + rank;
+      if (src.x1) dst.x1[d] = src.x1[i];
+      dst.x2[d] = src.x2[i];
+      dst.U1[d] = src.U1[i];
+      dst.U2[d] = src.U2[i];
+      dst.U3[d] = src.U3[i];
+      dst.pid[d] = src.pid[i];
+      if (src.x1o) dst.x1o[d] = src.x1o[i];
+      if (src.x2o) dst.x2o[d] = src.x2o[i];
+    }
+  }
+}
+
+// ================================================ cell access helpers
+struct CellRef {
+  const double* cell;
+  int C;
+  __device__ __forceinline__ double operator()(int f, int c) const { return cell[(size_t)f * C + c]; }
+};
+
+// volume of cell c exactly as make_cells builds it, src/myIO.cpp:1456-1465
+__device__ __forceinline__ double cell_volume(int c, const DevConsts& k) {
+  int j = c % k.N0, kk = c / k.N0;
+  double d0 = (double)j * k.dx, d1 = (double)(j + 1) * k.dx;
+  double d2 = (double)kk * k.dy, d3 = (double)(kk + 1) * k.dy;
+  double d4 = 0.0 * k.dz, d5 = 1.0 * k.dz;
+  return (d1 - d0) * (d3 - d2) * (d5 - d4);
+}
+
+// persistent two-phase scheduler: block-sized cells first, then one warp per
+// small cell.  fn_big(c) is called by the whole block, fn_small(c) by a warp.
+template <typename FB, typename FS>
+__device__ __forceinline__ void schedule_cells(const int32_t* list_big, const int32_t* list_small, const int32_t* wl,
+                                               int32_t* work, int wk_big, int wk_small, FB fn_big, FS fn_small) {
+  __shared__ int item;
+  const int nbig = wl[WL_NBIG], nsmall = wl[WL_NSMALL];
+  for (;;) {
+    if (threadIdx.x == 0) item = atomicAdd(&work[wk_big], 1);
+    __syncthreads();
+    int it = item;
+    __syncthreads();
+    if (it >= nbig) break;
+    fn_big(list_big[it]);
+  }
+  const int lane = threadIdx.x & 31;
+  for (;;) {
+    int it = 0;
+    if (lane == 0) it = atomicAdd(&work[wk_small], 1);
+    it = __shfl_sync(FULL, it, 0);
+    if (it >= nsmall) break;
+    fn_small(list_small[it]);
+  }
+}
+
+// ============================================================ moments (a4)
+// src/Main_Functions.cpp:2461-2593: mean velocity, then the central moments
+// up to fifth order about it; T, n, gamma* per cell.
+template <typename real> struct MomArgs {
+  DevConsts k;
+  double* cell;
+  const int32_t *off, *cnt, *list_small, *list_big, *wl;
+  int32_t* work;
+  const real *U1, *U2, *U3;
+};
+
+template <typename real, int TILE>
+__device__ void moments_cell(int c, const MomArgs<real>& a, Acc<real>* red) {
+  const int t = (TILE == 32) ? (threadIdx.x & 31) : threadIdx.x;
+  const int s0 = a.off[c], n = a.cnt[c];
+  Acc<real> u[3];
+#pragma unroll
+  for (int q = 0; q < 3; ++q) u[q].zero();
+  for (int i = t; i < n; i += TILE) {
+    u[0].add(a.U1[s0 + i]);
+    u[1].add(a.U2[s0 + i]);
+    u[2].add(a.U3[s0 + i]);
+  }
+  tile_reduce<real, 3, TILE>(u, red);
+  const double weight = (double)n;
+  double us0 = 0.0, us1 = 0.0, us2 = 0.0;
+  if (n > 0) { us0 = u[0].get() / weight; us1 = u[1].get() / weight; us2 = u[2].get() / weight; }
+  const real m0 = (real)us0, m1 = (real)us1, m2 = (real)us2;
+  Acc<real> q[29];
+#pragma unroll
+  for (int j = 0; j < 29; ++j) q[j].zero();
+  for (int i = t; i < n; i += TILE) {
+    real Mp1 = a.U1[s0 + i] - m0, Mp2 = a.U2[s0 + i] - m1, Mp3 = a.U3[s0 + i] - m2;
+    real energy = Mp1 * Mp1 + Mp2 * Mp2 + Mp3 * Mp3;
+    q[0].add(Mp1); q[1].add(Mp2); q[2].add(Mp3);
+    q[3].add(Mp1 * Mp1); q[4].add(Mp1 * Mp2); q[5].add(Mp1 * Mp3);
+    q[6].add(Mp2 * Mp2); q[7].add(Mp2 * Mp3); q[8].add(Mp3 * Mp3);
+    q[9].add(Mp1 * Mp1 * Mp1); q[10].add(Mp1 * Mp1 * Mp2); q[11].add(Mp1 * Mp1 * Mp3);
+    q[12].add(Mp1 * Mp2 * Mp2); q[13].add(Mp1 * Mp2 * Mp3); q[14].add(Mp1 * Mp3 * Mp3);
+    q[15].add(Mp2 * Mp2 * Mp2); q[16].add(Mp2 * Mp2 * Mp3); q[17].add(Mp2 * Mp3 * Mp3);
+    q[18].add(Mp3 * Mp3 * Mp3);
+    q[19].add(Mp1 * Mp1 * energy); q[20].add(Mp1 * Mp2 * energy); q[21].add(Mp1 * Mp3 * energy);
+    q[22].add(Mp2 * Mp2 * energy); q[23].add(Mp2 * Mp3 * energy); q[24].add(Mp3 * Mp3 * energy);
+    q[25].add(Mp1 * energy * energy); q[26].add(Mp2 * energy * energy); q[27].add(Mp3 * energy * energy);
+    q[28].add(energy);
+  }
+  tile_reduce<real, 29, TILE>(q, red);
+  if (t != 0) return;
+  const DevConsts& k = a.k;
+  double* cl = a.cell;
+  const int C = k.C;
+  auto W = [&](int f, double v) { cl[(size_t)f * C + c] = v; };
+  double P[6], M3[10], M4[6], M5[3], Mp[3], DM2, DM4 = 0.0, Q[3] = {0.0, 0.0, 0.0};
+  for (int j = 0; j < 3; ++j) Mp[j] = q[j].get();
+  for (int j = 0; j < 6; ++j) P[j] = q[3 + j].get();
+  for (int j = 0; j < 10; ++j) M3[j] = q[9 + j].get();
+  for (int j = 0; j < 6; ++j) M4[j] = q[19 + j].get();
+  for (int j = 0; j < 3; ++j) M5[j] = q[25 + j].get();
+  DM2 = q[28].get();
+  if (n > 0) {
+    for (int j = 0; j < 6; ++j) P[j] = P[j] / weight;
+    for (int j = 0; j < 10; ++j) M3[j] = M3[j] / weight;
+    for (int j = 0; j < 6; ++j) M4[j] = M4[j] / weight;
+    for (int j = 0; j < 3; ++j) M5[j] = M5[j] / weight;
+    for (int j = 0; j < 3; ++j) Mp[j] = Mp[j] / weight;
+    DM2 = DM2 / weight;
+    DM4 = M4[0] + M4[3] + M4[5];
+    Q[0] = M3[0] + M3[3] + M3[5];
+    Q[1] = M3[1] + M3[6] + M3[8];
+    Q[2] = M3[2] + M3[7] + M3[9];
+  }
+  W(MCPM_CF_NUM_INSIDE, (double)n);
+  W(MCPM_CF_U_SPACE + 0, us0); W(MCPM_CF_U_SPACE + 1, us1); W(MCPM_CF_U_SPACE + 2, us2);
+  for (int j = 0; j < 6; ++j) W(MCPM_CF_PIJ + j, P[j]);
+  for (int j = 0; j < 10; ++j) W(MCPM_CF_M3 + j, M3[j]);
+  for (int j = 0; j < 6; ++j) W(MCPM_CF_M4 + j, M4[j]);
+  for (int j = 0; j < 3; ++j) W(MCPM_CF_M5 + j, M5[j]);
+  for (int j = 0; j < 3; ++j) W(MCPM_CF_Q + j, Q[j]);
+  for (int j = 0; j < 3; ++j) W(MCPM_CF_MP + j, Mp[j]);
+  W(MCPM_CF_DM2, DM2);
+  W(MCPM_CF_DM4, DM4);
+  double T = k.m * DM2 / (3.0 * k.kb);
+  double nn = 1 * k.Fn * weight / cell_volume(c, k);
+  double Y = ycoll(nn, k.b);
+  W(MCPM_CF_T, T);
+  W(MCPM_CF_N, nn);
+  W(CFI_Y, Y);
+  if (weight > 1e-14) W(MCPM_CF_GAMMA_ST, -0.001 * (nn * k.b * Y / (k.kb * T / k.m)));
+}
+
+template <typename real>
+__global__ void __launch_bounds__(256) k_moments(MomArgs<real> a) {
+  __shared__ Acc<real> red[29 * 8];
+  schedule_cells(
+      a.list_big, a.list_small, a.wl, a.work, WK_MOM_BIG, WK_MOM_SMALL,
+      [&](int c) { moments_cell<real, 256>(c, a, red); }, [&](int c) { moments_cell<real, 32>(c, a, red); });
+}
+
+// ===================================================== per-cell solves
+// Gauss_Jordan, src/Math_Func.cpp:165-232, restated exactly: scaled partial
+// pivoting over the full row, reciprocal-then-multiply factor, full-row
+// updates, back substitution.
+__device__ __forceinline__ int gj_maxmag(const double* a, int n) {
+  double b = fabs(a[0]);
+  int l = 0;
+  for (int i = 0; i < n; ++i)
+    if (fabs(b) < fabs(a[i])) { b = fabs(a[i]); l = i; }
+  return l;
+}
+template <int n>
+__device__ void gauss_jordan(double* A, double* R, double* x) {
+  double z[n];
+  for (int i = 0; i < n - 1; ++i) {
+    for (int ii = 0; ii < n; ++ii) z[ii] = 0.0;
+    int k = 0;
+    for (int j = i; j < n; ++j) {
+      const double* row = &A[j * n];
+      int bb = gj_maxmag(row, n);
+      z[k] = fabs(row[i]) / fabs(row[bb]);
+      k++;
+    }
+    k = gj_maxmag(z, n);
+    k = i + k;
+    if (i != k && k < n) {
+      for (int j = 0; j < n; ++j) { double b = A[i * n + j]; A[i * n + j] = A[k * n + j]; A[k * n + j] = b; }
+      double c = R[i]; R[i] = R[k]; R[k] = c;
+    }
+    for (int j = i + 1; j < n; ++j) {
+      double F = (1.0 / A[i * n + i]) * A[j * n + i];
+      for (int kk = 0; kk < n; ++kk) A[j * n + kk] = A[j * n + kk] - F * A[i * n + kk];
+      R[j] = R[j] - F * R[i];
+    }
+  }
+  for (int i = n - 1; i >= 0; --i) {
+    double a = 0;
+    for (int j = i + 1; j < n; ++j) a = a + A[i * n + j] * x[j];
+    x[i] = (R[i] - a) / (A[i * n + i]);
+  }
+}
+
+// One thread per cell: Lambda (src/Main_Functions.cpp:2718-2728),
+// alpha/beta (src/Fokker_Planck.cpp:200-587; its 12x12 system is three
+// uncoupled 4x4 blocks -- unknowns (alpha_3b..3b+2, beta_b) -- and Gauss_Jordan
+// on the 12x12 performs exactly the arithmetic of the three 4x4 solves),
+// c/gamma (src/Fokker_Planck.cpp:590-804, 9x9), phi (:2734-2746) and the
+// Velocity_FP_parallel constants A1..A3 (src/Fokker_Planck.cpp:1099-1112).
+__global__ void __launch_bounds__(128) k_solve(DevConsts k, double* cell, int with_alpha, int fp_model,
+                                               uint32_t* status) {
+  const int C = k.C;
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= C) return;
+  auto R = [&](int f) -> double { return cell[(size_t)f * C + c]; };
+  auto Rc = [&](int f, int cc) -> double { return cell[(size_t)f * C + cc]; };
+  auto W = [&](int f, double v) { cell[(size_t)f * C + c] = v; };
+  const double weight = R(MCPM_CF_NUM_INSIDE);
+  const int ncnt = (int)weight;
+  double P[6], M3[10], M4[6], M5[3], Q[3], Mp[3];
+  for (int j = 0; j < 6; ++j) P[j] = R(MCPM_CF_PIJ + j);
+  for (int j = 0; j < 10; ++j) M3[j] = R(MCPM_CF_M3 + j);
+  for (int j = 0; j < 6; ++j) M4[j] = R(MCPM_CF_M4 + j);
+  for (int j = 0; j < 3; ++j) { M5[j] = R(MCPM_CF_M5 + j); Q[j] = R(MCPM_CF_Q + j); Mp[j] = R(MCPM_CF_MP + j); }
+  const double DM2 = R(MCPM_CF_DM2), DM4 = R(MCPM_CF_DM4), T = R(MCPM_CF_T), n = R(MCPM_CF_N);
+  const double gst = R(MCPM_CF_GAMMA_ST);
+  const double Ycell = R(CFI_Y);
+  uint32_t bad = 0;
+  double Lam = R(MCPM_CF_LAMBDA);
+  if (weight > 1e-14) {
+    double mu = scale_mu(T, k);
+    double tau = 2.0 * mu / (n * k.kb * T);
+    double L = (P[0] - DM2 / 3.0) * ((P[3] - DM2 / 3.0) * (P[5] - DM2 / 3.0) - P[4] * P[4]);
+    L = L - P[1] * (P[1] * (P[5] - DM2 / 3.0) - P[4] * P[2]);
+    L = L + P[2] * (P[1] * P[4] - P[2] * (P[3] - DM2 / 3.0));
+    L = -L / (tau * pow(DM2, 4.0));
+    Lam = L;
+    W(MCPM_CF_LAMBDA, Lam);
+  }
+  double al[9], be[3];
+  for (int j = 0; j < 9; ++j) al[j] = R(MCPM_CF_ALPHA + j);
+  for (int j = 0; j < 3; ++j) be[j] = R(MCPM_CF_BETA + j);
+  if (fp_model) {
+    // ---------------- alpha / beta (FP_dense, step > 0)
+    if (with_alpha) {
+      if (ncnt < 2) {
+        for (int j = 0; j < 9; ++j) al[j] = 0.0;
+        for (int j = 0; j < 3; ++j) be[j] = 0.0;
+      } else {
+        const double pi = acos(-1.0);
+        double trace = P[0] + P[3] + P[5];
+        double dev[6];
+        for (int j = 0; j < 6; ++j) dev[j] = P[j];
+        dev[0] = dev[0] - (1.0 / 3.0) * trace;
+        dev[3] = dev[3] - (1.0 / 3.0) * trace;
+        dev[5] = dev[5] - (1.0 / 3.0) * trace;
+        double ma = M3[0] + M3[3] + M3[5];
+        double mb = M3[1] + M3[6] + M3[8];
+        double mc = M3[2] + M3[7] + M3[9];
+        double d = M4[0] + M4[3] + M4[5] - DM2 * DM2;
+        double Y = Ycell;
+        double p_crr = (1.0 + n * k.b * Y);
+        double mu_crr = (1.0 + 2.0 * n * k.b * Y / 5.0);
+        double k_crr = (1.0 + 3.0 * n * k.b * Y / 5.0);
+        double w = (4.0 / 9.0) * sqrt(pi) * Y * (n * n) * pow(k.sigma, 4.0) * sqrt(k.m * k.kb * T);
+        double div_U;
+        const int last = C - 1;
+        if (C == 1) div_U = 0.0;
+        else if (c == 0) div_U = (Rc(MCPM_CF_U_SPACE + 1, c + 1) - Rc(MCPM_CF_U_SPACE + 1, c)) / k.dy;
+        else if (c == k.N1 - 1 || c == last)
+          div_U = (Rc(MCPM_CF_U_SPACE + 1, c) - Rc(MCPM_CF_U_SPACE + 1, c - 1)) / k.dy;
+        else div_U = (Rc(MCPM_CF_U_SPACE + 1, c + 1) - Rc(MCPM_CF_U_SPACE + 1, c - 1)) / k.dy / 2.0;
+        W(MCPM_CF_DIVU, div_U);
+        double nbY = n * k.b * Y;
+        double coeff_mu = 3.0 * 1.002 / 5.0 * (nbY * nbY) / (1 + 2.0 * n * k.b * Y / 5.0);
+        double coeff_k = 1.002 * (nbY * nbY) / (1 + 3.0 * n * k.b * Y / 5.0) / 5.0;
+        double rhs[12];
+        rhs[0] = (mu_crr - 1.0) * dev[0] + (p_crr - 1.0) * trace / 3.0 - w * div_U / (k.m * n) + coeff_mu * dev[0] - gst * M4[0];
+        rhs[1] = (mu_crr - 1.0) * dev[1] + coeff_mu * dev[1] - gst * M4[1];
+        rhs[2] = (mu_crr - 1.0) * dev[2] + coeff_mu * dev[2] - gst * M4[2];
+        rhs[3] = (mu_crr - 1.0) * dev[1] + coeff_mu * dev[1] - gst * M4[1];
+        rhs[4] = (mu_crr - 1.0) * dev[3] + (p_crr - 1.0) * trace / 3.0 - w * div_U / (k.m * n) + coeff_mu * dev[3] - gst * M4[3];
+        rhs[5] = (mu_crr - 1.0) * dev[4] + coeff_mu * dev[4] - gst * M4[4];
+        rhs[6] = (mu_crr - 1.0) * dev[2] + coeff_mu * dev[2] - gst * M4[2];
+        rhs[7] = (mu_crr - 1.0) * dev[4] + coeff_mu * dev[4] - gst * M4[4];
+        rhs[8] = (mu_crr - 1.0) * dev[5] + (p_crr - 1.0) * trace / 3.0 - w * div_U / (k.m * n) + coeff_mu * dev[5] - gst * M4[5];
+        rhs[9] = (k_crr - 1.0) * ma + coeff_k * ma - gst * (M5[0]) + gst * (DM2 * (M3[0] + M3[3] + M3[5]));
+        rhs[10] = (k_crr - 1.0) * mb + coeff_k * mb - gst * (M5[1]) + gst * (DM2 * (M3[1] + M3[6] + M3[8]));
+        rhs[11] = (k_crr - 1.0) * mc + coeff_k * mc - gst * (M5[2]) + gst * (DM2 * (M3[2] + M3[7] + M3[9]));
+        const double m3b[3] = {ma, mb, mc};
+        for (int blk = 0; blk < 3; ++blk) {
+          double A[16], r4[4], x4[4];
+          A[0] = P[0]; A[1] = P[1]; A[2] = P[2]; A[3] = m3b[blk];
+          A[4] = P[1]; A[5] = P[3]; A[6] = P[4]; A[7] = m3b[blk];
+          A[8] = P[2]; A[9] = P[4]; A[10] = P[5]; A[11] = m3b[blk];
+          A[12] = ma; A[13] = mb; A[14] = mc; A[15] = d;
+          r4[0] = rhs[3 * blk]; r4[1] = rhs[3 * blk + 1]; r4[2] = rhs[3 * blk + 2]; r4[3] = rhs[9 + blk];
+          gauss_jordan<4>(A, r4, x4);
+          al[3 * blk] = x4[0]; al[3 * blk + 1] = x4[1]; al[3 * blk + 2] = x4[2]; be[blk] = x4[3];
+        }
+        for (int j = 0; j < 9; ++j) if (al[j] != al[j]) bad |= MCPM_ERR_NAN;
+        for (int j = 0; j < 3; ++j) if (be[j] != be[j]) bad |= MCPM_ERR_NAN;
+      }
+      for (int j = 0; j < 9; ++j) W(MCPM_CF_ALPHA + j, al[j]);
+      for (int j = 0; j < 3; ++j) W(MCPM_CF_BETA + j, be[j]);
+    }
+    // ---------------- c / gamma
+    double x[9];
+    if (ncnt < 2) {
+      for (int j = 0; j < 9; ++j) x[j] = 0.0;
+    } else {
+      double A[81], rhs[9];
+      for (int j = 0; j < 81; ++j) A[j] = 0.0;
+      for (int j = 0; j < 9; ++j) { rhs[j] = 0.0; x[j] = 0.0; }
+#define AA(r, q) A[(r) * 9 + (q)]
+      AA(0, 0) = 2.0 * P[0]; AA(0, 1) = 2.0 * P[1]; AA(0, 2) = 2.0 * P[2]; AA(0, 6) = 2.0 * Q[0];
+      AA(1, 0) = P[1]; AA(1, 1) = P[0] + P[3]; AA(1, 2) = P[4]; AA(1, 3) = P[1]; AA(1, 4) = P[2];
+      AA(1, 6) = Q[1]; AA(1, 7) = Q[0];
+      AA(2, 0) = P[2]; AA(2, 1) = P[4]; AA(2, 2) = P[0] + P[5]; AA(2, 4) = P[1]; AA(2, 5) = P[2];
+      AA(2, 6) = Q[2]; AA(2, 8) = Q[0];
+      AA(3, 1) = 2.0 * P[1]; AA(3, 3) = 2.0 * P[3]; AA(3, 4) = 2.0 * P[4]; AA(3, 7) = 2.0 * Q[1];
+      AA(4, 1) = P[2]; AA(4, 2) = P[1]; AA(4, 3) = P[4]; AA(4, 4) = P[3] + P[5]; AA(4, 5) = P[4];
+      AA(4, 7) = Q[2]; AA(4, 8) = Q[1];
+      AA(5, 2) = 2.0 * P[2]; AA(5, 4) = 2.0 * P[4]; AA(5, 5) = 2.0 * P[5]; AA(5, 8) = 2.0 * Q[2];
+      AA(6, 0) = Q[0] + 2.0 * M3[0]; AA(6, 1) = Q[1] + 4.0 * M3[1]; AA(6, 2) = Q[2] + 4.0 * M3[2];
+      AA(6, 3) = 2.0 * M3[3]; AA(6, 4) = 4.0 * M3[4]; AA(6, 5) = 2.0 * M3[5];
+      AA(6, 6) = 2.0 * M4[0] - 2.0 * P[0] * DM2; AA(6, 7) = 2.0 * M4[1] - 2.0 * P[1] * DM2;
+      AA(6, 8) = 2.0 * M4[2] - 2.0 * P[2] * DM2;
+      AA(7, 0) = 2.0 * M3[1]; AA(7, 1) = Q[0] + 4.0 * M3[3]; AA(7, 2) = 4.0 * M3[4];
+      AA(7, 3) = Q[1] + 2.0 * M3[6]; AA(7, 4) = Q[2] + 4.0 * M3[7]; AA(7, 5) = 2.0 * M3[8];
+      AA(7, 6) = 2.0 * M4[1] - 2.0 * P[1] * DM2; AA(7, 7) = 2.0 * M4[3] - 2.0 * P[3] * DM2;
+      AA(7, 8) = 2.0 * M4[4] - 2.0 * P[4] * DM2;
+      AA(8, 0) = 2.0 * M3[2]; AA(8, 1) = 4.0 * M3[4]; AA(8, 2) = Q[0] + 4.0 * M3[5];
+      AA(8, 3) = 2.0 * M3[7]; AA(8, 4) = Q[1] + 4.0 * M3[8]; AA(8, 5) = Q[2] + 2.0 * M3[9];
+      AA(8, 6) = 2.0 * M4[2] - 2.0 * P[2] * DM2; AA(8, 7) = 2.0 * M4[4] - 2.0 * P[4] * DM2;
+      AA(8, 8) = 2.0 * M4[5] - 2.0 * P[5] * DM2;
+      AA(6, 6) += DM4 - (DM2) * (DM2);
+      AA(7, 7) += DM4 - (DM2) * (DM2);
+      AA(8, 8) += DM4 - (DM2) * (DM2);
+#undef AA
+      double Pr = 2.0 / 3.0;
+      double Y = (k.model == MCPM_MODEL_FP_DENSE) ? Ycell : 1.0;
+      double mu = scale_mu(T, k);
+      double tau = 2.0 * mu / (n * k.kb * T);
+      for (int j = 0; j < 6; ++j) rhs[j] = -2.0 * Lam * M4[j];
+      rhs[6] = Y * (3.0 / tau - 2.0 * Pr / tau) * Q[0];
+      rhs[7] = Y * (3.0 / tau - 2.0 * Pr / tau) * Q[1];
+      rhs[8] = Y * (3.0 / tau - 2.0 * Pr / tau) * Q[2];
+      rhs[6] += Lam * (-3.0 * M5[0] + DM2 * Q[0] + 2.0 * (P[0] * Q[0] + P[1] * Q[1] + P[2] * Q[2]));
+      rhs[7] += Lam * (-3.0 * M5[1] + DM2 * Q[1] + 2.0 * (P[1] * Q[0] + P[3] * Q[1] + P[4] * Q[2]));
+      rhs[8] += Lam * (-3.0 * M5[2] + DM2 * Q[2] + 2.0 * (P[2] * Q[0] + P[4] * Q[1] + P[5] * Q[2]));
+      gauss_jordan<9>(A, rhs, x);
+    }
+    for (int j = 0; j < 6; ++j) W(MCPM_CF_C + j, x[j]);
+    for (int j = 0; j < 3; ++j) W(MCPM_CF_GAMMA + j, x[6 + j]);
+    // ---------------- Velocity_FP_parallel per-cell constants
+    if (ncnt > 1) {
+      double mu = scale_mu(T, k);
+      double tau = 2.0 * mu / (n * k.kb * T);
+      double Y = (k.model == MCPM_MODEL_FP_DENSE) ? Ycell : 1.0;
+      tau = tau / Y;
+      W(CFI_A1, exp(-k.dt / tau));
+      W(CFI_A3, sqrt((1.0 - exp(-2.0 * k.dt / tau)) * k.kb * T / (1.0 * k.m)));
+      W(CFI_A2, (1.0 - exp(-k.dt / tau)) * tau);
+    }
+  }
+  W(CFI_3KT, 3.0 * k.kb * T / k.m);
+  W(MCPM_CF_PHI + 0, al[0] * Mp[0] + al[1] * Mp[1] + al[2] * Mp[2]);
+  W(MCPM_CF_PHI + 1, al[3] * Mp[0] + al[4] * Mp[1] + al[5] * Mp[2]);
+  W(MCPM_CF_PHI + 2, al[6] * Mp[0] + al[7] * Mp[1] + al[8] * Mp[2]);
+  raise_status(status, bad);
+}
+
+// ================================================== boundary conditions
+template <typename real> struct PState {
+  real x1, x2, x1o, x2o, u1, u2, u3;
+};
+
+// BC_specular_reflection, src/Main_Functions.cpp:6399-6525
+template <typename real>
+__device__ __forceinline__ void bc_specular(PState<real>& s, const DevConsts& k, uint32_t& bad) {
+  const real Tol1 = (real)1e-16, Tol2 = (real)-1e-16, L0 = (real)k.L0, L1 = (real)k.L1;
+  int it = 0;
+  for (;;) {
+    if (k.dir0 == 1) {
+      if (s.x1 - L0 > Tol2) { s.u1 = -s.u1; s.x1 = s.x1 - (real)2.0 * fabs(s.x1 - L0); }
+      else if (s.x1 < Tol1) { s.u1 = -s.u1; s.x1 = s.x1 + (real)2.0 * fabs(s.x1); }
+    }
+    if (k.dir1 == 1) {
+      if (s.x2 - L1 > Tol2) { s.u2 = -s.u2; s.x2 = s.x2 - (real)2.0 * fabs(s.x2 - L1); }
+      else if (s.x2 < Tol1) { s.u2 = -s.u2; s.x2 = s.x2 + (real)2.0 * fabs(s.x2); }
+    }
+    bool done = true;
+    if (k.dir0 == 1 && (s.x1 - L0 > (real)0 || s.x1 < (real)0)) done = false;
+    if (k.dir1 == 1 && (s.x2 - L1 > (real)0 || s.x2 < (real)0)) done = false;
+    if (done) break;
+    if (++it > 64) { bad |= MCPM_ERR_BC_LOOP; break; }
+  }
+}
+
+template <typename real>
+__device__ __forceinline__ void bc_periodic(PState<real>& s, const DevConsts& k) {
+  if (k.dir0 == 1) s.x1 = s.x1 - (real)k.L0 * floor(s.x1 / (real)k.L0);
+  if (k.dir1 == 1) s.x2 = s.x2 - (real)k.L1 * floor(s.x2 / (real)k.L1);
+}
+
+// one diffuse re-emission draw: Rayleigh factor + two normals
+template <typename real>
+__device__ __forceinline__ void wall_draw(int pid, int step, int call, int it, const DevConsts& k, real& ray,
+                                          real& z0, real& z1) {
+  uint4 r = philox(k.seed, (uint32_t)pid, (uint32_t)step, RNG_BC, (uint32_t)((call << 8) | (it & 0xff)));
+  if constexpr (sizeof(real) == 8) {
+    ray = sqrt(-log(u01d(r.x)));
+    double a = sqrt(-2.0 * log(u01d(r.y)));
+    double sn, cs;
+    sincos(kTwoPi * u01d(r.z), &sn, &cs);
+    z0 = a * cs; z1 = a * sn;
+  } else {
+    ray = sqrtf(-logf(u01f(r.x)));
+    float a = sqrtf(-2.0f * logf(u01f(r.y)));
+    float sn, cs;
+    sincospif(2.0f * u01f(r.z), &sn, &cs);
+    z0 = a * cs; z1 = a * sn;
+  }
+}
+
+// intersect_3D_x / _y, src/Main_Functions.cpp:2757-2806 (no motion in z)
+template <typename real>
+__device__ __forceinline__ real isect_x(real x, real xo, real yo, real xn, real yn) {
+  real n0 = xn - xo, n1 = yn - yo, n2 = 0;
+  real size = 0;
+  size += n0 * n0; size += n1 * n1; size += n2 * n2;
+  size = sqrt(size);
+  n0 = n0 / size; n1 = n1 / size;
+  if (fabs(n0) > (real)1e-16) return (n1 / n0) * (x - xo) + yo;
+  return yn;
+}
+template <typename real>
+__device__ __forceinline__ real isect_y(real y, real xo, real yo, real xn, real yn) {
+  real n0 = xn - xo, n1 = yn - yo, n2 = 0;
+  real size = 0;
+  size += n0 * n0; size += n1 * n1; size += n2 * n2;
+  size = sqrt(size);
+  n0 = n0 / size; n1 = n1 / size;
+  if (fabs(n1) > (real)1e-16) return (n0 / n1) * (y - yo) + xo;
+  return xn;
+}
+
+// BC_thermal_wall_3D, src/Main_Functions.cpp:4917-5250, in 2-D
+template <typename real>
+__device__ void bc_thermal_wall(PState<real>& s, int call, int pid, int step, const DevConsts& k, uint32_t& bad) {
+  const real eps = (real)1e-15, L0 = (real)k.L0, L1 = (real)k.L1, sg = (real)k.sigma, DT = (real)k.dt;
+  const real mm = (real)k.m, kb = (real)k.kb;
+  real dt = DT;
+  int it = 0;
+  const real Ue0 = fabs(s.x1 - s.x1o) / DT, Ue1 = fabs(s.x2 - s.x2o) / DT;
+  for (;;) {
+    real dt_remain, xw, yw, tU0, ray, z0, z1;
+    if (it > 20) { bad |= MCPM_ERR_BC_LOOP; break; }
+    if (dt < (real)1e-15) {
+      if (s.x1 < eps) s.x1 = eps;
+      else if (s.x1 > L0 - eps) s.x1 = L0 - eps;
+      if (s.x2 < eps) s.x2 = eps;
+      else if (s.x2 > L1 - eps) s.x2 = L1 - eps;
+    }
+    int wall = -1;
+    if (s.x1 - L0 > (real)0) wall = 3;
+    else if (s.x1 < (real)0) wall = 2;
+    else if (s.x2 > L1 - sg - eps) wall = 1;
+    else if (s.x2 < sg + eps) wall = 0;
+    if (wall >= 0) {
+      const real Tw = (real)k.Tw[wall], Uw = (real)k.Uw[wall];
+      if (wall >= 2) {  // x walls
+        xw = (wall == 3) ? L0 - eps : eps;
+        if (fabs(s.x1o - s.x1) > (real)1e-15) yw = isect_x<real>(xw, s.x1o, s.x2o, s.x1, s.x2);
+        else yw = (real)0.5 * (s.x2o + s.x2);
+        tU0 = (fabs(dt - DT) < (real)1e-15) ? Ue0 : s.u1;
+        wall_draw<real>(pid, step, call, it, k, ray, z0, z1);
+        real un = sqrt((real)2.0 * kb * Tw / (mm)) * ray;
+        s.u1 = (wall == 3) ? -un : un;
+        s.u2 = sqrt(kb * Tw / (mm)) * z0 + ((real)1.0 * Uw);
+        s.u3 = sqrt(kb * Tw / (mm)) * z1;
+        if (dt > (real)1e-15) {
+          dt_remain = fabs((s.x1 - xw) / tU0);
+          dt_remain = dt < dt_remain ? dt : dt_remain;
+          s.x1 = xw + dt_remain * s.u1;
+          s.x2 = yw + dt_remain * s.u2;
+          dt = dt - dt_remain;
+          s.x1o = xw; s.x2o = yw;
+        } else {
+          s.x1 = xw;
+        }
+      } else {  // y walls at sigma and Len1 - sigma
+        yw = (wall == 1) ? L1 - sg - eps : sg + eps;
+        xw = isect_y<real>(yw, s.x1o, s.x2o, s.x1, s.x2);
+        tU0 = (fabs(dt - DT) < (real)1e-15) ? Ue1 : s.u2;
+        wall_draw<real>(pid, step, call, it, k, ray, z0, z1);
+        s.u1 = sqrt(kb * Tw / (mm)) * z0 + ((real)1.0 * Uw);
+        real un = sqrt((real)2.0 * kb * Tw / (mm)) * ray;
+        s.u2 = (wall == 1) ? -un : un;
+        s.u3 = sqrt(kb * Tw / (mm)) * z1;
+        if (dt > (real)1e-15) {
+          dt_remain = fabs((s.x2 - yw) / tU0);
+          dt_remain = dt < dt_remain ? dt : dt_remain;
+          s.x1 = xw + dt_remain * s.u1;
+          s.x2 = yw + dt_remain * s.u2;
+          dt = dt - dt_remain;
+          s.x1o = xw; s.x2o = yw;
+        } else {
+          s.x2 = yw;
+        }
+      }
+    }
+    if (s.x1 - L0 < (real)0 && s.x1 > (real)0 && s.x2 - L1 < (real)0 && s.x2 > (real)0) break;
+    it++;
+  }
+}
+
+// BC_wall, src/Main_Functions.cpp:4816-4914 (1-D: diffuse y = 0, specular y = Len1)
+template <typename real>
+__device__ void bc_wall(PState<real>& s, int call, int pid, int step, const DevConsts& k, uint32_t& bad) {
+  const real eps = (real)1e-15, L1 = (real)k.L1, DT = (real)k.dt, mm = (real)k.m, kb = (real)k.kb;
+  const real Tw = (real)k.Tw[0], Uw = (real)k.Uw[0];
+  real dt = DT;
+  int it = 0;
+  const real Ue1 = fabs(s.x2 - s.x2o) / DT;
+  for (;;) {
+    if (it > 20) { bad |= MCPM_ERR_BC_LOOP; break; }
+    if (dt < (real)1e-15) {
+      if (s.x2 < eps) s.x2 = eps;
+      else if (s.x2 > L1 - eps) s.x2 = L1 - eps;
+    } else if (s.x2 > L1) {
+      s.u2 = -s.u2;
+      s.x2 = s.x2 - (real)2.0 * fabs(s.x2 - L1);
+    } else if (s.x2 < (real)0) {
+      real yw = eps, ray, z0, z1;
+      real tU0 = (fabs(dt - DT) < (real)1e-15) ? Ue1 : s.u2;
+      wall_draw<real>(pid, step, call, it, k, ray, z0, z1);
+      s.u1 = sqrt(kb * Tw / (mm)) * z0 + ((real)1.0 * Uw);
+      s.u2 = sqrt((real)2.0 * kb * Tw / (mm)) * ray;
+      s.u3 = sqrt(kb * Tw / mm) * z1;
+      if (dt > (real)1e-15) {
+        real dt_remain = fabs((s.x2 - yw) / tU0);
+        dt_remain = dt < dt_remain ? dt : dt_remain;
+        s.x2 = yw + dt_remain * s.u2;
+        dt = dt - dt_remain;
+        s.x2o = yw;
+      } else {
+        s.x2 = yw;
+      }
+    }
+    if (s.x2 - L1 < (real)0 && s.x2 > (real)0) break;
+    it++;
+  }
+}
+
+// apply_BC, src/Main_Functions.cpp:1451-1492
+template <typename real>
+__device__ __forceinline__ void apply_bc(PState<real>& s, int call, int pid, int step, const DevConsts& k,
+                                         uint32_t& bad) {
+  switch (k.problem) {
+    case MCPM_PROBLEM_CLOSED_BOX: bc_specular<real>(s, k, bad); break;
+    case MCPM_PROBLEM_COUETTE: bc_thermal_wall<real>(s, call, pid, step, k, bad); break;
+    case MCPM_PROBLEM_WALL: bc_wall<real>(s, call, pid, step, k, bad); break;
+    case MCPM_PROBLEM_PERIODIC: bc_periodic<real>(s, k); break;
+    default: break;
+  }
+}
+
+// ====================================================== fused update
+template <typename real> struct UpdArgs {
+  DevConsts k;
+  const double* cell;
+  const int32_t *off, *cnt, *list_small, *list_big, *wl;
+  int32_t* work;
+  PT<real> p;
+  int32_t* key_out;
+  int32_t* cnt_next;
+  const double* inj;
+  double* xi;
+  int64_t cap;
+  uint32_t* status;
+  int step, bin_step, rng_mode, bc_call_base;
+  uint32_t stages;
+  int wcap, bcap;
+};
+
+template <typename real>
+__device__ __forceinline__ void raw_normals(const UpdArgs<real>& a, int64_t p, real& z0, real& z1, real& z2) {
+  int pid = a.p.pid[p];
+  if (a.rng_mode == MCPM_RNG_INJECTED) {
+    z0 = (real)a.inj[pid]; z1 = (real)a.inj[a.cap + pid]; z2 = (real)a.inj[2 * a.cap + pid];
+  } else {
+    Normals3<real> z = normals3<real>(philox(a.k.seed, (uint32_t)pid, (uint32_t)a.step, RNG_FP, 0u));
+    z0 = z.z0; z1 = z.z1; z2 = z.z2;
+  }
+}
+
+// random_generator (src/Fokker_Planck.cpp:20-145) + Velocity_FP_parallel
+// (:1065-1182) + long-range kick (src/Main_Functions.cpp:3937, :3578) +
+// DFP_extra_streaming (src/Fokker_Planck.cpp:904-946) + apply_BC /
+// store_old_positions / stream_particles (src/main.cpp:478-514) + the binning
+// of the next cell_update, for one cell, by a tile of TILE threads.
+// xs stages the cell's normals in shared memory when the cell fits.
+template <typename real, int TILE>
+__device__ void update_cell(int c, const UpdArgs<real>& a, real* xs, int xcap, Acc<real>* red) {
+  const int t = (TILE == 32) ? (threadIdx.x & 31) : threadIdx.x;
+  const int64_t s0 = a.off[c];
+  const int n = a.cnt[c];
+  const DevConsts& k = a.k;
+  const uint32_t st = a.stages;
+  const bool rng = st & ST_RNG, fp = st & ST_FP, load_xi = st & ST_LOAD_XI, store_xi = st & ST_STORE_XI;
+  const bool staged = rng && n <= xcap;
+  const CellRef R{a.cell, k.C};
+  const real Us0 = (real)R(MCPM_CF_U_SPACE + 0, c), Us1 = (real)R(MCPM_CF_U_SPACE + 1, c),
+             Us2 = (real)R(MCPM_CF_U_SPACE + 2, c);
+  PT<real> P = a.p;
+  real mean0 = 0, mean1 = 0, mean2 = 0, rms0 = 1, rms1 = 1, rms2 = 1;
+  double frac1 = 0.0;
+  // ---- pass A: draws, their per-cell sums, sum |M'|^2
+  if (rng || fp) {
+    Acc<real> s4[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) s4[q].zero();
+    for (int i = t; i < n; i += TILE) {
+      int64_t p = s0 + i;
+      if (rng) {
+        real z0, z1, z2;
+        raw_normals(a, p, z0, z1, z2);
+        if (staged) { xs[3 * i] = z0; xs[3 * i + 1] = z1; xs[3 * i + 2] = z2; }
+        s4[0].add(z0); s4[1].add(z1); s4[2].add(z2);
+      }
+      if (fp) {
+        real m1 = P.U1[p] - Us0, m2 = P.U2[p] - Us1, m3 = P.U3[p] - Us2;
+        s4[3].add(m1 * m1 + m2 * m2 + m3 * m3);
+      }
+    }
+    tile_reduce<real, 4, TILE>(s4, red);
+    frac1 = s4[3].get();
+    if (rng) {
+      mean0 = (real)(s4[0].get() / (1.0 * n));
+      mean1 = (real)(s4[1].get() / (1.0 * n));
+      mean2 = (real)(s4[2].get() / (1.0 * n));
+      // ---- pass B: per-cell RMS of the centred draws
+      Acc<real> s3[3];
+#pragma unroll
+      for (int q = 0; q < 3; ++q) s3[q].zero();
+      for (int i = t; i < n; i += TILE) {
+        real z0, z1, z2;
+        if (staged) { z0 = xs[3 * i]; z1 = xs[3 * i + 1]; z2 = xs[3 * i + 2]; }
+        else raw_normals(a, s0 + i, z0, z1, z2);
+        real d0 = z0 - mean0, d1 = z1 - mean1, d2 = z2 - mean2;
+        s3[0].add(d0 * d0); s3[1].add(d1 * d1); s3[2].add(d2 * d2);
+      }
+      tile_reduce<real, 3, TILE>(s3, red);
+      rms0 = (real)sqrt(s3[0].get() / (1.0 * n));
+      rms1 = (real)sqrt(s3[1].get() / (1.0 * n));
+      rms2 = (real)sqrt(s3[2].get() / (1.0 * n));
+    }
+  }
+  // whitened normal of the i-th particle of the cell
+  auto xiw = [&](int i, real& z0, real& z1, real& z2) {
+    int64_t p = s0 + i;
+    if (load_xi) {
+      z0 = (real)a.xi[p]; z1 = (real)a.xi[a.cap + p]; z2 = (real)a.xi[2 * a.cap + p];
+      return;
+    }
+    if (staged) { z0 = xs[3 * i]; z1 = xs[3 * i + 1]; z2 = xs[3 * i + 2]; }
+    else raw_normals(a, p, z0, z1, z2);
+    if (n > 1) {
+      z0 = (z0 - mean0) / rms0; z1 = (z1 - mean1) / rms1; z2 = (z2 - mean2) / rms2;
+    }
+  };
+  // per-cell FP constants
+  real A1 = 0, A2 = 0, A3 = 0, eq = 0, Lam = 0, cc[6], gm[3], Q[3];
+  if (fp && n > 1) {
+    A1 = (real)R(CFI_A1, c); A2 = (real)R(CFI_A2, c); A3 = (real)R(CFI_A3, c);
+    eq = (real)R(CFI_3KT, c); Lam = (real)R(MCPM_CF_LAMBDA, c);
+#pragma unroll
+    for (int j = 0; j < 6; ++j) cc[j] = (real)R(MCPM_CF_C + j, c);
+#pragma unroll
+    for (int j = 0; j < 3; ++j) { gm[j] = (real)R(MCPM_CF_GAMMA + j, c); Q[j] = (real)R(MCPM_CF_Q + j, c); }
+  }
+  // the Ornstein-Uhlenbeck update of M' with the cubic drift
+  auto mnew = [&](int i, real& m1, real& m2, real& m3) {
+    int64_t p = s0 + i;
+    m1 = P.U1[p] - Us0; m2 = P.U2[p] - Us1; m3 = P.U3[p] - Us2;
+    if (n > 1) {
+      real z0, z1, z2;
+      xiw(i, z0, z1, z2);
+      real energy = m1 * m1 + m2 * m2 + m3 * m3;
+      real d0 = cc[0] * m1 + cc[1] * m2 + cc[2] * m3;
+      d0 += gm[0] * (energy - eq);
+      d0 += Lam * (m1 * energy - Q[0]);
+      real d1 = cc[1] * m1 + cc[3] * m2 + cc[4] * m3;
+      d1 += gm[1] * (energy - eq);
+      d1 += Lam * (m2 * energy - Q[1]);
+      real d2 = cc[2] * m1 + cc[4] * m2 + cc[5] * m3;
+      d2 += gm[2] * (energy - eq);
+      d2 += Lam * (m3 * energy - Q[2]);
+      m1 = A1 * m1 + A2 * d0 + A3 * z0;
+      m2 = A1 * m2 + A2 * d1 + A3 * z1;
+      m3 = A1 * m3 + A2 * d2 + A3 * z2;
+    } else {
+      m1 = 0; m2 = 0; m3 = 0;
+    }
+  };
+  // ---- pass C: whitened normals (staged / stored) and sum |M'_new|^2
+  double frac2 = 0.0;
+  uint32_t bad = 0;
+  if (rng && (staged || store_xi)) {
+    for (int i = t; i < n; i += TILE) {
+      real z0, z1, z2;
+      xiw(i, z0, z1, z2);
+      if (store_xi) {
+        int64_t p = s0 + i;
+        a.xi[p] = (double)z0; a.xi[a.cap + p] = (double)z1; a.xi[2 * a.cap + p] = (double)z2;
+      }
+      if (staged) { xs[3 * i] = z0; xs[3 * i + 1] = z1; xs[3 * i + 2] = z2; }
+    }
+  }
+  // after this point xiw must return the whitened values from the stage
+  const real sm0 = mean0, sm1 = mean1, sm2 = mean2;
+  if (staged) { mean0 = 0; mean1 = 0; mean2 = 0; rms0 = 1; rms1 = 1; rms2 = 1; }
+  (void)sm0; (void)sm1; (void)sm2;
+  if (fp) {
+    Acc<real> f2[1];
+    f2[0].zero();
+    for (int i = t; i < n; i += TILE) {
+      real m1, m2, m3;
+      mnew(i, m1, m2, m3);
+      if (m2 != m2) bad |= MCPM_ERR_NAN;
+      f2[0].add(m1 * m1 + m2 * m2 + m3 * m3);
+    }
+    tile_reduce<real, 1, TILE>(f2, red);
+    frac2 = f2[0].get();
+  }
+  const uint32_t pos_stages = ST_LR | ST_DFP | ST_BC1 | ST_OLD | ST_STREAM | ST_BC2 | ST_BC3 | ST_KEY;
+  if (!(fp || (st & pos_stages))) {
+    raise_status(a.status, bad);
+    return;
+  }
+  // ---- pass D: final velocities, then the position pipeline
+  const real scale = (fp && n > 1) ? (real)sqrt(fabs(frac1 / frac2)) : (real)1;
+  const real F2dt = (st & ST_LR) ? (real)(R(MCPM_CF_F2, c) * k.dt) : (real)0;
+  real al[6], be0 = 0, be1 = 0, gst = 0, eqd = 0, q0 = 0, q1 = 0, ph0 = 0, ph1 = 0;
+  if (st & ST_DFP) {
+#pragma unroll
+    for (int j = 0; j < 6; ++j) al[j] = (real)R(MCPM_CF_ALPHA + j, c);
+    be0 = (real)R(MCPM_CF_BETA + 0, c); be1 = (real)R(MCPM_CF_BETA + 1, c);
+    gst = (real)R(MCPM_CF_GAMMA_ST, c); eqd = (real)R(CFI_3KT, c);
+    q0 = (real)(R(MCPM_CF_M3 + 0, c)); q1 = (real)(R(MCPM_CF_M3 + 1, c));
+    ph0 = (real)R(MCPM_CF_PHI + 0, c); ph1 = (real)R(MCPM_CF_PHI + 1, c);
+  }
+  const real M3_3 = (st & ST_DFP) ? (real)R(MCPM_CF_M3 + 3, c) : (real)0;
+  const real M3_5 = (st & ST_DFP) ? (real)R(MCPM_CF_M3 + 5, c) : (real)0;
+  const real M3_6 = (st & ST_DFP) ? (real)R(MCPM_CF_M3 + 6, c) : (real)0;
+  const real M3_8 = (st & ST_DFP) ? (real)R(MCPM_CF_M3 + 8, c) : (real)0;
+  const real dtr = (real)k.dt;
+  const int iters = (n + TILE - 1) / TILE;
+  for (int r = 0; r < iters; ++r) {
+    const int i = r * TILE + t;
+    const bool act = i < n;
+    int key = 0;
+    if (act) {
+      const int64_t p = s0 + i;
+      PState<real> s;
+      s.u1 = P.U1[p]; s.u2 = P.U2[p]; s.u3 = P.U3[p];
+      s.x1 = P.x1 ? P.x1[p] : (real)0;
+      s.x2 = P.x2[p];
+      s.x1o = P.x1o ? P.x1o[p] : (real)0;
+      s.x2o = P.x2o ? P.x2o[p] : (real)0;
+      const int pid = P.pid[p];
+      if (fp) {
+        if (n > 1) {
+          real m1, m2, m3;
+          mnew(i, m1, m2, m3);
+          s.u1 = m1 * scale + Us0; s.u2 = m2 * scale + Us1; s.u3 = m3 * scale + Us2;
+        } else {
+          s.u1 = Us0; s.u2 = Us1; s.u3 = Us2;
+        }
+      }
+      if (st & ST_LR) s.u2 = s.u2 + F2dt;
+      if (st & ST_DFP) {
+        real e = (s.u1 - Us0) * (s.u1 - Us0) + (s.u2 - Us1) * (s.u2 - Us1) + (s.u3 - Us2) * (s.u3 - Us2);
+        if (k.dir0 == 1) {
+          s.x1 = s.x1 + dtr * ((s.u1 - Us0) * al[0] + (s.u2 - Us1) * al[1] + (s.u3 - Us2) * al[2] + be0 * (e - eqd)) +
+                 gst * ((s.u1 - Us1) * e - q0 - M3_3 - M3_5) * dtr;
+          s.x1 = s.x1 - dtr * ph0;
+        }
+        if (k.dir1 == 1) {
+          s.x2 = s.x2 + dtr * ((s.u1 - Us0) * al[3] + (s.u2 - Us1) * al[4] + (s.u3 - Us2) * al[5] + be1 * (e - eqd)) +
+                 gst * ((s.u2 - Us1) * e - q1 - M3_6 - M3_8) * dtr;
+          s.x2 = s.x2 - dtr * ph1;
+        }
+      }
+      if (st & ST_BC1) apply_bc<real>(s, a.bc_call_base + 0, pid, a.step, k, bad);
+      if (st & ST_OLD) { s.x1o = s.x1; s.x2o = s.x2; }
+      if (st & ST_STREAM) {
+        if (k.dir0 == 1) s.x1 = s.x1 + dtr * s.u1;
+        if (k.dir1 == 1) s.x2 = s.x2 + dtr * s.u2;
+      }
+      if (st & ST_BC2) apply_bc<real>(s, a.bc_call_base + 1, pid, a.step, k, bad);
+      if (st & ST_BC3) apply_bc<real>(s, a.bc_call_base + 2, pid, a.step, k, bad);
+      P.U1[p] = s.u1; P.U2[p] = s.u2; P.U3[p] = s.u3;
+      if (P.x1) P.x1[p] = s.x1;
+      P.x2[p] = s.x2;
+      if (P.x1o) P.x1o[p] = s.x1o;
+      if (P.x2o) P.x2o[p] = s.x2o;
+      if (st & ST_KEY) {
+        key = bin_one<real>(s.x1, s.x2, pid, a.bin_step, k, bad);
+        a.key_out[p] = key;
+      }
+    }
+    if (st & ST_KEY) {
+      if (TILE == 32) count_key(a.cnt_next, key, act);
+      else count_key(a.cnt_next, key, act);
+    }
+  }
+  raise_status(a.status, bad);
+}
+
+template <typename real>
+__global__ void __launch_bounds__(256) k_update(UpdArgs<real> a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ Acc<real> red[4 * 8];
+  real* xs = reinterpret_cast<real*>(smem_raw);
+  const int warp = threadIdx.x >> 5;
+  schedule_cells(
+      a.list_big, a.list_small, a.wl, a.work, WK_UPD_BIG, WK_UPD_SMALL,
+      [&](int c) { update_cell<real, 256>(c, a, xs, a.bcap, red); },
+      [&](int c) { update_cell<real, 32>(c, a, xs + (size_t)warp * 3 * a.wcap, a.wcap, red); });
+}
+
+// ========================================================= host<->device
+template <typename real>
+__global__ void k_convert_in(PT<real> p, const double* stage, int64_t n, int64_t cap) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    if (p.x1) p.x1[i] = (real)stage[i];
+    p.x2[i] = (real)stage[cap + i];
+    p.U1[i] = (real)stage[2 * cap + i];
+    p.U2[i] = (real)stage[3 * cap + i];
+    p.U3[i] = (real)stage[4 * cap + i];
+    p.pid[i] = (int32_t)i;
+    if (p.x1o) p.x1o[i] = p.x1 ? p.x1[i] : (real)0;
+    if (p.x2o) p.x2o[i] = p.x2[i];
+  }
+}
+template <typename real>
+__global__ void k_convert_out(PT<real> p, double* stage, int64_t n, int64_t cap) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    int q = p.pid[i];
+    stage[q] = p.x1 ? (double)p.x1[i] : 0.0;
+    stage[cap + q] = (double)p.x2[i];
+    stage[2 * cap + q] = (double)p.U1[i];
+    stage[3 * cap + q] = (double)p.U2[i];
+    stage[4 * cap + q] = (double)p.U3[i];
+  }
+}
+
+// ============================================================ launchers
+static inline int grid_for(int64_t n, int block, int max_blocks) {
+  int64_t g = (n + block - 1) / block;
+  if (g < 1) g = 1;
+  if (g > max_blocks) g = max_blocks;
+  return (int)g;
+}
+
+template <typename real> static int bin_impl(Session& s, int bin_step) {
+  PT<real> p = pt<real>(s.P[s.cur]);
+  // every key is recomputed: counts start from zero, whatever was pending
+  cudaMemsetAsync(s.cnt_next, 0, (size_t)s.C * sizeof(int32_t), s.stream);
+  k_bin<real><<<grid_for(s.N, 256, s.num_sms * 8), 256, 0, s.stream>>>(p, s.N, s.k, bin_step, s.key, s.cnt_next,
+                                                                         s.status);
+  return 1;
+}
+int launch_bin(Session& s, int bin_step) { return s.prec == MCPM_FP32 ? bin_impl<float>(s, bin_step) : bin_impl<double>(s, bin_step); }
+
+int launch_scan(Session& s) {
+  k_scan<<<1, SCAN_T, 0, s.stream>>>(s.cnt_next, s.cnt, s.off, s.cursor, s.list_small, s.list_big, s.wl, s.work,
+                                      s.C, s.tune.wcap);
+  return 1;
+}
+
+template <typename real> static int scatter_impl(Session& s) {
+  PT<real> src = pt<real>(s.P[s.cur]), dst = pt<real>(s.P[1 - s.cur]);
+  k_scatter<real><<<grid_for(s.N, 256, s.num_sms * 8), 256, 0, s.stream>>>(src, dst, s.key, s.off, s.cursor, s.N);
+  s.cur = 1 - s.cur;
+  return 1;
+}
+int launch_scatter(Session& s) { return s.prec == MCPM_FP32 ? scatter_impl<float>(s) : scatter_impl<double>(s); }
+
+template <typename real> static int moments_impl(Session& s) {
+  PT<real> p = pt<real>(s.P[s.cur]);
+  MomArgs<real> a{s.k, s.cell, s.off, s.cnt, s.list_small, s.list_big, s.wl, s.work, p.U1, p.U2, p.U3};
+  k_moments<real><<<s.tune.grid_mom, 256, 0, s.stream>>>(a);
+  return 1;
+}
+int launch_moments(Session& s) { return s.prec == MCPM_FP32 ? moments_impl<float>(s) : moments_impl<double>(s); }
+
+int launch_solve(Session& s, int with_alpha) {
+  int fp = (s.cfg.model == MCPM_MODEL_FP_DENSE || s.cfg.model == MCPM_MODEL_FP_IDEAL_GAS) ? 1 : 0;
+  k_solve<<<(s.C + 127) / 128, 128, 0, s.stream>>>(s.k, s.cell, with_alpha, fp, s.status);
+  return 1;
+}
+
+template <typename real> static size_t update_smem(const Session& s) {
+  size_t a = (size_t)s.tune.bcap, b = (size_t)(s.tune.block / 32) * s.tune.wcap;
+  return 3 * sizeof(real) * (a > b ? a : b);
+}
+
+template <typename real> static int update_impl(Session& s, uint32_t stages, int bc_call_base) {
+  UpdArgs<real> a;
+  a.k = s.k;
+  a.cell = s.cell;
+  a.off = s.off; a.cnt = s.cnt; a.list_small = s.list_small; a.list_big = s.list_big; a.wl = s.wl;
+  a.work = s.work;
+  a.p = pt<real>(s.P[s.cur]);
+  a.key_out = s.key;
+  a.cnt_next = s.cnt_next;
+  a.inj = s.inj;
+  a.xi = s.xi;
+  a.cap = s.cap;
+  a.status = s.status;
+  a.step = s.step;
+  a.bin_step = s.step + 1;
+  a.rng_mode = s.rng_mode;
+  a.bc_call_base = bc_call_base;
+  a.stages = stages;
+  a.wcap = s.tune.wcap;
+  a.bcap = s.tune.bcap;
+  size_t sm = update_smem<real>(s);
+  k_update<real><<<s.tune.grid_upd, 256, sm, s.stream>>>(a);
+  return 1;
+}
+int launch_update(Session& s, uint32_t stages, int bc_call_base) {
+  return s.prec == MCPM_FP32 ? update_impl<float>(s, stages, bc_call_base) : update_impl<double>(s, stages, bc_call_base);
+}
+
+template <typename real> static int conv_in_impl(Session& s, int64_t n) {
+  k_convert_in<real><<<grid_for(n, 256, s.num_sms * 8), 256, 0, s.stream>>>(pt<real>(s.P[s.cur]), s.stage, n, s.cap);
+  return 1;
+}
+int launch_convert_in(Session& s, int64_t n) { return s.prec == MCPM_FP32 ? conv_in_impl<float>(s, n) : conv_in_impl<double>(s, n); }
+template <typename real> static int conv_out_impl(Session& s, int64_t n) {
+  k_convert_out<real><<<grid_for(n, 256, s.num_sms * 8), 256, 0, s.stream>>>(pt<real>(s.P[s.cur]), s.stage, n, s.cap);
+  return 1;
+}
+int launch_convert_out(Session& s, int64_t n) { return s.prec == MCPM_FP32 ? conv_out_impl<float>(s, n) : conv_out_impl<double>(s, n); }
+
+// the dynamic shared memory the update kernel needs, for the session setup
+size_t update_smem_bytes(const Session& s) {
+  return s.prec == MCPM_FP32 ? update_smem<float>(s) : update_smem<double>(s);
+}
+cudaError_t update_set_smem_max() {
+  int dev = 0, mx = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&mx, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  mx -= 4 * 8 * 16 + 64;  // leave room for the static reduction scratch
+  cudaError_t e = cudaFuncSetAttribute(k_update<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(k_update<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+}
+int update_occupancy(const Session& s) {
+  int nb = 0;
+  size_t sm = update_smem_bytes(s);
+  if (s.prec == MCPM_FP32) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_update<float>, 256, sm);
+  else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_update<double>, 256, sm);
+  return nb < 1 ? 1 : nb;
+}
+int moments_occupancy(const Session& s) {
+  int nb = 0;
+  if (s.prec == MCPM_FP32) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_moments<float>, 256, 0);
+  else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_moments<double>, 256, 0);
+  return nb < 1 ? 1 : nb;
+}
+
+}  // namespace mcpm

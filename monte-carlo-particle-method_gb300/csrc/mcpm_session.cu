@@ -1,0 +1,525 @@
+// mcpm_session.cu -- the C-ABI of include/mcpm.h: session lifetime, host
+// copies, and the order in which the step's kernels run.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+
+#include "mcpm_internal.h"
+
+namespace mcpm {
+size_t update_smem_bytes(const Session& s);
+int update_occupancy(const Session& s);
+int moments_occupancy(const Session& s);
+int long_range_setup(Session& s);
+cudaError_t pcr_set_smem(int nf);
+cudaError_t update_set_smem_max();
+
+// ------------------------------------------------------- small kernels
+__global__ void k_unpermute3(const double* src, const int32_t* pid, double* dst, int64_t n, int64_t cap) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    int q = pid[i];
+    dst[q] = src[i];
+    dst[cap + q] = src[cap + i];
+    dst[2 * cap + q] = src[2 * cap + i];
+  }
+}
+// cell of every particle from the sorted segments (binary search in off)
+__global__ void k_index(const int32_t* off, int C, const int32_t* pid, int32_t* out, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    int lo = 0, hi = C;  // find c with off[c] <= i < off[c+1]
+    while (hi - lo > 1) {
+      int mid = (lo + hi) >> 1;
+      if (off[mid] <= i) lo = mid; else hi = mid;
+    }
+    out[pid[i]] = lo;
+  }
+}
+}  // namespace mcpm
+
+using namespace mcpm;
+
+struct mcpm_session : public Session {};
+
+static int fail(mcpm_session* s, int code, const char* msg) {
+  if (s) s->err = msg;
+  return code;
+}
+
+static int cuda_check(mcpm_session* s, cudaError_t e, const char* where) {
+  if (e == cudaSuccess) return MCPM_OK;
+  char buf[256];
+  snprintf(buf, sizeof buf, "%s: %s", where, cudaGetErrorString(e));
+  s->err = buf;
+  return MCPM_ERR_CUDA;
+}
+
+static int after_launch(mcpm_session* s, int n, const char* where) {
+  s->launches += n;
+  return cuda_check(s, cudaGetLastError(), where);
+}
+
+static cudaEvent_t prof_event(mcpm_session* s) {
+  if (!s->prof_pool.empty()) {
+    cudaEvent_t e = s->prof_pool.back();
+    s->prof_pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e;
+  cudaEventCreate(&e);
+  return e;
+}
+
+// runs launcher f (which returns its launch count) inside an event pair
+template <typename F> static int timed(mcpm_session* s, int cls, F f) {
+  if (!s->prof) return f();
+  cudaEvent_t a = prof_event(s), b = prof_event(s);
+  cudaEventRecord(a, s->stream);
+  int n = f();
+  cudaEventRecord(b, s->stream);
+  s->prof_recs.push_back({a, b, cls, n});
+  return n;
+}
+#define T_BIN(x) timed(s, MCPM_K_BIN, [&] { return (x); })
+#define T_SCAN(x) timed(s, MCPM_K_SCAN, [&] { return (x); })
+#define T_SCAT(x) timed(s, MCPM_K_SCATTER, [&] { return (x); })
+#define T_MOM(x) timed(s, MCPM_K_MOMENTS, [&] { return (x); })
+#define T_SOLVE(x) timed(s, MCPM_K_SOLVE, [&] { return (x); })
+#define T_ESMC(x) timed(s, MCPM_K_ESMC, [&] { return (x); })
+#define T_LR(x) timed(s, MCPM_K_LONG_RANGE, [&] { return (x); })
+#define T_UPD(x) timed(s, MCPM_K_UPDATE, [&] { return (x); })
+
+static inline bool is_fp_model(int m) { return m == MCPM_MODEL_FP_DENSE || m == MCPM_MODEL_FP_IDEAL_GAS; }
+
+extern "C" {
+
+int mcpm_config_derive(mcpm_config* c, int64_t n_particles) {
+  if (!c) return MCPM_ERR_ARG;
+  const double pi = acos(-1.0);
+  c->b = 2 * pi * pow(c->sigma, 3) / (3.0);  // src/myIO.cpp:2828
+  if (!(c->T0 > 0)) c->T0 = 273.0;           // :2234
+  if (!(c->visp > 0)) c->visp = 0.5;
+  if (!(c->mu > 0)) c->mu = 5.0 / (16.0 * c->sigma * c->sigma) * sqrt(c->m * c->kb * c->T0 / acos(-1.0));  // :2829
+  double vol = c->length[0] * c->length[1] * c->length[2];
+  if (n_particles > 0) c->Fn = c->n * vol / n_particles;  // :2225
+  if (!(c->eqdist > 0)) c->eqdist = c->sigma;
+  if (c->seed == 0) c->seed = 0x4D43504Dull;
+  if (c->max_particles < n_particles) c->max_particles = n_particles;
+  return MCPM_OK;
+}
+
+int mcpm_session_create(const mcpm_config* cfg, mcpm_session** out) {
+  if (!cfg || !out) return MCPM_ERR_ARG;
+  *out = nullptr;
+  const mcpm_config& c = *cfg;
+  if (c.n_cells[0] < 1 || c.n_cells[1] < 1 || c.n_cells[2] != 1) return MCPM_ERR_ARG;
+  if (c.direction[2] != 0 || c.max_particles < 1) return MCPM_ERR_ARG;
+  if ((int64_t)c.n_cells[0] * c.n_cells[1] > (1 << 24)) return MCPM_ERR_ARG;
+  if (c.max_particles > ((int64_t)1 << 31) - 1) return MCPM_ERR_ARG;
+  if (c.precision != MCPM_FP64 && c.precision != MCPM_FP32) return MCPM_ERR_ARG;
+  if (c.model < MCPM_MODEL_NONE || c.model > MCPM_MODEL_ESMC) return MCPM_ERR_ARG;
+  if (c.problem != MCPM_PROBLEM_CLOSED_BOX && c.problem != MCPM_PROBLEM_COUETTE && c.problem != MCPM_PROBLEM_WALL &&
+      c.problem != MCPM_PROBLEM_PERIODIC)
+    return MCPM_ERR_ARG;
+  if (c.long_range != MCPM_LR_NONE && c.long_range != MCPM_LR_DIRECT && c.long_range != MCPM_LR_SCREENED_POISSON)
+    return MCPM_ERR_ARG;
+  // the 1-D Vlasov routines index cells by row (src/Main_Functions.cpp:3772)
+  if (c.long_range != MCPM_LR_NONE && (c.n_cells[0] != 1 || c.n_cells[1] + 1 > 7000)) return MCPM_ERR_ARG;
+  if (!(c.sigma > 0 && c.m > 0 && c.kb > 0 && c.dt > 0 && c.mu > 0 && c.T0 > 0)) return MCPM_ERR_ARG;
+  for (int i = 0; i < 2; ++i)
+    if (!(c.length[i] > 0)) return MCPM_ERR_ARG;
+
+  mcpm_session* s = new (std::nothrow) mcpm_session();
+  if (!s) return MCPM_ERR_ARG;
+  s->cfg = c;
+  s->prec = c.precision;
+  s->rsz = c.precision == MCPM_FP32 ? 4 : 8;
+  s->cap = c.max_particles;
+  s->C = c.n_cells[0] * c.n_cells[1];
+  DevConsts& k = s->k;
+  k.N0 = c.n_cells[0]; k.N1 = c.n_cells[1]; k.C = s->C;
+  k.dir0 = c.direction[0]; k.dir1 = c.direction[1];
+  k.problem = c.problem; k.model = c.model; k.long_range = c.long_range;
+  k.dx = c.length[0] / c.n_cells[0]; k.dy = c.length[1] / c.n_cells[1]; k.dz = c.length[2] / c.n_cells[2];
+  k.L0 = c.length[0]; k.L1 = c.length[1];
+  k.sigma = c.sigma; k.m = c.m; k.kb = c.kb; k.n = c.n; k.Fn = c.Fn; k.T0 = c.T0; k.mu = c.mu; k.visp = c.visp;
+  k.b = c.b; k.dt = c.dt; k.phi = c.phi; k.eqdist = c.eqdist; k.ast = c.ast; k.bst = c.bst;
+  for (int i = 0; i < 4; ++i) { k.Tw[i] = c.T_wall[i]; k.Uw[i] = c.U_wall[i]; }
+  k.seed = c.seed;
+  s->need_old = (c.problem == MCPM_PROBLEM_COUETTE || c.problem == MCPM_PROBLEM_WALL);
+  s->need_x1 = (c.direction[0] == 1 || c.model == MCPM_MODEL_ESMC || c.problem == MCPM_PROBLEM_COUETTE);
+
+  int dev = 0;
+  int rc;
+  if ((rc = cuda_check(s, cudaGetDevice(&dev), "cudaGetDevice"))) { delete s; return rc; }
+  cudaDeviceGetAttribute(&s->num_sms, cudaDevAttrMultiProcessorCount, dev);
+  if ((rc = cuda_check(s, cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking), "stream"))) { delete s; return rc; }
+  s->own_stream = s->stream;
+
+  // tuning defaults (see mcpm_tune in the Python layer for the sweep)
+  s->tune.wcap = 256;
+  s->tune.block = 256;
+  s->tune.bcap = (s->prec == MCPM_FP32) ? 6144 : 3072;
+
+  const size_t cap = (size_t)s->cap, C = (size_t)s->C, rs = s->rsz;
+  auto A = [&](void** p, size_t bytes) -> bool { return cudaMalloc(p, bytes ? bytes : 16) == cudaSuccess; };
+  bool ok = true;
+  for (int b = 0; b < 2 && ok; ++b) {
+    PBuf& P = s->P[b];
+    if (s->need_x1) ok = ok && A(&P.x1, cap * rs);
+    ok = ok && A(&P.x2, cap * rs) && A(&P.U1, cap * rs) && A(&P.U2, cap * rs) && A(&P.U3, cap * rs) &&
+         A((void**)&P.pid, cap * 4);
+    if (s->need_old) {
+      if (s->need_x1) ok = ok && A(&P.x1o, cap * rs);
+      ok = ok && A(&P.x2o, cap * rs);
+    }
+  }
+  ok = ok && A((void**)&s->key, cap * 4) && A((void**)&s->cnt, C * 4) && A((void**)&s->cnt_next, C * 4) &&
+       A((void**)&s->off, (C + 1) * 4) && A((void**)&s->cursor, C * 4) && A((void**)&s->list_small, C * 4) &&
+       A((void**)&s->list_big, C * 4) && A((void**)&s->wl, WL_COUNT * 4) && A((void**)&s->work, WK_COUNT * 4) &&
+       A((void**)&s->cell, (size_t)CF_DEV_COUNT * C * 8) && A((void**)&s->xi, 3 * cap * 8) &&
+       A((void**)&s->inj, 3 * cap * 8) && A((void**)&s->stage, 5 * cap * 8) &&
+       A((void**)&s->faces, ((size_t)k.N1 + 1 + 5000) * 8) && A((void**)&s->status, 16);
+  if (!ok) {
+    s->err = "out of device memory";
+    mcpm_session_destroy(s);
+    return MCPM_ERR_CUDA;
+  }
+  cudaMemsetAsync(s->cnt_next, 0, C * 4, s->stream);
+  cudaMemsetAsync(s->cell, 0, (size_t)CF_DEV_COUNT * C * 8, s->stream);
+  cudaMemsetAsync(s->status, 0, 16, s->stream);
+  cudaMemsetAsync(s->work, 0, WK_COUNT * 4, s->stream);
+  cudaMemsetAsync(s->inj, 0, 3 * cap * 8, s->stream);
+  cudaMemsetAsync(s->xi, 0, 3 * cap * 8, s->stream);
+
+  if ((rc = cuda_check(s, update_set_smem_max(), "smem attribute"))) { mcpm_session_destroy(s); return rc; }
+  if (c.long_range == MCPM_LR_SCREENED_POISSON)
+    if ((rc = cuda_check(s, pcr_set_smem(k.N1 + 1), "pcr smem"))) { mcpm_session_destroy(s); return rc; }
+  s->tune.grid_mom = s->num_sms * moments_occupancy(*s);
+  s->tune.grid_upd = s->num_sms * update_occupancy(*s);
+  long_range_setup(*s);
+  if ((rc = cuda_check(s, cudaStreamSynchronize(s->stream), "session init"))) { mcpm_session_destroy(s); return rc; }
+  *out = s;
+  return MCPM_OK;
+}
+
+int mcpm_session_destroy(mcpm_session* s) {
+  if (!s) return MCPM_ERR_ARG;
+  if (s->stream) cudaStreamSynchronize(s->stream);
+  if (s->own_stream && s->own_stream != s->stream) cudaStreamSynchronize(s->own_stream);
+  for (int b = 0; b < 2; ++b) {
+    PBuf& P = s->P[b];
+    cudaFree(P.x1); cudaFree(P.x2); cudaFree(P.U1); cudaFree(P.U2); cudaFree(P.U3); cudaFree(P.pid);
+    cudaFree(P.x1o); cudaFree(P.x2o);
+  }
+  cudaFree(s->key); cudaFree(s->cnt); cudaFree(s->cnt_next); cudaFree(s->off); cudaFree(s->cursor);
+  cudaFree(s->list_small); cudaFree(s->list_big); cudaFree(s->wl); cudaFree(s->work); cudaFree(s->cell);
+  cudaFree(s->xi); cudaFree(s->inj); cudaFree(s->stage); cudaFree(s->faces); cudaFree(s->status);
+  if (s->graph) cudaGraphExecDestroy(s->graph);
+  for (auto& r : s->prof_recs) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
+  for (auto e : s->prof_pool) cudaEventDestroy(e);
+  if (s->own_stream) cudaStreamDestroy(s->own_stream);
+  delete s;
+  return MCPM_OK;
+}
+
+const char* mcpm_last_error(const mcpm_session* s) { return s ? s->err.c_str() : "no session"; }
+
+int mcpm_sync(mcpm_session* s) {
+  if (!s) return MCPM_ERR_ARG;
+  return cuda_check(s, cudaStreamSynchronize(s->stream), "sync");
+}
+
+int mcpm_check_status(mcpm_session* s) {
+  if (!s) return MCPM_ERR_ARG;
+  uint32_t st = 0;
+  int rc = cuda_check(s, cudaMemcpyAsync(&st, s->status, 4, cudaMemcpyDeviceToHost, s->stream), "status");
+  if (rc) return rc;
+  if ((rc = cuda_check(s, cudaStreamSynchronize(s->stream), "status sync"))) return rc;
+  if (st) {
+    cudaMemsetAsync(s->status, 0, 4, s->stream);
+    char buf[200];
+    snprintf(buf, sizeof buf, "device status 0x%x:%s%s%s%s", st, (st & MCPM_ERR_OUT_OF_BOX) ? " particle out of box" : "",
+             (st & MCPM_ERR_NAN) ? " NaN" : "", (st & MCPM_ERR_BC_LOOP) ? " wall re-flight did not converge" : "",
+             (st & MCPM_ERR_ITER_LIMIT) ? " iteration limit" : "");
+    s->err = buf;
+  }
+  return (int)st;
+}
+
+// binning + counting sort into cell order (the front of cell_update)
+static int sort_by_cell(mcpm_session* s) {
+  int n = 0;
+  if (!s->keys_current) n += T_BIN(launch_bin(*s, s->step));
+  n += T_SCAN(launch_scan(*s));
+  n += T_SCAT(launch_scatter(*s));
+  s->sorted = true;
+  s->keys_current = false;
+  return after_launch(s, n, "sort_by_cell");
+}
+
+int mcpm_upload_particles(mcpm_session* s, int64_t n, const double* x1, const double* x2, const double* U1,
+                          const double* U2, const double* U3) {
+  if (!s || n < 0 || n > s->cap || !x2 || !U1 || !U2 || !U3) return fail(s, MCPM_ERR_ARG, "upload: bad arguments");
+  if (!x1 && s->need_x1) return fail(s, MCPM_ERR_ARG, "upload: x1 required for this configuration");
+  s->N = n;
+  const size_t cap = (size_t)s->cap, b = (size_t)n * 8;
+  cudaStream_t st = s->stream;
+  if (x1) cudaMemcpyAsync(s->stage, x1, b, cudaMemcpyHostToDevice, st);
+  else cudaMemsetAsync(s->stage, 0, b, st);
+  cudaMemcpyAsync(s->stage + cap, x2, b, cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(s->stage + 2 * cap, U1, b, cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(s->stage + 3 * cap, U2, b, cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(s->stage + 4 * cap, U3, b, cudaMemcpyHostToDevice, st);
+  s->cur = 0;
+  int k = launch_convert_in(*s, n);
+  int rc = after_launch(s, k, "upload");
+  if (rc) return rc;
+  s->step = 0;
+  s->bc_calls = 0;
+  s->omega_init = false;
+  s->keys_current = false;
+  s->sorted = false;
+  s->have_particles = true;
+  return sort_by_cell(s);
+}
+
+int mcpm_download_particles(mcpm_session* s, int64_t n, double* x1, double* x2, double* U1, double* U2, double* U3) {
+  if (!s || n != s->N || !x2 || !U1 || !U2 || !U3) return fail(s, MCPM_ERR_ARG, "download: bad arguments");
+  const size_t cap = (size_t)s->cap, b = (size_t)n * 8;
+  cudaStream_t st = s->stream;
+  int k = launch_convert_out(*s, n);
+  int rc = after_launch(s, k, "download");
+  if (rc) return rc;
+  if (x1) cudaMemcpyAsync(x1, s->stage, b, cudaMemcpyDeviceToHost, st);
+  cudaMemcpyAsync(x2, s->stage + cap, b, cudaMemcpyDeviceToHost, st);
+  cudaMemcpyAsync(U1, s->stage + 2 * cap, b, cudaMemcpyDeviceToHost, st);
+  cudaMemcpyAsync(U2, s->stage + 3 * cap, b, cudaMemcpyDeviceToHost, st);
+  cudaMemcpyAsync(U3, s->stage + 4 * cap, b, cudaMemcpyDeviceToHost, st);
+  return cuda_check(s, cudaStreamSynchronize(st), "download");
+}
+
+int mcpm_cell_update(mcpm_session* s) {
+  if (!s || !s->have_particles) return fail(s, MCPM_ERR_STATE, "cell_update: no particles");
+  int rc;
+  if (s->needs_rebin) { s->sorted = false; s->needs_rebin = false; }  // cell_update always re-bins
+  if (!s->sorted && (rc = sort_by_cell(s))) return rc;
+  int n = 0;
+  cudaMemsetAsync(s->work, 0, WK_COUNT * 4, s->stream);
+  n += T_MOM(launch_moments(*s));
+  n += T_SOLVE(launch_solve(*s, (s->cfg.model == MCPM_MODEL_FP_DENSE && s->step > 0) ? 1 : 0));
+  return after_launch(s, n, "cell_update");
+}
+
+int mcpm_random_generator(mcpm_session* s) {
+  if (!s || !s->sorted) return fail(s, MCPM_ERR_STATE, "random_generator: call cell_update first");
+  if (!is_fp_model(s->cfg.model)) return MCPM_OK;  // src/main.cpp:442
+  cudaMemsetAsync(s->work, 0, WK_COUNT * 4, s->stream);
+  return after_launch(s, T_UPD(launch_update(*s, ST_RNG | ST_STORE_XI, 0)), "random_generator");
+}
+
+int mcpm_velocity_update(mcpm_session* s) {
+  if (!s || !s->sorted) return fail(s, MCPM_ERR_STATE, "velocity_update: call cell_update first");
+  int n = 0;
+  uint32_t stages = 0;
+  if (s->cfg.model == MCPM_MODEL_ESMC) n += T_ESMC(launch_esmc(*s));
+  else if (is_fp_model(s->cfg.model)) stages |= ST_LOAD_XI | ST_FP;
+  if (s->cfg.long_range != MCPM_LR_NONE) {
+    n += T_LR(launch_long_range(*s));
+    stages |= ST_LR;
+  }
+  if (stages) {
+    cudaMemsetAsync(s->work, 0, WK_COUNT * 4, s->stream);
+    n += T_UPD(launch_update(*s, stages, 0));
+  }
+  return after_launch(s, n, "velocity_update");
+}
+
+static int position_stage(mcpm_session* s, uint32_t stage, int base, const char* what) {
+  if (!s || !s->have_particles) return fail(s, MCPM_ERR_STATE, "no particles");
+  int rc;
+  if (!s->sorted && (rc = sort_by_cell(s))) return rc;  // group by the last binning
+  cudaMemsetAsync(s->work, 0, WK_COUNT * 4, s->stream);
+  rc = after_launch(s, T_UPD(launch_update(*s, stage, base)), what);
+  // positions changed: the layout is still grouped by the binning of this
+  // step (which DFP_extra_streaming needs), but it is stale for the next one
+  s->keys_current = false;
+  s->sorted = true;
+  s->needs_rebin = true;
+  return rc;
+}
+
+int mcpm_dfp_extra_streaming(mcpm_session* s) {
+  if (s && s->cfg.model != MCPM_MODEL_FP_DENSE) return MCPM_OK;  // src/main.cpp:478
+  return position_stage(s, ST_DFP, 0, "dfp_extra_streaming");
+}
+int mcpm_apply_bc(mcpm_session* s) {
+  if (!s) return MCPM_ERR_ARG;
+  int base = s->bc_calls++;
+  return position_stage(s, ST_BC1, base, "apply_bc");
+}
+int mcpm_store_old_positions(mcpm_session* s) {
+  if (s && !s->need_old) return MCPM_OK;
+  return position_stage(s, ST_OLD, 0, "store_old_positions");
+}
+int mcpm_stream_particles(mcpm_session* s) { return position_stage(s, ST_STREAM, 0, "stream_particles"); }
+
+int mcpm_end_step(mcpm_session* s) {
+  if (!s) return MCPM_ERR_ARG;
+  s->step++;
+  s->bc_calls = 0;
+  if (s->needs_rebin) { s->sorted = false; s->needs_rebin = false; }
+  return MCPM_OK;
+}
+
+int mcpm_step(mcpm_session* s, int32_t n_steps) {
+  if (!s || !s->have_particles || n_steps < 0) return fail(s, MCPM_ERR_STATE, "step: no particles");
+  const int m = s->cfg.model;
+  if (m == MCPM_MODEL_ESMC && !s->omega_init) {
+    // src/main.cpp:236-269: cell_update at the current positions, then the majorant
+    int rc = mcpm_cell_update(s);
+    if (rc) return rc;
+    if ((rc = mcpm_init_omega_max(s))) return rc;
+  }
+  if (s->step == 0) s->step = 1;  // the loop of src/main.cpp starts at step 1 (:389)
+  uint32_t stages = ST_BC1 | ST_OLD | ST_STREAM | ST_BC2 | ST_BC3 | ST_KEY;
+  if (is_fp_model(m)) stages |= ST_RNG | ST_FP;
+  if (m == MCPM_MODEL_FP_DENSE) stages |= ST_DFP;
+  if (s->cfg.long_range != MCPM_LR_NONE) stages |= ST_LR;
+  if (!s->need_old) stages &= ~ST_OLD;
+  for (int it = 0; it < n_steps; ++it) {
+    int n = 0;
+    if (s->needs_rebin) { s->sorted = false; s->needs_rebin = false; }
+    if (!s->sorted) {
+      if (!s->keys_current) n += T_BIN(launch_bin(*s, s->step));
+      n += T_SCAN(launch_scan(*s));
+      n += T_SCAT(launch_scatter(*s));
+    } else {
+      cudaMemsetAsync(s->work, 0, WK_COUNT * 4, s->stream);
+    }
+    n += T_MOM(launch_moments(*s));
+    n += T_SOLVE(launch_solve(*s, (m == MCPM_MODEL_FP_DENSE && s->step > 0) ? 1 : 0));
+    if (m == MCPM_MODEL_ESMC) n += T_ESMC(launch_esmc(*s));
+    if (s->cfg.long_range != MCPM_LR_NONE) n += T_LR(launch_long_range(*s));
+    n += T_UPD(launch_update(*s, stages, 0));
+    s->step++;
+    s->bc_calls = 0;
+    s->keys_current = true;
+    s->sorted = false;
+    int rc = after_launch(s, n, "step");
+    if (rc) return rc;
+  }
+  return mcpm_check_status(s);
+}
+
+int mcpm_inject_normals(mcpm_session* s, int64_t n, const double* a, const double* b, const double* c) {
+  if (!s || n != s->N || !a || !b || !c) return fail(s, MCPM_ERR_ARG, "inject_normals: bad arguments");
+  const size_t cap = (size_t)s->cap;
+  cudaMemcpyAsync(s->inj, a, n * 8, cudaMemcpyHostToDevice, s->stream);
+  cudaMemcpyAsync(s->inj + cap, b, n * 8, cudaMemcpyHostToDevice, s->stream);
+  cudaMemcpyAsync(s->inj + 2 * cap, c, n * 8, cudaMemcpyHostToDevice, s->stream);
+  s->rng_mode = MCPM_RNG_INJECTED;
+  return cuda_check(s, cudaGetLastError(), "inject_normals");
+}
+
+int mcpm_set_rng(mcpm_session* s, int32_t mode) {
+  if (!s || (mode != MCPM_RNG_PHILOX && mode != MCPM_RNG_INJECTED)) return MCPM_ERR_ARG;
+  s->rng_mode = mode;
+  return MCPM_OK;
+}
+
+int mcpm_get_cells(mcpm_session* s, double* out) {
+  if (!s || !out) return MCPM_ERR_ARG;
+  cudaMemcpyAsync(out, s->cell, (size_t)MCPM_CF_COUNT * s->C * 8, cudaMemcpyDeviceToHost, s->stream);
+  return cuda_check(s, cudaStreamSynchronize(s->stream), "get_cells");
+}
+
+int mcpm_get_index(mcpm_session* s, int32_t* index) {
+  if (!s || !index || !s->have_particles) return MCPM_ERR_ARG;
+  int rc;
+  if (s->needs_rebin || !s->sorted) {
+    if (s->needs_rebin) { s->sorted = false; s->needs_rebin = false; }
+    if ((rc = sort_by_cell(s))) return rc;
+  }
+  int32_t* tmp = (int32_t*)s->stage;
+  k_index<<<(int)((s->N + 255) / 256 > 4096 ? 4096 : (s->N + 255) / 256 + 1), 256, 0, s->stream>>>(s->off, s->C, s->P[s->cur].pid, tmp, s->N);
+  if ((rc = after_launch(s, 1, "get_index"))) return rc;
+  cudaMemcpyAsync(index, tmp, (size_t)s->N * 4, cudaMemcpyDeviceToHost, s->stream);
+  return cuda_check(s, cudaStreamSynchronize(s->stream), "get_index");
+}
+
+int mcpm_get_normals(mcpm_session* s, double* a, double* b, double* c) {
+  if (!s || !a || !b || !c) return MCPM_ERR_ARG;
+  const size_t cap = (size_t)s->cap;
+  k_unpermute3<<<(int)((s->N + 255) / 256 > 4096 ? 4096 : (s->N + 255) / 256 + 1), 256, 0, s->stream>>>(s->xi, s->P[s->cur].pid, s->stage, s->N, s->cap);
+  int rc = after_launch(s, 1, "get_normals");
+  if (rc) return rc;
+  cudaMemcpyAsync(a, s->stage, s->N * 8, cudaMemcpyDeviceToHost, s->stream);
+  cudaMemcpyAsync(b, s->stage + cap, s->N * 8, cudaMemcpyDeviceToHost, s->stream);
+  cudaMemcpyAsync(c, s->stage + 2 * cap, s->N * 8, cudaMemcpyDeviceToHost, s->stream);
+  return cuda_check(s, cudaStreamSynchronize(s->stream), "get_normals");
+}
+
+int mcpm_get_layout(mcpm_session* s, int32_t* pid_by_slot, int32_t* off) {
+  if (!s || !pid_by_slot || !off) return MCPM_ERR_ARG;
+  if (!s->sorted) return fail(s, MCPM_ERR_STATE, "get_layout: layout not sorted; call cell_update first");
+  cudaMemcpyAsync(pid_by_slot, s->P[s->cur].pid, (size_t)s->N * 4, cudaMemcpyDeviceToHost, s->stream);
+  cudaMemcpyAsync(off, s->off, (size_t)(s->C + 1) * 4, cudaMemcpyDeviceToHost, s->stream);
+  return cuda_check(s, cudaStreamSynchronize(s->stream), "get_layout");
+}
+
+int32_t mcpm_get_step(const mcpm_session* s) { return s ? s->step : -1; }
+int mcpm_set_step(mcpm_session* s, int32_t step) {
+  if (!s || step < 0) return MCPM_ERR_ARG;
+  s->step = step;
+  s->bc_calls = 0;
+  return MCPM_OK;
+}
+
+int mcpm_set_cell_field(mcpm_session* s, int32_t f, const double* v) {
+  if (!s || !v || f < 0 || f >= MCPM_CF_COUNT) return MCPM_ERR_ARG;
+  cudaMemcpyAsync(s->cell + (size_t)f * s->C, v, (size_t)s->C * 8, cudaMemcpyHostToDevice, s->stream);
+  return cuda_check(s, cudaStreamSynchronize(s->stream), "set_cell_field");
+}
+
+int mcpm_init_omega_max(mcpm_session* s) {
+  if (!s) return MCPM_ERR_ARG;
+  s->omega_init = true;
+  return after_launch(s, launch_init_omega(*s), "init_omega_max");
+}
+
+int64_t mcpm_kernel_launches(const mcpm_session* s) { return s ? s->launches : -1; }
+
+int mcpm_set_stream(mcpm_session* s, void* stream) {
+  if (!s) return MCPM_ERR_ARG;
+  cudaStreamSynchronize(s->stream);
+  s->stream = stream ? (cudaStream_t)stream : s->own_stream;
+  return MCPM_OK;
+}
+
+int mcpm_profile(mcpm_session* s, int32_t enable) {
+  if (!s) return MCPM_ERR_ARG;
+  s->prof = enable != 0;
+  return MCPM_OK;
+}
+
+int mcpm_profile_read(mcpm_session* s, double* ms, int64_t* launches, int32_t n) {
+  if (!s || n < 0 || n > MCPM_K_COUNT) return MCPM_ERR_ARG;
+  int rc = cuda_check(s, cudaStreamSynchronize(s->stream), "profile_read");
+  if (rc) return rc;
+  for (int i = 0; i < n; ++i) { if (ms) ms[i] = 0.0; if (launches) launches[i] = 0; }
+  for (auto& r : s->prof_recs) {
+    float t = 0.f;
+    cudaEventElapsedTime(&t, r.a, r.b);
+    if (r.cls < n) {
+      if (ms) ms[r.cls] += t;
+      if (launches) launches[r.cls] += r.n;
+    }
+    s->prof_pool.push_back(r.a);
+    s->prof_pool.push_back(r.b);
+  }
+  s->prof_recs.clear();
+  return MCPM_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,345 @@
+"""Python mirror of the reference's particle-loop routine surface over the
+C-ABI in include/mcpm.h (libmcpm.so, built in-tree by build.py).
+
+The reference drives its particle step from src/main.cpp:389-669 with free
+functions on caller-owned ``double*`` arrays; :class:`Session` keeps the same
+routine names and call order (``cell_update``, ``random_generator``,
+``velocity_update``, ``DFP_extra_streaming``, ``apply_BC``,
+``store_old_positions``, ``stream_particles``) over a device-resident state.
+There is no CPU fallback: constructing a Session without the compiled library
+raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libmcpm.so")
+
+# ---- enums (include/mcpm.h) -------------------------------------------------
+OK = 0
+ERR_ARG, ERR_CUDA, ERR_OUT_OF_BOX, ERR_NAN, ERR_CAPACITY, ERR_BC_LOOP, ERR_ITER_LIMIT, ERR_STATE = (
+    1, 2, 4, 8, 16, 32, 64, 128)
+PROBLEM_CLOSED_BOX, PROBLEM_COUETTE, PROBLEM_WALL, PROBLEM_PERIODIC = 1, 2, 11, 100
+MODEL_NONE, MODEL_FP_DENSE, MODEL_FP_IDEAL_GAS, MODEL_ESMC = 0, 1, 2, 3
+LR_NONE, LR_DIRECT, LR_SCREENED_POISSON = 0, 1, 3
+FP64, FP32 = 0, 1
+RNG_PHILOX, RNG_INJECTED = 0, 1
+
+CF = dict(NUM_INSIDE=0, U_SPACE=1, PIJ=4, M3=10, M4=20, M5=26, Q=29, DM2=32, DM4=33, MP=34, T=37, N=38,
+          GAMMA_ST=39, LAMBDA=40, C=41, GAMMA=47, ALPHA=50, BETA=59, PHI=62, F2=65, OMEGA_MAX=66, DIVU=67)
+CF_COUNT = 68
+K_NAMES = ["bin", "scan", "scatter", "moments", "solve", "esmc", "long_range", "update"]
+K_COUNT = len(K_NAMES)
+# (field, width) of every exported per-cell quantity
+CF_WIDTH = dict(NUM_INSIDE=1, U_SPACE=3, PIJ=6, M3=10, M4=6, M5=3, Q=3, DM2=1, DM4=1, MP=3, T=1, N=1,
+                GAMMA_ST=1, LAMBDA=1, C=6, GAMMA=3, ALPHA=9, BETA=3, PHI=3, F2=1, OMEGA_MAX=1, DIVU=1)
+
+
+class Config(C.Structure):
+    """mcpm_config: the subset of GAS/BOX (src/cpp_headers.h:145-269) the step reads."""
+    _fields_ = [
+        ("n_cells", C.c_int32 * 3), ("direction", C.c_int32 * 3), ("length", C.c_double * 3),
+        ("problem", C.c_int32), ("model", C.c_int32), ("long_range", C.c_int32), ("precision", C.c_int32),
+        ("sigma", C.c_double), ("m", C.c_double), ("kb", C.c_double), ("n", C.c_double), ("Fn", C.c_double),
+        ("T0", C.c_double), ("mu", C.c_double), ("visp", C.c_double), ("b", C.c_double), ("dt", C.c_double),
+        ("phi", C.c_double), ("eqdist", C.c_double), ("ast", C.c_double), ("bst", C.c_double),
+        ("T_wall", C.c_double * 4), ("U_wall", C.c_double * 4), ("seed", C.c_uint64),
+        ("max_particles", C.c_int64),
+    ]
+
+    def copy(self):
+        c = Config()
+        C.pointer(c)[0] = self
+        return c
+
+    def as_dict(self):
+        out = {}
+        for name, _ in self._fields_:
+            v = getattr(self, name)
+            out[name] = list(v) if hasattr(v, "__len__") else v
+        return out
+
+
+def derive(cfg: Config, n_particles: int) -> Config:
+    """Derived GAS fields as readSettingsFile fills them (src/myIO.cpp:2217-2233,
+    :2828-2830); identical to mcpm_config_derive in the library."""
+    cfg.b = 2 * math.pi * cfg.sigma ** 3 / 3.0
+    if not cfg.T0 > 0:
+        cfg.T0 = 273.0
+    if not cfg.visp > 0:
+        cfg.visp = 0.5
+    if not cfg.mu > 0:
+        cfg.mu = 5.0 / (16.0 * cfg.sigma * cfg.sigma) * math.sqrt(cfg.m * cfg.kb * cfg.T0 / math.acos(-1.0))
+    vol = cfg.length[0] * cfg.length[1] * cfg.length[2]
+    if n_particles > 0:
+        cfg.Fn = cfg.n * vol / n_particles
+    if not cfg.eqdist > 0:
+        cfg.eqdist = cfg.sigma
+    if cfg.seed == 0:
+        cfg.seed = 0x4D43504D
+    if cfg.max_particles < n_particles:
+        cfg.max_particles = n_particles
+    return cfg
+
+
+class MCPMError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("mcpm error %d: %s" % (code, msg))
+        self.code = code
+
+
+_lib = None
+
+
+def load_library(path: str | None = None):
+    """Loads libmcpm.so; raises if it is missing (there is no fallback path)."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise MCPMError(ERR_STATE, "libmcpm.so is not built (%s); run __graft_entry__.build()" % p)
+    L = C.CDLL(p)
+    vp, i64, i32, dp, ip = C.c_void_p, C.c_int64, C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_int32)
+    sig = {
+        "mcpm_config_derive": (C.c_int, [C.POINTER(Config), i64]),
+        "mcpm_session_create": (C.c_int, [C.POINTER(Config), C.POINTER(vp)]),
+        "mcpm_session_destroy": (C.c_int, [vp]),
+        "mcpm_last_error": (C.c_char_p, [vp]),
+        "mcpm_sync": (C.c_int, [vp]),
+        "mcpm_check_status": (C.c_int, [vp]),
+        "mcpm_upload_particles": (C.c_int, [vp, i64, dp, dp, dp, dp, dp]),
+        "mcpm_download_particles": (C.c_int, [vp, i64, dp, dp, dp, dp, dp]),
+        "mcpm_cell_update": (C.c_int, [vp]),
+        "mcpm_random_generator": (C.c_int, [vp]),
+        "mcpm_velocity_update": (C.c_int, [vp]),
+        "mcpm_dfp_extra_streaming": (C.c_int, [vp]),
+        "mcpm_apply_bc": (C.c_int, [vp]),
+        "mcpm_store_old_positions": (C.c_int, [vp]),
+        "mcpm_stream_particles": (C.c_int, [vp]),
+        "mcpm_end_step": (C.c_int, [vp]),
+        "mcpm_step": (C.c_int, [vp, i32]),
+        "mcpm_inject_normals": (C.c_int, [vp, i64, dp, dp, dp]),
+        "mcpm_set_rng": (C.c_int, [vp, i32]),
+        "mcpm_get_cells": (C.c_int, [vp, dp]),
+        "mcpm_get_index": (C.c_int, [vp, ip]),
+        "mcpm_get_normals": (C.c_int, [vp, dp, dp, dp]),
+        "mcpm_get_layout": (C.c_int, [vp, ip, ip]),
+        "mcpm_get_step": (i32, [vp]),
+        "mcpm_set_step": (C.c_int, [vp, i32]),
+        "mcpm_set_cell_field": (C.c_int, [vp, i32, dp]),
+        "mcpm_init_omega_max": (C.c_int, [vp]),
+        "mcpm_kernel_launches": (i64, [vp]),
+        "mcpm_set_stream": (C.c_int, [vp, vp]),
+        "mcpm_profile": (C.c_int, [vp, i32]),
+        "mcpm_profile_read": (C.c_int, [vp, dp, C.POINTER(C.c_int64), i32]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    if path is None:
+        _lib = L
+    return L
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _ip(a):
+    return a.ctypes.data_as(C.POINTER(C.c_int32))
+
+
+def _f64(a, n):
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    if a.shape != (n,):
+        raise ValueError("expected %d values" % n)
+    return a
+
+
+class Session:
+    """One device-resident particle system; methods follow the reference's
+    routines (file:line in include/mcpm.h)."""
+
+    def __init__(self, cfg: Config):
+        self.lib = load_library()
+        self.cfg = cfg.copy()
+        self.C = cfg.n_cells[0] * cfg.n_cells[1] * cfg.n_cells[2]
+        h = C.c_void_p()
+        rc = self.lib.mcpm_session_create(C.byref(self.cfg), C.byref(h))
+        if rc != OK:
+            raise MCPMError(rc, "session_create failed (configuration rejected or no device)")
+        self.h = h
+        self.N = 0
+
+    # -- plumbing
+    def _ck(self, rc, what):
+        if rc != OK:
+            msg = self.lib.mcpm_last_error(self.h)
+            raise MCPMError(rc, "%s: %s" % (what, msg.decode() if msg else ""))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.mcpm_session_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # -- particles
+    def upload(self, x1, x2, U1, U2, U3):
+        n = len(x2)
+        self._keep = [_f64(x1, n) if x1 is not None else None, _f64(x2, n), _f64(U1, n), _f64(U2, n), _f64(U3, n)]
+        k = self._keep
+        self._ck(self.lib.mcpm_upload_particles(self.h, n, _dp(k[0]) if k[0] is not None else None, _dp(k[1]),
+                                                _dp(k[2]), _dp(k[3]), _dp(k[4])), "upload_particles")
+        self.N = n
+
+    def download(self):
+        n = self.N
+        out = {k: np.empty(n) for k in ("x1", "x2", "U1", "U2", "U3")}
+        self._ck(self.lib.mcpm_download_particles(self.h, n, _dp(out["x1"]), _dp(out["x2"]), _dp(out["U1"]),
+                                                  _dp(out["U2"]), _dp(out["U3"])), "download_particles")
+        return out
+
+    # -- the reference routines
+    def cell_update(self):
+        self._ck(self.lib.mcpm_cell_update(self.h), "cell_update")
+
+    def random_generator(self):
+        self._ck(self.lib.mcpm_random_generator(self.h), "random_generator")
+
+    def velocity_update(self):
+        self._ck(self.lib.mcpm_velocity_update(self.h), "velocity_update")
+
+    def DFP_extra_streaming(self):
+        self._ck(self.lib.mcpm_dfp_extra_streaming(self.h), "DFP_extra_streaming")
+
+    def apply_BC(self):
+        self._ck(self.lib.mcpm_apply_bc(self.h), "apply_BC")
+
+    def store_old_positions(self):
+        self._ck(self.lib.mcpm_store_old_positions(self.h), "store_old_positions")
+
+    def stream_particles(self):
+        self._ck(self.lib.mcpm_stream_particles(self.h), "stream_particles")
+
+    def end_step(self):
+        self._ck(self.lib.mcpm_end_step(self.h), "end_step")
+
+    def loop_body(self):
+        """One iteration of src/main.cpp:389-669 through the individual routines."""
+        self.cell_update()
+        self.random_generator()
+        self.velocity_update()
+        self.DFP_extra_streaming()
+        self.apply_BC()
+        self.store_old_positions()
+        self.stream_particles()
+        self.apply_BC()
+        self.apply_BC()
+        self.end_step()
+        self.check_status()
+
+    def step(self, n=1):
+        self._ck(self.lib.mcpm_step(self.h, int(n)), "step")
+
+    # -- hooks
+    def check_status(self):
+        st = self.lib.mcpm_check_status(self.h)
+        if st != OK:
+            self._ck(st, "device status")
+
+    def sync(self):
+        self._ck(self.lib.mcpm_sync(self.h), "sync")
+
+    def inject_normals(self, xi1, xi2, xi3):
+        n = self.N
+        self._inj = [_f64(xi1, n), _f64(xi2, n), _f64(xi3, n)]
+        self._ck(self.lib.mcpm_inject_normals(self.h, n, *[_dp(a) for a in self._inj]), "inject_normals")
+
+    def set_rng(self, mode):
+        self._ck(self.lib.mcpm_set_rng(self.h, int(mode)), "set_rng")
+
+    def get_cells(self):
+        out = np.empty((CF_COUNT, self.C))
+        self._ck(self.lib.mcpm_get_cells(self.h, _dp(out)), "get_cells")
+        return out
+
+    def get_index(self):
+        out = np.empty(self.N, dtype=np.int32)
+        self._ck(self.lib.mcpm_get_index(self.h, _ip(out)), "get_index")
+        return out
+
+    def get_normals(self):
+        a, b, c = np.empty(self.N), np.empty(self.N), np.empty(self.N)
+        self._ck(self.lib.mcpm_get_normals(self.h, _dp(a), _dp(b), _dp(c)), "get_normals")
+        return a, b, c
+
+    def get_layout(self):
+        pid = np.empty(self.N, dtype=np.int32)
+        off = np.empty(self.C + 1, dtype=np.int32)
+        self._ck(self.lib.mcpm_get_layout(self.h, _ip(pid), _ip(off)), "get_layout")
+        return pid, off
+
+    @property
+    def step_count(self):
+        return int(self.lib.mcpm_get_step(self.h))
+
+    def set_step(self, step):
+        self._ck(self.lib.mcpm_set_step(self.h, int(step)), "set_step")
+
+    def set_cell_field(self, field, values):
+        v = _f64(values, self.C)
+        self._ck(self.lib.mcpm_set_cell_field(self.h, CF[field], _dp(v)), "set_cell_field")
+
+    def init_omega_max(self):
+        self._ck(self.lib.mcpm_init_omega_max(self.h), "init_omega_max")
+
+    def set_stream(self, stream_handle):
+        """Launch on an external cudaStream_t (e.g. torch's current stream)."""
+        self._ck(self.lib.mcpm_set_stream(self.h, C.c_void_p(stream_handle or None)), "set_stream")
+
+    def profile(self, enable=True):
+        self._ck(self.lib.mcpm_profile(self.h, 1 if enable else 0), "profile")
+
+    def profile_read(self):
+        ms = np.zeros(K_COUNT)
+        n = np.zeros(K_COUNT, dtype=np.int64)
+        self._ck(self.lib.mcpm_profile_read(self.h, _dp(ms), n.ctypes.data_as(C.POINTER(C.c_int64)), K_COUNT),
+                 "profile_read")
+        return {name: (float(ms[i]), int(n[i])) for i, name in enumerate(K_NAMES)}
+
+    def download_into(self, out):
+        """Download into caller arrays (e.g. pinned host buffers)."""
+        self._ck(self.lib.mcpm_download_particles(self.h, self.N, _dp(out["x1"]), _dp(out["x2"]), _dp(out["U1"]),
+                                                  _dp(out["U2"]), _dp(out["U3"])), "download_particles")
+
+    @property
+    def kernel_launches(self):
+        return int(self.lib.mcpm_kernel_launches(self.h))
+
+
+def cell_field(cells, name, cell_major=False):
+    """Slice one named field out of a [CF_COUNT][C] (or [C][CF_COUNT]) array."""
+    o, w = CF[name], CF_WIDTH[name]
+    if cell_major:
+        v = cells[:, o:o + w]
+        return v[:, 0] if w == 1 else v
+    v = cells[o:o + w]
+    return v[0] if w == 1 else v.T

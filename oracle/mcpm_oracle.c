@@ -1,0 +1,1190 @@
+/*
+ * mcpm_oracle.c -- CPU restatement (FP64) of the reference particle step.
+ *
+ * TEST INFRASTRUCTURE ONLY (see mcpm_oracle.h).  Built with -O2
+ * -ffp-contract=off so that every multiply and add rounds separately, as in
+ * the reference built for x86-64 without FMA.  Expressions keep the reference's
+ * evaluation order (C evaluates left to right), which is what makes the
+ * bit-for-bit comparison against oracle/_ref possible.
+ */
+#include "mcpm_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define CF MCPM_CF_COUNT
+#define CELL(s, c, f) ((s)->cell[(size_t)(c) * CF + (f)])
+
+enum { RNG_STREAM_FP = 0, RNG_STREAM_BC = 1, RNG_STREAM_ESMC = 2,
+       RNG_STREAM_BIN = 3, RNG_STREAM_ESMC_ACC = 4, RNG_STREAM_ESMC_M = 5 };
+
+struct orc_state {
+  mcpm_config cfg;
+  int64_t N;
+  int N0, N1, C;
+  double dx, dy, dz;
+  double* cell;      /* [C][CF] */
+  int* cnt;          /* num_inside */
+  int* off;          /* list offsets (C+1) */
+  int* list;         /* per-cell particle ids, ascending */
+  int32_t* index;    /* cell of each particle */
+  int step;
+  int status;
+  int rng_mode;
+  double* inj;       /* 3N injected normals */
+  double* xi;        /* 3N whitened normals (random_generator output) */
+};
+
+/* ------------------------------------------------------------------ RNG -- */
+/* Philox4x32-10, J. K. Salmon et al., "Parallel random numbers: as easy as
+   1, 2, 3", SC'11: ten rounds of two 32x32->64 multiplies with the published
+   multipliers and Weyl key increments. */
+void orc_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2],
+                       uint32_t out[4]) {
+  uint32_t c0 = ctr[0], c1 = ctr[1], c2 = ctr[2], c3 = ctr[3];
+  uint32_t k0 = key[0], k1 = key[1];
+  for (int r = 0; r < 10; ++r) {
+    uint64_t p0 = (uint64_t)0xD2511F53u * c0;
+    uint64_t p1 = (uint64_t)0xCD9E8D57u * c2;
+    uint32_t n0 = (uint32_t)(p1 >> 32) ^ c1 ^ k0;
+    uint32_t n1 = (uint32_t)p1;
+    uint32_t n2 = (uint32_t)(p0 >> 32) ^ c3 ^ k1;
+    uint32_t n3 = (uint32_t)p0;
+    c0 = n0; c1 = n1; c2 = n2; c3 = n3;
+    k0 += 0x9E3779B9u;
+    k1 += 0xBB67AE85u;
+  }
+  out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
+}
+
+static void philox(uint64_t seed, uint32_t c0, uint32_t c1, uint32_t c2,
+                   uint32_t c3, uint32_t out[4]) {
+  uint32_t ctr[4] = {c0, c1, c2, c3};
+  uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
+  orc_philox4x32_10(ctr, key, out);
+}
+
+static double u01(uint32_t x) { return ((double)x + 0.5) * (1.0 / 4294967296.0); }
+
+static const double TWO_PI = 6.283185307179586476925286766559;
+
+/* four standard normals by two Box-Muller pairs on the four Philox words */
+void orc_normals4(uint64_t seed, uint32_t c0, uint32_t c1, uint32_t c2,
+                  uint32_t c3, double z[4]) {
+  uint32_t r[4];
+  philox(seed, c0, c1, c2, c3, r);
+  double a = sqrt(-2.0 * log(u01(r[0])));
+  double b = sqrt(-2.0 * log(u01(r[2])));
+  z[0] = a * cos(TWO_PI * u01(r[1]));
+  z[1] = a * sin(TWO_PI * u01(r[1]));
+  z[2] = b * cos(TWO_PI * u01(r[3]));
+  z[3] = b * sin(TWO_PI * u01(r[3]));
+}
+
+/* uniform integer in [0, n) from one Philox word */
+static int pick(uint32_t r, int n) { return (int)(((uint64_t)r * (uint64_t)n) >> 32); }
+
+/* ------------------------------------------------------- small helpers -- */
+/* increase_collision_rate, src/Main_Functions.cpp:1906-1915 */
+static double Ycoll(const orc_state* s, double n) {
+  double nb = n * s->cfg.b;
+  return 1.0 + 0.625 * n * s->cfg.b + 0.2869 * pow(nb, 2.0) + 0.115 * pow(nb, 3.0);
+}
+/* scale_mu, src/Main_Functions.cpp:1970-1973 */
+static double scale_mu(const orc_state* s, double T) {
+  return s->cfg.mu * pow(T / s->cfg.T0, s->cfg.visp);
+}
+/* the cell volume exactly as make_cells builds it, src/myIO.cpp:1456-1465 */
+static double cell_volume(const orc_state* s, int c) {
+  int j = c % s->N0, k = c / s->N0;
+  double d0 = (double)j * s->dx, d1 = (double)(j + 1) * s->dx;
+  double d2 = (double)k * s->dy, d3 = (double)(k + 1) * s->dy;
+  double d4 = 0.0 * s->dz, d5 = 1.0 * s->dz;
+  return (d1 - d0) * (d3 - d2) * (d5 - d4);
+}
+
+/* ----------------------------------------------------------- lifecycle -- */
+orc_state* orc_create(const mcpm_config* cfg, int64_t n_particles) {
+  orc_state* s = (orc_state*)calloc(1, sizeof(orc_state));
+  s->cfg = *cfg;
+  s->N = n_particles;
+  s->N0 = cfg->n_cells[0];
+  s->N1 = cfg->n_cells[1];
+  s->C = s->N0 * s->N1;
+  s->dx = cfg->length[0] / cfg->n_cells[0];
+  s->dy = cfg->length[1] / cfg->n_cells[1];
+  s->dz = cfg->length[2] / cfg->n_cells[2];
+  s->cell = (double*)calloc((size_t)s->C * CF, sizeof(double));
+  s->cnt = (int*)calloc(s->C, sizeof(int));
+  s->off = (int*)calloc(s->C + 1, sizeof(int));
+  s->list = (int*)calloc(n_particles > 0 ? n_particles : 1, sizeof(int));
+  s->index = (int32_t*)calloc(n_particles > 0 ? n_particles : 1, sizeof(int32_t));
+  s->inj = (double*)calloc(3 * (n_particles > 0 ? n_particles : 1), sizeof(double));
+  s->xi = (double*)calloc(3 * (n_particles > 0 ? n_particles : 1), sizeof(double));
+  return s;
+}
+
+void orc_destroy(orc_state* s) {
+  if (!s) return;
+  free(s->cell); free(s->cnt); free(s->off); free(s->list); free(s->index);
+  free(s->inj); free(s->xi); free(s);
+}
+
+int orc_num_cells(const orc_state* s) { return s->C; }
+void orc_get_cells(const orc_state* s, double* out) {
+  memcpy(out, s->cell, sizeof(double) * (size_t)s->C * CF);
+}
+void orc_set_cell_field(orc_state* s, int f, const double* v) {
+  for (int c = 0; c < s->C; ++c) CELL(s, c, f) = v[c];
+}
+int orc_get_step(const orc_state* s) { return s->step; }
+void orc_set_step(orc_state* s, int step) { s->step = step; }
+int orc_status(orc_state* s) { int st = s->status; s->status = 0; return st; }
+void orc_set_rng(orc_state* s, int mode) { s->rng_mode = mode; }
+void orc_inject_normals(orc_state* s, const double* a, const double* b,
+                        const double* c) {
+  for (int64_t i = 0; i < s->N; ++i) {
+    s->inj[i] = a[i]; s->inj[s->N + i] = b[i]; s->inj[2 * s->N + i] = c[i];
+  }
+  s->rng_mode = MCPM_RNG_INJECTED;
+}
+
+/* --------------------------------------------------------- Gauss-Jordan -- */
+/* maxx_magnittude, src/Math_Func.cpp:107-119: first index of the largest |a| */
+static int maxx_magnitude(const double* a, int n) {
+  double b = fabs(a[0]);
+  int l = 0;
+  for (int i = 0; i < n; ++i)
+    if (fabs(b) < fabs(a[i])) { b = fabs(a[i]); l = i; }
+  return l;
+}
+/* Scalling, src/Math_Func.cpp:159-163 */
+static double scaling(const double* row, int i, int n) {
+  int b = maxx_magnitude(row, n);
+  return fabs(row[i]) / fabs(row[b]);
+}
+/* Gauss_Jordan, src/Math_Func.cpp:165-232: forward elimination with scaled
+   partial pivoting (full-row updates, reciprocal-then-multiply factor),
+   then back substitution. */
+void orc_gauss_jordan(double* A, double* RHS, int n, double* x) {
+  double z[16];
+  for (int i = 0; i < n - 1; ++i) {
+    for (int ii = 0; ii < n; ++ii) z[ii] = 0.0;
+    int k = 0;
+    for (int j = i; j < n; ++j) { z[k] = scaling(&A[j * n], i, n); k++; }
+    k = maxx_magnitude(z, n);
+    k = i + k;
+    if (i != k && k < n) {
+      for (int j = 0; j < n; ++j) {
+        double b = A[i * n + j]; A[i * n + j] = A[k * n + j]; A[k * n + j] = b;
+      }
+      double c = RHS[i]; RHS[i] = RHS[k]; RHS[k] = c;
+    }
+    for (int j = i + 1; j < n; ++j) {
+      double Factor = (1.0 / A[i * n + i]) * A[j * n + i];
+      for (int kk = 0; kk < n; ++kk) A[j * n + kk] = A[j * n + kk] - Factor * A[i * n + kk];
+      RHS[j] = RHS[j] - Factor * RHS[i];
+    }
+  }
+  for (int i = n - 1; i >= 0; --i) {
+    double a = 0;
+    for (int j = i + 1; j < n; ++j) a = a + A[i * n + j] * x[j];
+    x[i] = (RHS[i] - a) / (A[i * n + i]);
+  }
+}
+
+/* --------------------------------------------------- Gauss-Legendre tables */
+/* The reference hard-codes Gauss-Legendre tables: 50 points printed to 8
+   decimals (src/Main_Functions.cpp:3327-3346, :3649-3667, src/FEM.cpp:346-364)
+   and 100 points in full precision (src/FEM.cpp:636-637).  Both are the
+   Legendre roots and weights on [-1,1]; we compute them by Newton iteration
+   and round the 50-point table to 8 decimals as the reference's literals are. */
+void orc_gl_table(int n, double* xs, double* ws) {
+  for (int i = 0; i < n; ++i) {
+    double x = cos(3.14159265358979323846 * (i + 0.75) / (n + 0.5));
+    double dp = 0.0;
+    for (int it = 0; it < 100; ++it) {
+      double p0 = 1.0, p1 = x;
+      for (int k = 2; k <= n; ++k) {
+        double p2 = ((2.0 * k - 1.0) * x * p1 - (k - 1.0) * p0) / k;
+        p0 = p1; p1 = p2;
+      }
+      dp = n * (x * p1 - p0) / (x * x - 1.0);
+      double dx = p1 / dp;
+      x -= dx;
+      if (fabs(dx) < 1e-17) break;
+    }
+    {
+      double p0 = 1.0, p1 = x;
+      for (int k = 2; k <= n; ++k) {
+        double p2 = ((2.0 * k - 1.0) * x * p1 - (k - 1.0) * p0) / k;
+        p0 = p1; p1 = p2;
+      }
+      dp = n * (x * p1 - p0) / (x * x - 1.0);
+    }
+    /* ascending order */
+    xs[n - 1 - i] = x;
+    ws[n - 1 - i] = 2.0 / ((1.0 - x * x) * dp * dp);
+  }
+  for (int i = 0; i < n / 2; ++i) { /* exact symmetry */
+    double xa = 0.5 * (xs[n - 1 - i] - xs[i]);
+    double wa = 0.5 * (ws[n - 1 - i] + ws[i]);
+    xs[i] = -xa; xs[n - 1 - i] = xa; ws[i] = wa; ws[n - 1 - i] = wa;
+  }
+  if (n == 50) {
+    for (int i = 0; i < n; ++i) {
+      xs[i] = nearbyint(xs[i] * 1e8) / 1e8;
+      ws[i] = nearbyint(ws[i] * 1e8) / 1e8;
+    }
+  }
+}
+
+/* ---------------------------------------------------------- cell_update -- */
+/* binning, src/Main_Functions.cpp:2231-2266, and the per-cell index lists,
+   :2367-2376 (ascending particle id within a cell). */
+static void bin_particles(orc_state* s, const double* x1, const double* x2) {
+  const mcpm_config* g = &s->cfg;
+  for (int c = 0; c < s->C; ++c) s->cnt[c] = 0;
+  for (int64_t i = 0; i < s->N; ++i) {
+    int j = 0, k;
+    if (g->direction[0] == 1) j = (int)floor(x1[i] / s->dx);
+    k = (int)floor(x2[i] / s->dy);
+    if (k > 0 && k < s->N1 - 1) {
+      if (fabs(x2[i] - s->dy * k) < 1e-15 || fabs(x2[i] - s->dy * (k + 1)) < 1e-15) {
+        uint32_t r[4];
+        philox(g->seed, (uint32_t)i, (uint32_t)s->step, RNG_STREAM_BIN, 0, r);
+        int sgn = (u01(r[0]) > 0.5) ? 1 : -1;
+        k = (int)floor((x2[i] + 1e-14 * sgn) / s->dy);
+      }
+    }
+    /* the reference exits on an out-of-box particle; a particle on the far
+       wall (x == Len, or x/dx rounding up to N) is binned into the last cell */
+    if (g->direction[0] == 1 && !(x1[i] >= 0.0 && x1[i] <= g->length[0]))
+      s->status |= MCPM_ERR_OUT_OF_BOX;
+    if (!(x2[i] >= 0.0 && x2[i] <= g->length[1])) s->status |= MCPM_ERR_OUT_OF_BOX;
+    if (j < 0) j = 0;
+    if (j > s->N0 - 1) j = s->N0 - 1;
+    if (k < 0) k = 0;
+    if (k > s->N1 - 1) k = s->N1 - 1;
+    int num = k * s->N0 + j;
+    s->index[i] = num;
+    s->cnt[num]++;
+  }
+  s->off[0] = 0;
+  for (int c = 0; c < s->C; ++c) s->off[c + 1] = s->off[c] + s->cnt[c];
+  int* fill = (int*)calloc(s->C, sizeof(int));
+  for (int64_t i = 0; i < s->N; ++i) {
+    int num = s->index[i];
+    s->list[s->off[num] + fill[num]] = (int)i;
+    fill[num]++;
+  }
+  free(fill);
+}
+
+/* moments, src/Main_Functions.cpp:2461-2593 */
+static void moments(orc_state* s, const double* U1, const double* U2,
+                    const double* U3) {
+  const mcpm_config* g = &s->cfg;
+  for (int num = 0; num < s->C; ++num) {
+    double us0 = 0.0, us1 = 0.0, us2 = 0.0, weight = 0.0;
+    int n_in = s->cnt[num];
+    const int* L = &s->list[s->off[num]];
+    for (int i = 0; i < n_in; ++i) {
+      int id = L[i];
+      double w = 1.0;
+      us0 = us0 + U1[id] * w;
+      us1 = us1 + U2[id] * w;
+      us2 = us2 + U3[id] * w;
+      weight += w;
+    }
+    if (n_in > 0) { us0 = us0 / weight; us1 = us1 / weight; us2 = us2 / weight; }
+    double P[6] = {0}, M3[10] = {0}, M4[6] = {0}, M5[3] = {0}, Mp[3] = {0};
+    double DM2 = 0.0, DM4 = 0.0, Q[3] = {0};
+    for (int i = 0; i < n_in; ++i) {
+      int id = L[i];
+      double w = 1.0;
+      double Mp1 = U1[id] - us0, Mp2 = U2[id] - us1, Mp3 = U3[id] - us2;
+      Mp[0] += Mp1 * w; Mp[1] += Mp2 * w; Mp[2] += Mp3 * w;
+      P[0] = P[0] + Mp1 * Mp1 * w;
+      P[1] = P[1] + Mp1 * Mp2 * w;
+      P[2] = P[2] + Mp1 * Mp3 * w;
+      P[3] = P[3] + Mp2 * Mp2 * w;
+      P[4] = P[4] + Mp2 * Mp3 * w;
+      P[5] = P[5] + Mp3 * Mp3 * w;
+      double energy = Mp1 * Mp1 + Mp2 * Mp2 + Mp3 * Mp3;
+      M3[0] = M3[0] + Mp1 * Mp1 * Mp1 * w;
+      M3[1] = M3[1] + Mp1 * Mp1 * Mp2 * w;
+      M3[2] = M3[2] + Mp1 * Mp1 * Mp3 * w;
+      M3[3] = M3[3] + Mp1 * Mp2 * Mp2 * w;
+      M3[4] = M3[4] + Mp1 * Mp2 * Mp3 * w;
+      M3[5] = M3[5] + Mp1 * Mp3 * Mp3 * w;
+      M3[6] = M3[6] + Mp2 * Mp2 * Mp2 * w;
+      M3[7] = M3[7] + Mp2 * Mp2 * Mp3 * w;
+      M3[8] = M3[8] + Mp2 * Mp3 * Mp3 * w;
+      M3[9] = M3[9] + Mp3 * Mp3 * Mp3 * w;
+      M4[0] = M4[0] + Mp1 * Mp1 * energy * w;
+      M4[1] = M4[1] + Mp1 * Mp2 * energy * w;
+      M4[2] = M4[2] + Mp1 * Mp3 * energy * w;
+      M4[3] = M4[3] + Mp2 * Mp2 * energy * w;
+      M4[4] = M4[4] + Mp2 * Mp3 * energy * w;
+      M4[5] = M4[5] + Mp3 * Mp3 * energy * w;
+      M5[0] = M5[0] + Mp1 * energy * energy * w;
+      M5[1] = M5[1] + Mp2 * energy * energy * w;
+      M5[2] = M5[2] + Mp3 * energy * energy * w;
+      DM2 = DM2 + energy * w;
+    }
+    if (n_in > 0) {
+      for (int j = 0; j < 6; ++j) P[j] = P[j] / weight;
+      for (int j = 0; j < 10; ++j) M3[j] = M3[j] / weight;
+      for (int j = 0; j < 6; ++j) M4[j] = M4[j] / weight;
+      for (int j = 0; j < 3; ++j) M5[j] = M5[j] / weight;
+      for (int j = 0; j < 3; ++j) Mp[j] = Mp[j] / weight;
+      DM2 = DM2 / weight;
+      DM4 = M4[0] + M4[3] + M4[5];
+      Q[0] = M3[0] + M3[3] + M3[5];
+      Q[1] = M3[1] + M3[6] + M3[8];
+      Q[2] = M3[2] + M3[7] + M3[9];
+    }
+    CELL(s, num, MCPM_CF_NUM_INSIDE) = n_in;
+    CELL(s, num, MCPM_CF_U_SPACE + 0) = us0;
+    CELL(s, num, MCPM_CF_U_SPACE + 1) = us1;
+    CELL(s, num, MCPM_CF_U_SPACE + 2) = us2;
+    for (int j = 0; j < 6; ++j) CELL(s, num, MCPM_CF_PIJ + j) = P[j];
+    for (int j = 0; j < 10; ++j) CELL(s, num, MCPM_CF_M3 + j) = M3[j];
+    for (int j = 0; j < 6; ++j) CELL(s, num, MCPM_CF_M4 + j) = M4[j];
+    for (int j = 0; j < 3; ++j) CELL(s, num, MCPM_CF_M5 + j) = M5[j];
+    for (int j = 0; j < 3; ++j) CELL(s, num, MCPM_CF_Q + j) = Q[j];
+    for (int j = 0; j < 3; ++j) CELL(s, num, MCPM_CF_MP + j) = Mp[j];
+    CELL(s, num, MCPM_CF_DM2) = DM2;
+    CELL(s, num, MCPM_CF_DM4) = DM4;
+    double T = g->m * DM2 / (3.0 * g->kb);
+    double n = 1 * g->Fn * weight / cell_volume(s, num);
+    CELL(s, num, MCPM_CF_T) = T;
+    CELL(s, num, MCPM_CF_N) = n;
+    double Y = Ycoll(s, n);
+    if (weight > 1e-14)
+      CELL(s, num, MCPM_CF_GAMMA_ST) = -0.001 * (n * g->b * Y / (g->kb * T / g->m));
+  }
+}
+
+/* Lambda closed form, src/Main_Functions.cpp:2718-2728 */
+static void lambda_cells(orc_state* s) {
+  const mcpm_config* g = &s->cfg;
+  for (int num = 0; num < s->C; ++num) {
+    if (!(CELL(s, num, MCPM_CF_NUM_INSIDE) > 1e-14)) continue;
+    const double* P = &CELL(s, num, MCPM_CF_PIJ);
+    double DM2 = CELL(s, num, MCPM_CF_DM2), T = CELL(s, num, MCPM_CF_T);
+    double n = CELL(s, num, MCPM_CF_N);
+    double mu = scale_mu(s, T);
+    double tau = 2.0 * mu / (n * g->kb * T);
+    double L = (P[0] - DM2 / 3.0) * ((P[3] - DM2 / 3.0) * (P[5] - DM2 / 3.0) - P[4] * P[4]);
+    L = L - P[1] * (P[1] * (P[5] - DM2 / 3.0) - P[4] * P[2]);
+    L = L + P[2] * (P[1] * P[4] - P[2] * (P[3] - DM2 / 3.0));
+    L = -L / (tau * pow(DM2, 4.0));
+    CELL(s, num, MCPM_CF_LAMBDA) = L;
+  }
+}
+
+/* alpha_calculation, src/Fokker_Planck.cpp:200-587 (the live "with bulk
+   term" branch).  div_U uses the linear neighbours num-1, num+1
+   (src/Fokker_Planck.cpp:443-451); for the last cell of a 2-D grid, where the
+   reference reads one past the end of the cell array, the one-sided
+   difference of the upper end is used. */
+static void alpha_cells(orc_state* s) {
+  const mcpm_config* g = &s->cfg;
+  const double pi = acos(-1.0);
+  double A[144], rhs[12], x[12];
+  for (int num = 0; num < s->C; ++num) {
+    if (s->cnt[num] < 2) {
+      for (int ii = 0; ii < 9; ++ii) CELL(s, num, MCPM_CF_ALPHA + ii) = 0.0;
+      for (int ii = 0; ii < 3; ++ii) CELL(s, num, MCPM_CF_BETA + ii) = 0.0;
+      continue;
+    }
+    const double* P = &CELL(s, num, MCPM_CF_PIJ);
+    const double* M3 = &CELL(s, num, MCPM_CF_M3);
+    const double* M4 = &CELL(s, num, MCPM_CF_M4);
+    const double* M5 = &CELL(s, num, MCPM_CF_M5);
+    double DM2 = CELL(s, num, MCPM_CF_DM2);
+    double n = CELL(s, num, MCPM_CF_N), T = CELL(s, num, MCPM_CF_T);
+    double gst = CELL(s, num, MCPM_CF_GAMMA_ST);
+    double trace = P[0] + P[3] + P[5];
+    double dev[6];
+    for (int ii = 0; ii < 6; ++ii) dev[ii] = P[ii];
+    dev[0] = dev[0] - (1.0 / 3.0) * trace;
+    dev[3] = dev[3] - (1.0 / 3.0) * trace;
+    dev[5] = dev[5] - (1.0 / 3.0) * trace;
+    double a = M3[0] + M3[3] + M3[5];
+    double b = M3[1] + M3[6] + M3[8];
+    double c = M3[2] + M3[7] + M3[9];
+    double d = M4[0] + M4[3] + M4[5] - DM2 * DM2;
+    for (int ii = 0; ii < 144; ++ii) A[ii] = 0.0;
+#define AA(r, q) A[(r) * 12 + (q)]
+    AA(0, 0) = P[0]; AA(0, 1) = P[1]; AA(0, 2) = P[2]; AA(0, 9) = a;
+    AA(1, 0) = P[1]; AA(1, 1) = P[3]; AA(1, 2) = P[4]; AA(1, 9) = a;
+    AA(2, 0) = P[2]; AA(2, 1) = P[4]; AA(2, 2) = P[5]; AA(2, 9) = a;
+    AA(3, 3) = P[0]; AA(3, 4) = P[1]; AA(3, 5) = P[2]; AA(3, 10) = b;
+    AA(4, 3) = P[1]; AA(4, 4) = P[3]; AA(4, 5) = P[4]; AA(4, 10) = b;
+    AA(5, 3) = P[2]; AA(5, 4) = P[4]; AA(5, 5) = P[5]; AA(5, 10) = b;
+    AA(6, 6) = P[0]; AA(6, 7) = P[1]; AA(6, 8) = P[2]; AA(6, 11) = c;
+    AA(7, 6) = P[1]; AA(7, 7) = P[3]; AA(7, 8) = P[4]; AA(7, 11) = c;
+    AA(8, 6) = P[2]; AA(8, 7) = P[4]; AA(8, 8) = P[5]; AA(8, 11) = c;
+    AA(9, 0) = a; AA(9, 1) = b; AA(9, 2) = c; AA(9, 9) = d;
+    AA(10, 3) = a; AA(10, 4) = b; AA(10, 5) = c; AA(10, 10) = d;
+    AA(11, 6) = a; AA(11, 7) = b; AA(11, 8) = c; AA(11, 11) = d;
+#undef AA
+    double Y = Ycoll(s, n);
+    double p_crr = (1.0 + n * g->b * Y);
+    double mu_crr = (1.0 + 2.0 * n * g->b * Y / 5.0);
+    double k_crr = (1.0 + 3.0 * n * g->b * Y / 5.0);
+    double w = (4.0 / 9.0) * sqrt(pi) * Y * pow(n, 2.0) * pow(g->sigma, 4.0) * sqrt(g->m * g->kb * T);
+    double div_U;
+    int last = s->C - 1;
+    if (s->C == 1) {
+      div_U = 0.0;
+    } else if (num == 0) {
+      div_U = (CELL(s, num + 1, MCPM_CF_U_SPACE + 1) - CELL(s, num, MCPM_CF_U_SPACE + 1)) / s->dy;
+    } else if (num == s->N1 - 1 || num == last) {
+      div_U = (CELL(s, num, MCPM_CF_U_SPACE + 1) - CELL(s, num - 1, MCPM_CF_U_SPACE + 1)) / s->dy;
+    } else {
+      div_U = (CELL(s, num + 1, MCPM_CF_U_SPACE + 1) - CELL(s, num - 1, MCPM_CF_U_SPACE + 1)) / s->dy / 2.0;
+    }
+    CELL(s, num, MCPM_CF_DIVU) = div_U;
+    double coeff_mu = 3.0 * 1.002 / 5.0 * pow(n * g->b * Y, 2.0) / (1 + 2.0 * n * g->b * Y / 5.0);
+    double coeff_k = 1.002 * pow(n * g->b * Y, 2.0) / (1 + 3.0 * n * g->b * Y / 5.0) / 5.0;
+    rhs[0] = (mu_crr - 1.0) * dev[0] + (p_crr - 1.0) * trace / 3.0 - w * div_U / (g->m * n) + coeff_mu * dev[0] - gst * M4[0];
+    rhs[1] = (mu_crr - 1.0) * dev[1] + coeff_mu * dev[1] - gst * M4[1];
+    rhs[2] = (mu_crr - 1.0) * dev[2] + coeff_mu * dev[2] - gst * M4[2];
+    rhs[3] = (mu_crr - 1.0) * dev[1] + coeff_mu * dev[1] - gst * M4[1];
+    rhs[4] = (mu_crr - 1.0) * dev[3] + (p_crr - 1.0) * trace / 3.0 - w * div_U / (g->m * n) + coeff_mu * dev[3] - gst * M4[3];
+    rhs[5] = (mu_crr - 1.0) * dev[4] + coeff_mu * dev[4] - gst * M4[4];
+    rhs[6] = (mu_crr - 1.0) * dev[2] + coeff_mu * dev[2] - gst * M4[2];
+    rhs[7] = (mu_crr - 1.0) * dev[4] + coeff_mu * dev[4] - gst * M4[4];
+    rhs[8] = (mu_crr - 1.0) * dev[5] + (p_crr - 1.0) * trace / 3.0 - w * div_U / (g->m * n) + coeff_mu * dev[5] - gst * M4[5];
+    rhs[9] = (k_crr - 1.0) * a + coeff_k * a - gst * (M5[0]) + gst * (DM2 * (M3[0] + M3[3] + M3[5]));
+    rhs[10] = (k_crr - 1.0) * b + coeff_k * b - gst * (M5[1]) + gst * (DM2 * (M3[1] + M3[6] + M3[8]));
+    rhs[11] = (k_crr - 1.0) * c + coeff_k * c - gst * (M5[2]) + gst * (DM2 * (M3[2] + M3[7] + M3[9]));
+    orc_gauss_jordan(A, rhs, 12, x);
+    for (int ii = 0; ii < 12; ++ii)
+      if (x[ii] != x[ii]) s->status |= MCPM_ERR_NAN;
+    for (int ii = 0; ii < 9; ++ii) CELL(s, num, MCPM_CF_ALPHA + ii) = x[ii];
+    for (int ii = 0; ii < 3; ++ii) CELL(s, num, MCPM_CF_BETA + ii) = x[9 + ii];
+  }
+}
+
+/* c_gamma_calculation, src/Fokker_Planck.cpp:590-804 */
+static void c_gamma_cells(orc_state* s) {
+  const mcpm_config* g = &s->cfg;
+  double A[81], rhs[9], x[9];
+  for (int num = 0; num < s->C; ++num) {
+    if (s->cnt[num] < 2) {
+      for (int ii = 0; ii < 6; ++ii) CELL(s, num, MCPM_CF_C + ii) = 0.0;
+      for (int ii = 0; ii < 3; ++ii) CELL(s, num, MCPM_CF_GAMMA + ii) = 0.0;
+      continue;
+    }
+    const double* P = &CELL(s, num, MCPM_CF_PIJ);
+    const double* M3 = &CELL(s, num, MCPM_CF_M3);
+    const double* M4 = &CELL(s, num, MCPM_CF_M4);
+    const double* M5 = &CELL(s, num, MCPM_CF_M5);
+    const double* Q = &CELL(s, num, MCPM_CF_Q);
+    double DM2 = CELL(s, num, MCPM_CF_DM2), DM4 = CELL(s, num, MCPM_CF_DM4);
+    double n = CELL(s, num, MCPM_CF_N), T = CELL(s, num, MCPM_CF_T);
+    double Lam = CELL(s, num, MCPM_CF_LAMBDA);
+    for (int ii = 0; ii < 81; ++ii) A[ii] = 0.0;
+    for (int ii = 0; ii < 9; ++ii) { rhs[ii] = 0.0; x[ii] = 0.0; }
+#define AA(r, q) A[(r) * 9 + (q)]
+    AA(0, 0) = 2.0 * P[0]; AA(0, 1) = 2.0 * P[1]; AA(0, 2) = 2.0 * P[2]; AA(0, 6) = 2.0 * Q[0];
+    AA(1, 0) = P[1]; AA(1, 1) = P[0] + P[3]; AA(1, 2) = P[4]; AA(1, 3) = P[1]; AA(1, 4) = P[2];
+    AA(1, 6) = Q[1]; AA(1, 7) = Q[0];
+    AA(2, 0) = P[2]; AA(2, 1) = P[4]; AA(2, 2) = P[0] + P[5]; AA(2, 4) = P[1]; AA(2, 5) = P[2];
+    AA(2, 6) = Q[2]; AA(2, 8) = Q[0];
+    AA(3, 1) = 2.0 * P[1]; AA(3, 3) = 2.0 * P[3]; AA(3, 4) = 2.0 * P[4]; AA(3, 7) = 2.0 * Q[1];
+    AA(4, 1) = P[2]; AA(4, 2) = P[1]; AA(4, 3) = P[4]; AA(4, 4) = P[3] + P[5]; AA(4, 5) = P[4];
+    AA(4, 7) = Q[2]; AA(4, 8) = Q[1];
+    AA(5, 2) = 2.0 * P[2]; AA(5, 4) = 2.0 * P[4]; AA(5, 5) = 2.0 * P[5]; AA(5, 8) = 2.0 * Q[2];
+    AA(6, 0) = Q[0] + 2.0 * M3[0]; AA(6, 1) = Q[1] + 4.0 * M3[1]; AA(6, 2) = Q[2] + 4.0 * M3[2];
+    AA(6, 3) = 2.0 * M3[3]; AA(6, 4) = 4.0 * M3[4]; AA(6, 5) = 2.0 * M3[5];
+    AA(6, 6) = 2.0 * M4[0] - 2.0 * P[0] * DM2; AA(6, 7) = 2.0 * M4[1] - 2.0 * P[1] * DM2;
+    AA(6, 8) = 2.0 * M4[2] - 2.0 * P[2] * DM2;
+    AA(7, 0) = 2.0 * M3[1]; AA(7, 1) = Q[0] + 4.0 * M3[3]; AA(7, 2) = 4.0 * M3[4];
+    AA(7, 3) = Q[1] + 2.0 * M3[6]; AA(7, 4) = Q[2] + 4.0 * M3[7]; AA(7, 5) = 2.0 * M3[8];
+    AA(7, 6) = 2.0 * M4[1] - 2.0 * P[1] * DM2; AA(7, 7) = 2.0 * M4[3] - 2.0 * P[3] * DM2;
+    AA(7, 8) = 2.0 * M4[4] - 2.0 * P[4] * DM2;
+    AA(8, 0) = 2.0 * M3[2]; AA(8, 1) = 4.0 * M3[4]; AA(8, 2) = Q[0] + 4.0 * M3[5];
+    AA(8, 3) = 2.0 * M3[7]; AA(8, 4) = Q[1] + 4.0 * M3[8]; AA(8, 5) = Q[2] + 2.0 * M3[9];
+    AA(8, 6) = 2.0 * M4[2] - 2.0 * P[2] * DM2; AA(8, 7) = 2.0 * M4[4] - 2.0 * P[4] * DM2;
+    AA(8, 8) = 2.0 * M4[5] - 2.0 * P[5] * DM2;
+    AA(6, 6) += DM4 - (DM2) * (DM2);
+    AA(7, 7) += DM4 - (DM2) * (DM2);
+    AA(8, 8) += DM4 - (DM2) * (DM2);
+#undef AA
+    double Pr = 2.0 / 3.0;
+    double Y = (g->model == MCPM_MODEL_FP_DENSE) ? Ycoll(s, n) : 1.0;
+    double mu = scale_mu(s, T);
+    double tau = 2.0 * mu / (n * g->kb * T);
+    for (int ii = 0; ii < 6; ++ii) rhs[ii] = -2.0 * Lam * M4[ii];
+    rhs[6] = Y * (3.0 / tau - 2.0 * Pr / tau) * Q[0];
+    rhs[7] = Y * (3.0 / tau - 2.0 * Pr / tau) * Q[1];
+    rhs[8] = Y * (3.0 / tau - 2.0 * Pr / tau) * Q[2];
+    rhs[6] += Lam * (-3.0 * M5[0] + DM2 * Q[0] + 2.0 * (P[0] * Q[0] + P[1] * Q[1] + P[2] * Q[2]));
+    rhs[7] += Lam * (-3.0 * M5[1] + DM2 * Q[1] + 2.0 * (P[1] * Q[0] + P[3] * Q[1] + P[4] * Q[2]));
+    rhs[8] += Lam * (-3.0 * M5[2] + DM2 * Q[2] + 2.0 * (P[2] * Q[0] + P[4] * Q[1] + P[5] * Q[2]));
+    orc_gauss_jordan(A, rhs, 9, x);
+    for (int ii = 0; ii < 6; ++ii) CELL(s, num, MCPM_CF_C + ii) = x[ii];
+    for (int ii = 0; ii < 3; ++ii) CELL(s, num, MCPM_CF_GAMMA + ii) = x[6 + ii];
+  }
+}
+
+/* phi = alpha * <M'>, src/Main_Functions.cpp:2734-2746 */
+static void phi_cells(orc_state* s) {
+  for (int num = 0; num < s->C; ++num) {
+    const double* al = &CELL(s, num, MCPM_CF_ALPHA);
+    const double* Mp = &CELL(s, num, MCPM_CF_MP);
+    CELL(s, num, MCPM_CF_PHI + 0) = al[0] * Mp[0] + al[1] * Mp[1] + al[2] * Mp[2];
+    CELL(s, num, MCPM_CF_PHI + 1) = al[3] * Mp[0] + al[4] * Mp[1] + al[5] * Mp[2];
+    CELL(s, num, MCPM_CF_PHI + 2) = al[6] * Mp[0] + al[7] * Mp[1] + al[8] * Mp[2];
+  }
+}
+
+/* cell_update, src/Main_Functions.cpp:2138-2749, for the uniform Cartesian
+   grid.  The kernel-density smoothing (:2378-2427) feeds only long_range 2,
+   which is out of scope, and is not computed. */
+void orc_cell_update(orc_state* s, const double* x1, const double* x2,
+                     const double* U1, const double* U2, const double* U3,
+                     int32_t* index) {
+  bin_particles(s, x1, x2);
+  if (index) memcpy(index, s->index, sizeof(int32_t) * (size_t)s->N);
+  moments(s, U1, U2, U3);
+  lambda_cells(s);
+  int m = s->cfg.model;
+  if (m == MCPM_MODEL_FP_DENSE || m == MCPM_MODEL_FP_IDEAL_GAS) {
+    if (s->step > 0 && m == MCPM_MODEL_FP_DENSE) alpha_cells(s);
+    c_gamma_cells(s);
+  }
+  phi_cells(s);
+}
+
+/* ----------------------------------------------------- random_generator -- */
+/* src/Fokker_Planck.cpp:20-145: 3 draws per particle, centred per cell, then
+   divided by the per-cell RMS when the cell holds more than one particle.
+   Sums run in particle order as in the reference. */
+void orc_random_generator(orc_state* s, double* x1f, double* x2f, double* x3f) {
+  int64_t N = s->N;
+  for (int64_t i = 0; i < N; ++i) {
+    if (s->rng_mode == MCPM_RNG_INJECTED) {
+      x1f[i] = s->inj[i]; x2f[i] = s->inj[N + i]; x3f[i] = s->inj[2 * N + i];
+    } else {
+      double z[4];
+      orc_normals4(s->cfg.seed, (uint32_t)i, (uint32_t)s->step, RNG_STREAM_FP, 0, z);
+      x1f[i] = z[0]; x2f[i] = z[1]; x3f[i] = z[2];
+    }
+  }
+  double* s1 = (double*)calloc(s->C, sizeof(double));
+  double* s2 = (double*)calloc(s->C, sizeof(double));
+  double* s3 = (double*)calloc(s->C, sizeof(double));
+  double* y1 = (double*)malloc(sizeof(double) * (size_t)N);
+  double* y2 = (double*)malloc(sizeof(double) * (size_t)N);
+  double* y3 = (double*)malloc(sizeof(double) * (size_t)N);
+  for (int64_t i = 0; i < N; ++i) {
+    int num = s->index[i];
+    s1[num] += x1f[i]; s2[num] += x2f[i]; s3[num] += x3f[i];
+  }
+  for (int64_t i = 0; i < N; ++i) {
+    int num = s->index[i];
+    y1[i] = x1f[i] - s1[num] / (1.0 * s->cnt[num]);
+    y2[i] = x2f[i] - s2[num] / (1.0 * s->cnt[num]);
+    y3[i] = x3f[i] - s3[num] / (1.0 * s->cnt[num]);
+  }
+  for (int c = 0; c < s->C; ++c) { s1[c] = 0.0; s2[c] = 0.0; s3[c] = 0.0; }
+  for (int64_t i = 0; i < N; ++i) {
+    int num = s->index[i];
+    s1[num] += y1[i] * y1[i]; s2[num] += y2[i] * y2[i]; s3[num] += y3[i] * y3[i];
+  }
+  for (int c = 0; c < s->C; ++c) {
+    s1[c] = sqrt(s1[c] / (1.0 * s->cnt[c]));
+    s2[c] = sqrt(s2[c] / (1.0 * s->cnt[c]));
+    s3[c] = sqrt(s3[c] / (1.0 * s->cnt[c]));
+  }
+  for (int64_t i = 0; i < N; ++i) {
+    int num = s->index[i];
+    if (s->cnt[num] > 1) {
+      x1f[i] = y1[i] / s1[num]; x2f[i] = y2[i] / s2[num]; x3f[i] = y3[i] / s3[num];
+    }
+  }
+  for (int64_t i = 0; i < N; ++i) {
+    s->xi[i] = x1f[i]; s->xi[N + i] = x2f[i]; s->xi[2 * N + i] = x3f[i];
+  }
+  free(s1); free(s2); free(s3); free(y1); free(y2); free(y3);
+}
+
+/* ------------------------------------------------- Velocity_FP_parallel -- */
+/* src/Fokker_Planck.cpp:1065-1182: Ornstein-Uhlenbeck step with the cubic
+   drift, then per-cell rescaling that restores sum |M'|^2 exactly. */
+void orc_velocity_fp(orc_state* s, double* U1, double* U2, double* U3,
+                     const double* xi1, const double* xi2, const double* xi3) {
+  const mcpm_config* g = &s->cfg;
+  int64_t N = s->N;
+  double* frac1 = (double*)calloc(s->C, sizeof(double));
+  double* frac2 = (double*)calloc(s->C, sizeof(double));
+  double* Mp1 = (double*)malloc(sizeof(double) * (size_t)N);
+  double* Mp2 = (double*)malloc(sizeof(double) * (size_t)N);
+  double* Mp3 = (double*)malloc(sizeof(double) * (size_t)N);
+  for (int64_t id = 0; id < N; ++id) {
+    int num = s->index[id];
+    Mp1[id] = U1[id] - CELL(s, num, MCPM_CF_U_SPACE + 0);
+    Mp2[id] = U2[id] - CELL(s, num, MCPM_CF_U_SPACE + 1);
+    Mp3[id] = U3[id] - CELL(s, num, MCPM_CF_U_SPACE + 2);
+    frac1[num] += Mp1[id] * Mp1[id] + Mp2[id] * Mp2[id] + Mp3[id] * Mp3[id];
+  }
+  for (int64_t id = 0; id < N; ++id) {
+    int num = s->index[id];
+    if (s->cnt[num] > 1) {
+      double T = CELL(s, num, MCPM_CF_T), n = CELL(s, num, MCPM_CF_N);
+      double mu = scale_mu(s, T);
+      double tau = 2.0 * mu / (n * g->kb * T);
+      double Y = (g->model == MCPM_MODEL_FP_DENSE) ? Ycoll(s, n) : 1.0;
+      tau = tau / Y;
+      double A1 = exp(-g->dt / tau);
+      double A3 = sqrt((1.0 - exp(-2.0 * g->dt / tau)) * g->kb * T / (1.0 * g->m));
+      double A2 = (1.0 - exp(-g->dt / tau)) * tau;
+      double energy = Mp1[id] * Mp1[id] + Mp2[id] * Mp2[id] + Mp3[id] * Mp3[id];
+      const double* c = &CELL(s, num, MCPM_CF_C);
+      const double* gm = &CELL(s, num, MCPM_CF_GAMMA);
+      const double* Q = &CELL(s, num, MCPM_CF_Q);
+      double Lam = CELL(s, num, MCPM_CF_LAMBDA);
+      double d0, d1, d2;
+      d0 = c[0] * Mp1[id] + c[1] * Mp2[id] + c[2] * Mp3[id];
+      d0 += gm[0] * (energy - 3.0 * g->kb * T / g->m);
+      d0 += Lam * (Mp1[id] * energy - Q[0]);
+      d1 = c[1] * Mp1[id] + c[3] * Mp2[id] + c[4] * Mp3[id];
+      d1 += gm[1] * (energy - 3.0 * g->kb * T / g->m);
+      d1 += Lam * (Mp2[id] * energy - Q[1]);
+      d2 = c[2] * Mp1[id] + c[4] * Mp2[id] + c[5] * Mp3[id];
+      d2 += gm[2] * (energy - 3.0 * g->kb * T / g->m);
+      d2 += Lam * (Mp3[id] * energy - Q[2]);
+      Mp1[id] = A1 * Mp1[id] + A2 * d0 + A3 * xi1[id];
+      Mp2[id] = A1 * Mp2[id] + A2 * d1 + A3 * xi2[id];
+      Mp3[id] = A1 * Mp3[id] + A2 * d2 + A3 * xi3[id];
+    } else {
+      Mp1[id] = 0.0; Mp2[id] = 0.0; Mp3[id] = 0.0;
+    }
+    if (Mp2[id] != Mp2[id]) s->status |= MCPM_ERR_NAN;
+  }
+  for (int64_t id = 0; id < N; ++id) {
+    int num = s->index[id];
+    frac2[num] += Mp1[id] * Mp1[id] + Mp2[id] * Mp2[id] + Mp3[id] * Mp3[id];
+  }
+  for (int64_t id = 0; id < N; ++id) {
+    int num = s->index[id];
+    const double* Us = &CELL(s, num, MCPM_CF_U_SPACE);
+    if (s->cnt[num] > 1) {
+      double r = sqrt(fabs(frac1[num] / frac2[num]));
+      U1[id] = Mp1[id] * r + Us[0];
+      U2[id] = Mp2[id] * r + Us[1];
+      U3[id] = Mp3[id] * r + Us[2];
+    } else {
+      U1[id] = Us[0]; U2[id] = Us[1]; U3[id] = Us[2];
+    }
+  }
+  free(frac1); free(frac2); free(Mp1); free(Mp2); free(Mp3);
+}
+
+/* ------------------------------------------------------------------ ESMC -- */
+/* Collision_ESMC_new3, src/collisions.cpp:583-720, restated per cell.
+   The reference assigns its M = sum_c m_c candidates to cells by sampling
+   candidate slots without replacement through a linear prefix scan
+   (:631-646); that gives every cell exactly its m_c = floor(omega_max/2 N_c+u)
+   candidates, so here each cell simply runs its own m_c candidates.
+   Candidates that may touch the same particle are serialised: cells are
+   processed in colour classes whose partner neighbourhoods (+-R cells,
+   R = ceil(sigma/dx)) are disjoint, candidates of one cell in order.  This
+   is the order the GPU uses.  Per candidate, the physics is the
+   reference's: partner cell at r_i + sigma e, Y at the midpoint, acceptance
+   omega/omega_max > u, no g.e > 0 test, U_i -= (g.e)e, U_j += (g.e)e. */
+static void esmc_cell(orc_state* s, int I, const double* x1, const double* x2,
+                      double* U1, double* U2, double* U3) {
+  const mcpm_config* g = &s->cfg;
+  const double pi = acos(-1.0);
+  int NI = s->cnt[I];
+  uint32_t r[4];
+  philox(g->seed, (uint32_t)I, (uint32_t)s->step, RNG_STREAM_ESMC_M, 0, r);
+  double om_max = CELL(s, I, MCPM_CF_OMEGA_MAX);
+  int mI = (int)floor(0.5 * om_max * (1.0 * NI) + u01(r[0]));
+  double omega = 0.0;
+  if (NI > 0) {
+    for (int k = 0; k < mI; ++k) {
+      philox(g->seed, (uint32_t)I, (uint32_t)s->step, RNG_STREAM_ESMC, (uint32_t)k, r);
+      int i = s->list[s->off[I] + pick(r[0], NI)];
+      double theta = 2.0 * pi * u01(r[1]);
+      double cph = 2.0 * u01(r[2]) - 1.0;
+      double sph = sqrt(1.0 - cph * cph);
+      double dir0 = cos(theta) * sph, dir1 = sin(theta) * sph, dir2 = cph;
+      double xx = x1[i] + g->sigma * dir0;
+      double yy = x2[i] + g->sigma * dir1;
+      int i0 = (int)floor(xx / s->dx), i1 = (int)floor(yy / s->dy);
+      int J = i1 * s->N0 + i0;
+      if (!(i0 >= 0 && i0 < s->N0 && i1 >= 0 && i1 < s->N1)) continue;
+      int NJ = s->cnt[J];
+      if (NJ <= 0) continue;
+      int j = s->list[s->off[J] + pick(r[3], NJ)];
+      if (i == j) continue;
+      double xm0 = (x1[i] + x1[j]) / 2.0, xm1 = (x2[i] + x2[j]) / 2.0;
+      int m0 = (int)floor(xm0 / s->dx), m1 = (int)floor(xm1 / s->dy);
+      if (m0 < 0) m0 = 0; if (m0 > s->N0 - 1) m0 = s->N0 - 1;
+      if (m1 < 0) m1 = 0; if (m1 > s->N1 - 1) m1 = s->N1 - 1;
+      double Ymid = Ycoll(s, CELL(s, m1 * s->N0 + m0, MCPM_CF_N));
+      double g0 = U1[i] - U1[j], g1 = U2[i] - U2[j], g2 = U3[i] - U3[j];
+      double gd = g0 * dir0 + g1 * dir1 + g2 * dir2;
+      double dummy = 4.0 * pi * g->sigma * g->sigma * gd * Ymid * CELL(s, J, MCPM_CF_N) * g->dt;
+      if (dummy - omega > 0.0) omega = dummy;
+      uint32_t ra[4];
+      philox(g->seed, (uint32_t)I, (uint32_t)s->step, RNG_STREAM_ESMC_ACC, (uint32_t)k, ra);
+      if (dummy / om_max > u01(ra[0])) {
+        U1[i] = U1[i] - gd * dir0; U2[i] = U2[i] - gd * dir1; U3[i] = U3[i] - gd * dir2;
+        U1[j] = U1[j] + gd * dir0; U2[j] = U2[j] + gd * dir1; U3[j] = U3[j] + gd * dir2;
+      }
+    }
+  }
+  CELL(s, I, MCPM_CF_OMEGA_MAX) = omega > om_max ? omega : om_max;
+}
+
+void orc_esmc(orc_state* s, const double* x1, const double* x2, double* U1,
+              double* U2, double* U3) {
+  int Rx = (int)ceil(s->cfg.sigma / s->dx), Ry = (int)ceil(s->cfg.sigma / s->dy);
+  if (Rx < 1) Rx = 1;
+  if (Ry < 1) Ry = 1;
+  int Sx = (s->N0 > 1) ? 2 * Rx + 1 : 1, Sy = 2 * Ry + 1;
+  for (int cy = 0; cy < Sy; ++cy)
+    for (int cx = 0; cx < Sx; ++cx)
+      for (int k = cy; k < s->N1; k += Sy)
+        for (int j = cx; j < s->N0; j += Sx) esmc_cell(s, k * s->N0 + j, x1, x2, U1, U2, U3);
+}
+
+/* ESMC majorant initialisation, src/main.cpp:250-269 */
+void orc_init_omega_max(orc_state* s) {
+  const mcpm_config* g = &s->cfg;
+  double pi = acos(-1);
+  for (int num = 0; num < s->C; ++num) {
+    double thermal = sqrt(g->kb * CELL(s, num, MCPM_CF_T) / g->m);
+    double crm = 10.0 * (thermal);
+    double om = 4.0 * pi * g->sigma * g->sigma * crm * CELL(s, num, MCPM_CF_N) * g->dt;
+    if (g->model == MCPM_MODEL_ESMC) om = om * Ycoll(s, g->n);
+    CELL(s, num, MCPM_CF_OMEGA_MAX) = om;
+  }
+}
+
+/* ------------------------------------------------------------ Vlasov 1-D -- */
+/* density lookup with the reference's edge clamping */
+static double n_lookup(const orc_state* s, int num) {
+  if (num > -1 && num < s->N1) return CELL(s, num, MCPM_CF_N);
+  if (num < 0) return CELL(s, 0, MCPM_CF_N);
+  return CELL(s, s->N1 - 1, MCPM_CF_N);
+}
+
+/* vlasov_taking_the_integral, src/Main_Functions.cpp:3582-3942: face
+   potentials V_f = sum_{r,phi} (sigma/r)^6 r^2 2pi n(y_f + r cos phi) sin phi
+   on the GL(50) x GL(50) grid, r in [eqdist, 3 eqdist], phi in [0, pi]. */
+void orc_vlasov_face_potential(orc_state* s, double* V) {
+  const mcpm_config* g = &s->cfg;
+  double xi[50], wi[50], rr[50], dr[50], ph[50], dph[50];
+  orc_gl_table(50, xi, wi);
+  double pi = acos(-1);
+  double b = 3.0 * g->eqdist, a = 1.0 * g->eqdist, c = 0.0, d = pi;
+  for (int i = 0; i < 50; ++i) { rr[i] = (b - a) / 2.0 * xi[i] + (a + b) / 2.0; dr[i] = wi[i] * (b - a) / 2.0; }
+  for (int i = 0; i < 50; ++i) { ph[i] = (d - c) / 2.0 * xi[i] + (c + d) / 2.0; dph[i] = wi[i] * (d - c) / 2.0; }
+  double int_theta = 2.0 * pi;
+  int nf = s->N1 + 1;
+  for (int fc = 0; fc < nf; ++fc) {
+    V[fc] = 0.0;
+    for (int i = 0; i < 50; ++i) {
+      double radial_part = -(-pow(g->sigma / rr[i], 6.0)) * rr[i] * rr[i] * int_theta * dr[i];
+      for (int ii = 0; ii < 50; ++ii) {
+        double y = fc * s->dy + rr[i] * cos(ph[ii]);
+        int num = (int)floor(y / s->dy);
+        double n = n_lookup(s, num);
+        V[fc] += -radial_part * n * sin(ph[ii]) * dph[ii];
+      }
+    }
+  }
+}
+
+/* Thompson_3d, src/Math_Func.cpp:28-52 (b lower, c upper diagonal) */
+static void thomas(double* a, const double* b, const double* c, double* x,
+                   double* RHS, int n) {
+  for (int i = 1; i < n; ++i) {
+    double Factor = (1.0 / a[i - 1]) * b[i - 1];
+    a[i] = a[i] - c[i - 1] * Factor;
+    RHS[i] = RHS[i] - Factor * RHS[i - 1];
+  }
+  for (int i = n - 1; i >= 0; --i) {
+    double r = RHS[i];
+    if (i != n - 1) r = r - c[i] * x[i + 1];
+    x[i] = r / a[i];
+  }
+}
+
+/* poisson_solver, src/Main_Functions.cpp:3285-3581: screened-Poisson face
+   potential with Green's-function Dirichlet values at both walls, minus the
+   analytic r < sigma part. x receives the corrected face potential. */
+void orc_poisson_faces(orc_state* s, double* x) {
+  const mcpm_config* g = &s->cfg;
+  int nf = s->N1 + 1;
+  double* a = (double*)malloc(sizeof(double) * nf);
+  double* b = (double*)malloc(sizeof(double) * nf);
+  double* c = (double*)malloc(sizeof(double) * nf);
+  double* nj = (double*)malloc(sizeof(double) * nf);
+  double* rhs = (double*)malloc(sizeof(double) * nf);
+  double xi[50], wi[50], rr[50], dr[50], ph[50], dph[50];
+  orc_gl_table(50, xi, wi);
+  double pi = acos(-1);
+  for (int i = 0; i < nf; ++i) {
+    if (i == 0) nj[i] = CELL(s, 0, MCPM_CF_N);
+    else if (i == s->N1) nj[i] = CELL(s, s->N1 - 1, MCPM_CF_N);
+    else nj[i] = (CELL(s, i, MCPM_CF_N) + CELL(s, i - 1, MCPM_CF_N)) / 2.0;
+  }
+  for (int i = 0; i < nf; ++i) a[i] = (2.0 + pow(s->dy * g->bst, 2.0));
+  for (int i = 0; i < nf - 1; ++i) { b[i] = -1.0; c[i] = -1.0; }
+  for (int i = 0; i < nf; ++i) rhs[i] = nj[i] * pow(s->dy, 2.0);
+  double bb = 3.0 * g->eqdist, aa = 0.0 * g->eqdist, cc = 0.0, dd = pi;
+  for (int i = 0; i < 50; ++i) { rr[i] = (bb - aa) / 2.0 * xi[i] + (aa + bb) / 2.0; dr[i] = wi[i] * (bb - aa) / 2.0; }
+  for (int i = 0; i < 50; ++i) { ph[i] = (dd - cc) / 2.0 * xi[i] + (cc + dd) / 2.0; dph[i] = wi[i] * (dd - cc) / 2.0; }
+  double V_lw = 0.0, V_uw = 0.0, n = 0.0;
+  for (int fc = 0; fc < nf; fc = fc + nf - 1) {
+    for (int i = 0; i < 50; ++i) {
+      double radial_part = exp(-g->bst * rr[i]) / (2.0) * rr[i] * dr[i];
+      for (int ii = 0; ii < 50; ++ii) {
+        double y = fc * s->dy + rr[i] * cos(ph[ii]);
+        int num = (int)floor(y / s->dy);
+        n = n_lookup(s, num);
+        if (fc == 0) V_lw += radial_part * n * sin(ph[ii]) * dph[ii];
+        if (fc == nf - 1) V_uw += radial_part * n * sin(ph[ii]) * dph[ii];
+      }
+    }
+  }
+  c[0] = 0.0; a[0] = 1.0; rhs[0] = V_lw;
+  a[nf - 1] = 1.0; rhs[nf - 1] = V_uw; b[nf - 2] = 0.0;
+  thomas(a, b, c, x, rhs, nf);
+  double dummy = 1.0 - (g->sigma * g->bst + 1.0) * exp(-g->bst * g->sigma);
+  dummy = dummy / g->bst / g->bst;
+  for (int i = 0; i < nf; ++i) x[i] = x[i] - nj[i] * dummy;
+  free(a); free(b); free(c); free(nj); free(rhs);
+}
+
+/* long-range dispatch of velocity_update, src/Main_Functions.cpp:1618-1663,
+   for the 1-D paths: F2 per cell from the face potential, U2 += F2 dt. */
+void orc_long_range(orc_state* s, double* U2) {
+  const mcpm_config* g = &s->cfg;
+  if (g->long_range != MCPM_LR_DIRECT && g->long_range != MCPM_LR_SCREENED_POISSON) return;
+  int nf = s->N1 + 1;
+  double* V = (double*)malloc(sizeof(double) * nf);
+  double coef;
+  if (g->long_range == MCPM_LR_DIRECT) { orc_vlasov_face_potential(s, V); coef = g->phi; }
+  else { orc_poisson_faces(s, V); coef = g->ast; }
+  for (int num = 0; num < s->N1; ++num) {
+    int fc = num + 1;
+    double F2 = -(V[fc] - V[fc - 1]) / s->dy;
+    F2 = F2 / g->m * coef;
+    for (int j = 0; j < s->N0; ++j) CELL(s, num * s->N0 + j, MCPM_CF_F2) = F2;
+  }
+  for (int64_t id = 0; id < s->N; ++id) {
+    int num = s->index[id];
+    U2[id] = U2[id] + CELL(s, num, MCPM_CF_F2) * g->dt;
+  }
+  free(V);
+}
+
+/* ------------------------------------------------- DFP_extra_streaming -- */
+/* src/Fokker_Planck.cpp:904-946, including its use of U_space[1] in the x1
+   heat-flux term (:936). */
+void orc_dfp_extra_streaming(orc_state* s, const double* U1, const double* U2,
+                             const double* U3, double* x1, double* x2) {
+  const mcpm_config* g = &s->cfg;
+  double dummy = (g->model == MCPM_MODEL_FP_DENSE) ? 1.0 : 0.0;
+  double dt = g->dt;
+  for (int64_t ii = 0; ii < s->N; ++ii) {
+    int num = s->index[ii];
+    const double* Us = &CELL(s, num, MCPM_CF_U_SPACE);
+    const double* al = &CELL(s, num, MCPM_CF_ALPHA);
+    const double* be = &CELL(s, num, MCPM_CF_BETA);
+    const double* M3 = &CELL(s, num, MCPM_CF_M3);
+    const double* ph = &CELL(s, num, MCPM_CF_PHI);
+    double gst = CELL(s, num, MCPM_CF_GAMMA_ST), T = CELL(s, num, MCPM_CF_T);
+    double energy = (U1[ii] - Us[0]) * (U1[ii] - Us[0]) + (U2[ii] - Us[1]) * (U2[ii] - Us[1]) +
+                    (U3[ii] - Us[2]) * (U3[ii] - Us[2]);
+    if (g->direction[0] == 1) {
+      x1[ii] = x1[ii] + dummy * dt * ((U1[ii] - Us[0]) * al[0] + (U2[ii] - Us[1]) * al[1] + (U3[ii] - Us[2]) * al[2] +
+                                      be[0] * (energy - 3.0 * g->kb * T / g->m)) +
+               dummy * gst * ((U1[ii] - Us[1]) * energy - M3[0] - M3[3] - M3[5]) * dt;
+      x1[ii] = x1[ii] - dummy * dt * ph[0];
+    }
+    if (g->direction[1] == 1) {
+      x2[ii] = x2[ii] + dummy * dt * ((U1[ii] - Us[0]) * al[3] + (U2[ii] - Us[1]) * al[4] + (U3[ii] - Us[2]) * al[5] +
+                                      be[1] * (energy - 3.0 * g->kb * T / g->m)) +
+               dummy * gst * ((U2[ii] - Us[1]) * energy - M3[1] - M3[6] - M3[8]) * dt;
+      x2[ii] = x2[ii] - dummy * dt * ph[1];
+    }
+  }
+}
+
+/* ----------------------------------------------------- free flight, BCs -- */
+/* Position_FP_ideal_gas, src/Fokker_Planck.cpp:948-969 */
+void orc_stream(orc_state* s, double* x1, double* x2, const double* U1,
+                const double* U2, const double* U3) {
+  (void)U3;
+  if (s->cfg.direction[0] == 1)
+    for (int64_t i = 0; i < s->N; ++i) x1[i] = x1[i] + s->cfg.dt * U1[i];
+  if (s->cfg.direction[1] == 1)
+    for (int64_t i = 0; i < s->N; ++i) x2[i] = x2[i] + s->cfg.dt * U2[i];
+}
+
+/* store_old_positions, src/Main_Functions.cpp:5736-5760 */
+void orc_store_old_positions(orc_state* s, const double* x1, const double* x2,
+                             double* x1_old, double* x2_old) {
+  if (s->cfg.direction[0] == 1) memcpy(x1_old, x1, sizeof(double) * (size_t)s->N);
+  if (s->cfg.direction[1] == 1) memcpy(x2_old, x2, sizeof(double) * (size_t)s->N);
+}
+
+/* BC_specular_reflection, src/Main_Functions.cpp:6399-6525 (the wall
+   momentum tally gas.M is a diagnostic and is not kept) */
+static void bc_specular(orc_state* s, double* x1, double* x2, double* U1, double* U2) {
+  const mcpm_config* g = &s->cfg;
+  double Tol1 = 1e-16, Tol2 = -1e-16;
+  for (int64_t i = 0; i < s->N; ++i) {
+    int done = 0, it = 0;
+    while (done == 0) {
+      if (g->direction[0] == 1) {
+        if (x1[i] - g->length[0] > Tol2) { U1[i] = -U1[i]; x1[i] = x1[i] - 2.0 * fabs(x1[i] - g->length[0]); }
+        else if (x1[i] < Tol1) { U1[i] = -U1[i]; x1[i] = x1[i] + 2.0 * fabs(x1[i]); }
+      }
+      if (g->direction[1] == 1) {
+        if (x2[i] - g->length[1] > Tol2) { U2[i] = -U2[i]; x2[i] = x2[i] - 2.0 * fabs(x2[i] - g->length[1]); }
+        else if (x2[i] < Tol1) { U2[i] = -U2[i]; x2[i] = x2[i] + 2.0 * fabs(x2[i]); }
+      }
+      done = 1;
+      if (g->direction[0] == 1 && (x1[i] - g->length[0] > 0.0 || x1[i] < 0.0)) done = 0;
+      if (g->direction[1] == 1 && (x2[i] - g->length[1] > 0.0 || x2[i] < 0.0)) done = 0;
+      if (++it > 64) { s->status |= MCPM_ERR_BC_LOOP; break; }
+    }
+  }
+}
+
+/* periodic wrap in the active directions */
+static void bc_periodic(orc_state* s, double* x1, double* x2) {
+  const mcpm_config* g = &s->cfg;
+  for (int64_t i = 0; i < s->N; ++i) {
+    if (g->direction[0] == 1) x1[i] = x1[i] - g->length[0] * floor(x1[i] / g->length[0]);
+    if (g->direction[1] == 1) x2[i] = x2[i] - g->length[1] * floor(x2[i] / g->length[1]);
+  }
+}
+
+/* intersect_3D_x / intersect_3D_y, src/Main_Functions.cpp:2757-2806, with
+   z_new == z_old (no streaming in z) */
+static void intersect_x(double x, double* y, double xo, double yo, double xn, double yn) {
+  double n0 = xn - xo, n1 = yn - yo, n2 = 0.0;
+  double size = 0.0;
+  size += n0 * n0; size += n1 * n1; size += n2 * n2;
+  size = sqrt(size);
+  n0 = n0 / size; n1 = n1 / size;
+  if (fabs(n0) > 1e-16) *y = (n1 / n0) * (x - xo) + yo;
+  else *y = yn;
+}
+static void intersect_y(double* x, double y, double xo, double yo, double xn, double yn) {
+  double n0 = xn - xo, n1 = yn - yo, n2 = 0.0;
+  double size = 0.0;
+  size += n0 * n0; size += n1 * n1; size += n2 * n2;
+  size = sqrt(size);
+  n0 = n0 / size; n1 = n1 / size;
+  if (fabs(n1) > 1e-16) *x = (n0 / n1) * (y - yo) + xo;
+  else *x = xn;
+}
+
+/* one diffuse re-emission: tangential Maxwellian, normal Rayleigh */
+static void wall_draw(const orc_state* s, int64_t i, int call_no, int it, double z[2], double* ray) {
+  uint32_t r[4];
+  philox(s->cfg.seed, (uint32_t)i, (uint32_t)s->step, RNG_STREAM_BC,
+         (uint32_t)((call_no << 8) | (it & 0xff)), r);
+  *ray = sqrt(-log(u01(r[0])));
+  double a = sqrt(-2.0 * log(u01(r[1])));
+  z[0] = a * cos(TWO_PI * u01(r[2]));
+  z[1] = a * sin(TWO_PI * u01(r[2]));
+}
+
+/* BC_thermal_wall_3D, src/Main_Functions.cpp:4917-5250, in 2-D (direction[2]
+   = 0): diffuse walls at x = 0 (T_wall_3), x = Len0 (T_wall_4),
+   y = sigma (T_wall_1), y = Len1 - sigma (T_wall_2), with re-flight for the
+   rest of the step from the wall crossing point. */
+static void bc_thermal_wall(orc_state* s, int call_no, double* x1, double* x2,
+                            double* x1o, double* x2o, double* U1, double* U2, double* U3) {
+  const mcpm_config* g = &s->cfg;
+  const double eps = 1e-15;
+  const double L0 = g->length[0], L1 = g->length[1];
+  for (int64_t i = 0; i < s->N; ++i) {
+    double dt = g->dt;
+    int done = 0, it = 0;
+    double Ue0 = fabs(x1[i] - x1o[i]) / g->dt;
+    double Ue1 = fabs(x2[i] - x2o[i]) / g->dt;
+    while (done == 0) {
+      double dt_remain = 0.0, xw, yw, tU0, z[2], ray;
+      if (it > 20) { s->status |= MCPM_ERR_BC_LOOP; break; }
+      if (dt < 1e-15) {
+        if (x1[i] < eps) x1[i] = eps;
+        else if (x1[i] > L0 - eps) x1[i] = L0 - eps;
+        if (x2[i] < eps) x2[i] = eps;
+        else if (x2[i] > L1 - eps) x2[i] = L1 - eps;
+      }
+      if (x1[i] - L0 > 0.0) { /* right wall */
+        xw = L0 - eps;
+        if (fabs(x1o[i] - x1[i]) > 1e-15) intersect_x(xw, &yw, x1o[i], x2o[i], x1[i], x2[i]);
+        else yw = 0.5 * (x2o[i] + x2[i]);
+        tU0 = (fabs(dt - g->dt) < 1e-15) ? Ue0 : U1[i];
+        wall_draw(s, i, call_no, it, z, &ray);
+        U1[i] = -sqrt(2.0 * g->kb * g->T_wall[3] / (g->m)) * ray;
+        U2[i] = sqrt(g->kb * g->T_wall[3] / (g->m)) * z[0] + (1.0 * g->U_wall[3]);
+        U3[i] = sqrt(g->kb * g->T_wall[3] / (g->m)) * z[1];
+        if (dt > 1e-15) {
+          dt_remain = fabs((x1[i] - xw) / tU0);
+          dt_remain = dt < dt_remain ? dt : dt_remain;
+          x1[i] = xw + dt_remain * U1[i];
+          x2[i] = yw + dt_remain * U2[i];
+          dt = dt - dt_remain;
+          x1o[i] = xw; x2o[i] = yw;
+        } else x1[i] = xw;
+      } else if (x1[i] < 0.0) { /* left wall */
+        xw = eps;
+        if (fabs(x1o[i] - x1[i]) > 1e-15) intersect_x(xw, &yw, x1o[i], x2o[i], x1[i], x2[i]);
+        else yw = 0.5 * (x2o[i] + x2[i]);
+        tU0 = (fabs(dt - g->dt) < 1e-15) ? Ue0 : U1[i];
+        wall_draw(s, i, call_no, it, z, &ray);
+        U1[i] = sqrt(2.0 * g->kb * g->T_wall[2] / (g->m)) * ray;
+        U2[i] = sqrt(g->kb * g->T_wall[2] / g->m) * z[0] + (1.0 * g->U_wall[2]);
+        U3[i] = sqrt(g->kb * g->T_wall[2] / g->m) * z[1];
+        if (dt > 1e-15) {
+          dt_remain = fabs((x1[i] - xw) / tU0);
+          dt_remain = dt < dt_remain ? dt : dt_remain;
+          x1[i] = xw + dt_remain * U1[i];
+          x2[i] = yw + dt_remain * U2[i];
+          dt = dt - dt_remain;
+          x1o[i] = xw; x2o[i] = yw;
+        } else x1[i] = xw;
+      } else if (x2[i] > L1 - g->sigma - eps) { /* upper wall */
+        yw = L1 - g->sigma - eps;
+        intersect_y(&xw, yw, x1o[i], x2o[i], x1[i], x2[i]);
+        tU0 = (fabs(dt - g->dt) < 1e-15) ? Ue1 : U2[i];
+        wall_draw(s, i, call_no, it, z, &ray);
+        U1[i] = sqrt(g->kb * g->T_wall[1] / (g->m)) * z[0] + (1.0 * g->U_wall[1]);
+        U2[i] = -sqrt(2.0 * g->kb * g->T_wall[1] / (g->m)) * ray;
+        U3[i] = sqrt(g->kb * g->T_wall[1] / (g->m)) * z[1];
+        if (dt > 1e-15) {
+          dt_remain = fabs((x2[i] - yw) / tU0);
+          dt_remain = dt < dt_remain ? dt : dt_remain;
+          x1[i] = xw + dt_remain * U1[i];
+          x2[i] = yw + dt_remain * U2[i];
+          dt = dt - dt_remain;
+          x1o[i] = xw; x2o[i] = yw;
+        } else x2[i] = yw;
+      } else if (x2[i] < g->sigma + eps) { /* lower wall */
+        yw = g->sigma + eps;
+        intersect_y(&xw, yw, x1o[i], x2o[i], x1[i], x2[i]);
+        tU0 = (fabs(dt - g->dt) < 1e-15) ? Ue1 : U2[i];
+        wall_draw(s, i, call_no, it, z, &ray);
+        U1[i] = sqrt(g->kb * g->T_wall[0] / (g->m)) * z[0] + (1.0 * g->U_wall[0]);
+        U2[i] = sqrt(2.0 * g->kb * g->T_wall[0] / (g->m)) * ray;
+        U3[i] = sqrt(g->kb * g->T_wall[0] / g->m) * z[1];
+        if (dt > 1e-15) {
+          dt_remain = fabs((x2[i] - yw) / tU0);
+          dt_remain = dt < dt_remain ? dt : dt_remain;
+          x1[i] = xw + dt_remain * U1[i];
+          x2[i] = yw + dt_remain * U2[i];
+          dt = dt - dt_remain;
+          x1o[i] = xw; x2o[i] = yw;
+        } else x2[i] = yw;
+      }
+      if (x1[i] - L0 < 0.0 && x1[i] > 0.0 && x2[i] - L1 < 0.0 && x2[i] > 0.0) done = 1;
+      it++;
+    }
+  }
+}
+
+/* BC_wall, src/Main_Functions.cpp:4816-4914: diffuse lower wall at y = 0
+   (T_wall_1), specular upper wall, 1-D in y. */
+static void bc_wall(orc_state* s, int call_no, double* x2, double* x2o,
+                    double* U1, double* U2, double* U3) {
+  const mcpm_config* g = &s->cfg;
+  const double eps = 1e-15;
+  const double L1 = g->length[1];
+  for (int64_t i = 0; i < s->N; ++i) {
+    double dt = g->dt;
+    int done = 0, it = 0;
+    double Ue1 = fabs(x2[i] - x2o[i]) / g->dt;
+    while (done == 0) {
+      double dt_remain = 0.0, tU0, z[2], ray;
+      if (it > 20) { s->status |= MCPM_ERR_BC_LOOP; break; }
+      if (dt < 1e-15) {
+        if (x2[i] < eps) x2[i] = eps;
+        else if (x2[i] > L1 - eps) x2[i] = L1 - eps;
+      } else if (x2[i] > L1) {
+        U2[i] = -U2[i];
+        x2[i] = x2[i] - 2.0 * fabs(x2[i] - L1);
+      } else if (x2[i] < 0.0) {
+        double yw = eps;
+        tU0 = (fabs(dt - g->dt) < 1e-15) ? Ue1 : U2[i];
+        wall_draw(s, i, call_no, it, z, &ray);
+        U1[i] = sqrt(g->kb * g->T_wall[0] / (g->m)) * z[0] + (1.0 * g->U_wall[0]);
+        U2[i] = sqrt(2.0 * g->kb * g->T_wall[0] / (g->m)) * ray;
+        U3[i] = sqrt(g->kb * g->T_wall[0] / g->m) * z[1];
+        if (dt > 1e-15) {
+          dt_remain = fabs((x2[i] - yw) / tU0);
+          dt_remain = dt < dt_remain ? dt : dt_remain;
+          x2[i] = yw + dt_remain * U2[i];
+          dt = dt - dt_remain;
+          x2o[i] = yw;
+        } else x2[i] = yw;
+      }
+      if (x2[i] - L1 < 0.0 && x2[i] > 0.0) done = 1;
+      it++;
+    }
+  }
+}
+
+/* apply_BC, src/Main_Functions.cpp:1451-1492 */
+void orc_apply_bc(orc_state* s, int call_no, double* x1, double* x2,
+                  double* x1_old, double* x2_old, double* U1, double* U2, double* U3) {
+  switch (s->cfg.problem) {
+    case MCPM_PROBLEM_CLOSED_BOX: bc_specular(s, x1, x2, U1, U2); break;
+    case MCPM_PROBLEM_COUETTE: bc_thermal_wall(s, call_no, x1, x2, x1_old, x2_old, U1, U2, U3); break;
+    case MCPM_PROBLEM_WALL: bc_wall(s, call_no, x2, x2_old, U1, U2, U3); break;
+    case MCPM_PROBLEM_PERIODIC: bc_periodic(s, x1, x2); break;
+    default: break;
+  }
+}
+
+/* --------------------------------------------------------------- step -- */
+/* one iteration of src/main.cpp:389-669 for the in-scope models */
+void orc_step(orc_state* s, double* x1, double* x2, double* x1_old,
+              double* x2_old, double* U1, double* U2, double* U3, int32_t* index) {
+  int m = s->cfg.model;
+  int64_t N = s->N;
+  orc_cell_update(s, x1, x2, U1, U2, U3, index);
+  if (m == MCPM_MODEL_FP_DENSE || m == MCPM_MODEL_FP_IDEAL_GAS) {
+    orc_random_generator(s, s->xi, s->xi + N, s->xi + 2 * N);
+    orc_velocity_fp(s, U1, U2, U3, s->xi, s->xi + N, s->xi + 2 * N);
+  } else if (m == MCPM_MODEL_ESMC) {
+    orc_esmc(s, x1, x2, U1, U2, U3);
+  }
+  orc_long_range(s, U2);
+  if (m == MCPM_MODEL_FP_DENSE) orc_dfp_extra_streaming(s, U1, U2, U3, x1, x2);
+  orc_apply_bc(s, 0, x1, x2, x1_old, x2_old, U1, U2, U3);
+  orc_store_old_positions(s, x1, x2, x1_old, x2_old);
+  orc_stream(s, x1, x2, U1, U2, U3);
+  orc_apply_bc(s, 1, x1, x2, x1_old, x2_old, U1, U2, U3);
+  orc_apply_bc(s, 2, x1, x2, x1_old, x2_old, U1, U2, U3);
+  s->step++;
+}
+
+/* take the per-cell particle order from the caller (e.g. the GPU's slot
+   layout) instead of ascending particle ids; counts must match the binning */
+void orc_set_layout(orc_state* s, const int32_t* off, const int32_t* list) {
+  for (int c = 0; c <= s->C; ++c) s->off[c] = off[c];
+  for (int c = 0; c < s->C; ++c) s->cnt[c] = off[c + 1] - off[c];
+  for (int64_t i = 0; i < s->N; ++i) s->list[i] = list[i];
+}

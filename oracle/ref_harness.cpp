@@ -1,0 +1,265 @@
+// ref_harness.cpp -- drives the reference's own routines on caller data.
+//
+// TEST INFRASTRUCTURE ONLY.  Compiled by oracle/build.py together with the
+// reference translation units (src/Main_Functions.cpp, src/Fokker_Planck.cpp,
+// src/Math_Func.cpp, src/collisions.cpp, src/FEM.cpp, src/myIO.cpp, ...)
+// straight from the reference tree into oracle/_ref/libref.so.  The reference
+// is used unmodified; this file only
+//   * replaces the translation unit src/random_generator.cpp with a
+//     generateGaussianNoise that returns injected draws in call order, so that
+//     random_generator (src/Fokker_Planck.cpp:84-90) is reproducible;
+//   * supplies solver_pardiso (src/solver_pardiso.cpp needs MKL) as a dense LU
+//     with partial pivoting on the CSR matrix compute_SP_2D builds;
+//   * stubs dgesv, whose only caller (src/solver.cpp) is dead code;
+//   * fills GAS/BOX/CELLS from an mcpm_config and exposes extern "C" calls.
+#include "../include/mcpm.h"  // before the reference header: it #defines short names
+
+#include "cpp_headers.h"
+
+#include <fcntl.h>
+#include <unistd.h>
+
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+// ---------------------------------------------------------------- injected
+static std::vector<double> g_inj;
+static size_t g_inj_pos = 0;
+
+double generateGaussianNoise(double mu, double sigma) {
+  double z = g_inj.empty() ? 0.0 : g_inj[g_inj_pos % g_inj.size()];
+  g_inj_pos++;
+  return z * sigma + mu;
+}
+
+int solver_pardiso(int* ia, int* ja, double* a, int n, double* b, double* x) {
+  // CSR with 1-based indices (src/FEM.cpp:120-157) -> dense, LU with partial pivoting
+  std::vector<double> A((size_t)n * n, 0.0), r(b, b + n);
+  for (int i = 0; i < n; ++i)
+    for (int p = ia[i] - 1; p < ia[i + 1] - 1; ++p) A[(size_t)i * n + (ja[p] - 1)] = a[p];
+  for (int k = 0; k < n; ++k) {
+    int piv = k;
+    for (int i = k + 1; i < n; ++i)
+      if (fabs(A[(size_t)i * n + k]) > fabs(A[(size_t)piv * n + k])) piv = i;
+    if (piv != k) {
+      for (int j = 0; j < n; ++j) std::swap(A[(size_t)k * n + j], A[(size_t)piv * n + j]);
+      std::swap(r[k], r[piv]);
+    }
+    for (int i = k + 1; i < n; ++i) {
+      double f = A[(size_t)i * n + k] / A[(size_t)k * n + k];
+      if (f == 0.0) continue;
+      for (int j = k; j < n; ++j) A[(size_t)i * n + j] -= f * A[(size_t)k * n + j];
+      r[i] -= f * r[k];
+    }
+  }
+  for (int i = n - 1; i >= 0; --i) {
+    double s = r[i];
+    for (int j = i + 1; j < n; ++j) s -= A[(size_t)i * n + j] * x[j];
+    x[i] = s / A[(size_t)i * n + i];
+  }
+  return 0;
+}
+
+extern "C" void dgesv(const int*, const int*, double*, const int*, int*, double*, const int*, int* info) {
+  if (info) *info = -1;
+}
+
+// ------------------------------------------------------------- stdout gag
+struct Quiet {
+  int saved;
+  Quiet() {
+    fflush(stdout);
+    saved = dup(1);
+    int devnull = open("/dev/null", O_WRONLY);
+    dup2(devnull, 1);
+    close(devnull);
+  }
+  ~Quiet() {
+    fflush(stdout);
+    dup2(saved, 1);
+    close(saved);
+  }
+};
+
+struct Ref {
+  GAS gas;
+  BOX box;
+  CELLS* cells;
+  int C;
+  long N;
+  std::vector<double> x3, x3_old, Mp1, Mp2, Mp3, xi1, xi2, xi3, T, rho;
+  std::vector<int> color, flag;
+};
+
+static const char* model_name(int m) {
+  switch (m) {
+    case MCPM_MODEL_FP_DENSE: return "FP_dense";
+    case MCPM_MODEL_FP_IDEAL_GAS: return "FP_ideal_gas";
+    case MCPM_MODEL_ESMC: return "ESMC";
+    default: return "none";
+  }
+}
+
+extern "C" {
+
+void* ref_create(const mcpm_config* c, long N) {
+  Quiet q;
+  Ref* r = new Ref();
+  GAS& g = r->gas;
+  BOX& b = r->box;
+  g.sigma = c->sigma; g.m = c->m; g.kb = c->kb; g.n = c->n; g.Fn = c->Fn;
+  g.T0 = c->T0; g.mu = c->mu; g.visp = c->visp; g.b = c->b; g.delta_t = c->dt;
+  g.phi = c->phi; g.eqdist = c->eqdist; g.ast = c->ast; g.bst = c->bst;
+  g.long_range = c->long_range; g.model = model_name(c->model); g.N = N;
+  g.n_ratio = 1; g.times = 1.0;
+  for (int i = 0; i < 3; ++i) {
+    b.N[i] = c->n_cells[i]; b.Len[i] = c->length[i];
+    b.delta_dim[i] = c->length[i] / c->n_cells[i]; b.direction[i] = c->direction[i];
+  }
+  b.problem = (c->problem == MCPM_PROBLEM_PERIODIC) ? relaxation : c->problem;
+  b.T_wall_1 = c->T_wall[0]; b.T_wall_2 = c->T_wall[1]; b.T_wall_3 = c->T_wall[2]; b.T_wall_4 = c->T_wall[3];
+  b.U_wall_1 = c->U_wall[0]; b.U_wall_2 = c->U_wall[1]; b.U_wall_3 = c->U_wall[2]; b.U_wall_4 = c->U_wall[3];
+  b.every = 1 << 30; b.after = 1 << 30; b.init_step = 0; b.step = 0;
+  b.Ny = 1; b.s = 2.0; b.Ly = 1.0;
+  r->C = b.N[0] * b.N[1] * b.N[2];
+  r->N = N;
+  r->cells = (CELLS*)calloc(r->C, sizeof(CELLS));
+  make_cells(&b, r->cells, &g);
+  for (int k = 0; k < r->C; ++k) {
+    r->cells[k].indices_inside = (int*)malloc(sizeof(int));
+    r->cells[k].indices_inside[0] = -1;
+  }
+  r->x3.assign(N, 0.5 * c->length[2]); r->x3_old = r->x3;
+  r->Mp1.assign(N, 0.0); r->Mp2.assign(N, 0.0); r->Mp3.assign(N, 0.0);
+  r->xi1.assign(N, 0.0); r->xi2.assign(N, 0.0); r->xi3.assign(N, 0.0);
+  r->T.assign(N, 0.0); r->rho.assign(N, 0.0);
+  r->color.assign(N, 0); r->flag.assign(N, 0);
+  return r;
+}
+
+void ref_destroy(void* h) {
+  Ref* r = (Ref*)h;
+  for (int k = 0; k < r->C; ++k) free(r->cells[k].indices_inside);
+  free(r->cells);
+  delete r;
+}
+
+void ref_set_step(void* h, int step) { ((Ref*)h)->box.step = step; }
+
+void ref_inject_normals(const double* a, const double* b, const double* c, long N) {
+  g_inj.assign(a, a + N);
+  g_inj.insert(g_inj.end(), b, b + N);
+  g_inj.insert(g_inj.end(), c, c + N);
+  g_inj_pos = 0;
+}
+
+void ref_cell_update(void* h, double* x1, double* x2, double* U1, double* U2, double* U3, int* index) {
+  Quiet q;
+  Ref* r = (Ref*)h;
+  double* T = r->T.data();
+  cell_update(x1, x2, U1, U2, U3, &r->gas, r->cells, &r->box, index, &T, r->rho.data(), r->color.data());
+}
+
+void ref_random_generator(void* h, int* index, double* xi1f, double* xi2f, double* xi3f) {
+  Quiet q;
+  Ref* r = (Ref*)h;
+  g_inj_pos = 0;
+  random_generator(r->xi1.data(), r->xi2.data(), r->xi3.data(), xi1f, xi2f, xi3f, r->cells, &r->box, &r->gas, index);
+}
+
+void ref_velocity_fp(void* h, double* U1, double* U2, double* U3, int* index, double* xi1f, double* xi2f,
+                     double* xi3f) {
+  Quiet q;
+  Ref* r = (Ref*)h;
+  Velocity_FP_parallel(U1, U2, U3, &r->gas, r->cells, &r->box, index, xi1f, xi2f, xi3f, r->Mp1.data(),
+                       r->Mp2.data(), r->Mp3.data());
+}
+
+void ref_long_range(void* h, double* x1, double* x2, double* U2, int* index) {
+  Quiet q;
+  Ref* r = (Ref*)h;
+  if (r->gas.long_range == 1) vlasov_taking_the_integral(U2, &r->gas, &r->box, r->cells, index, x1, x2, r->x3.data());
+  else if (r->gas.long_range == 3) poisson_solver(U2, x1, x2, r->x3.data(), &r->gas, &r->box, r->cells, index);
+}
+
+void ref_dfp_extra_streaming(void* h, double* U1, double* U2, double* U3, double* x1, double* x2, int* index) {
+  Quiet q;
+  Ref* r = (Ref*)h;
+  DFP_extra_streaming(U1, U2, U3, x1, x2, &r->gas, &r->box, r->cells, index, r->gas.delta_t);
+}
+
+void ref_apply_bc(void* h, double* U1, double* U2, double* U3, double* x1, double* x2, double* x1_old,
+                  double* x2_old, int* index) {
+  Quiet q;
+  Ref* r = (Ref*)h;
+  if (r->box.problem == relaxation) return;  // the periodic wrap is not a reference routine
+  apply_BC(U1, U2, U3, x1, x2, r->x3.data(), x1_old, x2_old, r->x3_old.data(), &r->gas, &r->box, r->cells, index,
+           r->flag.data(), r->xi1.data(), r->xi2.data(), r->xi3.data(), r->xi1.data(), r->xi2.data(), r->xi3.data(),
+           r->Mp1.data(), r->Mp2.data(), r->Mp3.data(), r->T.data());
+}
+
+void ref_store_old_positions(void* h, double* x1, double* x2, double* x1_old, double* x2_old) {
+  Quiet q;
+  Ref* r = (Ref*)h;
+  store_old_positions(x1, x2, r->x3.data(), x1_old, x2_old, r->x3_old.data(), &r->gas, &r->box);
+}
+
+void ref_stream(void* h, double* U1, double* U2, double* U3, double* x1, double* x2, double* x1_old,
+                double* x2_old, int* index) {
+  Quiet q;
+  Ref* r = (Ref*)h;
+  stream_particles(U1, U2, U3, x1, x2, r->x3.data(), x1_old, x2_old, r->x3_old.data(), &r->gas, &r->box,
+                   r->cells, index);
+}
+
+void ref_esmc(void* h, double* U1, double* U2, double* U3, double* x1, double* x2, int* index) {
+  Quiet q;
+  Ref* r = (Ref*)h;
+  Collision_ESMC_new3(U1, U2, U3, x1, x2, &r->gas, &r->box, r->cells, index);
+}
+
+void ref_init_omega_max(void* h) {
+  // src/main.cpp:250-269
+  Ref* r = (Ref*)h;
+  double pi = acos(-1);
+  for (int num = 0; num < r->C; ++num) {
+    double thermal = sqrt(r->gas.kb * r->cells[num].T / r->gas.m);
+    r->cells[num].crm = 10.0 * ((thermal));
+    r->cells[num].omega_max = 4.0 * pi * r->gas.sigma * r->gas.sigma * r->cells[num].crm * r->cells[num].n * r->gas.delta_t;
+    if (r->gas.model == "ESMC") r->cells[num].omega_max = r->cells[num].omega_max * increase_collision_rate(r->gas.n, &r->gas);
+  }
+}
+
+// the CELLS fields of enum mcpm_cell_field, cell-major [C][MCPM_CF_COUNT]
+void ref_get_cells(void* h, double* out) {
+  Ref* r = (Ref*)h;
+  for (int c = 0; c < r->C; ++c) {
+    const CELLS& k = r->cells[c];
+    double* o = out + (size_t)c * MCPM_CF_COUNT;
+    o[MCPM_CF_NUM_INSIDE] = k.num_inside;
+    for (int i = 0; i < 3; ++i) o[MCPM_CF_U_SPACE + i] = k.U_space[i];
+    for (int i = 0; i < 6; ++i) o[MCPM_CF_PIJ + i] = k.PIJ[i];
+    for (int i = 0; i < 10; ++i) o[MCPM_CF_M3 + i] = k.M3[i];
+    for (int i = 0; i < 6; ++i) o[MCPM_CF_M4 + i] = k.M4[i];
+    for (int i = 0; i < 3; ++i) o[MCPM_CF_M5 + i] = k.M5[i];
+    for (int i = 0; i < 3; ++i) o[MCPM_CF_Q + i] = k.Q[i];
+    o[MCPM_CF_DM2] = k.DM2;
+    o[MCPM_CF_DM4] = k.DM4;
+    for (int i = 0; i < 3; ++i) o[MCPM_CF_MP + i] = k.Mp[i];
+    o[MCPM_CF_T] = k.T;
+    o[MCPM_CF_N] = k.n;
+    o[MCPM_CF_GAMMA_ST] = k.gamma_st;
+    o[MCPM_CF_LAMBDA] = k.Lambda;
+    for (int i = 0; i < 6; ++i) o[MCPM_CF_C + i] = k.c[i];
+    for (int i = 0; i < 3; ++i) o[MCPM_CF_GAMMA + i] = k.gamma[i];
+    for (int i = 0; i < 9; ++i) o[MCPM_CF_ALPHA + i] = k.alpha[i];
+    for (int i = 0; i < 3; ++i) o[MCPM_CF_BETA + i] = k.beta[i];
+    for (int i = 0; i < 3; ++i) o[MCPM_CF_PHI + i] = k.phi[i];
+    o[MCPM_CF_F2] = k.F2;
+    o[MCPM_CF_OMEGA_MAX] = k.omega_max;
+    o[MCPM_CF_DIVU] = k.divU;
+  }
+}
+
+}  // extern "C"

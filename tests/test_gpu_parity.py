@@ -1,0 +1,308 @@
+"""CUDA path (libmcpm.so through the C-ABI) against the FP64 CPU restatement
+on identical inputs and draws.
+
+Tolerances (FP64 path): cell indices and counts bit-exact; moments within
+1e-12 of the natural scale of each field (velocity^k for a k-th moment);
+velocities and positions within 1e-12 of max(1, |value|); the per-cell
+drift coefficients (outputs of ill-conditioned 9x9 / 12x12 solves) within
+1e-9 of their field's largest magnitude.  FP32 path: 2e-5 of the same scales.
+"""
+import numpy as np
+import pytest
+
+import mcpm
+import workloads as W
+from oracle import Oracle
+
+pytestmark = pytest.mark.gpu
+
+VEL_POW = dict(U_SPACE=1, MP=1, PIJ=2, DM2=2, M3=3, Q=3, M4=4, DM4=4, M5=5)
+
+
+def _pair(cfg, parts, seed=11, step=1, inject=True):
+    s = mcpm.Session(cfg)
+    s.upload(parts.get("x1"), parts["x2"], parts["U1"], parts["U2"], parts["U3"])
+    o = Oracle(cfg, parts)
+    if inject:
+        rng = np.random.default_rng(seed)
+        xi = [rng.standard_normal(o.N) for _ in range(3)]
+        s.inject_normals(*xi)
+        o.inject_normals(*xi)
+    s.set_step(step)
+    o.set_step(step)
+    return s, o
+
+
+def _close_particles(g, o, tol, keys=("x1", "x2", "U1", "U2", "U3")):
+    for k in keys:
+        a, b = g[k], getattr(o.s, k)
+        err = np.max(np.abs(a - b)) / max(1.0, np.max(np.abs(b)))
+        assert err <= tol, "%s: %.3e > %.1e" % (k, err, tol)
+
+
+def _close_cells(cg, co, tol, tol_coef):
+    """cg: [CF][C] from the GPU, co: [C][CF] from the oracle."""
+    n = mcpm.cell_field(co, "NUM_INSIDE", True)
+    assert np.array_equal(mcpm.cell_field(cg, "NUM_INSIDE"), n)
+    vs = np.sqrt(max(np.max(mcpm.cell_field(co, "DM2", True)), 1e-300))
+    for f, p in VEL_POW.items():
+        a, b = mcpm.cell_field(cg, f), mcpm.cell_field(co, f, True)
+        assert np.max(np.abs(a - b)) <= tol * vs ** p, f
+    for f in ("T", "N", "GAMMA_ST", "LAMBDA"):
+        a, b = mcpm.cell_field(cg, f), mcpm.cell_field(co, f, True)
+        m = n > 1
+        sc = np.max(np.abs(b[m])) if m.any() else 1.0
+        assert np.max(np.abs(a[m] - b[m])) <= tol * sc, f
+    for f in ("C", "GAMMA", "ALPHA", "BETA"):
+        a, b = mcpm.cell_field(cg, f), mcpm.cell_field(co, f, True)
+        sc = max(np.max(np.abs(b)), 1e-300)
+        assert np.max(np.abs(a - b)) <= tol_coef * sc, f
+
+
+# ------------------------------------------------------------- binning
+@pytest.mark.parametrize("maker", ["relax", "uneven"])
+def test_binning_bit_exact(cuda_ok, maker):
+    cfg, parts = (W.homogeneous_relaxation_1d(n_cells=37, ppc=53) if maker == "relax"
+                  else W.uneven_cells_2d(n_cells=(19, 23), hi=400, precision=mcpm.FP64))
+    s, o = _pair(cfg, parts)
+    o.cell_update()
+    s.cell_update()
+    assert np.array_equal(s.get_index(), o.s.index)
+    assert np.array_equal(mcpm.cell_field(s.get_cells(), "NUM_INSIDE"), mcpm.cell_field(o.cells(), "NUM_INSIDE", True))
+    pid, off = s.get_layout()
+    assert off[-1] == o.N and np.all(np.diff(off) >= 0)
+    assert np.array_equal(np.sort(pid), np.arange(o.N))
+
+
+def test_binning_edges_and_out_of_box(cuda_ok):
+    """Particles on the far wall bin into the last cell; a particle outside
+    the box raises MCPM_ERR_OUT_OF_BOX (the reference exits)."""
+    cfg, parts = W.homogeneous_relaxation_1d(n_cells=8, ppc=16)
+    parts = {k: v.copy() for k, v in parts.items()}
+    parts["x2"][0] = cfg.length[1]          # exactly on the wall
+    parts["x2"][1] = 0.0
+    s, o = _pair(cfg, parts)
+    s.cell_update()
+    o.cell_update()
+    idx = s.get_index()
+    assert idx[0] == 7 and idx[1] == 0
+    assert np.array_equal(idx, o.s.index)
+    s.check_status()
+    bad = {k: v.copy() for k, v in parts.items()}
+    bad["x2"][5] = cfg.length[1] + 0.5
+    s2 = mcpm.Session(cfg)
+    s2.upload(bad["x1"], bad["x2"], bad["U1"], bad["U2"], bad["U3"])
+    with pytest.raises(mcpm.MCPMError) as e:
+        s2.check_status()
+    assert e.value.code & mcpm.ERR_OUT_OF_BOX
+
+
+# -------------------------------------------------------- cell update
+@pytest.mark.parametrize("step", [0, 1])
+def test_cell_update_fp64(cuda_ok, step):
+    cfg, parts = W.homogeneous_relaxation_1d(n_cells=40, ppc=150)
+    s, o = _pair(cfg, parts, step=step)
+    o.cell_update()
+    s.cell_update()
+    _close_cells(s.get_cells(), o.cells(), 1e-12, 1e-9)
+
+
+def test_cell_update_fp64_uneven_2d(cuda_ok):
+    """log-normal occupancy: both the warp-per-cell and block-per-cell paths"""
+    cfg, parts = W.uneven_cells_2d(n_cells=(24, 20), precision=mcpm.FP64, hi=1500)
+    s, o = _pair(cfg, parts, step=3)
+    o.cell_update()
+    s.cell_update()
+    _close_cells(s.get_cells(), o.cells(), 1e-12, 1e-9)
+
+
+def test_cell_update_fp32(cuda_ok):
+    cfg, parts = W.uneven_cells_2d(n_cells=(16, 16), precision=mcpm.FP32, hi=1200)
+    s, o = _pair(cfg, parts, step=2)
+    # the FP32 path stores float velocities: give the oracle the rounded state
+    for k in ("U1", "U2", "U3"):
+        getattr(o.s, k)[:] = getattr(o.s, k).astype(np.float32).astype(np.float64)
+    o.cell_update()
+    s.cell_update()
+    cg, co = s.get_cells(), o.cells()
+    vs = np.sqrt(np.max(mcpm.cell_field(co, "DM2", True)))
+    for f, p in VEL_POW.items():
+        if f == "MP":
+            continue
+        assert np.max(np.abs(mcpm.cell_field(cg, f) - mcpm.cell_field(co, f, True))) <= 2e-5 * vs ** p, f
+
+
+# ------------------------------------------- random generator + FP update
+def test_random_generator_and_velocity_fp64(cuda_ok):
+    cfg, parts = W.homogeneous_relaxation_1d(n_cells=30, ppc=120)
+    s, o = _pair(cfg, parts)
+    o.cell_update()
+    o.random_generator()
+    o.velocity_fp()
+    s.cell_update()
+    s.random_generator()
+    xg = s.get_normals()
+    for a, b in zip(xg, o.xi):
+        assert np.max(np.abs(a - b)) <= 1e-12 * max(1.0, np.max(np.abs(b)))
+    s.velocity_update()
+    _close_particles(s.download(), o, 1e-12, keys=("U1", "U2", "U3"))
+
+
+def test_fp_update_conserves_cell_momentum_and_energy(cuda_ok):
+    """Size-independent invariants of Velocity_FP_parallel on a 1M-particle
+    uneven box: per-cell sum of U and sum |U - U_cell|^2 are unchanged
+    (centred noise, src/Fokker_Planck.cpp:109-114; energy rescale :1169-1172)."""
+    cfg, parts = W.uneven_cells_2d(n_cells=(64, 64), precision=mcpm.FP64, hi=2000)
+    s, _ = _pair(cfg, parts, inject=False)
+    s.set_rng(mcpm.RNG_PHILOX)
+    s.cell_update()
+    c0 = s.get_cells()
+    s.random_generator()
+    s.velocity_update()
+    g = s.download()
+    idx = s.get_index()
+    C = s.C
+    cnt = np.bincount(idx, minlength=C)
+    for k, f in ((0, "U1"), (1, "U2"), (2, "U3")):
+        sums = np.bincount(idx, weights=g[f], minlength=C)
+        us = c0[mcpm.CF["U_SPACE"] + k]
+        np.testing.assert_allclose(sums, us * cnt, rtol=0, atol=1e-9 * (1 + np.abs(us * cnt)).max())
+    us = c0[mcpm.CF["U_SPACE"]:mcpm.CF["U_SPACE"] + 3][:, idx]
+    e = np.bincount(idx, weights=((g["U1"] - us[0]) ** 2 + (g["U2"] - us[1]) ** 2 + (g["U3"] - us[2]) ** 2),
+                    minlength=C)
+    e0 = c0[mcpm.CF["DM2"]] * cnt
+    np.testing.assert_allclose(e, e0, rtol=1e-10, atol=1e-12)
+
+
+# ------------------------------------------------------------ full step
+def test_loop_body_routines_fp64(cuda_ok):
+    cfg, parts = W.homogeneous_relaxation_1d(n_cells=20, ppc=100)
+    s, o = _pair(cfg, parts)
+    for _ in range(3):
+        rng = np.random.default_rng(o.step_count)
+        xi = [rng.standard_normal(o.N) for _ in range(3)]
+        s.inject_normals(*xi)
+        o.inject_normals(*xi)
+        s.loop_body()
+        o.step(1)
+    _close_particles(s.download(), o, 1e-11, keys=("x2", "U1", "U2", "U3"))
+
+
+@pytest.mark.parametrize("maker", ["relax", "slab_gf", "slab_direct", "uneven"])
+def test_fused_step_philox_fp64(cuda_ok, maker):
+    """mcpm_step (fused kernels) against orc_step, both drawing the same
+    Philox streams keyed by particle id and step."""
+    if maker == "relax":
+        cfg, parts = W.homogeneous_relaxation_1d(n_cells=25, ppc=80)
+    elif maker == "slab_gf":
+        cfg, parts = W.vlasov_slab_1d(n_cells=80, mean_ppc=60, long_range=mcpm.LR_SCREENED_POISSON)
+    elif maker == "slab_direct":
+        cfg, parts = W.vlasov_slab_1d(n_cells=80, mean_ppc=60, long_range=mcpm.LR_DIRECT)
+    else:
+        cfg, parts = W.uneven_cells_2d(n_cells=(12, 10), precision=mcpm.FP64, hi=700)
+    s, o = _pair(cfg, parts, inject=False)
+    s.set_rng(mcpm.RNG_PHILOX)
+    o.set_rng(mcpm.RNG_PHILOX)
+    s.step(3)
+    o.step(3)
+    _close_particles(s.download(), o, 1e-10)
+    cg, co = s.get_cells(), o.cells()
+    if cfg.long_range:
+        a, b = mcpm.cell_field(cg, "F2"), mcpm.cell_field(co, "F2", True)
+        assert np.max(np.abs(a - b)) <= 1e-10 * np.max(np.abs(b))
+
+
+def test_fused_step_fp32_tolerance(cuda_ok):
+    cfg64, parts = W.uneven_cells_2d(n_cells=(16, 16), precision=mcpm.FP64, hi=900)
+    cfg32 = cfg64.copy()
+    cfg32.precision = mcpm.FP32
+    s = mcpm.Session(cfg32)
+    s.upload(parts["x1"], parts["x2"], parts["U1"], parts["U2"], parts["U3"])
+    o = Oracle(cfg64, parts)
+    s.set_step(1)
+    o.set_step(1)
+    s.step(1)
+    o.step(1)
+    g = s.download()
+    for k in ("U1", "U2", "U3"):
+        err = np.max(np.abs(g[k] - getattr(o.s, k)))
+        assert err < 5e-4, (k, err)
+    # moment error of the FP32 step against FP64: the 1% bar of the benchmark
+    T32 = mcpm.cell_field(s.get_cells(), "T")
+    s64 = mcpm.Session(cfg64)
+    s64.upload(parts["x1"], parts["x2"], parts["U1"], parts["U2"], parts["U3"])
+    s64.set_step(1)
+    s64.step(1)
+    s.cell_update()
+    s64.cell_update()
+    T32, T64 = mcpm.cell_field(s.get_cells(), "T"), mcpm.cell_field(s64.get_cells(), "T")
+    assert np.max(np.abs(T32 - T64) / T64) < 1e-3
+
+
+# --------------------------------------------------------------- walls
+@pytest.mark.parametrize("problem", [mcpm.PROBLEM_COUETTE, mcpm.PROBLEM_WALL])
+def test_diffuse_walls_fp64(cuda_ok, problem):
+    if problem == mcpm.PROBLEM_COUETTE:
+        cfg, parts = W.esmc_box_2d(n_cells=(12, 12), ppc=40, precision=mcpm.FP64)
+        cfg.model = mcpm.MODEL_FP_DENSE
+    else:
+        cfg, parts = W.vlasov_slab_1d(n_cells=30, mean_ppc=40, long_range=mcpm.LR_NONE)
+        cfg.problem = mcpm.PROBLEM_WALL
+        cfg.T_wall[0] = 1.3
+    parts = {k: v.copy() for k, v in parts.items()}
+    parts["U2"] *= 5.0  # many wall hits
+    if problem == mcpm.PROBLEM_COUETTE:
+        parts["U1"] *= 5.0
+    s, o = _pair(cfg, parts, inject=False)
+    s.set_rng(mcpm.RNG_PHILOX)
+    o.set_rng(mcpm.RNG_PHILOX)
+    s.step(2)
+    o.step(2)
+    _close_particles(s.download(), o, 1e-10, keys=("x2", "U1", "U2", "U3") if problem == mcpm.PROBLEM_WALL
+                     else ("x1", "x2", "U1", "U2", "U3"))
+
+
+# ---------------------------------------------------------------- ESMC
+@pytest.mark.parametrize("shape", [(1, 30), (14, 12)])
+def test_esmc_fp64_same_layout(cuda_ok, shape):
+    """ESMC with the GPU's in-cell order given to the oracle: candidate picks,
+    directions, partners and acceptances then coincide."""
+    if shape[0] == 1:
+        cfg, parts = W.homogeneous_relaxation_1d(n_cells=shape[1], ppc=80)
+        cfg.model = mcpm.MODEL_ESMC
+    else:
+        cfg, parts = W.esmc_box_2d(n_cells=shape, ppc=60, precision=mcpm.FP64)
+    s, o = _pair(cfg, parts, inject=False)
+    s.set_step(0)
+    o.set_step(0)
+    s.cell_update()
+    o.cell_update()
+    s.init_omega_max()
+    o.init_omega_max()
+    s.set_step(1)
+    o.set_step(1)
+    s.cell_update()
+    o.cell_update()
+    pid, off = s.get_layout()
+    o.set_layout(off, pid)
+    s.velocity_update()
+    o.esmc()
+    _close_particles(s.download(), o, 1e-12, keys=("U1", "U2", "U3"))
+    om_g = mcpm.cell_field(s.get_cells(), "OMEGA_MAX")
+    om_o = mcpm.cell_field(o.cells(), "OMEGA_MAX", True)
+    assert np.max(np.abs(om_g - om_o)) <= 1e-12 * np.max(om_o)
+    # collisions conserve momentum and energy
+    g = s.download()
+    assert abs(g["U1"].sum() - parts["U1"].sum()) < 1e-8 * len(g["U1"])
+
+
+def test_esmc_fused_step_runs_fp32(cuda_ok):
+    cfg, parts = W.esmc_box_2d(n_cells=(32, 32), ppc=50, precision=mcpm.FP32)
+    s = mcpm.Session(cfg)
+    s.upload(parts["x1"], parts["x2"], parts["U1"], parts["U2"], parts["U3"])
+    s.cell_update()
+    s.init_omega_max()
+    s.step(5)
+    g = s.download()
+    assert np.all(np.isfinite(g["U1"]))
+    assert np.all((g["x2"] > 0) & (g["x2"] < cfg.length[1]))
