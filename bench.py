@@ -103,7 +103,7 @@ class ClockSampler:
             if pw > 200.0:
                 sm.append(s)
             for k, nm in enumerate(names):
-                if len(r) > 5 + k and "Active" in r[5 + k]:
+                if len(r) > 5 + k and r[5 + k].strip() == "Active":
                     reasons.add(nm)
         if not sm and rows:
             try:

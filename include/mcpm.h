@@ -179,7 +179,9 @@ int mcpm_check_status(mcpm_session* s);
 int mcpm_upload_particles(mcpm_session* s, int64_t n, const double* x1,
                           const double* x2, const double* U1, const double* U2,
                           const double* U3);
-/* Copies the device state back into caller arrays, in particle-id order. */
+/* Copies the device state back into caller arrays, in particle-id order.
+   When x1 never changes (direction[0] == 0 and not ESMC) the device does not
+   keep it and the caller's x1 is left untouched. */
 int mcpm_download_particles(mcpm_session* s, int64_t n, double* x1, double* x2,
                             double* U1, double* U2, double* U3);
 

@@ -102,6 +102,7 @@ template <> struct Acc<double> {
   __device__ __forceinline__ void zero() { v = 0.0; }
   __device__ __forceinline__ void add(double x) { v += x; }
   __device__ __forceinline__ double get() const { return v; }
+  __device__ __forceinline__ double getr() const { return v; }
   __device__ __forceinline__ void shfl_xor(int m) { v += __shfl_xor_sync(0xffffffffu, v, m); }
   __device__ __forceinline__ void merge(const Acc& o) { v += o.v; }
 };
@@ -110,6 +111,8 @@ template <> struct Acc<float> {
   __device__ __forceinline__ void zero() { c.hi = 0.f; c.lo = 0.f; }
   __device__ __forceinline__ void add(float x) { cadd(c, x); }
   __device__ __forceinline__ double get() const { return cvalue(c); }
+  // the value in float (no FP64 instruction)
+  __device__ __forceinline__ float getr() const { return c.hi + c.lo; }
   __device__ __forceinline__ void shfl_xor(int m) {
     CSum o;
     o.hi = __shfl_xor_sync(0xffffffffu, c.hi, m);
@@ -143,6 +146,37 @@ __device__ __forceinline__ void tile_reduce(Acc<real> (&a)[K], Acc<real>* smem) 
       a[q] = t;
     }
   }
+}
+
+// Reduce K <= 32 accumulators over a tile; returns to lane l (of warp 0
+// when TILE > 32) the total of accumulator l, so that K results can be
+// written by K lanes at once.
+template <typename real, int K, int TILE>
+__device__ __forceinline__ Acc<real> tile_reduce_lanes(Acc<real> (&a)[K], Acc<real>* smem) {
+  static_assert(K <= 32, "one accumulator per lane");
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int m = 16; m >= 1; m >>= 1)
+#pragma unroll
+    for (int q = 0; q < K; ++q) a[q].shfl_xor(m);
+  Acc<real> r;
+  r.zero();
+#pragma unroll
+  for (int q = 0; q < K; ++q)
+    if (lane == q) r = a[q];
+  if constexpr (TILE > 32) {
+    constexpr int W = TILE / 32;
+    const int warp = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane < K) smem[lane * W + warp] = r;
+    __syncthreads();
+    if (warp == 0 && lane < K) {
+      Acc<real> t = smem[lane * W];
+      for (int w = 1; w < W; ++w) t.merge(smem[lane * W + w]);
+      r = t;
+    }
+  }
+  return r;
 }
 
 __device__ __forceinline__ void raise_status(uint32_t* status, uint32_t bits) {

@@ -224,13 +224,16 @@ __global__ void k_face_quad(DevConsts k, const double* cell, const double* qoff,
 }
 
 // F2 per cell from the face potential, src/Main_Functions.cpp:3924-3938 / :3568-3577
-__global__ void k_face_force(DevConsts k, double* cell, const double* V, double coef) {
+__global__ void k_face_force(DevConsts k, double* cell, float* pcell, const double* V, double coef) {
   const int C = k.C;
   int num = blockIdx.x * blockDim.x + threadIdx.x;
   if (num >= k.N1) return;
   double F2 = -(V[num + 1] - V[num]) / k.dy;
   F2 = F2 / k.m * coef;
-  for (int j = 0; j < k.N0; ++j) cell[(size_t)MCPM_CF_F2 * C + num * k.N0 + j] = F2;
+  for (int j = 0; j < k.N0; ++j) {
+    cell[(size_t)MCPM_CF_F2 * C + num * k.N0 + j] = F2;
+    if (pcell) pcell[(size_t)(num * k.N0 + j) * PF_STRIDE + PF_F2DT] = (float)(F2 * k.dt);
+  }
 }
 
 // poisson_solver's tridiagonal system (src/Main_Functions.cpp:3375-3470)
@@ -287,7 +290,7 @@ int launch_long_range(Session& s) {
   if (mode == MCPM_LR_DIRECT) {
     k_face_quad<<<(nf * 32 + 127) / 128, 128, 0, s.stream>>>(s.k, s.cell, qoff, qw, V, nf, 0, 1);
     ++n;
-    k_face_force<<<(s.k.N1 + 127) / 128, 128, 0, s.stream>>>(s.k, s.cell, V, s.cfg.phi);
+    k_face_force<<<(s.k.N1 + 127) / 128, 128, 0, s.stream>>>(s.k, s.cell, s.prec == MCPM_FP32 ? s.pcell : nullptr, V, s.cfg.phi);
     ++n;
   } else {
     // the two wall values, then the PCR solve
@@ -295,7 +298,7 @@ int launch_long_range(Session& s) {
     ++n;
     k_poisson_pcr<<<1, 1024, 4 * nf * sizeof(double), s.stream>>>(s.k, s.cell, V, nf);
     ++n;
-    k_face_force<<<(s.k.N1 + 127) / 128, 128, 0, s.stream>>>(s.k, s.cell, V, s.cfg.ast);
+    k_face_force<<<(s.k.N1 + 127) / 128, 128, 0, s.stream>>>(s.k, s.cell, s.prec == MCPM_FP32 ? s.pcell : nullptr, V, s.cfg.ast);
     ++n;
   }
   return n;

@@ -18,7 +18,20 @@ enum {
   CFI_A2,                 // (1 - exp(-dt/tau)) tau
   CFI_A3,                 // sqrt((1 - exp(-2 dt/tau)) kT/m)
   CFI_3KT,                // 3 kb T / m
-  CF_DEV_COUNT
+  CFI_RAW,                // 29 raw central-moment sums from the moments kernel:
+                          // Mp(3) PIJ(6) M3(10) M4(6) M5(3) DM2(1), finalised by k_solve
+  CF_DEV_COUNT = CFI_RAW + 29
+};
+
+// Packed FP32 per-cell record the FP32 update kernel reads (written by the
+// solve and long-range kernels), so that the particle pass runs no FP64.
+enum {
+  PF_US0, PF_US1, PF_US2, PF_A1, PF_A2, PF_A3, PF_EQ, PF_LAM,
+  PF_C0, PF_C1, PF_C2, PF_C3, PF_C4, PF_C5, PF_G0, PF_G1, PF_G2, PF_Q0, PF_Q1, PF_Q2,
+  PF_AL0, PF_AL1, PF_AL2, PF_AL3, PF_AL4, PF_AL5, PF_BE0, PF_BE1, PF_GST,
+  PF_HQ0, PF_HQ1,          // M3[0]+M3[3]+M3[5], M3[1]+M3[6]+M3[8] (DFP heat-flux terms)
+  PF_PH0, PF_PH1, PF_F2DT, PF_N,
+  PF_STRIDE = 36
 };
 
 // Stages of the fused per-cell particle pass (update kernel).
@@ -90,6 +103,7 @@ struct Session {
   int32_t* wl = nullptr;        // [WL_COUNT]
   int32_t* work = nullptr;      // [WK_COUNT]
   double* cell = nullptr;       // [CF_DEV_COUNT][C]
+  float* pcell = nullptr;       // [C][PF_STRIDE] packed FP32 record
   double* xi = nullptr;         // [3][cap] whitened normals, slot order
   double* inj = nullptr;        // [3][cap] injected raw normals, particle-id order
   double* stage = nullptr;      // [5][cap] host<->device staging (double)

@@ -224,8 +224,10 @@ template <typename real> struct MomArgs {
 
 template <typename real, int TILE>
 __device__ void moments_cell(int c, const MomArgs<real>& a, Acc<real>* red) {
-  const int t = (TILE == 32) ? (threadIdx.x & 31) : threadIdx.x;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int t = (TILE == 32) ? lane : threadIdx.x;
   const int s0 = a.off[c], n = a.cnt[c];
+  const int C = a.k.C;
   Acc<real> u[3];
 #pragma unroll
   for (int q = 0; q < 3; ++q) u[q].zero();
@@ -235,10 +237,18 @@ __device__ void moments_cell(int c, const MomArgs<real>& a, Acc<real>* red) {
     u[2].add(a.U3[s0 + i]);
   }
   tile_reduce<real, 3, TILE>(u, red);
-  const double weight = (double)n;
-  double us0 = 0.0, us1 = 0.0, us2 = 0.0;
-  if (n > 0) { us0 = u[0].get() / weight; us1 = u[1].get() / weight; us2 = u[2].get() / weight; }
-  const real m0 = (real)us0, m1 = (real)us1, m2 = (real)us2;
+  // cell mean velocity U_space (src/Main_Functions.cpp:2493-2500); in the
+  // FP32 path the mean is formed in float, and stored widened
+  real m0 = 0, m1 = 0, m2 = 0;
+  if (n > 0) {
+    if constexpr (sizeof(real) == 8) {
+      const double weight = (double)n;
+      m0 = u[0].get() / weight; m1 = u[1].get() / weight; m2 = u[2].get() / weight;
+    } else {
+      const float w = (float)n;
+      m0 = u[0].getr() / w; m1 = u[1].getr() / w; m2 = u[2].getr() / w;
+    }
+  }
   Acc<real> q[29];
 #pragma unroll
   for (int j = 0; j < 29; ++j) q[j].zero();
@@ -257,48 +267,17 @@ __device__ void moments_cell(int c, const MomArgs<real>& a, Acc<real>* red) {
     q[25].add(Mp1 * energy * energy); q[26].add(Mp2 * energy * energy); q[27].add(Mp3 * energy * energy);
     q[28].add(energy);
   }
-  tile_reduce<real, 29, TILE>(q, red);
-  if (t != 0) return;
-  const DevConsts& k = a.k;
-  double* cl = a.cell;
-  const int C = k.C;
-  auto W = [&](int f, double v) { cl[(size_t)f * C + c] = v; };
-  double P[6], M3[10], M4[6], M5[3], Mp[3], DM2, DM4 = 0.0, Q[3] = {0.0, 0.0, 0.0};
-  for (int j = 0; j < 3; ++j) Mp[j] = q[j].get();
-  for (int j = 0; j < 6; ++j) P[j] = q[3 + j].get();
-  for (int j = 0; j < 10; ++j) M3[j] = q[9 + j].get();
-  for (int j = 0; j < 6; ++j) M4[j] = q[19 + j].get();
-  for (int j = 0; j < 3; ++j) M5[j] = q[25 + j].get();
-  DM2 = q[28].get();
-  if (n > 0) {
-    for (int j = 0; j < 6; ++j) P[j] = P[j] / weight;
-    for (int j = 0; j < 10; ++j) M3[j] = M3[j] / weight;
-    for (int j = 0; j < 6; ++j) M4[j] = M4[j] / weight;
-    for (int j = 0; j < 3; ++j) M5[j] = M5[j] / weight;
-    for (int j = 0; j < 3; ++j) Mp[j] = Mp[j] / weight;
-    DM2 = DM2 / weight;
-    DM4 = M4[0] + M4[3] + M4[5];
-    Q[0] = M3[0] + M3[3] + M3[5];
-    Q[1] = M3[1] + M3[6] + M3[8];
-    Q[2] = M3[2] + M3[7] + M3[9];
+  // raw sums, one field per lane; the FP64 finalisation (divisions by the
+  // weight, T, n, Y, gamma*) runs once per cell in k_solve
+  Acc<real> tot = tile_reduce_lanes<real, 29, TILE>(q, red);
+  if (TILE == 32 || warp == 0) {
+    double* cl = a.cell;
+    if (lane < 29) cl[(size_t)(CFI_RAW + lane) * C + c] = tot.get();
+    else if (lane == 29) cl[(size_t)(MCPM_CF_U_SPACE + 0) * C + c] = (double)m0;
+    else if (lane == 30) cl[(size_t)(MCPM_CF_U_SPACE + 1) * C + c] = (double)m1;
+    else cl[(size_t)(MCPM_CF_U_SPACE + 2) * C + c] = (double)m2;
+    if (lane == 0) cl[(size_t)MCPM_CF_NUM_INSIDE * C + c] = (double)n;
   }
-  W(MCPM_CF_NUM_INSIDE, (double)n);
-  W(MCPM_CF_U_SPACE + 0, us0); W(MCPM_CF_U_SPACE + 1, us1); W(MCPM_CF_U_SPACE + 2, us2);
-  for (int j = 0; j < 6; ++j) W(MCPM_CF_PIJ + j, P[j]);
-  for (int j = 0; j < 10; ++j) W(MCPM_CF_M3 + j, M3[j]);
-  for (int j = 0; j < 6; ++j) W(MCPM_CF_M4 + j, M4[j]);
-  for (int j = 0; j < 3; ++j) W(MCPM_CF_M5 + j, M5[j]);
-  for (int j = 0; j < 3; ++j) W(MCPM_CF_Q + j, Q[j]);
-  for (int j = 0; j < 3; ++j) W(MCPM_CF_MP + j, Mp[j]);
-  W(MCPM_CF_DM2, DM2);
-  W(MCPM_CF_DM4, DM4);
-  double T = k.m * DM2 / (3.0 * k.kb);
-  double nn = 1 * k.Fn * weight / cell_volume(c, k);
-  double Y = ycoll(nn, k.b);
-  W(MCPM_CF_T, T);
-  W(MCPM_CF_N, nn);
-  W(CFI_Y, Y);
-  if (weight > 1e-14) W(MCPM_CF_GAMMA_ST, -0.001 * (nn * k.b * Y / (k.kb * T / k.m)));
 }
 
 template <typename real>
@@ -313,11 +292,23 @@ __global__ void __launch_bounds__(256) k_moments(MomArgs<real> a) {
 // Gauss_Jordan, src/Math_Func.cpp:165-232, restated exactly: scaled partial
 // pivoting over the full row, reciprocal-then-multiply factor, full-row
 // updates, back substitution.
+// maxx_magnittude (src/Math_Func.cpp:107-119): first index of the largest
+// |a_i|.  For non-NaN doubles |x| orders like the integer value of its bits
+// with the sign cleared, so the comparisons run on the integer pipe; NaN
+// entries never win a comparison, and a NaN a[0] makes every comparison
+// false (index 0), as in the reference.
+__device__ __forceinline__ unsigned long long absbits(double x) {
+  return (unsigned long long)__double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFull;
+}
 __device__ __forceinline__ int gj_maxmag(const double* a, int n) {
-  double b = fabs(a[0]);
+  const unsigned long long INF = 0x7FF0000000000000ull;
+  unsigned long long b = absbits(a[0]);
+  if (b > INF) return 0;
   int l = 0;
-  for (int i = 0; i < n; ++i)
-    if (fabs(b) < fabs(a[i])) { b = fabs(a[i]); l = i; }
+  for (int i = 0; i < n; ++i) {
+    unsigned long long v = absbits(a[i]);
+    if (v <= INF && b < v) { b = v; l = i; }
+  }
   return l;
 }
 template <int n>
@@ -338,8 +329,9 @@ __device__ void gauss_jordan(double* A, double* R, double* x) {
       for (int j = 0; j < n; ++j) { double b = A[i * n + j]; A[i * n + j] = A[k * n + j]; A[k * n + j] = b; }
       double c = R[i]; R[i] = R[k]; R[k] = c;
     }
+    const double rinv = 1.0 / A[i * n + i];
     for (int j = i + 1; j < n; ++j) {
-      double F = (1.0 / A[i * n + i]) * A[j * n + i];
+      double F = rinv * A[j * n + i];
       for (int kk = 0; kk < n; ++kk) A[j * n + kk] = A[j * n + kk] - F * A[i * n + kk];
       R[j] = R[j] - F * R[i];
     }
@@ -357,8 +349,8 @@ __device__ void gauss_jordan(double* A, double* R, double* x) {
 // on the 12x12 performs exactly the arithmetic of the three 4x4 solves),
 // c/gamma (src/Fokker_Planck.cpp:590-804, 9x9), phi (:2734-2746) and the
 // Velocity_FP_parallel constants A1..A3 (src/Fokker_Planck.cpp:1099-1112).
-__global__ void __launch_bounds__(128) k_solve(DevConsts k, double* cell, int with_alpha, int fp_model,
-                                               uint32_t* status) {
+__global__ void __launch_bounds__(128) k_solve(DevConsts k, double* cell, float* pcell, int with_alpha,
+                                               int fp_model, uint32_t* status) {
   const int C = k.C;
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= C) return;
@@ -367,14 +359,45 @@ __global__ void __launch_bounds__(128) k_solve(DevConsts k, double* cell, int wi
   auto W = [&](int f, double v) { cell[(size_t)f * C + c] = v; };
   const double weight = R(MCPM_CF_NUM_INSIDE);
   const int ncnt = (int)weight;
-  double P[6], M3[10], M4[6], M5[3], Q[3], Mp[3];
-  for (int j = 0; j < 6; ++j) P[j] = R(MCPM_CF_PIJ + j);
-  for (int j = 0; j < 10; ++j) M3[j] = R(MCPM_CF_M3 + j);
-  for (int j = 0; j < 6; ++j) M4[j] = R(MCPM_CF_M4 + j);
-  for (int j = 0; j < 3; ++j) { M5[j] = R(MCPM_CF_M5 + j); Q[j] = R(MCPM_CF_Q + j); Mp[j] = R(MCPM_CF_MP + j); }
-  const double DM2 = R(MCPM_CF_DM2), DM4 = R(MCPM_CF_DM4), T = R(MCPM_CF_T), n = R(MCPM_CF_N);
-  const double gst = R(MCPM_CF_GAMMA_ST);
-  const double Ycell = R(CFI_Y);
+  // ---- moment finalisation, src/Main_Functions.cpp:2563-2593
+  double P[6], M3[10], M4[6], M5[3], Q[3] = {0.0, 0.0, 0.0}, Mp[3], DM2, DM4 = 0.0;
+  for (int j = 0; j < 3; ++j) Mp[j] = R(CFI_RAW + j);
+  for (int j = 0; j < 6; ++j) P[j] = R(CFI_RAW + 3 + j);
+  for (int j = 0; j < 10; ++j) M3[j] = R(CFI_RAW + 9 + j);
+  for (int j = 0; j < 6; ++j) M4[j] = R(CFI_RAW + 19 + j);
+  for (int j = 0; j < 3; ++j) M5[j] = R(CFI_RAW + 25 + j);
+  DM2 = R(CFI_RAW + 28);
+  if (ncnt > 0) {
+    for (int j = 0; j < 6; ++j) P[j] = P[j] / weight;
+    for (int j = 0; j < 10; ++j) M3[j] = M3[j] / weight;
+    for (int j = 0; j < 6; ++j) M4[j] = M4[j] / weight;
+    for (int j = 0; j < 3; ++j) M5[j] = M5[j] / weight;
+    for (int j = 0; j < 3; ++j) Mp[j] = Mp[j] / weight;
+    DM2 = DM2 / weight;
+    DM4 = M4[0] + M4[3] + M4[5];
+    Q[0] = M3[0] + M3[3] + M3[5];
+    Q[1] = M3[1] + M3[6] + M3[8];
+    Q[2] = M3[2] + M3[7] + M3[9];
+  }
+  for (int j = 0; j < 6; ++j) W(MCPM_CF_PIJ + j, P[j]);
+  for (int j = 0; j < 10; ++j) W(MCPM_CF_M3 + j, M3[j]);
+  for (int j = 0; j < 6; ++j) W(MCPM_CF_M4 + j, M4[j]);
+  for (int j = 0; j < 3; ++j) W(MCPM_CF_M5 + j, M5[j]);
+  for (int j = 0; j < 3; ++j) W(MCPM_CF_Q + j, Q[j]);
+  for (int j = 0; j < 3; ++j) W(MCPM_CF_MP + j, Mp[j]);
+  W(MCPM_CF_DM2, DM2);
+  W(MCPM_CF_DM4, DM4);
+  const double T = k.m * DM2 / (3.0 * k.kb);
+  const double n = 1 * k.Fn * weight / cell_volume(c, k);
+  const double Ycell = ycoll(n, k.b);
+  W(MCPM_CF_T, T);
+  W(MCPM_CF_N, n);
+  W(CFI_Y, Ycell);
+  double gst = R(MCPM_CF_GAMMA_ST);
+  if (weight > 1e-14) {
+    gst = -0.001 * (n * k.b * Ycell / (k.kb * T / k.m));
+    W(MCPM_CF_GAMMA_ST, gst);
+  }
   uint32_t bad = 0;
   double Lam = R(MCPM_CF_LAMBDA);
   if (weight > 1e-14) {
@@ -514,10 +537,32 @@ __global__ void __launch_bounds__(128) k_solve(DevConsts k, double* cell, int wi
       W(CFI_A2, (1.0 - exp(-k.dt / tau)) * tau);
     }
   }
-  W(CFI_3KT, 3.0 * k.kb * T / k.m);
-  W(MCPM_CF_PHI + 0, al[0] * Mp[0] + al[1] * Mp[1] + al[2] * Mp[2]);
-  W(MCPM_CF_PHI + 1, al[3] * Mp[0] + al[4] * Mp[1] + al[5] * Mp[2]);
+  const double eq3 = 3.0 * k.kb * T / k.m;
+  W(CFI_3KT, eq3);
+  const double ph0 = al[0] * Mp[0] + al[1] * Mp[1] + al[2] * Mp[2];
+  const double ph1 = al[3] * Mp[0] + al[4] * Mp[1] + al[5] * Mp[2];
+  W(MCPM_CF_PHI + 0, ph0);
+  W(MCPM_CF_PHI + 1, ph1);
   W(MCPM_CF_PHI + 2, al[6] * Mp[0] + al[7] * Mp[1] + al[8] * Mp[2]);
+  if (pcell) {
+    // the FP32 update kernel's per-cell record
+    float* pf = pcell + (size_t)c * PF_STRIDE;
+    pf[PF_US0] = (float)R(MCPM_CF_U_SPACE + 0);
+    pf[PF_US1] = (float)R(MCPM_CF_U_SPACE + 1);
+    pf[PF_US2] = (float)R(MCPM_CF_U_SPACE + 2);
+    pf[PF_A1] = (float)R(CFI_A1); pf[PF_A2] = (float)R(CFI_A2); pf[PF_A3] = (float)R(CFI_A3);
+    pf[PF_EQ] = (float)eq3;
+    pf[PF_LAM] = (float)Lam;
+    for (int j = 0; j < 6; ++j) pf[PF_C0 + j] = (float)R(MCPM_CF_C + j);
+    for (int j = 0; j < 3; ++j) { pf[PF_G0 + j] = (float)R(MCPM_CF_GAMMA + j); pf[PF_Q0 + j] = (float)Q[j]; }
+    for (int j = 0; j < 6; ++j) pf[PF_AL0 + j] = (float)al[j];
+    pf[PF_BE0] = (float)be[0]; pf[PF_BE1] = (float)be[1];
+    pf[PF_GST] = (float)gst;
+    pf[PF_HQ0] = (float)(M3[0] + M3[3] + M3[5]);
+    pf[PF_HQ1] = (float)(M3[1] + M3[6] + M3[8]);
+    pf[PF_PH0] = (float)ph0; pf[PF_PH1] = (float)ph1;
+    pf[PF_N] = (float)ncnt;
+  }
   raise_status(status, bad);
 }
 
@@ -721,6 +766,7 @@ __device__ __forceinline__ void apply_bc(PState<real>& s, int call, int pid, int
 template <typename real> struct UpdArgs {
   DevConsts k;
   const double* cell;
+  const float* pcell;
   const int32_t *off, *cnt, *list_small, *list_big, *wl;
   int32_t* work;
   PT<real> p;
@@ -746,6 +792,52 @@ __device__ __forceinline__ void raw_normals(const UpdArgs<real>& a, int64_t p, r
   }
 }
 
+// Per-cell constants of the particle pass.  FP64: read from the double cell
+// array, expressions as in the reference.  FP32: the packed float record.
+template <typename real> struct CellK {
+  real us0, us1, us2, A1, A2, A3, eq, lam, c[6], g[3], q[3];
+  real al[6], be0, be1, gst, m3_0, m3_3, m3_5, m3_1, m3_6, m3_8, hq0, hq1, ph0, ph1, f2dt;
+};
+template <typename real>
+__device__ __forceinline__ void load_cellk(CellK<real>& K, int c, const UpdArgs<real>& a, uint32_t st) {
+  if constexpr (sizeof(real) == 4) {
+    const float* pf = a.pcell + (size_t)c * PF_STRIDE;
+    K.us0 = pf[PF_US0]; K.us1 = pf[PF_US1]; K.us2 = pf[PF_US2];
+    K.A1 = pf[PF_A1]; K.A2 = pf[PF_A2]; K.A3 = pf[PF_A3]; K.eq = pf[PF_EQ]; K.lam = pf[PF_LAM];
+#pragma unroll
+    for (int j = 0; j < 6; ++j) { K.c[j] = pf[PF_C0 + j]; K.al[j] = pf[PF_AL0 + j]; }
+#pragma unroll
+    for (int j = 0; j < 3; ++j) { K.g[j] = pf[PF_G0 + j]; K.q[j] = pf[PF_Q0 + j]; }
+    K.be0 = pf[PF_BE0]; K.be1 = pf[PF_BE1]; K.gst = pf[PF_GST];
+    K.hq0 = pf[PF_HQ0]; K.hq1 = pf[PF_HQ1]; K.ph0 = pf[PF_PH0]; K.ph1 = pf[PF_PH1];
+    K.f2dt = pf[PF_F2DT];
+    K.m3_0 = K.m3_3 = K.m3_5 = K.m3_1 = K.m3_6 = K.m3_8 = 0.f;
+  } else {
+    const CellRef R{a.cell, a.k.C};
+    K.us0 = R(MCPM_CF_U_SPACE + 0, c); K.us1 = R(MCPM_CF_U_SPACE + 1, c); K.us2 = R(MCPM_CF_U_SPACE + 2, c);
+    K.A1 = R(CFI_A1, c); K.A2 = R(CFI_A2, c); K.A3 = R(CFI_A3, c); K.eq = R(CFI_3KT, c);
+    K.lam = R(MCPM_CF_LAMBDA, c);
+    for (int j = 0; j < 6; ++j) { K.c[j] = R(MCPM_CF_C + j, c); K.al[j] = R(MCPM_CF_ALPHA + j, c); }
+    for (int j = 0; j < 3; ++j) { K.g[j] = R(MCPM_CF_GAMMA + j, c); K.q[j] = R(MCPM_CF_Q + j, c); }
+    K.be0 = R(MCPM_CF_BETA + 0, c); K.be1 = R(MCPM_CF_BETA + 1, c); K.gst = R(MCPM_CF_GAMMA_ST, c);
+    K.m3_0 = R(MCPM_CF_M3 + 0, c); K.m3_3 = R(MCPM_CF_M3 + 3, c); K.m3_5 = R(MCPM_CF_M3 + 5, c);
+    K.m3_1 = R(MCPM_CF_M3 + 1, c); K.m3_6 = R(MCPM_CF_M3 + 6, c); K.m3_8 = R(MCPM_CF_M3 + 8, c);
+    K.hq0 = K.hq1 = 0.0;
+    K.ph0 = R(MCPM_CF_PHI + 0, c); K.ph1 = R(MCPM_CF_PHI + 1, c);
+    K.f2dt = (st & ST_LR) ? R(MCPM_CF_F2, c) * a.k.dt : 0.0;
+  }
+}
+
+// sum / n and sqrt(sum / n) in the path's precision
+template <typename real> __device__ __forceinline__ real cmean(const Acc<real>& s, int n) {
+  if constexpr (sizeof(real) == 4) return s.getr() / (float)n;
+  else return s.get() / (1.0 * n);
+}
+template <typename real> __device__ __forceinline__ real crms(const Acc<real>& s, int n) {
+  if constexpr (sizeof(real) == 4) return sqrtf(s.getr() / (float)n);
+  else return sqrt(s.get() / (1.0 * n));
+}
+
 // random_generator (src/Fokker_Planck.cpp:20-145) + Velocity_FP_parallel
 // (:1065-1182) + long-range kick (src/Main_Functions.cpp:3937, :3578) +
 // DFP_extra_streaming (src/Fokker_Planck.cpp:904-946) + apply_BC /
@@ -761,12 +853,13 @@ __device__ void update_cell(int c, const UpdArgs<real>& a, real* xs, int xcap, A
   const uint32_t st = a.stages;
   const bool rng = st & ST_RNG, fp = st & ST_FP, load_xi = st & ST_LOAD_XI, store_xi = st & ST_STORE_XI;
   const bool staged = rng && n <= xcap;
-  const CellRef R{a.cell, k.C};
-  const real Us0 = (real)R(MCPM_CF_U_SPACE + 0, c), Us1 = (real)R(MCPM_CF_U_SPACE + 1, c),
-             Us2 = (real)R(MCPM_CF_U_SPACE + 2, c);
+  CellK<real> K;
+  load_cellk<real>(K, c, a, st);
+  const real Us0 = K.us0, Us1 = K.us1, Us2 = K.us2;
   PT<real> P = a.p;
   real mean0 = 0, mean1 = 0, mean2 = 0, rms0 = 1, rms1 = 1, rms2 = 1;
-  double frac1 = 0.0;
+  Acc<real> f1acc;
+  f1acc.zero();
   // ---- pass A: draws, their per-cell sums, sum |M'|^2
   if (rng || fp) {
     Acc<real> s4[4];
@@ -786,11 +879,9 @@ __device__ void update_cell(int c, const UpdArgs<real>& a, real* xs, int xcap, A
       }
     }
     tile_reduce<real, 4, TILE>(s4, red);
-    frac1 = s4[3].get();
+    f1acc = s4[3];
     if (rng) {
-      mean0 = (real)(s4[0].get() / (1.0 * n));
-      mean1 = (real)(s4[1].get() / (1.0 * n));
-      mean2 = (real)(s4[2].get() / (1.0 * n));
+      mean0 = cmean(s4[0], n); mean1 = cmean(s4[1], n); mean2 = cmean(s4[2], n);
       // ---- pass B: per-cell RMS of the centred draws
       Acc<real> s3[3];
 #pragma unroll
@@ -803,12 +894,12 @@ __device__ void update_cell(int c, const UpdArgs<real>& a, real* xs, int xcap, A
         s3[0].add(d0 * d0); s3[1].add(d1 * d1); s3[2].add(d2 * d2);
       }
       tile_reduce<real, 3, TILE>(s3, red);
-      rms0 = (real)sqrt(s3[0].get() / (1.0 * n));
-      rms1 = (real)sqrt(s3[1].get() / (1.0 * n));
-      rms2 = (real)sqrt(s3[2].get() / (1.0 * n));
+      rms0 = crms(s3[0], n); rms1 = crms(s3[1], n); rms2 = crms(s3[2], n);
     }
   }
-  // whitened normal of the i-th particle of the cell
+  // whitened normal of the i-th particle of the cell (after pass C the
+  // staged values are already whitened and whiten == false)
+  bool whiten = true;
   auto xiw = [&](int i, real& z0, real& z1, real& z2) {
     int64_t p = s0 + i;
     if (load_xi) {
@@ -817,20 +908,10 @@ __device__ void update_cell(int c, const UpdArgs<real>& a, real* xs, int xcap, A
     }
     if (staged) { z0 = xs[3 * i]; z1 = xs[3 * i + 1]; z2 = xs[3 * i + 2]; }
     else raw_normals(a, p, z0, z1, z2);
-    if (n > 1) {
+    if (whiten && n > 1) {
       z0 = (z0 - mean0) / rms0; z1 = (z1 - mean1) / rms1; z2 = (z2 - mean2) / rms2;
     }
   };
-  // per-cell FP constants
-  real A1 = 0, A2 = 0, A3 = 0, eq = 0, Lam = 0, cc[6], gm[3], Q[3];
-  if (fp && n > 1) {
-    A1 = (real)R(CFI_A1, c); A2 = (real)R(CFI_A2, c); A3 = (real)R(CFI_A3, c);
-    eq = (real)R(CFI_3KT, c); Lam = (real)R(MCPM_CF_LAMBDA, c);
-#pragma unroll
-    for (int j = 0; j < 6; ++j) cc[j] = (real)R(MCPM_CF_C + j, c);
-#pragma unroll
-    for (int j = 0; j < 3; ++j) { gm[j] = (real)R(MCPM_CF_GAMMA + j, c); Q[j] = (real)R(MCPM_CF_Q + j, c); }
-  }
   // the Ornstein-Uhlenbeck update of M' with the cubic drift
   auto mnew = [&](int i, real& m1, real& m2, real& m3) {
     int64_t p = s0 + i;
@@ -839,24 +920,23 @@ __device__ void update_cell(int c, const UpdArgs<real>& a, real* xs, int xcap, A
       real z0, z1, z2;
       xiw(i, z0, z1, z2);
       real energy = m1 * m1 + m2 * m2 + m3 * m3;
-      real d0 = cc[0] * m1 + cc[1] * m2 + cc[2] * m3;
-      d0 += gm[0] * (energy - eq);
-      d0 += Lam * (m1 * energy - Q[0]);
-      real d1 = cc[1] * m1 + cc[3] * m2 + cc[4] * m3;
-      d1 += gm[1] * (energy - eq);
-      d1 += Lam * (m2 * energy - Q[1]);
-      real d2 = cc[2] * m1 + cc[4] * m2 + cc[5] * m3;
-      d2 += gm[2] * (energy - eq);
-      d2 += Lam * (m3 * energy - Q[2]);
-      m1 = A1 * m1 + A2 * d0 + A3 * z0;
-      m2 = A1 * m2 + A2 * d1 + A3 * z1;
-      m3 = A1 * m3 + A2 * d2 + A3 * z2;
+      real d0 = K.c[0] * m1 + K.c[1] * m2 + K.c[2] * m3;
+      d0 += K.g[0] * (energy - K.eq);
+      d0 += K.lam * (m1 * energy - K.q[0]);
+      real d1 = K.c[1] * m1 + K.c[3] * m2 + K.c[4] * m3;
+      d1 += K.g[1] * (energy - K.eq);
+      d1 += K.lam * (m2 * energy - K.q[1]);
+      real d2 = K.c[2] * m1 + K.c[4] * m2 + K.c[5] * m3;
+      d2 += K.g[2] * (energy - K.eq);
+      d2 += K.lam * (m3 * energy - K.q[2]);
+      m1 = K.A1 * m1 + K.A2 * d0 + K.A3 * z0;
+      m2 = K.A1 * m2 + K.A2 * d1 + K.A3 * z1;
+      m3 = K.A1 * m3 + K.A2 * d2 + K.A3 * z2;
     } else {
       m1 = 0; m2 = 0; m3 = 0;
     }
   };
   // ---- pass C: whitened normals (staged / stored) and sum |M'_new|^2
-  double frac2 = 0.0;
   uint32_t bad = 0;
   if (rng && (staged || store_xi)) {
     for (int i = t; i < n; i += TILE) {
@@ -868,11 +948,10 @@ __device__ void update_cell(int c, const UpdArgs<real>& a, real* xs, int xcap, A
       }
       if (staged) { xs[3 * i] = z0; xs[3 * i + 1] = z1; xs[3 * i + 2] = z2; }
     }
+    if (staged) whiten = false;
   }
-  // after this point xiw must return the whitened values from the stage
-  const real sm0 = mean0, sm1 = mean1, sm2 = mean2;
-  if (staged) { mean0 = 0; mean1 = 0; mean2 = 0; rms0 = 1; rms1 = 1; rms2 = 1; }
-  (void)sm0; (void)sm1; (void)sm2;
+  Acc<real> f2acc;
+  f2acc.zero();
   if (fp) {
     Acc<real> f2[1];
     f2[0].zero();
@@ -883,7 +962,7 @@ __device__ void update_cell(int c, const UpdArgs<real>& a, real* xs, int xcap, A
       f2[0].add(m1 * m1 + m2 * m2 + m3 * m3);
     }
     tile_reduce<real, 1, TILE>(f2, red);
-    frac2 = f2[0].get();
+    f2acc = f2[0];
   }
   const uint32_t pos_stages = ST_LR | ST_DFP | ST_BC1 | ST_OLD | ST_STREAM | ST_BC2 | ST_BC3 | ST_KEY;
   if (!(fp || (st & pos_stages))) {
@@ -891,21 +970,12 @@ __device__ void update_cell(int c, const UpdArgs<real>& a, real* xs, int xcap, A
     return;
   }
   // ---- pass D: final velocities, then the position pipeline
-  const real scale = (fp && n > 1) ? (real)sqrt(fabs(frac1 / frac2)) : (real)1;
-  const real F2dt = (st & ST_LR) ? (real)(R(MCPM_CF_F2, c) * k.dt) : (real)0;
-  real al[6], be0 = 0, be1 = 0, gst = 0, eqd = 0, q0 = 0, q1 = 0, ph0 = 0, ph1 = 0;
-  if (st & ST_DFP) {
-#pragma unroll
-    for (int j = 0; j < 6; ++j) al[j] = (real)R(MCPM_CF_ALPHA + j, c);
-    be0 = (real)R(MCPM_CF_BETA + 0, c); be1 = (real)R(MCPM_CF_BETA + 1, c);
-    gst = (real)R(MCPM_CF_GAMMA_ST, c); eqd = (real)R(CFI_3KT, c);
-    q0 = (real)(R(MCPM_CF_M3 + 0, c)); q1 = (real)(R(MCPM_CF_M3 + 1, c));
-    ph0 = (real)R(MCPM_CF_PHI + 0, c); ph1 = (real)R(MCPM_CF_PHI + 1, c);
+  real scale = (real)1;
+  if (fp && n > 1) {
+    if constexpr (sizeof(real) == 4) scale = sqrtf(fabsf(f1acc.getr() / f2acc.getr()));
+    else scale = sqrt(fabs(f1acc.get() / f2acc.get()));
   }
-  const real M3_3 = (st & ST_DFP) ? (real)R(MCPM_CF_M3 + 3, c) : (real)0;
-  const real M3_5 = (st & ST_DFP) ? (real)R(MCPM_CF_M3 + 5, c) : (real)0;
-  const real M3_6 = (st & ST_DFP) ? (real)R(MCPM_CF_M3 + 6, c) : (real)0;
-  const real M3_8 = (st & ST_DFP) ? (real)R(MCPM_CF_M3 + 8, c) : (real)0;
+  const real F2dt = (st & ST_LR) ? K.f2dt : (real)0;
   const real dtr = (real)k.dt;
   const int iters = (n + TILE - 1) / TILE;
   for (int r = 0; r < iters; ++r) {
@@ -933,15 +1003,32 @@ __device__ void update_cell(int c, const UpdArgs<real>& a, real* xs, int xcap, A
       if (st & ST_LR) s.u2 = s.u2 + F2dt;
       if (st & ST_DFP) {
         real e = (s.u1 - Us0) * (s.u1 - Us0) + (s.u2 - Us1) * (s.u2 - Us1) + (s.u3 - Us2) * (s.u3 - Us2);
-        if (k.dir0 == 1) {
-          s.x1 = s.x1 + dtr * ((s.u1 - Us0) * al[0] + (s.u2 - Us1) * al[1] + (s.u3 - Us2) * al[2] + be0 * (e - eqd)) +
-                 gst * ((s.u1 - Us1) * e - q0 - M3_3 - M3_5) * dtr;
-          s.x1 = s.x1 - dtr * ph0;
-        }
-        if (k.dir1 == 1) {
-          s.x2 = s.x2 + dtr * ((s.u1 - Us0) * al[3] + (s.u2 - Us1) * al[4] + (s.u3 - Us2) * al[5] + be1 * (e - eqd)) +
-                 gst * ((s.u2 - Us1) * e - q1 - M3_6 - M3_8) * dtr;
-          s.x2 = s.x2 - dtr * ph1;
+        if constexpr (sizeof(real) == 8) {
+          if (k.dir0 == 1) {
+            s.x1 = s.x1 + dtr * ((s.u1 - Us0) * K.al[0] + (s.u2 - Us1) * K.al[1] + (s.u3 - Us2) * K.al[2] +
+                                 K.be0 * (e - K.eq)) +
+                   K.gst * ((s.u1 - Us1) * e - K.m3_0 - K.m3_3 - K.m3_5) * dtr;
+            s.x1 = s.x1 - dtr * K.ph0;
+          }
+          if (k.dir1 == 1) {
+            s.x2 = s.x2 + dtr * ((s.u1 - Us0) * K.al[3] + (s.u2 - Us1) * K.al[4] + (s.u3 - Us2) * K.al[5] +
+                                 K.be1 * (e - K.eq)) +
+                   K.gst * ((s.u2 - Us1) * e - K.m3_1 - K.m3_6 - K.m3_8) * dtr;
+            s.x2 = s.x2 - dtr * K.ph1;
+          }
+        } else {
+          if (k.dir0 == 1) {
+            s.x1 = s.x1 + dtr * ((s.u1 - Us0) * K.al[0] + (s.u2 - Us1) * K.al[1] + (s.u3 - Us2) * K.al[2] +
+                                 K.be0 * (e - K.eq)) +
+                   K.gst * ((s.u1 - Us1) * e - K.hq0) * dtr;
+            s.x1 = s.x1 - dtr * K.ph0;
+          }
+          if (k.dir1 == 1) {
+            s.x2 = s.x2 + dtr * ((s.u1 - Us0) * K.al[3] + (s.u2 - Us1) * K.al[4] + (s.u3 - Us2) * K.al[5] +
+                                 K.be1 * (e - K.eq)) +
+                   K.gst * ((s.u2 - Us1) * e - K.hq1) * dtr;
+            s.x2 = s.x2 - dtr * K.ph1;
+          }
         }
       }
       if (st & ST_BC1) apply_bc<real>(s, a.bc_call_base + 0, pid, a.step, k, bad);
@@ -962,10 +1049,7 @@ __device__ void update_cell(int c, const UpdArgs<real>& a, real* xs, int xcap, A
         a.key_out[p] = key;
       }
     }
-    if (st & ST_KEY) {
-      if (TILE == 32) count_key(a.cnt_next, key, act);
-      else count_key(a.cnt_next, key, act);
-    }
+    if (st & ST_KEY) count_key(a.cnt_next, key, act);
   }
   raise_status(a.status, bad);
 }
@@ -1050,7 +1134,8 @@ int launch_moments(Session& s) { return s.prec == MCPM_FP32 ? moments_impl<float
 
 int launch_solve(Session& s, int with_alpha) {
   int fp = (s.cfg.model == MCPM_MODEL_FP_DENSE || s.cfg.model == MCPM_MODEL_FP_IDEAL_GAS) ? 1 : 0;
-  k_solve<<<(s.C + 127) / 128, 128, 0, s.stream>>>(s.k, s.cell, with_alpha, fp, s.status);
+  k_solve<<<(s.C + 127) / 128, 128, 0, s.stream>>>(s.k, s.cell, s.prec == MCPM_FP32 ? s.pcell : nullptr,
+                                                    with_alpha, fp, s.status);
   return 1;
 }
 
@@ -1063,6 +1148,7 @@ template <typename real> static int update_impl(Session& s, uint32_t stages, int
   UpdArgs<real> a;
   a.k = s.k;
   a.cell = s.cell;
+  a.pcell = s.pcell;
   a.off = s.off; a.cnt = s.cnt; a.list_small = s.list_small; a.list_big = s.list_big; a.wl = s.wl;
   a.work = s.work;
   a.p = pt<real>(s.P[s.cur]);

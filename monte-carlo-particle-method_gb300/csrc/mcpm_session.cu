@@ -177,7 +177,7 @@ int mcpm_session_create(const mcpm_config* cfg, mcpm_session** out) {
   ok = ok && A((void**)&s->key, cap * 4) && A((void**)&s->cnt, C * 4) && A((void**)&s->cnt_next, C * 4) &&
        A((void**)&s->off, (C + 1) * 4) && A((void**)&s->cursor, C * 4) && A((void**)&s->list_small, C * 4) &&
        A((void**)&s->list_big, C * 4) && A((void**)&s->wl, WL_COUNT * 4) && A((void**)&s->work, WK_COUNT * 4) &&
-       A((void**)&s->cell, (size_t)CF_DEV_COUNT * C * 8) && A((void**)&s->xi, 3 * cap * 8) &&
+       A((void**)&s->cell, (size_t)CF_DEV_COUNT * C * 8) && A((void**)&s->pcell, (size_t)PF_STRIDE * C * 4) && A((void**)&s->xi, 3 * cap * 8) &&
        A((void**)&s->inj, 3 * cap * 8) && A((void**)&s->stage, 5 * cap * 8) &&
        A((void**)&s->faces, ((size_t)k.N1 + 1 + 5000) * 8) && A((void**)&s->status, 16);
   if (!ok) {
@@ -187,6 +187,7 @@ int mcpm_session_create(const mcpm_config* cfg, mcpm_session** out) {
   }
   cudaMemsetAsync(s->cnt_next, 0, C * 4, s->stream);
   cudaMemsetAsync(s->cell, 0, (size_t)CF_DEV_COUNT * C * 8, s->stream);
+  cudaMemsetAsync(s->pcell, 0, (size_t)PF_STRIDE * C * 4, s->stream);
   cudaMemsetAsync(s->status, 0, 16, s->stream);
   cudaMemsetAsync(s->work, 0, WK_COUNT * 4, s->stream);
   cudaMemsetAsync(s->inj, 0, 3 * cap * 8, s->stream);
@@ -213,7 +214,7 @@ int mcpm_session_destroy(mcpm_session* s) {
     cudaFree(P.x1o); cudaFree(P.x2o);
   }
   cudaFree(s->key); cudaFree(s->cnt); cudaFree(s->cnt_next); cudaFree(s->off); cudaFree(s->cursor);
-  cudaFree(s->list_small); cudaFree(s->list_big); cudaFree(s->wl); cudaFree(s->work); cudaFree(s->cell);
+  cudaFree(s->list_small); cudaFree(s->list_big); cudaFree(s->wl); cudaFree(s->work); cudaFree(s->cell); cudaFree(s->pcell);
   cudaFree(s->xi); cudaFree(s->inj); cudaFree(s->stage); cudaFree(s->faces); cudaFree(s->status);
   if (s->graph) cudaGraphExecDestroy(s->graph);
   for (auto& r : s->prof_recs) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
@@ -291,7 +292,9 @@ int mcpm_download_particles(mcpm_session* s, int64_t n, double* x1, double* x2, 
   int k = launch_convert_out(*s, n);
   int rc = after_launch(s, k, "download");
   if (rc) return rc;
-  if (x1) cudaMemcpyAsync(x1, s->stage, b, cudaMemcpyDeviceToHost, st);
+  // x1 is not tracked when it never changes (no x streaming, no ESMC):
+  // the caller's array is left as it is, like the reference's x1
+  if (x1 && s->need_x1) cudaMemcpyAsync(x1, s->stage, b, cudaMemcpyDeviceToHost, st);
   cudaMemcpyAsync(x2, s->stage + cap, b, cudaMemcpyDeviceToHost, st);
   cudaMemcpyAsync(U1, s->stage + 2 * cap, b, cudaMemcpyDeviceToHost, st);
   cudaMemcpyAsync(U2, s->stage + 3 * cap, b, cudaMemcpyDeviceToHost, st);

@@ -213,6 +213,10 @@ class Session:
     def download(self):
         n = self.N
         out = {k: np.empty(n) for k in ("x1", "x2", "U1", "U2", "U3")}
+        if self._keep[0] is not None:
+            out["x1"][:] = self._keep[0]  # kept when the device does not track x1
+        else:
+            out["x1"][:] = 0.0
         self._ck(self.lib.mcpm_download_particles(self.h, n, _dp(out["x1"]), _dp(out["x2"]), _dp(out["U1"]),
                                                   _dp(out["U2"]), _dp(out["U3"])), "download_particles")
         return out
