@@ -55,6 +55,26 @@ template <> __device__ __forceinline__ Normals3<float> normals3<float>(uint4 r) 
   return {a * c1, a * s1, b * cospif(2.0f * u01f(r.w))};
 }
 
+// ------------------------------------------------ constants in real type
+// The FP32 kernels read float copies prepared on the host, so that no
+// double->float conversion (an FP64-pipe instruction) runs per particle.
+template <typename real> struct KC {
+  real dx, dy, L0, L1, dt, sigma, m, kb, Tw[4], Uw[4];
+};
+template <typename real> __device__ __forceinline__ KC<real> make_kc(const DevConsts& k) {
+  KC<real> c;
+  if constexpr (sizeof(real) == 4) {
+    c.dx = k.f_dx; c.dy = k.f_dy; c.L0 = k.f_L0; c.L1 = k.f_L1; c.dt = k.f_dt;
+    c.sigma = k.f_sigma; c.m = k.f_m; c.kb = k.f_kb;
+    for (int i = 0; i < 4; ++i) { c.Tw[i] = k.f_Tw[i]; c.Uw[i] = k.f_Uw[i]; }
+  } else {
+    c.dx = k.dx; c.dy = k.dy; c.L0 = k.L0; c.L1 = k.L1; c.dt = k.dt;
+    c.sigma = k.sigma; c.m = k.m; c.kb = k.kb;
+    for (int i = 0; i < 4; ++i) { c.Tw[i] = k.Tw[i]; c.Uw[i] = k.Uw[i]; }
+  }
+  return c;
+}
+
 // --------------------------------------------------------------- laws
 // increase_collision_rate, src/Main_Functions.cpp:1906-1915
 __device__ __forceinline__ double ycoll(double n, double b) {
@@ -105,6 +125,11 @@ template <> struct Acc<double> {
   __device__ __forceinline__ double getr() const { return v; }
   __device__ __forceinline__ void shfl_xor(int m) { v += __shfl_xor_sync(0xffffffffu, v, m); }
   __device__ __forceinline__ void merge(const Acc& o) { v += o.v; }
+  __device__ __forceinline__ Acc xor_fetch(int m) const {
+    Acc o;
+    o.v = __shfl_xor_sync(0xffffffffu, v, m);
+    return o;
+  }
 };
 template <> struct Acc<float> {
   CSum c;
@@ -120,32 +145,52 @@ template <> struct Acc<float> {
     c = ccombine(c, o);
   }
   __device__ __forceinline__ void merge(const Acc& o) { c = ccombine(c, o.c); }
+  __device__ __forceinline__ Acc xor_fetch(int m) const {
+    Acc o;
+    o.c.hi = __shfl_xor_sync(0xffffffffu, c.hi, m);
+    o.c.lo = __shfl_xor_sync(0xffffffffu, c.lo, m);
+    return o;
+  }
 };
 
-// Reduce K accumulators over a tile of TILE threads (32 = one warp, or a
-// whole block).  Every thread of the tile gets the totals.  smem must hold
-// K * (TILE/32) Acc entries when TILE > 32.
-template <typename real, int K, int TILE>
-__device__ __forceinline__ void tile_reduce(Acc<real> (&a)[K], Acc<real>* smem) {
+// Warp reduction of K <= 32 accumulators by recursive halving: at each
+// butterfly stage a lane keeps half of its fields and ships the other half to
+// its partner, so a warp does 31 combines instead of 5K.  On return every
+// lane holds the warp total of one field, *field.
+template <typename real, int K>
+__device__ __forceinline__ Acc<real> warp_reduce_halving(Acc<real> (&a)[K], int* field) {
+  static_assert(K <= 32, "one accumulator per lane");
+  constexpr int P = K <= 1 ? 1 : K <= 2 ? 2 : K <= 4 ? 4 : K <= 8 ? 8 : K <= 16 ? 16 : 32;
+  const int lane = threadIdx.x & 31;
+  Acc<real> v[P];
 #pragma unroll
-  for (int m = 16; m >= 1; m >>= 1)
+  for (int q = 0; q < P; ++q) {
+    if (q < K) v[q] = a[q];
+    else v[q].zero();
+  }
+  int base = 0;
 #pragma unroll
-    for (int q = 0; q < K; ++q) a[q].shfl_xor(m);
-  if constexpr (TILE > 32) {
-    constexpr int W = TILE / 32;
-    int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    __syncthreads();
-    if (lane == 0)
+  for (int F = P, m = 16; m >= 1; m >>= 1) {
+    if (F > 1) {
+      const bool up = (lane & m) != 0;
+      const int h = F / 2;
 #pragma unroll
-      for (int q = 0; q < K; ++q) smem[q * W + warp] = a[q];
-    __syncthreads();
-#pragma unroll
-    for (int q = 0; q < K; ++q) {
-      Acc<real> t = smem[q * W];
-      for (int w = 1; w < W; ++w) t.merge(smem[q * W + w]);
-      a[q] = t;
+      for (int j = 0; j < P / 2; ++j) {
+        if (j < h) {
+          Acc<real> keep = up ? v[j + h] : v[j];
+          Acc<real> send = up ? v[j] : v[j + h];
+          keep.merge(send.xor_fetch(m));  // the partner ships its copy of my field
+          v[j] = keep;
+        }
+      }
+      if (up) base += h;
+      F = h;
+    } else {
+      v[0].shfl_xor(m);
     }
   }
+  *field = base;
+  return v[0];
 }
 
 // Reduce K <= 32 accumulators over a tile; returns to lane l (of warp 0
@@ -153,17 +198,11 @@ __device__ __forceinline__ void tile_reduce(Acc<real> (&a)[K], Acc<real>* smem) 
 // written by K lanes at once.
 template <typename real, int K, int TILE>
 __device__ __forceinline__ Acc<real> tile_reduce_lanes(Acc<real> (&a)[K], Acc<real>* smem) {
-  static_assert(K <= 32, "one accumulator per lane");
+  static_assert(K > 16 && K <= 32, "one accumulator per lane");
   const int lane = threadIdx.x & 31;
-#pragma unroll
-  for (int m = 16; m >= 1; m >>= 1)
-#pragma unroll
-    for (int q = 0; q < K; ++q) a[q].shfl_xor(m);
-  Acc<real> r;
-  r.zero();
-#pragma unroll
-  for (int q = 0; q < K; ++q)
-    if (lane == q) r = a[q];
+  int f;
+  Acc<real> r = warp_reduce_halving<real, K>(a, &f);
+  // for K > 16 every lane holds a distinct field f == lane
   if constexpr (TILE > 32) {
     constexpr int W = TILE / 32;
     const int warp = threadIdx.x >> 5;
@@ -177,6 +216,51 @@ __device__ __forceinline__ Acc<real> tile_reduce_lanes(Acc<real> (&a)[K], Acc<re
     }
   }
   return r;
+}
+
+// lane that holds field q after warp_reduce_halving with P fields
+template <int P> __device__ __forceinline__ int halving_lane(int q) {
+  int l = 0, m = 16;
+#pragma unroll
+  for (int h = P / 2; h >= 1; h >>= 1, m >>= 1)
+    if (q & h) l |= m;
+  return l;
+}
+
+// Reduce K accumulators over a tile of TILE threads (32 = one warp, or a
+// whole block); every thread of the tile gets all K totals.  smem must hold
+// K * (TILE/32) Acc entries when TILE > 32.
+template <typename real, int K, int TILE>
+__device__ __forceinline__ void tile_reduce(Acc<real> (&a)[K], Acc<real>* smem) {
+  constexpr int P = K <= 1 ? 1 : K <= 2 ? 2 : K <= 4 ? 4 : K <= 8 ? 8 : K <= 16 ? 16 : 32;
+  int f;
+  Acc<real> r = warp_reduce_halving<real, K>(a, &f);
+  if constexpr (TILE == 32) {
+#pragma unroll
+    for (int q = 0; q < K; ++q) {
+      Acc<real> t;
+      // fetch field q from the lane that holds it
+      if constexpr (sizeof(real) == 8) {
+        t.v = __shfl_sync(0xffffffffu, r.v, halving_lane<P>(q));
+      } else {
+        t.c.hi = __shfl_sync(0xffffffffu, r.c.hi, halving_lane<P>(q));
+        t.c.lo = __shfl_sync(0xffffffffu, r.c.lo, halving_lane<P>(q));
+      }
+      a[q] = t;
+    }
+  } else {
+    constexpr int W = TILE / 32;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    __syncthreads();
+    if ((lane & (32 / P - 1)) == 0 && f < K) smem[f * W + warp] = r;
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < K; ++q) {
+      Acc<real> t = smem[q * W];
+      for (int w = 1; w < W; ++w) t.merge(smem[q * W + w]);
+      a[q] = t;
+    }
+  }
 }
 
 __device__ __forceinline__ void raise_status(uint32_t* status, uint32_t bits) {

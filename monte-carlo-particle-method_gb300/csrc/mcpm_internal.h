@@ -61,6 +61,8 @@ struct DevConsts {
   double sigma, m, kb, n, Fn, T0, mu, visp, b, dt, phi, eqdist, ast, bst;
   double Tw[4], Uw[4];
   uint64_t seed;
+  // float copies for the FP32 kernels
+  float f_dx, f_dy, f_L0, f_L1, f_dt, f_sigma, f_m, f_kb, f_Tw[4], f_Uw[4];
 };
 
 // One set of device particle arrays (SoA).  real is float or double.
@@ -102,6 +104,7 @@ struct Session {
   int32_t* list_big = nullptr;
   int32_t* wl = nullptr;        // [WL_COUNT]
   int32_t* work = nullptr;      // [WK_COUNT]
+  int32_t* scan_blk = nullptr;  // [4][C/1024 + 1] block totals / bases of the scan
   double* cell = nullptr;       // [CF_DEV_COUNT][C]
   float* pcell = nullptr;       // [C][PF_STRIDE] packed FP32 record
   double* xi = nullptr;         // [3][cap] whitened normals, slot order

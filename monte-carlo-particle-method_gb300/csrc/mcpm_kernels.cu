@@ -36,19 +36,20 @@ template <typename real> static PT<real> pt(const PBuf& b) {
 // MCPM_ERR_OUT_OF_BOX (the reference exits); a particle on the far wall is
 // binned into the last cell.
 template <typename real>
-__device__ __forceinline__ int bin_one(real x1, real x2, int pid, int step, const DevConsts& k, uint32_t& bad) {
+__device__ __forceinline__ int bin_one(real x1, real x2, int pid, int step, const DevConsts& k, const KC<real>& kc,
+                                       uint32_t& bad) {
   int j = 0;
   if (k.dir0 == 1) {
-    j = (int)floor(x1 / (real)k.dx);
-    if (!(x1 >= (real)0 && x1 <= (real)k.L0)) bad |= MCPM_ERR_OUT_OF_BOX;
+    j = (int)floor(x1 / kc.dx);
+    if (!(x1 >= (real)0 && x1 <= kc.L0)) bad |= MCPM_ERR_OUT_OF_BOX;
   }
-  real dy = (real)k.dy;
+  const real dy = kc.dy;
   int kk = (int)floor(x2 / dy);
-  if (!(x2 >= (real)0 && x2 <= (real)k.L1)) bad |= MCPM_ERR_OUT_OF_BOX;
+  if (!(x2 >= (real)0 && x2 <= kc.L1)) bad |= MCPM_ERR_OUT_OF_BOX;
   if (kk > 0 && kk < k.N1 - 1) {
     if (fabs(x2 - dy * kk) < (real)1e-15 || fabs(x2 - dy * (kk + 1)) < (real)1e-15) {
       uint4 r = philox(k.seed, (uint32_t)pid, (uint32_t)step, RNG_BIN, 0u);
-      int sgn = (u01d(r.x) > 0.5) ? 1 : -1;
+      int sgn = (r.x >= 0x80000000u) ? 1 : -1;  // u01(r.x) > 0.5
       kk = (int)floor((x2 + (real)1e-14 * sgn) / dy);
     }
   }
@@ -61,13 +62,14 @@ template <typename real>
 __global__ void k_bin(PT<real> p, int64_t n, DevConsts k, int step, int32_t* key, int32_t* cnt_next,
                       uint32_t* status) {
   uint32_t bad = 0;
+  const KC<real> kc = make_kc<real>(k);
   for (int64_t i0 = (int64_t)blockIdx.x * blockDim.x; i0 < n; i0 += (int64_t)gridDim.x * blockDim.x) {
     int64_t i = i0 + threadIdx.x;
     bool act = i < n;
     int c = 0;
     if (act) {
       real x1 = p.x1 ? p.x1[i] : (real)0;
-      c = bin_one<real>(x1, p.x2[i], p.pid[i], step, k, bad);
+      c = bin_one<real>(x1, p.x2[i], p.pid[i], step, k, kc, bad);
       key[i] = c;
     }
     count_key(cnt_next, c, act);
@@ -76,66 +78,106 @@ __global__ void k_bin(PT<real> p, int64_t n, DevConsts k, int step, int32_t* key
 }
 
 // ================================================ scan + work lists
-// One block: counts of the new layout -> cnt, exclusive offsets, the two
-// work lists (cells with <= wcap particles, cells with more), max count;
-// resets the accumulation counters and cursors for the next step.
+// Counts of the new layout -> cnt, exclusive offsets, the two work lists
+// (cells with <= wcap particles / more), max count; resets the accumulation
+// counters and cursors for the next step.  Three passes over blocks of 1024
+// cells: block totals, scan of the totals, block-local scan + writes.
 constexpr int SCAN_T = 1024;
-__global__ void __launch_bounds__(SCAN_T) k_scan(int32_t* cnt_next, int32_t* cnt, int32_t* off, int32_t* cursor,
-                                                 int32_t* list_small, int32_t* list_big, int32_t* wl,
-                                                 int32_t* work, int C, int wcap) {
-  __shared__ int sh[3][SCAN_T / 32];
-  __shared__ int shmax[SCAN_T / 32];
-  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
-  const int items = (C + SCAN_T - 1) / SCAN_T;
-  const int b = t * items, e = min(C, b + items);
-  int s_cnt = 0, s_small = 0, s_big = 0, mx = 0;
-  for (int c = b; c < e; ++c) {
-    int v = cnt_next[c];
-    s_cnt += v;
-    if (v > wcap) s_big++; else s_small++;
-    mx = max(mx, v);
-  }
-  // inclusive warp scans of the three totals
-  int v0 = s_cnt, v1 = s_small, v2 = s_big;
+
+__device__ __forceinline__ void block_scan3(int& v0, int& v1, int& v2, int& t0, int& t1, int& t2, int (*sh)[32]) {
+  // inclusive scan of three ints over a 1024-thread block; t* = block totals
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
   for (int d = 1; d < 32; d <<= 1) {
     int a0 = __shfl_up_sync(FULL, v0, d), a1 = __shfl_up_sync(FULL, v1, d), a2 = __shfl_up_sync(FULL, v2, d);
     if (lane >= d) { v0 += a0; v1 += a1; v2 += a2; }
   }
-#pragma unroll
-  for (int d = 16; d >= 1; d >>= 1) mx = max(mx, __shfl_xor_sync(FULL, mx, d));
   if (lane == 31) { sh[0][warp] = v0; sh[1][warp] = v1; sh[2][warp] = v2; }
-  if (lane == 0) shmax[warp] = mx;
   __syncthreads();
   if (warp == 0) {
-    int w0 = sh[0][lane], w1 = sh[1][lane], w2 = sh[2][lane], m2 = shmax[lane];
+    int w0 = sh[0][lane], w1 = sh[1][lane], w2 = sh[2][lane];
 #pragma unroll
     for (int d = 1; d < 32; d <<= 1) {
       int a0 = __shfl_up_sync(FULL, w0, d), a1 = __shfl_up_sync(FULL, w1, d), a2 = __shfl_up_sync(FULL, w2, d);
       if (lane >= d) { w0 += a0; w1 += a1; w2 += a2; }
     }
-#pragma unroll
-    for (int d = 16; d >= 1; d >>= 1) m2 = max(m2, __shfl_xor_sync(FULL, m2, d));
     sh[0][lane] = w0; sh[1][lane] = w1; sh[2][lane] = w2;
-    if (lane == 31) {
-      wl[WL_N] = w0; wl[WL_NSMALL] = w1; wl[WL_NBIG] = w2; wl[WL_MAXCNT] = m2;
-    }
   }
   __syncthreads();
-  int base0 = (warp ? sh[0][warp - 1] : 0) + v0 - s_cnt;
-  int base1 = (warp ? sh[1][warp - 1] : 0) + v1 - s_small;
-  int base2 = (warp ? sh[2][warp - 1] : 0) + v2 - s_big;
-  for (int c = b; c < e; ++c) {
-    int v = cnt_next[c];
+  if (warp) { v0 += sh[0][warp - 1]; v1 += sh[1][warp - 1]; v2 += sh[2][warp - 1]; }
+  t0 = sh[0][31]; t1 = sh[1][31]; t2 = sh[2][31];
+}
+
+// pass 1: per-block totals (count, small cells, big cells, max count)
+__global__ void __launch_bounds__(SCAN_T) k_scan_blocks(const int32_t* cnt_next, int32_t* blk, int C, int wcap) {
+  __shared__ int sh[3][32];
+  __shared__ int shm[32];
+  const int c = blockIdx.x * SCAN_T + threadIdx.x;
+  const int v = c < C ? cnt_next[c] : 0;
+  int v0 = v, v1 = (c < C && v <= wcap) ? 1 : 0, v2 = (c < C && v > wcap) ? 1 : 0, t0, t1, t2;
+  int mx = v;
+#pragma unroll
+  for (int d = 16; d >= 1; d >>= 1) mx = max(mx, __shfl_xor_sync(FULL, mx, d));
+  if ((threadIdx.x & 31) == 0) shm[threadIdx.x >> 5] = mx;
+  block_scan3(v0, v1, v2, t0, t1, t2, sh);
+  if (threadIdx.x == 0) {
+    int m = shm[0];
+    for (int w = 1; w < 32; ++w) m = max(m, shm[w]);
+    blk[4 * blockIdx.x + 0] = t0; blk[4 * blockIdx.x + 1] = t1; blk[4 * blockIdx.x + 2] = t2;
+    blk[4 * blockIdx.x + 3] = m;
+  }
+}
+
+// pass 2: exclusive scan of the block totals (one block), list lengths
+__global__ void __launch_bounds__(SCAN_T) k_scan_totals(int32_t* blk, int nblk, int32_t* wl, int32_t* work) {
+  __shared__ int sh[3][32];
+  int carry0 = 0, carry1 = 0, carry2 = 0, mx = 0;
+  for (int base = 0; base < nblk; base += SCAN_T) {
+    const int b = base + threadIdx.x;
+    int v0 = 0, v1 = 0, v2 = 0, m = 0, t0, t1, t2;
+    if (b < nblk) { v0 = blk[4 * b]; v1 = blk[4 * b + 1]; v2 = blk[4 * b + 2]; m = blk[4 * b + 3]; }
+    const int e0 = v0, e1 = v1, e2 = v2;
+    block_scan3(v0, v1, v2, t0, t1, t2, sh);
+    if (b < nblk) {  // exclusive bases in place of the totals
+      blk[4 * b] = carry0 + v0 - e0; blk[4 * b + 1] = carry1 + v1 - e1; blk[4 * b + 2] = carry2 + v2 - e2;
+    }
+#pragma unroll
+    for (int d = 16; d >= 1; d >>= 1) m = max(m, __shfl_xor_sync(FULL, m, d));
+    mx = max(mx, m);
+    carry0 += t0; carry1 += t1; carry2 += t2;
+    __syncthreads();
+  }
+  __shared__ int shm[32];
+  if ((threadIdx.x & 31) == 0) shm[threadIdx.x >> 5] = mx;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int m = shm[0];
+    for (int w = 1; w < 32; ++w) m = max(m, shm[w]);
+    wl[WL_N] = carry0; wl[WL_NSMALL] = carry1; wl[WL_NBIG] = carry2; wl[WL_MAXCNT] = m;
+  }
+  if (threadIdx.x < WK_COUNT) work[threadIdx.x] = 0;
+}
+
+// pass 3: block-local scan plus the block base; writes the layout
+__global__ void __launch_bounds__(SCAN_T) k_scan_write(int32_t* cnt_next, int32_t* cnt, int32_t* off,
+                                                       int32_t* cursor, int32_t* list_small, int32_t* list_big,
+                                                       const int32_t* blk, int C, int wcap) {
+  __shared__ int sh[3][32];
+  const int c = blockIdx.x * SCAN_T + threadIdx.x;
+  const int v = c < C ? cnt_next[c] : 0;
+  const bool small = c < C && v <= wcap, big = c < C && v > wcap;
+  int v0 = v, v1 = small ? 1 : 0, v2 = big ? 1 : 0, t0, t1, t2;
+  block_scan3(v0, v1, v2, t0, t1, t2, sh);
+  if (c < C) {
+    const int o = blk[4 * blockIdx.x] + v0 - v;
     cnt[c] = v;
-    off[c] = base0;
-    base0 += v;
-    if (v > wcap) list_big[base2++] = c; else list_small[base1++] = c;
+    off[c] = o;
+    if (small) list_small[blk[4 * blockIdx.x + 1] + v1 - 1] = c;
+    if (big) list_big[blk[4 * blockIdx.x + 2] + v2 - 1] = c;
     cnt_next[c] = 0;
     cursor[c] = 0;
+    if (c == C - 1) off[C] = o + v;
   }
-  if (t == SCAN_T - 1) off[C] = base0;
-  if (t < WK_COUNT) work[t] = 0;
 }
 
 // ============================================================ scatter
@@ -343,12 +385,47 @@ __device__ void gauss_jordan(double* A, double* R, double* x) {
   }
 }
 
+// Gauss-Jordan for the FP32 path's per-cell solve (still FP64): partial
+// pivoting on |A[j][i]|, reciprocal of the pivot, FMA elimination of the
+// columns right of the pivot only.  Same precision class as the reference's
+// solve at about a third of its FP64 instruction count.
+template <int n>
+__device__ void gauss_jordan_fast(double* A, double* R, double* x) {
+  const unsigned long long INF = 0x7FF0000000000000ull;
+  double rinv[n];
+  for (int i = 0; i < n; ++i) {
+    int k = i;
+    unsigned long long b = absbits(A[i * n + i]);
+    for (int j = i + 1; j < n; ++j) {
+      unsigned long long v = absbits(A[j * n + i]);
+      if (v <= INF && v > b) { b = v; k = j; }
+    }
+    if (k != i) {
+      for (int j = i; j < n; ++j) { double t = A[i * n + j]; A[i * n + j] = A[k * n + j]; A[k * n + j] = t; }
+      double t = R[i]; R[i] = R[k]; R[k] = t;
+    }
+    const double r = 1.0 / A[i * n + i];
+    rinv[i] = r;
+    for (int j = i + 1; j < n; ++j) {
+      const double F = r * A[j * n + i];
+      for (int kk = i + 1; kk < n; ++kk) A[j * n + kk] = fma(-F, A[i * n + kk], A[j * n + kk]);
+      R[j] = fma(-F, R[i], R[j]);
+    }
+  }
+  for (int i = n - 1; i >= 0; --i) {
+    double a = R[i];
+    for (int j = i + 1; j < n; ++j) a = fma(-A[i * n + j], x[j], a);
+    x[i] = a * rinv[i];
+  }
+}
+
 // One thread per cell: Lambda (src/Main_Functions.cpp:2718-2728),
 // alpha/beta (src/Fokker_Planck.cpp:200-587; its 12x12 system is three
 // uncoupled 4x4 blocks -- unknowns (alpha_3b..3b+2, beta_b) -- and Gauss_Jordan
 // on the 12x12 performs exactly the arithmetic of the three 4x4 solves),
 // c/gamma (src/Fokker_Planck.cpp:590-804, 9x9), phi (:2734-2746) and the
 // Velocity_FP_parallel constants A1..A3 (src/Fokker_Planck.cpp:1099-1112).
+template <bool EXACT>
 __global__ void __launch_bounds__(128) k_solve(DevConsts k, double* cell, float* pcell, int with_alpha,
                                                int fp_model, uint32_t* status) {
   const int C = k.C;
@@ -368,12 +445,22 @@ __global__ void __launch_bounds__(128) k_solve(DevConsts k, double* cell, float*
   for (int j = 0; j < 3; ++j) M5[j] = R(CFI_RAW + 25 + j);
   DM2 = R(CFI_RAW + 28);
   if (ncnt > 0) {
-    for (int j = 0; j < 6; ++j) P[j] = P[j] / weight;
-    for (int j = 0; j < 10; ++j) M3[j] = M3[j] / weight;
-    for (int j = 0; j < 6; ++j) M4[j] = M4[j] / weight;
-    for (int j = 0; j < 3; ++j) M5[j] = M5[j] / weight;
-    for (int j = 0; j < 3; ++j) Mp[j] = Mp[j] / weight;
-    DM2 = DM2 / weight;
+    if (EXACT) {
+      for (int j = 0; j < 6; ++j) P[j] = P[j] / weight;
+      for (int j = 0; j < 10; ++j) M3[j] = M3[j] / weight;
+      for (int j = 0; j < 6; ++j) M4[j] = M4[j] / weight;
+      for (int j = 0; j < 3; ++j) M5[j] = M5[j] / weight;
+      for (int j = 0; j < 3; ++j) Mp[j] = Mp[j] / weight;
+      DM2 = DM2 / weight;
+    } else {
+      const double rw = 1.0 / weight;
+      for (int j = 0; j < 6; ++j) P[j] *= rw;
+      for (int j = 0; j < 10; ++j) M3[j] *= rw;
+      for (int j = 0; j < 6; ++j) M4[j] *= rw;
+      for (int j = 0; j < 3; ++j) M5[j] *= rw;
+      for (int j = 0; j < 3; ++j) Mp[j] *= rw;
+      DM2 *= rw;
+    }
     DM4 = M4[0] + M4[3] + M4[5];
     Q[0] = M3[0] + M3[3] + M3[5];
     Q[1] = M3[1] + M3[6] + M3[8];
@@ -389,7 +476,13 @@ __global__ void __launch_bounds__(128) k_solve(DevConsts k, double* cell, float*
   W(MCPM_CF_DM4, DM4);
   const double T = k.m * DM2 / (3.0 * k.kb);
   const double n = 1 * k.Fn * weight / cell_volume(c, k);
-  const double Ycell = ycoll(n, k.b);
+  double Ycell;
+  if (EXACT) {
+    Ycell = ycoll(n, k.b);
+  } else {
+    const double nb = n * k.b;
+    Ycell = 1.0 + nb * (0.625 + nb * (0.2869 + 0.115 * nb));
+  }
   W(MCPM_CF_T, T);
   W(MCPM_CF_N, n);
   W(CFI_Y, Ycell);
@@ -406,7 +499,8 @@ __global__ void __launch_bounds__(128) k_solve(DevConsts k, double* cell, float*
     double L = (P[0] - DM2 / 3.0) * ((P[3] - DM2 / 3.0) * (P[5] - DM2 / 3.0) - P[4] * P[4]);
     L = L - P[1] * (P[1] * (P[5] - DM2 / 3.0) - P[4] * P[2]);
     L = L + P[2] * (P[1] * P[4] - P[2] * (P[3] - DM2 / 3.0));
-    L = -L / (tau * pow(DM2, 4.0));
+    const double dm4 = EXACT ? pow(DM2, 4.0) : (DM2 * DM2) * (DM2 * DM2);
+    L = -L / (tau * dm4);
     Lam = L;
     W(MCPM_CF_LAMBDA, Lam);
   }
@@ -468,7 +562,8 @@ __global__ void __launch_bounds__(128) k_solve(DevConsts k, double* cell, float*
           A[8] = P[2]; A[9] = P[4]; A[10] = P[5]; A[11] = m3b[blk];
           A[12] = ma; A[13] = mb; A[14] = mc; A[15] = d;
           r4[0] = rhs[3 * blk]; r4[1] = rhs[3 * blk + 1]; r4[2] = rhs[3 * blk + 2]; r4[3] = rhs[9 + blk];
-          gauss_jordan<4>(A, r4, x4);
+          if (EXACT) gauss_jordan<4>(A, r4, x4);
+          else gauss_jordan_fast<4>(A, r4, x4);
           al[3 * blk] = x4[0]; al[3 * blk + 1] = x4[1]; al[3 * blk + 2] = x4[2]; be[blk] = x4[3];
         }
         for (int j = 0; j < 9; ++j) if (al[j] != al[j]) bad |= MCPM_ERR_NAN;
@@ -522,7 +617,8 @@ __global__ void __launch_bounds__(128) k_solve(DevConsts k, double* cell, float*
       rhs[6] += Lam * (-3.0 * M5[0] + DM2 * Q[0] + 2.0 * (P[0] * Q[0] + P[1] * Q[1] + P[2] * Q[2]));
       rhs[7] += Lam * (-3.0 * M5[1] + DM2 * Q[1] + 2.0 * (P[1] * Q[0] + P[3] * Q[1] + P[4] * Q[2]));
       rhs[8] += Lam * (-3.0 * M5[2] + DM2 * Q[2] + 2.0 * (P[2] * Q[0] + P[4] * Q[1] + P[5] * Q[2]));
-      gauss_jordan<9>(A, rhs, x);
+      if (EXACT) gauss_jordan<9>(A, rhs, x);
+      else gauss_jordan_fast<9>(A, rhs, x);
     }
     for (int j = 0; j < 6; ++j) W(MCPM_CF_C + j, x[j]);
     for (int j = 0; j < 3; ++j) W(MCPM_CF_GAMMA + j, x[6 + j]);
@@ -532,9 +628,16 @@ __global__ void __launch_bounds__(128) k_solve(DevConsts k, double* cell, float*
       double tau = 2.0 * mu / (n * k.kb * T);
       double Y = (k.model == MCPM_MODEL_FP_DENSE) ? Ycell : 1.0;
       tau = tau / Y;
-      W(CFI_A1, exp(-k.dt / tau));
-      W(CFI_A3, sqrt((1.0 - exp(-2.0 * k.dt / tau)) * k.kb * T / (1.0 * k.m)));
-      W(CFI_A2, (1.0 - exp(-k.dt / tau)) * tau);
+      if (EXACT) {
+        W(CFI_A1, exp(-k.dt / tau));
+        W(CFI_A3, sqrt((1.0 - exp(-2.0 * k.dt / tau)) * k.kb * T / (1.0 * k.m)));
+        W(CFI_A2, (1.0 - exp(-k.dt / tau)) * tau);
+      } else {
+        const double e1 = exp(-k.dt / tau);  // exp(-2 dt/tau) = e1^2
+        W(CFI_A1, e1);
+        W(CFI_A3, sqrt((1.0 - e1 * e1) * k.kb * T / k.m));
+        W(CFI_A2, (1.0 - e1) * tau);
+      }
     }
   }
   const double eq3 = 3.0 * k.kb * T / k.m;
@@ -573,8 +676,8 @@ template <typename real> struct PState {
 
 // BC_specular_reflection, src/Main_Functions.cpp:6399-6525
 template <typename real>
-__device__ __forceinline__ void bc_specular(PState<real>& s, const DevConsts& k, uint32_t& bad) {
-  const real Tol1 = (real)1e-16, Tol2 = (real)-1e-16, L0 = (real)k.L0, L1 = (real)k.L1;
+__device__ __forceinline__ void bc_specular(PState<real>& s, const DevConsts& k, const KC<real>& kc, uint32_t& bad) {
+  const real Tol1 = (real)1e-16, Tol2 = (real)-1e-16, L0 = kc.L0, L1 = kc.L1;
   int it = 0;
   for (;;) {
     if (k.dir0 == 1) {
@@ -594,9 +697,9 @@ __device__ __forceinline__ void bc_specular(PState<real>& s, const DevConsts& k,
 }
 
 template <typename real>
-__device__ __forceinline__ void bc_periodic(PState<real>& s, const DevConsts& k) {
-  if (k.dir0 == 1) s.x1 = s.x1 - (real)k.L0 * floor(s.x1 / (real)k.L0);
-  if (k.dir1 == 1) s.x2 = s.x2 - (real)k.L1 * floor(s.x2 / (real)k.L1);
+__device__ __forceinline__ void bc_periodic(PState<real>& s, const DevConsts& k, const KC<real>& kc) {
+  if (k.dir0 == 1) s.x1 = s.x1 - kc.L0 * floor(s.x1 / kc.L0);
+  if (k.dir1 == 1) s.x2 = s.x2 - kc.L1 * floor(s.x2 / kc.L1);
 }
 
 // one diffuse re-emission draw: Rayleigh factor + two normals
@@ -643,9 +746,10 @@ __device__ __forceinline__ real isect_y(real y, real xo, real yo, real xn, real 
 
 // BC_thermal_wall_3D, src/Main_Functions.cpp:4917-5250, in 2-D
 template <typename real>
-__device__ void bc_thermal_wall(PState<real>& s, int call, int pid, int step, const DevConsts& k, uint32_t& bad) {
-  const real eps = (real)1e-15, L0 = (real)k.L0, L1 = (real)k.L1, sg = (real)k.sigma, DT = (real)k.dt;
-  const real mm = (real)k.m, kb = (real)k.kb;
+__device__ void bc_thermal_wall(PState<real>& s, int call, int pid, int step, const DevConsts& k, const KC<real>& kc,
+                                uint32_t& bad) {
+  const real eps = (real)1e-15, L0 = kc.L0, L1 = kc.L1, sg = kc.sigma, DT = kc.dt;
+  const real mm = kc.m, kb = kc.kb;
   real dt = DT;
   int it = 0;
   const real Ue0 = fabs(s.x1 - s.x1o) / DT, Ue1 = fabs(s.x2 - s.x2o) / DT;
@@ -664,7 +768,7 @@ __device__ void bc_thermal_wall(PState<real>& s, int call, int pid, int step, co
     else if (s.x2 > L1 - sg - eps) wall = 1;
     else if (s.x2 < sg + eps) wall = 0;
     if (wall >= 0) {
-      const real Tw = (real)k.Tw[wall], Uw = (real)k.Uw[wall];
+      const real Tw = kc.Tw[wall], Uw = kc.Uw[wall];
       if (wall >= 2) {  // x walls
         xw = (wall == 3) ? L0 - eps : eps;
         if (fabs(s.x1o - s.x1) > (real)1e-15) yw = isect_x<real>(xw, s.x1o, s.x2o, s.x1, s.x2);
@@ -713,9 +817,10 @@ __device__ void bc_thermal_wall(PState<real>& s, int call, int pid, int step, co
 
 // BC_wall, src/Main_Functions.cpp:4816-4914 (1-D: diffuse y = 0, specular y = Len1)
 template <typename real>
-__device__ void bc_wall(PState<real>& s, int call, int pid, int step, const DevConsts& k, uint32_t& bad) {
-  const real eps = (real)1e-15, L1 = (real)k.L1, DT = (real)k.dt, mm = (real)k.m, kb = (real)k.kb;
-  const real Tw = (real)k.Tw[0], Uw = (real)k.Uw[0];
+__device__ void bc_wall(PState<real>& s, int call, int pid, int step, const DevConsts& k, const KC<real>& kc,
+                        uint32_t& bad) {
+  const real eps = (real)1e-15, L1 = kc.L1, DT = kc.dt, mm = kc.m, kb = kc.kb;
+  const real Tw = kc.Tw[0], Uw = kc.Uw[0];
   real dt = DT;
   int it = 0;
   const real Ue1 = fabs(s.x2 - s.x2o) / DT;
@@ -752,12 +857,12 @@ __device__ void bc_wall(PState<real>& s, int call, int pid, int step, const DevC
 // apply_BC, src/Main_Functions.cpp:1451-1492
 template <typename real>
 __device__ __forceinline__ void apply_bc(PState<real>& s, int call, int pid, int step, const DevConsts& k,
-                                         uint32_t& bad) {
+                                         const KC<real>& kc, uint32_t& bad) {
   switch (k.problem) {
-    case MCPM_PROBLEM_CLOSED_BOX: bc_specular<real>(s, k, bad); break;
-    case MCPM_PROBLEM_COUETTE: bc_thermal_wall<real>(s, call, pid, step, k, bad); break;
-    case MCPM_PROBLEM_WALL: bc_wall<real>(s, call, pid, step, k, bad); break;
-    case MCPM_PROBLEM_PERIODIC: bc_periodic<real>(s, k); break;
+    case MCPM_PROBLEM_CLOSED_BOX: bc_specular<real>(s, k, kc, bad); break;
+    case MCPM_PROBLEM_COUETTE: bc_thermal_wall<real>(s, call, pid, step, k, kc, bad); break;
+    case MCPM_PROBLEM_WALL: bc_wall<real>(s, call, pid, step, k, kc, bad); break;
+    case MCPM_PROBLEM_PERIODIC: bc_periodic<real>(s, k, kc); break;
     default: break;
   }
 }
@@ -843,13 +948,19 @@ template <typename real> __device__ __forceinline__ real crms(const Acc<real>& s
 // DFP_extra_streaming (src/Fokker_Planck.cpp:904-946) + apply_BC /
 // store_old_positions / stream_particles (src/main.cpp:478-514) + the binning
 // of the next cell_update, for one cell, by a tile of TILE threads.
-// xs stages the cell's normals in shared memory when the cell fits.
+// xs stages three values per particle in shared memory when the cell fits:
+// the raw normals, then the new peculiar velocities M'.
+// The FP64 path follows the reference's two-pass centring/normalisation of
+// the normals; the FP32 path takes the per-cell mean and RMS from one pass
+// of compensated sums of z and z^2.
 template <typename real, int TILE>
 __device__ void update_cell(int c, const UpdArgs<real>& a, real* xs, int xcap, Acc<real>* red) {
+  constexpr bool F32 = sizeof(real) == 4;
   const int t = (TILE == 32) ? (threadIdx.x & 31) : threadIdx.x;
   const int64_t s0 = a.off[c];
   const int n = a.cnt[c];
   const DevConsts& k = a.k;
+  const KC<real> kc = make_kc<real>(k);
   const uint32_t st = a.stages;
   const bool rng = st & ST_RNG, fp = st & ST_FP, load_xi = st & ST_LOAD_XI, store_xi = st & ST_STORE_XI;
   const bool staged = rng && n <= xcap;
@@ -862,44 +973,51 @@ __device__ void update_cell(int c, const UpdArgs<real>& a, real* xs, int xcap, A
   f1acc.zero();
   // ---- pass A: draws, their per-cell sums, sum |M'|^2
   if (rng || fp) {
-    Acc<real> s4[4];
+    constexpr int KA = F32 ? 7 : 4;
+    Acc<real> sa[KA];
 #pragma unroll
-    for (int q = 0; q < 4; ++q) s4[q].zero();
+    for (int q = 0; q < KA; ++q) sa[q].zero();
     for (int i = t; i < n; i += TILE) {
       int64_t p = s0 + i;
       if (rng) {
         real z0, z1, z2;
         raw_normals(a, p, z0, z1, z2);
         if (staged) { xs[3 * i] = z0; xs[3 * i + 1] = z1; xs[3 * i + 2] = z2; }
-        s4[0].add(z0); s4[1].add(z1); s4[2].add(z2);
+        sa[0].add(z0); sa[1].add(z1); sa[2].add(z2);
+        if constexpr (F32) { sa[4].add(z0 * z0); sa[5].add(z1 * z1); sa[6].add(z2 * z2); }
       }
       if (fp) {
         real m1 = P.U1[p] - Us0, m2 = P.U2[p] - Us1, m3 = P.U3[p] - Us2;
-        s4[3].add(m1 * m1 + m2 * m2 + m3 * m3);
+        sa[3].add(m1 * m1 + m2 * m2 + m3 * m3);
       }
     }
-    tile_reduce<real, 4, TILE>(s4, red);
-    f1acc = s4[3];
+    tile_reduce<real, KA, TILE>(sa, red);
+    f1acc = sa[3];
     if (rng) {
-      mean0 = cmean(s4[0], n); mean1 = cmean(s4[1], n); mean2 = cmean(s4[2], n);
-      // ---- pass B: per-cell RMS of the centred draws
-      Acc<real> s3[3];
+      mean0 = cmean(sa[0], n); mean1 = cmean(sa[1], n); mean2 = cmean(sa[2], n);
+      if constexpr (F32) {
+        const float rn = 1.0f / (float)n;
+        rms0 = sqrtf(fmaxf(sa[4].getr() * rn - mean0 * mean0, 0.f));
+        rms1 = sqrtf(fmaxf(sa[5].getr() * rn - mean1 * mean1, 0.f));
+        rms2 = sqrtf(fmaxf(sa[6].getr() * rn - mean2 * mean2, 0.f));
+      } else {
+        // ---- pass B: per-cell RMS of the centred draws
+        Acc<real> s3[3];
 #pragma unroll
-      for (int q = 0; q < 3; ++q) s3[q].zero();
-      for (int i = t; i < n; i += TILE) {
-        real z0, z1, z2;
-        if (staged) { z0 = xs[3 * i]; z1 = xs[3 * i + 1]; z2 = xs[3 * i + 2]; }
-        else raw_normals(a, s0 + i, z0, z1, z2);
-        real d0 = z0 - mean0, d1 = z1 - mean1, d2 = z2 - mean2;
-        s3[0].add(d0 * d0); s3[1].add(d1 * d1); s3[2].add(d2 * d2);
+        for (int q = 0; q < 3; ++q) s3[q].zero();
+        for (int i = t; i < n; i += TILE) {
+          real z0, z1, z2;
+          if (staged) { z0 = xs[3 * i]; z1 = xs[3 * i + 1]; z2 = xs[3 * i + 2]; }
+          else raw_normals(a, s0 + i, z0, z1, z2);
+          real d0 = z0 - mean0, d1 = z1 - mean1, d2 = z2 - mean2;
+          s3[0].add(d0 * d0); s3[1].add(d1 * d1); s3[2].add(d2 * d2);
+        }
+        tile_reduce<real, 3, TILE>(s3, red);
+        rms0 = crms(s3[0], n); rms1 = crms(s3[1], n); rms2 = crms(s3[2], n);
       }
-      tile_reduce<real, 3, TILE>(s3, red);
-      rms0 = crms(s3[0], n); rms1 = crms(s3[1], n); rms2 = crms(s3[2], n);
     }
   }
-  // whitened normal of the i-th particle of the cell (after pass C the
-  // staged values are already whitened and whiten == false)
-  bool whiten = true;
+  // whitened normal of the i-th particle of the cell
   auto xiw = [&](int i, real& z0, real& z1, real& z2) {
     int64_t p = s0 + i;
     if (load_xi) {
@@ -908,7 +1026,7 @@ __device__ void update_cell(int c, const UpdArgs<real>& a, real* xs, int xcap, A
     }
     if (staged) { z0 = xs[3 * i]; z1 = xs[3 * i + 1]; z2 = xs[3 * i + 2]; }
     else raw_normals(a, p, z0, z1, z2);
-    if (whiten && n > 1) {
+    if (n > 1) {
       z0 = (z0 - mean0) / rms0; z1 = (z1 - mean1) / rms1; z2 = (z2 - mean2) / rms2;
     }
   };
@@ -936,20 +1054,17 @@ __device__ void update_cell(int c, const UpdArgs<real>& a, real* xs, int xcap, A
       m1 = 0; m2 = 0; m3 = 0;
     }
   };
-  // ---- pass C: whitened normals (staged / stored) and sum |M'_new|^2
   uint32_t bad = 0;
-  if (rng && (staged || store_xi)) {
+  // ---- pass C (split mode): keep the whitened normals for velocity_update
+  if (rng && store_xi) {
     for (int i = t; i < n; i += TILE) {
       real z0, z1, z2;
       xiw(i, z0, z1, z2);
-      if (store_xi) {
-        int64_t p = s0 + i;
-        a.xi[p] = (double)z0; a.xi[a.cap + p] = (double)z1; a.xi[2 * a.cap + p] = (double)z2;
-      }
-      if (staged) { xs[3 * i] = z0; xs[3 * i + 1] = z1; xs[3 * i + 2] = z2; }
+      int64_t p = s0 + i;
+      a.xi[p] = (double)z0; a.xi[a.cap + p] = (double)z1; a.xi[2 * a.cap + p] = (double)z2;
     }
-    if (staged) whiten = false;
   }
+  // ---- pass C: M'_new, sum |M'_new|^2; M'_new replaces the staged normals
   Acc<real> f2acc;
   f2acc.zero();
   if (fp) {
@@ -960,6 +1075,7 @@ __device__ void update_cell(int c, const UpdArgs<real>& a, real* xs, int xcap, A
       mnew(i, m1, m2, m3);
       if (m2 != m2) bad |= MCPM_ERR_NAN;
       f2[0].add(m1 * m1 + m2 * m2 + m3 * m3);
+      if (staged) { xs[3 * i] = m1; xs[3 * i + 1] = m2; xs[3 * i + 2] = m3; }
     }
     tile_reduce<real, 1, TILE>(f2, red);
     f2acc = f2[0];
@@ -972,11 +1088,11 @@ __device__ void update_cell(int c, const UpdArgs<real>& a, real* xs, int xcap, A
   // ---- pass D: final velocities, then the position pipeline
   real scale = (real)1;
   if (fp && n > 1) {
-    if constexpr (sizeof(real) == 4) scale = sqrtf(fabsf(f1acc.getr() / f2acc.getr()));
+    if constexpr (F32) scale = sqrtf(fabsf(f1acc.getr() / f2acc.getr()));
     else scale = sqrt(fabs(f1acc.get() / f2acc.get()));
   }
   const real F2dt = (st & ST_LR) ? K.f2dt : (real)0;
-  const real dtr = (real)k.dt;
+  const real dtr = kc.dt;
   const int iters = (n + TILE - 1) / TILE;
   for (int r = 0; r < iters; ++r) {
     const int i = r * TILE + t;
@@ -994,7 +1110,8 @@ __device__ void update_cell(int c, const UpdArgs<real>& a, real* xs, int xcap, A
       if (fp) {
         if (n > 1) {
           real m1, m2, m3;
-          mnew(i, m1, m2, m3);
+          if (staged) { m1 = xs[3 * i]; m2 = xs[3 * i + 1]; m3 = xs[3 * i + 2]; }
+          else mnew(i, m1, m2, m3);
           s.u1 = m1 * scale + Us0; s.u2 = m2 * scale + Us1; s.u3 = m3 * scale + Us2;
         } else {
           s.u1 = Us0; s.u2 = Us1; s.u3 = Us2;
@@ -1003,7 +1120,7 @@ __device__ void update_cell(int c, const UpdArgs<real>& a, real* xs, int xcap, A
       if (st & ST_LR) s.u2 = s.u2 + F2dt;
       if (st & ST_DFP) {
         real e = (s.u1 - Us0) * (s.u1 - Us0) + (s.u2 - Us1) * (s.u2 - Us1) + (s.u3 - Us2) * (s.u3 - Us2);
-        if constexpr (sizeof(real) == 8) {
+        if constexpr (!F32) {
           if (k.dir0 == 1) {
             s.x1 = s.x1 + dtr * ((s.u1 - Us0) * K.al[0] + (s.u2 - Us1) * K.al[1] + (s.u3 - Us2) * K.al[2] +
                                  K.be0 * (e - K.eq)) +
@@ -1031,21 +1148,21 @@ __device__ void update_cell(int c, const UpdArgs<real>& a, real* xs, int xcap, A
           }
         }
       }
-      if (st & ST_BC1) apply_bc<real>(s, a.bc_call_base + 0, pid, a.step, k, bad);
+      if (st & ST_BC1) apply_bc<real>(s, a.bc_call_base + 0, pid, a.step, k, kc, bad);
       if (st & ST_OLD) { s.x1o = s.x1; s.x2o = s.x2; }
       if (st & ST_STREAM) {
         if (k.dir0 == 1) s.x1 = s.x1 + dtr * s.u1;
         if (k.dir1 == 1) s.x2 = s.x2 + dtr * s.u2;
       }
-      if (st & ST_BC2) apply_bc<real>(s, a.bc_call_base + 1, pid, a.step, k, bad);
-      if (st & ST_BC3) apply_bc<real>(s, a.bc_call_base + 2, pid, a.step, k, bad);
+      if (st & ST_BC2) apply_bc<real>(s, a.bc_call_base + 1, pid, a.step, k, kc, bad);
+      if (st & ST_BC3) apply_bc<real>(s, a.bc_call_base + 2, pid, a.step, k, kc, bad);
       P.U1[p] = s.u1; P.U2[p] = s.u2; P.U3[p] = s.u3;
       if (P.x1) P.x1[p] = s.x1;
       P.x2[p] = s.x2;
       if (P.x1o) P.x1o[p] = s.x1o;
       if (P.x2o) P.x2o[p] = s.x2o;
       if (st & ST_KEY) {
-        key = bin_one<real>(s.x1, s.x2, pid, a.bin_step, k, bad);
+        key = bin_one<real>(s.x1, s.x2, pid, a.bin_step, k, kc, bad);
         a.key_out[p] = key;
       }
     }
@@ -1057,7 +1174,7 @@ __device__ void update_cell(int c, const UpdArgs<real>& a, real* xs, int xcap, A
 template <typename real>
 __global__ void __launch_bounds__(256) k_update(UpdArgs<real> a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  __shared__ Acc<real> red[4 * 8];
+  __shared__ Acc<real> red[8 * 8];
   real* xs = reinterpret_cast<real*>(smem_raw);
   const int warp = threadIdx.x >> 5;
   schedule_cells(
@@ -1111,9 +1228,12 @@ template <typename real> static int bin_impl(Session& s, int bin_step) {
 int launch_bin(Session& s, int bin_step) { return s.prec == MCPM_FP32 ? bin_impl<float>(s, bin_step) : bin_impl<double>(s, bin_step); }
 
 int launch_scan(Session& s) {
-  k_scan<<<1, SCAN_T, 0, s.stream>>>(s.cnt_next, s.cnt, s.off, s.cursor, s.list_small, s.list_big, s.wl, s.work,
-                                      s.C, s.tune.wcap);
-  return 1;
+  const int nblk = (s.C + SCAN_T - 1) / SCAN_T;
+  k_scan_blocks<<<nblk, SCAN_T, 0, s.stream>>>(s.cnt_next, s.scan_blk, s.C, s.tune.wcap);
+  k_scan_totals<<<1, SCAN_T, 0, s.stream>>>(s.scan_blk, nblk, s.wl, s.work);
+  k_scan_write<<<nblk, SCAN_T, 0, s.stream>>>(s.cnt_next, s.cnt, s.off, s.cursor, s.list_small, s.list_big,
+                                               s.scan_blk, s.C, s.tune.wcap);
+  return 3;
 }
 
 template <typename real> static int scatter_impl(Session& s) {
@@ -1134,8 +1254,12 @@ int launch_moments(Session& s) { return s.prec == MCPM_FP32 ? moments_impl<float
 
 int launch_solve(Session& s, int with_alpha) {
   int fp = (s.cfg.model == MCPM_MODEL_FP_DENSE || s.cfg.model == MCPM_MODEL_FP_IDEAL_GAS) ? 1 : 0;
-  k_solve<<<(s.C + 127) / 128, 128, 0, s.stream>>>(s.k, s.cell, s.prec == MCPM_FP32 ? s.pcell : nullptr,
-                                                    with_alpha, fp, s.status);
+  // the FP64 path reproduces the reference's solve exactly; the FP32 path
+  // runs the leaner FP64 variant
+  if (s.prec == MCPM_FP32)
+    k_solve<false><<<(s.C + 127) / 128, 128, 0, s.stream>>>(s.k, s.cell, s.pcell, with_alpha, fp, s.status);
+  else
+    k_solve<true><<<(s.C + 127) / 128, 128, 0, s.stream>>>(s.k, s.cell, nullptr, with_alpha, fp, s.status);
   return 1;
 }
 

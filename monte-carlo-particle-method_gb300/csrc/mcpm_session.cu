@@ -146,6 +146,9 @@ int mcpm_session_create(const mcpm_config* cfg, mcpm_session** out) {
   k.b = c.b; k.dt = c.dt; k.phi = c.phi; k.eqdist = c.eqdist; k.ast = c.ast; k.bst = c.bst;
   for (int i = 0; i < 4; ++i) { k.Tw[i] = c.T_wall[i]; k.Uw[i] = c.U_wall[i]; }
   k.seed = c.seed;
+  k.f_dx = (float)k.dx; k.f_dy = (float)k.dy; k.f_L0 = (float)k.L0; k.f_L1 = (float)k.L1;
+  k.f_dt = (float)k.dt; k.f_sigma = (float)k.sigma; k.f_m = (float)k.m; k.f_kb = (float)k.kb;
+  for (int i = 0; i < 4; ++i) { k.f_Tw[i] = (float)k.Tw[i]; k.f_Uw[i] = (float)k.Uw[i]; }
   s->need_old = (c.problem == MCPM_PROBLEM_COUETTE || c.problem == MCPM_PROBLEM_WALL);
   s->need_x1 = (c.direction[0] == 1 || c.model == MCPM_MODEL_ESMC || c.problem == MCPM_PROBLEM_COUETTE);
 
@@ -177,6 +180,7 @@ int mcpm_session_create(const mcpm_config* cfg, mcpm_session** out) {
   ok = ok && A((void**)&s->key, cap * 4) && A((void**)&s->cnt, C * 4) && A((void**)&s->cnt_next, C * 4) &&
        A((void**)&s->off, (C + 1) * 4) && A((void**)&s->cursor, C * 4) && A((void**)&s->list_small, C * 4) &&
        A((void**)&s->list_big, C * 4) && A((void**)&s->wl, WL_COUNT * 4) && A((void**)&s->work, WK_COUNT * 4) &&
+       A((void**)&s->scan_blk, 4 * (C / 1024 + 2) * 4) &&
        A((void**)&s->cell, (size_t)CF_DEV_COUNT * C * 8) && A((void**)&s->pcell, (size_t)PF_STRIDE * C * 4) && A((void**)&s->xi, 3 * cap * 8) &&
        A((void**)&s->inj, 3 * cap * 8) && A((void**)&s->stage, 5 * cap * 8) &&
        A((void**)&s->faces, ((size_t)k.N1 + 1 + 5000) * 8) && A((void**)&s->status, 16);
@@ -214,7 +218,7 @@ int mcpm_session_destroy(mcpm_session* s) {
     cudaFree(P.x1o); cudaFree(P.x2o);
   }
   cudaFree(s->key); cudaFree(s->cnt); cudaFree(s->cnt_next); cudaFree(s->off); cudaFree(s->cursor);
-  cudaFree(s->list_small); cudaFree(s->list_big); cudaFree(s->wl); cudaFree(s->work); cudaFree(s->cell); cudaFree(s->pcell);
+  cudaFree(s->list_small); cudaFree(s->list_big); cudaFree(s->wl); cudaFree(s->work); cudaFree(s->scan_blk); cudaFree(s->cell); cudaFree(s->pcell);
   cudaFree(s->xi); cudaFree(s->inj); cudaFree(s->stage); cudaFree(s->faces); cudaFree(s->status);
   if (s->graph) cudaGraphExecDestroy(s->graph);
   for (auto& r : s->prof_recs) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
