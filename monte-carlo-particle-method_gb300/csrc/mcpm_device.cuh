@@ -47,19 +47,28 @@ template <> __device__ __forceinline__ Normals3<double> normals3<double>(uint4 r
   sincos(kTwoPi * u01d(r.y), &s1, &c1);
   return {a * c1, a * s1, b * cos(kTwoPi * u01d(r.w))};
 }
+// FP32 path: the hardware approximations of log and sin/cos (a few ulp,
+// about 1e-6 absolute on [0, 2 pi)) -- ample for Monte Carlo draws
 template <> __device__ __forceinline__ Normals3<float> normals3<float>(uint4 r) {
-  float a = sqrtf(-2.0f * logf(u01f(r.x)));
-  float b = sqrtf(-2.0f * logf(u01f(r.z)));
+  const float a = sqrtf(-2.0f * __logf(u01f(r.x)));
+  const float b = sqrtf(-2.0f * __logf(u01f(r.z)));
   float s1, c1;
-  sincospif(2.0f * u01f(r.y), &s1, &c1);
-  return {a * c1, a * s1, b * cospif(2.0f * u01f(r.w))};
+  __sincosf(6.28318530717958647692f * u01f(r.y), &s1, &c1);
+  return {a * c1, a * s1, b * __cosf(6.28318530717958647692f * u01f(r.w))};
 }
+
+// a*b + c: one rounding (FMA) in the FP32 path, two roundings in the FP64
+// path, which reproduces the reference's arithmetic
+template <typename real> __device__ __forceinline__ real mad(real a, real b, real c);
+template <> __device__ __forceinline__ float mad<float>(float a, float b, float c) { return fmaf(a, b, c); }
+template <> __device__ __forceinline__ double mad<double>(double a, double b, double c) { return a * b + c; }
 
 // ------------------------------------------------ constants in real type
 // The FP32 kernels read float copies prepared on the host, so that no
 // double->float conversion (an FP64-pipe instruction) runs per particle.
 template <typename real> struct KC {
   real dx, dy, L0, L1, dt, sigma, m, kb, Tw[4], Uw[4];
+  real idx, idy;  // 1/dx, 1/dy (FP32 binning)
 };
 template <typename real> __device__ __forceinline__ KC<real> make_kc(const DevConsts& k) {
   KC<real> c;
@@ -67,10 +76,12 @@ template <typename real> __device__ __forceinline__ KC<real> make_kc(const DevCo
     c.dx = k.f_dx; c.dy = k.f_dy; c.L0 = k.f_L0; c.L1 = k.f_L1; c.dt = k.f_dt;
     c.sigma = k.f_sigma; c.m = k.f_m; c.kb = k.f_kb;
     for (int i = 0; i < 4; ++i) { c.Tw[i] = k.f_Tw[i]; c.Uw[i] = k.f_Uw[i]; }
+    c.idx = k.f_idx; c.idy = k.f_idy;
   } else {
     c.dx = k.dx; c.dy = k.dy; c.L0 = k.L0; c.L1 = k.L1; c.dt = k.dt;
     c.sigma = k.sigma; c.m = k.m; c.kb = k.kb;
     for (int i = 0; i < 4; ++i) { c.Tw[i] = k.Tw[i]; c.Uw[i] = k.Uw[i]; }
+    c.idx = 1.0 / k.dx; c.idy = 1.0 / k.dy;
   }
   return c;
 }

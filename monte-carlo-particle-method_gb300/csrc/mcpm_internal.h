@@ -62,7 +62,7 @@ struct DevConsts {
   double Tw[4], Uw[4];
   uint64_t seed;
   // float copies for the FP32 kernels
-  float f_dx, f_dy, f_L0, f_L1, f_dt, f_sigma, f_m, f_kb, f_Tw[4], f_Uw[4];
+  float f_dx, f_dy, f_L0, f_L1, f_dt, f_sigma, f_m, f_kb, f_Tw[4], f_Uw[4], f_idx, f_idy;
 };
 
 // One set of device particle arrays (SoA).  real is float or double.

@@ -38,13 +38,15 @@ template <typename real> static PT<real> pt(const PBuf& b) {
 template <typename real>
 __device__ __forceinline__ int bin_one(real x1, real x2, int pid, int step, const DevConsts& k, const KC<real>& kc,
                                        uint32_t& bad) {
+  // FP64: floor(x / dx) as the reference; FP32: x * (1/dx)
+  constexpr bool F32 = sizeof(real) == 4;
   int j = 0;
   if (k.dir0 == 1) {
-    j = (int)floor(x1 / kc.dx);
+    j = (int)floor(F32 ? x1 * kc.idx : x1 / kc.dx);
     if (!(x1 >= (real)0 && x1 <= kc.L0)) bad |= MCPM_ERR_OUT_OF_BOX;
   }
   const real dy = kc.dy;
-  int kk = (int)floor(x2 / dy);
+  int kk = (int)floor(F32 ? x2 * kc.idy : x2 / dy);
   if (!(x2 >= (real)0 && x2 <= kc.L1)) bad |= MCPM_ERR_OUT_OF_BOX;
   if (kk > 0 && kk < k.N1 - 1) {
     if (fabs(x2 - dy * kk) < (real)1e-15 || fabs(x2 - dy * (kk + 1)) < (real)1e-15) {
@@ -906,7 +908,10 @@ template <typename real> struct CellK {
 template <typename real>
 __device__ __forceinline__ void load_cellk(CellK<real>& K, int c, const UpdArgs<real>& a, uint32_t st) {
   if constexpr (sizeof(real) == 4) {
-    const float* pf = a.pcell + (size_t)c * PF_STRIDE;
+    float pf[PF_STRIDE];
+    const float4* src = reinterpret_cast<const float4*>(a.pcell + (size_t)c * PF_STRIDE);
+#pragma unroll
+    for (int j = 0; j < PF_STRIDE / 4; ++j) reinterpret_cast<float4*>(pf)[j] = __ldg(src + j);
     K.us0 = pf[PF_US0]; K.us1 = pf[PF_US1]; K.us2 = pf[PF_US2];
     K.A1 = pf[PF_A1]; K.A2 = pf[PF_A2]; K.A3 = pf[PF_A3]; K.eq = pf[PF_EQ]; K.lam = pf[PF_LAM];
 #pragma unroll
@@ -1017,6 +1022,7 @@ __device__ void update_cell(int c, const UpdArgs<real>& a, real* xs, int xcap, A
       }
     }
   }
+  const real irms0 = (real)1 / rms0, irms1 = (real)1 / rms1, irms2 = (real)1 / rms2;
   // whitened normal of the i-th particle of the cell
   auto xiw = [&](int i, real& z0, real& z1, real& z2) {
     int64_t p = s0 + i;
@@ -1027,7 +1033,11 @@ __device__ void update_cell(int c, const UpdArgs<real>& a, real* xs, int xcap, A
     if (staged) { z0 = xs[3 * i]; z1 = xs[3 * i + 1]; z2 = xs[3 * i + 2]; }
     else raw_normals(a, p, z0, z1, z2);
     if (n > 1) {
-      z0 = (z0 - mean0) / rms0; z1 = (z1 - mean1) / rms1; z2 = (z2 - mean2) / rms2;
+      if constexpr (F32) {
+        z0 = (z0 - mean0) * irms0; z1 = (z1 - mean1) * irms1; z2 = (z2 - mean2) * irms2;
+      } else {
+        z0 = (z0 - mean0) / rms0; z1 = (z1 - mean1) / rms1; z2 = (z2 - mean2) / rms2;
+      }
     }
   };
   // the Ornstein-Uhlenbeck update of M' with the cubic drift
@@ -1037,19 +1047,21 @@ __device__ void update_cell(int c, const UpdArgs<real>& a, real* xs, int xcap, A
     if (n > 1) {
       real z0, z1, z2;
       xiw(i, z0, z1, z2);
-      real energy = m1 * m1 + m2 * m2 + m3 * m3;
-      real d0 = K.c[0] * m1 + K.c[1] * m2 + K.c[2] * m3;
-      d0 += K.g[0] * (energy - K.eq);
-      d0 += K.lam * (m1 * energy - K.q[0]);
-      real d1 = K.c[1] * m1 + K.c[3] * m2 + K.c[4] * m3;
-      d1 += K.g[1] * (energy - K.eq);
-      d1 += K.lam * (m2 * energy - K.q[1]);
-      real d2 = K.c[2] * m1 + K.c[4] * m2 + K.c[5] * m3;
-      d2 += K.g[2] * (energy - K.eq);
-      d2 += K.lam * (m3 * energy - K.q[2]);
-      m1 = K.A1 * m1 + K.A2 * d0 + K.A3 * z0;
-      m2 = K.A1 * m2 + K.A2 * d1 + K.A3 * z1;
-      m3 = K.A1 * m3 + K.A2 * d2 + K.A3 * z2;
+      // the expressions of src/Fokker_Planck.cpp:1114-1130, evaluated left
+      // to right; mad() fuses in the FP32 path only
+      real energy = mad(m3, m3, mad(m2, m2, m1 * m1));
+      real d0 = mad(K.c[2], m3, mad(K.c[1], m2, K.c[0] * m1));
+      d0 = mad(K.g[0], energy - K.eq, d0);
+      d0 = mad(K.lam, mad(m1, energy, -K.q[0]), d0);
+      real d1 = mad(K.c[4], m3, mad(K.c[3], m2, K.c[1] * m1));
+      d1 = mad(K.g[1], energy - K.eq, d1);
+      d1 = mad(K.lam, mad(m2, energy, -K.q[1]), d1);
+      real d2 = mad(K.c[5], m3, mad(K.c[4], m2, K.c[2] * m1));
+      d2 = mad(K.g[2], energy - K.eq, d2);
+      d2 = mad(K.lam, mad(m3, energy, -K.q[2]), d2);
+      m1 = mad(K.A3, z0, mad(K.A2, d0, K.A1 * m1));
+      m2 = mad(K.A3, z1, mad(K.A2, d1, K.A1 * m2));
+      m3 = mad(K.A3, z2, mad(K.A2, d2, K.A1 * m3));
     } else {
       m1 = 0; m2 = 0; m3 = 0;
     }
@@ -1172,7 +1184,7 @@ __device__ void update_cell(int c, const UpdArgs<real>& a, real* xs, int xcap, A
 }
 
 template <typename real>
-__global__ void __launch_bounds__(256) k_update(UpdArgs<real> a) {
+__global__ void __launch_bounds__(256, sizeof(real) == 4 ? 3 : 1) k_update(UpdArgs<real> a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ Acc<real> red[8 * 8];
   real* xs = reinterpret_cast<real*>(smem_raw);

@@ -149,6 +149,7 @@ int mcpm_session_create(const mcpm_config* cfg, mcpm_session** out) {
   k.f_dx = (float)k.dx; k.f_dy = (float)k.dy; k.f_L0 = (float)k.L0; k.f_L1 = (float)k.L1;
   k.f_dt = (float)k.dt; k.f_sigma = (float)k.sigma; k.f_m = (float)k.m; k.f_kb = (float)k.kb;
   for (int i = 0; i < 4; ++i) { k.f_Tw[i] = (float)k.Tw[i]; k.f_Uw[i] = (float)k.Uw[i]; }
+  k.f_idx = (float)(1.0 / k.dx); k.f_idy = (float)(1.0 / k.dy);
   s->need_old = (c.problem == MCPM_PROBLEM_COUETTE || c.problem == MCPM_PROBLEM_WALL);
   s->need_x1 = (c.direction[0] == 1 || c.model == MCPM_MODEL_ESMC || c.problem == MCPM_PROBLEM_COUETTE);
 
