@@ -244,6 +244,24 @@ int mcpm_profile(mcpm_session* s, int32_t enable);
 /* Synchronises; per class: total milliseconds and launches since the last
    read (n <= MCPM_K_COUNT entries each). */
 int mcpm_profile_read(mcpm_session* s, double* ms, int64_t* launches, int32_t n);
+/* ---- allocation-free entry point -------------------------------------- */
+/* No counterpart in the reference.  For callers that cannot allocate device
+   memory (a host framework that owns the GPU allocator, code running between
+   CUDA-graph replays, plugins handed only their input and output buffers):
+   the screened-Poisson Vlasov force of poisson_solver for a 1-D column of
+   cells, from n_cell[n_cells] (device, cell number densities) into
+   F2[n_cells] (device, per-cell force), with the geometry and constants taken
+   from cfg (length[1], sigma, eqdist, bst, ast, m).  It allocates nothing:
+   its scratch is a fixed array of the library that every GPU loading the
+   library holds until exit.  n_cells above MCPM_NOALLOC_MAX_CELLS returns
+   MCPM_ERR_CAPACITY.  The first call on a device resolves the scratch's
+   device address (call it once before any stream capture).  All calls share
+   the scratch, so calls that overlap on the GPU race.  stream may be NULL.
+   Synchronises the stream before returning. */
+#define MCPM_NOALLOC_MAX_CELLS 6999
+int mcpm_poisson_force_1d_noalloc(const double* n_cell, int32_t n_cells,
+                                  const mcpm_config* cfg, double* F2,
+                                  void* stream);
 /* Number of kernel launches the session issued since creation. */
 int64_t mcpm_kernel_launches(const mcpm_session* s);
 

@@ -138,6 +138,7 @@ def load_library(path: str | None = None):
         "mcpm_set_stream": (C.c_int, [vp, vp]),
         "mcpm_profile": (C.c_int, [vp, i32]),
         "mcpm_profile_read": (C.c_int, [vp, dp, C.POINTER(C.c_int64), i32]),
+        "mcpm_poisson_force_1d_noalloc": (C.c_int, [vp, i32, C.POINTER(Config), vp, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
