@@ -178,6 +178,7 @@ def run_mcpm(args):
     if cfg.model == mcpm.MODEL_ESMC:
         s.cell_update()
         s.init_omega_max()
+    wcap = s.autotune(3)  # threads-per-cell split; the state is restored
     clocks = ClockSampler(local)
     s.step(args.warmup)
     torch.cuda.synchronize()
@@ -261,7 +262,8 @@ def run_mcpm(args):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic (seeded)",
-        "config": dict(desc, l2="inputs larger than L2 (no flush)", replicas=ws, precision="fp32 state, fp64 solves"),
+        "config": dict(desc, l2="inputs larger than L2 (no flush)", replicas=ws, precision="fp32 state, fp64 solves",
+                       wcap_autotuned=wcap),
         "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "gpu_launches": launches, "clocks": ck,
         "finite": ok,
     }

@@ -244,6 +244,16 @@ int mcpm_profile(mcpm_session* s, int32_t enable);
 /* Synchronises; per class: total milliseconds and launches since the last
    read (n <= MCPM_K_COUNT entries each). */
 int mcpm_profile_read(mcpm_session* s, double* ms, int64_t* launches, int32_t n);
+/* ---- work split between warps and blocks -------------------------------- */
+/* Cells with at most wcap particles are processed by one warp each, larger
+   cells by a 256-thread block; wcap <= 768 (FP32) / 384 (FP64). */
+int mcpm_set_wcap(mcpm_session* s, int32_t wcap);
+int32_t mcpm_get_wcap(const mcpm_session* s);
+/* Times `steps` fused steps per candidate wcap on the session's particles,
+   restoring the state after each trial, and keeps the fastest (written to
+   *chosen).  Leaves the particle and cell state as it found it. */
+int mcpm_autotune(mcpm_session* s, int32_t steps, int32_t* chosen);
+
 /* ---- allocation-free entry point -------------------------------------- */
 /* No counterpart in the reference.  For callers that cannot allocate device
    memory (a host framework that owns the GPU allocator, code running between

@@ -30,8 +30,11 @@ __device__ __forceinline__ uint4 philox(uint64_t seed, uint32_t c0, uint32_t c1,
 }
 
 __device__ __forceinline__ double u01d(uint32_t x) { return ((double)x + 0.5) * (1.0 / 4294967296.0); }
-// 24-bit uniform in (0,1), exact in float
-__device__ __forceinline__ float u01f(uint32_t x) { return ((float)(x >> 8) + 0.5f) * (1.0f / 16777216.0f); }
+// uniform in (0,1) from the top 23 bits, built in the mantissa of a float in
+// [1,2) (no integer-to-float conversion): k 2^-23 + 2^-24, k = x >> 9
+__device__ __forceinline__ float u01f(uint32_t x) {
+  return __uint_as_float(0x3F800000u | (x >> 9)) - 0.99999994039535522461f;
+}
 __device__ __forceinline__ int pick(uint32_t r, int n) { return (int)(((uint64_t)r * (uint64_t)n) >> 32); }
 
 constexpr double kTwoPi = 6.283185307179586476925286766559;
@@ -62,6 +65,20 @@ template <> __device__ __forceinline__ Normals3<float> normals3<float>(uint4 r) 
 template <typename real> __device__ __forceinline__ real mad(real a, real b, real c);
 template <> __device__ __forceinline__ float mad<float>(float a, float b, float c) { return fmaf(a, b, c); }
 template <> __device__ __forceinline__ double mad<double>(double a, double b, double c) { return a * b + c; }
+
+// ------------------------------------------- math in the path's precision
+// Explicit float/double overloads, so that a float argument never goes
+// through a double routine (GB300's FP64 rate is 1/64 of FP32).
+__device__ __forceinline__ float r_floor(float x) { return floorf(x); }
+__device__ __forceinline__ double r_floor(double x) { return ::floor(x); }
+__device__ __forceinline__ float r_fabs(float x) { return fabsf(x); }
+__device__ __forceinline__ double r_fabs(double x) { return ::fabs(x); }
+__device__ __forceinline__ float r_sqrt(float x) { return sqrtf(x); }
+__device__ __forceinline__ double r_sqrt(double x) { return ::sqrt(x); }
+__device__ __forceinline__ float r_log(float x) { return __logf(x); }
+__device__ __forceinline__ double r_log(double x) { return ::log(x); }
+__device__ __forceinline__ void r_sincos(float x, float* s, float* c) { __sincosf(x, s, c); }
+__device__ __forceinline__ void r_sincos(double x, double* s, double* c) { ::sincos(x, s, c); }
 
 // ------------------------------------------------ constants in real type
 // The FP32 kernels read float copies prepared on the host, so that no

@@ -32,7 +32,7 @@ __global__ void __launch_bounds__(128) k_esmc(DevConsts k, double* cell, const i
   const int C = k.C;
   const int NI = cnt[I];
   const double om_max = cell[(size_t)MCPM_CF_OMEGA_MAX * C + I];
-  const double mreal = floor(0.5 * om_max * (1.0 * NI) + u01d(philox(k.seed, (uint32_t)I, (uint32_t)step, RNG_ESMC_M, 0u).x));
+  const double mreal = r_floor(0.5 * om_max * (1.0 * NI) + u01d(philox(k.seed, (uint32_t)I, (uint32_t)step, RNG_ESMC_M, 0u).x));
   // a non-finite or absurd majorant would make the candidate loop unbounded
   const double mcap = 64.0 * NI + 4096.0;
   int mI = 0;
@@ -54,11 +54,13 @@ __global__ void __launch_bounds__(128) k_esmc(DevConsts k, double* cell, const i
         si = (int64_t)off[I] + pick(r.x, NI);
         real theta = (real)2.0 * pi * (real)u01d(r.y);
         real cph = (real)2.0 * (real)u01d(r.z) - (real)1.0;
-        real sph = sqrt((real)1.0 - cph * cph);
-        d0 = cos(theta) * sph; d1 = sin(theta) * sph; d2 = cph;
+        real sph = r_sqrt((real)1.0 - cph * cph);
+        real sn, cs;
+        r_sincos(theta, &sn, &cs);
+        d0 = cs * sph; d1 = sn * sph; d2 = cph;
         real xi1 = p.x1[si], xi2 = p.x2[si];
         real xx = xi1 + sg * d0, yy = xi2 + sg * d1;
-        int i0 = (int)floor(xx / (real)k.dx), i1 = (int)floor(yy / (real)k.dy);
+        int i0 = (int)r_floor(xx / (real)k.dx), i1 = (int)r_floor(yy / (real)k.dy);
         if (i0 >= 0 && i0 < k.N0 && i1 >= 0 && i1 < k.N1) {
           int J = i1 * k.N0 + i0;
           int NJ = cnt[J];
@@ -66,7 +68,7 @@ __global__ void __launch_bounds__(128) k_esmc(DevConsts k, double* cell, const i
             sj = (int64_t)off[J] + pick(r.w, NJ);
             if (sj != si) {
               real xm0 = (xi1 + p.x1[sj]) / (real)2.0, xm1 = (xi2 + p.x2[sj]) / (real)2.0;
-              int m0 = (int)floor(xm0 / (real)k.dx), m1 = (int)floor(xm1 / (real)k.dy);
+              int m0 = (int)r_floor(xm0 / (real)k.dx), m1 = (int)r_floor(xm1 / (real)k.dy);
               m0 = m0 < 0 ? 0 : (m0 > k.N0 - 1 ? k.N0 - 1 : m0);
               m1 = m1 < 0 ? 0 : (m1 > k.N1 - 1 ? k.N1 - 1 : m1);
               Ymid = cell[(size_t)CFI_Y * C + m1 * k.N0 + m0];

@@ -38,21 +38,22 @@ template <typename real> static PT<real> pt(const PBuf& b) {
 template <typename real>
 __device__ __forceinline__ int bin_one(real x1, real x2, int pid, int step, const DevConsts& k, const KC<real>& kc,
                                        uint32_t& bad) {
-  // FP64: floor(x / dx) as the reference; FP32: x * (1/dx)
+  // FP64: r_floor(x / dx) as the reference; FP32: x * (1/dx)
   constexpr bool F32 = sizeof(real) == 4;
   int j = 0;
   if (k.dir0 == 1) {
-    j = (int)floor(F32 ? x1 * kc.idx : x1 / kc.dx);
+    j = (int)r_floor(F32 ? x1 * kc.idx : x1 / kc.dx);
     if (!(x1 >= (real)0 && x1 <= kc.L0)) bad |= MCPM_ERR_OUT_OF_BOX;
   }
   const real dy = kc.dy;
-  int kk = (int)floor(F32 ? x2 * kc.idy : x2 / dy);
+  const real tk = r_floor(F32 ? x2 * kc.idy : x2 / dy);  // k as a real: dy * k needs no conversion
+  int kk = (int)tk;
   if (!(x2 >= (real)0 && x2 <= kc.L1)) bad |= MCPM_ERR_OUT_OF_BOX;
   if (kk > 0 && kk < k.N1 - 1) {
-    if (fabs(x2 - dy * kk) < (real)1e-15 || fabs(x2 - dy * (kk + 1)) < (real)1e-15) {
+    if (r_fabs(x2 - dy * tk) < (real)1e-15 || r_fabs(x2 - dy * (tk + (real)1)) < (real)1e-15) {
       uint4 r = philox(k.seed, (uint32_t)pid, (uint32_t)step, RNG_BIN, 0u);
       int sgn = (r.x >= 0x80000000u) ? 1 : -1;  // u01(r.x) > 0.5
-      kk = (int)floor((x2 + (real)1e-14 * sgn) / dy);
+      kk = (int)r_floor((x2 + (real)1e-14 * sgn) / dy);
     }
   }
   j = j < 0 ? 0 : (j > k.N0 - 1 ? k.N0 - 1 : j);
@@ -296,20 +297,43 @@ __device__ void moments_cell(int c, const MomArgs<real>& a, Acc<real>* red) {
   Acc<real> q[29];
 #pragma unroll
   for (int j = 0; j < 29; ++j) q[j].zero();
-  for (int i = t; i < n; i += TILE) {
+  // the 29 products of src/Main_Functions.cpp:2502-2560 for particle i
+  auto terms = [&](int i, real (&v)[29]) {
     real Mp1 = a.U1[s0 + i] - m0, Mp2 = a.U2[s0 + i] - m1, Mp3 = a.U3[s0 + i] - m2;
     real energy = Mp1 * Mp1 + Mp2 * Mp2 + Mp3 * Mp3;
-    q[0].add(Mp1); q[1].add(Mp2); q[2].add(Mp3);
-    q[3].add(Mp1 * Mp1); q[4].add(Mp1 * Mp2); q[5].add(Mp1 * Mp3);
-    q[6].add(Mp2 * Mp2); q[7].add(Mp2 * Mp3); q[8].add(Mp3 * Mp3);
-    q[9].add(Mp1 * Mp1 * Mp1); q[10].add(Mp1 * Mp1 * Mp2); q[11].add(Mp1 * Mp1 * Mp3);
-    q[12].add(Mp1 * Mp2 * Mp2); q[13].add(Mp1 * Mp2 * Mp3); q[14].add(Mp1 * Mp3 * Mp3);
-    q[15].add(Mp2 * Mp2 * Mp2); q[16].add(Mp2 * Mp2 * Mp3); q[17].add(Mp2 * Mp3 * Mp3);
-    q[18].add(Mp3 * Mp3 * Mp3);
-    q[19].add(Mp1 * Mp1 * energy); q[20].add(Mp1 * Mp2 * energy); q[21].add(Mp1 * Mp3 * energy);
-    q[22].add(Mp2 * Mp2 * energy); q[23].add(Mp2 * Mp3 * energy); q[24].add(Mp3 * Mp3 * energy);
-    q[25].add(Mp1 * energy * energy); q[26].add(Mp2 * energy * energy); q[27].add(Mp3 * energy * energy);
-    q[28].add(energy);
+    v[0] = Mp1; v[1] = Mp2; v[2] = Mp3;
+    v[3] = Mp1 * Mp1; v[4] = Mp1 * Mp2; v[5] = Mp1 * Mp3;
+    v[6] = Mp2 * Mp2; v[7] = Mp2 * Mp3; v[8] = Mp3 * Mp3;
+    v[9] = Mp1 * Mp1 * Mp1; v[10] = Mp1 * Mp1 * Mp2; v[11] = Mp1 * Mp1 * Mp3;
+    v[12] = Mp1 * Mp2 * Mp2; v[13] = Mp1 * Mp2 * Mp3; v[14] = Mp1 * Mp3 * Mp3;
+    v[15] = Mp2 * Mp2 * Mp2; v[16] = Mp2 * Mp2 * Mp3; v[17] = Mp2 * Mp3 * Mp3;
+    v[18] = Mp3 * Mp3 * Mp3;
+    v[19] = Mp1 * Mp1 * energy; v[20] = Mp1 * Mp2 * energy; v[21] = Mp1 * Mp3 * energy;
+    v[22] = Mp2 * Mp2 * energy; v[23] = Mp2 * Mp3 * energy; v[24] = Mp3 * Mp3 * energy;
+    v[25] = Mp1 * energy * energy; v[26] = Mp2 * energy * energy; v[27] = Mp3 * energy * energy;
+    v[28] = energy;
+  };
+  if constexpr (sizeof(real) == 8) {
+    for (int i = t; i < n; i += TILE) {
+      real v[29];
+      terms(i, v);
+#pragma unroll
+      for (int j = 0; j < 29; ++j) q[j].add(v[j]);
+    }
+  } else {
+    // compensated pairwise accumulation: the terms of two particles are
+    // added in float, then the pair enters the compensated sum
+    for (int i = t; i < n; i += 2 * TILE) {
+      real v[29], w[29];
+      terms(i, v);
+      if (i + TILE < n) {
+        terms(i + TILE, w);
+#pragma unroll
+        for (int j = 0; j < 29; ++j) v[j] += w[j];
+      }
+#pragma unroll
+      for (int j = 0; j < 29; ++j) q[j].add(v[j]);
+    }
   }
   // raw sums, one field per lane; the FP64 finalisation (divisions by the
   // weight, T, n, Y, gamma*) runs once per cell in k_solve
@@ -683,12 +707,12 @@ __device__ __forceinline__ void bc_specular(PState<real>& s, const DevConsts& k,
   int it = 0;
   for (;;) {
     if (k.dir0 == 1) {
-      if (s.x1 - L0 > Tol2) { s.u1 = -s.u1; s.x1 = s.x1 - (real)2.0 * fabs(s.x1 - L0); }
-      else if (s.x1 < Tol1) { s.u1 = -s.u1; s.x1 = s.x1 + (real)2.0 * fabs(s.x1); }
+      if (s.x1 - L0 > Tol2) { s.u1 = -s.u1; s.x1 = s.x1 - (real)2.0 * r_fabs(s.x1 - L0); }
+      else if (s.x1 < Tol1) { s.u1 = -s.u1; s.x1 = s.x1 + (real)2.0 * r_fabs(s.x1); }
     }
     if (k.dir1 == 1) {
-      if (s.x2 - L1 > Tol2) { s.u2 = -s.u2; s.x2 = s.x2 - (real)2.0 * fabs(s.x2 - L1); }
-      else if (s.x2 < Tol1) { s.u2 = -s.u2; s.x2 = s.x2 + (real)2.0 * fabs(s.x2); }
+      if (s.x2 - L1 > Tol2) { s.u2 = -s.u2; s.x2 = s.x2 - (real)2.0 * r_fabs(s.x2 - L1); }
+      else if (s.x2 < Tol1) { s.u2 = -s.u2; s.x2 = s.x2 + (real)2.0 * r_fabs(s.x2); }
     }
     bool done = true;
     if (k.dir0 == 1 && (s.x1 - L0 > (real)0 || s.x1 < (real)0)) done = false;
@@ -700,8 +724,8 @@ __device__ __forceinline__ void bc_specular(PState<real>& s, const DevConsts& k,
 
 template <typename real>
 __device__ __forceinline__ void bc_periodic(PState<real>& s, const DevConsts& k, const KC<real>& kc) {
-  if (k.dir0 == 1) s.x1 = s.x1 - kc.L0 * floor(s.x1 / kc.L0);
-  if (k.dir1 == 1) s.x2 = s.x2 - kc.L1 * floor(s.x2 / kc.L1);
+  if (k.dir0 == 1) s.x1 = s.x1 - kc.L0 * r_floor(s.x1 / kc.L0);
+  if (k.dir1 == 1) s.x2 = s.x2 - kc.L1 * r_floor(s.x2 / kc.L1);
 }
 
 // one diffuse re-emission draw: Rayleigh factor + two normals
@@ -710,8 +734,8 @@ __device__ __forceinline__ void wall_draw(int pid, int step, int call, int it, c
                                           real& z0, real& z1) {
   uint4 r = philox(k.seed, (uint32_t)pid, (uint32_t)step, RNG_BC, (uint32_t)((call << 8) | (it & 0xff)));
   if constexpr (sizeof(real) == 8) {
-    ray = sqrt(-log(u01d(r.x)));
-    double a = sqrt(-2.0 * log(u01d(r.y)));
+    ray = r_sqrt(-log(u01d(r.x)));
+    double a = r_sqrt(-2.0 * log(u01d(r.y)));
     double sn, cs;
     sincos(kTwoPi * u01d(r.z), &sn, &cs);
     z0 = a * cs; z1 = a * sn;
@@ -730,9 +754,9 @@ __device__ __forceinline__ real isect_x(real x, real xo, real yo, real xn, real 
   real n0 = xn - xo, n1 = yn - yo, n2 = 0;
   real size = 0;
   size += n0 * n0; size += n1 * n1; size += n2 * n2;
-  size = sqrt(size);
+  size = r_sqrt(size);
   n0 = n0 / size; n1 = n1 / size;
-  if (fabs(n0) > (real)1e-16) return (n1 / n0) * (x - xo) + yo;
+  if (r_fabs(n0) > (real)1e-16) return (n1 / n0) * (x - xo) + yo;
   return yn;
 }
 template <typename real>
@@ -740,9 +764,9 @@ __device__ __forceinline__ real isect_y(real y, real xo, real yo, real xn, real 
   real n0 = xn - xo, n1 = yn - yo, n2 = 0;
   real size = 0;
   size += n0 * n0; size += n1 * n1; size += n2 * n2;
-  size = sqrt(size);
+  size = r_sqrt(size);
   n0 = n0 / size; n1 = n1 / size;
-  if (fabs(n1) > (real)1e-16) return (n0 / n1) * (y - yo) + xo;
+  if (r_fabs(n1) > (real)1e-16) return (n0 / n1) * (y - yo) + xo;
   return xn;
 }
 
@@ -754,7 +778,7 @@ __device__ void bc_thermal_wall(PState<real>& s, int call, int pid, int step, co
   const real mm = kc.m, kb = kc.kb;
   real dt = DT;
   int it = 0;
-  const real Ue0 = fabs(s.x1 - s.x1o) / DT, Ue1 = fabs(s.x2 - s.x2o) / DT;
+  const real Ue0 = r_fabs(s.x1 - s.x1o) / DT, Ue1 = r_fabs(s.x2 - s.x2o) / DT;
   for (;;) {
     real dt_remain, xw, yw, tU0, ray, z0, z1;
     if (it > 20) { bad |= MCPM_ERR_BC_LOOP; break; }
@@ -773,16 +797,16 @@ __device__ void bc_thermal_wall(PState<real>& s, int call, int pid, int step, co
       const real Tw = kc.Tw[wall], Uw = kc.Uw[wall];
       if (wall >= 2) {  // x walls
         xw = (wall == 3) ? L0 - eps : eps;
-        if (fabs(s.x1o - s.x1) > (real)1e-15) yw = isect_x<real>(xw, s.x1o, s.x2o, s.x1, s.x2);
+        if (r_fabs(s.x1o - s.x1) > (real)1e-15) yw = isect_x<real>(xw, s.x1o, s.x2o, s.x1, s.x2);
         else yw = (real)0.5 * (s.x2o + s.x2);
-        tU0 = (fabs(dt - DT) < (real)1e-15) ? Ue0 : s.u1;
+        tU0 = (r_fabs(dt - DT) < (real)1e-15) ? Ue0 : s.u1;
         wall_draw<real>(pid, step, call, it, k, ray, z0, z1);
-        real un = sqrt((real)2.0 * kb * Tw / (mm)) * ray;
+        real un = r_sqrt((real)2.0 * kb * Tw / (mm)) * ray;
         s.u1 = (wall == 3) ? -un : un;
-        s.u2 = sqrt(kb * Tw / (mm)) * z0 + ((real)1.0 * Uw);
-        s.u3 = sqrt(kb * Tw / (mm)) * z1;
+        s.u2 = r_sqrt(kb * Tw / (mm)) * z0 + ((real)1.0 * Uw);
+        s.u3 = r_sqrt(kb * Tw / (mm)) * z1;
         if (dt > (real)1e-15) {
-          dt_remain = fabs((s.x1 - xw) / tU0);
+          dt_remain = r_fabs((s.x1 - xw) / tU0);
           dt_remain = dt < dt_remain ? dt : dt_remain;
           s.x1 = xw + dt_remain * s.u1;
           s.x2 = yw + dt_remain * s.u2;
@@ -794,14 +818,14 @@ __device__ void bc_thermal_wall(PState<real>& s, int call, int pid, int step, co
       } else {  // y walls at sigma and Len1 - sigma
         yw = (wall == 1) ? L1 - sg - eps : sg + eps;
         xw = isect_y<real>(yw, s.x1o, s.x2o, s.x1, s.x2);
-        tU0 = (fabs(dt - DT) < (real)1e-15) ? Ue1 : s.u2;
+        tU0 = (r_fabs(dt - DT) < (real)1e-15) ? Ue1 : s.u2;
         wall_draw<real>(pid, step, call, it, k, ray, z0, z1);
-        s.u1 = sqrt(kb * Tw / (mm)) * z0 + ((real)1.0 * Uw);
-        real un = sqrt((real)2.0 * kb * Tw / (mm)) * ray;
+        s.u1 = r_sqrt(kb * Tw / (mm)) * z0 + ((real)1.0 * Uw);
+        real un = r_sqrt((real)2.0 * kb * Tw / (mm)) * ray;
         s.u2 = (wall == 1) ? -un : un;
-        s.u3 = sqrt(kb * Tw / (mm)) * z1;
+        s.u3 = r_sqrt(kb * Tw / (mm)) * z1;
         if (dt > (real)1e-15) {
-          dt_remain = fabs((s.x2 - yw) / tU0);
+          dt_remain = r_fabs((s.x2 - yw) / tU0);
           dt_remain = dt < dt_remain ? dt : dt_remain;
           s.x1 = xw + dt_remain * s.u1;
           s.x2 = yw + dt_remain * s.u2;
@@ -825,7 +849,7 @@ __device__ void bc_wall(PState<real>& s, int call, int pid, int step, const DevC
   const real Tw = kc.Tw[0], Uw = kc.Uw[0];
   real dt = DT;
   int it = 0;
-  const real Ue1 = fabs(s.x2 - s.x2o) / DT;
+  const real Ue1 = r_fabs(s.x2 - s.x2o) / DT;
   for (;;) {
     if (it > 20) { bad |= MCPM_ERR_BC_LOOP; break; }
     if (dt < (real)1e-15) {
@@ -833,16 +857,16 @@ __device__ void bc_wall(PState<real>& s, int call, int pid, int step, const DevC
       else if (s.x2 > L1 - eps) s.x2 = L1 - eps;
     } else if (s.x2 > L1) {
       s.u2 = -s.u2;
-      s.x2 = s.x2 - (real)2.0 * fabs(s.x2 - L1);
+      s.x2 = s.x2 - (real)2.0 * r_fabs(s.x2 - L1);
     } else if (s.x2 < (real)0) {
       real yw = eps, ray, z0, z1;
-      real tU0 = (fabs(dt - DT) < (real)1e-15) ? Ue1 : s.u2;
+      real tU0 = (r_fabs(dt - DT) < (real)1e-15) ? Ue1 : s.u2;
       wall_draw<real>(pid, step, call, it, k, ray, z0, z1);
-      s.u1 = sqrt(kb * Tw / (mm)) * z0 + ((real)1.0 * Uw);
-      s.u2 = sqrt((real)2.0 * kb * Tw / (mm)) * ray;
-      s.u3 = sqrt(kb * Tw / mm) * z1;
+      s.u1 = r_sqrt(kb * Tw / (mm)) * z0 + ((real)1.0 * Uw);
+      s.u2 = r_sqrt((real)2.0 * kb * Tw / (mm)) * ray;
+      s.u3 = r_sqrt(kb * Tw / mm) * z1;
       if (dt > (real)1e-15) {
-        real dt_remain = fabs((s.x2 - yw) / tU0);
+        real dt_remain = r_fabs((s.x2 - yw) / tU0);
         dt_remain = dt < dt_remain ? dt : dt_remain;
         s.x2 = yw + dt_remain * s.u2;
         dt = dt - dt_remain;
@@ -1101,7 +1125,7 @@ __device__ void update_cell(int c, const UpdArgs<real>& a, real* xs, int xcap, A
   real scale = (real)1;
   if (fp && n > 1) {
     if constexpr (F32) scale = sqrtf(fabsf(f1acc.getr() / f2acc.getr()));
-    else scale = sqrt(fabs(f1acc.get() / f2acc.get()));
+    else scale = r_sqrt(r_fabs(f1acc.get() / f2acc.get()));
   }
   const real F2dt = (st & ST_LR) ? K.f2dt : (real)0;
   const real dtr = kc.dt;
@@ -1192,7 +1216,7 @@ __global__ void __launch_bounds__(256, sizeof(real) == 4 ? 3 : 1) k_update(UpdAr
   schedule_cells(
       a.list_big, a.list_small, a.wl, a.work, WK_UPD_BIG, WK_UPD_SMALL,
       [&](int c) { update_cell<real, 256>(c, a, xs, a.bcap, red); },
-      [&](int c) { update_cell<real, 32>(c, a, xs + (size_t)warp * 3 * a.wcap, a.wcap, red); });
+      [&](int c) { update_cell<real, 32>(c, a, xs + (size_t)warp * 3 * (a.bcap / 8), a.bcap / 8, red); });
 }
 
 // ========================================================= host<->device
@@ -1275,9 +1299,10 @@ int launch_solve(Session& s, int with_alpha) {
   return 1;
 }
 
+// shared staging: bcap particles for the block path, bcap / 8 per warp for
+// the warp path (cells above that capacity recompute instead of staging)
 template <typename real> static size_t update_smem(const Session& s) {
-  size_t a = (size_t)s.tune.bcap, b = (size_t)(s.tune.block / 32) * s.tune.wcap;
-  return 3 * sizeof(real) * (a > b ? a : b);
+  return 3 * sizeof(real) * (size_t)s.tune.bcap;
 }
 
 template <typename real> static int update_impl(Session& s, uint32_t stages, int bc_call_base) {

@@ -161,9 +161,9 @@ int mcpm_session_create(const mcpm_config* cfg, mcpm_session** out) {
   s->own_stream = s->stream;
 
   // tuning defaults (see mcpm_tune in the Python layer for the sweep)
-  s->tune.wcap = 256;
-  s->tune.block = 256;
   s->tune.bcap = (s->prec == MCPM_FP32) ? 6144 : 3072;
+  s->tune.wcap = 256;  // <= bcap / 8 (a warp's staging capacity); mcpm_autotune picks it
+  s->tune.block = 256;
 
   const size_t cap = (size_t)s->cap, C = (size_t)s->C, rs = s->rsz;
   auto A = [&](void** p, size_t bytes) -> bool { return cudaMalloc(p, bytes ? bytes : 16) == cudaSuccess; };
@@ -497,6 +497,86 @@ int mcpm_init_omega_max(mcpm_session* s) {
 }
 
 int64_t mcpm_kernel_launches(const mcpm_session* s) { return s ? s->launches : -1; }
+
+int mcpm_set_wcap(mcpm_session* s, int32_t wcap) {
+  if (!s || wcap < 1 || wcap > s->tune.bcap / 8) return MCPM_ERR_ARG;
+  s->tune.wcap = wcap;
+  s->sorted = s->sorted && !s->have_particles;  // the work lists are rebuilt by the next scan
+  if (s->have_particles) s->keys_current = false;
+  return MCPM_OK;
+}
+int32_t mcpm_get_wcap(const mcpm_session* s) { return s ? s->tune.wcap : -1; }
+
+// Autotuner: times `steps` fused steps for each candidate threads-per-cell
+// split (cells up to wcap particles get a warp, larger ones a block) on the
+// session's own particles, restoring the full state after every trial, and
+// keeps the fastest.  The particle state is unchanged on return.
+int mcpm_autotune(mcpm_session* s, int32_t steps, int32_t* chosen) {
+  if (!s || !s->have_particles || steps < 1) return MCPM_ERR_STATE;
+  const size_t rs = s->rsz, N = (size_t)s->N, C = (size_t)s->C;
+  const PBuf& P = s->P[s->cur];
+  void* arrs[7] = {P.x1, P.x2, P.U1, P.U2, P.U3, P.x1o, P.x2o};
+  size_t bytes = 0;
+  for (int i = 0; i < 7; ++i) if (arrs[i]) bytes += N * rs;
+  bytes += N * 4 + (size_t)CF_DEV_COUNT * C * 8 + (size_t)PF_STRIDE * C * 4;
+  char* save = nullptr;
+  int rc = cuda_check(s, cudaMalloc(&save, bytes), "autotune scratch");
+  if (rc) return rc;
+  cudaStream_t st = s->stream;
+  auto copy_all = [&](bool to_save) {
+    size_t o = 0;
+    auto cp = [&](void* p, size_t b) {
+      if (!p) return;
+      if (to_save) cudaMemcpyAsync(save + o, p, b, cudaMemcpyDeviceToDevice, st);
+      else cudaMemcpyAsync(p, save + o, b, cudaMemcpyDeviceToDevice, st);
+      o += b;
+    };
+    for (int i = 0; i < 7; ++i) cp(arrs[i], N * rs);
+    cp(P.pid, N * 4);
+    cp(s->cell, (size_t)CF_DEV_COUNT * C * 8);
+    cp(s->pcell, (size_t)PF_STRIDE * C * 4);
+  };
+  const int cur0 = s->cur, step0 = s->step;
+  const bool sorted0 = s->sorted, keys0 = s->keys_current, rebin0 = s->needs_rebin, om0 = s->omega_init;
+  const int64_t launches0 = s->launches;
+  copy_all(true);
+  const int cands[4] = {128, 256, 512, 768};
+  int best = s->tune.wcap;
+  float best_ms = 1e30f;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  for (int ci = 0; ci < 4 && rc == MCPM_OK; ++ci) {
+    if (cands[ci] > s->tune.bcap / 8) continue;
+    s->tune.wcap = cands[ci];
+    s->cur = cur0; s->step = step0; s->keys_current = false; s->sorted = false; s->needs_rebin = false;
+    s->omega_init = om0;
+    rc = mcpm_step(s, 1);  // warm-up (and a re-scan with this split)
+    if (rc) break;
+    cudaEventRecord(e0, st);
+    rc = mcpm_step(s, steps);
+    cudaEventRecord(e1, st);
+    cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (ms < best_ms) { best_ms = ms; best = cands[ci]; }
+    // put the saved state back into the buffer set it came from
+    s->cur = cur0;
+    copy_all(false);
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  s->cur = cur0; s->step = step0; s->sorted = sorted0; s->keys_current = keys0; s->needs_rebin = rebin0;
+  s->omega_init = om0;
+  s->tune.wcap = best;
+  // the saved layout's work lists were built with the old split: rebuild
+  if (s->sorted) { s->sorted = false; s->keys_current = false; }
+  s->launches = launches0;
+  cudaStreamSynchronize(st);
+  cudaFree(save);
+  if (chosen) *chosen = best;
+  return rc;
+}
 
 int mcpm_set_stream(mcpm_session* s, void* stream) {
   if (!s) return MCPM_ERR_ARG;

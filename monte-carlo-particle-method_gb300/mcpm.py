@@ -139,6 +139,9 @@ def load_library(path: str | None = None):
         "mcpm_profile": (C.c_int, [vp, i32]),
         "mcpm_profile_read": (C.c_int, [vp, dp, C.POINTER(C.c_int64), i32]),
         "mcpm_poisson_force_1d_noalloc": (C.c_int, [vp, i32, C.POINTER(Config), vp, vp]),
+        "mcpm_set_wcap": (C.c_int, [vp, i32]),
+        "mcpm_get_wcap": (i32, [vp]),
+        "mcpm_autotune": (C.c_int, [vp, i32, C.POINTER(i32)]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -319,6 +322,19 @@ class Session:
     def set_stream(self, stream_handle):
         """Launch on an external cudaStream_t (e.g. torch's current stream)."""
         self._ck(self.lib.mcpm_set_stream(self.h, C.c_void_p(stream_handle or None)), "set_stream")
+
+    def autotune(self, steps=3):
+        """Pick the warp/block split by timing steps on this state (state restored)."""
+        ch = C.c_int32()
+        self._ck(self.lib.mcpm_autotune(self.h, int(steps), C.byref(ch)), "autotune")
+        return ch.value
+
+    def set_wcap(self, wcap):
+        self._ck(self.lib.mcpm_set_wcap(self.h, int(wcap)), "set_wcap")
+
+    @property
+    def wcap(self):
+        return int(self.lib.mcpm_get_wcap(self.h))
 
     def profile(self, enable=True):
         self._ck(self.lib.mcpm_profile(self.h, 1 if enable else 0), "profile")

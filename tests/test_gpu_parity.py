@@ -306,3 +306,34 @@ def test_esmc_fused_step_runs_fp32(cuda_ok):
     g = s.download()
     assert np.all(np.isfinite(g["U1"]))
     assert np.all((g["x2"] > 0) & (g["x2"] < cfg.length[1]))
+
+
+def test_autotune_restores_state(cuda_ok):
+    """The autotuner times steps on the session's own particles and must hand
+    back exactly the state it was given.  Different warp/block splits change
+    only the summation order; trajectories then diverge (a rounding-level
+    change can move a particle into the neighbouring cell), so the check
+    across splits is on an invariant: the FP update rescales each cell to its
+    own kinetic energy and specular walls conserve it, so the total kinetic
+    energy agrees to FP32 rounding."""
+    cfg, parts = W.uneven_cells_2d(n_cells=(20, 20), precision=mcpm.FP32, hi=1500)
+    s = mcpm.Session(cfg)
+    s.upload(parts["x1"], parts["x2"], parts["U1"], parts["U2"], parts["U3"])
+    s.step(2)
+    before = s.download()
+    w = s.autotune(2)
+    assert w in (128, 256, 512, 768) and s.wcap == w
+    after = s.download()
+    for k in before:
+        assert np.array_equal(before[k], after[k]), k
+    s.step(1)
+    g1 = s.download()
+    s2 = mcpm.Session(cfg)
+    s2.upload(parts["x1"], parts["x2"], parts["U1"], parts["U2"], parts["U3"])
+    s2.set_wcap(128 if w != 128 else 512)
+    s2.step(3)
+    g2 = s2.download()
+    e0 = np.sum(parts["U1"] ** 2 + parts["U2"] ** 2 + parts["U3"] ** 2)
+    e1 = np.sum(g1["U1"] ** 2 + g1["U2"] ** 2 + g1["U3"] ** 2)
+    e2 = np.sum(g2["U1"] ** 2 + g2["U2"] ** 2 + g2["U3"] ** 2)
+    assert abs(e1 - e0) < 1e-5 * e0 and abs(e2 - e0) < 1e-5 * e0
