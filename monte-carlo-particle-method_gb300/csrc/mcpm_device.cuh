@@ -86,6 +86,7 @@ __device__ __forceinline__ void r_sincos(double x, double* s, double* c) { ::sin
 template <typename real> struct KC {
   real dx, dy, L0, L1, dt, sigma, m, kb, Tw[4], Uw[4];
   real idx, idy;  // 1/dx, 1/dy (FP32 binning)
+  real eps_x, eps_y;  // diffuse-wall offsets
 };
 template <typename real> __device__ __forceinline__ KC<real> make_kc(const DevConsts& k) {
   KC<real> c;
@@ -93,12 +94,12 @@ template <typename real> __device__ __forceinline__ KC<real> make_kc(const DevCo
     c.dx = k.f_dx; c.dy = k.f_dy; c.L0 = k.f_L0; c.L1 = k.f_L1; c.dt = k.f_dt;
     c.sigma = k.f_sigma; c.m = k.f_m; c.kb = k.f_kb;
     for (int i = 0; i < 4; ++i) { c.Tw[i] = k.f_Tw[i]; c.Uw[i] = k.f_Uw[i]; }
-    c.idx = k.f_idx; c.idy = k.f_idy;
+    c.idx = k.f_idx; c.idy = k.f_idy; c.eps_x = k.f_eps_x; c.eps_y = k.f_eps_y;
   } else {
     c.dx = k.dx; c.dy = k.dy; c.L0 = k.L0; c.L1 = k.L1; c.dt = k.dt;
     c.sigma = k.sigma; c.m = k.m; c.kb = k.kb;
     for (int i = 0; i < 4; ++i) { c.Tw[i] = k.Tw[i]; c.Uw[i] = k.Uw[i]; }
-    c.idx = 1.0 / k.dx; c.idy = 1.0 / k.dy;
+    c.idx = 1.0 / k.dx; c.idy = 1.0 / k.dy; c.eps_x = k.eps_x; c.eps_y = k.eps_y;
   }
   return c;
 }
@@ -277,18 +278,32 @@ __device__ __forceinline__ void tile_reduce(Acc<real> (&a)[K], Acc<real>* smem) 
       a[q] = t;
     }
   } else {
+    // one partial per warp and field; warp 0 merges (lane q takes field q)
+    // and leaves the totals in smem[q * W] for every thread to read
     constexpr int W = TILE / 32;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     __syncthreads();
     if ((lane & (32 / P - 1)) == 0 && f < K) smem[f * W + warp] = r;
     __syncthreads();
-#pragma unroll
-    for (int q = 0; q < K; ++q) {
-      Acc<real> t = smem[q * W];
-      for (int w = 1; w < W; ++w) t.merge(smem[q * W + w]);
-      a[q] = t;
+    if (warp == 0 && lane < K) {
+      Acc<real> t = smem[lane * W];
+      for (int w = 1; w < W; ++w) t.merge(smem[lane * W + w]);
+      smem[lane * W] = t;
     }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < K; ++q) a[q] = smem[q * W];
   }
+}
+
+// floor(t) for -1 < t < 2^23 without a float-to-int conversion instruction:
+// adding 2^23 with rounding toward -inf leaves floor(t) in the mantissa.
+// Values outside that range come out below 0 or at or above 2^23 and are
+// clamped by the caller.  Returns the integer; *tf gets floor(t) as a float.
+__device__ __forceinline__ int floor_to_int(float t, float* tf) {
+  const float f = __fadd_rd(t, 8388608.0f);
+  *tf = f - 8388608.0f;
+  return __float_as_int(f) - 0x4B000000;
 }
 
 __device__ __forceinline__ void raise_status(uint32_t* status, uint32_t bits) {

@@ -1,4 +1,6 @@
 // mcpm_forces.cu -- ESMC collisions and the 1-D Vlasov long-range force.
+#include <algorithm>
+#include <cstring>
 #include <vector>
 
 #include "mcpm_device.cuh"
@@ -205,121 +207,227 @@ static void build_quad(const Session& s, int mode, std::vector<double>& off, std
   }
 }
 
-// face potential by direct quadrature: one warp per face
-__global__ void k_face_quad(DevConsts k, const double* cell, const double* qoff, const double* qw, double* V,
-                            int nfaces, int face0, int face_stride) {
-  const int lane = threadIdx.x & 31;
-  const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  if (wid >= nfaces) return;
-  const int fc = face0 + wid * face_stride;
-  const int C = k.C;
-  double acc = 0.0;
-  for (int q = lane; q < 2500; q += 32) {
-    double y = fc * k.dy + qoff[q];
-    int num = (int)floor(y / k.dy);
-    int nc = num > -1 && num < k.N1 ? num : (num < 0 ? 0 : k.N1 - 1);
-    acc += qw[q] * cell[(size_t)MCPM_CF_N * C + nc];
-  }
-#pragma unroll
-  for (int m = 16; m >= 1; m >>= 1) acc += __shfl_xor_sync(FULL, acc, m);
-  if (lane == 0) V[fc] = acc;
-}
+// ---- per-session tables (device), laid out in Session::lr_tab:
+//  direct:  int dmin, dmax; double W[dmax - dmin + 1]; exceptions (fc, q, da, dg, w)
+//  screened Poisson: int idx0[2500], idxN[2500]; double w[2500];
+//                    double alpha[L][nf], gamma[L][nf], dfin[nf]
+struct LRTab {
+  int mode, nf, levels;
+  int dmin, dmax;
+  int n_exc;
+  const double* W;       // stencil weights, dmax - dmin + 1
+  const int* exc_i;      // [n_exc][4]: face, cell of the point, cell the stencil assumes
+  const double* exc_w;   // [n_exc] the point's weight
+  const int* idx0;       // GF wall points: cell of each point for face 0 / face N1
+  const int* idxN;
+  const double* wq;      // GF point weights
+  const double* pa;      // PCR coefficients [levels][nf]
+  const double* pg;
+  const double* dfin;    // final diagonal
+};
 
-// F2 per cell from the face potential, src/Main_Functions.cpp:3924-3938 / :3568-3577
-__global__ void k_face_force(DevConsts k, double* cell, float* pcell, const double* V, double coef) {
-  const int C = k.C;
-  int num = blockIdx.x * blockDim.x + threadIdx.x;
-  if (num >= k.N1) return;
-  double F2 = -(V[num + 1] - V[num]) / k.dy;
-  F2 = F2 / k.m * coef;
-  for (int j = 0; j < k.N0; ++j) {
-    cell[(size_t)MCPM_CF_F2 * C + num * k.N0 + j] = F2;
-    if (pcell) pcell[(size_t)(num * k.N0 + j) * PF_STRIDE + PF_F2DT] = (float)(F2 * k.dt);
-  }
-}
-
-// poisson_solver's tridiagonal system (src/Main_Functions.cpp:3375-3470)
-// solved by parallel cyclic reduction in one block; afterwards the analytic
-// r < sigma part is subtracted (:3539-3558).  V[0], V[nf-1] hold the wall
-// values on entry.
-__global__ void k_poisson_pcr(DevConsts k, const double* cell, double* V, int nf) {
+// One block: the whole 1-D long-range force.  direct (long_range 1,
+// vlasov_taking_the_integral): V_f = sum_D W[D] n[clamp(f + D)] with the
+// stencil verified against the reference's per-point cell lookup at session
+// set-up, plus any points where that lookup is not translation invariant.
+// screened Poisson (long_range 3, poisson_solver): wall values by the
+// per-point quadrature, the constant tridiagonal matrix solved by parallel
+// cyclic reduction with precomputed coefficients, minus the analytic r < sigma
+// part.  Then F2 = -(V_{f+1} - V_f)/dy / m * coef per cell.
+__global__ void __launch_bounds__(1024) k_long_range_1d(DevConsts k, double* cell, float* pcell, LRTab t,
+                                                        double coef) {
   extern __shared__ double sh[];
-  double *l = sh, *d = sh + nf, *u = sh + 2 * nf, *r = sh + 3 * nf;
-  const int C = k.C;
-  const double a_diag = 2.0 + (k.dy * k.bst) * (k.dy * k.bst);
-  const double dy2 = k.dy * k.dy;
-  auto nj = [&](int i) -> double {
-    if (i == 0) return cell[(size_t)MCPM_CF_N * C + 0];
-    if (i == k.N1) return cell[(size_t)MCPM_CF_N * C + (k.N1 - 1)];
-    return (cell[(size_t)MCPM_CF_N * C + i] + cell[(size_t)MCPM_CF_N * C + i - 1]) / 2.0;
-  };
-  for (int i = threadIdx.x; i < nf; i += blockDim.x) {
-    if (i == 0) { l[i] = 0.0; d[i] = 1.0; u[i] = 0.0; r[i] = V[0]; }
-    else if (i == nf - 1) { l[i] = 0.0; d[i] = 1.0; u[i] = 0.0; r[i] = V[nf - 1]; }
-    else { l[i] = -1.0; d[i] = a_diag; u[i] = -1.0; r[i] = nj(i) * dy2; }
-  }
-  __syncthreads();
-  for (int s = 1; s < nf; s <<= 1) {
-    // each thread updates its equations into registers, then writes back
-    double nl[8], nd[8], nu[8], nr[8];
-    int cntq = 0;
-    for (int i = threadIdx.x; i < nf; i += blockDim.x, ++cntq) {
-      double al = 0.0, ga = 0.0;
-      double li = l[i], di = d[i], ui = u[i], ri = r[i];
-      double lo = 0.0, uo = 0.0, ro = 0.0, dd = di;
-      if (i - s >= 0) { al = -li / d[i - s]; lo = al * l[i - s]; dd += al * u[i - s]; ro += al * r[i - s]; }
-      if (i + s < nf) { ga = -ui / d[i + s]; uo = ga * u[i + s]; dd += ga * l[i + s]; ro += ga * r[i + s]; }
-      nl[cntq] = lo; nd[cntq] = dd; nu[cntq] = uo; nr[cntq] = ri + ro;
+  const int nf = t.nf, N1 = k.N1, C = k.C;
+  const double* n = cell + (size_t)MCPM_CF_N * C;
+  double* V = sh;            // [nf]
+  double* r2 = sh + nf;      // [nf] (PCR ping-pong)
+  auto ncl = [&](int c) -> double { return n[c < 0 ? 0 : (c > N1 - 1 ? N1 - 1 : c)]; };
+  if (t.mode == MCPM_LR_DIRECT) {
+    for (int fc = threadIdx.x; fc < nf; fc += blockDim.x) {
+      double v = 0.0;
+      for (int d = t.dmin; d <= t.dmax; ++d) v += t.W[d - t.dmin] * ncl(fc + d);
+      V[fc] = v;
     }
     __syncthreads();
-    cntq = 0;
-    for (int i = threadIdx.x; i < nf; i += blockDim.x, ++cntq) { l[i] = nl[cntq]; d[i] = nd[cntq]; u[i] = nu[cntq]; r[i] = nr[cntq]; }
+    if (threadIdx.x == 0)
+      for (int e = 0; e < t.n_exc; ++e) {
+        const int* x = t.exc_i + 4 * e;
+        V[x[0]] += t.exc_w[e] * (ncl(x[1]) - ncl(x[2]));
+      }
+    __syncthreads();
+  } else {
+    // wall values: warp 0 -> face 0, warp 1 -> face N1, lane-strided sums
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (warp < 2) {
+      const int* idx = warp == 0 ? t.idx0 : t.idxN;
+      double acc = 0.0;
+      for (int q = lane; q < 2500; q += 32) acc += t.wq[q] * n[idx[q]];
+#pragma unroll
+      for (int m = 16; m >= 1; m >>= 1) acc += __shfl_xor_sync(FULL, acc, m);
+      if (lane == 0) V[warp == 0 ? 0 : nf - 1] = acc;
+    }
+    __syncthreads();
+    const double dy2 = k.dy * k.dy;
+    for (int i = threadIdx.x; i < nf; i += blockDim.x) {
+      if (i == 0 || i == nf - 1) r2[i] = V[i];
+      else r2[i] = ((n[i] + n[i - 1]) / 2.0) * dy2;
+    }
+    __syncthreads();
+    double* src = r2;
+    double* dst = V;
+    for (int lv = 0, s = 1; lv < t.levels; ++lv, s <<= 1) {
+      const double* pa = t.pa + (size_t)lv * nf;
+      const double* pg = t.pg + (size_t)lv * nf;
+      for (int i = threadIdx.x; i < nf; i += blockDim.x) {
+        double v = src[i];
+        if (i - s >= 0) v += pa[i] * src[i - s];
+        if (i + s < nf) v += pg[i] * src[i + s];
+        dst[i] = v;
+      }
+      __syncthreads();
+      double* tmp = src; src = dst; dst = tmp;
+    }
+    double corr = 1.0 - (k.sigma * k.bst + 1.0) * exp(-k.bst * k.sigma);
+    corr = corr / k.bst / k.bst;
+    for (int i = threadIdx.x; i < nf; i += blockDim.x) {
+      double nj = i == 0 ? n[0] : (i == N1 ? n[N1 - 1] : (n[i] + n[i - 1]) / 2.0);
+      dst[i] = src[i] / t.dfin[i] - nj * corr;
+    }
+    __syncthreads();
+    if (dst != V)
+      for (int i = threadIdx.x; i < nf; i += blockDim.x) V[i] = dst[i];
     __syncthreads();
   }
-  double dummy = 1.0 - (k.sigma * k.bst + 1.0) * exp(-k.bst * k.sigma);
-  dummy = dummy / k.bst / k.bst;
-  for (int i = threadIdx.x; i < nf; i += blockDim.x) V[i] = r[i] / d[i] - nj(i) * dummy;
+  for (int num = threadIdx.x; num < N1; num += blockDim.x) {
+    double F2 = -(V[num + 1] - V[num]) / k.dy;
+    F2 = F2 / k.m * coef;
+    for (int j = 0; j < k.N0; ++j) {
+      cell[(size_t)MCPM_CF_F2 * C + num * k.N0 + j] = F2;
+      if (pcell) pcell[(size_t)(num * k.N0 + j) * PF_STRIDE + PF_F2DT] = (float)(F2 * k.dt);
+    }
+  }
 }
 
 int launch_long_range(Session& s) {
   const int mode = s.cfg.long_range;
   if (mode != MCPM_LR_DIRECT && mode != MCPM_LR_SCREENED_POISSON) return 0;
-  const int nf = s.k.N1 + 1;
-  double* V = s.faces;
-  double* qoff = s.faces + nf;          // 2500
-  double* qw = s.faces + nf + 2500;     // 2500
-  int n = 0;
-  if (mode == MCPM_LR_DIRECT) {
-    k_face_quad<<<(nf * 32 + 127) / 128, 128, 0, s.stream>>>(s.k, s.cell, qoff, qw, V, nf, 0, 1);
-    ++n;
-    k_face_force<<<(s.k.N1 + 127) / 128, 128, 0, s.stream>>>(s.k, s.cell, s.prec == MCPM_FP32 ? s.pcell : nullptr, V, s.cfg.phi);
-    ++n;
-  } else {
-    // the two wall values, then the PCR solve
-    k_face_quad<<<1, 64, 0, s.stream>>>(s.k, s.cell, qoff, qw, V, 2, 0, nf - 1);
-    ++n;
-    k_poisson_pcr<<<1, 1024, 4 * nf * sizeof(double), s.stream>>>(s.k, s.cell, V, nf);
-    ++n;
-    k_face_force<<<(s.k.N1 + 127) / 128, 128, 0, s.stream>>>(s.k, s.cell, s.prec == MCPM_FP32 ? s.pcell : nullptr, V, s.cfg.ast);
-    ++n;
-  }
-  return n;
+  const LRTab* t = reinterpret_cast<const LRTab*>(s.lr_host);
+  const double coef = mode == MCPM_LR_DIRECT ? s.cfg.phi : s.cfg.ast;
+  k_long_range_1d<<<1, 1024, 2 * t->nf * sizeof(double), s.stream>>>(
+      s.k, s.cell, s.prec == MCPM_FP32 ? s.pcell : nullptr, *t, coef);
+  return 1;
 }
 
-// host-side table upload for the session (called at creation)
+// host-side tables for the session (called at creation): see LRTab
 int long_range_setup(Session& s) {
   const int mode = s.cfg.long_range;
   if (mode != MCPM_LR_DIRECT && mode != MCPM_LR_SCREENED_POISSON) return 0;
   std::vector<double> off, w;
   build_quad(s, mode, off, w);
-  const int nf = s.k.N1 + 1;
-  cudaMemcpy(s.faces + nf, off.data(), 2500 * sizeof(double), cudaMemcpyHostToDevice);
-  cudaMemcpy(s.faces + nf + 2500, w.data(), 2500 * sizeof(double), cudaMemcpyHostToDevice);
+  const int N1 = s.k.N1, nf = N1 + 1;
+  const double dy = s.k.dy;
+  LRTab t{};
+  t.mode = mode;
+  t.nf = nf;
+  std::vector<char> blob;
+  auto put = [&](const void* p, size_t b) -> size_t {
+    size_t o = (blob.size() + 15) & ~size_t(15);
+    blob.resize(o + b);
+    memcpy(blob.data() + o, p, b);
+    return o;
+  };
+  size_t oW = 0, oEi = 0, oEw = 0, oI0 = 0, oIN = 0, oWq = 0, oPa = 0, oPg = 0, oDf = 0;
+  if (mode == MCPM_LR_DIRECT) {
+    // the reference's cell of point q seen from face fc (src/Main_Functions.cpp:3772-3773)
+    auto cellof = [&](int fc, int q) { return (int)floor((fc * dy + off[q]) / dy); };
+    std::vector<int> dgen(2500);
+    int dmin = 1 << 30, dmax = -(1 << 30);
+    const int fref = nf / 2;
+    for (int q = 0; q < 2500; ++q) {
+      dgen[q] = cellof(fref, q) - fref;
+      dmin = std::min(dmin, dgen[q]);
+      dmax = std::max(dmax, dgen[q]);
+    }
+    std::vector<double> W(dmax - dmin + 1, 0.0);
+    for (int q = 0; q < 2500; ++q) W[dgen[q] - dmin] += w[q];
+    std::vector<int> exi;
+    std::vector<double> exw;
+    for (int fc = 0; fc < nf; ++fc)
+      for (int q = 0; q < 2500; ++q) {
+        int c = cellof(fc, q);
+        if (c - fc != dgen[q]) {
+          exi.push_back(fc); exi.push_back(c); exi.push_back(fc + dgen[q]); exi.push_back(q);
+          exw.push_back(w[q]);
+        }
+      }
+    t.dmin = dmin;
+    t.dmax = dmax;
+    t.n_exc = (int)exw.size();
+    oW = put(W.data(), W.size() * 8);
+    if (!exw.empty()) {
+      oEi = put(exi.data(), exi.size() * 4);
+      oEw = put(exw.data(), exw.size() * 8);
+    }
+  } else {
+    std::vector<int> i0(2500), iN(2500);
+    for (int q = 0; q < 2500; ++q) {
+      int c0 = (int)floor((0 * dy + off[q]) / dy), cN = (int)floor((N1 * dy + off[q]) / dy);
+      i0[q] = c0 < 0 ? 0 : (c0 > N1 - 1 ? N1 - 1 : c0);
+      iN[q] = cN < 0 ? 0 : (cN > N1 - 1 ? N1 - 1 : cN);
+    }
+    oI0 = put(i0.data(), 2500 * 4);
+    oIN = put(iN.data(), 2500 * 4);
+    oWq = put(w.data(), 2500 * 8);
+    // PCR of the constant matrix (src/Main_Functions.cpp:3375-3466):
+    // row 0 and row nf-1 are the Dirichlet rows, interior rows -1, 2+(dy b)^2, -1
+    std::vector<double> l(nf), d(nf), u(nf);
+    const double ad = 2.0 + (dy * s.cfg.bst) * (dy * s.cfg.bst);
+    for (int i = 0; i < nf; ++i) {
+      if (i == 0 || i == nf - 1) { l[i] = 0.0; d[i] = 1.0; u[i] = 0.0; }
+      else { l[i] = -1.0; d[i] = ad; u[i] = -1.0; }
+    }
+    int levels = 0;
+    while ((1 << levels) < nf) ++levels;
+    std::vector<double> pa((size_t)levels * nf), pg((size_t)levels * nf);
+    for (int lv = 0, st = 1; lv < levels; ++lv, st <<= 1) {
+      std::vector<double> nl(nf), nd(nf), nu(nf);
+      for (int i = 0; i < nf; ++i) {
+        double al = 0.0, ga = 0.0, dd = d[i], lo = 0.0, uo = 0.0;
+        if (i - st >= 0) { al = -l[i] / d[i - st]; lo = al * l[i - st]; dd += al * u[i - st]; }
+        if (i + st < nf) { ga = -u[i] / d[i + st]; uo = ga * u[i + st]; dd += ga * l[i + st]; }
+        pa[(size_t)lv * nf + i] = al;
+        pg[(size_t)lv * nf + i] = ga;
+        nl[i] = lo; nd[i] = dd; nu[i] = uo;
+      }
+      l.swap(nl); d.swap(nd); u.swap(nu);
+    }
+    t.levels = levels;
+    oPa = put(pa.data(), pa.size() * 8);
+    oPg = put(pg.data(), pg.size() * 8);
+    oDf = put(d.data(), nf * 8);
+  }
+  if (cudaMalloc(&s.lr_tab, blob.size() + 16) != cudaSuccess) return 1;
+  cudaMemcpy(s.lr_tab, blob.data(), blob.size(), cudaMemcpyHostToDevice);
+  char* base = (char*)s.lr_tab;
+  if (mode == MCPM_LR_DIRECT) {
+    t.W = (const double*)(base + oW);
+    t.exc_i = t.n_exc ? (const int*)(base + oEi) : nullptr;
+    t.exc_w = t.n_exc ? (const double*)(base + oEw) : nullptr;
+  } else {
+    t.idx0 = (const int*)(base + oI0);
+    t.idxN = (const int*)(base + oIN);
+    t.wq = (const double*)(base + oWq);
+    t.pa = (const double*)(base + oPa);
+    t.pg = (const double*)(base + oPg);
+    t.dfin = (const double*)(base + oDf);
+  }
+  static_assert(sizeof(LRTab) <= sizeof(s.lr_host), "LRTab fits the session's slot");
+  memcpy(s.lr_host, &t, sizeof(LRTab));
   return 0;
 }
 
 cudaError_t pcr_set_smem(int nf) {
-  return cudaFuncSetAttribute(k_poisson_pcr, cudaFuncAttributeMaxDynamicSharedMemorySize, 4 * nf * (int)sizeof(double));
+  return cudaFuncSetAttribute(k_long_range_1d, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * nf * (int)sizeof(double));
 }
 
 }  // namespace mcpm

@@ -61,8 +61,10 @@ struct DevConsts {
   double sigma, m, kb, n, Fn, T0, mu, visp, b, dt, phi, eqdist, ast, bst;
   double Tw[4], Uw[4];
   uint64_t seed;
+  // wall offset of the diffuse walls, max(1e-15, 4 ulp(Len)) per direction
+  double eps_x, eps_y;
   // float copies for the FP32 kernels
-  float f_dx, f_dy, f_L0, f_L1, f_dt, f_sigma, f_m, f_kb, f_Tw[4], f_Uw[4], f_idx, f_idy;
+  float f_dx, f_dy, f_L0, f_L1, f_dt, f_sigma, f_m, f_kb, f_Tw[4], f_Uw[4], f_idx, f_idy, f_eps_x, f_eps_y;
 };
 
 // One set of device particle arrays (SoA).  real is float or double.
@@ -111,6 +113,8 @@ struct Session {
   double* inj = nullptr;        // [3][cap] injected raw normals, particle-id order
   double* stage = nullptr;      // [5][cap] host<->device staging (double)
   double* faces = nullptr;      // [4][N1+1] long-range face scratch
+  void* lr_tab = nullptr;       // long-range tables (stencil / PCR coefficients)
+  alignas(16) char lr_host[160];  // the kernel's view of lr_tab
   uint32_t* status = nullptr;
   cudaStream_t stream = nullptr;
   int step = 0;

@@ -41,13 +41,24 @@ __device__ __forceinline__ int bin_one(real x1, real x2, int pid, int step, cons
   // FP64: r_floor(x / dx) as the reference; FP32: x * (1/dx)
   constexpr bool F32 = sizeof(real) == 4;
   int j = 0;
-  if (k.dir0 == 1) {
-    j = (int)r_floor(F32 ? x1 * kc.idx : x1 / kc.dx);
-    if (!(x1 >= (real)0 && x1 <= kc.L0)) bad |= MCPM_ERR_OUT_OF_BOX;
-  }
   const real dy = kc.dy;
-  const real tk = r_floor(F32 ? x2 * kc.idy : x2 / dy);  // k as a real: dy * k needs no conversion
-  int kk = (int)tk;
+  real tk;  // k as a real: dy * k needs no conversion
+  int kk;
+  if constexpr (F32) {
+    if (k.dir0 == 1) {
+      float tj;
+      j = floor_to_int(x1 * kc.idx, &tj);
+      if (!(x1 >= 0.f && x1 <= kc.L0)) bad |= MCPM_ERR_OUT_OF_BOX;
+    }
+    kk = floor_to_int(x2 * kc.idy, &tk);
+  } else {
+    if (k.dir0 == 1) {
+      j = (int)r_floor(x1 / kc.dx);
+      if (!(x1 >= (real)0 && x1 <= kc.L0)) bad |= MCPM_ERR_OUT_OF_BOX;
+    }
+    tk = r_floor(x2 / dy);
+    kk = (int)tk;
+  }
   if (!(x2 >= (real)0 && x2 <= kc.L1)) bad |= MCPM_ERR_OUT_OF_BOX;
   if (kk > 0 && kk < k.N1 - 1) {
     if (r_fabs(x2 - dy * tk) < (real)1e-15 || r_fabs(x2 - dy * (tk + (real)1)) < (real)1e-15) {
@@ -774,7 +785,7 @@ __device__ __forceinline__ real isect_y(real y, real xo, real yo, real xn, real 
 template <typename real>
 __device__ void bc_thermal_wall(PState<real>& s, int call, int pid, int step, const DevConsts& k, const KC<real>& kc,
                                 uint32_t& bad) {
-  const real eps = (real)1e-15, L0 = kc.L0, L1 = kc.L1, sg = kc.sigma, DT = kc.dt;
+  const real ex = kc.eps_x, ey = kc.eps_y, L0 = kc.L0, L1 = kc.L1, sg = kc.sigma, DT = kc.dt;
   const real mm = kc.m, kb = kc.kb;
   real dt = DT;
   int it = 0;
@@ -783,20 +794,22 @@ __device__ void bc_thermal_wall(PState<real>& s, int call, int pid, int step, co
     real dt_remain, xw, yw, tU0, ray, z0, z1;
     if (it > 20) { bad |= MCPM_ERR_BC_LOOP; break; }
     if (dt < (real)1e-15) {
-      if (s.x1 < eps) s.x1 = eps;
-      else if (s.x1 > L0 - eps) s.x1 = L0 - eps;
-      if (s.x2 < eps) s.x2 = eps;
-      else if (s.x2 > L1 - eps) s.x2 = L1 - eps;
+      if (s.x1 < ex) s.x1 = ex;
+      else if (s.x1 > L0 - ex) s.x1 = L0 - ex;
+      if (s.x2 < ey) s.x2 = ey;
+      else if (s.x2 > L1 - ey) s.x2 = L1 - ey;
     }
+    // a particle exactly on the x walls counts as having reached them (the
+    // reference's > / < leave x == Len neither inside nor outside)
     int wall = -1;
-    if (s.x1 - L0 > (real)0) wall = 3;
-    else if (s.x1 < (real)0) wall = 2;
-    else if (s.x2 > L1 - sg - eps) wall = 1;
-    else if (s.x2 < sg + eps) wall = 0;
+    if (s.x1 - L0 >= (real)0) wall = 3;
+    else if (s.x1 <= (real)0) wall = 2;
+    else if (s.x2 > L1 - sg - ey) wall = 1;
+    else if (s.x2 < sg + ey) wall = 0;
     if (wall >= 0) {
       const real Tw = kc.Tw[wall], Uw = kc.Uw[wall];
       if (wall >= 2) {  // x walls
-        xw = (wall == 3) ? L0 - eps : eps;
+        xw = (wall == 3) ? L0 - ex : ex;
         if (r_fabs(s.x1o - s.x1) > (real)1e-15) yw = isect_x<real>(xw, s.x1o, s.x2o, s.x1, s.x2);
         else yw = (real)0.5 * (s.x2o + s.x2);
         tU0 = (r_fabs(dt - DT) < (real)1e-15) ? Ue0 : s.u1;
@@ -816,7 +829,7 @@ __device__ void bc_thermal_wall(PState<real>& s, int call, int pid, int step, co
           s.x1 = xw;
         }
       } else {  // y walls at sigma and Len1 - sigma
-        yw = (wall == 1) ? L1 - sg - eps : sg + eps;
+        yw = (wall == 1) ? L1 - sg - ey : sg + ey;
         xw = isect_y<real>(yw, s.x1o, s.x2o, s.x1, s.x2);
         tU0 = (r_fabs(dt - DT) < (real)1e-15) ? Ue1 : s.u2;
         wall_draw<real>(pid, step, call, it, k, ray, z0, z1);
@@ -845,7 +858,7 @@ __device__ void bc_thermal_wall(PState<real>& s, int call, int pid, int step, co
 template <typename real>
 __device__ void bc_wall(PState<real>& s, int call, int pid, int step, const DevConsts& k, const KC<real>& kc,
                         uint32_t& bad) {
-  const real eps = (real)1e-15, L1 = kc.L1, DT = kc.dt, mm = kc.m, kb = kc.kb;
+  const real eps = kc.eps_y, L1 = kc.L1, DT = kc.dt, mm = kc.m, kb = kc.kb;
   const real Tw = kc.Tw[0], Uw = kc.Uw[0];
   real dt = DT;
   int it = 0;
@@ -855,10 +868,10 @@ __device__ void bc_wall(PState<real>& s, int call, int pid, int step, const DevC
     if (dt < (real)1e-15) {
       if (s.x2 < eps) s.x2 = eps;
       else if (s.x2 > L1 - eps) s.x2 = L1 - eps;
-    } else if (s.x2 > L1) {
+    } else if (s.x2 >= L1) {  // >= / <=: see bc_thermal_wall
       s.u2 = -s.u2;
       s.x2 = s.x2 - (real)2.0 * r_fabs(s.x2 - L1);
-    } else if (s.x2 < (real)0) {
+    } else if (s.x2 <= (real)0) {
       real yw = eps, ray, z0, z1;
       real tU0 = (r_fabs(dt - DT) < (real)1e-15) ? Ue1 : s.u2;
       wall_draw<real>(pid, step, call, it, k, ray, z0, z1);
@@ -982,7 +995,7 @@ template <typename real> __device__ __forceinline__ real crms(const Acc<real>& s
 // The FP64 path follows the reference's two-pass centring/normalisation of
 // the normals; the FP32 path takes the per-cell mean and RMS from one pass
 // of compensated sums of z and z^2.
-template <typename real, int TILE>
+template <typename real, int TILE, uint32_t CST>
 __device__ void update_cell(int c, const UpdArgs<real>& a, real* xs, int xcap, Acc<real>* red) {
   constexpr bool F32 = sizeof(real) == 4;
   const int t = (TILE == 32) ? (threadIdx.x & 31) : threadIdx.x;
@@ -990,7 +1003,8 @@ __device__ void update_cell(int c, const UpdArgs<real>& a, real* xs, int xcap, A
   const int n = a.cnt[c];
   const DevConsts& k = a.k;
   const KC<real> kc = make_kc<real>(k);
-  const uint32_t st = a.stages;
+  // stages known at compile time (CST) are folded by the compiler
+  const uint32_t st = CST ? CST : a.stages;
   const bool rng = st & ST_RNG, fp = st & ST_FP, load_xi = st & ST_LOAD_XI, store_xi = st & ST_STORE_XI;
   const bool staged = rng && n <= xcap;
   CellK<real> K;
@@ -1207,7 +1221,7 @@ __device__ void update_cell(int c, const UpdArgs<real>& a, real* xs, int xcap, A
   raise_status(a.status, bad);
 }
 
-template <typename real>
+template <typename real, uint32_t CST>
 __global__ void __launch_bounds__(256, sizeof(real) == 4 ? 3 : 1) k_update(UpdArgs<real> a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ Acc<real> red[8 * 8];
@@ -1215,9 +1229,13 @@ __global__ void __launch_bounds__(256, sizeof(real) == 4 ? 3 : 1) k_update(UpdAr
   const int warp = threadIdx.x >> 5;
   schedule_cells(
       a.list_big, a.list_small, a.wl, a.work, WK_UPD_BIG, WK_UPD_SMALL,
-      [&](int c) { update_cell<real, 256>(c, a, xs, a.bcap, red); },
-      [&](int c) { update_cell<real, 32>(c, a, xs + (size_t)warp * 3 * (a.bcap / 8), a.bcap / 8, red); });
+      [&](int c) { update_cell<real, 256, CST>(c, a, xs, a.bcap, red); },
+      [&](int c) { update_cell<real, 32, CST>(c, a, xs + (size_t)warp * 3 * (a.bcap / 8), a.bcap / 8, red); });
 }
+
+// the fused FP_dense step with specular or periodic walls and no long-range
+// force: every stage fixed at compile time
+constexpr uint32_t ST_FUSED_FP = ST_RNG | ST_FP | ST_DFP | ST_BC1 | ST_STREAM | ST_BC2 | ST_BC3 | ST_KEY;
 
 // ========================================================= host<->device
 template <typename real>
@@ -1327,7 +1345,8 @@ template <typename real> static int update_impl(Session& s, uint32_t stages, int
   a.wcap = s.tune.wcap;
   a.bcap = s.tune.bcap;
   size_t sm = update_smem<real>(s);
-  k_update<real><<<s.tune.grid_upd, 256, sm, s.stream>>>(a);
+  if (stages == ST_FUSED_FP) k_update<real, ST_FUSED_FP><<<s.tune.grid_upd, 256, sm, s.stream>>>(a);
+  else k_update<real, 0u><<<s.tune.grid_upd, 256, sm, s.stream>>>(a);
   return 1;
 }
 int launch_update(Session& s, uint32_t stages, int bc_call_base) {
@@ -1354,15 +1373,19 @@ cudaError_t update_set_smem_max() {
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&mx, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
   mx -= 4 * 8 * 16 + 64;  // leave room for the static reduction scratch
-  cudaError_t e = cudaFuncSetAttribute(k_update<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
-  if (e != cudaSuccess) return e;
-  return cudaFuncSetAttribute(k_update<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+  cudaError_t e = cudaFuncSetAttribute(k_update<float, 0u>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_update<double, 0u>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_update<float, ST_FUSED_FP>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_update<double, ST_FUSED_FP>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+  return e;
 }
 int update_occupancy(const Session& s) {
   int nb = 0;
   size_t sm = update_smem_bytes(s);
-  if (s.prec == MCPM_FP32) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_update<float>, 256, sm);
-  else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_update<double>, 256, sm);
+  if (s.prec == MCPM_FP32) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_update<float, 0u>, 256, sm);
+  else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_update<double, 0u>, 256, sm);
   return nb < 1 ? 1 : nb;
 }
 int moments_occupancy(const Session& s) {

@@ -150,6 +150,14 @@ int mcpm_session_create(const mcpm_config* cfg, mcpm_session** out) {
   k.f_dt = (float)k.dt; k.f_sigma = (float)k.sigma; k.f_m = (float)k.m; k.f_kb = (float)k.kb;
   for (int i = 0; i < 4; ++i) { k.f_Tw[i] = (float)k.Tw[i]; k.f_Uw[i] = (float)k.Uw[i]; }
   k.f_idx = (float)(1.0 / k.dx); k.f_idy = (float)(1.0 / k.dy);
+  // The reference offsets re-emitted particles by epsilon = 1e-15 from a
+  // diffuse wall (src/Main_Functions.cpp:4933), an absolute length meant for
+  // SI boxes; where 1e-15 is below the resolution of the box length the
+  // offset is 4 ulp(Len) instead, in the precision of the particle state.
+  k.eps_x = fmax(1e-15, 4.0 * (nextafter(k.L0, 2.0 * k.L0 + 1.0) - k.L0));
+  k.eps_y = fmax(1e-15, 4.0 * (nextafter(k.L1, 2.0 * k.L1 + 1.0) - k.L1));
+  k.f_eps_x = fmaxf(1e-15f, 4.0f * (nextafterf(k.f_L0, 2.0f * k.f_L0 + 1.0f) - k.f_L0));
+  k.f_eps_y = fmaxf(1e-15f, 4.0f * (nextafterf(k.f_L1, 2.0f * k.f_L1 + 1.0f) - k.f_L1));
   s->need_old = (c.problem == MCPM_PROBLEM_COUETTE || c.problem == MCPM_PROBLEM_WALL);
   s->need_x1 = (c.direction[0] == 1 || c.model == MCPM_MODEL_ESMC || c.problem == MCPM_PROBLEM_COUETTE);
 
@@ -199,11 +207,11 @@ int mcpm_session_create(const mcpm_config* cfg, mcpm_session** out) {
   cudaMemsetAsync(s->xi, 0, 3 * cap * 8, s->stream);
 
   if ((rc = cuda_check(s, update_set_smem_max(), "smem attribute"))) { mcpm_session_destroy(s); return rc; }
-  if (c.long_range == MCPM_LR_SCREENED_POISSON)
-    if ((rc = cuda_check(s, pcr_set_smem(k.N1 + 1), "pcr smem"))) { mcpm_session_destroy(s); return rc; }
+  if (c.long_range != MCPM_LR_NONE)
+    if ((rc = cuda_check(s, pcr_set_smem(k.N1 + 1), "long-range smem"))) { mcpm_session_destroy(s); return rc; }
   s->tune.grid_mom = s->num_sms * moments_occupancy(*s);
   s->tune.grid_upd = s->num_sms * update_occupancy(*s);
-  long_range_setup(*s);
+  if (long_range_setup(*s)) { s->err = "long-range tables"; mcpm_session_destroy(s); return MCPM_ERR_CUDA; }
   if ((rc = cuda_check(s, cudaStreamSynchronize(s->stream), "session init"))) { mcpm_session_destroy(s); return rc; }
   *out = s;
   return MCPM_OK;
@@ -220,7 +228,7 @@ int mcpm_session_destroy(mcpm_session* s) {
   }
   cudaFree(s->key); cudaFree(s->cnt); cudaFree(s->cnt_next); cudaFree(s->off); cudaFree(s->cursor);
   cudaFree(s->list_small); cudaFree(s->list_big); cudaFree(s->wl); cudaFree(s->work); cudaFree(s->scan_blk); cudaFree(s->cell); cudaFree(s->pcell);
-  cudaFree(s->xi); cudaFree(s->inj); cudaFree(s->stage); cudaFree(s->faces); cudaFree(s->status);
+  cudaFree(s->xi); cudaFree(s->inj); cudaFree(s->stage); cudaFree(s->faces); cudaFree(s->lr_tab); cudaFree(s->status);
   if (s->graph) cudaGraphExecDestroy(s->graph);
   for (auto& r : s->prof_recs) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
   for (auto e : s->prof_pool) cudaEventDestroy(e);

@@ -1013,10 +1013,15 @@ static void wall_draw(const orc_state* s, int64_t i, int call_no, int it, double
    = 0): diffuse walls at x = 0 (T_wall_3), x = Len0 (T_wall_4),
    y = sigma (T_wall_1), y = Len1 - sigma (T_wall_2), with re-flight for the
    rest of the step from the wall crossing point. */
+/* The reference's diffuse-wall offset epsilon = 1e-15 (:4933) is an absolute
+   length meant for SI boxes; where it is below the resolution of the box
+   length the offset is 4 ulp(Len) instead (the same rule as the GPU). */
+static double wall_eps(double L) { return fmax(1e-15, 4.0 * (nextafter(L, 2.0 * L + 1.0) - L)); }
+
 static void bc_thermal_wall(orc_state* s, int call_no, double* x1, double* x2,
                             double* x1o, double* x2o, double* U1, double* U2, double* U3) {
   const mcpm_config* g = &s->cfg;
-  const double eps = 1e-15;
+  const double ex = wall_eps(g->length[0]), ey = wall_eps(g->length[1]);
   const double L0 = g->length[0], L1 = g->length[1];
   for (int64_t i = 0; i < s->N; ++i) {
     double dt = g->dt;
@@ -1027,13 +1032,15 @@ static void bc_thermal_wall(orc_state* s, int call_no, double* x1, double* x2,
       double dt_remain = 0.0, xw, yw, tU0, z[2], ray;
       if (it > 20) { s->status |= MCPM_ERR_BC_LOOP; break; }
       if (dt < 1e-15) {
-        if (x1[i] < eps) x1[i] = eps;
-        else if (x1[i] > L0 - eps) x1[i] = L0 - eps;
-        if (x2[i] < eps) x2[i] = eps;
-        else if (x2[i] > L1 - eps) x2[i] = L1 - eps;
+        if (x1[i] < ex) x1[i] = ex;
+        else if (x1[i] > L0 - ex) x1[i] = L0 - ex;
+        if (x2[i] < ey) x2[i] = ey;
+        else if (x2[i] > L1 - ey) x2[i] = L1 - ey;
       }
-      if (x1[i] - L0 > 0.0) { /* right wall */
-        xw = L0 - eps;
+      /* a particle exactly on an x wall counts as having reached it (the
+         reference's > / < leave x == Len neither inside nor outside) */
+      if (x1[i] - L0 >= 0.0) { /* right wall */
+        xw = L0 - ex;
         if (fabs(x1o[i] - x1[i]) > 1e-15) intersect_x(xw, &yw, x1o[i], x2o[i], x1[i], x2[i]);
         else yw = 0.5 * (x2o[i] + x2[i]);
         tU0 = (fabs(dt - g->dt) < 1e-15) ? Ue0 : U1[i];
@@ -1049,8 +1056,8 @@ static void bc_thermal_wall(orc_state* s, int call_no, double* x1, double* x2,
           dt = dt - dt_remain;
           x1o[i] = xw; x2o[i] = yw;
         } else x1[i] = xw;
-      } else if (x1[i] < 0.0) { /* left wall */
-        xw = eps;
+      } else if (x1[i] <= 0.0) { /* left wall */
+        xw = ex;
         if (fabs(x1o[i] - x1[i]) > 1e-15) intersect_x(xw, &yw, x1o[i], x2o[i], x1[i], x2[i]);
         else yw = 0.5 * (x2o[i] + x2[i]);
         tU0 = (fabs(dt - g->dt) < 1e-15) ? Ue0 : U1[i];
@@ -1066,8 +1073,8 @@ static void bc_thermal_wall(orc_state* s, int call_no, double* x1, double* x2,
           dt = dt - dt_remain;
           x1o[i] = xw; x2o[i] = yw;
         } else x1[i] = xw;
-      } else if (x2[i] > L1 - g->sigma - eps) { /* upper wall */
-        yw = L1 - g->sigma - eps;
+      } else if (x2[i] > L1 - g->sigma - ey) { /* upper wall */
+        yw = L1 - g->sigma - ey;
         intersect_y(&xw, yw, x1o[i], x2o[i], x1[i], x2[i]);
         tU0 = (fabs(dt - g->dt) < 1e-15) ? Ue1 : U2[i];
         wall_draw(s, i, call_no, it, z, &ray);
@@ -1082,8 +1089,8 @@ static void bc_thermal_wall(orc_state* s, int call_no, double* x1, double* x2,
           dt = dt - dt_remain;
           x1o[i] = xw; x2o[i] = yw;
         } else x2[i] = yw;
-      } else if (x2[i] < g->sigma + eps) { /* lower wall */
-        yw = g->sigma + eps;
+      } else if (x2[i] < g->sigma + ey) { /* lower wall */
+        yw = g->sigma + ey;
         intersect_y(&xw, yw, x1o[i], x2o[i], x1[i], x2[i]);
         tU0 = (fabs(dt - g->dt) < 1e-15) ? Ue1 : U2[i];
         wall_draw(s, i, call_no, it, z, &ray);
@@ -1110,7 +1117,7 @@ static void bc_thermal_wall(orc_state* s, int call_no, double* x1, double* x2,
 static void bc_wall(orc_state* s, int call_no, double* x2, double* x2o,
                     double* U1, double* U2, double* U3) {
   const mcpm_config* g = &s->cfg;
-  const double eps = 1e-15;
+  const double eps = wall_eps(g->length[1]);
   const double L1 = g->length[1];
   for (int64_t i = 0; i < s->N; ++i) {
     double dt = g->dt;
@@ -1122,10 +1129,10 @@ static void bc_wall(orc_state* s, int call_no, double* x2, double* x2o,
       if (dt < 1e-15) {
         if (x2[i] < eps) x2[i] = eps;
         else if (x2[i] > L1 - eps) x2[i] = L1 - eps;
-      } else if (x2[i] > L1) {
+      } else if (x2[i] >= L1) { /* >= / <=: see bc_thermal_wall */
         U2[i] = -U2[i];
         x2[i] = x2[i] - 2.0 * fabs(x2[i] - L1);
-      } else if (x2[i] < 0.0) {
+      } else if (x2[i] <= 0.0) {
         double yw = eps;
         tU0 = (fabs(dt - g->dt) < 1e-15) ? Ue1 : U2[i];
         wall_draw(s, i, call_no, it, z, &ray);
