@@ -53,8 +53,9 @@ template <> __device__ __forceinline__ Normals3<double> normals3<double>(uint4 r
 // FP32 path: the hardware approximations of log and sin/cos (a few ulp,
 // about 1e-6 absolute on [0, 2 pi)) -- ample for Monte Carlo draws
 template <> __device__ __forceinline__ Normals3<float> normals3<float>(uint4 r) {
-  const float a = sqrtf(-2.0f * __logf(u01f(r.x)));
-  const float b = sqrtf(-2.0f * __logf(u01f(r.z)));
+  // the approximate log of u just below 1 may come out slightly positive
+  const float a = sqrtf(fmaxf(-2.0f * __logf(u01f(r.x)), 0.0f));
+  const float b = sqrtf(fmaxf(-2.0f * __logf(u01f(r.z)), 0.0f));
   float s1, c1;
   __sincosf(6.28318530717958647692f * u01f(r.y), &s1, &c1);
   return {a * c1, a * s1, b * __cosf(6.28318530717958647692f * u01f(r.w))};

@@ -297,12 +297,14 @@ def test_esmc_fp64_same_layout(cuda_ok, shape):
 
 
 def test_esmc_fused_step_runs_fp32(cuda_ok):
-    cfg, parts = W.esmc_box_2d(n_cells=(32, 32), ppc=50, precision=mcpm.FP32)
+    """ESMC with diffuse walls in FP32: positions rounding onto a wall must
+    not stall the re-flight loop (MCPM_ERR_BC_LOOP)."""
+    cfg, parts = W.esmc_box_2d(n_cells=(64, 64), ppc=100, precision=mcpm.FP32)
     s = mcpm.Session(cfg)
     s.upload(parts["x1"], parts["x2"], parts["U1"], parts["U2"], parts["U3"])
     s.cell_update()
     s.init_omega_max()
-    s.step(5)
+    s.step(20)
     g = s.download()
     assert np.all(np.isfinite(g["U1"]))
     assert np.all((g["x2"] > 0) & (g["x2"] < cfg.length[1]))
