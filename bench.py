@@ -114,6 +114,21 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(rows)}
 
 
+def aggregate_ranks(ms_local, particles_local, steps, dist=None):
+    """Whole-job throughput of N replicas: the slowest rank's time (max over
+    ranks) and the particles of all ranks (sum).  Returns (ms_max, value)."""
+    import torch
+    t = torch.tensor([float(ms_local)], dtype=torch.float64)
+    n = torch.tensor([float(particles_local)], dtype=torch.float64)
+    if dist is not None and dist.is_initialized():
+        dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+        t, n = t.to(dev), n.to(dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dist.all_reduce(n, op=dist.ReduceOp.SUM)
+    ms_max = float(t.item())
+    return ms_max, float(n.item()) * steps / (ms_max / 1e3)
+
+
 def build_workload(args):
     import mcpm
     import workloads as W
@@ -201,11 +216,7 @@ def run_mcpm(args):
         s.step(20)
         torch.cuda.synchronize()
     ck = clocks.stop()
-    t = torch.tensor([ms], dtype=torch.float64, device="cuda")
-    if dist:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    ms_max = float(t.item())
-    value = N * ws * args.steps / (ms_max / 1e3)
+    ms_max, value = aggregate_ranks(ms, N, args.steps, dist)
 
     # per-kernel device times (separate short run with CUDA events per launch)
     s.profile(True)
