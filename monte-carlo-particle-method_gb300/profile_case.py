@@ -1,0 +1,48 @@
+"""A small, self-contained particle-step run for ncu captures.
+
+    python monte-carlo-particle-method_gb300/profile_case.py [workload] [n] [fp64]
+
+workload:
+  uneven  n x n cells of the log-normal uneven-cells workload (default n=160:
+          25,600 cells, ~6.3M particles, 175 MB of FP32 state -- larger than
+          the 129 MB L2, a few hundred MB on the device)
+  esmc    n x n cells of the 2-D ESMC Couette box (100 particles per cell)
+  slab    the 1-D Enskog-Vlasov slab with n cells (1000 particles per cell)
+
+Runs three fused steps (the first launches of each kernel are the warm-up,
+so an ncu capture takes `-s 2 -c 1` of the kernel it names) and exits 0.
+"""
+from __future__ import annotations
+
+import os
+import sys
+
+sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+
+import mcpm  # noqa: E402
+import workloads as W  # noqa: E402
+
+
+def main(argv):
+    kind = argv[1] if len(argv) > 1 else "uneven"
+    n = int(argv[2]) if len(argv) > 2 else 160
+    prec = mcpm.FP64 if (len(argv) > 3 and argv[3] == "fp64") else mcpm.FP32
+    if kind == "uneven":
+        cfg, parts = W.uneven_cells_2d(n_cells=(n, n), precision=prec, streaming=True)
+    elif kind == "esmc":
+        cfg, parts = W.esmc_box_2d(n_cells=(n, n), precision=prec)
+    elif kind == "slab":
+        cfg, parts = W.vlasov_slab_1d(n_cells=n, precision=prec)
+    else:
+        raise SystemExit("unknown workload %r" % kind)
+    s = mcpm.Session(cfg)
+    s.upload(parts["x1"], parts["x2"], parts["U1"], parts["U2"], parts["U3"])
+    s.step(3)
+    s.sync()
+    s.check_status()
+    print("ok", kind, n, len(parts["x2"]))
+    s.close()
+
+
+if __name__ == "__main__":
+    main(sys.argv)

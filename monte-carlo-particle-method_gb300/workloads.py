@@ -175,3 +175,53 @@ def uneven_cells_2d(n_cells=(256, 256), precision=FP32, seed=BASE_SEED + 3, stre
     U1, U2, U3 = rng.normal(0, sT, N), rng.normal(0, sT, N), rng.normal(0, sT, N)
     derive(c, N)
     return c, dict(x1=x1, x2=x2, U1=U1, U2=U2, U3=U3, sigma_lognormal=s)
+
+
+def density_field(rng, n_cells, length, K=6, nbar=None):
+    """One seeded 2-D packing-fraction field n b(x, y) at the cell centres:
+    nbar + sum_{k=1..K} a_k sin(2 pi (kx x / L0 + ky y / L1) + phi_k), with
+    nbar ~ U[0.15, 0.35], sum |a_k| <= 0.1, integer wave vectors of norm
+    1..8, clipped to [0.05, 0.45]."""
+    N0, N1 = n_cells
+    xc = (np.arange(N0) + 0.5) * (length[0] / N0)
+    yc = (np.arange(N1) + 0.5) * (length[1] / N1)
+    X, Y = np.meshgrid(xc, yc)  # [N1][N0]
+    nb = np.full(X.shape, rng.uniform(0.15, 0.35) if nbar is None else nbar)
+    amp = rng.uniform(0.0, 1.0, K)
+    amp *= rng.uniform(0.0, 0.1) / max(amp.sum(), 1e-12)
+    for a in amp:
+        while True:
+            kx, ky = rng.integers(-8, 9, 2)
+            if 1.0 <= math.hypot(kx, ky) <= 8.0:
+                break
+        ph = rng.uniform(0.0, 2.0 * math.pi)
+        nb += a * np.sin(2.0 * math.pi * (kx * X / length[0] + ky * Y / length[1]) + ph)
+    return np.clip(nb, 0.05, 0.45).reshape(-1)
+
+
+def vlasov_box_2d(n_cells=(256, 256), total=16_000_000, precision=FP32, seed=BASE_SEED + 4, T=0.8,
+                  long_range=LR_SCREENED_POISSON, eps=1.0, model=MODEL_FP_DENSE, dx=1.0):
+    """2-D Enskog-Vlasov box: square cells of side dx, particles per cell in
+    proportion to a density_field (at least one per cell, `total` in all),
+    Maxwellian kT = T, specular walls, Sutherland attraction
+    phi(r) = -eps (sigma/r)^6 through the 2-D Vlasov force (long_range 1:
+    direct node quadrature; 3: screened-Poisson FEM with Green's-function
+    wall values)."""
+    rng = np.random.default_rng(seed)
+    N0, N1 = n_cells
+    L = (N0 * dx, N1 * dx, 1.0)
+    nb = density_field(rng, n_cells, L)
+    counts = np.maximum(1, np.rint(total * nb / nb.sum())).astype(np.int64)
+    N = int(counts.sum())
+    n_mean = float(nb.mean()) / B_HS
+    c = _base(n_cells, L, (1, 1), PROBLEM_CLOSED_BOX, model, precision, n_mean, T, seed=seed)
+    c.long_range = long_range
+    c.phi = -eps
+    c.eqdist = 1.0
+    c.bst = BST_RED
+    c.ast = AST_RED_4EPS * (eps / 4.0)
+    x1, x2 = _fill_cells(rng, counts, n_cells, L)
+    s = math.sqrt(T)
+    U1, U2, U3 = rng.normal(0, s, N), rng.normal(0, s, N), rng.normal(0, s, N)
+    derive(c, N)
+    return c, dict(x1=x1, x2=x2, U1=U1, U2=U2, U3=U3)

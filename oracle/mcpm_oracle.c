@@ -34,6 +34,7 @@ struct orc_state {
   int rng_mode;
   double* inj;       /* 3N injected normals */
   double* xi;        /* 3N whitened normals (random_generator output) */
+  double* nn;        /* [C][4] nodal densities n_n of the last cell_update */
 };
 
 /* ------------------------------------------------------------------ RNG -- */
@@ -104,6 +105,81 @@ static double cell_volume(const orc_state* s, int c) {
   return (d1 - d0) * (d3 - d2) * (d5 - d4);
 }
 
+
+/* cell geometry exactly as make_cells builds it (src/myIO.cpp:1456-1479):
+   dx_c = dim[1] - dim[0], centre = (dim[0] + dim[1]) / 2, node k of the
+   cell at centre -/+ dx_c / 2 (k = 0 lower left, 1 lower right, 2 upper
+   left, 3 upper right) */
+typedef struct { double dxc, dyc, cx, cy, xn[4], yn[4]; } cell_geo;
+static cell_geo geometry(const orc_state* s, int c) {
+  cell_geo g;
+  int j = c % s->N0, k = c / s->N0;
+  double d0 = (double)j * s->dx, d1 = (double)(j + 1) * s->dx;
+  double d2 = (double)k * s->dy, d3 = (double)(k + 1) * s->dy;
+  g.dxc = d1 - d0; g.dyc = d3 - d2;
+  g.cx = 0.5 * (d0 + d1); g.cy = 0.5 * (d2 + d3);
+  g.xn[0] = g.cx - g.dxc / 2.0; g.xn[1] = g.cx + g.dxc / 2.0;
+  g.xn[2] = g.cx - g.dxc / 2.0; g.xn[3] = g.cx + g.dxc / 2.0;
+  g.yn[0] = g.cy - g.dyc / 2.0; g.yn[1] = g.cy - g.dyc / 2.0;
+  g.yn[2] = g.cy + g.dyc / 2.0; g.yn[3] = g.cy + g.dyc / 2.0;
+  return g;
+}
+/* node ids of cell c: id[0] = k (N0+1) + j, id[1] = id[0] + 1,
+   id[2] = id[0] + N0 + 1, id[3] = id[2] + 1 (src/myIO.cpp:1448-1451) */
+static void node_ids(const orc_state* s, int c, int id[4]) {
+  int j = c % s->N0, k = c / s->N0;
+  id[0] = k * (s->N0 + 1) + j; id[1] = id[0] + 1;
+  id[2] = (k + 1) * (s->N0 + 1) + j; id[3] = id[2] + 1;
+}
+
+/* nodal density n_n, src/Main_Functions.cpp:2268-2364: every particle adds
+   Fn/volume to the node of its own cell nearest to it, in every cell that
+   shares that node; wall nodes are then doubled per wall they lie on. */
+#define NN(c, q) s->nn[(size_t)(c) * 4 + (q)]
+static void node_density(orc_state* s, const double* x1, const double* x2) {
+  const mcpm_config* g = &s->cfg;
+  const int N0 = s->N0, N1 = s->N1;
+  for (size_t i = 0; i < (size_t)s->C * 4; ++i) s->nn[i] = 0.0;
+  for (int64_t i = 0; i < s->N; ++i) {
+    int num = s->index[i], j = num % N0, k = num / N0, kk, jj, num2;
+    cell_geo cg = geometry(s, num);
+#define ADD(c, q) NN(c, q) += g->Fn / cell_volume(s, c)
+    if (x1[i] < cg.cx) {
+      if (x2[i] < cg.cy) {
+        ADD(num, 0);
+        kk = k; jj = j - 1; if (jj >= 0) { num2 = kk * N0 + jj; ADD(num2, 1); }
+        kk = k - 1; jj = j; if (kk >= 0) { num2 = kk * N0 + jj; ADD(num2, 2); }
+        kk = k - 1; jj = j - 1; if (kk >= 0 && jj >= 0) { num2 = kk * N0 + jj; ADD(num2, 3); }
+      } else {
+        ADD(num, 2);
+        kk = k; jj = j - 1; if (jj >= 0) { num2 = kk * N0 + jj; ADD(num2, 3); }
+        kk = k + 1; jj = j; if (kk <= N1 - 1) { num2 = kk * N0 + jj; ADD(num2, 0); }
+        kk = k + 1; jj = j - 1; if (kk <= N1 - 1 && jj >= 0) { num2 = kk * N0 + jj; ADD(num2, 1); }
+      }
+    } else {
+      if (x2[i] < cg.cy) {
+        ADD(num, 1);
+        kk = k; jj = j + 1; if (jj <= N0 - 1) { num2 = kk * N0 + jj; ADD(num2, 0); }
+        kk = k - 1; jj = j; if (kk >= 0) { num2 = kk * N0 + jj; ADD(num2, 3); }
+        kk = k - 1; jj = j + 1; if (kk >= 0 && jj <= N0 - 1) { num2 = kk * N0 + jj; ADD(num2, 2); }
+      } else {
+        ADD(num, 3);
+        kk = k; jj = j + 1; if (jj <= N0 - 1) { num2 = kk * N0 + jj; ADD(num2, 2); }
+        kk = k + 1; jj = j; if (kk <= N1 - 1) { num2 = kk * N0 + jj; ADD(num2, 1); }
+        kk = k + 1; jj = j + 1; if (kk <= N1 - 1 && jj <= N0 - 1) { num2 = kk * N0 + jj; ADD(num2, 0); }
+      }
+    }
+#undef ADD
+  }
+  for (int jj = 0; jj < N0; ++jj) { int c = jj; NN(c, 0) = NN(c, 0) * 2.0; NN(c, 1) = NN(c, 1) * 2.0; }
+  for (int jj = 0; jj < N0; ++jj) { int c = (N1 - 1) * N0 + jj; NN(c, 2) = NN(c, 2) * 2.0; NN(c, 3) = NN(c, 3) * 2.0; }
+  for (int kk = 0; kk < N1; ++kk) { int c = kk * N0; NN(c, 0) = NN(c, 0) * 2.0; NN(c, 2) = NN(c, 2) * 2.0; }
+  for (int kk = 0; kk < N1; ++kk) { int c = kk * N0 + N0 - 1; NN(c, 1) = NN(c, 1) * 2.0; NN(c, 3) = NN(c, 3) * 2.0; }
+}
+void orc_get_node_density(const orc_state* s, double* out) {
+  memcpy(out, s->nn, sizeof(double) * (size_t)s->C * 4);
+}
+
 /* ----------------------------------------------------------- lifecycle -- */
 orc_state* orc_create(const mcpm_config* cfg, int64_t n_particles) {
   orc_state* s = (orc_state*)calloc(1, sizeof(orc_state));
@@ -122,13 +198,14 @@ orc_state* orc_create(const mcpm_config* cfg, int64_t n_particles) {
   s->index = (int32_t*)calloc(n_particles > 0 ? n_particles : 1, sizeof(int32_t));
   s->inj = (double*)calloc(3 * (n_particles > 0 ? n_particles : 1), sizeof(double));
   s->xi = (double*)calloc(3 * (n_particles > 0 ? n_particles : 1), sizeof(double));
+  s->nn = (double*)calloc((size_t)s->C * 4, sizeof(double));
   return s;
 }
 
 void orc_destroy(orc_state* s) {
   if (!s) return;
   free(s->cell); free(s->cnt); free(s->off); free(s->list); free(s->index);
-  free(s->inj); free(s->xi); free(s);
+  free(s->inj); free(s->xi); free(s->nn); free(s);
 }
 
 int orc_num_cells(const orc_state* s) { return s->C; }
@@ -553,6 +630,7 @@ void orc_cell_update(orc_state* s, const double* x1, const double* x2,
                      const double* U1, const double* U2, const double* U3,
                      int32_t* index) {
   bin_particles(s, x1, x2);
+  if (x1) node_density(s, x1, x2);
   if (index) memcpy(index, s->index, sizeof(int32_t) * (size_t)s->N);
   moments(s, U1, U2, U3);
   lambda_cells(s);
@@ -893,6 +971,240 @@ void orc_long_range(orc_state* s, double* U2) {
   free(V);
 }
 
+
+/* ---------------------------------------------------- 2-D long range -- */
+/* shape-function derivatives of the bilinear element, src/FEM.cpp:22-49 */
+static double dNxi(int i, double xi, double eta) {
+  (void)xi;
+  if (i == 0) return eta - 1.0;
+  if (i == 1) return 1.0 - eta;
+  if (i == 2) return -eta;
+  return eta;
+}
+static double dNeta(int i, double xi, double eta) {
+  (void)eta;
+  if (i == 0) return xi - 1.0;
+  if (i == 1) return -xi;
+  if (i == 2) return -xi + 1;
+  return xi;
+}
+
+/* r, phi, theta quadrature of the 2-D routines: GL(npts) on [a, b] x
+   [0, 2 pi] x [0, pi] (src/FEM.cpp:352-371, :657-671) */
+typedef struct {
+  int n;
+  double rr[100], dr[100], ph[100], dph[100], th[100], dth[100];
+  double cph[100], sph[100], sth[100];
+} sph_quad;
+static void sph_quad_make(sph_quad* q, int npts, double a, double b) {
+  double xi[100], wi[100];
+  double pi = acos(-1.0);
+  orc_gl_table(npts, xi, wi);
+  q->n = npts;
+  double cc = 0.0, dd = 2 * pi, ee = 0.0, ff = pi;
+  for (int i = 0; i < npts; ++i) {
+    q->rr[i] = (b - a) / 2.0 * xi[i] + (a + b) / 2.0; q->dr[i] = wi[i] * (b - a) / 2.0;
+    q->ph[i] = (dd - cc) / 2.0 * xi[i] + (cc + dd) / 2.0; q->dph[i] = wi[i] * (dd - cc) / 2.0;
+    q->th[i] = (ff - ee) / 2.0 * xi[i] + (ff + ee) / 2.0; q->dth[i] = wi[i] * (ff - ee) / 2.0;
+  }
+  for (int i = 0; i < npts; ++i) { q->cph[i] = cos(q->ph[i]); q->sph[i] = sin(q->ph[i]); q->sth[i] = sin(q->th[i]); }
+}
+/* vlasov_taking_the_integral_2D (src/FEM.cpp:158-202, kind 1) and
+   Compute_SP_using_Green_Function (:203-247, kind 3): the potential at
+   (xx, yy) from the cell densities, points outside the box taking the
+   density of the nearest edge cell. */
+static double sphere_integral(const orc_state* s, const sph_quad* q, int kind, double xx, double yy) {
+  const mcpm_config* g = &s->cfg;
+  double pi = acos(-1);
+  double V = 0.0;
+  for (int i = 0; i < q->n; ++i) {
+    double radial_part = kind == 1 ? pow(g->sigma / q->rr[i], 6.0) * q->rr[i] * q->rr[i] * q->dr[i]
+                                   : exp(-g->bst * q->rr[i]) / (4.0 * pi) * q->rr[i] * q->dr[i];
+    for (int ii = 0; ii < q->n; ++ii) {
+      for (int iii = 0; iii < q->n; ++iii) {
+        double x = xx + q->rr[i] * q->cph[ii] * q->sth[iii];
+        double y = yy + q->rr[i] * q->sph[ii] * q->sth[iii];
+        int j = (int)floor(x / s->dx);
+        int k = (int)floor(y / s->dy);
+        if (j < 0) j = 0; else if (j > s->N0 - 1) j = s->N0 - 1;
+        if (k < 0) k = 0; else if (k > s->N1 - 1) k = s->N1 - 1;
+        double n = CELL(s, k * s->N0 + j, MCPM_CF_N);
+        V += radial_part * n * q->dph[ii] * q->sth[iii] * q->dth[iii];
+      }
+    }
+  }
+  return V;
+}
+/* the cell and corner through which the node loops of src/FEM.cpp:511-545,
+   :675-700 reach node (i, j) */
+static void node_cell(const orc_state* s, int i, int j, int* num, int* k) {
+  int ii = i, jj = j;
+  *k = 0;
+  if (i == s->N0) { ii = i - 1; jj = j; *k = 1; }
+  if (j == s->N1) { ii = i; jj = j - 1; *k = 2; }
+  if (i == s->N0 && j == s->N1) { ii = i - 1; jj = j - 1; *k = 3; }
+  *num = jj * s->N0 + ii;
+}
+
+/* compute_Vlasov_2D node potentials, src/FEM.cpp:613-701: GL(100)^3 over
+   r in [sigma, 3 sigma] at every node */
+void orc_vlasov2d_nodes(orc_state* s, double* V) {
+  sph_quad q;
+  sph_quad_make(&q, 100, 1.0 * s->cfg.sigma, 3.0 * s->cfg.sigma);
+  for (int j = 0; j < s->N1 + 1; ++j)
+    for (int i = 0; i < s->N0 + 1; ++i) {
+      int num, k;
+      node_cell(s, i, j, &num, &k);
+      cell_geo cg = geometry(s, num);
+      V[j * (s->N0 + 1) + i] = sphere_integral(s, &q, 1, cg.xn[k], cg.yn[k]);
+    }
+}
+
+/* dense LU with partial pivoting: the solve that stands in for PARDISO
+   (src/solver_pardiso.cpp:33-158, MKL, not available) */
+static void dense_lu_solve(double* A, double* r, int n, double* x) {
+  for (int k = 0; k < n; ++k) {
+    int piv = k;
+    for (int i = k + 1; i < n; ++i)
+      if (fabs(A[(size_t)i * n + k]) > fabs(A[(size_t)piv * n + k])) piv = i;
+    if (piv != k) {
+      for (int j = 0; j < n; ++j) { double t = A[(size_t)k * n + j]; A[(size_t)k * n + j] = A[(size_t)piv * n + j]; A[(size_t)piv * n + j] = t; }
+      double t = r[k]; r[k] = r[piv]; r[piv] = t;
+    }
+    for (int i = k + 1; i < n; ++i) {
+      double f = A[(size_t)i * n + k] / A[(size_t)k * n + k];
+      if (f == 0.0) continue;
+      for (int j = k; j < n; ++j) A[(size_t)i * n + j] -= f * A[(size_t)k * n + j];
+      r[i] -= f * r[k];
+    }
+  }
+  for (int i = n - 1; i >= 0; --i) {
+    double sm = r[i];
+    for (int j = i + 1; j < n; ++j) sm -= A[(size_t)i * n + j] * x[j];
+    x[i] = sm / A[(size_t)i * n + i];
+  }
+}
+
+/* compute_SP_2D node potentials, src/FEM.cpp:249-610: bilinear FEM of
+   -lap V + bst^2 V = n_n with the Green's-function values on the walls
+   (GL(50)^3 over r in [0, 3 sigma]), minus the analytic near-field part.
+   Dense; for small grids only. */
+void orc_sp2d_nodes(orc_state* s, double* x) {
+  const mcpm_config* g = &s->cfg;
+  const int N0 = s->N0, N1 = s->N1, nn = (N0 + 1) * (N1 + 1), nc = s->C;
+  static const double dudv[4][4] = {{2.0 / 3.0, -1.0 / 6.0, -1.0 / 6.0, -1.0 / 3.0},
+                                    {-1.0 / 6.0, 2.0 / 3.0, -1.0 / 3.0, -1.0 / 6.0},
+                                    {-1.0 / 6.0, -1.0 / 3.0, 2.0 / 3.0, -1.0 / 6.0},
+                                    {-1.0 / 3.0, -1.0 / 6.0, -1.0 / 6.0, 2.0 / 3.0}};
+  static const double uv[4][4] = {{1.0 / 9.0, 1.0 / 18.0, 1.0 / 18.0, 1.0 / 36.0},
+                                  {1.0 / 18.0, 1.0 / 9.0, 1.0 / 36.0, 1.0 / 18.0},
+                                  {1.0 / 18.0, 1.0 / 36.0, 1.0 / 9.0, 1.0 / 18.0},
+                                  {1.0 / 36.0, 1.0 / 18.0, 1.0 / 18.0, 1.0 / 9.0}};
+  double* A = (double*)calloc((size_t)nn * nn, sizeof(double));
+  double* b = (double*)calloc(nn, sizeof(double));
+  double lambda2 = pow(g->bst, 2.0);
+  for (int i = 0; i < nn; ++i) x[i] = 0.0;
+  for (int num = 0; num < nc; ++num) {
+    int id[4];
+    double v[4];
+    node_ids(s, num, id);
+    double vol = cell_volume(s, num);
+    for (int i = 0; i < 4; ++i) {
+      v[i] = 0.0;
+      for (int j = 0; j < 4; ++j) v[i] += NN(num, j) * uv[i][j];
+    }
+    for (int i = 0; i < 4; ++i) {
+      for (int j = 0; j < 4; ++j) {
+        A[(size_t)id[i] * nn + id[j]] += dudv[i][j];
+        A[(size_t)id[i] * nn + id[j]] += lambda2 * uv[i][j] * vol;
+      }
+      b[id[i]] += v[i] * vol;
+    }
+  }
+  sph_quad q;
+  sph_quad_make(&q, 50, 0.0, 3.0 * g->sigma);
+  /* Dirichlet rows: lower, upper, left, right wall (:396-455) */
+  const int walls[4][2] = {{0, 1}, {2, 3}, {0, 2}, {1, 3}};
+  for (int w = 0; w < 4; ++w) {
+    int cnt = w < 2 ? N0 : N1;
+    for (int jj = 0; jj < cnt; ++jj) {
+      int num = w == 0 ? jj : (w == 1 ? (N1 - 1) * N0 + jj : (w == 2 ? jj * N0 : jj * N0 + N0 - 1));
+      int id[4];
+      node_ids(s, num, id);
+      cell_geo cg = geometry(s, num);
+      for (int t = 0; t < 2; ++t) {
+        int k = walls[w][t], i = id[k];
+        for (int j = 0; j < nn; ++j) A[(size_t)i * nn + j] = 0.0;
+        A[(size_t)i * nn + i] = 1.0;
+        b[i] = sphere_integral(s, &q, 3, cg.xn[k], cg.yn[k]);
+      }
+    }
+  }
+  dense_lu_solve(A, b, nn, x);
+  double dummy = 1.0 - (g->sigma * g->bst + 1.0) * exp(-g->bst * g->sigma);
+  dummy = dummy / g->bst / g->bst;
+  double dummy2 = (-1.0 / 6.0 * pow(g->bst, 3) * pow(g->sigma, 3) - 1.0 / 2.0 * pow(g->bst, 2) * pow(g->sigma, 2) -
+                   g->bst * g->sigma + exp(g->bst * g->sigma) - 1) *
+                  exp(-g->bst * g->sigma) / pow(g->bst, 4);
+  dummy2 = dummy2 / pow(s->dx, 2);
+  for (int j = 0; j < N1 + 1; ++j) {
+    for (int i = 0; i < N0 + 1; ++i) {
+      int id = j * (N0 + 1) + i, ii = i, jj = j, k = 0;
+      int ipm[4] = {0, -1, 0, 0}, jpm[4] = {0, 0, 0, -1}, kpm[4] = {1, 0, 2, 0};
+      if (i == N0) { ii = i - 1; jj = j; k = 1; kpm[0] = k; }
+      if (j == N1) { ii = i; jj = j - 1; k = 2; kpm[2] = k; }
+      if (i == N0 && j == N1) { ii = i - 1; jj = j - 1; k = 3; kpm[0] = k; kpm[2] = k; }
+      if (i == 0) { ipm[1] = 0; jpm[1] = 0; kpm[1] = 0; }
+      if (j == 0) { ipm[3] = 0; jpm[3] = 0; kpm[3] = 0; }
+      int num = jj * N0 + ii;
+      double d2 = NN(num, k) * dummy;
+      double d3 = -4.0 * NN(num, k) * dummy2;
+      for (int ll = 0; ll < 4; ++ll) {
+        num = (jj + jpm[ll]) * N0 + ii + ipm[ll];
+        d3 += NN(num, kpm[ll]) * dummy2;
+      }
+      x[id] += -(d2 + d3);
+    }
+  }
+  free(A); free(b);
+}
+
+/* the kick of compute_Vlasov_2D / compute_SP_2D (src/FEM.cpp:567-578,
+   :703-714): bilinear gradient of the node potential at the particle */
+static void kick_2d(orc_state* s, const double* V, double coef, const double* x1, const double* x2,
+                    double* U1, double* U2) {
+  const mcpm_config* g = &s->cfg;
+  for (int64_t i = 0; i < s->N; ++i) {
+    int num = s->index[i], id[4];
+    cell_geo cg = geometry(s, num);
+    node_ids(s, num, id);
+    double xi = (x1[i] - cg.xn[0]) / cg.dxc;
+    double eta = (x2[i] - cg.yn[0]) / cg.dyc;
+    double F1 = 0.0, F2 = 0.0;
+    for (int j = 0; j < 4; ++j) {
+      F1 += dNxi(j, xi, eta) * V[id[j]];
+      F2 += dNeta(j, xi, eta) * V[id[j]];
+    }
+    F1 = F1 / g->m * coef / cg.dxc; F2 = F2 / g->m * coef / cg.dyc;
+    U1[i] = U1[i] - F1 * g->dt;
+    U2[i] = U2[i] - F2 * g->dt;
+  }
+}
+
+/* long-range dispatch for 2-D boxes: compute_Vlasov_2D (long_range 1) or
+   compute_SP_2D (long_range 3), src/Main_Functions.cpp:1618-1663.  The
+   reference reaches them for its 2-D injection problem; here any 2-D box. */
+void orc_long_range_2d(orc_state* s, const double* x1, const double* x2, double* U1, double* U2, double* V) {
+  const mcpm_config* g = &s->cfg;
+  if (g->long_range != MCPM_LR_DIRECT && g->long_range != MCPM_LR_SCREENED_POISSON) return;
+  int nn = (s->N0 + 1) * (s->N1 + 1);
+  double* W = V ? V : (double*)malloc(sizeof(double) * nn);
+  if (g->long_range == MCPM_LR_DIRECT) orc_vlasov2d_nodes(s, W);
+  else orc_sp2d_nodes(s, W);
+  kick_2d(s, W, g->long_range == MCPM_LR_DIRECT ? g->phi : g->ast, x1, x2, U1, U2);
+  if (!V) free(W);
+}
+
 /* ------------------------------------------------- DFP_extra_streaming -- */
 /* src/Fokker_Planck.cpp:904-946, including its use of U_space[1] in the x1
    heat-flux term (:936). */
@@ -1178,7 +1490,8 @@ void orc_step(orc_state* s, double* x1, double* x2, double* x1_old,
   } else if (m == MCPM_MODEL_ESMC) {
     orc_esmc(s, x1, x2, U1, U2, U3);
   }
-  orc_long_range(s, U2);
+  if (s->cfg.direction[0] == 1) orc_long_range_2d(s, x1, x2, U1, U2, NULL);
+  else orc_long_range(s, U2);
   if (m == MCPM_MODEL_FP_DENSE) orc_dfp_extra_streaming(s, U1, U2, U3, x1, x2);
   orc_apply_bc(s, 0, x1, x2, x1_old, x2_old, U1, U2, U3);
   orc_store_old_positions(s, x1, x2, x1_old, x2_old);

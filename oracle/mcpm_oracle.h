@@ -79,6 +79,13 @@ void orc_gauss_jordan(double* A /* n*n row-major, destroyed */, double* rhs,
 void orc_gl_table(int npts, double* nodes, double* weights);
 void orc_vlasov_face_potential(orc_state* s, double* V /* N1+1 */);
 void orc_poisson_faces(orc_state* s, double* x /* N1+1 */);
+/* 2-D long range: node potentials ((N0+1)(N1+1), node id j (N0+1) + i) and
+   the full dispatch (V may be NULL); nodal densities [C][4] */
+void orc_get_node_density(const orc_state* s, double* out);
+void orc_vlasov2d_nodes(orc_state* s, double* V);
+void orc_sp2d_nodes(orc_state* s, double* V);
+void orc_long_range_2d(orc_state* s, const double* x1, const double* x2,
+                       double* U1, double* U2, double* V);
 
 #ifdef __cplusplus
 }

@@ -70,6 +70,10 @@ def _load_oracle():
         "orc_gl_table": (None, [C.c_int, dp, dp]),
         "orc_vlasov_face_potential": (None, [vp, dp]),
         "orc_poisson_faces": (None, [vp, dp]),
+        "orc_get_node_density": (None, [vp, dp]),
+        "orc_vlasov2d_nodes": (None, [vp, dp]),
+        "orc_sp2d_nodes": (None, [vp, dp]),
+        "orc_long_range_2d": (None, [vp, dp, dp, dp, dp, dp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -174,7 +178,25 @@ class Oracle:
         self.L.orc_esmc(self.h, _dp(s.x1), _dp(s.x2), _dp(s.U1), _dp(s.U2), _dp(s.U3))
 
     def long_range(self):
-        self.L.orc_long_range(self.h, _dp(self.s.U2))
+        """velocity_update's long-range kick: the 1-D face paths, or the 2-D
+        node paths when the box is 2-D (returns the node potential then)."""
+        s = self.s
+        if self.cfg.direction[0] == 1:
+            V = np.empty((self.cfg.n_cells[0] + 1) * (self.cfg.n_cells[1] + 1))
+            self.L.orc_long_range_2d(self.h, _dp(s.x1), _dp(s.x2), _dp(s.U1), _dp(s.U2), _dp(V))
+            return V
+        self.L.orc_long_range(self.h, _dp(s.U2))
+        return None
+
+    def node_density(self):
+        out = np.empty((self.C, 4))
+        self.L.orc_get_node_density(self.h, _dp(out))
+        return out
+
+    def node_potential(self, mode):
+        V = np.empty((self.cfg.n_cells[0] + 1) * (self.cfg.n_cells[1] + 1))
+        (self.L.orc_vlasov2d_nodes if mode == 1 else self.L.orc_sp2d_nodes)(self.h, _dp(V))
+        return V
 
     def dfp_extra_streaming(self):
         s = self.s
@@ -255,6 +277,8 @@ def ref_lib(build=True):
         "ref_esmc": (None, [vp, dp, dp, dp, dp, dp, ip]),
         "ref_init_omega_max": (None, [vp]),
         "ref_get_cells": (None, [vp, dp]),
+        "ref_long_range_2d": (None, [vp, dp, dp, dp, dp, ip]),
+        "ref_get_node_density": (None, [vp, dp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -309,7 +333,15 @@ class Reference:
 
     def long_range(self):
         s = self.s
-        self.L.ref_long_range(self.h, _dp(s.x1), _dp(s.x2), _dp(s.U2), _ip(s.index))
+        if self.cfg.direction[0] == 1:
+            self.L.ref_long_range_2d(self.h, _dp(s.x1), _dp(s.x2), _dp(s.U1), _dp(s.U2), _ip(s.index))
+        else:
+            self.L.ref_long_range(self.h, _dp(s.x1), _dp(s.x2), _dp(s.U2), _ip(s.index))
+
+    def node_density(self):
+        out = np.empty((self.C, 4))
+        self.L.ref_get_node_density(self.h, _dp(out))
+        return out
 
     def dfp_extra_streaming(self):
         s = self.s

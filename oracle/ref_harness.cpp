@@ -183,6 +183,22 @@ void ref_long_range(void* h, double* x1, double* x2, double* U2, int* index) {
   else if (r->gas.long_range == 3) poisson_solver(U2, x1, x2, r->x3.data(), &r->gas, &r->box, r->cells, index);
 }
 
+// the 2-D routines, src/FEM.cpp:249-726 (the reference calls them for its
+// 2-D injection problem, src/Main_Functions.cpp:1622, :1656)
+void ref_long_range_2d(void* h, double* x1, double* x2, double* U1, double* U2, int* index) {
+  Quiet q;
+  Ref* r = (Ref*)h;
+  if (r->gas.long_range == 1) compute_Vlasov_2D(&r->gas, &r->box, r->cells, x1, x2, U1, U2, index);
+  else if (r->gas.long_range == 3) compute_SP_2D(&r->gas, &r->box, r->cells, x1, x2, U1, U2, index);
+}
+
+// nodal densities n_n of the last cell_update, [C][4]
+void ref_get_node_density(void* h, double* out) {
+  Ref* r = (Ref*)h;
+  for (int c = 0; c < r->C; ++c)
+    for (int k = 0; k < 4; ++k) out[(size_t)c * 4 + k] = r->cells[c].n_n[k];
+}
+
 void ref_dfp_extra_streaming(void* h, double* U1, double* U2, double* U3, double* x1, double* x2, int* index) {
   Quiet q;
   Ref* r = (Ref*)h;
