@@ -18,6 +18,9 @@
  *     Collision_ESMC_new3  src/collisions.cpp:583             (model ESMC)
  *     vlasov_taking_the_integral src/Main_Functions.cpp:3582  (long_range 1, 1-D)
  *     poisson_solver       src/Main_Functions.cpp:3285        (long_range 3, 1-D)
+ *     compute_Vlasov_2D    src/FEM.cpp:613                    (long_range 1, 2-D)
+ *     compute_SP_2D        src/FEM.cpp:249                    (long_range 3, 2-D)
+ *   cells[].n_n (cell_update) src/Main_Functions.cpp:2268   mcpm_get_node_density
  *   DFP_extra_streaming  src/Fokker_Planck.cpp:904          mcpm_dfp_extra_streaming
  *   apply_BC             src/Main_Functions.cpp:1451        mcpm_apply_bc
  *   store_old_positions  src/Main_Functions.cpp:5736        mcpm_store_old_positions
@@ -205,7 +208,7 @@ int mcpm_end_step(mcpm_session* s);
 /* n_steps iterations of the main loop body (src/main.cpp:389-669) for the
    in-scope models: cell_update, random_generator, velocity_update,
    DFP_extra_streaming, apply_BC, store_old_positions, stream_particles,
-   apply_BC.  Kernels are fused and the step is replayed as a CUDA graph. */
+   apply_BC.  The particle-side stages run fused in one kernel per step. */
 int mcpm_step(mcpm_session* s, int32_t n_steps);
 
 /* ---- test and diagnostic hooks ---------------------------------------- */
@@ -219,6 +222,17 @@ int mcpm_set_rng(mcpm_session* s, int32_t mode);
 int mcpm_get_cells(mcpm_session* s, double* out);
 /* Cell index of every particle, in particle-id order (cell_update's index[]). */
 int mcpm_get_index(mcpm_session* s, int32_t* index);
+/* Nodal densities n_n of the last cell_update, [C][4] doubles (cell-major,
+   corner 0 lower left, 1 lower right, 2 upper left, 3 upper right), as
+   cell_update deposits them (src/Main_Functions.cpp:2268-2364).  Computed
+   only by sessions whose Vlasov force is the 2-D screened-Poisson one
+   (their only consumer, src/FEM.cpp:285-288); MCPM_ERR_STATE otherwise. */
+int mcpm_get_node_density(mcpm_session* s, double* out);
+/* Node potential of the last 2-D Vlasov force evaluation, (N0+1)(N1+1)
+   doubles, node (i, j) at j (N0+1) + i: the direct quadrature
+   (compute_Vlasov_2D, src/FEM.cpp:675-701) or the screened-Poisson FEM
+   solution after the near-field correction (compute_SP_2D, :458-546). */
+int mcpm_get_node_potential(mcpm_session* s, double* out);
 /* Whitened normals last produced by random_generator, per particle id. */
 int mcpm_get_normals(mcpm_session* s, double* xi1, double* xi2, double* xi3);
 int32_t mcpm_get_step(const mcpm_session* s);

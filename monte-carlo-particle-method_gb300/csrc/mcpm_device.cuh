@@ -320,4 +320,13 @@ __device__ __forceinline__ void count_key(int32_t* cnt, int key, bool active) {
   if ((int)(threadIdx.x & 31) == leader) atomicAdd(&cnt[key], __popc(peers));
 }
 
+// volume of cell c exactly as make_cells builds it, src/myIO.cpp:1456-1465
+__device__ __forceinline__ double cell_volume(int c, const DevConsts& k) {
+  int j = c % k.N0, kk = c / k.N0;
+  double d0 = (double)j * k.dx, d1 = (double)(j + 1) * k.dx;
+  double d2 = (double)kk * k.dy, d3 = (double)(kk + 1) * k.dy;
+  double d4 = 0.0 * k.dz, d5 = 1.0 * k.dz;
+  return (d1 - d0) * (d3 - d2) * (d5 - d4);
+}
+
 }  // namespace mcpm

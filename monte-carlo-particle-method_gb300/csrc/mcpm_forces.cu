@@ -311,6 +311,7 @@ __global__ void __launch_bounds__(1024) k_long_range_1d(DevConsts k, double* cel
 int launch_long_range(Session& s) {
   const int mode = s.cfg.long_range;
   if (mode != MCPM_LR_DIRECT && mode != MCPM_LR_SCREENED_POISSON) return 0;
+  if (s.k.lr2d) return launch_long_range_2d(s);
   const LRTab* t = reinterpret_cast<const LRTab*>(s.lr_host);
   const double coef = mode == MCPM_LR_DIRECT ? s.cfg.phi : s.cfg.ast;
   k_long_range_1d<<<1, 1024, 2 * t->nf * sizeof(double), s.stream>>>(

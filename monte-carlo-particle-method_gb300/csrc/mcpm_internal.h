@@ -31,8 +31,12 @@ enum {
   PF_AL0, PF_AL1, PF_AL2, PF_AL3, PF_AL4, PF_AL5, PF_BE0, PF_BE1, PF_GST,
   PF_HQ0, PF_HQ1,          // M3[0]+M3[3]+M3[5], M3[1]+M3[6]+M3[8] (DFP heat-flux terms)
   PF_PH0, PF_PH1, PF_F2DT, PF_N,
-  PF_STRIDE = 36
+  // 2-D Vlasov kick: U1 -= LA1 + LB1 eta, U2 -= LA2 + LB2 xi (xi, eta the
+  // particle's bilinear coordinates in its cell), one float4 of its own
+  PF_LA1 = 36, PF_LB1, PF_LA2, PF_LB2,
+  PF_STRIDE = 40
 };
+static_assert(PF_N < PF_LA1 && PF_LA1 % 4 == 0 && PF_STRIDE % 4 == 0, "packed record: float4 groups");
 
 // Stages of the fused per-cell particle pass (update kernel).
 enum : uint32_t {
@@ -63,6 +67,10 @@ struct DevConsts {
   uint64_t seed;
   // wall offset of the diffuse walls, max(1e-15, 4 ulp(Len)) per direction
   double eps_x, eps_y;
+  // 2-D long range: 1 when the Vlasov force acts on the node grid of a 2-D
+  // box; its coefficient (phi for the direct path, ast for screened Poisson)
+  int lr2d;
+  double lr_coef;
   // float copies for the FP32 kernels
   float f_dx, f_dy, f_L0, f_L1, f_dt, f_sigma, f_m, f_kb, f_Tw[4], f_Uw[4], f_idx, f_idy, f_eps_x, f_eps_y;
 };
@@ -85,6 +93,8 @@ struct Tuning {
   int grid_mom;     // persistent grid sizes
   int grid_upd;
 };
+
+struct LR2D;  // 2-D long-range tables and buffers (mcpm_lr2d.cu)
 
 struct Session {
   mcpm_config cfg{};
@@ -115,6 +125,8 @@ struct Session {
   double* faces = nullptr;      // [4][N1+1] long-range face scratch
   void* lr_tab = nullptr;       // long-range tables (stencil / PCR coefficients)
   alignas(16) char lr_host[160];  // the kernel's view of lr_tab
+  LR2D* lr2d = nullptr;         // 2-D long range (node grid), when configured
+  bool nodes_valid = false;     // nodal densities describe the last cell_update
   uint32_t* status = nullptr;
   cudaStream_t stream = nullptr;
   int step = 0;
@@ -152,6 +164,15 @@ int launch_update(Session& s, uint32_t stages, int bc_call_base);
 int launch_esmc(Session& s);
 int launch_long_range(Session& s);
 int launch_init_omega(Session& s);
+// 2-D long range (mcpm_lr2d.cu): set-up / release, the nodal deposit of
+// cell_update, the node potential + kick coefficients, device views
+int lr2d_setup(Session& s);
+void lr2d_free(Session& s);
+int launch_node_density(Session& s);
+int launch_long_range_2d(Session& s);
+const double* lr2d_potential(const Session& s);
+const double* lr2d_node_density(const Session& s);
+int lr2d_num_nodes(const Session& s);
 int launch_convert_in(Session& s, int64_t n);
 int launch_convert_out(Session& s, int64_t n);
 

@@ -233,15 +233,6 @@ struct CellRef {
   __device__ __forceinline__ double operator()(int f, int c) const { return cell[(size_t)f * C + c]; }
 };
 
-// volume of cell c exactly as make_cells builds it, src/myIO.cpp:1456-1465
-__device__ __forceinline__ double cell_volume(int c, const DevConsts& k) {
-  int j = c % k.N0, kk = c / k.N0;
-  double d0 = (double)j * k.dx, d1 = (double)(j + 1) * k.dx;
-  double d2 = (double)kk * k.dy, d3 = (double)(kk + 1) * k.dy;
-  double d4 = 0.0 * k.dz, d5 = 1.0 * k.dz;
-  return (d1 - d0) * (d3 - d2) * (d5 - d4);
-}
-
 // persistent two-phase scheduler: block-sized cells first, then one warp per
 // small cell.  fn_big(c) is called by the whole block, fn_small(c) by a warp.
 template <typename FB, typename FS>
@@ -923,6 +914,7 @@ template <typename real> struct UpdArgs {
   int step, bin_step, rng_mode, bc_call_base;
   uint32_t stages;
   int wcap, bcap;
+  const double* Vn;  // node potential of the 2-D Vlasov force (FP64 path)
 };
 
 template <typename real>
@@ -941,6 +933,10 @@ __device__ __forceinline__ void raw_normals(const UpdArgs<real>& a, int64_t p, r
 template <typename real> struct CellK {
   real us0, us1, us2, A1, A2, A3, eq, lam, c[6], g[3], q[3];
   real al[6], be0, be1, gst, m3_0, m3_3, m3_5, m3_1, m3_6, m3_8, hq0, hq1, ph0, ph1, f2dt;
+  // 2-D Vlasov kick: FP32 the packed coefficients (la1 lb1 la2 lb2), FP64
+  // the four node potentials and the cell's corner / size (v, xn0 yn0 dxc dyc)
+  real l2[4];
+  double v[4], xn0, yn0, dxc, dyc;
 };
 template <typename real>
 __device__ __forceinline__ void load_cellk(CellK<real>& K, int c, const UpdArgs<real>& a, uint32_t st) {
@@ -948,7 +944,11 @@ __device__ __forceinline__ void load_cellk(CellK<real>& K, int c, const UpdArgs<
     float pf[PF_STRIDE];
     const float4* src = reinterpret_cast<const float4*>(a.pcell + (size_t)c * PF_STRIDE);
 #pragma unroll
-    for (int j = 0; j < PF_STRIDE / 4; ++j) reinterpret_cast<float4*>(pf)[j] = __ldg(src + j);
+    for (int j = 0; j < PF_LA1 / 4; ++j) reinterpret_cast<float4*>(pf)[j] = __ldg(src + j);
+    if ((st & ST_LR) && a.k.lr2d) {
+      float4 l = __ldg(src + PF_LA1 / 4);
+      K.l2[0] = l.x; K.l2[1] = l.y; K.l2[2] = l.z; K.l2[3] = l.w;
+    }
     K.us0 = pf[PF_US0]; K.us1 = pf[PF_US1]; K.us2 = pf[PF_US2];
     K.A1 = pf[PF_A1]; K.A2 = pf[PF_A2]; K.A3 = pf[PF_A3]; K.eq = pf[PF_EQ]; K.lam = pf[PF_LAM];
 #pragma unroll
@@ -972,6 +972,17 @@ __device__ __forceinline__ void load_cellk(CellK<real>& K, int c, const UpdArgs<
     K.hq0 = K.hq1 = 0.0;
     K.ph0 = R(MCPM_CF_PHI + 0, c); K.ph1 = R(MCPM_CF_PHI + 1, c);
     K.f2dt = (st & ST_LR) ? R(MCPM_CF_F2, c) * a.k.dt : 0.0;
+    if ((st & ST_LR) && a.k.lr2d) {
+      // cells[num].x_n[0], y_n[0], dx, dy as make_cells builds them (src/myIO.cpp:1456-1479)
+      const int j = c % a.k.N0, kk = c / a.k.N0;
+      double d0 = (double)j * a.k.dx, d1 = (double)(j + 1) * a.k.dx;
+      double d2 = (double)kk * a.k.dy, d3 = (double)(kk + 1) * a.k.dy;
+      K.dxc = d1 - d0; K.dyc = d3 - d2;
+      K.xn0 = 0.5 * (d0 + d1) - K.dxc / 2.0;
+      K.yn0 = 0.5 * (d2 + d3) - K.dyc / 2.0;
+      const int id0 = kk * (a.k.N0 + 1) + j, id2 = id0 + a.k.N0 + 1;
+      K.v[0] = a.Vn[id0]; K.v[1] = a.Vn[id0 + 1]; K.v[2] = a.Vn[id2]; K.v[3] = a.Vn[id2 + 1];
+    }
   }
 }
 
@@ -1167,7 +1178,30 @@ __device__ void update_cell(int c, const UpdArgs<real>& a, real* xs, int xcap, A
           s.u1 = Us0; s.u2 = Us1; s.u3 = Us2;
         }
       }
-      if (st & ST_LR) s.u2 = s.u2 + F2dt;
+      if (st & ST_LR) {
+        if (k.lr2d) {
+          if constexpr (F32) {
+            // U -= grad(V) coef/m dt with the bilinear coordinates of the particle
+            const float xi = s.x1 * kc.idx - (float)(c % k.N0), eta = s.x2 * kc.idy - (float)(c / k.N0);
+            s.u1 = s.u1 - (K.l2[0] + K.l2[1] * eta);
+            s.u2 = s.u2 - (K.l2[2] + K.l2[3] * xi);
+          } else {
+            // src/FEM.cpp:703-714 in its order of operations
+            const double xi = (s.x1 - K.xn0) / K.dxc, eta = (s.x2 - K.yn0) / K.dyc;
+            double F1 = 0.0, Fy = 0.0;
+            F1 += (eta - 1.0) * K.v[0]; Fy += (xi - 1.0) * K.v[0];
+            F1 += (1.0 - eta) * K.v[1]; Fy += (-xi) * K.v[1];
+            F1 += (-eta) * K.v[2]; Fy += (-xi + 1) * K.v[2];
+            F1 += eta * K.v[3]; Fy += xi * K.v[3];
+            F1 = F1 / k.m * k.lr_coef / K.dxc;
+            Fy = Fy / k.m * k.lr_coef / K.dyc;
+            s.u1 = s.u1 - F1 * k.dt;
+            s.u2 = s.u2 - Fy * k.dt;
+          }
+        } else {
+          s.u2 = s.u2 + F2dt;
+        }
+      }
       if (st & ST_DFP) {
         real e = (s.u1 - Us0) * (s.u1 - Us0) + (s.u2 - Us1) * (s.u2 - Us1) + (s.u3 - Us2) * (s.u3 - Us2);
         if constexpr (!F32) {
@@ -1344,6 +1378,7 @@ template <typename real> static int update_impl(Session& s, uint32_t stages, int
   a.stages = stages;
   a.wcap = s.tune.wcap;
   a.bcap = s.tune.bcap;
+  a.Vn = lr2d_potential(s);
   size_t sm = update_smem<real>(s);
   if (stages == ST_FUSED_FP) k_update<real, ST_FUSED_FP><<<s.tune.grid_upd, 256, sm, s.stream>>>(a);
   else k_update<real, 0u><<<s.tune.grid_upd, 256, sm, s.stream>>>(a);

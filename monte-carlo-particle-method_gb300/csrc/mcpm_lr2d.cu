@@ -1,0 +1,545 @@
+// mcpm_lr2d.cu -- the Vlasov force of a 2-D box on the node grid.
+//
+// Reference: compute_Vlasov_2D (src/FEM.cpp:613-726, long_range 1) and
+// compute_SP_2D (src/FEM.cpp:249-610, long_range 3), reached from
+// velocity_update (src/Main_Functions.cpp:1618-1663), with the nodal
+// deposit n_n of cell_update (src/Main_Functions.cpp:2268-2364).
+//
+// Node (i, j), 0 <= i <= N0, 0 <= j <= N1, has id j (N0 + 1) + i and sits at
+// the corner of the cells around it; its coordinates are the ones make_cells
+// gives the cell corners (src/myIO.cpp:1456-1479), which are separable:
+// xx_i depends on the column only, yy_j on the row only.
+//
+// Both paths integrate the cell density n(x) over a sphere around a point by
+// a GL(q)^3 product rule in (r, phi, theta), looking up the cell of each
+// point with the box edges clamped.  Seen from any node the point with
+// offset (r cos phi sin theta, r sin phi sin theta) lands in the cell at a
+// fixed offset (dj, dk) from the node, except for points whose offset lies
+// within rounding distance of a cell face; so the integral is a fixed stencil
+// of per-offset weight sums, W[dk][dj], applied to the clamped densities.
+// The set-up checks every point whose offset is that close to a face against
+// each row and column the exact way the reference computes it, and records
+// per node the points whose cell differs (corrections the node kernels add).
+//
+// direct (long_range 1): V(node) = sum W n over GL(100)^3, r in [sigma,
+//   3 sigma], weight (sigma/r)^6 r^2 dr dphi sin(theta) dtheta.
+// screened Poisson (long_range 3): bilinear FEM of -lap V + bst^2 V = n_n on
+//   the node grid with Dirichlet rows on the walls holding the Green's-
+//   function potential (GL(50)^3, r in [0, 3 sigma], weight exp(-bst r)/(4 pi)
+//   r dr ...).  The interior operator is K (x) M + M (x) K + bst^2 vol M (x) M
+//   of the 1-D unit stiffness K = tridiag(-1, 2, -1) and mass
+//   M = tridiag(1/6, 2/3, 1/6) -- the reference assembles exactly these
+//   element matrices (src/FEM.cpp:50-106) -- so it is diagonalised by the
+//   discrete sine transform: U = S_y ((S_y B S_x) / mu) S_x with the
+//   orthonormal DST-I matrices S and mu_qp = kx_p my_q + mx_p ky_q +
+//   bst^2 vol mx_p my_q.  The reference solves the same system with PARDISO.
+//   Then the analytic near-field part is subtracted (src/FEM.cpp:491-546).
+// The kick (src/FEM.cpp:567-578, :703-714): U -= grad_bilinear(V) coef / m dt
+// with coef = phi (direct) or ast (screened Poisson), applied by the particle
+// pass (update kernel) from the node values (FP64) or from per-cell
+// coefficients packed here (FP32).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "mcpm_device.cuh"
+
+namespace mcpm {
+
+#define FULL 0xffffffffu
+
+struct LR2D {
+  int mode;                 // MCPM_LR_DIRECT or MCPM_LR_SCREENED_POISSON
+  int N0, N1, nn, nx, ny;   // cells per row / column, nodes, interior nodes per row / column
+  int R0lo, R0hi, R1lo, R1hi;  // stencil offsets dj in [R0lo, R0hi], dk in [R1lo, R1hi]
+  int sw;                   // stencil width R0hi - R0lo + 1
+  int n_exc;
+  double* W = nullptr;      // stencil [R1hi - R1lo + 1][sw]
+  int* exc_off = nullptr;   // [nn + 1] per-node range of correction points
+  int* exc_i = nullptr;     // [n_exc][4]: dj, dk the point's cell, dj, dk the stencil's
+  double* exc_w = nullptr;  // [n_exc]
+  double* V = nullptr;      // [nn] node potential
+  double* nnd = nullptr;    // [C][4] nodal densities n_n
+  int32_t* qc = nullptr;    // [C][4] particles per cell quadrant
+  double *Sx = nullptr, *Sy = nullptr, *mu = nullptr, *B = nullptr, *T = nullptr;
+  int* wall = nullptr;      // [n_wall] ids of the wall nodes
+  int n_wall;
+  size_t smem;              // dynamic shared memory of the node kernels
+};
+
+// ------------------------------------------------------------ geometry --
+// the corner coordinate of column i (row j) as make_cells builds the cells
+// (cells[num].x_n, src/myIO.cpp:1472-1479), from the cell left of / right of it
+__host__ __device__ inline double node_coord(int i, int N, double d) {
+  const int c = i < N ? i : N - 1;
+  double d0 = (double)c * d, d1 = (double)(c + 1) * d;
+  double dc = d1 - d0, cen = 0.5 * (d0 + d1);
+  return i < N ? cen - dc / 2.0 : cen + dc / 2.0;
+}
+__device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
+
+// ------------------------------------------------------------- kernels --
+// quadrant counts of cell_update's nodal deposit: particle on the left of
+// the cell centre and below it -> 0, right/below 1, left/above 2, right/above 3
+template <typename real>
+__global__ void k_quadrants(DevConsts k, const int32_t* off, const int32_t* cnt, const real* x1, const real* x2,
+                            int32_t* qc) {
+  const int lane = threadIdx.x & 31;
+  const int warps = (gridDim.x * blockDim.x) >> 5;
+  for (int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < k.C; c += warps) {
+    const int j = c % k.N0, kk = c / k.N0;
+    const double cx = 0.5 * ((double)j * k.dx + (double)(j + 1) * k.dx);
+    const double cy = 0.5 * ((double)kk * k.dy + (double)(kk + 1) * k.dy);
+    const int64_t s0 = off[c];
+    const int n = cnt[c];
+    int q[4] = {0, 0, 0, 0};
+    for (int i = lane; i - lane < n; i += 32) {
+      int quad = -1;
+      if (i < n) quad = ((double)x1[s0 + i] < cx ? 0 : 1) + ((double)x2[s0 + i] < cy ? 0 : 2);
+#pragma unroll
+      for (int t = 0; t < 4; ++t) q[t] += __popc(__ballot_sync(FULL, quad == t));
+    }
+    if (lane < 4) qc[(size_t)c * 4 + lane] = q[lane];
+  }
+}
+
+// n_n[c][slot]: the particles nearest to the slot's node, counted over every
+// cell sharing the node, each adding Fn/volume(c); wall nodes doubled per
+// wall (src/Main_Functions.cpp:2268-2364).  exact: the sum of equal terms in
+// sequence, as the reference accumulates it.
+__global__ void k_node_density(DevConsts k, const int32_t* qc, double* nnd, int exact) {
+  const int N0 = k.N0, N1 = k.N1;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < 4 * k.C; e += gridDim.x * blockDim.x) {
+    const int c = e >> 2, slot = e & 3;
+    const int j = c % N0, kk = c / N0;
+    const int ni = j + (slot & 1), nj = kk + (slot >> 1);  // the node
+    int count = 0;
+    // the cells around node (ni, nj) and the quadrant of each that is nearest to it
+    if (ni < N0 && nj < N1) count += qc[(size_t)(nj * N0 + ni) * 4 + 0];
+    if (ni > 0 && nj < N1) count += qc[(size_t)(nj * N0 + ni - 1) * 4 + 1];
+    if (ni < N0 && nj > 0) count += qc[(size_t)((nj - 1) * N0 + ni) * 4 + 2];
+    if (ni > 0 && nj > 0) count += qc[(size_t)((nj - 1) * N0 + ni - 1) * 4 + 3];
+    const double v = k.Fn / cell_volume(c, k);
+    double acc = 0.0;
+    if (exact) {
+      for (int t = 0; t < count; ++t) acc += v;
+    } else {
+      acc = (double)count * v;
+    }
+    if (kk == 0 && slot < 2) acc = acc * 2.0;
+    if (kk == N1 - 1 && slot >= 2) acc = acc * 2.0;
+    if (j == 0 && (slot & 1) == 0) acc = acc * 2.0;
+    if (j == N0 - 1 && (slot & 1) == 1) acc = acc * 2.0;
+    nnd[e] = acc;
+  }
+}
+
+// the sphere integral at node (i, j): the stencil on the clamped cell
+// densities plus the node's correction points
+__device__ __forceinline__ double node_integral(const LR2D& t, const double* W, const double* n, int i, int j,
+                                                int node) {
+  double v = 0.0;
+  const int N0 = t.N0, N1 = t.N1;
+  for (int dk = t.R1lo; dk <= t.R1hi; ++dk) {
+    const double* n_row = n + (size_t)clampi(j + dk, 0, N1 - 1) * N0;
+    const double* w_row = W + (size_t)(dk - t.R1lo) * t.sw - t.R0lo;
+    for (int dj = t.R0lo; dj <= t.R0hi; ++dj) v += w_row[dj] * n_row[clampi(i + dj, 0, N0 - 1)];
+  }
+  for (int e = t.exc_off[node]; e < t.exc_off[node + 1]; ++e) {
+    const int* x = t.exc_i + 4 * e;
+    double na = n[(size_t)clampi(j + x[1], 0, N1 - 1) * N0 + clampi(i + x[0], 0, N0 - 1)];
+    double nc = n[(size_t)clampi(j + x[3], 0, N1 - 1) * N0 + clampi(i + x[2], 0, N0 - 1)];
+    v += t.exc_w[e] * (na - nc);
+  }
+  return v;
+}
+
+// direct path: every node; screened Poisson: the wall nodes (their
+// Green's-function values, stored in V until the finish kernel)
+__global__ void k_node_potential(LR2D t, const double* n, int walls_only) {
+  extern __shared__ double Ws[];
+  const int nw = (t.R1hi - t.R1lo + 1) * t.sw;
+  for (int q = threadIdx.x; q < nw; q += blockDim.x) Ws[q] = t.W[q];
+  __syncthreads();
+  const int total = walls_only ? t.n_wall : t.nn;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
+    const int node = walls_only ? t.wall[e] : e;
+    const int i = node % (t.N0 + 1), j = node / (t.N0 + 1);
+    t.V[node] = node_integral(t, Ws, n, i, j, node);
+  }
+}
+
+// element matrices of compute_SP_2D (src/FEM.cpp:50-106)
+__constant__ double c_dudv[4][4] = {{2.0 / 3.0, -1.0 / 6.0, -1.0 / 6.0, -1.0 / 3.0},
+                                    {-1.0 / 6.0, 2.0 / 3.0, -1.0 / 3.0, -1.0 / 6.0},
+                                    {-1.0 / 6.0, -1.0 / 3.0, 2.0 / 3.0, -1.0 / 6.0},
+                                    {-1.0 / 3.0, -1.0 / 6.0, -1.0 / 6.0, 2.0 / 3.0}};
+__constant__ double c_uv[4][4] = {{1.0 / 9.0, 1.0 / 18.0, 1.0 / 18.0, 1.0 / 36.0},
+                                  {1.0 / 18.0, 1.0 / 9.0, 1.0 / 36.0, 1.0 / 18.0},
+                                  {1.0 / 18.0, 1.0 / 36.0, 1.0 / 9.0, 1.0 / 18.0},
+                                  {1.0 / 36.0, 1.0 / 18.0, 1.0 / 18.0, 1.0 / 9.0}};
+
+// right-hand side of the interior rows: the load vector sum_cells (uv n_n)
+// vol in cell order (src/FEM.cpp:276-300), minus the columns of the wall
+// nodes times their Dirichlet values (the wall rows are identities)
+__global__ void k_sp_rhs(LR2D t, DevConsts k) {
+  const int nx = t.nx, ny = t.ny, N0 = t.N0;
+  const double lambda2 = k.bst * k.bst;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < nx * ny; e += gridDim.x * blockDim.x) {
+    const int i = e % nx + 1, j = e / nx + 1;  // interior node
+    double b = 0.0, elim = 0.0;
+    // cells (i-1, j-1), (i, j-1), (i-1, j), (i, j): the node is their corner 3, 2, 1, 0
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int ci = i - 1 + (q & 1), cj = j - 1 + (q >> 1), slot = 3 - q;
+      const int c = cj * N0 + ci;
+      const double vol = cell_volume(c, k);
+      const double* nn = t.nnd + (size_t)c * 4;
+      double v = 0.0;
+      for (int l = 0; l < 4; ++l) v += nn[l] * c_uv[slot][l];
+      b += v * vol;
+      for (int l = 0; l < 4; ++l) {
+        const int gi = ci + (l & 1), gj = cj + (l >> 1);
+        if (gi == 0 || gi == N0 || gj == 0 || gj == t.N1) {
+          const double a = c_dudv[slot][l] + lambda2 * c_uv[slot][l] * vol;
+          elim += a * t.V[gj * (N0 + 1) + gi];
+        }
+      }
+    }
+    t.B[e] = b - elim;
+  }
+}
+
+// C[M][N] = A[M][K] B[K][N] (row-major), optionally divided elementwise by D;
+// 16 x 16 outputs per block, K staged through shared memory in slices of 16
+__global__ void __launch_bounds__(256) k_dgemm(int M, int N, int K, const double* A, const double* B, double* C,
+                                               const double* D) {
+  __shared__ double As[16][17], Bs[16][17];
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  const int row = blockIdx.y * 16 + ty, col = blockIdx.x * 16 + tx;
+  double acc = 0.0;
+  for (int k0 = 0; k0 < K; k0 += 16) {
+    As[ty][tx] = (row < M && k0 + tx < K) ? A[(size_t)row * K + k0 + tx] : 0.0;
+    Bs[ty][tx] = (k0 + ty < K && col < N) ? B[(size_t)(k0 + ty) * N + col] : 0.0;
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < 16; ++q) acc += As[ty][q] * Bs[q][tx];
+    __syncthreads();
+  }
+  if (row < M && col < N) C[(size_t)row * N + col] = D ? acc / D[(size_t)row * N + col] : acc;
+}
+
+// node potential of the screened-Poisson path: the solved interior values
+// or the wall values, minus the analytic near-field part
+// (src/FEM.cpp:491-546; the corner and edge index rules restated)
+__global__ void k_sp_finish(LR2D t, DevConsts k) {
+  const int N0 = t.N0, N1 = t.N1;
+  double dummy = 1.0 - (k.sigma * k.bst + 1.0) * exp(-k.bst * k.sigma);
+  dummy = dummy / k.bst / k.bst;
+  const double b = k.bst, sg = k.sigma;
+  double dummy2 = (-1.0 / 6.0 * pow(b, 3.0) * pow(sg, 3.0) - 1.0 / 2.0 * pow(b, 2.0) * pow(sg, 2.0) - b * sg +
+                   exp(b * sg) - 1) * exp(-b * sg) / pow(b, 4.0);
+  dummy2 = dummy2 / pow(k.dx, 2.0);
+  for (int id = blockIdx.x * blockDim.x + threadIdx.x; id < t.nn; id += gridDim.x * blockDim.x) {
+    const int i = id % (N0 + 1), j = id / (N0 + 1);
+    double x = (i > 0 && i < N0 && j > 0 && j < N1) ? t.B[(size_t)(j - 1) * t.nx + (i - 1)] : t.V[id];
+    int ii = i, jj = j, kq = 0;
+    int ipm[4] = {0, -1, 0, 0}, jpm[4] = {0, 0, 0, -1}, kpm[4] = {1, 0, 2, 0};
+    if (i == N0) { ii = i - 1; jj = j; kq = 1; kpm[0] = kq; }
+    if (j == N1) { ii = i; jj = j - 1; kq = 2; kpm[2] = kq; }
+    if (i == N0 && j == N1) { ii = i - 1; jj = j - 1; kq = 3; kpm[0] = kq; kpm[2] = kq; }
+    if (i == 0) { ipm[1] = 0; jpm[1] = 0; kpm[1] = 0; }
+    if (j == 0) { ipm[3] = 0; jpm[3] = 0; kpm[3] = 0; }
+    int num = jj * N0 + ii;
+    const double d2 = t.nnd[(size_t)num * 4 + kq] * dummy;
+    double d3 = -4.0 * t.nnd[(size_t)num * 4 + kq] * dummy2;
+#pragma unroll
+    for (int ll = 0; ll < 4; ++ll) {
+      num = (jj + jpm[ll]) * N0 + ii + ipm[ll];
+      d3 += t.nnd[(size_t)num * 4 + kpm[ll]] * dummy2;
+    }
+    t.V[id] = x + -(d2 + d3);
+  }
+}
+
+// FP32 path: the kick per cell as U1 -= LA1 + LB1 eta, U2 -= LA2 + LB2 xi,
+// the node differences taken in FP64
+__global__ void k_lr2d_pack(DevConsts k, const double* V, float* pcell) {
+  const int N0 = k.N0;
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < k.C; c += gridDim.x * blockDim.x) {
+    const int j = c % N0, kk = c / N0;
+    const int id0 = kk * (N0 + 1) + j, id2 = id0 + N0 + 1;
+    const double v0 = V[id0], v1 = V[id0 + 1], v2 = V[id2], v3 = V[id2 + 1];
+    const double g1 = k.lr_coef / k.m / k.dx * k.dt, g2 = k.lr_coef / k.m / k.dy * k.dt;
+    const double cross = (v0 - v1) - (v2 - v3);
+    float* pf = pcell + (size_t)c * PF_STRIDE;
+    pf[PF_LA1] = (float)((v1 - v0) * g1);
+    pf[PF_LB1] = (float)(cross * g1);
+    pf[PF_LA2] = (float)((v2 - v0) * g2);
+    pf[PF_LB2] = (float)(cross * g2);
+  }
+}
+
+// ------------------------------------------------------------ set-up --
+static void gl_table(int n, double* xs, double* ws) {
+  for (int i = 0; i < n; ++i) {
+    double x = cos(3.14159265358979323846 * (i + 0.75) / (n + 0.5)), dp = 0.0;
+    for (int it = 0; it < 100; ++it) {
+      double p0 = 1.0, p1 = x;
+      for (int kk = 2; kk <= n; ++kk) { double p2 = ((2.0 * kk - 1.0) * x * p1 - (kk - 1.0) * p0) / kk; p0 = p1; p1 = p2; }
+      dp = n * (x * p1 - p0) / (x * x - 1.0);
+      double d = p1 / dp;
+      x -= d;
+      if (fabs(d) < 1e-17) break;
+    }
+    double p0 = 1.0, p1 = x;
+    for (int kk = 2; kk <= n; ++kk) { double p2 = ((2.0 * kk - 1.0) * x * p1 - (kk - 1.0) * p0) / kk; p0 = p1; p1 = p2; }
+    dp = n * (x * p1 - p0) / (x * x - 1.0);
+    xs[n - 1 - i] = x;
+    ws[n - 1 - i] = 2.0 / ((1.0 - x * x) * dp * dp);
+  }
+  for (int i = 0; i < n / 2; ++i) {
+    double xa = 0.5 * (xs[n - 1 - i] - xs[i]), wa = 0.5 * (ws[n - 1 - i] + ws[i]);
+    xs[i] = -xa; xs[n - 1 - i] = xa; ws[i] = wa; ws[n - 1 - i] = wa;
+  }
+  if (n == 50)  // the 8-decimal table of compute_SP_2D (src/FEM.cpp:333-351)
+    for (int i = 0; i < n; ++i) { xs[i] = nearbyint(xs[i] * 1e8) / 1e8; ws[i] = nearbyint(ws[i] * 1e8) / 1e8; }
+}
+
+struct Stencil {
+  int R0lo, R0hi, R1lo, R1hi;
+  std::vector<double> W;
+  std::vector<int> exc_off, exc_i;
+  std::vector<double> exc_w;
+};
+
+// the per-offset weights of the sphere rule and the per-node corrections
+// (see the file comment).  kind 1: compute_Vlasov_2D, kind 3: the
+// Green's-function wall values of compute_SP_2D.
+static bool build_stencil(const Session& s, int kind, Stencil& st, std::string& err) {
+  const DevConsts& k = s.k;
+  const int N0 = k.N0, N1 = k.N1;
+  const int nq = kind == 1 ? 100 : 50;
+  const double pi = acos(-1.0);
+  std::vector<double> xi(nq), wi(nq), rr(nq), dr(nq), ph(nq), dph(nq), th(nq), dth(nq), cph(nq), sph(nq), sth(nq);
+  gl_table(nq, xi.data(), wi.data());
+  const double a = kind == 1 ? 1.0 * k.sigma : 0.0, b = 3.0 * k.sigma;
+  const double cc = 0.0, dd = 2 * pi, ee = 0.0, ff = pi;
+  for (int i = 0; i < nq; ++i) {
+    rr[i] = (b - a) / 2.0 * xi[i] + (a + b) / 2.0; dr[i] = wi[i] * (b - a) / 2.0;
+    ph[i] = (dd - cc) / 2.0 * xi[i] + (cc + dd) / 2.0; dph[i] = wi[i] * (dd - cc) / 2.0;
+    th[i] = (ff - ee) / 2.0 * xi[i] + (ff + ee) / 2.0; dth[i] = wi[i] * (ff - ee) / 2.0;
+    cph[i] = cos(ph[i]); sph[i] = sin(ph[i]); sth[i] = sin(th[i]);
+  }
+  const size_t Q = (size_t)nq * nq * nq;
+  std::vector<double> ox(Q), oy(Q), w(Q);
+  for (int i = 0; i < nq; ++i) {
+    const double radial = kind == 1 ? pow(k.sigma / rr[i], 6.0) * rr[i] * rr[i] * dr[i]
+                                    : exp(-k.bst * rr[i]) / (4.0 * pi) * rr[i] * dr[i];
+    for (int ii = 0; ii < nq; ++ii)
+      for (int iii = 0; iii < nq; ++iii) {
+        const size_t q = ((size_t)i * nq + ii) * nq + iii;
+        ox[q] = rr[i] * cph[ii] * sth[iii];
+        oy[q] = rr[i] * sph[ii] * sth[iii];
+        w[q] = radial * dph[ii] * sth[iii] * dth[iii];
+      }
+  }
+  // node coordinates of every column / row
+  std::vector<double> xc(N0 + 1), yc(N1 + 1);
+  for (int i = 0; i <= N0; ++i) xc[i] = node_coord(i, N0, k.dx);
+  for (int j = 0; j <= N1; ++j) yc[j] = node_coord(j, N1, k.dy);
+  // the offsets a node sees, and the points close enough to a face that
+  // the rounding of the node coordinate may move them
+  const double mx = 1e-13 * (N0 + 4) + 1e-12, my = 1e-13 * (N1 + 4) + 1e-12;
+  std::vector<int> djc(Q), dkc(Q);
+  std::vector<size_t> unsafe;
+  st.R0lo = st.R1lo = 1 << 30;
+  st.R0hi = st.R1hi = -(1 << 30);
+  for (size_t q = 0; q < Q; ++q) {
+    const double tx = ox[q] / k.dx, ty = oy[q] / k.dy;
+    const double fx = floor(tx), fy = floor(ty);
+    djc[q] = (int)fx; dkc[q] = (int)fy;
+    if (std::min(tx - fx, fx + 1.0 - tx) < mx || std::min(ty - fy, fy + 1.0 - ty) < my) unsafe.push_back(q);
+    st.R0lo = std::min(st.R0lo, djc[q]); st.R0hi = std::max(st.R0hi, djc[q]);
+    st.R1lo = std::min(st.R1lo, dkc[q]); st.R1hi = std::max(st.R1hi, dkc[q]);
+  }
+  // corrections: for an unsafe point the reference's own lookup per column
+  // and row (src/FEM.cpp:177-178, :225-226)
+  struct Ent { int node, dja, dka, djc, dkc; double w; };
+  std::vector<Ent> ents;
+  for (size_t q : unsafe) {
+    std::vector<int> dja(N0 + 1), dka(N1 + 1);
+    bool any = false;
+    for (int i = 0; i <= N0; ++i) {
+      dja[i] = (int)floor((xc[i] + ox[q]) / k.dx) - i;
+      any |= dja[i] != djc[q];
+    }
+    for (int j = 0; j <= N1; ++j) {
+      dka[j] = (int)floor((yc[j] + oy[q]) / k.dy) - j;
+      any |= dka[j] != dkc[q];
+    }
+    if (!any) continue;
+    for (int j = 0; j <= N1; ++j)
+      for (int i = 0; i <= N0; ++i) {
+        if (dja[i] == djc[q] && dka[j] == dkc[q]) continue;
+        if (kind == 3 && i > 0 && i < N0 && j > 0 && j < N1) continue;  // wall nodes only
+        ents.push_back({j * (N0 + 1) + i, dja[i], dka[j], djc[q], dkc[q], w[q]});
+        if (ents.size() > (size_t)4 << 20) { err = "too many face-coincident quadrature points"; return false; }
+      }
+  }
+  std::stable_sort(ents.begin(), ents.end(), [](const Ent& x, const Ent& y) { return x.node < y.node; });
+  const int nn = (N0 + 1) * (N1 + 1);
+  st.exc_off.assign(nn + 1, 0);
+  for (const Ent& e : ents) st.exc_off[e.node + 1]++;
+  for (int i = 0; i < nn; ++i) st.exc_off[i + 1] += st.exc_off[i];
+  for (const Ent& e : ents) {
+    st.exc_i.insert(st.exc_i.end(), {e.dja, e.dka, e.djc, e.dkc});
+    st.exc_w.push_back(e.w);
+  }
+  const int sw = st.R0hi - st.R0lo + 1, sh = st.R1hi - st.R1lo + 1;
+  if ((size_t)sw * sh > 20000) { err = "Vlasov stencil too wide for the cell size"; return false; }
+  st.W.assign((size_t)sw * sh, 0.0);
+  for (size_t q = 0; q < Q; ++q) st.W[(size_t)(dkc[q] - st.R1lo) * sw + (djc[q] - st.R0lo)] += w[q];
+  return true;
+}
+
+// orthonormal DST-I matrix of order n: S[a][p] = sqrt(2/(n+1)) sin(pi (a+1)(p+1)/(n+1))
+static void dst_matrix(int n, std::vector<double>& S, std::vector<double>& lamK, std::vector<double>& lamM) {
+  S.resize((size_t)n * n);
+  lamK.resize(n);
+  lamM.resize(n);
+  const double pi = acos(-1.0), sc = sqrt(2.0 / (n + 1));
+  const long period = 2L * (n + 1);
+  for (int a = 0; a < n; ++a)
+    for (int p = 0; p < n; ++p) {
+      long m = ((long)(a + 1) * (p + 1)) % period;  // reduce the angle exactly
+      S[(size_t)a * n + p] = sc * sin(pi * (double)m / (double)(n + 1));
+    }
+  for (int p = 0; p < n; ++p) {
+    const double cth = cos(pi * (p + 1) / (double)(n + 1));
+    lamK[p] = 2.0 - 2.0 * cth;
+    lamM[p] = 2.0 / 3.0 + cth / 3.0;
+  }
+}
+
+int lr2d_setup(Session& s) {
+  const int mode = s.cfg.long_range;
+  if (!(s.k.lr2d)) return 0;
+  LR2D* t = new (std::nothrow) LR2D();
+  if (!t) return 1;
+  s.lr2d = t;
+  const DevConsts& k = s.k;
+  t->mode = mode;
+  t->N0 = k.N0; t->N1 = k.N1;
+  t->nn = (k.N0 + 1) * (k.N1 + 1);
+  t->nx = k.N0 - 1; t->ny = k.N1 - 1;
+  Stencil st;
+  if (!build_stencil(s, mode == MCPM_LR_DIRECT ? 1 : 3, st, s.err)) return 1;
+  t->R0lo = st.R0lo; t->R0hi = st.R0hi; t->R1lo = st.R1lo; t->R1hi = st.R1hi;
+  t->sw = st.R0hi - st.R0lo + 1;
+  t->n_exc = (int)st.exc_w.size();
+  t->smem = st.W.size() * sizeof(double);
+  auto A = [&](void** p, size_t bytes) { return cudaMalloc(p, bytes ? bytes : 16) == cudaSuccess; };
+  auto H = [&](void* d, const void* h, size_t bytes) {
+    return bytes == 0 || cudaMemcpy(d, h, bytes, cudaMemcpyHostToDevice) == cudaSuccess;
+  };
+  bool ok = A((void**)&t->W, t->smem) && H(t->W, st.W.data(), t->smem) &&
+            A((void**)&t->exc_off, st.exc_off.size() * 4) && H(t->exc_off, st.exc_off.data(), st.exc_off.size() * 4) &&
+            A((void**)&t->exc_i, st.exc_i.size() * 4) && H(t->exc_i, st.exc_i.data(), st.exc_i.size() * 4) &&
+            A((void**)&t->exc_w, st.exc_w.size() * 8) && H(t->exc_w, st.exc_w.data(), st.exc_w.size() * 8) &&
+            A((void**)&t->V, (size_t)t->nn * 8) && A((void**)&t->nnd, (size_t)k.C * 4 * 8) &&
+            A((void**)&t->qc, (size_t)k.C * 4 * 4);
+  if (ok && mode == MCPM_LR_SCREENED_POISSON) {
+    std::vector<double> Sx, Sy, kx, mx, ky, my;
+    dst_matrix(t->nx, Sx, kx, mx);
+    dst_matrix(t->ny, Sy, ky, my);
+    const double c = k.bst * k.bst * (k.dx * k.dy * k.dz);
+    std::vector<double> mu((size_t)t->nx * t->ny);
+    for (int q = 0; q < t->ny; ++q)
+      for (int p = 0; p < t->nx; ++p) mu[(size_t)q * t->nx + p] = kx[p] * my[q] + mx[p] * ky[q] + c * mx[p] * my[q];
+    std::vector<int> wall;
+    for (int j = 0; j <= k.N1; ++j)
+      for (int i = 0; i <= k.N0; ++i)
+        if (i == 0 || i == k.N0 || j == 0 || j == k.N1) wall.push_back(j * (k.N0 + 1) + i);
+    t->n_wall = (int)wall.size();
+    const size_t nxy = (size_t)t->nx * t->ny;  // T: the transforms' scratch
+    ok = A((void**)&t->Sx, Sx.size() * 8) && H(t->Sx, Sx.data(), Sx.size() * 8) &&
+         A((void**)&t->Sy, Sy.size() * 8) && H(t->Sy, Sy.data(), Sy.size() * 8) &&
+         A((void**)&t->mu, nxy * 8) && H(t->mu, mu.data(), nxy * 8) && A((void**)&t->B, nxy * 8) &&
+         A((void**)&t->T, nxy * 8) && A((void**)&t->wall, wall.size() * 4) &&
+         H(t->wall, wall.data(), wall.size() * 4);
+  }
+  if (!ok) { s.err = "2-D long-range tables: out of device memory"; return 1; }
+  if (t->smem > 48 * 1024 &&
+      cudaFuncSetAttribute(k_node_potential, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)t->smem) != cudaSuccess) {
+    s.err = "2-D long-range stencil: shared memory";
+    return 1;
+  }
+  cudaMemset(t->V, 0, (size_t)t->nn * 8);
+  cudaMemset(t->nnd, 0, (size_t)k.C * 4 * 8);
+  return 0;
+}
+
+void lr2d_free(Session& s) {
+  LR2D* t = s.lr2d;
+  if (!t) return;
+  cudaFree(t->W); cudaFree(t->exc_off); cudaFree(t->exc_i); cudaFree(t->exc_w); cudaFree(t->V); cudaFree(t->nnd);
+  cudaFree(t->qc); cudaFree(t->Sx); cudaFree(t->Sy); cudaFree(t->mu); cudaFree(t->B); cudaFree(t->T); cudaFree(t->wall);
+  delete t;
+  s.lr2d = nullptr;
+}
+
+const double* lr2d_potential(const Session& s) { return s.lr2d ? s.lr2d->V : nullptr; }
+const double* lr2d_node_density(const Session& s) { return s.lr2d ? s.lr2d->nnd : nullptr; }
+int lr2d_num_nodes(const Session& s) { return s.lr2d ? s.lr2d->nn : 0; }
+
+// ------------------------------------------------------------ launches --
+static int blocks_for(long n, int bs, int cap) { return (int)std::max(1L, std::min((n + bs - 1) / bs, (long)cap)); }
+
+int launch_node_density(Session& s) {
+  LR2D* t = s.lr2d;
+  if (!t || t->mode != MCPM_LR_SCREENED_POISSON) return 0;
+  const int g = blocks_for((long)s.C * 32, 256, s.num_sms * 16);
+  if (s.prec == MCPM_FP32) {
+    const PBuf& P = s.P[s.cur];
+    k_quadrants<float><<<g, 256, 0, s.stream>>>(s.k, s.off, s.cnt, (const float*)P.x1, (const float*)P.x2, t->qc);
+  } else {
+    const PBuf& P = s.P[s.cur];
+    k_quadrants<double><<<g, 256, 0, s.stream>>>(s.k, s.off, s.cnt, (const double*)P.x1, (const double*)P.x2, t->qc);
+  }
+  k_node_density<<<blocks_for(4L * s.C, 256, s.num_sms * 16), 256, 0, s.stream>>>(s.k, t->qc, t->nnd,
+                                                                                    s.prec == MCPM_FP64);
+  return 2;
+}
+
+int launch_long_range_2d(Session& s) {
+  LR2D* t = s.lr2d;
+  if (!t) return 0;
+  const double* n = s.cell + (size_t)MCPM_CF_N * s.C;
+  int launches = 0;
+  const int cap = s.num_sms * 16;
+  if (t->mode == MCPM_LR_DIRECT) {
+    k_node_potential<<<blocks_for(t->nn, 128, cap), 128, t->smem, s.stream>>>(*t, n, 0);
+    launches = 1;
+  } else {
+    k_node_potential<<<blocks_for(t->n_wall, 128, cap), 128, t->smem, s.stream>>>(*t, n, 1);
+    k_sp_rhs<<<blocks_for((long)t->nx * t->ny, 256, cap), 256, 0, s.stream>>>(*t, s.k);
+    const int nx = t->nx, ny = t->ny;
+    dim3 g((nx + 15) / 16, (ny + 15) / 16);
+    // B <- S_y B S_x / mu, then U = S_y B S_x  (rows y, columns x)
+    k_dgemm<<<g, 256, 0, s.stream>>>(ny, nx, ny, t->Sy, t->B, t->T, nullptr);
+    k_dgemm<<<g, 256, 0, s.stream>>>(ny, nx, nx, t->T, t->Sx, t->B, t->mu);
+    k_dgemm<<<g, 256, 0, s.stream>>>(ny, nx, ny, t->Sy, t->B, t->T, nullptr);
+    k_dgemm<<<g, 256, 0, s.stream>>>(ny, nx, nx, t->T, t->Sx, t->B, nullptr);
+    k_sp_finish<<<blocks_for(t->nn, 256, cap), 256, 0, s.stream>>>(*t, s.k);
+    launches = 7;
+  }
+  if (s.prec == MCPM_FP32) {
+    k_lr2d_pack<<<blocks_for(s.C, 256, cap), 256, 0, s.stream>>>(s.k, t->V, s.pcell);
+    ++launches;
+  }
+  return launches;
+}
+
+}  // namespace mcpm

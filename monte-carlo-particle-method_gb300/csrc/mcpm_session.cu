@@ -123,8 +123,18 @@ int mcpm_session_create(const mcpm_config* cfg, mcpm_session** out) {
     return MCPM_ERR_ARG;
   if (c.long_range != MCPM_LR_NONE && c.long_range != MCPM_LR_DIRECT && c.long_range != MCPM_LR_SCREENED_POISSON)
     return MCPM_ERR_ARG;
-  // the 1-D Vlasov routines index cells by row (src/Main_Functions.cpp:3772)
-  if (c.long_range != MCPM_LR_NONE && (c.n_cells[0] != 1 || c.n_cells[1] + 1 > 7000)) return MCPM_ERR_ARG;
+  if (c.long_range != MCPM_LR_NONE) {
+    if (c.direction[0] == 1) {
+      // 2-D: the node-grid paths of src/FEM.cpp; the screened-Poisson solve
+      // needs interior nodes and keeps two dense DST matrices of order <= 2047
+      if (c.n_cells[0] > 2048 || c.n_cells[1] > 2048) return MCPM_ERR_ARG;
+      if (c.long_range == MCPM_LR_SCREENED_POISSON && (c.n_cells[0] < 2 || c.n_cells[1] < 2)) return MCPM_ERR_ARG;
+      if (c.long_range == MCPM_LR_SCREENED_POISSON && !(c.bst > 0)) return MCPM_ERR_ARG;
+    } else if (c.n_cells[0] != 1 || c.n_cells[1] + 1 > 7000) {
+      // the 1-D Vlasov routines index cells by row (src/Main_Functions.cpp:3772)
+      return MCPM_ERR_ARG;
+    }
+  }
   if (!(c.sigma > 0 && c.m > 0 && c.kb > 0 && c.dt > 0 && c.mu > 0 && c.T0 > 0)) return MCPM_ERR_ARG;
   for (int i = 0; i < 2; ++i)
     if (!(c.length[i] > 0)) return MCPM_ERR_ARG;
@@ -146,6 +156,8 @@ int mcpm_session_create(const mcpm_config* cfg, mcpm_session** out) {
   k.b = c.b; k.dt = c.dt; k.phi = c.phi; k.eqdist = c.eqdist; k.ast = c.ast; k.bst = c.bst;
   for (int i = 0; i < 4; ++i) { k.Tw[i] = c.T_wall[i]; k.Uw[i] = c.U_wall[i]; }
   k.seed = c.seed;
+  k.lr2d = (c.long_range != MCPM_LR_NONE && c.direction[0] == 1) ? 1 : 0;
+  k.lr_coef = c.long_range == MCPM_LR_DIRECT ? c.phi : c.ast;
   k.f_dx = (float)k.dx; k.f_dy = (float)k.dy; k.f_L0 = (float)k.L0; k.f_L1 = (float)k.L1;
   k.f_dt = (float)k.dt; k.f_sigma = (float)k.sigma; k.f_m = (float)k.m; k.f_kb = (float)k.kb;
   for (int i = 0; i < 4; ++i) { k.f_Tw[i] = (float)k.Tw[i]; k.f_Uw[i] = (float)k.Uw[i]; }
@@ -207,11 +219,17 @@ int mcpm_session_create(const mcpm_config* cfg, mcpm_session** out) {
   cudaMemsetAsync(s->xi, 0, 3 * cap * 8, s->stream);
 
   if ((rc = cuda_check(s, update_set_smem_max(), "smem attribute"))) { mcpm_session_destroy(s); return rc; }
-  if (c.long_range != MCPM_LR_NONE)
+  if (c.long_range != MCPM_LR_NONE && !k.lr2d)
     if ((rc = cuda_check(s, pcr_set_smem(k.N1 + 1), "long-range smem"))) { mcpm_session_destroy(s); return rc; }
   s->tune.grid_mom = s->num_sms * moments_occupancy(*s);
   s->tune.grid_upd = s->num_sms * update_occupancy(*s);
-  if (long_range_setup(*s)) { s->err = "long-range tables"; mcpm_session_destroy(s); return MCPM_ERR_CUDA; }
+  if (!k.lr2d && long_range_setup(*s)) { s->err = "long-range tables"; mcpm_session_destroy(s); return MCPM_ERR_CUDA; }
+  if (k.lr2d && lr2d_setup(*s)) {
+    if (s->err.empty()) s->err = "2-D long-range tables";
+    int code = s->err.find("memory") != std::string::npos ? MCPM_ERR_CUDA : MCPM_ERR_ARG;
+    mcpm_session_destroy(s);
+    return code;
+  }
   if ((rc = cuda_check(s, cudaStreamSynchronize(s->stream), "session init"))) { mcpm_session_destroy(s); return rc; }
   *out = s;
   return MCPM_OK;
@@ -229,6 +247,7 @@ int mcpm_session_destroy(mcpm_session* s) {
   cudaFree(s->key); cudaFree(s->cnt); cudaFree(s->cnt_next); cudaFree(s->off); cudaFree(s->cursor);
   cudaFree(s->list_small); cudaFree(s->list_big); cudaFree(s->wl); cudaFree(s->work); cudaFree(s->scan_blk); cudaFree(s->cell); cudaFree(s->pcell);
   cudaFree(s->xi); cudaFree(s->inj); cudaFree(s->stage); cudaFree(s->faces); cudaFree(s->lr_tab); cudaFree(s->status);
+  lr2d_free(*s);
   if (s->graph) cudaGraphExecDestroy(s->graph);
   for (auto& r : s->prof_recs) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
   for (auto e : s->prof_pool) cudaEventDestroy(e);
@@ -324,6 +343,8 @@ int mcpm_cell_update(mcpm_session* s) {
   cudaMemsetAsync(s->work, 0, WK_COUNT * 4, s->stream);
   n += T_MOM(launch_moments(*s));
   n += T_SOLVE(launch_solve(*s, (s->cfg.model == MCPM_MODEL_FP_DENSE && s->step > 0) ? 1 : 0));
+  n += T_LR(launch_node_density(*s));  // n_n (src/Main_Functions.cpp:2268-2364), 2-D screened Poisson only
+  s->nodes_valid = s->lr2d != nullptr;
   return after_launch(s, n, "cell_update");
 }
 
@@ -415,6 +436,8 @@ int mcpm_step(mcpm_session* s, int32_t n_steps) {
     }
     n += T_MOM(launch_moments(*s));
     n += T_SOLVE(launch_solve(*s, (m == MCPM_MODEL_FP_DENSE && s->step > 0) ? 1 : 0));
+    n += T_LR(launch_node_density(*s));
+    s->nodes_valid = s->lr2d != nullptr;
     if (m == MCPM_MODEL_ESMC) n += T_ESMC(launch_esmc(*s));
     if (s->cfg.long_range != MCPM_LR_NONE) n += T_LR(launch_long_range(*s));
     n += T_UPD(launch_update(*s, stages, 0));
@@ -448,6 +471,21 @@ int mcpm_get_cells(mcpm_session* s, double* out) {
   if (!s || !out) return MCPM_ERR_ARG;
   cudaMemcpyAsync(out, s->cell, (size_t)MCPM_CF_COUNT * s->C * 8, cudaMemcpyDeviceToHost, s->stream);
   return cuda_check(s, cudaStreamSynchronize(s->stream), "get_cells");
+}
+
+int mcpm_get_node_density(mcpm_session* s, double* out) {
+  if (!s || !out) return MCPM_ERR_ARG;
+  if (!s->lr2d || s->cfg.long_range != MCPM_LR_SCREENED_POISSON || !s->nodes_valid)
+    return fail(s, MCPM_ERR_STATE, "get_node_density: needs a 2-D screened-Poisson session after cell_update");
+  cudaMemcpyAsync(out, lr2d_node_density(*s), (size_t)s->C * 4 * 8, cudaMemcpyDeviceToHost, s->stream);
+  return cuda_check(s, cudaStreamSynchronize(s->stream), "get_node_density");
+}
+
+int mcpm_get_node_potential(mcpm_session* s, double* out) {
+  if (!s || !out) return MCPM_ERR_ARG;
+  if (!s->lr2d) return fail(s, MCPM_ERR_STATE, "get_node_potential: needs a 2-D long-range session");
+  cudaMemcpyAsync(out, lr2d_potential(*s), (size_t)lr2d_num_nodes(*s) * 8, cudaMemcpyDeviceToHost, s->stream);
+  return cuda_check(s, cudaStreamSynchronize(s->stream), "get_node_potential");
 }
 
 int mcpm_get_index(mcpm_session* s, int32_t* index) {

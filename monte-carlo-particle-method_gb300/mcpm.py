@@ -129,6 +129,8 @@ def load_library(path: str | None = None):
         "mcpm_get_cells": (C.c_int, [vp, dp]),
         "mcpm_get_index": (C.c_int, [vp, ip]),
         "mcpm_get_normals": (C.c_int, [vp, dp, dp, dp]),
+        "mcpm_get_node_density": (C.c_int, [vp, dp]),
+        "mcpm_get_node_potential": (C.c_int, [vp, dp]),
         "mcpm_get_layout": (C.c_int, [vp, ip, ip]),
         "mcpm_get_step": (i32, [vp]),
         "mcpm_set_step": (C.c_int, [vp, i32]),
@@ -298,6 +300,19 @@ class Session:
         a, b, c = np.empty(self.N), np.empty(self.N), np.empty(self.N)
         self._ck(self.lib.mcpm_get_normals(self.h, _dp(a), _dp(b), _dp(c)), "get_normals")
         return a, b, c
+
+    def get_node_density(self):
+        """n_n of the last cell_update, [C][4] (2-D screened-Poisson sessions)."""
+        out = np.empty((self.C, 4))
+        self._ck(self.lib.mcpm_get_node_density(self.h, _dp(out)), "get_node_density")
+        return out
+
+    def get_node_potential(self):
+        """Node potential of the last 2-D Vlasov force, (N0+1)(N1+1) values."""
+        n = (self.cfg.n_cells[0] + 1) * (self.cfg.n_cells[1] + 1)
+        out = np.empty(n)
+        self._ck(self.lib.mcpm_get_node_potential(self.h, _dp(out)), "get_node_potential")
+        return out
 
     def get_layout(self):
         pid = np.empty(self.N, dtype=np.int32)

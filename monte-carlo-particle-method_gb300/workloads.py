@@ -180,15 +180,15 @@ def uneven_cells_2d(n_cells=(256, 256), precision=FP32, seed=BASE_SEED + 3, stre
 def density_field(rng, n_cells, length, K=6, nbar=None):
     """One seeded 2-D packing-fraction field n b(x, y) at the cell centres:
     nbar + sum_{k=1..K} a_k sin(2 pi (kx x / L0 + ky y / L1) + phi_k), with
-    nbar ~ U[0.15, 0.35], sum |a_k| <= 0.1, integer wave vectors of norm
-    1..8, clipped to [0.05, 0.45]."""
+    nbar ~ U[0.15, 0.35], sum |a_k| ~ U[0.05, 0.1], integer wave vectors of
+    norm 1..8, clipped to [0.05, 0.45]."""
     N0, N1 = n_cells
     xc = (np.arange(N0) + 0.5) * (length[0] / N0)
     yc = (np.arange(N1) + 0.5) * (length[1] / N1)
     X, Y = np.meshgrid(xc, yc)  # [N1][N0]
     nb = np.full(X.shape, rng.uniform(0.15, 0.35) if nbar is None else nbar)
     amp = rng.uniform(0.0, 1.0, K)
-    amp *= rng.uniform(0.0, 0.1) / max(amp.sum(), 1e-12)
+    amp *= rng.uniform(0.05, 0.1) / max(amp.sum(), 1e-12)
     for a in amp:
         while True:
             kx, ky = rng.integers(-8, 9, 2)
