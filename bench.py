@@ -45,7 +45,8 @@ UNIT = "particle-steps/s"
 # algorithmic bytes per particle of one launch (FP32 state, 2-D positions):
 #  update: read x1 x2 U1 U2 U3 pid (24 B), write x1 x2 U1 U2 U3 key (24 B)
 #  moments: read U1 U2 U3 (12 B); scatter (not credited): read 28 B, write 24 B
-ALG_BYTES = {"update": 48, "moments": 12, "scatter": 52}
+#  esmc: read x1 x2 U1 U2 U3 (20 B), write U1 U2 U3 (12 B)
+ALG_BYTES = {"update": 48, "moments": 12, "scatter": 52, "esmc": 32}
 
 
 def _peaks():
@@ -142,6 +143,12 @@ def build_workload(args):
         cfg, parts = W.esmc_box_2d(precision=mcpm.FP32)
         desc = {"workload": "ESMC 256x256 100/cell nb=0.2 diffuse walls fp32", "cells": 65536,
                 "particles": int(len(parts["x2"]))}
+    elif args.workload == "vlasov16m":
+        cfg, parts = W.vlasov_box_2d(n_cells=(256, 256), total=16_000_000, precision=mcpm.FP32,
+                                     long_range=mcpm.LR_SCREENED_POISSON, model=mcpm.MODEL_FP_DENSE)
+        desc = {"workload": "2-D Enskog-Vlasov box 256x256 sinusoidal density (nb 0.05..0.45) FP_dense fp32, "
+                            "screened-Poisson FEM force with Green's-function walls every step (plain path)",
+                "cells": 65536, "particles": int(len(parts["x2"]))}
     elif args.workload == "slab1m":
         cfg, parts = W.vlasov_slab_1d(precision=mcpm.FP32)
         desc = {"workload": "1-D Enskog-Vlasov slab 1000 cells 1M fp32 screened-Poisson",
@@ -363,7 +370,7 @@ def main():
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="mcpm", choices=["mcpm", "reference"])
-    ap.add_argument("--workload", default="uneven16m", choices=["uneven16m", "esmc6m", "slab1m"])
+    ap.add_argument("--workload", default="uneven16m", choices=["uneven16m", "esmc6m", "slab1m", "vlasov16m"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "mcpm":

@@ -208,7 +208,9 @@ int mcpm_end_step(mcpm_session* s);
 /* n_steps iterations of the main loop body (src/main.cpp:389-669) for the
    in-scope models: cell_update, random_generator, velocity_update,
    DFP_extra_streaming, apply_BC, store_old_positions, stream_particles,
-   apply_BC.  The particle-side stages run fused in one kernel per step. */
+   apply_BC.  The particle-side stages run fused in one kernel per step;
+   once the cell layout is in its steady state, pairs of steps are replayed
+   as one CUDA graph (not in profiling mode). */
 int mcpm_step(mcpm_session* s, int32_t n_steps);
 
 /* ---- test and diagnostic hooks ---------------------------------------- */

@@ -24,7 +24,7 @@ template <typename real> struct PT2 {
 // after another in order.
 template <typename real>
 __global__ void __launch_bounds__(128) k_esmc(DevConsts k, double* cell, const int32_t* off, const int32_t* cnt,
-                                              PT2<real> p, int step, int cx, int cy, int Sx, int Sy,
+                                              PT2<real> p, const int32_t* dstep, int cx, int cy, int Sx, int Sy,
                                               uint32_t* status) {
   const int lane = threadIdx.x & 31;
   const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -32,6 +32,7 @@ __global__ void __launch_bounds__(128) k_esmc(DevConsts k, double* cell, const i
   if (gw >= nA * nB) return;
   const int I = (cy + Sy * (gw / nA)) * k.N0 + (cx + Sx * (gw % nA));
   const int C = k.C;
+  const int step = *dstep;
   const int NI = cnt[I];
   const double om_max = cell[(size_t)MCPM_CF_OMEGA_MAX * C + I];
   const double mreal = r_floor(0.5 * om_max * (1.0 * NI) + u01d(philox(k.seed, (uint32_t)I, (uint32_t)step, RNG_ESMC_M, 0u).x));
@@ -111,20 +112,20 @@ __global__ void __launch_bounds__(128) k_esmc(DevConsts k, double* cell, const i
 }
 
 template <typename real> static int esmc_impl(Session& s) {
+  int n = sync_dstep(s);
   const PBuf& b = s.P[s.cur];
   PT2<real> p{(real*)b.x1, (real*)b.x2, (real*)b.U1, (real*)b.U2, (real*)b.U3};
   int Rx = (int)ceil(s.k.sigma / s.k.dx), Ry = (int)ceil(s.k.sigma / s.k.dy);
   if (Rx < 1) Rx = 1;
   if (Ry < 1) Ry = 1;
   int Sx = (s.k.N0 > 1) ? 2 * Rx + 1 : 1, Sy = 2 * Ry + 1;
-  int n = 0;
   for (int cy = 0; cy < Sy; ++cy)
     for (int cx = 0; cx < Sx; ++cx) {
       int nA = (s.k.N0 - cx + Sx - 1) / Sx, nB = (s.k.N1 - cy + Sy - 1) / Sy;
       int warps = nA * nB;
       if (warps <= 0) continue;
       int blocks = (warps * 32 + 127) / 128;
-      k_esmc<real><<<blocks, 128, 0, s.stream>>>(s.k, s.cell, s.off, s.cnt, p, s.step, cx, cy, Sx, Sy, s.status);
+      k_esmc<real><<<blocks, 128, 0, s.stream>>>(s.k, s.cell, s.off, s.cnt, p, s.dstep, cx, cy, Sx, Sy, s.status);
       ++n;
     }
   return n;

@@ -128,6 +128,8 @@ struct Session {
   LR2D* lr2d = nullptr;         // 2-D long range (node grid), when configured
   bool nodes_valid = false;     // nodal densities describe the last cell_update
   uint32_t* status = nullptr;
+  int32_t* dstep = nullptr;     // device copy of the step number the kernels read
+  int dstep_val = -1;           // the value it holds once queued work has run (-1: unknown)
   cudaStream_t stream = nullptr;
   int step = 0;
   int bc_calls = 0;             // apply_BC calls in the current step (split mode)
@@ -146,9 +148,13 @@ struct Session {
   struct ProfRec { cudaEvent_t a, b; int cls; int n; };
   std::vector<ProfRec> prof_recs;
   std::vector<cudaEvent_t> prof_pool;
-  // graph of one fused step
+  // graph of two fused steps (the buffer pair returns to its start), replayed
+  // by mcpm_step; rebuilt when its signature (stream, layout parity, stages,
+  // tuning) changes
   cudaGraphExec_t graph = nullptr;
   uint64_t graph_sig = 0;
+  int graph_launches = 0;
+  bool use_graphs = true;
   std::string err;
 };
 
@@ -173,6 +179,9 @@ int launch_long_range_2d(Session& s);
 const double* lr2d_potential(const Session& s);
 const double* lr2d_node_density(const Session& s);
 int lr2d_num_nodes(const Session& s);
+// the device step number made equal to s.step (a one-thread kernel when it
+// differs); returns the launches it made
+int sync_dstep(Session& s);
 int launch_convert_in(Session& s, int64_t n);
 int launch_convert_out(Session& s, int64_t n);
 

@@ -911,19 +911,21 @@ template <typename real> struct UpdArgs {
   double* xi;
   int64_t cap;
   uint32_t* status;
-  int step, bin_step, rng_mode, bc_call_base;
+  const int32_t* dstep;  // the step number (device copy: graph replays advance it)
+  int rng_mode, bc_call_base;
   uint32_t stages;
   int wcap, bcap;
   const double* Vn;  // node potential of the 2-D Vlasov force (FP64 path)
 };
 
 template <typename real>
-__device__ __forceinline__ void raw_normals(const UpdArgs<real>& a, int64_t p, real& z0, real& z1, real& z2) {
+__device__ __forceinline__ void raw_normals(const UpdArgs<real>& a, int step, int64_t p, real& z0, real& z1,
+                                            real& z2) {
   int pid = a.p.pid[p];
   if (a.rng_mode == MCPM_RNG_INJECTED) {
     z0 = (real)a.inj[pid]; z1 = (real)a.inj[a.cap + pid]; z2 = (real)a.inj[2 * a.cap + pid];
   } else {
-    Normals3<real> z = normals3<real>(philox(a.k.seed, (uint32_t)pid, (uint32_t)a.step, RNG_FP, 0u));
+    Normals3<real> z = normals3<real>(philox(a.k.seed, (uint32_t)pid, (uint32_t)step, RNG_FP, 0u));
     z0 = z.z0; z1 = z.z1; z2 = z.z2;
   }
 }
@@ -1007,7 +1009,7 @@ template <typename real> __device__ __forceinline__ real crms(const Acc<real>& s
 // the normals; the FP32 path takes the per-cell mean and RMS from one pass
 // of compensated sums of z and z^2.
 template <typename real, int TILE, uint32_t CST>
-__device__ void update_cell(int c, const UpdArgs<real>& a, real* xs, int xcap, Acc<real>* red) {
+__device__ void update_cell(int c, const UpdArgs<real>& a, int step, real* xs, int xcap, Acc<real>* red) {
   constexpr bool F32 = sizeof(real) == 4;
   const int t = (TILE == 32) ? (threadIdx.x & 31) : threadIdx.x;
   const int64_t s0 = a.off[c];
@@ -1035,7 +1037,7 @@ __device__ void update_cell(int c, const UpdArgs<real>& a, real* xs, int xcap, A
       int64_t p = s0 + i;
       if (rng) {
         real z0, z1, z2;
-        raw_normals(a, p, z0, z1, z2);
+        raw_normals(a, step, p, z0, z1, z2);
         if (staged) { xs[3 * i] = z0; xs[3 * i + 1] = z1; xs[3 * i + 2] = z2; }
         sa[0].add(z0); sa[1].add(z1); sa[2].add(z2);
         if constexpr (F32) { sa[4].add(z0 * z0); sa[5].add(z1 * z1); sa[6].add(z2 * z2); }
@@ -1062,7 +1064,7 @@ __device__ void update_cell(int c, const UpdArgs<real>& a, real* xs, int xcap, A
         for (int i = t; i < n; i += TILE) {
           real z0, z1, z2;
           if (staged) { z0 = xs[3 * i]; z1 = xs[3 * i + 1]; z2 = xs[3 * i + 2]; }
-          else raw_normals(a, s0 + i, z0, z1, z2);
+          else raw_normals(a, step, s0 + i, z0, z1, z2);
           real d0 = z0 - mean0, d1 = z1 - mean1, d2 = z2 - mean2;
           s3[0].add(d0 * d0); s3[1].add(d1 * d1); s3[2].add(d2 * d2);
         }
@@ -1080,7 +1082,7 @@ __device__ void update_cell(int c, const UpdArgs<real>& a, real* xs, int xcap, A
       return;
     }
     if (staged) { z0 = xs[3 * i]; z1 = xs[3 * i + 1]; z2 = xs[3 * i + 2]; }
-    else raw_normals(a, p, z0, z1, z2);
+    else raw_normals(a, step, p, z0, z1, z2);
     if (n > 1) {
       if constexpr (F32) {
         z0 = (z0 - mean0) * irms0; z1 = (z1 - mean1) * irms1; z2 = (z2 - mean2) * irms2;
@@ -1232,21 +1234,21 @@ __device__ void update_cell(int c, const UpdArgs<real>& a, real* xs, int xcap, A
           }
         }
       }
-      if (st & ST_BC1) apply_bc<real>(s, a.bc_call_base + 0, pid, a.step, k, kc, bad);
+      if (st & ST_BC1) apply_bc<real>(s, a.bc_call_base + 0, pid, step, k, kc, bad);
       if (st & ST_OLD) { s.x1o = s.x1; s.x2o = s.x2; }
       if (st & ST_STREAM) {
         if (k.dir0 == 1) s.x1 = s.x1 + dtr * s.u1;
         if (k.dir1 == 1) s.x2 = s.x2 + dtr * s.u2;
       }
-      if (st & ST_BC2) apply_bc<real>(s, a.bc_call_base + 1, pid, a.step, k, kc, bad);
-      if (st & ST_BC3) apply_bc<real>(s, a.bc_call_base + 2, pid, a.step, k, kc, bad);
+      if (st & ST_BC2) apply_bc<real>(s, a.bc_call_base + 1, pid, step, k, kc, bad);
+      if (st & ST_BC3) apply_bc<real>(s, a.bc_call_base + 2, pid, step, k, kc, bad);
       P.U1[p] = s.u1; P.U2[p] = s.u2; P.U3[p] = s.u3;
       if (P.x1) P.x1[p] = s.x1;
       P.x2[p] = s.x2;
       if (P.x1o) P.x1o[p] = s.x1o;
       if (P.x2o) P.x2o[p] = s.x2o;
       if (st & ST_KEY) {
-        key = bin_one<real>(s.x1, s.x2, pid, a.bin_step, k, kc, bad);
+        key = bin_one<real>(s.x1, s.x2, pid, step + 1, k, kc, bad);
         a.key_out[p] = key;
       }
     }
@@ -1261,10 +1263,11 @@ __global__ void __launch_bounds__(256, sizeof(real) == 4 ? 3 : 1) k_update(UpdAr
   __shared__ Acc<real> red[8 * 8];
   real* xs = reinterpret_cast<real*>(smem_raw);
   const int warp = threadIdx.x >> 5;
+  const int step = *a.dstep;
   schedule_cells(
       a.list_big, a.list_small, a.wl, a.work, WK_UPD_BIG, WK_UPD_SMALL,
-      [&](int c) { update_cell<real, 256, CST>(c, a, xs, a.bcap, red); },
-      [&](int c) { update_cell<real, 32, CST>(c, a, xs + (size_t)warp * 3 * (a.bcap / 8), a.bcap / 8, red); });
+      [&](int c) { update_cell<real, 256, CST>(c, a, step, xs, a.bcap, red); },
+      [&](int c) { update_cell<real, 32, CST>(c, a, step, xs + (size_t)warp * 3 * (a.bcap / 8), a.bcap / 8, red); });
 }
 
 // the fused FP_dense step with specular or periodic walls and no long-range
@@ -1358,6 +1361,7 @@ template <typename real> static size_t update_smem(const Session& s) {
 }
 
 template <typename real> static int update_impl(Session& s, uint32_t stages, int bc_call_base) {
+  const int n = sync_dstep(s);
   UpdArgs<real> a;
   a.k = s.k;
   a.cell = s.cell;
@@ -1371,8 +1375,7 @@ template <typename real> static int update_impl(Session& s, uint32_t stages, int
   a.xi = s.xi;
   a.cap = s.cap;
   a.status = s.status;
-  a.step = s.step;
-  a.bin_step = s.step + 1;
+  a.dstep = s.dstep;
   a.rng_mode = s.rng_mode;
   a.bc_call_base = bc_call_base;
   a.stages = stages;
@@ -1382,7 +1385,7 @@ template <typename real> static int update_impl(Session& s, uint32_t stages, int
   size_t sm = update_smem<real>(s);
   if (stages == ST_FUSED_FP) k_update<real, ST_FUSED_FP><<<s.tune.grid_upd, 256, sm, s.stream>>>(a);
   else k_update<real, 0u><<<s.tune.grid_upd, 256, sm, s.stream>>>(a);
-  return 1;
+  return n + 1;
 }
 int launch_update(Session& s, uint32_t stages, int bc_call_base) {
   return s.prec == MCPM_FP32 ? update_impl<float>(s, stages, bc_call_base) : update_impl<double>(s, stages, bc_call_base);

@@ -35,6 +35,15 @@ __global__ void k_index(const int32_t* off, int C, const int32_t* pid, int32_t* 
     out[pid[i]] = lo;
   }
 }
+__global__ void k_set_step(int32_t* dstep, int v) { *dstep = v; }
+__global__ void k_step_advance(int32_t* dstep) { *dstep += 1; }
+
+int sync_dstep(Session& s) {
+  if (s.dstep_val == s.step) return 0;
+  k_set_step<<<1, 1, 0, s.stream>>>(s.dstep, s.step);
+  s.dstep_val = s.step;
+  return 1;
+}
 }  // namespace mcpm
 
 using namespace mcpm;
@@ -204,7 +213,8 @@ int mcpm_session_create(const mcpm_config* cfg, mcpm_session** out) {
        A((void**)&s->scan_blk, 4 * (C / 1024 + 2) * 4) &&
        A((void**)&s->cell, (size_t)CF_DEV_COUNT * C * 8) && A((void**)&s->pcell, (size_t)PF_STRIDE * C * 4) && A((void**)&s->xi, 3 * cap * 8) &&
        A((void**)&s->inj, 3 * cap * 8) && A((void**)&s->stage, 5 * cap * 8) &&
-       A((void**)&s->faces, ((size_t)k.N1 + 1 + 5000) * 8) && A((void**)&s->status, 16);
+       A((void**)&s->faces, ((size_t)k.N1 + 1 + 5000) * 8) && A((void**)&s->status, 16) &&
+       A((void**)&s->dstep, 16);
   if (!ok) {
     s->err = "out of device memory";
     mcpm_session_destroy(s);
@@ -246,7 +256,7 @@ int mcpm_session_destroy(mcpm_session* s) {
   }
   cudaFree(s->key); cudaFree(s->cnt); cudaFree(s->cnt_next); cudaFree(s->off); cudaFree(s->cursor);
   cudaFree(s->list_small); cudaFree(s->list_big); cudaFree(s->wl); cudaFree(s->work); cudaFree(s->scan_blk); cudaFree(s->cell); cudaFree(s->pcell);
-  cudaFree(s->xi); cudaFree(s->inj); cudaFree(s->stage); cudaFree(s->faces); cudaFree(s->lr_tab); cudaFree(s->status);
+  cudaFree(s->xi); cudaFree(s->inj); cudaFree(s->stage); cudaFree(s->faces); cudaFree(s->lr_tab); cudaFree(s->status); cudaFree(s->dstep);
   lr2d_free(*s);
   if (s->graph) cudaGraphExecDestroy(s->graph);
   for (auto& r : s->prof_recs) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
@@ -409,6 +419,83 @@ int mcpm_end_step(mcpm_session* s) {
   return MCPM_OK;
 }
 
+// one iteration of the loop body as fused kernels; returns the launches
+static int step_once(mcpm_session* s, uint32_t stages) {
+  const int m = s->cfg.model;
+  int n = 0;
+  if (s->needs_rebin) { s->sorted = false; s->needs_rebin = false; }
+  if (!s->sorted) {
+    if (!s->keys_current) n += T_BIN(launch_bin(*s, s->step));
+    n += T_SCAN(launch_scan(*s));
+    n += T_SCAT(launch_scatter(*s));
+  } else {
+    cudaMemsetAsync(s->work, 0, WK_COUNT * 4, s->stream);
+  }
+  n += T_MOM(launch_moments(*s));
+  n += T_SOLVE(launch_solve(*s, (m == MCPM_MODEL_FP_DENSE && s->step > 0) ? 1 : 0));
+  n += T_LR(launch_node_density(*s));
+  s->nodes_valid = s->lr2d != nullptr;
+  if (m == MCPM_MODEL_ESMC) n += T_ESMC(launch_esmc(*s));
+  if (s->cfg.long_range != MCPM_LR_NONE) n += T_LR(launch_long_range(*s));
+  n += T_UPD(launch_update(*s, stages, 0));
+  k_step_advance<<<1, 1, 0, s->stream>>>(s->dstep);
+  ++n;
+  s->step++;
+  s->dstep_val = s->step;
+  s->bc_calls = 0;
+  s->keys_current = true;
+  s->sorted = false;
+  return n;
+}
+
+// everything a captured step depends on besides device memory
+static uint64_t graph_signature(const mcpm_session* s, uint32_t stages) {
+  uint64_t h = 1469598103934665603ull;
+  auto mix = [&](uint64_t v) { h = (h ^ v) * 1099511628211ull; };
+  mix((uint64_t)(uintptr_t)s->stream);
+  mix((uint64_t)s->cur);
+  mix(stages);
+  mix((uint64_t)s->tune.wcap);
+  mix((uint64_t)s->tune.bcap);
+  mix((uint64_t)s->tune.grid_mom);
+  mix((uint64_t)s->tune.grid_upd);
+  mix((uint64_t)s->rng_mode);
+  return h;
+}
+
+// record two steady-state steps into s->graph; the host-side state is left
+// as before the capture (nothing has run yet)
+static int capture_pair(mcpm_session* s, uint32_t stages, uint64_t sig) {
+  if (s->graph) { cudaGraphExecDestroy(s->graph); s->graph = nullptr; }
+  int rc = after_launch(s, sync_dstep(*s), "step");
+  if (rc) return rc;
+  const int step0 = s->step, cur0 = s->cur, dval0 = s->dstep_val;
+  const int64_t launches0 = s->launches;
+  cudaGraph_t g = nullptr;
+  if (cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+    cudaGetLastError();
+    s->use_graphs = false;
+    return MCPM_OK;
+  }
+  int n = step_once(s, stages);
+  n += step_once(s, stages);
+  cudaError_t e = cudaStreamEndCapture(s->stream, &g);
+  s->step = step0; s->cur = cur0; s->dstep_val = dval0; s->launches = launches0;
+  s->keys_current = true; s->sorted = false; s->needs_rebin = false;
+  if (e == cudaSuccess && g) e = cudaGraphInstantiate(&s->graph, g, 0);
+  if (g) cudaGraphDestroy(g);
+  if (e != cudaSuccess) {
+    // a stream that cannot be captured: run the steps eagerly from now on
+    cudaGetLastError();
+    s->graph = nullptr;
+    s->use_graphs = false;
+    return MCPM_OK;
+  }
+  s->graph_sig = sig;
+  s->graph_launches = n;
+  return MCPM_OK;
+}
+
 int mcpm_step(mcpm_session* s, int32_t n_steps) {
   if (!s || !s->have_particles || n_steps < 0) return fail(s, MCPM_ERR_STATE, "step: no particles");
   const int m = s->cfg.model;
@@ -424,30 +511,36 @@ int mcpm_step(mcpm_session* s, int32_t n_steps) {
   if (m == MCPM_MODEL_FP_DENSE) stages |= ST_DFP;
   if (s->cfg.long_range != MCPM_LR_NONE) stages |= ST_LR;
   if (!s->need_old) stages &= ~ST_OLD;
-  for (int it = 0; it < n_steps; ++it) {
-    int n = 0;
-    if (s->needs_rebin) { s->sorted = false; s->needs_rebin = false; }
-    if (!s->sorted) {
-      if (!s->keys_current) n += T_BIN(launch_bin(*s, s->step));
-      n += T_SCAN(launch_scan(*s));
-      n += T_SCAT(launch_scatter(*s));
-    } else {
-      cudaMemsetAsync(s->work, 0, WK_COUNT * 4, s->stream);
-    }
-    n += T_MOM(launch_moments(*s));
-    n += T_SOLVE(launch_solve(*s, (m == MCPM_MODEL_FP_DENSE && s->step > 0) ? 1 : 0));
-    n += T_LR(launch_node_density(*s));
-    s->nodes_valid = s->lr2d != nullptr;
-    if (m == MCPM_MODEL_ESMC) n += T_ESMC(launch_esmc(*s));
-    if (s->cfg.long_range != MCPM_LR_NONE) n += T_LR(launch_long_range(*s));
-    n += T_UPD(launch_update(*s, stages, 0));
-    s->step++;
-    s->bc_calls = 0;
-    s->keys_current = true;
-    s->sorted = false;
-    int rc = after_launch(s, n, "step");
-    if (rc) return rc;
+  int it = 0, rc;
+  // eager steps until the layout is in its steady state (binned by the
+  // previous step's update kernel, not yet reordered)
+  while (it < n_steps && (s->needs_rebin || s->sorted || !s->keys_current || n_steps - it < 2 || s->prof ||
+                          !s->use_graphs)) {
+    if ((rc = after_launch(s, step_once(s, stages), "step"))) return rc;
+    ++it;
   }
+  // then pairs of steps as one CUDA graph: the scatter ping-pongs the buffer
+  // pair, so two steps leave every pointer where it started; the step number
+  // the kernels read lives on the device and the graph advances it
+  const int pairs = (n_steps - it) / 2;
+  if (pairs > 0) {
+    const uint64_t sig = graph_signature(s, stages);
+    if (!s->graph || s->graph_sig != sig) {
+      if ((rc = capture_pair(s, stages, sig))) return rc;
+    }
+    if (s->graph) {
+      if ((rc = after_launch(s, sync_dstep(*s), "step"))) return rc;
+      for (int p = 0; p < pairs; ++p)
+        if ((rc = cuda_check(s, cudaGraphLaunch(s->graph, s->stream), "graph launch"))) return rc;
+      s->launches += (int64_t)pairs * s->graph_launches;
+      s->step += 2 * pairs;
+      s->dstep_val = s->step;
+      it += 2 * pairs;
+      s->nodes_valid = s->lr2d != nullptr;
+    }
+  }
+  for (; it < n_steps; ++it)
+    if ((rc = after_launch(s, step_once(s, stages), "step"))) return rc;
   return mcpm_check_status(s);
 }
 
