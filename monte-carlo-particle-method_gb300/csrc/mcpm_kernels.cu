@@ -1384,6 +1384,7 @@ template <typename real> static int update_impl(Session& s, uint32_t stages, int
   a.Vn = lr2d_potential(s);
   size_t sm = update_smem<real>(s);
   if (stages == ST_FUSED_FP) k_update<real, ST_FUSED_FP><<<s.tune.grid_upd, 256, sm, s.stream>>>(a);
+  else if (stages == (ST_FUSED_FP | ST_LR)) k_update<real, ST_FUSED_FP | ST_LR><<<s.tune.grid_upd, 256, sm, s.stream>>>(a);
   else k_update<real, 0u><<<s.tune.grid_upd, 256, sm, s.stream>>>(a);
   return n + 1;
 }
@@ -1417,6 +1418,10 @@ cudaError_t update_set_smem_max() {
     e = cudaFuncSetAttribute(k_update<float, ST_FUSED_FP>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(k_update<double, ST_FUSED_FP>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_update<float, ST_FUSED_FP | ST_LR>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_update<double, ST_FUSED_FP | ST_LR>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
   return e;
 }
 int update_occupancy(const Session& s) {

@@ -33,6 +33,11 @@
 //   discrete sine transform: U = S_y ((S_y B S_x) / mu) S_x with the
 //   orthonormal DST-I matrices S and mu_qp = kx_p my_q + mx_p ky_q +
 //   bst^2 vol mx_p my_q.  The reference solves the same system with PARDISO.
+//   The operator's condition number is about 2 (mu lies in [~3.3, ~5.5] for
+//   bst ~ 2.3 and unit cells), so the transforms run in FP32 and the solution
+//   is accumulated in FP64 by iterative refinement: U += solve32(b - L U),
+//   with the residual of the 9-point operator taken in FP64; each pass gains
+//   ~6 digits.
 //   Then the analytic near-field part is subtracted (src/FEM.cpp:491-546).
 // The kick (src/FEM.cpp:567-578, :703-714): U -= grad_bilinear(V) coef / m dt
 // with coef = phi (direct) or ast (screened Poisson), applied by the particle
@@ -62,7 +67,11 @@ struct LR2D {
   double* V = nullptr;      // [nn] node potential
   double* nnd = nullptr;    // [C][4] nodal densities n_n
   int32_t* qc = nullptr;    // [C][4] particles per cell quadrant
-  double *Sx = nullptr, *Sy = nullptr, *mu = nullptr, *B = nullptr, *T = nullptr;
+  float *Sx = nullptr, *Sy = nullptr, *mu = nullptr, *Bf = nullptr, *Tf = nullptr;  // FP32 transforms
+  double *B = nullptr, *U = nullptr;  // FP64 right-hand side and solution (interior, rows y)
+  double lambda2vol;                  // bst^2 vol, the mass coefficient of the operator
+  double near1, near2;                // the near-field constants of src/FEM.cpp:491-496
+  int iters;                          // refinement passes
   int* wall = nullptr;      // [n_wall] ids of the wall nodes
   int n_wall;
   size_t smem;              // dynamic shared memory of the node kernels
@@ -91,12 +100,22 @@ __global__ void k_quadrants(DevConsts k, const int32_t* off, const int32_t* cnt,
     const int j = c % k.N0, kk = c / k.N0;
     const double cx = 0.5 * ((double)j * k.dx + (double)(j + 1) * k.dx);
     const double cy = 0.5 * ((double)kk * k.dy + (double)(kk + 1) * k.dy);
+    // x < cx in exact arithmetic, compared in the state's precision: for
+    // float x, x < cx  <=>  x < the smallest float >= cx
+    real tx, ty;
+    if constexpr (sizeof(real) == 4) {
+      float fx = (float)cx, fy = (float)cy;
+      tx = (double)fx >= cx ? fx : nextafterf(fx, INFINITY);
+      ty = (double)fy >= cy ? fy : nextafterf(fy, INFINITY);
+    } else {
+      tx = cx; ty = cy;
+    }
     const int64_t s0 = off[c];
     const int n = cnt[c];
     int q[4] = {0, 0, 0, 0};
     for (int i = lane; i - lane < n; i += 32) {
       int quad = -1;
-      if (i < n) quad = ((double)x1[s0 + i] < cx ? 0 : 1) + ((double)x2[s0 + i] < cy ? 0 : 2);
+      if (i < n) quad = (x1[s0 + i] < tx ? 0 : 1) + (x2[s0 + i] < ty ? 0 : 2);
 #pragma unroll
       for (int t = 0; t < 4; ++t) q[t] += __popc(__ballot_sync(FULL, quad == t));
     }
@@ -211,39 +230,85 @@ __global__ void k_sp_rhs(LR2D t, DevConsts k) {
   }
 }
 
-// C[M][N] = A[M][K] B[K][N] (row-major), optionally divided elementwise by D;
-// 16 x 16 outputs per block, K staged through shared memory in slices of 16
-__global__ void __launch_bounds__(256) k_dgemm(int M, int N, int K, const double* A, const double* B, double* C,
-                                               const double* D) {
-  __shared__ double As[16][17], Bs[16][17];
+// C[M][N] = A[M][K] B[K][N] (row-major, FP32): 32 x 32 outputs per block of
+// 256 threads, 2 x 2 per thread, K staged through shared memory in slices of
+// 32.  Epilogue: mode 0 store, 1 store divided elementwise by D, 2 U = acc
+// (FP64), 3 U += acc (FP64).
+__global__ void __launch_bounds__(256) k_sgemm(int M, int N, int K, const float* A, const float* B, float* C,
+                                               const float* D, double* U, int mode) {
+  __shared__ float As[32][33], Bs[32][33];
   const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-  const int row = blockIdx.y * 16 + ty, col = blockIdx.x * 16 + tx;
-  double acc = 0.0;
-  for (int k0 = 0; k0 < K; k0 += 16) {
-    As[ty][tx] = (row < M && k0 + tx < K) ? A[(size_t)row * K + k0 + tx] : 0.0;
-    Bs[ty][tx] = (k0 + ty < K && col < N) ? B[(size_t)(k0 + ty) * N + col] : 0.0;
+  const int r0 = blockIdx.y * 32, c0 = blockIdx.x * 32;
+  float acc[2][2] = {{0.f, 0.f}, {0.f, 0.f}};
+  for (int k0 = 0; k0 < K; k0 += 32) {
+    for (int e = threadIdx.x; e < 32 * 32; e += 256) {
+      const int r = e >> 5, q = e & 31;
+      As[r][q] = (r0 + r < M && k0 + q < K) ? A[(size_t)(r0 + r) * K + k0 + q] : 0.f;
+      Bs[r][q] = (k0 + r < K && c0 + q < N) ? B[(size_t)(k0 + r) * N + c0 + q] : 0.f;
+    }
     __syncthreads();
-#pragma unroll
-    for (int q = 0; q < 16; ++q) acc += As[ty][q] * Bs[q][tx];
+#pragma unroll 8
+    for (int q = 0; q < 32; ++q) {
+      const float a0 = As[2 * ty][q], a1 = As[2 * ty + 1][q];
+      const float b0 = Bs[q][2 * tx], b1 = Bs[q][2 * tx + 1];
+      acc[0][0] = fmaf(a0, b0, acc[0][0]); acc[0][1] = fmaf(a0, b1, acc[0][1]);
+      acc[1][0] = fmaf(a1, b0, acc[1][0]); acc[1][1] = fmaf(a1, b1, acc[1][1]);
+    }
     __syncthreads();
   }
-  if (row < M && col < N) C[(size_t)row * N + col] = D ? acc / D[(size_t)row * N + col] : acc;
+#pragma unroll
+  for (int i = 0; i < 2; ++i)
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+      const int row = r0 + 2 * ty + i, col = c0 + 2 * tx + j;
+      if (row >= M || col >= N) continue;
+      const size_t o = (size_t)row * N + col;
+      if (mode == 0) C[o] = acc[i][j];
+      else if (mode == 1) C[o] = acc[i][j] / D[o];
+      else if (mode == 2) U[o] = (double)acc[i][j];
+      else U[o] += (double)acc[i][j];
+    }
+}
+
+// the right-hand side in FP32 for the first pass
+__global__ void k_to_f32(const double* a, float* b, int n) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) b[i] = (float)a[i];
+}
+
+// residual b - L U of the interior rows in FP64 (the wall columns are in b):
+// L = K (x) M + M (x) K + c M (x) M on the 3 x 3 neighbourhood, with the 1-D
+// unit stiffness K (2, -1) and mass M (2/3, 1/6)
+__global__ void k_sp_residual(LR2D t) {
+  const int nx = t.nx, ny = t.ny;
+  const double c = t.lambda2vol;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < nx * ny; e += gridDim.x * blockDim.x) {
+    const int p = e % nx, q = e / nx;
+    double lu = 0.0;
+#pragma unroll
+    for (int dq = -1; dq <= 1; ++dq) {
+      const int qq = q + dq;
+      if (qq < 0 || qq >= ny) continue;
+      const double ky = dq == 0 ? 2.0 : -1.0, my = dq == 0 ? 2.0 / 3.0 : 1.0 / 6.0;
+#pragma unroll
+      for (int dp = -1; dp <= 1; ++dp) {
+        const int pp = p + dp;
+        if (pp < 0 || pp >= nx) continue;
+        const double kx = dp == 0 ? 2.0 : -1.0, mx = dp == 0 ? 2.0 / 3.0 : 1.0 / 6.0;
+        lu += (kx * my + mx * ky + c * mx * my) * t.U[(size_t)qq * nx + pp];
+      }
+    }
+    t.Bf[e] = (float)(t.B[e] - lu);
+  }
 }
 
 // node potential of the screened-Poisson path: the solved interior values
 // or the wall values, minus the analytic near-field part
 // (src/FEM.cpp:491-546; the corner and edge index rules restated)
-__global__ void k_sp_finish(LR2D t, DevConsts k) {
+__global__ void k_sp_finish(LR2D t, double dummy, double dummy2) {
   const int N0 = t.N0, N1 = t.N1;
-  double dummy = 1.0 - (k.sigma * k.bst + 1.0) * exp(-k.bst * k.sigma);
-  dummy = dummy / k.bst / k.bst;
-  const double b = k.bst, sg = k.sigma;
-  double dummy2 = (-1.0 / 6.0 * pow(b, 3.0) * pow(sg, 3.0) - 1.0 / 2.0 * pow(b, 2.0) * pow(sg, 2.0) - b * sg +
-                   exp(b * sg) - 1) * exp(-b * sg) / pow(b, 4.0);
-  dummy2 = dummy2 / pow(k.dx, 2.0);
   for (int id = blockIdx.x * blockDim.x + threadIdx.x; id < t.nn; id += gridDim.x * blockDim.x) {
     const int i = id % (N0 + 1), j = id / (N0 + 1);
-    double x = (i > 0 && i < N0 && j > 0 && j < N1) ? t.B[(size_t)(j - 1) * t.nx + (i - 1)] : t.V[id];
+    double x = (i > 0 && i < N0 && j > 0 && j < N1) ? t.U[(size_t)(j - 1) * t.nx + (i - 1)] : t.V[id];
     int ii = i, jj = j, kq = 0;
     int ipm[4] = {0, -1, 0, 0}, jpm[4] = {0, 0, 0, -1}, kpm[4] = {1, 0, 2, 0};
     if (i == N0) { ii = i - 1; jj = j; kq = 1; kpm[0] = kq; }
@@ -455,19 +520,31 @@ int lr2d_setup(Session& s) {
     dst_matrix(t->nx, Sx, kx, mx);
     dst_matrix(t->ny, Sy, ky, my);
     const double c = k.bst * k.bst * (k.dx * k.dy * k.dz);
-    std::vector<double> mu((size_t)t->nx * t->ny);
+    std::vector<float> mu((size_t)t->nx * t->ny), Sxf(Sx.begin(), Sx.end()), Syf(Sy.begin(), Sy.end());
     for (int q = 0; q < t->ny; ++q)
-      for (int p = 0; p < t->nx; ++p) mu[(size_t)q * t->nx + p] = kx[p] * my[q] + mx[p] * ky[q] + c * mx[p] * my[q];
+      for (int p = 0; p < t->nx; ++p)
+        mu[(size_t)q * t->nx + p] = (float)(kx[p] * my[q] + mx[p] * ky[q] + c * mx[p] * my[q]);
+    t->lambda2vol = c;
+    {
+      const double b = k.bst, sg = k.sigma;
+      double d1 = 1.0 - (sg * b + 1.0) * exp(-b * sg);
+      t->near1 = d1 / b / b;
+      double d2 = (-1.0 / 6.0 * pow(b, 3) * pow(sg, 3) - 1.0 / 2.0 * pow(b, 2) * pow(sg, 2) - b * sg + exp(b * sg) - 1) *
+                  exp(-b * sg) / pow(b, 4);
+      t->near2 = d2 / pow(k.dx, 2);
+    }
+    t->iters = s.prec == MCPM_FP64 ? 3 : 2;
     std::vector<int> wall;
     for (int j = 0; j <= k.N1; ++j)
       for (int i = 0; i <= k.N0; ++i)
         if (i == 0 || i == k.N0 || j == 0 || j == k.N1) wall.push_back(j * (k.N0 + 1) + i);
     t->n_wall = (int)wall.size();
     const size_t nxy = (size_t)t->nx * t->ny;  // T: the transforms' scratch
-    ok = A((void**)&t->Sx, Sx.size() * 8) && H(t->Sx, Sx.data(), Sx.size() * 8) &&
-         A((void**)&t->Sy, Sy.size() * 8) && H(t->Sy, Sy.data(), Sy.size() * 8) &&
-         A((void**)&t->mu, nxy * 8) && H(t->mu, mu.data(), nxy * 8) && A((void**)&t->B, nxy * 8) &&
-         A((void**)&t->T, nxy * 8) && A((void**)&t->wall, wall.size() * 4) &&
+    ok = A((void**)&t->Sx, Sxf.size() * 4) && H(t->Sx, Sxf.data(), Sxf.size() * 4) &&
+         A((void**)&t->Sy, Syf.size() * 4) && H(t->Sy, Syf.data(), Syf.size() * 4) &&
+         A((void**)&t->mu, nxy * 4) && H(t->mu, mu.data(), nxy * 4) && A((void**)&t->B, nxy * 8) &&
+         A((void**)&t->U, nxy * 8) && A((void**)&t->Bf, nxy * 4) && A((void**)&t->Tf, nxy * 4) &&
+         A((void**)&t->wall, wall.size() * 4) &&
          H(t->wall, wall.data(), wall.size() * 4);
   }
   if (!ok) { s.err = "2-D long-range tables: out of device memory"; return 1; }
@@ -485,7 +562,8 @@ void lr2d_free(Session& s) {
   LR2D* t = s.lr2d;
   if (!t) return;
   cudaFree(t->W); cudaFree(t->exc_off); cudaFree(t->exc_i); cudaFree(t->exc_w); cudaFree(t->V); cudaFree(t->nnd);
-  cudaFree(t->qc); cudaFree(t->Sx); cudaFree(t->Sy); cudaFree(t->mu); cudaFree(t->B); cudaFree(t->T); cudaFree(t->wall);
+  cudaFree(t->qc); cudaFree(t->Sx); cudaFree(t->Sy); cudaFree(t->mu); cudaFree(t->B); cudaFree(t->U); cudaFree(t->Bf); cudaFree(t->Tf);
+  cudaFree(t->wall);
   delete t;
   s.lr2d = nullptr;
 }
@@ -526,14 +604,24 @@ int launch_long_range_2d(Session& s) {
     k_node_potential<<<blocks_for(t->n_wall, 128, cap), 128, t->smem, s.stream>>>(*t, n, 1);
     k_sp_rhs<<<blocks_for((long)t->nx * t->ny, 256, cap), 256, 0, s.stream>>>(*t, s.k);
     const int nx = t->nx, ny = t->ny;
-    dim3 g((nx + 15) / 16, (ny + 15) / 16);
-    // B <- S_y B S_x / mu, then U = S_y B S_x  (rows y, columns x)
-    k_dgemm<<<g, 256, 0, s.stream>>>(ny, nx, ny, t->Sy, t->B, t->T, nullptr);
-    k_dgemm<<<g, 256, 0, s.stream>>>(ny, nx, nx, t->T, t->Sx, t->B, t->mu);
-    k_dgemm<<<g, 256, 0, s.stream>>>(ny, nx, ny, t->Sy, t->B, t->T, nullptr);
-    k_dgemm<<<g, 256, 0, s.stream>>>(ny, nx, nx, t->T, t->Sx, t->B, nullptr);
-    k_sp_finish<<<blocks_for(t->nn, 256, cap), 256, 0, s.stream>>>(*t, s.k);
-    launches = 7;
+    dim3 g((nx + 31) / 32, (ny + 31) / 32);
+    const int nxy = nx * ny;
+    k_to_f32<<<blocks_for(nxy, 256, cap), 256, 0, s.stream>>>(t->B, t->Bf, nxy);
+    launches = 3;
+    for (int it = 0; it < t->iters; ++it) {
+      if (it > 0) {
+        k_sp_residual<<<blocks_for(nxy, 256, cap), 256, 0, s.stream>>>(*t);
+        ++launches;
+      }
+      // delta = S_y ((S_y r S_x) / mu) S_x  (rows y, columns x); U (+)= delta
+      k_sgemm<<<g, 256, 0, s.stream>>>(ny, nx, ny, t->Sy, t->Bf, t->Tf, nullptr, nullptr, 0);
+      k_sgemm<<<g, 256, 0, s.stream>>>(ny, nx, nx, t->Tf, t->Sx, t->Bf, t->mu, nullptr, 1);
+      k_sgemm<<<g, 256, 0, s.stream>>>(ny, nx, ny, t->Sy, t->Bf, t->Tf, nullptr, nullptr, 0);
+      k_sgemm<<<g, 256, 0, s.stream>>>(ny, nx, nx, t->Tf, t->Sx, nullptr, nullptr, t->U, it == 0 ? 2 : 3);
+      launches += 4;
+    }
+    k_sp_finish<<<blocks_for(t->nn, 256, cap), 256, 0, s.stream>>>(*t, t->near1, t->near2);
+    ++launches;
   }
   if (s.prec == MCPM_FP32) {
     k_lr2d_pack<<<blocks_for(s.C, 256, cap), 256, 0, s.stream>>>(s.k, t->V, s.pcell);

@@ -8,6 +8,8 @@ workload:
           the 129 MB L2, a few hundred MB on the device)
   esmc    n x n cells of the 2-D ESMC Couette box (100 particles per cell)
   slab    the 1-D Enskog-Vlasov slab with n cells (1000 particles per cell)
+  vlasov  n x n cells of the 2-D Enskog-Vlasov box with the screened-Poisson
+          force (244 particles per cell on average: 16.0M at n = 256)
 
 Runs three fused steps (the first launches of each kernel are the warm-up,
 so an ncu capture takes `-s 2 -c 1` of the kernel it names) and exits 0.
@@ -31,6 +33,9 @@ def main(argv):
         cfg, parts = W.uneven_cells_2d(n_cells=(n, n), precision=prec, streaming=True)
     elif kind == "esmc":
         cfg, parts = W.esmc_box_2d(n_cells=(n, n), precision=prec)
+    elif kind == "vlasov":
+        cfg, parts = W.vlasov_box_2d(n_cells=(n, n), total=244 * n * n, precision=prec,
+                                     long_range=mcpm.LR_SCREENED_POISSON, model=mcpm.MODEL_FP_DENSE)
     elif kind == "slab":
         cfg, parts = W.vlasov_slab_1d(n_cells=n, precision=prec)
     else:
