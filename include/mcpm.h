@@ -252,7 +252,7 @@ int mcpm_set_stream(mcpm_session* s, void* stream);
 /* Kernel classes timed by the profiling mode, in mcpm_profile_read order. */
 enum mcpm_kernel_class {
   MCPM_K_BIN = 0, MCPM_K_SCAN, MCPM_K_SCATTER, MCPM_K_MOMENTS, MCPM_K_SOLVE,
-  MCPM_K_ESMC, MCPM_K_LONG_RANGE, MCPM_K_UPDATE, MCPM_K_COUNT
+  MCPM_K_ESMC, MCPM_K_LONG_RANGE, MCPM_K_UPDATE, MCPM_K_SURROGATE, MCPM_K_COUNT
 };
 /* enable != 0: bracket every kernel launch with CUDA events on the launch
    stream and accumulate device time per kernel class. */
@@ -288,6 +288,101 @@ int mcpm_autotune(mcpm_session* s, int32_t steps, int32_t* chosen);
 int mcpm_poisson_force_1d_noalloc(const double* n_cell, int32_t n_cells,
                                   const mcpm_config* cfg, double* F2,
                                   void* stream);
+/* ---- learned Vlasov force of a 2-D box --------------------------------- */
+/* No counterpart in the reference (its only learned model, the hybrid NN/GPR
+   of src/hybrid.cpp, is not on the particle path).  A 4-layer convolutional
+   operator on the N1 x N0 cell grid maps the nodal and cell densities that
+   the node-grid force reads (compute_SP_2D / compute_Vlasov_2D inputs,
+   src/FEM.cpp:249, :613) to the corner-potential differences of every cell
+   that the kick applies (src/FEM.cpp:567-578, :703-714):
+     input  [cells][MCPM_SUR_IN] bf16 (raw uint16 bits): v_k = 10 (b n_n[k] - 0.25)
+            for the 4 corner nodal densities and v_4 = 10 (b n - 0.25), each
+            as hi = bf16(v_k) in channel k and lo = bf16(v_k - hi) in channel
+            6 + k; channel 5 = 1; channels 11..15 = 0;
+     conv3x3 16->64, ReLU, 64->64, ReLU, 64->64, ReLU, 64->16 (zero padding);
+     output [cells][MCPM_SUR_OUT] fp32 = (V1-V0, V3-V2, V2-V0, V3-V1) / out_scale.
+   Parameters: MCPM_SUR_NPARAM floats, conv weights [co][tap][ci] with
+   tap = 3 (dy + 1) + (dx + 1) followed by the biases, per layer:
+   W1[64][9][16] b1[64] W2[64][9][64] b2[64] W3[64][9][64] b3[64]
+   W4[16][9][64] b4[16] (input channels 11..15 and outputs 4..15 unused).
+   Forward, backward and the Adam step run on the GPU in BF16 with FP32
+   accumulation.  Device pointers below are on the surrogate's device; the
+   standalone calls run on the surrogate's own stream and synchronise. */
+typedef struct mcpm_surrogate mcpm_surrogate;
+#define MCPM_SUR_IN 16
+#define MCPM_SUR_OUT 4
+#define MCPM_SUR_NPARAM 92368
+/* Network for batches of up to max_batch grids of n1 x n0 cells. */
+int mcpm_surrogate_create(int32_t n0, int32_t n1, int32_t max_batch, mcpm_surrogate** out);
+int mcpm_surrogate_destroy(mcpm_surrogate* m);
+const char* mcpm_surrogate_last_error(const mcpm_surrogate* m);
+/* Sets the parameters (host, MCPM_SUR_NPARAM floats) and the output scale,
+   and clears the Adam moments. */
+int mcpm_surrogate_set_params(mcpm_surrogate* m, const float* params, int64_t n, double out_scale);
+int mcpm_surrogate_get_params(mcpm_surrogate* m, float* params, int64_t n);
+/* tcgen05 != 0: the 64->64 layers of inference (forward, and the step's
+   force) run on the tcgen05 tensor cores; 0: on mma.sync, the path the
+   backward pass differentiates.  Default 1. */
+int mcpm_surrogate_set_tensor_path(mcpm_surrogate* m, int32_t tcgen05);
+/* tcgen05 launches so far and whether that path is on (it turns itself off,
+   with a message in mcpm_surrogate_last_error, if a TMA descriptor is
+   refused). */
+int mcpm_surrogate_launches(const mcpm_surrogate* m, int64_t* tcgen05_launches, int32_t* tcgen05_on);
+/* y[batch][cells][MCPM_SUR_OUT] = network(x[batch][cells][MCPM_SUR_IN]),
+   device pointers, outputs in units of out_scale. */
+int mcpm_surrogate_forward(mcpm_surrogate* m, const uint16_t* x, int32_t batch, float* y);
+/* Loss L = mean over cells and outputs of (y - target_scale target)^2 and
+   its gradient with respect to every parameter (host grad[MCPM_SUR_NPARAM],
+   may be NULL); loss[2] = (sum of squared errors, sum of squared scaled
+   targets), may be NULL. */
+int mcpm_surrogate_gradients(mcpm_surrogate* m, const uint16_t* x, const float* target, int32_t batch,
+                             double target_scale, float* grad, double* loss);
+/* One Adam step (beta 0.9 / 0.999, eps 1e-8, step number t >= 1) on the
+   loss of mcpm_surrogate_gradients.  loss may be NULL (no synchronisation). */
+int mcpm_surrogate_train_step(mcpm_surrogate* m, const uint16_t* x, const float* target, int32_t batch,
+                              double target_scale, double lr, int32_t t, double* loss);
+int mcpm_surrogate_sync(mcpm_surrogate* m);
+
+/* Training snapshots from the plain node-grid force of a 2-D long-range
+   session: for snapshot i the packing fraction
+     n b(x, y) = f[0] + sum_w f[1+4w] sin(2 pi (f[2+4w] x / L0 + f[3+4w] y / L1) + f[4+4w]),
+   clipped to [0.05, 0.45] (f = fields + i (1 + 4 n_waves)), gives quadrant
+   counts round(lambda + sqrt(lambda) z) per cell quadrant (lambda =
+   n vol / 4 / Fn, z a Philox normal keyed by seed, i, quadrant), from which
+   the nodal densities, the cell densities and the session's plain force
+   (long_range 1 or 3) are computed; x[i] (device, [cells][MCPM_SUR_IN]) gets
+   the network input and y[i] (device, [cells][4]) the corner-potential
+   differences.  Overwrites the session's cell densities and nodal data
+   (mcpm_get_node_density / mcpm_get_node_potential then describe the last
+   snapshot). */
+int mcpm_vlasov_snapshots(mcpm_session* s, int32_t n_snap, const double* fields, int32_t n_waves, uint64_t seed,
+                          uint16_t* x, float* y);
+/* Attaches a trained network (m NULL detaches) to an FP32 2-D long-range
+   session of the same grid: mcpm_step then takes the Vlasov kick from the
+   network, and every judge_every steps (the first step included) runs the
+   plain path as the judge, compares the two kicks and keeps the plain one
+   for that step; while the relative L2 error of the kick coefficients of
+   the last judge step exceeds threshold the plain path supplies the force.
+   The network's buffers are used on the session's stream. */
+int mcpm_attach_surrogate(mcpm_session* s, mcpm_surrogate* m, int32_t judge_every, double threshold);
+typedef struct mcpm_surrogate_stats {
+  double last_error;        /* relative L2 kick error of the last judge step (-1: none yet) */
+  int64_t judged;           /* judge steps                                   */
+  int64_t takeovers;        /* judge steps whose error exceeded the threshold */
+  int64_t surrogate_steps;  /* steps whose force came from the network        */
+  int64_t plain_steps;      /* steps whose force came from the plain path     */
+  int32_t active;           /* the network supplies the force now             */
+} mcpm_surrogate_stats;
+int mcpm_get_surrogate_stats(mcpm_session* s, mcpm_surrogate_stats* out);
+/* Re-evaluates the 2-D Vlasov kick of the last cell_update (or step) with
+   the plain path (method 0) or the attached network (method 1) into the
+   session's per-cell kick coefficients. */
+int mcpm_eval_vlasov_2d(mcpm_session* s, int32_t method);
+/* The per-cell kick coefficients of an FP32 2-D long-range session,
+   [cells][4] floats (LA1, LB1, LA2, LB2: U1 -= LA1 + LB1 eta,
+   U2 -= LA2 + LB2 xi, xi/eta the particle's bilinear coordinates). */
+int mcpm_get_kick_2d(mcpm_session* s, float* out);
+
 /* Number of kernel launches the session issued since creation. */
 int64_t mcpm_kernel_launches(const mcpm_session* s);
 

@@ -94,7 +94,8 @@ struct Tuning {
   int grid_upd;
 };
 
-struct LR2D;  // 2-D long-range tables and buffers (mcpm_lr2d.cu)
+struct LR2D;          // 2-D long-range tables and buffers (mcpm_lr2d.cu)
+struct SurrogateNet;  // learned 2-D Vlasov force (mcpm_surrogate.cu)
 
 struct Session {
   mcpm_config cfg{};
@@ -155,6 +156,18 @@ struct Session {
   uint64_t graph_sig = 0;
   int graph_launches = 0;
   bool use_graphs = true;
+  // learned 2-D Vlasov force: attached network (not owned), the plain path
+  // re-run as judge every sur_every steps, taking over while the relative
+  // kick error exceeds sur_thr
+  SurrogateNet* sur = nullptr;
+  int sur_every = 10;
+  double sur_thr = 0.01;
+  bool sur_active = true;       // the network supplies the force
+  bool sur_judge_now = false;   // this step runs both paths and compares
+  double* sur_err = nullptr;    // device [2]: sum |kick_net - kick_plain|^2, sum |kick_plain|^2
+  double* sur_err_h = nullptr;  // pinned host copy
+  double sur_last_err = -1.0;
+  int64_t sur_judged = 0, sur_takeovers = 0, sur_steps = 0, sur_plain_steps = 0;
   std::string err;
 };
 
@@ -176,6 +189,9 @@ int lr2d_setup(Session& s);
 void lr2d_free(Session& s);
 int launch_node_density(Session& s);
 int launch_long_range_2d(Session& s);
+int launch_node_density_from(Session& s, const int32_t* qc);
+int32_t* lr2d_quadrants(Session& s);
+double* lr2d_node_density_mut(Session& s);
 const double* lr2d_potential(const Session& s);
 const double* lr2d_node_density(const Session& s);
 int lr2d_num_nodes(const Session& s);

@@ -575,9 +575,21 @@ int lr2d_num_nodes(const Session& s) { return s.lr2d ? s.lr2d->nn : 0; }
 // ------------------------------------------------------------ launches --
 static int blocks_for(long n, int bs, int cap) { return (int)std::max(1L, std::min((n + bs - 1) / bs, (long)cap)); }
 
+int32_t* lr2d_quadrants(Session& s) { return s.lr2d ? s.lr2d->qc : nullptr; }
+double* lr2d_node_density_mut(Session& s) { return s.lr2d ? s.lr2d->nnd : nullptr; }
+
+// nodal densities from given quadrant counts (training snapshots)
+int launch_node_density_from(Session& s, const int32_t* qc) {
+  LR2D* t = s.lr2d;
+  if (!t) return 0;
+  k_node_density<<<blocks_for(4L * s.C, 256, s.num_sms * 16), 256, 0, s.stream>>>(s.k, qc, t->nnd, 0);
+  return 1;
+}
+
 int launch_node_density(Session& s) {
   LR2D* t = s.lr2d;
-  if (!t || t->mode != MCPM_LR_SCREENED_POISSON) return 0;
+  // the screened-Poisson force and the learned force read them
+  if (!t || (t->mode != MCPM_LR_SCREENED_POISSON && !s.sur)) return 0;
   const int g = blocks_for((long)s.C * 32, 256, s.num_sms * 16);
   if (s.prec == MCPM_FP32) {
     const PBuf& P = s.P[s.cur];

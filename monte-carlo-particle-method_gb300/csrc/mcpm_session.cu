@@ -1,13 +1,16 @@
 // mcpm_session.cu -- the C-ABI of include/mcpm.h: session lifetime, host
 // copies, and the order in which the step's kernels run.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <new>
 
 #include "mcpm_internal.h"
+#include "mcpm_surrogate.h"
 
 namespace mcpm {
+SurrogateNet* sur_net(mcpm_surrogate* m);
 size_t update_smem_bytes(const Session& s);
 int update_occupancy(const Session& s);
 int moments_occupancy(const Session& s);
@@ -97,10 +100,12 @@ template <typename F> static int timed(mcpm_session* s, int cls, F f) {
 #define T_ESMC(x) timed(s, MCPM_K_ESMC, [&] { return (x); })
 #define T_LR(x) timed(s, MCPM_K_LONG_RANGE, [&] { return (x); })
 #define T_UPD(x) timed(s, MCPM_K_UPDATE, [&] { return (x); })
+#define T_SUR(x) timed(s, MCPM_K_SURROGATE, [&] { return (x); })
 
 static inline bool is_fp_model(int m) { return m == MCPM_MODEL_FP_DENSE || m == MCPM_MODEL_FP_IDEAL_GAS; }
 
 extern "C" {
+static int long_range_force(mcpm_session* s);
 
 int mcpm_config_derive(mcpm_config* c, int64_t n_particles) {
   if (!c) return MCPM_ERR_ARG;
@@ -258,6 +263,8 @@ int mcpm_session_destroy(mcpm_session* s) {
   cudaFree(s->list_small); cudaFree(s->list_big); cudaFree(s->wl); cudaFree(s->work); cudaFree(s->scan_blk); cudaFree(s->cell); cudaFree(s->pcell);
   cudaFree(s->xi); cudaFree(s->inj); cudaFree(s->stage); cudaFree(s->faces); cudaFree(s->lr_tab); cudaFree(s->status); cudaFree(s->dstep);
   lr2d_free(*s);
+  cudaFree(s->sur_err);
+  if (s->sur_err_h) cudaFreeHost(s->sur_err_h);
   if (s->graph) cudaGraphExecDestroy(s->graph);
   for (auto& r : s->prof_recs) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
   for (auto e : s->prof_pool) cudaEventDestroy(e);
@@ -372,7 +379,7 @@ int mcpm_velocity_update(mcpm_session* s) {
   if (s->cfg.model == MCPM_MODEL_ESMC) n += T_ESMC(launch_esmc(*s));
   else if (is_fp_model(s->cfg.model)) stages |= ST_LOAD_XI | ST_FP;
   if (s->cfg.long_range != MCPM_LR_NONE) {
-    n += T_LR(launch_long_range(*s));
+    n += long_range_force(s);
     stages |= ST_LR;
   }
   if (stages) {
@@ -419,6 +426,18 @@ int mcpm_end_step(mcpm_session* s) {
   return MCPM_OK;
 }
 
+// the long-range force of a step: the attached network while it is in
+// charge, else the plain path -- and on a judge step the plain path (whose
+// kick is kept) followed by the network and the comparison of the two
+static int long_range_force(mcpm_session* s) {
+  const double* ncell = s->cell + (size_t)MCPM_CF_N * s->C;
+  if (s->sur && s->sur_active && !s->sur_judge_now)
+    return T_SUR(sur_forward_kick(*s, lr2d_node_density(*s), ncell));
+  int n = T_LR(launch_long_range(*s));
+  if (s->sur && s->sur_judge_now) n += T_SUR(sur_judge(*s, lr2d_node_density(*s), ncell));
+  return n;
+}
+
 // one iteration of the loop body as fused kernels; returns the launches
 static int step_once(mcpm_session* s, uint32_t stages) {
   const int m = s->cfg.model;
@@ -436,7 +455,7 @@ static int step_once(mcpm_session* s, uint32_t stages) {
   n += T_LR(launch_node_density(*s));
   s->nodes_valid = s->lr2d != nullptr;
   if (m == MCPM_MODEL_ESMC) n += T_ESMC(launch_esmc(*s));
-  if (s->cfg.long_range != MCPM_LR_NONE) n += T_LR(launch_long_range(*s));
+  if (s->cfg.long_range != MCPM_LR_NONE) n += long_range_force(s);
   n += T_UPD(launch_update(*s, stages, 0));
   k_step_advance<<<1, 1, 0, s->stream>>>(s->dstep);
   ++n;
@@ -460,6 +479,8 @@ static uint64_t graph_signature(const mcpm_session* s, uint32_t stages) {
   mix((uint64_t)s->tune.grid_mom);
   mix((uint64_t)s->tune.grid_upd);
   mix((uint64_t)s->rng_mode);
+  mix((uint64_t)(uintptr_t)s->sur);
+  mix((uint64_t)s->sur_active);
   return h;
 }
 
@@ -496,32 +517,19 @@ static int capture_pair(mcpm_session* s, uint32_t stages, uint64_t sig) {
   return MCPM_OK;
 }
 
-int mcpm_step(mcpm_session* s, int32_t n_steps) {
-  if (!s || !s->have_particles || n_steps < 0) return fail(s, MCPM_ERR_STATE, "step: no particles");
-  const int m = s->cfg.model;
-  if (m == MCPM_MODEL_ESMC && !s->omega_init) {
-    // src/main.cpp:236-269: cell_update at the current positions, then the majorant
-    int rc = mcpm_cell_update(s);
-    if (rc) return rc;
-    if ((rc = mcpm_init_omega_max(s))) return rc;
-  }
-  if (s->step == 0) s->step = 1;  // the loop of src/main.cpp starts at step 1 (:389)
-  uint32_t stages = ST_BC1 | ST_OLD | ST_STREAM | ST_BC2 | ST_BC3 | ST_KEY;
-  if (is_fp_model(m)) stages |= ST_RNG | ST_FP;
-  if (m == MCPM_MODEL_FP_DENSE) stages |= ST_DFP;
-  if (s->cfg.long_range != MCPM_LR_NONE) stages |= ST_LR;
-  if (!s->need_old) stages &= ~ST_OLD;
+// n_steps consecutive steps without a judge step: eager steps until the
+// layout is in its steady state (binned by the previous step's update
+// kernel, not yet reordered), then pairs of steps as one CUDA graph (the
+// scatter ping-pongs the buffer pair, so two steps leave every pointer where
+// it started; the step number the kernels read lives on the device and the
+// graph advances it), then the odd step eagerly
+static int run_steps(mcpm_session* s, int n_steps, uint32_t stages) {
   int it = 0, rc;
-  // eager steps until the layout is in its steady state (binned by the
-  // previous step's update kernel, not yet reordered)
   while (it < n_steps && (s->needs_rebin || s->sorted || !s->keys_current || n_steps - it < 2 || s->prof ||
                           !s->use_graphs)) {
     if ((rc = after_launch(s, step_once(s, stages), "step"))) return rc;
     ++it;
   }
-  // then pairs of steps as one CUDA graph: the scatter ping-pongs the buffer
-  // pair, so two steps leave every pointer where it started; the step number
-  // the kernels read lives on the device and the graph advances it
   const int pairs = (n_steps - it) / 2;
   if (pairs > 0) {
     const uint64_t sig = graph_signature(s, stages);
@@ -541,7 +549,134 @@ int mcpm_step(mcpm_session* s, int32_t n_steps) {
   }
   for (; it < n_steps; ++it)
     if ((rc = after_launch(s, step_once(s, stages), "step"))) return rc;
+  return MCPM_OK;
+}
+
+// the judge's verdict: relative L2 error of the network's kick against the
+// plain path's on the step just run
+static int read_judge(mcpm_session* s) {
+  cudaMemcpyAsync(s->sur_err_h, s->sur_err, 16, cudaMemcpyDeviceToHost, s->stream);
+  int rc = cuda_check(s, cudaStreamSynchronize(s->stream), "judge");
+  if (rc) return rc;
+  const double se = s->sur_err_h[0], sp = s->sur_err_h[1];
+  const double e = sp > 0.0 ? sqrt(se / sp) : (se > 0.0 ? INFINITY : 0.0);
+  s->sur_last_err = e;
+  ++s->sur_judged;
+  s->sur_active = e <= s->sur_thr;
+  if (!s->sur_active) ++s->sur_takeovers;
+  return MCPM_OK;
+}
+
+int mcpm_step(mcpm_session* s, int32_t n_steps) {
+  if (!s || !s->have_particles || n_steps < 0) return fail(s, MCPM_ERR_STATE, "step: no particles");
+  const int m = s->cfg.model;
+  if (m == MCPM_MODEL_ESMC && !s->omega_init) {
+    // src/main.cpp:236-269: cell_update at the current positions, then the majorant
+    int rc = mcpm_cell_update(s);
+    if (rc) return rc;
+    if ((rc = mcpm_init_omega_max(s))) return rc;
+  }
+  if (s->step == 0) s->step = 1;  // the loop of src/main.cpp starts at step 1 (:389)
+  uint32_t stages = ST_BC1 | ST_OLD | ST_STREAM | ST_BC2 | ST_BC3 | ST_KEY;
+  if (is_fp_model(m)) stages |= ST_RNG | ST_FP;
+  if (m == MCPM_MODEL_FP_DENSE) stages |= ST_DFP;
+  if (s->cfg.long_range != MCPM_LR_NONE) stages |= ST_LR;
+  if (!s->need_old) stages &= ~ST_OLD;
+  int it = 0, rc;
+  while (it < n_steps) {
+    if (s->sur && (s->step - 1) % s->sur_every == 0) {
+      // judge step: both paths, the plain kick applied, eagerly
+      s->sur_judge_now = true;
+      rc = after_launch(s, step_once(s, stages), "step");
+      s->sur_judge_now = false;
+      if (rc || (rc = read_judge(s))) return rc;
+      ++s->sur_plain_steps;
+      ++it;
+      continue;
+    }
+    int run = n_steps - it;
+    if (s->sur) run = std::min(run, s->sur_every - (s->step - 1) % s->sur_every);
+    if (s->sur) (s->sur_active ? s->sur_steps : s->sur_plain_steps) += run;
+    if ((rc = run_steps(s, run, stages))) return rc;
+    it += run;
+  }
   return mcpm_check_status(s);
+}
+
+// ------------------------------------------------- learned Vlasov force
+int mcpm_attach_surrogate(mcpm_session* s, mcpm_surrogate* m, int32_t judge_every, double threshold) {
+  if (!s) return MCPM_ERR_ARG;
+  if (!m) {
+    s->sur = nullptr;
+    return MCPM_OK;
+  }
+  SurrogateNet* n = sur_net(m);
+  if (!s->lr2d || s->prec != MCPM_FP32)
+    return fail(s, MCPM_ERR_ARG, "attach_surrogate: needs an FP32 session with a 2-D Vlasov force");
+  if (n->N0 != s->k.N0 || n->N1 != s->k.N1) return fail(s, MCPM_ERR_ARG, "attach_surrogate: grid size differs");
+  if (judge_every < 1 || !(threshold > 0.0)) return fail(s, MCPM_ERR_ARG, "attach_surrogate: bad judge settings");
+  if (!s->sur_err) {
+    if (cudaMalloc((void**)&s->sur_err, 16) != cudaSuccess || cudaMallocHost((void**)&s->sur_err_h, 16) != cudaSuccess) {
+      cudaGetLastError();
+      return fail(s, MCPM_ERR_CUDA, "attach_surrogate: out of memory");
+    }
+  }
+  s->sur = n;
+  s->sur_every = judge_every;
+  s->sur_thr = threshold;
+  s->sur_active = true;
+  s->sur_last_err = -1.0;
+  s->sur_judged = s->sur_takeovers = s->sur_steps = s->sur_plain_steps = 0;
+  return MCPM_OK;
+}
+
+int mcpm_get_surrogate_stats(mcpm_session* s, mcpm_surrogate_stats* out) {
+  if (!s || !out) return MCPM_ERR_ARG;
+  out->last_error = s->sur_last_err;
+  out->judged = s->sur_judged;
+  out->takeovers = s->sur_takeovers;
+  out->surrogate_steps = s->sur_steps;
+  out->plain_steps = s->sur_plain_steps;
+  out->active = (s->sur && s->sur_active) ? 1 : 0;
+  return MCPM_OK;
+}
+
+int mcpm_eval_vlasov_2d(mcpm_session* s, int32_t method) {
+  if (!s || (method != 0 && method != 1)) return MCPM_ERR_ARG;
+  if (!s->lr2d || !s->nodes_valid) return fail(s, MCPM_ERR_STATE, "eval_vlasov_2d: needs a 2-D session after cell_update");
+  if (method == 1 && !s->sur) return fail(s, MCPM_ERR_STATE, "eval_vlasov_2d: no network attached");
+  const double* ncell = s->cell + (size_t)MCPM_CF_N * s->C;
+  int n = method == 0 ? T_LR(launch_long_range(*s)) : T_SUR(sur_forward_kick(*s, lr2d_node_density(*s), ncell));
+  return after_launch(s, n, "eval_vlasov_2d");
+}
+
+int mcpm_get_kick_2d(mcpm_session* s, float* out) {
+  if (!s || !out) return MCPM_ERR_ARG;
+  if (!s->lr2d || s->prec != MCPM_FP32) return fail(s, MCPM_ERR_STATE, "get_kick_2d: needs an FP32 2-D session");
+  cudaMemcpy2DAsync(out, 16, s->pcell + PF_LA1, PF_STRIDE * 4, 16, s->C, cudaMemcpyDeviceToHost, s->stream);
+  return cuda_check(s, cudaStreamSynchronize(s->stream), "get_kick_2d");
+}
+
+int mcpm_vlasov_snapshots(mcpm_session* s, int32_t n_snap, const double* fields, int32_t n_waves, uint64_t seed,
+                          uint16_t* x, float* y) {
+  if (!s || n_snap < 0 || n_waves < 0 || !fields || !x || !y) return MCPM_ERR_ARG;
+  if (!s->lr2d) return fail(s, MCPM_ERR_STATE, "vlasov_snapshots: needs a 2-D long-range session");
+  const size_t per = 1 + 4 * (size_t)n_waves;
+  double* fd = nullptr;
+  int rc = cuda_check(s, cudaMalloc((void**)&fd, (size_t)n_snap * per * 8 + 8), "vlasov_snapshots");
+  if (rc) return rc;
+  cudaMemcpyAsync(fd, fields, (size_t)n_snap * per * 8, cudaMemcpyHostToDevice, s->stream);
+  int n = 0;
+  for (int i = 0; i < n_snap; ++i)
+    n += sur_snapshot(*s, fd + i * per, n_waves, seed, (uint32_t)i, lr2d_quadrants(*s), lr2d_node_density_mut(*s),
+                      s->cell + (size_t)MCPM_CF_N * s->C, x + (size_t)i * s->C * MCPM_SUR_IN,
+                      y + (size_t)i * s->C * MCPM_SUR_OUT);
+  rc = after_launch(s, n, "vlasov_snapshots");
+  cudaStreamSynchronize(s->stream);
+  cudaFree(fd);
+  s->nodes_valid = true;  // the nodal data now describe the last snapshot
+  s->sorted = false;
+  return rc ? rc : cuda_check(s, cudaGetLastError(), "vlasov_snapshots");
 }
 
 int mcpm_inject_normals(mcpm_session* s, int64_t n, const double* a, const double* b, const double* c) {

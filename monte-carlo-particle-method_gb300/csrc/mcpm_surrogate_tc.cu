@@ -1,0 +1,343 @@
+// mcpm_surrogate_tc.cu -- the 64 -> 64 channel 3x3 convolutions of the
+// learned Vlasov force on the fifth-generation tensor cores (tcgen05).
+//
+// Implicit GEMM per output tile of 128 consecutive cells of one grid row
+// (M = 128) and all 64 output channels (N = 64), reduced over 9 taps x 64
+// input channels (K = 576):
+//   * the activations are an NHWC bf16 tensor [B][N1][N0][64]; the tile of
+//     tap (dy, dx) is one TMA box {64 ch, 128 cells, 1, 1} at (0, x0 + dx,
+//     y + dy, b) -- boxes reaching past the grid are zero-filled by the TMA
+//     unit, which is the convolution's zero padding;
+//   * the 9 weight tiles [64 co][64 ci] stay in shared memory for the life
+//     of the persistent block (72 KB);
+//   * both operands land with the 128-byte swizzle that the K-major UMMA
+//     shared-memory descriptor reads; each tap issues 4 tcgen05.mma of
+//     K = 16 into an fp32 accumulator of 64 TMEM columns;
+//   * two accumulators alternate so that the epilogue of one tile (TMEM ->
+//     registers, + bias, ReLU, bf16, global store) overlaps the MMAs of the
+//     next.
+// Warp roles (6 warps): warp 0 issues the TMA loads, warp 1 allocates TMEM
+// and issues the MMAs, warps 2-5 drain the accumulators (warp w reads TMEM
+// lanes 32 (w % 4) .. 32 (w % 4) + 31).  Every mbarrier wait is bounded
+// (1 s by the global timer): a wait that runs out raises
+// MCPM_ERR_ITER_LIMIT in the status word, every role stops, the block waits
+// (bounded) for its own copies and MMAs in flight, frees its TMEM and exits.
+#include <cuda.h>
+#include <cuda_bf16.h>
+
+#include <cstdint>
+#include <cstring>
+
+#include "../../include/mcpm.h"
+#include "mcpm_surrogate.h"
+
+namespace mcpm {
+namespace tc {
+
+constexpr int TM = 128, TN = 64, NSTAGE = 4, NTHREADS = 192;
+constexpr int A_BYTES = TM * 128;              // one tap of the activation tile
+constexpr int B_BYTES = TN * 128;              // one tap of the weights
+constexpr int SMEM_B = 0;                      // 9 weight taps
+constexpr int SMEM_A = SMEM_B + 9 * B_BYTES;   // NSTAGE activation stages
+constexpr int SMEM_BAR = SMEM_A + NSTAGE * A_BYTES;
+constexpr int SMEM_BYTES = SMEM_BAR + 256 + 1024;  // barriers + alignment slack
+constexpr uint32_t TMEM_COLS = 128;            // two accumulators of 64 columns
+constexpr uint64_t WAIT_NS = 1000000000ull;    // bound of every wait
+
+struct Bars {
+  uint64_t full[NSTAGE], empty[NSTAGE], acc_full[2], acc_empty[2], wbar, done;
+  uint32_t tmem_base;
+  int abort;
+};
+
+__device__ __forceinline__ uint32_t su32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ uint64_t gtimer() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+__device__ __forceinline__ void bar_init(uint64_t* b, uint32_t n) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(su32(b)), "r"(n) : "memory");
+}
+__device__ __forceinline__ void bar_expect_tx(uint64_t* b, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(su32(b)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void bar_arrive(uint64_t* b) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(su32(b)) : "memory");
+}
+__device__ __forceinline__ bool bar_try(uint64_t* b, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(su32(b)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// waits for the phase of the given parity to complete; false if the block
+// is aborting or the wait ran out (which starts the abort)
+__device__ __forceinline__ bool bar_wait(uint64_t* b, uint32_t parity, volatile int* abort, uint32_t* status,
+                                         bool heed_abort = true) {
+  if (bar_try(b, parity)) return true;
+  const uint64_t t0 = gtimer();
+  while (true) {
+    if (bar_try(b, parity)) return true;
+    if (heed_abort && *abort) return false;
+    if (gtimer() - t0 > WAIT_NS) {
+      *abort = 1;
+      atomicOr(status, (uint32_t)MCPM_ERR_ITER_LIMIT);
+      return false;
+    }
+  }
+}
+__device__ __forceinline__ void tma_load_4d(void* dst, const CUtensorMap* map, int c0, int c1, int c2, int c3,
+                                            uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
+      "[%6];" ::"r"(su32(dst)),
+      "l"((uint64_t)map), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(su32(bar))
+      : "memory");
+}
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int c0, int c1, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+          su32(dst)),
+      "l"((uint64_t)map), "r"(c0), "r"(c1), "r"(su32(bar))
+      : "memory");
+}
+// K-major operand with 128-byte rows, 128-byte swizzle, 8-row groups 1024
+// bytes apart (stride byte offset), descriptor version 1, layout code 2
+__device__ __forceinline__ uint64_t sdesc(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr & 0x3FFFF) >> 4);
+  d |= (uint64_t)1 << 16;             // leading byte offset (unused for swizzled K-major)
+  d |= (uint64_t)(1024 >> 4) << 32;   // stride byte offset
+  d |= (uint64_t)1 << 46;             // version
+  d |= (uint64_t)2 << 61;             // SWIZZLE_128B
+  return d;
+}
+// kind::f16 instruction descriptor: fp32 accumulator, bf16 A and B, both
+// K-major, N = 64, M = 128
+constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(TN >> 3) << 17) | ((uint32_t)(TM >> 4) << 24);
+
+__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t acc) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
+          d_tmem),
+      "l"(a), "l"(b), "r"(IDESC), "r"(acc)
+      : "memory");
+}
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(su32(bar))
+               : "memory");
+}
+__device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+}
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+struct Args {
+  const float* bias;        // [64]
+  __nv_bfloat16* out;       // [P][64]
+  uint32_t* status;
+  int N0, N1, rows, tiles_per_row, ntiles;  // rows = B N1
+};
+
+__global__ void __launch_bounds__(NTHREADS, 1)
+    k_conv64_tc(const __grid_constant__ CUtensorMap tmx, const __grid_constant__ CUtensorMap tmw, Args a) {
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  Bars* bars = reinterpret_cast<Bars*>(smem + SMEM_BAR);
+  volatile int* abort = &bars->abort;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < NSTAGE; ++s) { bar_init(&bars->full[s], 1); bar_init(&bars->empty[s], 1); }
+    for (int b = 0; b < 2; ++b) { bar_init(&bars->acc_full[b], 1); bar_init(&bars->acc_empty[b], 4); }
+    bar_init(&bars->wbar, 1);
+    bar_init(&bars->done, 1);
+    bars->abort = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(su32(&bars->tmem_base)),
+                 "r"(TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  fence_before();
+  __syncthreads();
+  fence_after();
+  const uint32_t tmem = bars->tmem_base;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      // producer: the weights once, then one activation box per tap
+      asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&tmx) : "memory");
+      bar_expect_tx(&bars->wbar, 9 * B_BYTES);
+      for (int t = 0; t < 9; ++t) tma_load_2d(smem + SMEM_B + t * B_BYTES, &tmw, t * 64, 0, &bars->wbar);
+      int last_par[NSTAGE];
+      for (int s = 0; s < NSTAGE; ++s) last_par[s] = -1;
+      uint32_t i = 0;
+      bool ok = true;
+      for (int tile = blockIdx.x; tile < a.ntiles && ok; tile += gridDim.x) {
+        const int row = tile / a.tiles_per_row, x0 = (tile - row * a.tiles_per_row) * TM;
+        const int b = row / a.N1, y = row - b * a.N1;
+        for (int tap = 0; tap < 9; ++tap, ++i) {
+          const int s = i % NSTAGE;
+          const uint32_t ph = (i / NSTAGE) & 1;
+          if (!(ok = bar_wait(&bars->empty[s], ph ^ 1, abort, a.status))) break;
+          bar_expect_tx(&bars->full[s], A_BYTES);
+          tma_load_4d(smem + SMEM_A + s * A_BYTES, &tmx, 0, x0 + tap % 3 - 1, y + tap / 3 - 1, b, &bars->full[s]);
+          last_par[s] = (int)ph;
+        }
+      }
+      // our own copies in flight land before the block exits
+      bar_wait(&bars->wbar, 0, abort, a.status, false);
+      for (int s = 0; s < NSTAGE; ++s)
+        if (last_par[s] >= 0) bar_wait(&bars->full[s], (uint32_t)last_par[s], abort, a.status, false);
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      // MMA issuer
+      bool ok = bar_wait(&bars->wbar, 0, abort, a.status);
+      fence_after();
+      uint32_t i = 0, j = 0;
+      const uint32_t sa = su32(smem + SMEM_A), sb = su32(smem + SMEM_B);
+      for (int tile = blockIdx.x; tile < a.ntiles && ok; tile += gridDim.x, ++j) {
+        const uint32_t buf = j & 1, aph = (j >> 1) & 1;
+        if (!(ok = bar_wait(&bars->acc_empty[buf], aph ^ 1, abort, a.status))) break;
+        fence_after();
+        const uint32_t d = tmem + buf * TN;
+        for (int tap = 0; tap < 9; ++tap, ++i) {
+          const int s = i % NSTAGE;
+          if (!(ok = bar_wait(&bars->full[s], (i / NSTAGE) & 1, abort, a.status))) break;
+          fence_after();
+#pragma unroll
+          for (int kk = 0; kk < 4; ++kk)
+            mma_bf16(d, sdesc(sa + s * A_BYTES + kk * 32), sdesc(sb + tap * B_BYTES + kk * 32),
+                     (tap | kk) != 0 ? 1u : 0u);
+          mma_commit(&bars->empty[s]);  // the stage is free once these MMAs have read it
+        }
+        if (!ok) break;
+        mma_commit(&bars->acc_full[buf]);
+      }
+      // every MMA issued here has completed before the block exits
+      mma_commit(&bars->done);
+      bar_wait(&bars->done, 0, abort, a.status, false);
+    }
+  } else {
+    // epilogue: warp w drains TMEM lanes 32 (w % 4) .. + 31 = tile rows
+    const int q = warp & 3;
+    uint32_t j = 0;
+    for (int tile = blockIdx.x; tile < a.ntiles; tile += gridDim.x, ++j) {
+      const uint32_t buf = j & 1, aph = (j >> 1) & 1;
+      if (!bar_wait(&bars->acc_full[buf], aph, abort, a.status)) break;
+      __syncwarp();
+      fence_after();
+      uint32_t r[4][16];
+      const uint32_t taddr = tmem + ((uint32_t)(32 * q) << 16) + buf * TN;
+#pragma unroll
+      for (int c = 0; c < 4; ++c) tmem_ld16(taddr + c * 16, r[c]);
+      tmem_wait_ld();
+      fence_before();
+      __syncwarp();
+      if (lane == 0) bar_arrive(&bars->acc_empty[buf]);
+      const int row = tile / a.tiles_per_row, x0 = (tile - row * a.tiles_per_row) * TM;
+      const int x = x0 + 32 * q + lane;
+      if (x < a.N0) {
+        const size_t p = (size_t)row * a.N0 + x;
+        uint4* o = reinterpret_cast<uint4*>(a.out + p * 64);
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+          __nv_bfloat162 h[8];
+#pragma unroll
+          for (int e = 0; e < 8; ++e) {
+            const float v0 = fmaxf(__uint_as_float(r[c][2 * e]) + a.bias[c * 16 + 2 * e], 0.f);
+            const float v1 = fmaxf(__uint_as_float(r[c][2 * e + 1]) + a.bias[c * 16 + 2 * e + 1], 0.f);
+            h[e] = __floats2bfloat162_rn(v0, v1);
+          }
+          o[2 * c] = *reinterpret_cast<uint4*>(&h[0]);
+          o[2 * c + 1] = *reinterpret_cast<uint4*>(&h[4]);
+        }
+      }
+    }
+  }
+  fence_before();
+  __syncthreads();
+  fence_after();
+  if (warp == 1)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
+}
+
+typedef CUresult (*EncodeTiled)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+static EncodeTiled g_encode = nullptr;
+
+}  // namespace tc
+
+int tc_setup() {
+  using namespace tc;
+  if (!g_encode) {
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess || !fn) {
+      cudaGetLastError();
+      return 1;
+    }
+    g_encode = (EncodeTiled)fn;
+  }
+  if (cudaFuncSetAttribute(k_conv64_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES) != cudaSuccess) {
+    cudaGetLastError();
+    return 1;
+  }
+  return 0;
+}
+
+int tc_conv64_relu(const __nv_bfloat16* x, const __nv_bfloat16* w, const float* bias, __nv_bfloat16* out, int N0,
+                   int N1, int P, int num_sms, uint32_t* status, cudaStream_t st) {
+  using namespace tc;
+  if (!g_encode || P <= 0) return 0;
+  const int rows = P / N0, B = rows / N1;
+  CUtensorMap mx, mw;
+  {
+    cuuint64_t dims[4] = {64, (cuuint64_t)N0, (cuuint64_t)N1, (cuuint64_t)B};
+    cuuint64_t strides[3] = {128, (cuuint64_t)N0 * 128, (cuuint64_t)N0 * N1 * 128};
+    cuuint32_t box[4] = {64, TM, 1, 1}, es[4] = {1, 1, 1, 1};
+    if (g_encode(&mx, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, (void*)x, dims, strides, box, es,
+                 CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                 CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+      return -1;
+  }
+  {
+    cuuint64_t dims[2] = {576, 64};
+    cuuint64_t strides[1] = {576 * 2};
+    cuuint32_t box[2] = {64, 64}, es[2] = {1, 1};
+    if (g_encode(&mw, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (void*)w, dims, strides, box, es,
+                 CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                 CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+      return -1;
+  }
+  Args a;
+  a.bias = bias;
+  a.out = out;
+  a.status = status;
+  a.N0 = N0;
+  a.N1 = N1;
+  a.rows = rows;
+  a.tiles_per_row = (N0 + TM - 1) / TM;
+  a.ntiles = rows * a.tiles_per_row;
+  const int grid = a.ntiles < num_sms ? a.ntiles : num_sms;
+  k_conv64_tc<<<grid, NTHREADS, SMEM_BYTES, st>>>(mx, mw, a);
+  return 1;
+}
+
+}  // namespace mcpm

@@ -33,7 +33,7 @@ RNG_PHILOX, RNG_INJECTED = 0, 1
 CF = dict(NUM_INSIDE=0, U_SPACE=1, PIJ=4, M3=10, M4=20, M5=26, Q=29, DM2=32, DM4=33, MP=34, T=37, N=38,
           GAMMA_ST=39, LAMBDA=40, C=41, GAMMA=47, ALPHA=50, BETA=59, PHI=62, F2=65, OMEGA_MAX=66, DIVU=67)
 CF_COUNT = 68
-K_NAMES = ["bin", "scan", "scatter", "moments", "solve", "esmc", "long_range", "update"]
+K_NAMES = ["bin", "scan", "scatter", "moments", "solve", "esmc", "long_range", "update", "surrogate"]
 K_COUNT = len(K_NAMES)
 # (field, width) of every exported per-cell quantity
 CF_WIDTH = dict(NUM_INSIDE=1, U_SPACE=3, PIJ=6, M3=10, M4=6, M5=3, Q=3, DM2=1, DM4=1, MP=3, T=1, N=1,
@@ -85,6 +85,15 @@ def derive(cfg: Config, n_particles: int) -> Config:
     if cfg.max_particles < n_particles:
         cfg.max_particles = n_particles
     return cfg
+
+
+class SurrogateStats(C.Structure):
+    """mcpm_surrogate_stats: what the judge of the learned force saw."""
+    _fields_ = [("last_error", C.c_double), ("judged", C.c_int64), ("takeovers", C.c_int64),
+                ("surrogate_steps", C.c_int64), ("plain_steps", C.c_int64), ("active", C.c_int32)]
+
+
+SUR_IN, SUR_OUT, SUR_NPARAM = 16, 4, 92368
 
 
 class MCPMError(RuntimeError):
@@ -144,6 +153,22 @@ def load_library(path: str | None = None):
         "mcpm_set_wcap": (C.c_int, [vp, i32]),
         "mcpm_get_wcap": (i32, [vp]),
         "mcpm_autotune": (C.c_int, [vp, i32, C.POINTER(i32)]),
+        "mcpm_surrogate_create": (C.c_int, [i32, i32, i32, C.POINTER(vp)]),
+        "mcpm_surrogate_destroy": (C.c_int, [vp]),
+        "mcpm_surrogate_last_error": (C.c_char_p, [vp]),
+        "mcpm_surrogate_set_params": (C.c_int, [vp, C.POINTER(C.c_float), i64, C.c_double]),
+        "mcpm_surrogate_get_params": (C.c_int, [vp, C.POINTER(C.c_float), i64]),
+        "mcpm_surrogate_set_tensor_path": (C.c_int, [vp, i32]),
+        "mcpm_surrogate_launches": (C.c_int, [vp, C.POINTER(C.c_int64), C.POINTER(i32)]),
+        "mcpm_surrogate_forward": (C.c_int, [vp, vp, i32, vp]),
+        "mcpm_surrogate_gradients": (C.c_int, [vp, vp, vp, i32, C.c_double, C.POINTER(C.c_float), dp]),
+        "mcpm_surrogate_train_step": (C.c_int, [vp, vp, vp, i32, C.c_double, C.c_double, i32, dp]),
+        "mcpm_surrogate_sync": (C.c_int, [vp]),
+        "mcpm_vlasov_snapshots": (C.c_int, [vp, i32, dp, i32, C.c_uint64, vp, vp]),
+        "mcpm_attach_surrogate": (C.c_int, [vp, vp, i32, C.c_double]),
+        "mcpm_get_surrogate_stats": (C.c_int, [vp, C.POINTER(SurrogateStats)]),
+        "mcpm_eval_vlasov_2d": (C.c_int, [vp, i32]),
+        "mcpm_get_kick_2d": (C.c_int, [vp, C.POINTER(C.c_float)]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -369,6 +394,111 @@ class Session:
     @property
     def kernel_launches(self):
         return int(self.lib.mcpm_kernel_launches(self.h))
+
+    # -- learned 2-D Vlasov force (no counterpart in the reference)
+    def vlasov_snapshots(self, fields, n_waves, seed, x_ptr, y_ptr):
+        """Training snapshots of the plain force into device buffers x
+        ([n][C][16] bf16) and y ([n][C][4] fp32); fields [n][1 + 4 n_waves]."""
+        f = np.ascontiguousarray(fields, dtype=np.float64)
+        n = f.shape[0]
+        if f.shape[1] != 1 + 4 * n_waves:
+            raise ValueError("fields must be [n][1 + 4 n_waves]")
+        self._ck(self.lib.mcpm_vlasov_snapshots(self.h, n, _dp(f), int(n_waves), C.c_uint64(seed), C.c_void_p(x_ptr),
+                                                C.c_void_p(y_ptr)), "vlasov_snapshots")
+
+    def attach_surrogate(self, sur, judge_every=10, threshold=0.01):
+        self._ck(self.lib.mcpm_attach_surrogate(self.h, sur.h if sur is not None else None, int(judge_every),
+                                                float(threshold)), "attach_surrogate")
+        self._sur = sur
+
+    def surrogate_stats(self):
+        st = SurrogateStats()
+        self._ck(self.lib.mcpm_get_surrogate_stats(self.h, C.byref(st)), "surrogate_stats")
+        return {k: getattr(st, k) for k, _ in SurrogateStats._fields_}
+
+    def eval_vlasov_2d(self, method):
+        """Re-evaluate the kick of the current cell state: 0 plain path, 1 network."""
+        self._ck(self.lib.mcpm_eval_vlasov_2d(self.h, int(method)), "eval_vlasov_2d")
+
+    def get_kick_2d(self):
+        out = np.empty((self.C, 4), dtype=np.float32)
+        self._ck(self.lib.mcpm_get_kick_2d(self.h, out.ctypes.data_as(C.POINTER(C.c_float))), "get_kick_2d")
+        return out
+
+
+class Surrogate:
+    """mcpm_surrogate: the learned 2-D Vlasov force network (include/mcpm.h).
+    Device buffers are passed as raw pointers (e.g. torch tensors' data_ptr())."""
+
+    def __init__(self, n0, n1, max_batch=1):
+        self.lib = load_library()
+        h = C.c_void_p()
+        rc = self.lib.mcpm_surrogate_create(int(n0), int(n1), int(max_batch), C.byref(h))
+        if rc != OK:
+            raise MCPMError(rc, "surrogate_create failed")
+        self.h = h
+        self.n0, self.n1, self.max_batch = int(n0), int(n1), int(max_batch)
+        self.C = self.n0 * self.n1
+
+    def _ck(self, rc, what):
+        if rc != OK:
+            msg = self.lib.mcpm_surrogate_last_error(self.h)
+            raise MCPMError(rc, "%s: %s" % (what, msg.decode() if msg else ""))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.mcpm_surrogate_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_params(self, params, out_scale):
+        p = np.ascontiguousarray(params, dtype=np.float32)
+        if p.shape != (SUR_NPARAM,):
+            raise ValueError("expected %d parameters" % SUR_NPARAM)
+        self._ck(self.lib.mcpm_surrogate_set_params(self.h, p.ctypes.data_as(C.POINTER(C.c_float)), SUR_NPARAM,
+                                                    float(out_scale)), "surrogate_set_params")
+
+    def get_params(self):
+        p = np.empty(SUR_NPARAM, dtype=np.float32)
+        self._ck(self.lib.mcpm_surrogate_get_params(self.h, p.ctypes.data_as(C.POINTER(C.c_float)), SUR_NPARAM),
+                 "surrogate_get_params")
+        return p
+
+    def set_tensor_path(self, tcgen05):
+        self._ck(self.lib.mcpm_surrogate_set_tensor_path(self.h, 1 if tcgen05 else 0), "surrogate_set_tensor_path")
+
+    def tensor_path(self):
+        """(tcgen05 launches so far, tcgen05 path on)"""
+        n, on = C.c_int64(), C.c_int32()
+        self._ck(self.lib.mcpm_surrogate_launches(self.h, C.byref(n), C.byref(on)), "surrogate_launches")
+        return int(n.value), bool(on.value)
+
+    def forward(self, x_ptr, batch, y_ptr):
+        self._ck(self.lib.mcpm_surrogate_forward(self.h, C.c_void_p(x_ptr), int(batch), C.c_void_p(y_ptr)),
+                 "surrogate_forward")
+
+    def gradients(self, x_ptr, t_ptr, batch, target_scale):
+        g = np.empty(SUR_NPARAM, dtype=np.float32)
+        loss = np.zeros(2)
+        self._ck(self.lib.mcpm_surrogate_gradients(self.h, C.c_void_p(x_ptr), C.c_void_p(t_ptr), int(batch),
+                                                   float(target_scale), g.ctypes.data_as(C.POINTER(C.c_float)),
+                                                   _dp(loss)), "surrogate_gradients")
+        return g, loss
+
+    def train_step(self, x_ptr, t_ptr, batch, target_scale, lr, t, want_loss=False):
+        loss = np.zeros(2) if want_loss else None
+        self._ck(self.lib.mcpm_surrogate_train_step(self.h, C.c_void_p(x_ptr), C.c_void_p(t_ptr), int(batch),
+                                                    float(target_scale), float(lr), int(t),
+                                                    _dp(loss) if want_loss else None), "surrogate_train_step")
+        return loss
+
+    def sync(self):
+        self._ck(self.lib.mcpm_surrogate_sync(self.h), "surrogate_sync")
 
 
 def cell_field(cells, name, cell_major=False):

@@ -200,7 +200,7 @@ def density_field(rng, n_cells, length, K=6, nbar=None):
 
 
 def vlasov_box_2d(n_cells=(256, 256), total=16_000_000, precision=FP32, seed=BASE_SEED + 4, T=0.8,
-                  long_range=LR_SCREENED_POISSON, eps=1.0, model=MODEL_FP_DENSE, dx=1.0):
+                  long_range=LR_SCREENED_POISSON, eps=1.0, model=MODEL_FP_DENSE, dx=1.0, particles=True):
     """2-D Enskog-Vlasov box: square cells of side dx, particles per cell in
     proportion to a density_field (at least one per cell, `total` in all),
     Maxwellian kT = T, specular walls, Sutherland attraction
@@ -220,6 +220,9 @@ def vlasov_box_2d(n_cells=(256, 256), total=16_000_000, precision=FP32, seed=BAS
     c.eqdist = 1.0
     c.bst = BST_RED
     c.ast = AST_RED_4EPS * (eps / 4.0)
+    if not particles:  # the configuration alone
+        derive(c, N)
+        return c, None
     x1, x2 = _fill_cells(rng, counts, n_cells, L)
     s = math.sqrt(T)
     U1, U2, U3 = rng.normal(0, s, N), rng.normal(0, s, N), rng.normal(0, s, N)
