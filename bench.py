@@ -1,13 +1,20 @@
 #!/usr/bin/env python3
 """Particle-step throughput on GB300 (one JSON line on stdout, rank 0).
 
-Workload (default): batched uneven cells -- 65,536 cells (256 x 256) with
-log-normal occupancy (median 100, clipped 10..5000, 16.0M particles),
-Enskog-Fokker-Planck (FP_dense), FP32 particle state with compensated FP32
-moment sums and FP64 per-cell drift solves, free flight with specular walls.
-A step is one iteration of the reference's main loop (src/main.cpp:389-669):
-cell_update, random_generator, velocity_update, DFP_extra_streaming,
-apply_BC, store_old_positions, stream_particles, apply_BC.
+Workload (default, surrogate16m): the 2-D Enskog-Vlasov box -- 256 x 256
+unit cells, 16.0M particles with a sinusoidally perturbed density (n b
+between 0.05 and 0.45), Enskog-Fokker-Planck (FP_dense), FP32 particle state
+with compensated FP32 moment sums and FP64 per-cell drift solves, specular
+walls, and the Vlasov mean-field force from the learned convolutional
+operator, judged every 10 steps by the plain screened-Poisson FEM path
+(which takes over while the kick error exceeds 1%).  A step is one
+iteration of the reference's main loop (src/main.cpp:389-669): cell_update,
+random_generator, velocity_update, DFP_extra_streaming, apply_BC,
+store_old_positions, stream_particles, apply_BC.  The line also carries the
+plain path on the same workload (FP32 and FP64 particle-steps/s) and the
+errors of the surrogate run against the FP64 plain run in n, T and the
+force field.  Other workloads (--workload): uneven16m (65,536 cells with
+log-normal occupancy), esmc6m, slab1m, vlasov16m (the plain 2-D force).
 
   value  particle-steps/s with the state resident in HBM (CUDA events on the
          launch stream, max over ranks).  The particle state (16M x 20 B +
@@ -143,6 +150,13 @@ def build_workload(args):
         cfg, parts = W.esmc_box_2d(precision=mcpm.FP32)
         desc = {"workload": "ESMC 256x256 100/cell nb=0.2 diffuse walls fp32", "cells": 65536,
                 "particles": int(len(parts["x2"]))}
+    elif args.workload == "surrogate16m":
+        cfg, parts = W.vlasov_box_2d(n_cells=(256, 256), total=16_000_000, precision=mcpm.FP32,
+                                     long_range=mcpm.LR_SCREENED_POISSON, model=mcpm.MODEL_FP_DENSE)
+        desc = {"workload": "2-D Enskog-Vlasov box 256x256 sinusoidal density (nb 0.05..0.45) FP_dense fp32, "
+                            "Vlasov force from the learned conv operator (bf16, tcgen05), plain screened-Poisson "
+                            "FEM judge every 10 steps, takeover above 1% kick error",
+                "cells": 65536, "particles": int(len(parts["x2"]))}
     elif args.workload == "vlasov16m":
         cfg, parts = W.vlasov_box_2d(n_cells=(256, 256), total=16_000_000, precision=mcpm.FP32,
                                      long_range=mcpm.LR_SCREENED_POISSON, model=mcpm.MODEL_FP_DENSE)
@@ -158,14 +172,111 @@ def build_workload(args):
     return cfg, parts, desc
 
 
-def cpu_baseline_sample(seconds=12.0):
+def _bf16_peak():
+    p = os.path.join(REPO, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        if "bf16_tflops" in d:
+            return float(d["bf16_tflops"]), "measured"
+    return 1900.0, "fallback"
+
+
+# algorithmic FLOPs of one inference of the learned force per cell: the used
+# input channels (11) and outputs (4): 2 (9 11 64 + 2 9 64 64 + 9 64 4)
+SURROGATE_FLOP_PER_CELL = 2 * (9 * 11 * 64 + 2 * 9 * 64 * 64 + 9 * 64 * 4)
+
+
+def _rel(a, b):
+    import numpy as np
+    a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def surrogate_comparison(args, cfg, parts, s, stream):
+    """The plain path on the same workload (FP32 and FP64 particle-steps/s),
+    and the errors of the surrogate run against the FP64 plain run after the
+    same number of steps from the same state: cell density n and temperature
+    T (relative L2 over cells), and the kick field of the last state (network
+    against plain path, relative L2 over the four kick coefficients of every
+    cell)."""
+    import torch
+
+    import mcpm
+    import surrogate as SG
+    N = len(parts["x2"])
+    stats = s.surrogate_stats()
+
+    def timed(sess, k):
+        sess.step(3)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        sess.step(k)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return N * k / (e0.elapsed_time(e1) / 1e3)
+
+    k = max(10, min(30, args.steps))
+    s.attach_surrogate(None)
+    plain32 = timed(s, k)
+    cfg64 = cfg.copy()
+    cfg64.precision = mcpm.FP64
+    s64 = mcpm.Session(cfg64)
+    s64.set_stream(stream.cuda_stream)
+    s64.upload(parts["x1"], parts["x2"], parts["U1"], parts["U2"], parts["U3"])
+    s64.set_wcap(min(s.wcap, 384))
+    plain64 = timed(s64, max(5, k // 3))
+    # accuracy: the same start, the same number of steps
+    n_acc = 20
+    s64.upload(parts["x1"], parts["x2"], parts["U1"], parts["U2"], parts["U3"])
+    s.upload(parts["x1"], parts["x2"], parts["U1"], parts["U2"], parts["U3"])
+    sur = SG.attach(s, judge_every=10, threshold=0.01)
+    s64.step(n_acc)
+    s.step(n_acc)
+    s64.cell_update()
+    s.cell_update()
+    c64, c32 = s64.get_cells(), s.get_cells()
+    err_n = _rel(c32[mcpm.CF["N"]], c64[mcpm.CF["N"]])
+    err_T = _rel(c32[mcpm.CF["T"]], c64[mcpm.CF["T"]])
+    s.eval_vlasov_2d(0)
+    kp = s.get_kick_2d()
+    s.eval_vlasov_2d(1)
+    kn = s.get_kick_2d()
+    err_F = _rel(kn, kp)
+    st2 = s.surrogate_stats()
+    s64.close()
+    sur_info = SG.load()[2]
+    return {
+        "plain": {"fp32_value": plain32, "fp64_value": plain64, "unit": UNIT,
+                  "steps_timed": [k, max(5, k // 3)],
+                  "note": "the same workload with the plain screened-Poisson FEM force every step"},
+        "accuracy": {"steps": n_acc, "against": "FP64 plain GPU step (parity-tested against the FP64 oracle)",
+                     "n_rel_l2": err_n, "T_rel_l2": err_T, "force_rel_l2": err_F,
+                     "judge_last_error": st2["last_error"]},
+        "surrogate": {"judge_every": 10, "threshold": 0.01, "timed_run": stats,
+                      "trained_on": {kk: sur_info.get(kk) for kk in ("n_snap", "epochs", "batch", "steps",
+                                                                    "val_kick_error", "train_s", "gen_s")}},
+    }
+
+
+def cpu_baseline_sample(args, seconds=12.0):
     """The oracle (FP64 CPU restatement of the reference step, 1 core) on a
-    32 x 32-cell sample of the same workload; returns particle-steps/s."""
+    small sub-box of the same workload; returns particle-steps/s."""
     sys.path.insert(0, os.path.join(REPO, "oracle"))
     import mcpm
     import workloads as W
     from oracle import Oracle
-    cfg, parts = W.uneven_cells_2d(n_cells=(32, 32), precision=mcpm.FP64, streaming=True)
+    if args.workload in ("surrogate16m", "vlasov16m"):
+        # 24 x 24 cells at the benchmark's particles per cell; the 2-D force
+        # by the oracle's dense-LU FEM (the reference's PARDISO is absent)
+        cfg, parts = W.vlasov_box_2d(n_cells=(24, 24), total=int(round(16_000_000 * 576 / 65536)),
+                                     precision=mcpm.FP64, long_range=mcpm.LR_SCREENED_POISSON,
+                                     model=mcpm.MODEL_FP_DENSE)
+        what = "24x24-cell box of the same workload, plain screened-Poisson FEM force (dense LU)"
+    else:
+        cfg, parts = W.uneven_cells_2d(n_cells=(32, 32), precision=mcpm.FP64, streaming=True)
+        what = "32x32-cell sub-box of the same workload"
     o = Oracle(cfg, parts)
     o.set_step(1)
     o.step(1)  # warm-up
@@ -176,7 +287,7 @@ def cpu_baseline_sample(seconds=12.0):
         el = time.perf_counter() - t0
         if el > seconds or steps >= 50:
             break
-    return o.N * steps / el, o.N, steps
+    return o.N * steps / el, o.N, steps, what
 
 
 def run_mcpm(args):
@@ -201,6 +312,10 @@ def run_mcpm(args):
         s.cell_update()
         s.init_omega_max()
     wcap = s.autotune(3)  # threads-per-cell split; the state is restored
+    sur = None
+    if args.workload == "surrogate16m":
+        import surrogate as SG
+        sur = SG.attach(s, judge_every=10, threshold=0.01)
     clocks = ClockSampler(local)
     s.step(args.warmup)
     torch.cuda.synchronize()
@@ -245,6 +360,16 @@ def run_mcpm(args):
                 "unit": "GB/s", "frac": round(achieved / hbm, 4), "peak_kind": peak_kind,
                 "traffic": traffic, "bytes_per_launch": bytes_per_launch, "avg_launch_ms": round(dom_ms, 4),
                 "share": {k: round(v[0] / tot, 4) for k, v in prof.items() if v[0] > 0}}
+    if sur is not None:
+        # the learned force: algorithmic FLOPs of one inference (used channels)
+        # over its mean device time per step, against the measured bf16 peak
+        sur_ms = prof["surrogate"][0] / max(1, prof["surrogate"][1])
+        fl = SURROGATE_FLOP_PER_CELL * cfg.n_cells[0] * cfg.n_cells[1]
+        tf, tf_kind = _bf16_peak()
+        roofline["surrogate"] = {"bound": "tensor", "kernels": "k_input + 4 conv (2 x k_conv64_tc)",
+                                 "achieved": round(fl / (sur_ms / 1e3) / 1e12, 2), "peak": tf, "unit": "TFLOP/s",
+                                 "frac": round(fl / (sur_ms / 1e3) / 1e12 / tf, 4), "peak_kind": tf_kind,
+                                 "flop_per_inference": fl, "avg_ms": round(sur_ms, 4)}
 
     # end to end through the C-ABI with pinned host buffers
     pin = lambda: torch.empty(N, dtype=torch.float64, pin_memory=True).numpy()  # noqa: E731
@@ -255,8 +380,10 @@ def run_mcpm(args):
     e2e_steps = max(2, min(5, args.steps))
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    for _ in range(e2e_steps):
+    step0 = s.step_count
+    for i in range(e2e_steps):
         s.upload(hin["x1"], hin["x2"], hin["U1"], hin["U2"], hin["U3"])
+        s.set_step(step0 + i)  # the caller's simulation continues (upload restarts the counter)
         s.step(1)
         s.download_into(hout)
     torch.cuda.synchronize()
@@ -264,14 +391,16 @@ def run_mcpm(args):
     e2e = {"value": N * ws / (e2e_ms / 1e3), "unit": UNIT, "h2d_bytes_per_step": 5 * 8 * N,
            "d2h_bytes_per_step": 5 * 8 * N, "ms_per_step": round(e2e_ms, 3)}
     ok = bool(np.all(np.isfinite(hout["U1"])))
+    extra = {}
+    if sur is not None:
+        extra = surrogate_comparison(args, cfg, parts, s, stream)
     s.close()
 
     cpu = None
     if rank == 0 and not args.no_cpu:
-        v, n, st = cpu_baseline_sample()
+        v, n, st, what = cpu_baseline_sample(args)
         cpu = {"value": v, "unit": UNIT, "cores": 1, "kind": "port",
-               "sample": "oracle FP64 restatement, 32x32-cell sub-box of the same workload (%d particles), %d steps"
-                         % (n, st)}
+               "sample": "oracle FP64 restatement, %s (%d particles), %d steps" % (what, n, st)}
     if dist:
         dist.destroy_process_group()
     if rank != 0:
@@ -285,30 +414,67 @@ def run_mcpm(args):
         "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "gpu_launches": launches, "clocks": ck,
         "finite": ok,
     }
+    line.update(extra)
     print(json.dumps(line))
 
 
 # --------------------------------------------------------- reference arm
-def _ref_worker_init(cfg_dict, sub):
+def _ref_worker_init(jobs):
     global _W
     sys.path.insert(0, PKG)
     sys.path.insert(0, os.path.join(REPO, "oracle"))
     import mcpm
     from oracle import Oracle
-    c = mcpm.Config()
-    for k, v in cfg_dict.items():
-        f = getattr(c, k)
-        if hasattr(f, "__len__"):
-            f[:] = v
-        else:
-            setattr(c, k, v)
-    _W = Oracle(c, sub)
-    _W.set_step(1)
+    _W = []
+    for cfg_dict, sub in jobs:
+        c = mcpm.Config()
+        for k, v in cfg_dict.items():
+            f = getattr(c, k)
+            if hasattr(f, "__len__"):
+                f[:] = v
+            else:
+                setattr(c, k, v)
+        o = Oracle(c, sub)
+        o.set_step(1)
+        _W.append(o)
 
 
 def _ref_worker_step(n):
-    _W.step(n)
-    return _W.N * n
+    done = 0
+    for o in _W:
+        o.step(n)
+        done += o.N * n
+    return done
+
+
+def _ref_split(cfg, parts, P):
+    """Sub-boxes of the workload for P worker processes: strips of cell rows,
+    or, for a 2-D box with the node-grid Vlasov force (whose dense-LU FEM
+    grows as the cube of the node count), square tiles of 32 x 32 cells."""
+    import numpy as np
+    N0, N1 = cfg.n_cells[0], cfg.n_cells[1]
+    dx, dy = cfg.length[0] / N0, cfg.length[1] / N1
+    kx = np.floor(parts["x1"] / dx).astype(np.int64)
+    ky = np.floor(parts["x2"] / dy).astype(np.int64)
+    if cfg.long_range and cfg.direction[0] == 1:
+        T = 32
+        boxes = [(x0, min(N0, x0 + T), y0, min(N1, y0 + T)) for y0 in range(0, N1, T) for x0 in range(0, N0, T)]
+        how = "square tiles of %d x %d cells (%d boxes, each with its own walls)" % (T, T, len(boxes))
+    else:
+        boxes = [(0, N0, i * N1 // P, (i + 1) * N1 // P) for i in range(P)]
+        how = "%d strips of cell rows" % P
+    jobs = [[] for _ in range(P)]
+    for b, (x0, x1_, y0, y1) in enumerate(boxes):
+        m = (kx >= x0) & (kx < x1_) & (ky >= y0) & (ky < y1)
+        sub = {kk: np.ascontiguousarray(parts[kk][m]) for kk in ("x1", "x2", "U1", "U2", "U3")}
+        sub["x1"] = sub["x1"] - x0 * dx
+        sub["x2"] = sub["x2"] - y0 * dy
+        c = cfg.copy()
+        c.n_cells[0], c.n_cells[1] = x1_ - x0, y1 - y0
+        c.length[0], c.length[1] = (x1_ - x0) * dx, (y1 - y0) * dy
+        c.max_particles = int(m.sum())
+        jobs[b % P].append((c.as_dict(), sub))
+    return [j for j in jobs if j], how
 
 
 def run_reference(args):
@@ -317,29 +483,16 @@ def run_reference(args):
         return
     import multiprocessing as mp
 
-    import numpy as np
-
     import mcpm
     cores = os.cpu_count() or 1
     P = max(1, min(cores, 64))
     cfg, parts, desc = build_workload(args)
     cfg.precision = mcpm.FP64
     Ntot = len(parts["x2"])
-    N1 = cfg.n_cells[1]
-    dy = cfg.length[1] / N1
-    k = np.floor(parts["x2"] / dy).astype(np.int64)
+    jobs, how = _ref_split(cfg, parts, P)
+    P = len(jobs)
     ctx = mp.get_context("spawn")
-    pools = []
-    for i in range(P):
-        lo, hi = i * N1 // P, (i + 1) * N1 // P
-        m = (k >= lo) & (k < hi)
-        sub = {kk: np.ascontiguousarray(parts[kk][m]) for kk in ("x1", "x2", "U1", "U2", "U3")}
-        sub["x2"] = sub["x2"] - lo * dy
-        c = cfg.copy()
-        c.n_cells[1] = hi - lo
-        c.length[1] = (hi - lo) * dy
-        c.max_particles = int(m.sum())
-        pools.append(ctx.Pool(1, initializer=_ref_worker_init, initargs=(c.as_dict(), sub)))
+    pools = [ctx.Pool(1, initializer=_ref_worker_init, initargs=(j,)) for j in jobs]
     del parts
     try:
         if args.warmup:
@@ -356,10 +509,11 @@ def run_reference(args):
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": el * 1e3 / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
-            "config": dict(desc, precision="fp64 (reference CPU path)"), "impl": "reference",
+            "config": dict(desc, precision="fp64 (reference CPU path: the plain force, no learned part)"),
+            "impl": "reference",
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": P, "kind": "port",
-                             "sample": "the full workload (%d particles) split into %d strips of cell rows, "
-                                       "one oracle process per core, every step" % (Ntot, P)},
+                             "sample": "the full workload (%d particles) split into %s, one oracle process per "
+                                       "core, every step" % (Ntot, how)},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
@@ -370,14 +524,15 @@ def main():
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="mcpm", choices=["mcpm", "reference"])
-    ap.add_argument("--workload", default="uneven16m", choices=["uneven16m", "esmc6m", "slab1m", "vlasov16m"])
+    ap.add_argument("--workload", default="surrogate16m",
+                    choices=["surrogate16m", "uneven16m", "esmc6m", "slab1m", "vlasov16m"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "mcpm":
         args.warmup = 3
     if args.impl == "reference":
-        # one reference step of the 16M workload is ~0.5-1 s on 16 cores
-        args.steps = min(args.steps, 60)
+        # one reference step of a 16M workload is ~0.5-5 s on 16 cores
+        args.steps = min(args.steps, 60 if args.workload not in ("surrogate16m", "vlasov16m") else 4)
         args.warmup = min(args.warmup, 1)
         run_reference(args)
     else:

@@ -75,3 +75,18 @@ def test_unused_channels_have_zero_gradient():
     _, _, _, g = SO.loss_and_grad(p, x, t, 1.0, exact=False)
     d = SO.unpack(g)
     assert np.all(d["W4"][4:] == 0) and np.all(d["b4"][4:] == 0)
+
+
+def test_committed_weights_load_and_run_on_the_oracle():
+    """The trained parameters shipped with the package: layout, training
+    record, unused rows zero, and a finite forward pass on the oracle."""
+    import surrogate as S
+    p, scale, info = S.load()
+    assert p.shape == (SO.NPARAM,) and p.dtype == np.float32 and scale > 0
+    assert info["val_kick_error"] < 0.01 and info["n_snap"] >= 20000 and info["grid"] == [256, 256]
+    d = SO.unpack(p)
+    assert np.all(d["W4"][4:] == 0) and np.all(d["b4"][4:] == 0) and np.all(d["W1"][:, :, 11:] == 0)
+    x = np.zeros((1, 8, 8, 16), np.float32)
+    x[..., 5] = 1.0
+    y, _ = SO.forward(p, x)
+    assert np.all(np.isfinite(y))
