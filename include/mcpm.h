@@ -262,7 +262,8 @@ int mcpm_profile(mcpm_session* s, int32_t enable);
 int mcpm_profile_read(mcpm_session* s, double* ms, int64_t* launches, int32_t n);
 /* ---- work split between warps and blocks -------------------------------- */
 /* Cells with at most wcap particles are processed by one warp each, larger
-   cells by a 256-thread block; wcap <= 768 (FP32) / 384 (FP64). */
+   cells by a 256-thread block; wcap <= 384 (the shared-memory staging of a
+   warp in the particle pass). */
 int mcpm_set_wcap(mcpm_session* s, int32_t wcap);
 int32_t mcpm_get_wcap(const mcpm_session* s);
 /* Times `steps` fused steps per candidate wcap on the session's particles,

@@ -89,7 +89,7 @@ template <typename real> struct KC {
   real idx, idy;  // 1/dx, 1/dy (FP32 binning)
   real eps_x, eps_y;  // diffuse-wall offsets
 };
-template <typename real> __device__ __forceinline__ KC<real> make_kc(const DevConsts& k) {
+template <typename real> __host__ __device__ __forceinline__ KC<real> make_kc(const DevConsts& k) {
   KC<real> c;
   if constexpr (sizeof(real) == 4) {
     c.dx = k.f_dx; c.dy = k.f_dy; c.L0 = k.f_L0; c.L1 = k.f_L1; c.dt = k.f_dt;

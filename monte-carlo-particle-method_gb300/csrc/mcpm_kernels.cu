@@ -916,6 +916,8 @@ template <typename real> struct UpdArgs {
   uint32_t stages;
   int wcap, bcap;
   const double* Vn;  // node potential of the 2-D Vlasov force (FP64 path)
+  KC<real> kc;       // constants in the state's precision (read from the
+                     // parameter bank, so they cost no registers)
 };
 
 template <typename real>
@@ -1257,17 +1259,279 @@ __device__ void update_cell(int c, const UpdArgs<real>& a, int step, real* xs, i
   raise_status(a.status, bad);
 }
 
-template <typename real, uint32_t CST>
-__global__ void __launch_bounds__(256, sizeof(real) == 4 ? 3 : 1) k_update(UpdArgs<real> a) {
+// Launch shape of the FP32 particle pass: blocks of 256 threads resident
+// per SM (the register budget: 5 blocks = 48 registers, measured fastest on
+// GB300 against 3, 4 and 6 -- the pass is latency-bound, so warps in flight
+// beat the few spills), and the unroll factor of its particle loops.
+#ifndef MCPM_UPD_MINB
+#define MCPM_UPD_MINB 5
+#endif
+#ifndef MCPM_UPD_UNROLL
+#define MCPM_UPD_UNROLL 1
+#endif
+#define MCPM_STR2(x) #x
+#define MCPM_STR(x) MCPM_STR2(x)
+#define UPD_UNROLL _Pragma(MCPM_STR(unroll MCPM_UPD_UNROLL))
+
+// Sums of K floats over a tile of TILE threads (one warp or the block):
+// per-lane running sums combined by an XOR butterfly (pairwise), every
+// thread gets the totals.  red holds K * TILE / 32 floats.
+template <int K, int TILE>
+__device__ __forceinline__ void tile_sum_f32(float (&v)[K], float* red) {
+#pragma unroll
+  for (int q = 0; q < K; ++q)
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v[q] += __shfl_xor_sync(FULL, v[q], o);
+  if constexpr (TILE > 32) {
+    constexpr int W = TILE / 32;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) {
+#pragma unroll
+      for (int q = 0; q < K; ++q) red[q * W + warp] = v[q];
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < K; ++q) {
+      float t = 0.f;
+#pragma unroll
+      for (int w = 0; w < W; ++w) t += red[q * W + w];
+      v[q] = t;
+    }
+  }
+}
+
+// The FP32 particle pass: the stages of update_cell for float state, with
+// plain FP32 per-lane sums of the whitening and energy terms combined
+// pairwise (tile_sum_f32; the compensated sums stay in the moment pass),
+// fused multiply-adds throughout, and the packed per-cell record read into
+// registers where each pass needs it.
+template <int TILE, uint32_t CST, int PB>
+__device__ void update_cell_f32(int c, const UpdArgs<float>& a, int step, float* xs, int xcap, float* red,
+                                float* R) {
+  const int t = (TILE == 32) ? (threadIdx.x & 31) : threadIdx.x;
+  const int64_t s0 = a.off[c];
+  const int n = a.cnt[c];
+  const DevConsts& k = a.k;
+  const KC<float>& kc = a.kc;
+  const uint32_t st = CST ? CST : a.stages;
+  const bool rng = st & ST_RNG, fp = st & ST_FP, load_xi = st & ST_LOAD_XI, store_xi = st & ST_STORE_XI;
+  const bool staged = rng && n <= xcap;
+  // the cell's packed record in shared memory (R: PF_STRIDE floats of this
+  // warp or block), read by broadcast where each pass needs a constant
+  if (TILE == 32) __syncwarp();
+  else __syncthreads();
+  if (t < PF_STRIDE / 4)
+    reinterpret_cast<float4*>(R)[t] = __ldg(reinterpret_cast<const float4*>(a.pcell + (size_t)c * PF_STRIDE) + t);
+  if (TILE == 32) __syncwarp();
+  else __syncthreads();
+  const float Us0 = R[PF_US0], Us1 = R[PF_US1], Us2 = R[PF_US2];
+  const PT<float>& P = a.p;  // pointers stay in the parameter bank
+  float mean0 = 0.f, mean1 = 0.f, mean2 = 0.f, irms0 = 1.f, irms1 = 1.f, irms2 = 1.f, f1 = 0.f;
+  // ---- pass A: draws, their per-cell sums, sum |M'|^2
+  if (rng || fp) {
+    float sa[7] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};  // z0 z1 z2 |M'|^2 z0^2 z1^2 z2^2
+    UPD_UNROLL
+    for (int i = t; i < n; i += TILE) {
+      const int64_t p = s0 + i;
+      if (rng) {
+        float z0, z1, z2;
+        raw_normals(a, step, p, z0, z1, z2);
+        if (staged) { xs[3 * i] = z0; xs[3 * i + 1] = z1; xs[3 * i + 2] = z2; }
+        sa[0] += z0; sa[1] += z1; sa[2] += z2;
+        sa[4] = fmaf(z0, z0, sa[4]); sa[5] = fmaf(z1, z1, sa[5]); sa[6] = fmaf(z2, z2, sa[6]);
+      }
+      if (fp) {
+        const float m1 = P.U1[p] - Us0, m2 = P.U2[p] - Us1, m3 = P.U3[p] - Us2;
+        sa[3] = fmaf(m3, m3, fmaf(m2, m2, fmaf(m1, m1, sa[3])));
+      }
+    }
+    tile_sum_f32<7, TILE>(sa, red);
+    f1 = sa[3];
+    if (rng) {
+      const float rn = 1.0f / (float)n;
+      mean0 = sa[0] * rn; mean1 = sa[1] * rn; mean2 = sa[2] * rn;
+      irms0 = 1.0f / sqrtf(fmaxf(fmaf(-mean0, mean0, sa[4] * rn), 0.f));
+      irms1 = 1.0f / sqrtf(fmaxf(fmaf(-mean1, mean1, sa[5] * rn), 0.f));
+      irms2 = 1.0f / sqrtf(fmaxf(fmaf(-mean2, mean2, sa[6] * rn), 0.f));
+    }
+  }
+  // whitened normal of the i-th particle of the cell
+  auto xiw = [&](int i, float& z0, float& z1, float& z2) {
+    const int64_t p = s0 + i;
+    if (load_xi) {
+      z0 = (float)a.xi[p]; z1 = (float)a.xi[a.cap + p]; z2 = (float)a.xi[2 * a.cap + p];
+      return;
+    }
+    if (staged) { z0 = xs[3 * i]; z1 = xs[3 * i + 1]; z2 = xs[3 * i + 2]; }
+    else raw_normals(a, step, p, z0, z1, z2);
+    if (n > 1) { z0 = (z0 - mean0) * irms0; z1 = (z1 - mean1) * irms1; z2 = (z2 - mean2) * irms2; }
+  };
+  uint32_t bad = 0;
+  // ---- pass C (split mode): keep the whitened normals for velocity_update
+  if (rng && store_xi) {
+    for (int i = t; i < n; i += TILE) {
+      float z0, z1, z2;
+      xiw(i, z0, z1, z2);
+      const int64_t p = s0 + i;
+      a.xi[p] = (double)z0; a.xi[a.cap + p] = (double)z1; a.xi[2 * a.cap + p] = (double)z2;
+    }
+  }
+  // the Ornstein-Uhlenbeck update of M' with the cubic drift
+  // (src/Fokker_Planck.cpp:1114-1130), constants from the shared record
+  auto mnew = [&](int i, float& m1, float& m2, float& m3) {
+    const int64_t p = s0 + i;
+    m1 = P.U1[p] - Us0; m2 = P.U2[p] - Us1; m3 = P.U3[p] - Us2;
+    if (n > 1) {
+      float z0, z1, z2;
+      xiw(i, z0, z1, z2);
+      const float energy = fmaf(m3, m3, fmaf(m2, m2, m1 * m1));
+      const float ee = energy - R[PF_EQ], lam = R[PF_LAM];
+      float d0 = fmaf(R[PF_C0 + 2], m3, fmaf(R[PF_C0 + 1], m2, R[PF_C0] * m1));
+      d0 = fmaf(lam, fmaf(m1, energy, -R[PF_Q0]), fmaf(R[PF_G0], ee, d0));
+      float d1 = fmaf(R[PF_C0 + 4], m3, fmaf(R[PF_C0 + 3], m2, R[PF_C0 + 1] * m1));
+      d1 = fmaf(lam, fmaf(m2, energy, -R[PF_Q1]), fmaf(R[PF_G1], ee, d1));
+      float d2 = fmaf(R[PF_C0 + 5], m3, fmaf(R[PF_C0 + 4], m2, R[PF_C0 + 2] * m1));
+      d2 = fmaf(lam, fmaf(m3, energy, -R[PF_Q2]), fmaf(R[PF_G2], ee, d2));
+      const float A1 = R[PF_A1], A2 = R[PF_A2], A3 = R[PF_A3];
+      m1 = fmaf(A3, z0, fmaf(A2, d0, A1 * m1));
+      m2 = fmaf(A3, z1, fmaf(A2, d1, A1 * m2));
+      m3 = fmaf(A3, z2, fmaf(A2, d2, A1 * m3));
+    } else {
+      m1 = 0.f; m2 = 0.f; m3 = 0.f;
+    }
+  };
+  // ---- pass C: M'_new, sum |M'_new|^2; M'_new replaces the staged normals
+  float scale = 1.f;
+  if (fp) {
+    float f2[1] = {0.f};
+    UPD_UNROLL
+    for (int i = t; i < n; i += TILE) {
+      float m1, m2, m3;
+      mnew(i, m1, m2, m3);
+      if (m2 != m2) bad |= MCPM_ERR_NAN;
+      f2[0] = fmaf(m3, m3, fmaf(m2, m2, fmaf(m1, m1, f2[0])));
+      if (staged) { xs[3 * i] = m1; xs[3 * i + 1] = m2; xs[3 * i + 2] = m3; }
+    }
+    tile_sum_f32<1, TILE>(f2, red);
+    if (n > 1) scale = sqrtf(fabsf(f1 / f2[0]));
+  }
+  const uint32_t pos_stages = ST_LR | ST_DFP | ST_BC1 | ST_OLD | ST_STREAM | ST_BC2 | ST_BC3 | ST_KEY;
+  if (!(fp || (st & pos_stages))) {
+    raise_status(a.status, bad);
+    return;
+  }
+  // ---- pass D: final velocities, then the position pipeline
+  const float dtr = kc.dt;
+  const float fj = (float)(c % k.N0), fk = (float)(c / k.N0);
+  const int iters = (n + TILE - 1) / TILE;
+  UPD_UNROLL
+  for (int r = 0; r < iters; ++r) {
+    const int i = r * TILE + t;
+    const bool act = i < n;
+    int key = 0;
+    if (act) {
+      const int64_t p = s0 + i;
+      PState<float> s;
+      s.x1 = P.x1 ? P.x1[p] : 0.f;
+      s.x2 = P.x2[p];
+      s.x1o = P.x1o ? P.x1o[p] : 0.f;
+      s.x2o = P.x2o ? P.x2o[p] : 0.f;
+      const int pid = P.pid[p];
+      if (fp) {
+        if (n > 1) {
+          float m1, m2, m3;
+          if (staged) { m1 = xs[3 * i]; m2 = xs[3 * i + 1]; m3 = xs[3 * i + 2]; }
+          else mnew(i, m1, m2, m3);
+          s.u1 = fmaf(m1, scale, Us0); s.u2 = fmaf(m2, scale, Us1); s.u3 = fmaf(m3, scale, Us2);
+        } else {
+          s.u1 = Us0; s.u2 = Us1; s.u3 = Us2;
+        }
+      } else {
+        s.u1 = P.U1[p]; s.u2 = P.U2[p]; s.u3 = P.U3[p];
+      }
+      if (st & ST_LR) {
+        if (k.lr2d) {
+          // U -= grad(V) coef/m dt with the bilinear coordinates of the particle
+          const float xi = fmaf(s.x1, kc.idx, -fj), eta = fmaf(s.x2, kc.idy, -fk);
+          s.u1 = s.u1 - fmaf(R[PF_LB1], eta, R[PF_LA1]);
+          s.u2 = s.u2 - fmaf(R[PF_LB2], xi, R[PF_LA2]);
+        } else {
+          s.u2 = s.u2 + R[PF_F2DT];
+        }
+      }
+      if (st & ST_DFP) {
+        // DFP_extra_streaming, src/Fokker_Planck.cpp:904-946 (the x1
+        // heat-flux term uses U_space[1], as there)
+        const float w1 = s.u1 - Us0, w2 = s.u2 - Us1, w3 = s.u3 - Us2;
+        const float e = fmaf(w3, w3, fmaf(w2, w2, w1 * w1));
+        const float ee = e - R[PF_EQ], gst = R[PF_GST];
+        if (k.dir0 == 1) {
+          const float v = fmaf(R[PF_BE0], ee, fmaf(R[PF_AL0 + 2], w3, fmaf(R[PF_AL0 + 1], w2, R[PF_AL0] * w1)));
+          const float h = gst * fmaf(s.u1 - Us1, e, -R[PF_HQ0]);
+          s.x1 = fmaf(h, dtr, fmaf(dtr, v, s.x1));
+          s.x1 = fmaf(-dtr, R[PF_PH0], s.x1);
+        }
+        if (k.dir1 == 1) {
+          const float v = fmaf(R[PF_BE1], ee, fmaf(R[PF_AL0 + 5], w3, fmaf(R[PF_AL0 + 4], w2, R[PF_AL0 + 3] * w1)));
+          const float h = gst * fmaf(w2, e, -R[PF_HQ1]);
+          s.x2 = fmaf(h, dtr, fmaf(dtr, v, s.x2));
+          s.x2 = fmaf(-dtr, R[PF_PH1], s.x2);
+        }
+      }
+      // apply_BC: the box's wall type fixed at compile time where the
+      // launch knows it (PB), else the run-time dispatch
+      auto bc = [&](int call) {
+        if constexpr (PB == MCPM_PROBLEM_CLOSED_BOX) bc_specular<float>(s, k, kc, bad);
+        else if constexpr (PB == MCPM_PROBLEM_PERIODIC) bc_periodic<float>(s, k, kc);
+        else apply_bc<float>(s, a.bc_call_base + call, pid, step, k, kc, bad);
+      };
+      if (st & ST_BC1) bc(0);
+      if (st & ST_OLD) { s.x1o = s.x1; s.x2o = s.x2; }
+      if (st & ST_STREAM) {
+        if (k.dir0 == 1) s.x1 = fmaf(dtr, s.u1, s.x1);
+        if (k.dir1 == 1) s.x2 = fmaf(dtr, s.u2, s.x2);
+      }
+      if (st & ST_BC2) bc(1);
+      if (st & ST_BC3) bc(2);
+      P.U1[p] = s.u1; P.U2[p] = s.u2; P.U3[p] = s.u3;
+      if (P.x1) P.x1[p] = s.x1;
+      P.x2[p] = s.x2;
+      if (P.x1o) P.x1o[p] = s.x1o;
+      if (P.x2o) P.x2o[p] = s.x2o;
+      if (st & ST_KEY) {
+        key = bin_one<float>(s.x1, s.x2, pid, step + 1, k, kc, bad);
+        a.key_out[p] = key;
+      }
+    }
+    if (st & ST_KEY) count_key(a.cnt_next, key, act);
+  }
+  raise_status(a.status, bad);
+}
+
+template <typename real, uint32_t CST, int PB = 0>
+__global__ void __launch_bounds__(256, sizeof(real) == 4 ? (CST ? MCPM_UPD_MINB : 3) : 1) k_update(UpdArgs<real> a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ Acc<real> red[8 * 8];
   real* xs = reinterpret_cast<real*>(smem_raw);
   const int warp = threadIdx.x >> 5;
   const int step = *a.dstep;
-  schedule_cells(
-      a.list_big, a.list_small, a.wl, a.work, WK_UPD_BIG, WK_UPD_SMALL,
-      [&](int c) { update_cell<real, 256, CST>(c, a, step, xs, a.bcap, red); },
-      [&](int c) { update_cell<real, 32, CST>(c, a, step, xs + (size_t)warp * 3 * (a.bcap / 8), a.bcap / 8, red); });
+  if constexpr (sizeof(real) == 4) {
+    float* rf = reinterpret_cast<float*>(red);
+    __shared__ __align__(16) float recs[8][PF_STRIDE];
+    schedule_cells(
+        a.list_big, a.list_small, a.wl, a.work, WK_UPD_BIG, WK_UPD_SMALL,
+        [&](int c) { update_cell_f32<256, CST, PB>(c, a, step, xs, a.bcap, rf, recs[0]); },
+        [&](int c) {
+          update_cell_f32<32, CST, PB>(c, a, step, xs + (size_t)warp * 3 * (a.bcap / 8), a.bcap / 8, rf,
+                                       recs[warp]);
+        });
+  } else {
+    schedule_cells(
+        a.list_big, a.list_small, a.wl, a.work, WK_UPD_BIG, WK_UPD_SMALL,
+        [&](int c) { update_cell<real, 256, CST>(c, a, step, xs, a.bcap, red); },
+        [&](int c) { update_cell<real, 32, CST>(c, a, step, xs + (size_t)warp * 3 * (a.bcap / 8), a.bcap / 8, red); });
+  }
 }
 
 // the fused FP_dense step with specular or periodic walls and no long-range
@@ -1382,10 +1646,29 @@ template <typename real> static int update_impl(Session& s, uint32_t stages, int
   a.wcap = s.tune.wcap;
   a.bcap = s.tune.bcap;
   a.Vn = lr2d_potential(s);
+  a.kc = make_kc<real>(s.k);
   size_t sm = update_smem<real>(s);
-  if (stages == ST_FUSED_FP) k_update<real, ST_FUSED_FP><<<s.tune.grid_upd, 256, sm, s.stream>>>(a);
-  else if (stages == (ST_FUSED_FP | ST_LR)) k_update<real, ST_FUSED_FP | ST_LR><<<s.tune.grid_upd, 256, sm, s.stream>>>(a);
-  else k_update<real, 0u><<<s.tune.grid_upd, 256, sm, s.stream>>>(a);
+  const dim3 g(s.tune.grid_upd), b(256);
+  const bool spec = s.k.problem == MCPM_PROBLEM_CLOSED_BOX, per = s.k.problem == MCPM_PROBLEM_PERIODIC;
+  constexpr int SPEC = MCPM_PROBLEM_CLOSED_BOX, PER = MCPM_PROBLEM_PERIODIC;
+  constexpr uint32_t F = ST_FUSED_FP, FL = ST_FUSED_FP | ST_LR;
+  if constexpr (sizeof(real) == 4) {
+    if (stages == F) {
+      if (spec) k_update<real, F, SPEC><<<g, b, sm, s.stream>>>(a);
+      else if (per) k_update<real, F, PER><<<g, b, sm, s.stream>>>(a);
+      else k_update<real, F><<<g, b, sm, s.stream>>>(a);
+      return n + 1;
+    }
+    if (stages == FL) {
+      if (spec) k_update<real, FL, SPEC><<<g, b, sm, s.stream>>>(a);
+      else if (per) k_update<real, FL, PER><<<g, b, sm, s.stream>>>(a);
+      else k_update<real, FL><<<g, b, sm, s.stream>>>(a);
+      return n + 1;
+    }
+  }
+  if (stages == F) k_update<real, F><<<g, b, sm, s.stream>>>(a);
+  else if (stages == FL) k_update<real, FL><<<g, b, sm, s.stream>>>(a);
+  else k_update<real, 0u><<<g, b, sm, s.stream>>>(a);
   return n + 1;
 }
 int launch_update(Session& s, uint32_t stages, int bc_call_base) {
@@ -1411,23 +1694,26 @@ cudaError_t update_set_smem_max() {
   int dev = 0, mx = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&mx, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-  mx -= 4 * 8 * 16 + 64;  // leave room for the static reduction scratch
-  cudaError_t e = cudaFuncSetAttribute(k_update<float, 0u>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_update<double, 0u>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
-  if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(k_update<float, ST_FUSED_FP>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
-  if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(k_update<double, ST_FUSED_FP>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
-  if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(k_update<float, ST_FUSED_FP | ST_LR>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
-  if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(k_update<double, ST_FUSED_FP | ST_LR>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+  mx -= 4096;  // leave room for the static reduction scratch and cell records
+  constexpr uint32_t F = ST_FUSED_FP, FL = ST_FUSED_FP | ST_LR;
+  constexpr int SPEC = MCPM_PROBLEM_CLOSED_BOX, PER = MCPM_PROBLEM_PERIODIC;
+  const void* fns[] = {
+      (const void*)k_update<float, 0u>,          (const void*)k_update<double, 0u>,
+      (const void*)k_update<float, F>,           (const void*)k_update<double, F>,
+      (const void*)k_update<float, FL>,          (const void*)k_update<double, FL>,
+      (const void*)k_update<float, F, SPEC>,     (const void*)k_update<float, F, PER>,
+      (const void*)k_update<float, FL, SPEC>,    (const void*)k_update<float, FL, PER>};
+  cudaError_t e = cudaSuccess;
+  for (const void* f : fns)
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
   return e;
 }
 int update_occupancy(const Session& s) {
   int nb = 0;
   size_t sm = update_smem_bytes(s);
-  if (s.prec == MCPM_FP32) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_update<float, 0u>, 256, sm);
+  // the fused step's kernel sets the persistent grid (the split-mode
+  // variant, with every stage decided at run time, holds fewer blocks)
+  if (s.prec == MCPM_FP32) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_update<float, ST_FUSED_FP>, 256, sm);
   else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_update<double, 0u>, 256, sm);
   return nb < 1 ? 1 : nb;
 }

@@ -9,6 +9,12 @@
 #include "mcpm_internal.h"
 #include "mcpm_surrogate.h"
 
+// particles per block staged in shared memory by the FP32 particle pass
+// (bcap / 8 per warp): 36 KB per block, so that 6 blocks fit in an SM
+#ifndef MCPM_UPD_BCAP
+#define MCPM_UPD_BCAP 3072
+#endif
+
 namespace mcpm {
 SurrogateNet* sur_net(mcpm_surrogate* m);
 size_t update_smem_bytes(const Session& s);
@@ -195,7 +201,7 @@ int mcpm_session_create(const mcpm_config* cfg, mcpm_session** out) {
   s->own_stream = s->stream;
 
   // tuning defaults (see mcpm_tune in the Python layer for the sweep)
-  s->tune.bcap = (s->prec == MCPM_FP32) ? 6144 : 3072;
+  s->tune.bcap = (s->prec == MCPM_FP32) ? MCPM_UPD_BCAP : 3072;
   s->tune.wcap = 256;  // <= bcap / 8 (a warp's staging capacity); mcpm_autotune picks it
   s->tune.block = 256;
 
@@ -814,13 +820,13 @@ int mcpm_autotune(mcpm_session* s, int32_t steps, int32_t* chosen) {
   const bool sorted0 = s->sorted, keys0 = s->keys_current, rebin0 = s->needs_rebin, om0 = s->omega_init;
   const int64_t launches0 = s->launches;
   copy_all(true);
-  const int cands[4] = {128, 256, 512, 768};
+  const int cands[5] = {128, 256, 384, 512, 768};
   int best = s->tune.wcap;
   float best_ms = 1e30f;
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
-  for (int ci = 0; ci < 4 && rc == MCPM_OK; ++ci) {
+  for (int ci = 0; ci < 5 && rc == MCPM_OK; ++ci) {
     if (cands[ci] > s->tune.bcap / 8) continue;
     s->tune.wcap = cands[ci];
     s->cur = cur0; s->step = step0; s->keys_current = false; s->sorted = false; s->needs_rebin = false;

@@ -324,7 +324,7 @@ def test_autotune_restores_state(cuda_ok):
     s.step(2)
     before = s.download()
     w = s.autotune(2)
-    assert w in (128, 256, 512, 768) and s.wcap == w
+    assert w in (128, 256, 384) and s.wcap == w
     after = s.download()
     for k in before:
         assert np.array_equal(before[k], after[k]), k
@@ -332,7 +332,7 @@ def test_autotune_restores_state(cuda_ok):
     g1 = s.download()
     s2 = mcpm.Session(cfg)
     s2.upload(parts["x1"], parts["x2"], parts["U1"], parts["U2"], parts["U3"])
-    s2.set_wcap(128 if w != 128 else 512)
+    s2.set_wcap(128 if w != 128 else 384)
     s2.step(3)
     g2 = s2.download()
     e0 = np.sum(parts["U1"] ** 2 + parts["U2"] ** 2 + parts["U3"] ** 2)
