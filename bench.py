@@ -187,6 +187,28 @@ def _bf16_peak():
 SURROGATE_FLOP_PER_CELL = 2 * (9 * 11 * 64 + 2 * 9 * 64 * 64 + 9 * 64 * 4)
 
 
+def force_eval_ms(s, stream, method, reps=20, replays=5):
+    """Device time of one 2-D Vlasov force evaluation on the session's
+    current cell state (method 0: plain path, 1: the network), from a CUDA
+    graph of `reps` evaluations replayed `replays` times."""
+    import torch
+    s.eval_vlasov_2d(method)  # warm
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=stream):
+        for _ in range(reps):
+            s.eval_vlasov_2d(method)
+    g.replay()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(replays):
+        g.replay()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / (reps * replays)
+
+
 def _rel(a, b):
     import numpy as np
     a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
@@ -362,14 +384,19 @@ def run_mcpm(args):
                 "share": {k: round(v[0] / tot, 4) for k, v in prof.items() if v[0] > 0}}
     if sur is not None:
         # the learned force: algorithmic FLOPs of one inference (used channels)
-        # over its mean device time per step, against the measured bf16 peak
-        sur_ms = prof["surrogate"][0] / max(1, prof["surrogate"][1])
+        # over its device time, against the measured bf16 peak; the time of
+        # one evaluation of each force path is taken from a CUDA graph of 20
+        # back-to-back evaluations on the current state (no launch gaps)
+        s.cell_update()
+        sur_ms = force_eval_ms(s, stream, 1)
+        plain_ms = force_eval_ms(s, stream, 0)
         fl = SURROGATE_FLOP_PER_CELL * cfg.n_cells[0] * cfg.n_cells[1]
         tf, tf_kind = _bf16_peak()
         roofline["surrogate"] = {"bound": "tensor", "kernels": "k_input + 4 conv (2 x k_conv64_tc)",
                                  "achieved": round(fl / (sur_ms / 1e3) / 1e12, 2), "peak": tf, "unit": "TFLOP/s",
                                  "frac": round(fl / (sur_ms / 1e3) / 1e12 / tf, 4), "peak_kind": tf_kind,
-                                 "flop_per_inference": fl, "avg_ms": round(sur_ms, 4)}
+                                 "flop_per_inference": fl, "ms_per_inference": round(sur_ms, 4),
+                                 "plain_force_ms": round(plain_ms, 4)}
 
     # end to end through the C-ABI with pinned host buffers
     pin = lambda: torch.empty(N, dtype=torch.float64, pin_memory=True).numpy()  # noqa: E731

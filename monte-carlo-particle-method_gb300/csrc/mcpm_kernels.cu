@@ -16,6 +16,8 @@
 // the compensated FP32 sums require.
 #include <cfloat>
 
+#include <type_traits>
+
 #include "mcpm_device.cuh"
 
 namespace mcpm {
@@ -315,6 +317,43 @@ __device__ void moments_cell(int c, const MomArgs<real>& a, Acc<real>* red) {
     v[25] = Mp1 * energy * energy; v[26] = Mp2 * energy * energy; v[27] = Mp3 * energy * energy;
     v[28] = energy;
   };
+  if constexpr (sizeof(real) == 4) {
+    // FP32: the 29 sums in two groups (terms 0..14, then 15..28), each a
+    // pass over the cell's velocities (the second pass reads them from
+    // L1): half the accumulators live at a time, so more warps fit per SM.
+    // Within a group: compensated pairwise accumulation -- the terms of two
+    // particles are added in float, then the pair enters the compensated sum.
+    auto group = [&](auto J0c, auto Kc) {
+      constexpr int J0 = decltype(J0c)::value, K = decltype(Kc)::value;
+      Acc<real> g[K];
+#pragma unroll
+      for (int j = 0; j < K; ++j) g[j].zero();
+      for (int i = t; i < n; i += 2 * TILE) {
+        real v[29], w[29];
+        terms(i, v);
+        if (i + TILE < n) {
+          terms(i + TILE, w);
+#pragma unroll
+          for (int j = 0; j < K; ++j) v[J0 + j] += w[J0 + j];
+        }
+#pragma unroll
+        for (int j = 0; j < K; ++j) g[j].add(v[J0 + j]);
+      }
+      tile_reduce_write<real, K, TILE>(g, red, [&](int f, const Acc<real>& tot) {
+        a.cell[(size_t)(CFI_RAW + J0 + f) * C + c] = tot.get();
+      });
+    };
+    group(std::integral_constant<int, 0>(), std::integral_constant<int, 15>());
+    group(std::integral_constant<int, 15>(), std::integral_constant<int, 14>());
+    if (TILE == 32 || warp == 0) {
+      double* cl = a.cell;
+      if (lane == 29) cl[(size_t)(MCPM_CF_U_SPACE + 0) * C + c] = (double)m0;
+      else if (lane == 30) cl[(size_t)(MCPM_CF_U_SPACE + 1) * C + c] = (double)m1;
+      else if (lane == 31) cl[(size_t)(MCPM_CF_U_SPACE + 2) * C + c] = (double)m2;
+      if (lane == 0) cl[(size_t)MCPM_CF_NUM_INSIDE * C + c] = (double)n;
+    }
+    return;
+  }
   if constexpr (sizeof(real) == 8) {
     for (int i = t; i < n; i += TILE) {
       real v[29];
@@ -350,8 +389,13 @@ __device__ void moments_cell(int c, const MomArgs<real>& a, Acc<real>* red) {
   }
 }
 
+// blocks of 256 threads resident per SM in the FP32 moment pass (4: 64
+// registers, the two-group accumulation fits without spilling)
+#ifndef MCPM_MOM_MINB
+#define MCPM_MOM_MINB 4
+#endif
 template <typename real>
-__global__ void __launch_bounds__(256) k_moments(MomArgs<real> a) {
+__global__ void __launch_bounds__(256, sizeof(real) == 4 ? MCPM_MOM_MINB : 1) k_moments(MomArgs<real> a) {
   __shared__ Acc<real> red[29 * 8];
   schedule_cells(
       a.list_big, a.list_small, a.wl, a.work, WK_MOM_BIG, WK_MOM_SMALL,
@@ -1482,7 +1526,13 @@ __device__ void update_cell_f32(int c, const UpdArgs<float>& a, int step, float*
       // apply_BC: the box's wall type fixed at compile time where the
       // launch knows it (PB), else the run-time dispatch
       auto bc = [&](int call) {
-        if constexpr (PB == MCPM_PROBLEM_CLOSED_BOX) bc_specular<float>(s, k, kc, bad);
+        if constexpr (PB == MCPM_PROBLEM_CLOSED_BOX) {
+          // the first-pass tests of BC_specular_reflection: a particle that
+          // triggers none of them is left as it is
+          const bool r1 = k.dir0 == 1 && (s.x1 - kc.L0 > -1e-16f || s.x1 < 1e-16f);
+          const bool r2 = k.dir1 == 1 && (s.x2 - kc.L1 > -1e-16f || s.x2 < 1e-16f);
+          if (r1 || r2) bc_specular<float>(s, k, kc, bad);
+        }
         else if constexpr (PB == MCPM_PROBLEM_PERIODIC) bc_periodic<float>(s, k, kc);
         else apply_bc<float>(s, a.bc_call_base + call, pid, step, k, kc, bad);
       };
