@@ -209,21 +209,28 @@ __global__ void k_scatter(PT<real> src, PT<real> dst, const int32_t* key, const 
     int c = act ? key[i] : -1;
     unsigned am = __ballot_sync(FULL, act);
     if (act) {
+      // the particle's loads go out before the cursor atomic, so their
+      // latency overlaps it
+      const real x2 = src.x2[i], u1 = src.U1[i], u2 = src.U2[i], u3 = src.U3[i];
+      const int32_t pid = src.pid[i];
+      const real x1 = src.x1 ? src.x1[i] : (real)0;
+      const real x1o = src.x1o ? src.x1o[i] : (real)0, x2o = src.x2o ? src.x2o[i] : (real)0;
+      const int base = off[c];
       unsigned peers = __match_any_sync(am, c);
       int leader = __ffs(peers) - 1;
       int rank = __popc(peers & ((1u << lane) - 1u));
       int bse = 0;
       if (lane == leader) bse = atomicAdd(&cursor[c], __popc(peers));
       bse = __shfl_sync(peers, bse, leader);
-      int64_t d = (int64_t)off[c] + bse + rank;
-      if (src.x1) dst.x1[d] = src.x1[i];
-      dst.x2[d] = src.x2[i];
-      dst.U1[d] = src.U1[i];
-      dst.U2[d] = src.U2[i];
-      dst.U3[d] = src.U3[i];
-      dst.pid[d] = src.pid[i];
-      if (src.x1o) dst.x1o[d] = src.x1o[i];
-      if (src.x2o) dst.x2o[d] = src.x2o[i];
+      int64_t d = (int64_t)base + bse + rank;
+      if (src.x1) dst.x1[d] = x1;
+      dst.x2[d] = x2;
+      dst.U1[d] = u1;
+      dst.U2[d] = u2;
+      dst.U3[d] = u3;
+      dst.pid[d] = pid;
+      if (src.x1o) dst.x1o[d] = x1o;
+      if (src.x2o) dst.x2o[d] = x2o;
     }
   }
 }
