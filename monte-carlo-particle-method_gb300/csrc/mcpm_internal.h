@@ -31,12 +31,13 @@ enum {
   PF_AL0, PF_AL1, PF_AL2, PF_AL3, PF_AL4, PF_AL5, PF_BE0, PF_BE1, PF_GST,
   PF_HQ0, PF_HQ1,          // M3[0]+M3[3]+M3[5], M3[1]+M3[6]+M3[8] (DFP heat-flux terms)
   PF_PH0, PF_PH1, PF_F2DT, PF_N,
+  PF_E2,                   // sum over the cell of |M'|^2 (the moment pass's energy sum)
   // 2-D Vlasov kick: U1 -= LA1 + LB1 eta, U2 -= LA2 + LB2 xi (xi, eta the
   // particle's bilinear coordinates in its cell), one float4 of its own
   PF_LA1 = 36, PF_LB1, PF_LA2, PF_LB2,
   PF_STRIDE = 40
 };
-static_assert(PF_N < PF_LA1 && PF_LA1 % 4 == 0 && PF_STRIDE % 4 == 0, "packed record: float4 groups");
+static_assert(PF_E2 < PF_LA1 && PF_LA1 % 4 == 0 && PF_STRIDE % 4 == 0, "packed record: float4 groups");
 
 // Stages of the fused per-cell particle pass (update kernel).
 enum : uint32_t {
@@ -128,6 +129,10 @@ struct Session {
   alignas(16) char lr_host[160];  // the kernel's view of lr_tab
   LR2D* lr2d = nullptr;         // 2-D long range (node grid), when configured
   bool nodes_valid = false;     // nodal densities describe the last cell_update
+  bool qc_fuse_now = false;     // this particle pass also counts cell quadrants
+  // the 2-D force reads nodal densities (screened Poisson or the learned force)
+  bool lr2d_nodes_needed() const { return lr2d && (cfg.long_range == MCPM_LR_SCREENED_POISSON || sur); }
+  bool qc_ready = false;        // those counts describe the positions the keys bin
   uint32_t* status = nullptr;
   int32_t* dstep = nullptr;     // device copy of the step number the kernels read
   int dstep_val = -1;           // the value it holds once queued work has run (-1: unknown)
@@ -191,6 +196,10 @@ int launch_node_density(Session& s);
 int launch_long_range_2d(Session& s);
 int launch_node_density_from(Session& s, const int32_t* qc);
 int32_t* lr2d_quadrants(Session& s);
+// the quadrant-count buffer the FP32 particle pass fills and its cell-centre
+// thresholds; false when the session has none
+bool lr2d_quad_fuse(Session& s, int32_t** qc, const float** qtx, const float** qty);
+int32_t* lr2d_quad_next(Session& s);
 double* lr2d_node_density_mut(Session& s);
 const double* lr2d_potential(const Session& s);
 const double* lr2d_node_density(const Session& s);

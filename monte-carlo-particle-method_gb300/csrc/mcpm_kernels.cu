@@ -39,7 +39,7 @@ template <typename real> static PT<real> pt(const PBuf& b) {
 // binned into the last cell.
 template <typename real>
 __device__ __forceinline__ int bin_one(real x1, real x2, int pid, int step, const DevConsts& k, const KC<real>& kc,
-                                       uint32_t& bad) {
+                                       uint32_t& bad, int* jo = nullptr, int* ko = nullptr) {
   // FP64: r_floor(x / dx) as the reference; FP32: x * (1/dx)
   constexpr bool F32 = sizeof(real) == 4;
   int j = 0;
@@ -71,6 +71,8 @@ __device__ __forceinline__ int bin_one(real x1, real x2, int pid, int step, cons
   }
   j = j < 0 ? 0 : (j > k.N0 - 1 ? k.N0 - 1 : j);
   kk = kk < 0 ? 0 : (kk > k.N1 - 1 ? k.N1 - 1 : kk);
+  if (jo) *jo = j;
+  if (ko) *ko = kk;
   return kk * k.N0 + j;
 }
 
@@ -744,6 +746,7 @@ __global__ void __launch_bounds__(128) k_solve(DevConsts k, double* cell, float*
     pf[PF_HQ1] = (float)(M3[1] + M3[6] + M3[8]);
     pf[PF_PH0] = (float)ph0; pf[PF_PH1] = (float)ph1;
     pf[PF_N] = (float)ncnt;
+    pf[PF_E2] = (float)R(CFI_RAW + 28);
   }
   raise_status(status, bad);
 }
@@ -969,6 +972,11 @@ template <typename real> struct UpdArgs {
   const double* Vn;  // node potential of the 2-D Vlasov force (FP64 path)
   KC<real> kc;       // constants in the state's precision (read from the
                      // parameter bank, so they cost no registers)
+  // quadrant counts of the new positions for the next step's nodal deposit
+  // (FP32 2-D Vlasov sessions; null otherwise): qc[cell][quadrant] and the
+  // cell-centre thresholds per column / row
+  int32_t* qc;
+  const float *qtx, *qty;
 };
 
 template <typename real>
@@ -1379,33 +1387,26 @@ __device__ void update_cell_f32(int c, const UpdArgs<float>& a, int step, float*
   const float Us0 = R[PF_US0], Us1 = R[PF_US1], Us2 = R[PF_US2];
   const PT<float>& P = a.p;  // pointers stay in the parameter bank
   float mean0 = 0.f, mean1 = 0.f, mean2 = 0.f, irms0 = 1.f, irms1 = 1.f, irms2 = 1.f, f1 = 0.f;
-  // ---- pass A: draws, their per-cell sums, sum |M'|^2
-  if (rng || fp) {
-    float sa[7] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};  // z0 z1 z2 |M'|^2 z0^2 z1^2 z2^2
+  // ---- pass A: draws and their per-cell sums.  sum |M'|^2 before the
+  // update is the moment pass's energy sum (the same M' = U - U_space)
+  f1 = R[PF_E2];
+  if (rng) {
+    float sa[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};  // z0 z1 z2 z0^2 z1^2 z2^2
     UPD_UNROLL
     for (int i = t; i < n; i += TILE) {
       const int64_t p = s0 + i;
-      if (rng) {
-        float z0, z1, z2;
-        raw_normals(a, step, p, z0, z1, z2);
-        if (staged) { xs[3 * i] = z0; xs[3 * i + 1] = z1; xs[3 * i + 2] = z2; }
-        sa[0] += z0; sa[1] += z1; sa[2] += z2;
-        sa[4] = fmaf(z0, z0, sa[4]); sa[5] = fmaf(z1, z1, sa[5]); sa[6] = fmaf(z2, z2, sa[6]);
-      }
-      if (fp) {
-        const float m1 = P.U1[p] - Us0, m2 = P.U2[p] - Us1, m3 = P.U3[p] - Us2;
-        sa[3] = fmaf(m3, m3, fmaf(m2, m2, fmaf(m1, m1, sa[3])));
-      }
+      float z0, z1, z2;
+      raw_normals(a, step, p, z0, z1, z2);
+      if (staged) { xs[3 * i] = z0; xs[3 * i + 1] = z1; xs[3 * i + 2] = z2; }
+      sa[0] += z0; sa[1] += z1; sa[2] += z2;
+      sa[3] = fmaf(z0, z0, sa[3]); sa[4] = fmaf(z1, z1, sa[4]); sa[5] = fmaf(z2, z2, sa[5]);
     }
-    tile_sum_f32<7, TILE>(sa, red);
-    f1 = sa[3];
-    if (rng) {
-      const float rn = 1.0f / (float)n;
-      mean0 = sa[0] * rn; mean1 = sa[1] * rn; mean2 = sa[2] * rn;
-      irms0 = 1.0f / sqrtf(fmaxf(fmaf(-mean0, mean0, sa[4] * rn), 0.f));
-      irms1 = 1.0f / sqrtf(fmaxf(fmaf(-mean1, mean1, sa[5] * rn), 0.f));
-      irms2 = 1.0f / sqrtf(fmaxf(fmaf(-mean2, mean2, sa[6] * rn), 0.f));
-    }
+    tile_sum_f32<6, TILE>(sa, red);
+    const float rn = 1.0f / (float)n;
+    mean0 = sa[0] * rn; mean1 = sa[1] * rn; mean2 = sa[2] * rn;
+    irms0 = 1.0f / sqrtf(fmaxf(fmaf(-mean0, mean0, sa[3] * rn), 0.f));
+    irms1 = 1.0f / sqrtf(fmaxf(fmaf(-mean1, mean1, sa[4] * rn), 0.f));
+    irms2 = 1.0f / sqrtf(fmaxf(fmaf(-mean2, mean2, sa[5] * rn), 0.f));
   }
   // whitened normal of the i-th particle of the cell
   auto xiw = [&](int i, float& z0, float& z1, float& z2) {
@@ -1480,7 +1481,7 @@ __device__ void update_cell_f32(int c, const UpdArgs<float>& a, int step, float*
   for (int r = 0; r < iters; ++r) {
     const int i = r * TILE + t;
     const bool act = i < n;
-    int key = 0;
+    int key = 0, qkey = 0;
     if (act) {
       const int64_t p = s0 + i;
       PState<float> s;
@@ -1557,11 +1558,19 @@ __device__ void update_cell_f32(int c, const UpdArgs<float>& a, int step, float*
       if (P.x1o) P.x1o[p] = s.x1o;
       if (P.x2o) P.x2o[p] = s.x2o;
       if (st & ST_KEY) {
-        key = bin_one<float>(s.x1, s.x2, pid, step + 1, k, kc, bad);
+        int jn, kn;
+        key = bin_one<float>(s.x1, s.x2, pid, step + 1, k, kc, bad, &jn, &kn);
         a.key_out[p] = key;
+        // its quadrant in the new cell, as the nodal deposit counts it
+        // (left of / below the centre: the threshold is the smallest float
+        // at or above the centre)
+        if (a.qc) qkey = 4 * key + (s.x1 < a.qtx[jn] ? 0 : 1) + (s.x2 < a.qty[kn] ? 0 : 2);
       }
     }
-    if (st & ST_KEY) count_key(a.cnt_next, key, act);
+    if (st & ST_KEY) {
+      count_key(a.cnt_next, key, act);
+      if (a.qc) count_key(a.qc, qkey, act);
+    }
   }
   raise_status(a.status, bad);
 }
@@ -1631,6 +1640,7 @@ static inline int grid_for(int64_t n, int block, int max_blocks) {
 
 template <typename real> static int bin_impl(Session& s, int bin_step) {
   PT<real> p = pt<real>(s.P[s.cur]);
+  s.qc_ready = false;  // the quadrant counts follow the particle pass's keys only
   // every key is recomputed: counts start from zero, whatever was pending
   cudaMemsetAsync(s.cnt_next, 0, (size_t)s.C * sizeof(int32_t), s.stream);
   k_bin<real><<<grid_for(s.N, 256, s.num_sms * 8), 256, 0, s.stream>>>(p, s.N, s.k, bin_step, s.key, s.cnt_next,
@@ -1704,6 +1714,9 @@ template <typename real> static int update_impl(Session& s, uint32_t stages, int
   a.bcap = s.tune.bcap;
   a.Vn = lr2d_potential(s);
   a.kc = make_kc<real>(s.k);
+  a.qc = nullptr;
+  a.qtx = a.qty = nullptr;
+  if (sizeof(real) == 4 && s.qc_fuse_now) lr2d_quad_fuse(s, &a.qc, &a.qtx, &a.qty);
   size_t sm = update_smem<real>(s);
   const dim3 g(s.tune.grid_upd), b(256);
   const bool spec = s.k.problem == MCPM_PROBLEM_CLOSED_BOX, per = s.k.problem == MCPM_PROBLEM_PERIODIC;

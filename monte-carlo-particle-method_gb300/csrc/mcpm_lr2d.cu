@@ -72,6 +72,8 @@ struct LR2D {
   double lambda2vol;                  // bst^2 vol, the mass coefficient of the operator
   double near1, near2;                // the near-field constants of src/FEM.cpp:491-496
   int iters;                          // refinement passes
+  int32_t* qc_next = nullptr;  // [C][4] quadrant counts accumulated by the FP32 particle pass
+  float *qtx = nullptr, *qty = nullptr;  // [N0], [N1] cell-centre thresholds (smallest float >= centre)
   int* wall = nullptr;      // [n_wall] ids of the wall nodes
   int n_wall;
   size_t smem;              // dynamic shared memory of the node kernels
@@ -515,6 +517,24 @@ int lr2d_setup(Session& s) {
             A((void**)&t->exc_w, st.exc_w.size() * 8) && H(t->exc_w, st.exc_w.data(), st.exc_w.size() * 8) &&
             A((void**)&t->V, (size_t)t->nn * 8) && A((void**)&t->nnd, (size_t)k.C * 4 * 8) &&
             A((void**)&t->qc, (size_t)k.C * 4 * 4);
+  if (ok && s.prec == MCPM_FP32) {
+    // the particle pass counts quadrants of the new positions: x < the
+    // centre of the column / row in exact arithmetic <=> x < the smallest
+    // float at or above it (the comparison k_quadrants makes)
+    std::vector<float> tx(k.N0), ty(k.N1);
+    for (int j = 0; j < k.N0; ++j) {
+      const double cx = 0.5 * ((double)j * k.dx + (double)(j + 1) * k.dx);
+      const float f = (float)cx;
+      tx[j] = (double)f >= cx ? f : nextafterf(f, INFINITY);
+    }
+    for (int j = 0; j < k.N1; ++j) {
+      const double cy = 0.5 * ((double)j * k.dy + (double)(j + 1) * k.dy);
+      const float f = (float)cy;
+      ty[j] = (double)f >= cy ? f : nextafterf(f, INFINITY);
+    }
+    ok = A((void**)&t->qc_next, (size_t)k.C * 4 * 4) && A((void**)&t->qtx, tx.size() * 4) &&
+         H(t->qtx, tx.data(), tx.size() * 4) && A((void**)&t->qty, ty.size() * 4) && H(t->qty, ty.data(), ty.size() * 4);
+  }
   if (ok && mode == MCPM_LR_SCREENED_POISSON) {
     std::vector<double> Sx, Sy, kx, mx, ky, my;
     dst_matrix(t->nx, Sx, kx, mx);
@@ -563,7 +583,7 @@ void lr2d_free(Session& s) {
   if (!t) return;
   cudaFree(t->W); cudaFree(t->exc_off); cudaFree(t->exc_i); cudaFree(t->exc_w); cudaFree(t->V); cudaFree(t->nnd);
   cudaFree(t->qc); cudaFree(t->Sx); cudaFree(t->Sy); cudaFree(t->mu); cudaFree(t->B); cudaFree(t->U); cudaFree(t->Bf); cudaFree(t->Tf);
-  cudaFree(t->wall);
+  cudaFree(t->wall); cudaFree(t->qc_next); cudaFree(t->qtx); cudaFree(t->qty);
   delete t;
   s.lr2d = nullptr;
 }
@@ -576,6 +596,15 @@ int lr2d_num_nodes(const Session& s) { return s.lr2d ? s.lr2d->nn : 0; }
 static int blocks_for(long n, int bs, int cap) { return (int)std::max(1L, std::min((n + bs - 1) / bs, (long)cap)); }
 
 int32_t* lr2d_quadrants(Session& s) { return s.lr2d ? s.lr2d->qc : nullptr; }
+bool lr2d_quad_fuse(Session& s, int32_t** qc, const float** qtx, const float** qty) {
+  LR2D* t = s.lr2d;
+  if (!t || !t->qc_next) return false;
+  *qc = t->qc_next;
+  *qtx = t->qtx;
+  *qty = t->qty;
+  return true;
+}
+int32_t* lr2d_quad_next(Session& s) { return s.lr2d ? s.lr2d->qc_next : nullptr; }
 double* lr2d_node_density_mut(Session& s) { return s.lr2d ? s.lr2d->nnd : nullptr; }
 
 // nodal densities from given quadrant counts (training snapshots)
@@ -590,6 +619,12 @@ int launch_node_density(Session& s) {
   LR2D* t = s.lr2d;
   // the screened-Poisson force and the learned force read them
   if (!t || (t->mode != MCPM_LR_SCREENED_POISSON && !s.sur)) return 0;
+  if (s.qc_ready && t->qc_next) {
+    // the previous particle pass counted the quadrants of these positions
+    k_node_density<<<blocks_for(4L * s.C, 256, s.num_sms * 16), 256, 0, s.stream>>>(s.k, t->qc_next, t->nnd,
+                                                                                      s.prec == MCPM_FP64);
+    return 1;
+  }
   const int g = blocks_for((long)s.C * 32, 256, s.num_sms * 16);
   if (s.prec == MCPM_FP32) {
     const PBuf& P = s.P[s.cur];

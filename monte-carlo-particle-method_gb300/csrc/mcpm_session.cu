@@ -462,7 +462,14 @@ static int step_once(mcpm_session* s, uint32_t stages) {
   s->nodes_valid = s->lr2d != nullptr;
   if (m == MCPM_MODEL_ESMC) n += T_ESMC(launch_esmc(*s));
   if (s->cfg.long_range != MCPM_LR_NONE) n += long_range_force(s);
+  // FP32 sessions with nodal densities: the particle pass also counts the
+  // quadrants of the new positions, which the next step's deposit reads
+  int32_t* qn = lr2d_quad_next(*s);
+  s->qc_fuse_now = qn && (stages & ST_KEY) && (s->lr2d_nodes_needed());
+  if (s->qc_fuse_now) cudaMemsetAsync(qn, 0, (size_t)s->C * 4 * sizeof(int32_t), s->stream);
   n += T_UPD(launch_update(*s, stages, 0));
+  s->qc_ready = s->qc_fuse_now;
+  s->qc_fuse_now = false;
   k_step_advance<<<1, 1, 0, s->stream>>>(s->dstep);
   ++n;
   s->step++;

@@ -111,3 +111,18 @@ def test_fused_step_fp_dense_2d_vlasov(cuda_ok, lr):
         a, b = g[k], getattr(o.s, k)
         err = np.max(np.abs(a - b)) / max(1.0, np.max(np.abs(b)))
         assert err <= 1e-9, (k, err)
+
+
+def test_fused_quadrant_counts_equal_the_deposit_pass(cuda_ok):
+    """FP32 sessions count the quadrants of the new positions inside the
+    particle pass; the next deposit must equal the one the separate
+    quadrant pass makes from the same positions (exact: counts x Fn/vol)."""
+    cfg, parts = _box(mcpm.LR_SCREENED_POISSON, prec=mcpm.FP32, n_cells=(24, 20), ppc=60, model=mcpm.MODEL_FP_DENSE)
+    s = _session(cfg, parts)
+    s.step(3)
+    s.cell_update()  # bins by the particle pass's keys: the fused counts
+    fused = s.get_node_density()
+    g = s.download()
+    r = _session(cfg, g)  # the same positions, binned and counted afresh
+    r.cell_update()
+    assert np.array_equal(fused, r.get_node_density())
