@@ -595,7 +595,7 @@ __global__ void __launch_bounds__(128) k_solve(DevConsts k, double* cell, float*
         for (int j = 0; j < 9; ++j) al[j] = 0.0;
         for (int j = 0; j < 3; ++j) be[j] = 0.0;
       } else {
-        const double pi = acos(-1.0);
+        const double pi = 3.141592653589793;  // acos(-1.0), correctly rounded
         double trace = P[0] + P[3] + P[5];
         double dev[6];
         for (int j = 0; j < 6; ++j) dev[j] = P[j];
@@ -610,7 +610,13 @@ __global__ void __launch_bounds__(128) k_solve(DevConsts k, double* cell, float*
         double p_crr = (1.0 + n * k.b * Y);
         double mu_crr = (1.0 + 2.0 * n * k.b * Y / 5.0);
         double k_crr = (1.0 + 3.0 * n * k.b * Y / 5.0);
-        double w = (4.0 / 9.0) * sqrt(pi) * Y * (n * n) * pow(k.sigma, 4.0) * sqrt(k.m * k.kb * T);
+        double w;
+        if (EXACT) {
+          w = (4.0 / 9.0) * sqrt(pi) * Y * (n * n) * pow(k.sigma, 4.0) * sqrt(k.m * k.kb * T);
+        } else {
+          const double s2 = k.sigma * k.sigma;
+          w = (4.0 / 9.0) * 1.7724538509055159 * Y * (n * n) * (s2 * s2) * sqrt(k.m * k.kb * T);
+        }
         double div_U;
         const int last = C - 1;
         if (C == 1) div_U = 0.0;
@@ -623,6 +629,23 @@ __global__ void __launch_bounds__(128) k_solve(DevConsts k, double* cell, float*
         double coeff_mu = 3.0 * 1.002 / 5.0 * (nbY * nbY) / (1 + 2.0 * n * k.b * Y / 5.0);
         double coeff_k = 1.002 * (nbY * nbY) / (1 + 3.0 * n * k.b * Y / 5.0) / 5.0;
         double rhs[12];
+        if (!EXACT) {
+          // the same terms with the common factors formed once
+          const double pt3 = (p_crr - 1.0) * trace * (1.0 / 3.0) - w * div_U / (k.m * n);
+          const double cm = (mu_crr - 1.0) + coeff_mu, ck = (k_crr - 1.0) + coeff_k;
+          rhs[0] = cm * dev[0] + pt3 - gst * M4[0];
+          rhs[1] = cm * dev[1] - gst * M4[1];
+          rhs[2] = cm * dev[2] - gst * M4[2];
+          rhs[3] = rhs[1];
+          rhs[4] = cm * dev[3] + pt3 - gst * M4[3];
+          rhs[5] = cm * dev[4] - gst * M4[4];
+          rhs[6] = rhs[2];
+          rhs[7] = rhs[5];
+          rhs[8] = cm * dev[5] + pt3 - gst * M4[5];
+          rhs[9] = ck * ma - gst * M5[0] + gst * (DM2 * ma);
+          rhs[10] = ck * mb - gst * M5[1] + gst * (DM2 * mb);
+          rhs[11] = ck * mc - gst * M5[2] + gst * (DM2 * mc);
+        } else {
         rhs[0] = (mu_crr - 1.0) * dev[0] + (p_crr - 1.0) * trace / 3.0 - w * div_U / (k.m * n) + coeff_mu * dev[0] - gst * M4[0];
         rhs[1] = (mu_crr - 1.0) * dev[1] + coeff_mu * dev[1] - gst * M4[1];
         rhs[2] = (mu_crr - 1.0) * dev[2] + coeff_mu * dev[2] - gst * M4[2];
@@ -635,6 +658,7 @@ __global__ void __launch_bounds__(128) k_solve(DevConsts k, double* cell, float*
         rhs[9] = (k_crr - 1.0) * ma + coeff_k * ma - gst * (M5[0]) + gst * (DM2 * (M3[0] + M3[3] + M3[5]));
         rhs[10] = (k_crr - 1.0) * mb + coeff_k * mb - gst * (M5[1]) + gst * (DM2 * (M3[1] + M3[6] + M3[8]));
         rhs[11] = (k_crr - 1.0) * mc + coeff_k * mc - gst * (M5[2]) + gst * (DM2 * (M3[2] + M3[7] + M3[9]));
+        }
         const double m3b[3] = {ma, mb, mc};
         for (int blk = 0; blk < 3; ++blk) {
           double A[16], r4[4], x4[4];
@@ -692,9 +716,14 @@ __global__ void __launch_bounds__(128) k_solve(DevConsts k, double* cell, float*
       double mu = scale_mu(T, k);
       double tau = 2.0 * mu / (n * k.kb * T);
       for (int j = 0; j < 6; ++j) rhs[j] = -2.0 * Lam * M4[j];
-      rhs[6] = Y * (3.0 / tau - 2.0 * Pr / tau) * Q[0];
-      rhs[7] = Y * (3.0 / tau - 2.0 * Pr / tau) * Q[1];
-      rhs[8] = Y * (3.0 / tau - 2.0 * Pr / tau) * Q[2];
+      if (EXACT) {
+        rhs[6] = Y * (3.0 / tau - 2.0 * Pr / tau) * Q[0];
+        rhs[7] = Y * (3.0 / tau - 2.0 * Pr / tau) * Q[1];
+        rhs[8] = Y * (3.0 / tau - 2.0 * Pr / tau) * Q[2];
+      } else {
+        const double f = Y * (3.0 - 2.0 * Pr) / tau;
+        rhs[6] = f * Q[0]; rhs[7] = f * Q[1]; rhs[8] = f * Q[2];
+      }
       rhs[6] += Lam * (-3.0 * M5[0] + DM2 * Q[0] + 2.0 * (P[0] * Q[0] + P[1] * Q[1] + P[2] * Q[2]));
       rhs[7] += Lam * (-3.0 * M5[1] + DM2 * Q[1] + 2.0 * (P[1] * Q[0] + P[3] * Q[1] + P[4] * Q[2]));
       rhs[8] += Lam * (-3.0 * M5[2] + DM2 * Q[2] + 2.0 * (P[2] * Q[0] + P[4] * Q[1] + P[5] * Q[2]));
