@@ -330,23 +330,32 @@ __device__ void moments_cell(int c, const MomArgs<real>& a, Acc<real>* red) {
     // FP32: the 29 sums in two groups (terms 0..14, then 15..28), each a
     // pass over the cell's velocities (the second pass reads them from
     // L1): half the accumulators live at a time, so more warps fit per SM.
-    // Within a group: compensated pairwise accumulation -- the terms of two
-    // particles are added in float, then the pair enters the compensated sum.
+    // Within a group: compensated accumulation of partials -- the terms of
+    // up to four of a lane's particles are summed in float, then the partial
+    // enters the compensated sum.
     auto group = [&](auto J0c, auto Kc) {
       constexpr int J0 = decltype(J0c)::value, K = decltype(Kc)::value;
       Acc<real> g[K];
 #pragma unroll
       for (int j = 0; j < K; ++j) g[j].zero();
-      for (int i = t; i < n; i += 2 * TILE) {
-        real v[29], w[29];
-        terms(i, v);
-        if (i + TILE < n) {
-          terms(i + TILE, w);
+      for (int i = t; i < n; i += 4 * TILE) {
+        real ps[K];
+        {
+          real v[29];
+          terms(i, v);
 #pragma unroll
-          for (int j = 0; j < K; ++j) v[J0 + j] += w[J0 + j];
+          for (int j = 0; j < K; ++j) ps[j] = v[J0 + j];
+        }
+#pragma unroll 1
+        for (int q = 1; q < 4; ++q) {
+          if (i + q * TILE >= n) break;
+          real v[29];
+          terms(i + q * TILE, v);
+#pragma unroll
+          for (int j = 0; j < K; ++j) ps[j] += v[J0 + j];
         }
 #pragma unroll
-        for (int j = 0; j < K; ++j) g[j].add(v[J0 + j]);
+        for (int j = 0; j < K; ++j) g[j].add(ps[j]);
       }
       tile_reduce_write<real, K, TILE>(g, red, [&](int f, const Acc<real>& tot) {
         a.cell[(size_t)(CFI_RAW + J0 + f) * C + c] = tot.get();
