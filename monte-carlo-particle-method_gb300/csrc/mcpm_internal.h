@@ -169,6 +169,7 @@ struct Session {
   double sur_thr = 0.01;
   bool sur_active = true;       // the network supplies the force
   bool sur_judge_now = false;   // this step runs both paths and compares
+  bool sur_xin_ready = false;   // the nodal deposit also wrote the network input
   double* sur_err = nullptr;    // device [2]: sum |kick_net - kick_plain|^2, sum |kick_plain|^2
   double* sur_err_h = nullptr;  // pinned host copy
   double sur_last_err = -1.0;

@@ -621,6 +621,7 @@ int mcpm_attach_surrogate(mcpm_session* s, mcpm_surrogate* m, int32_t judge_ever
   if (!s) return MCPM_ERR_ARG;
   if (!m) {
     s->sur = nullptr;
+    s->sur_xin_ready = false;
     return MCPM_OK;
   }
   SurrogateNet* n = sur_net(m);
@@ -635,6 +636,7 @@ int mcpm_attach_surrogate(mcpm_session* s, mcpm_surrogate* m, int32_t judge_ever
     }
   }
   s->sur = n;
+  s->sur_xin_ready = false;  // the next nodal deposit writes this network's input
   s->sur_every = judge_every;
   s->sur_thr = threshold;
   s->sur_active = true;

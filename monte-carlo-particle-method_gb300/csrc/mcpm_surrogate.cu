@@ -245,6 +245,118 @@ __global__ void __launch_bounds__(NT) k_conv(ConvArgs a) {
     }
 }
 
+// Inference variant for the narrow layers (16 -> 64 and 64 -> 16): one
+// block per 128-cell row segment stages the whole 3-row halo of its input
+// (3 x 130 cells, zero outside the grid) and all nine weight taps once, then
+// runs the nine taps from shared memory -- a third of the per-tap tiles'
+// L2 traffic and one wait instead of nine.  Tiles never cross a grid row.
+template <int CIN, int COUT> constexpr int halo_a_bytes() { return 3 * (TM + 2) * CIN * 2; }
+template <int CIN, int COUT> constexpr int halo_smem() {
+  return ((halo_a_bytes<CIN, COUT>() + 127) / 128) * 128 + COUT * (9 * CIN + 8) * 2;
+}
+
+template <int CIN, int COUT, int EPI>
+__global__ void __launch_bounds__(NT) k_conv_halo(ConvArgs a, int tiles_per_row) {
+  constexpr int CH = CIN / 8, HW = TM + 2, HROWS = 3 * HW;
+  constexpr int KW = 9 * CIN, KWP = KW + 8;  // weight row, padded to an odd number of 16-byte chunks
+  constexpr int WN = COUT >= 64 ? 2 : 1, WM = 8 / WN, WTM = TM / WM, WTN = COUT / WN;
+  constexpr int MI = WTM / 16, NI = WTN / 8;
+  static_assert(NI % 2 == 0 && MI >= 1, "warp tile");
+  extern __shared__ __align__(128) unsigned char smem[];
+  unsigned char* As = smem;
+  unsigned char* Bs = smem + ((halo_a_bytes<CIN, COUT>() + 127) / 128) * 128;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int wm = warp % WM, wn = warp / WM;
+  const int row = blockIdx.x / tiles_per_row, x0 = (blockIdx.x - row * tiles_per_row) * TM;
+  const int N0 = a.N0, N1 = a.N1;
+  const int b = row / N1, y = row - b * N1;
+  for (int e = tid; e < HROWS * CH; e += NT) {
+    const int hr = e / CH, ch = e - hr * CH, r3 = hr / HW, px = hr - r3 * HW;
+    const int yy = y + r3 - 1, xx = x0 + px - 1;
+    const bool v = yy >= 0 && yy < N1 && xx >= 0 && xx < N0;
+    const bf16* src = v ? a.x + ((size_t)(b * a.C + yy * N0 + xx) * CIN + ch * 8) : a.x;
+    cp_async16(smem_u32(As + swz<CH>(hr, ch)), src, v);
+  }
+  for (int e = tid; e < COUT * (KW / 8); e += NT) {
+    const int co = e / (KW / 8), kc = e - co * (KW / 8);
+    cp_async16(smem_u32(Bs + ((size_t)co * KWP + kc * 8) * 2), a.w + (size_t)co * KW + kc * 8, true);
+  }
+  cp_async_commit();
+  cp_async_wait<0>();
+  __syncthreads();
+
+  float acc[MI][NI][4];
+#pragma unroll
+  for (int i = 0; i < MI; ++i)
+#pragma unroll
+    for (int j = 0; j < NI; ++j)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) acc[i][j][q] = 0.f;
+#pragma unroll 1
+  for (int tap = 0; tap < 9; ++tap) {
+    const int dy = tap / 3 - 1, dx = tap % 3 - 1;
+#pragma unroll
+    for (int kk = 0; kk < CIN / 16; ++kk) {
+      uint32_t af[MI][4], bfr[NI][2];
+#pragma unroll
+      for (int mi = 0; mi < MI; ++mi) {
+        const int hr = (dy + 1) * HW + wm * WTM + mi * 16 + (lane & 15) + dx + 1;
+        ldsm_x4(af[mi], smem_u32(As + swz<CH>(hr, kk * 2 + (lane >> 4))));
+      }
+#pragma unroll
+      for (int ni = 0; ni < NI; ni += 2) {
+        const int co = wn * WTN + ni * 8 + (lane & 7) + ((lane >> 4) << 3);
+        const int kq = tap * CIN + kk * 16 + ((lane >> 3) & 1) * 8;
+        uint32_t r[4];
+        ldsm_x4(r, smem_u32(Bs + ((size_t)co * KWP + kq) * 2));
+        bfr[ni][0] = r[0]; bfr[ni][1] = r[1]; bfr[ni + 1][0] = r[2]; bfr[ni + 1][1] = r[3];
+      }
+#pragma unroll
+      for (int mi = 0; mi < MI; ++mi)
+#pragma unroll
+        for (int ni = 0; ni < NI; ++ni) mma16816(acc[mi][ni], af[mi], bfr[ni][0], bfr[ni][1]);
+    }
+  }
+
+#pragma unroll
+  for (int mi = 0; mi < MI; ++mi)
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int xi = x0 + wm * WTM + mi * 16 + (lane >> 2) + h * 8;
+      const bool ok = xi < N0;
+      const int p = row * N0 + xi;
+#pragma unroll
+      for (int ni = 0; ni < NI; ++ni) {
+        const int col = wn * WTN + ni * 8 + 2 * (lane & 3);
+        float v0 = acc[mi][ni][2 * h], v1 = acc[mi][ni][2 * h + 1];
+        if constexpr (EPI == EPI_RELU) {
+          v0 = fmaxf(v0 + a.bias[col], 0.f);
+          v1 = fmaxf(v1 + a.bias[col + 1], 0.f);
+          if (ok)
+            *reinterpret_cast<__nv_bfloat162*>(static_cast<bf16*>(a.out) + (size_t)p * COUT + col) =
+                __floats2bfloat162_rn(v0, v1);
+        } else if constexpr (EPI == EPI_OUT) {
+          if (col < 4 && ok) {
+            float* o = static_cast<float*>(a.out) + (size_t)p * 4 + col;
+            o[0] = v0 + a.bias[col];
+            o[1] = v1 + a.bias[col + 1];
+          }
+        } else {  // EPI_KICK: lanes 4q hold outputs 0, 1 of a cell, lanes 4q + 1 outputs 2, 3
+          static_assert(EPI == EPI_KICK, "inference epilogues");
+          if (ni == 0 && wn == 0) {
+            const float w2 = __shfl_down_sync(0xffffffffu, v0, 1), w3 = __shfl_down_sync(0xffffffffu, v1, 1);
+            if ((lane & 3) == 0 && ok) {
+              const float d0 = (v0 + a.bias[0]) * a.oscale, d1 = (v1 + a.bias[1]) * a.oscale;
+              const float d2 = (w2 + a.bias[2]) * a.oscale, d3 = (w3 + a.bias[3]) * a.oscale;
+              *reinterpret_cast<float4*>(a.pcell + (size_t)p * PF_STRIDE + PF_LA1) =
+                  make_float4(d0 * a.g1, (d1 - d0) * a.g1, d2 * a.g2, (d3 - d2) * a.g2);
+            }
+          }
+        }
+      }
+    }
+}
+
 struct WgArgs {
   const bf16* x;   // [P][CIN] layer input
   const bf16* dz;  // [P][COUT] gradient of the layer's pre-activation
@@ -440,17 +552,13 @@ __global__ void k_flip(const bf16* W, int cout, int cin, bf16* F) {
 // hi) (channels 0..4 and 6..10), so the input keeps ~16 significant bits --
 // the kick follows from density differences between neighbouring nodes,
 // a few percent of the density, below a single bf16's resolution
-__device__ __forceinline__ void hi_lo(double v, __nv_bfloat16& hi, __nv_bfloat16& lo) {
-  hi = __float2bfloat16_rn((float)v);
-  lo = __float2bfloat16_rn((float)(v - (double)__bfloat162float(hi)));
-}
 __global__ void k_input(const double* nnd, const double* n, double b, int C, bf16* x) {
   for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < C; c += gridDim.x * blockDim.x) {
     __align__(16) bf16 q[16];
     const double* nn = nnd + (size_t)c * 4;
 #pragma unroll
-    for (int k = 0; k < 4; ++k) hi_lo(10.0 * (b * nn[k] - 0.25), q[k], q[6 + k]);
-    hi_lo(10.0 * (b * n[c] - 0.25), q[4], q[10]);
+    for (int k = 0; k < 4; ++k) sur_hi_lo(10.0 * (b * nn[k] - 0.25), q[k], q[6 + k]);
+    sur_hi_lo(10.0 * (b * n[c] - 0.25), q[4], q[10]);
     q[5] = __float2bfloat16_rn(1.0f);
 #pragma unroll
     for (int k = 11; k < 16; ++k) q[k] = __float2bfloat16_rn(0.0f);
@@ -547,6 +655,9 @@ static bool set_smem_attrs() {
   set((const void*)k_conv<64, 16, EPI_KICK>, conv_smem<64, 16>());
   set((const void*)k_conv<16, 64, EPI_MASK>, conv_smem<16, 64>());
   set((const void*)k_conv<64, 64, EPI_MASK>, conv_smem<64, 64>());
+  set((const void*)k_conv_halo<16, 64, EPI_RELU>, halo_smem<16, 64>());
+  set((const void*)k_conv_halo<64, 16, EPI_KICK>, halo_smem<64, 16>());
+  set((const void*)k_conv_halo<64, 16, EPI_OUT>, halo_smem<64, 16>());
   set((const void*)k_wgrad<16, 64>, wgrad_smem<16, 64>());
   set((const void*)k_wgrad<64, 64>, wgrad_smem<64, 64>());
   set((const void*)k_wgrad<64, 16>, wgrad_smem<64, 16>());
@@ -570,9 +681,14 @@ static int forward(SurrogateNet& n, const bf16* x, int B, float* y, float* pcell
                    cudaStream_t st, bool allow_tc, uint32_t* status) {
   const int P = B * n.C;
   int launches = 0;
+  // the inference path (allow_tc): halo-tiled narrow layers, tcgen05 wide
+  // ones; the training path: the per-tap kernels the backward pass mirrors
+  const bool infer = allow_tc && n.tc;
+  const int tpr = (n.N0 + TM - 1) / TM, htiles = B * n.N1 * tpr;
   ConvArgs a = cargs(n, P);
   a.x = x; a.w = n.w16 + SP_OFF_W1; a.bias = n.p32 + SP_OFF_B1; a.out = n.a1;
-  conv<16, 64, EPI_RELU>(n, a, st);
+  if (infer) k_conv_halo<16, 64, EPI_RELU><<<htiles, NT, halo_smem<16, 64>(), st>>>(a, tpr);
+  else conv<16, 64, EPI_RELU>(n, a, st);
   ++launches;
   for (int l = 0; l < 2; ++l) {
     const bf16* in = l == 0 ? n.a1 : n.a2;
@@ -598,10 +714,12 @@ static int forward(SurrogateNet& n, const bf16* x, int B, float* y, float* pcell
   a.x = n.a3; a.w = n.w16 + SP_OFF_W4; a.bias = n.p32 + SP_OFF_B4;
   if (pcell) {
     a.pcell = pcell; a.g1 = g1; a.g2 = g2; a.oscale = (float)n.oscale;
-    conv<64, 16, EPI_KICK>(n, a, st);
+    if (infer) k_conv_halo<64, 16, EPI_KICK><<<htiles, NT, halo_smem<64, 16>(), st>>>(a, tpr);
+    else conv<64, 16, EPI_KICK>(n, a, st);
   } else {
     a.out = y;
-    conv<64, 16, EPI_OUT>(n, a, st);
+    if (infer) k_conv_halo<64, 16, EPI_OUT><<<htiles, NT, halo_smem<64, 16>(), st>>>(a, tpr);
+    else conv<64, 16, EPI_OUT>(n, a, st);
   }
   return launches + 1;
 }
@@ -652,18 +770,26 @@ static void refresh_weights(SurrogateNet& n, cudaStream_t st, bool from_p32) {
 }
 
 // ------------------------------------------------ session-side launchers
+// the network input of the session's cells: already written by the nodal
+// deposit when it ran with the network attached, else packed here
+static int sur_input(Session& s, const double* nnd, const double* ncell) {
+  if (s.sur_xin_ready) return 0;
+  k_input<<<gblocks(s.C, 256, s.num_sms * 8), 256, 0, s.stream>>>(nnd, ncell, s.k.b, s.C, s.sur->xin);
+  return 1;
+}
+
 int sur_forward_kick(Session& s, const double* nnd, const double* ncell) {
   SurrogateNet& n = *s.sur;
   const double g1 = s.k.lr_coef / s.k.m / s.k.dx * s.k.dt, g2 = s.k.lr_coef / s.k.m / s.k.dy * s.k.dt;
-  k_input<<<gblocks(s.C, 256, s.num_sms * 8), 256, 0, s.stream>>>(nnd, ncell, s.k.b, s.C, n.xin);
-  return 1 + forward(n, n.xin, 1, nullptr, s.pcell, (float)g1, (float)g2, s.stream, true, s.status);
+  const int in = sur_input(s, nnd, ncell);
+  return in + forward(n, n.xin, 1, nullptr, s.pcell, (float)g1, (float)g2, s.stream, true, s.status);
 }
 
 int sur_judge(Session& s, const double* nnd, const double* ncell) {
   SurrogateNet& n = *s.sur;
   const double g1 = s.k.lr_coef / s.k.m / s.k.dx * s.k.dt, g2 = s.k.lr_coef / s.k.m / s.k.dy * s.k.dt;
-  k_input<<<gblocks(s.C, 256, s.num_sms * 8), 256, 0, s.stream>>>(nnd, ncell, s.k.b, s.C, n.xin);
-  int launches = 1 + forward(n, n.xin, 1, n.y, nullptr, 0.f, 0.f, s.stream, true, s.status);
+  int launches = sur_input(s, nnd, ncell);
+  launches += forward(n, n.xin, 1, n.y, nullptr, 0.f, 0.f, s.stream, true, s.status);
   const int Gj = gblocks(s.C, NT, RED_G);
   k_judge<<<Gj, NT, 0, s.stream>>>(n.y, (float)n.oscale, (float)g1, (float)g2, s.pcell, s.C, n.lpart);
   k_pair_reduce<<<1, 32, 0, s.stream>>>(n.lpart, Gj, s.sur_err);

@@ -57,6 +57,13 @@ struct SurrogateNet {
 };
 struct Session;
 
+// a network input value v = 10 (b n - 0.25) as the bf16 pair (hi, lo):
+// hi = bf16(v), lo = bf16(v - hi)
+__device__ __forceinline__ void sur_hi_lo(double v, __nv_bfloat16& hi, __nv_bfloat16& lo) {
+  hi = __float2bfloat16_rn((float)v);
+  lo = __float2bfloat16_rn((float)(v - (double)__bfloat162float(hi)));
+}
+
 // tcgen05 implicit-GEMM 3x3 convolution 64 -> 64 channels with bias and
 // ReLU (mcpm_surrogate_tc.cu); returns the launches
 int tc_setup();
