@@ -367,3 +367,50 @@ def test_graph_replay_matches_eager_steps(cuda_ok, maker):
         err = np.max(np.abs(ga[k] - gb[k])) / max(1.0, np.max(np.abs(gb[k])))
         assert err <= 1e-9, (k, err)
     assert a.kernel_launches - l0 >= 7 * 6
+
+
+def _ragged_box(prec):
+    """12 cells with very uneven occupancy -- an empty cell, small, warp-,
+    block- and beyond-staging-sized cells (20 to 4,000) -- Maxwellian T = 1.
+    (Cells of 1 to 3 particles are left out: there the reference's own
+    formulas divide by a zero temperature or solve a singular 4x4 system and
+    its positions become NaN, which the GPU step reports as the reference
+    would exit.)"""
+    cfg, _ = W.uneven_cells_2d(n_cells=(4, 3), precision=prec, streaming=True)
+    counts = np.array([4000, 3500, 60, 20, 0, 200, 3100, 100, 40, 2000, 800, 30])
+    rng = np.random.default_rng(21)
+    cell = np.repeat(np.arange(12), counts)
+    x1 = (cell % 4 + rng.random(cell.size)) * 1.0
+    x2 = (cell // 4 + rng.random(cell.size)) * 1.0
+    N = cell.size
+    parts = dict(x1=x1, x2=x2, U1=rng.normal(0, 1, N), U2=rng.normal(0, 1, N), U3=rng.normal(0, 1, N))
+    mcpm.derive(cfg, N)
+    cfg.max_particles = N
+    return cfg, parts
+
+
+def test_ragged_cells_fused_steps(cuda_ok):
+    """Cells from empty to 4,000 particles (past the shared staging of the
+    particle pass, which then recomputes its draws): two fused FP64 steps
+    against the oracle drawing the same Philox streams, one FP32 step within
+    its tolerance."""
+    cfg, parts = _ragged_box(mcpm.FP64)
+    s, o = _pair(cfg, parts, inject=False)
+    s.set_rng(mcpm.RNG_PHILOX)
+    o.set_rng(mcpm.RNG_PHILOX)
+    s.step(2)
+    o.step(2)
+    _close_particles(s.download(), o, 1e-10)
+    cfg32 = cfg.copy()
+    cfg32.precision = mcpm.FP32
+    s32 = mcpm.Session(cfg32)
+    s32.upload(parts["x1"], parts["x2"], parts["U1"], parts["U2"], parts["U3"])
+    o1 = Oracle(cfg, parts)
+    for x in (s32, o1):
+        x.set_rng(mcpm.RNG_PHILOX)
+        x.set_step(1)
+        x.step(1)
+    g = s32.download()
+    for k in ("U1", "U2", "U3"):
+        err = np.max(np.abs(g[k] - getattr(o1.s, k)))
+        assert err < 5e-4, (k, err)
