@@ -41,7 +41,14 @@ __global__ void __launch_bounds__(128) k_esmc(DevConsts k, double* cell, const i
   int mI = 0;
   if (mreal >= 0.0 && mreal <= mcap) mI = (int)mreal;
   else if (lane == 0) raise_status(status, MCPM_ERR_ITER_LIMIT);
+  // FP32 sessions run the candidate arithmetic in float (uniforms from the
+  // top 23 bits, the acceptance test as dummy > u om_max); FP64 sessions
+  // keep the reference's double arithmetic
+  constexpr bool F32 = sizeof(real) == 4;
   double omega = 0.0;
+  float omega_f = 0.f;
+  const float om_max_f = (float)om_max;
+  const float coef_f = (float)(4.0 * 3.14159265358979323846 * k.sigma * k.sigma * k.dt);
   const real pi = (real)3.14159265358979323846;
   const real sg = (real)k.sigma;
   if (NI > 0) {
@@ -52,11 +59,13 @@ __global__ void __launch_bounds__(128) k_esmc(DevConsts k, double* cell, const i
       int64_t si = -1, sj = -1;
       real d0 = 0, d1 = 0, d2 = 0;
       double Ymid = 0.0, nJ = 0.0;
+      float Ymid_f = 0.f, nJ_f = 0.f;
       if (kc < mI) {
         uint4 r = philox(k.seed, (uint32_t)I, (uint32_t)step, RNG_ESMC, (uint32_t)kc);
         si = (int64_t)off[I] + pick(r.x, NI);
-        real theta = (real)2.0 * pi * (real)u01d(r.y);
-        real cph = (real)2.0 * (real)u01d(r.z) - (real)1.0;
+        const real uy = F32 ? (real)u01f(r.y) : (real)u01d(r.y), uz = F32 ? (real)u01f(r.z) : (real)u01d(r.z);
+        real theta = (real)2.0 * pi * uy;
+        real cph = (real)2.0 * uz - (real)1.0;
         real sph = r_sqrt((real)1.0 - cph * cph);
         real sn, cs;
         r_sincos(theta, &sn, &cs);
@@ -76,6 +85,7 @@ __global__ void __launch_bounds__(128) k_esmc(DevConsts k, double* cell, const i
               m1 = m1 < 0 ? 0 : (m1 > k.N1 - 1 ? k.N1 - 1 : m1);
               Ymid = cell[(size_t)CFI_Y * C + m1 * k.N0 + m0];
               nJ = cell[(size_t)MCPM_CF_N * C + J];
+              if constexpr (F32) { Ymid_f = (float)Ymid; nJ_f = (float)nJ; }
               valid = true;
             }
           }
@@ -94,10 +104,19 @@ __global__ void __launch_bounds__(128) k_esmc(DevConsts k, double* cell, const i
       if (lane < take && valid) {
         real g0 = p.U1[si] - p.U1[sj], g1 = p.U2[si] - p.U2[sj], g2 = p.U3[si] - p.U3[sj];
         real gd = g0 * d0 + g1 * d1 + g2 * d2;
-        double dummy = 4.0 * 3.14159265358979323846 * k.sigma * k.sigma * (double)gd * Ymid * nJ * k.dt;
-        if (dummy - omega > 0.0) omega = dummy;
-        double u = u01d(philox(k.seed, (uint32_t)I, (uint32_t)step, RNG_ESMC_ACC, (uint32_t)kc).x);
-        if (dummy / om_max > u) {
+        bool accept;
+        if constexpr (F32) {
+          const float dummy = coef_f * (float)gd * Ymid_f * nJ_f;
+          omega_f = fmaxf(omega_f, dummy);
+          const float u = u01f(philox(k.seed, (uint32_t)I, (uint32_t)step, RNG_ESMC_ACC, (uint32_t)kc).x);
+          accept = dummy > u * om_max_f;
+        } else {
+          double dummy = 4.0 * 3.14159265358979323846 * k.sigma * k.sigma * (double)gd * Ymid * nJ * k.dt;
+          if (dummy - omega > 0.0) omega = dummy;
+          double u = u01d(philox(k.seed, (uint32_t)I, (uint32_t)step, RNG_ESMC_ACC, (uint32_t)kc).x);
+          accept = dummy / om_max > u;
+        }
+        if (accept) {
           p.U1[si] = p.U1[si] - gd * d0; p.U2[si] = p.U2[si] - gd * d1; p.U3[si] = p.U3[si] - gd * d2;
           p.U1[sj] = p.U1[sj] + gd * d0; p.U2[sj] = p.U2[sj] + gd * d1; p.U3[sj] = p.U3[sj] + gd * d2;
         }
@@ -106,8 +125,14 @@ __global__ void __launch_bounds__(128) k_esmc(DevConsts k, double* cell, const i
       base += take;
     }
   }
+  if constexpr (F32) {
 #pragma unroll
-  for (int m = 16; m >= 1; m >>= 1) omega = fmax(omega, __shfl_xor_sync(FULL, omega, m));
+    for (int m = 16; m >= 1; m >>= 1) omega_f = fmaxf(omega_f, __shfl_xor_sync(FULL, omega_f, m));
+    omega = (double)omega_f;
+  } else {
+#pragma unroll
+    for (int m = 16; m >= 1; m >>= 1) omega = fmax(omega, __shfl_xor_sync(FULL, omega, m));
+  }
   if (lane == 0) cell[(size_t)MCPM_CF_OMEGA_MAX * C + I] = omega > om_max ? omega : om_max;
 }
 
