@@ -332,12 +332,15 @@ __device__ void moments_cell(int c, const MomArgs<real>& a, Acc<real>* red) {
     // L1): half the accumulators live at a time, so more warps fit per SM.
     // Within a group: compensated accumulation of partials -- the terms of
     // up to four of a lane's particles are summed in float, then the partial
-    // enters the compensated sum.
+    // enters the lane's compensated sum.
     auto group = [&](auto J0c, auto Kc) {
       constexpr int J0 = decltype(J0c)::value, K = decltype(Kc)::value;
-      Acc<real> g[K];
+      // Kahan's compensated sum per lane (4 additions per term; the
+      // library is built without contraction, so the compensation holds),
+      // merged across lanes as (sum, -compensation) pairs
+      float ks[K], kc[K];
 #pragma unroll
-      for (int j = 0; j < K; ++j) g[j].zero();
+      for (int j = 0; j < K; ++j) { ks[j] = 0.f; kc[j] = 0.f; }
       for (int i = t; i < n; i += 4 * TILE) {
         real ps[K];
         {
@@ -355,8 +358,15 @@ __device__ void moments_cell(int c, const MomArgs<real>& a, Acc<real>* red) {
           for (int j = 0; j < K; ++j) ps[j] += v[J0 + j];
         }
 #pragma unroll
-        for (int j = 0; j < K; ++j) g[j].add(ps[j]);
+        for (int j = 0; j < K; ++j) {
+          const float y = ps[j] - kc[j], tt = ks[j] + y;
+          kc[j] = (tt - ks[j]) - y;
+          ks[j] = tt;
+        }
       }
+      Acc<real> g[K];
+#pragma unroll
+      for (int j = 0; j < K; ++j) { g[j].c.hi = ks[j]; g[j].c.lo = -kc[j]; }
       tile_reduce_write<real, K, TILE>(g, red, [&](int f, const Acc<real>& tot) {
         a.cell[(size_t)(CFI_RAW + J0 + f) * C + c] = tot.get();
       });
