@@ -127,11 +127,23 @@ __device__ __forceinline__ void block_scan3(int& v0, int& v1, int& v2, int& t0, 
 }
 
 // pass 1: per-block totals (count, small cells, big cells, max count)
-__global__ void __launch_bounds__(SCAN_T) k_scan_blocks(const int32_t* cnt_next, int32_t* blk, int C, int wcap) {
+// particles binned into cell c for the next layout: the counter, or -- when
+// the particle pass counted quadrants -- the sum of the cell's four
+// quadrant counts (then the pass keeps no separate counter)
+__device__ __forceinline__ int next_count(const int32_t* cnt_next, const int32_t* qc, int c) {
+  if (qc) {
+    const int4 q = *reinterpret_cast<const int4*>(qc + 4 * (size_t)c);
+    return q.x + q.y + q.z + q.w;
+  }
+  return cnt_next[c];
+}
+
+__global__ void __launch_bounds__(SCAN_T) k_scan_blocks(const int32_t* cnt_next, const int32_t* qc, int32_t* blk,
+                                                        int C, int wcap) {
   __shared__ int sh[3][32];
   __shared__ int shm[32];
   const int c = blockIdx.x * SCAN_T + threadIdx.x;
-  const int v = c < C ? cnt_next[c] : 0;
+  const int v = c < C ? next_count(cnt_next, qc, c) : 0;
   int v0 = v, v1 = (c < C && v <= wcap) ? 1 : 0, v2 = (c < C && v > wcap) ? 1 : 0, t0, t1, t2;
   int mx = v;
 #pragma unroll
@@ -177,12 +189,12 @@ __global__ void __launch_bounds__(SCAN_T) k_scan_totals(int32_t* blk, int nblk, 
 }
 
 // pass 3: block-local scan plus the block base; writes the layout
-__global__ void __launch_bounds__(SCAN_T) k_scan_write(int32_t* cnt_next, int32_t* cnt, int32_t* off,
-                                                       int32_t* cursor, int32_t* list_small, int32_t* list_big,
-                                                       const int32_t* blk, int C, int wcap) {
+__global__ void __launch_bounds__(SCAN_T) k_scan_write(int32_t* cnt_next, const int32_t* qc, int32_t* cnt,
+                                                       int32_t* off, int32_t* cursor, int32_t* list_small,
+                                                       int32_t* list_big, const int32_t* blk, int C, int wcap) {
   __shared__ int sh[3][32];
   const int c = blockIdx.x * SCAN_T + threadIdx.x;
-  const int v = c < C ? cnt_next[c] : 0;
+  const int v = c < C ? next_count(cnt_next, qc, c) : 0;
   const bool small = c < C && v <= wcap, big = c < C && v > wcap;
   int v0 = v, v1 = small ? 1 : 0, v2 = big ? 1 : 0, t0, t1, t2;
   block_scan3(v0, v1, v2, t0, t1, t2, sh);
@@ -1616,8 +1628,9 @@ __device__ void update_cell_f32(int c, const UpdArgs<float>& a, int step, float*
       }
     }
     if (st & ST_KEY) {
-      count_key(a.cnt_next, key, act);
+      // with quadrant counting the cell's count is their sum (read by the scan)
       if (a.qc) count_key(a.qc, qkey, act);
+      else count_key(a.cnt_next, key, act);
     }
   }
   raise_status(a.status, bad);
@@ -1699,9 +1712,11 @@ int launch_bin(Session& s, int bin_step) { return s.prec == MCPM_FP32 ? bin_impl
 
 int launch_scan(Session& s) {
   const int nblk = (s.C + SCAN_T - 1) / SCAN_T;
-  k_scan_blocks<<<nblk, SCAN_T, 0, s.stream>>>(s.cnt_next, s.scan_blk, s.C, s.tune.wcap);
+  // the particle pass that binned the current keys counted quadrants only
+  const int32_t* qc = s.qc_ready ? lr2d_quad_next(s) : nullptr;
+  k_scan_blocks<<<nblk, SCAN_T, 0, s.stream>>>(s.cnt_next, qc, s.scan_blk, s.C, s.tune.wcap);
   k_scan_totals<<<1, SCAN_T, 0, s.stream>>>(s.scan_blk, nblk, s.wl, s.work);
-  k_scan_write<<<nblk, SCAN_T, 0, s.stream>>>(s.cnt_next, s.cnt, s.off, s.cursor, s.list_small, s.list_big,
+  k_scan_write<<<nblk, SCAN_T, 0, s.stream>>>(s.cnt_next, qc, s.cnt, s.off, s.cursor, s.list_small, s.list_big,
                                                s.scan_blk, s.C, s.tune.wcap);
   return 3;
 }
