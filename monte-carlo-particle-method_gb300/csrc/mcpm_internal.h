@@ -112,8 +112,24 @@ struct Session {
   int32_t* key = nullptr;       // cell of each slot, current layout
   int32_t* cnt = nullptr;       // [C] particles per cell, current layout
   int32_t* cnt_next = nullptr;  // [C] counts accumulated for the next layout
-  int32_t* off = nullptr;       // [C+1]
+  int32_t* off = nullptr;       // [C+1] first slot of each cell, current layout
   int32_t* cursor = nullptr;    // [C]
+  // Slotted layouts (FP32 fused steps): the particle pass writes each
+  // particle straight into its new cell's region of the other buffer, a
+  // region of capacity doff[c+1] - doff[c] with slack over the cell's count,
+  // slots handed out by dcur; a region that fills up sends the rest to the
+  // overflow arrays, which the next scan's repair pass folds back
+  int64_t slots = 0;            // slots per particle array (>= cap)
+  int32_t* doff = nullptr;      // [C+1] region bases of the destination layout
+  int32_t* noff = nullptr;      // [C+1] packed offsets of the totals (repair / compaction)
+  int32_t* dcur = nullptr;      // [C] slots taken per destination region (= particles binned there)
+  PBuf ovf{};                   // overflow particles (cap each)
+  int32_t* ovf_key = nullptr;   // [cap] their cells
+  int32_t* ovf_n = nullptr;     // [2] overflow counts, alternating between steps
+  int ovf_par = 0;              // the overflow counter the next slotted pass uses
+  bool use_slotted = false;     // the session writes slotted layouts (FP32)
+  bool slotted = false;         // P[cur] holds a slotted layout (off = doff of that pass,
+                                // counts in dcur): the next scan finalises it
   int32_t* list_small = nullptr;
   int32_t* list_big = nullptr;
   int32_t* wl = nullptr;        // [WL_COUNT]
@@ -183,9 +199,18 @@ struct Session {
 int launch_bin(Session& s, int bin_step);
 int launch_scan(Session& s);
 int launch_scatter(Session& s);
+// slotted layouts: the scan that finalises one (counts from dcur, packed
+// offsets, the next destination layout), the overflow repair (two launches
+// that return at once when nothing overflowed; force: compact the layout
+// into the other buffer instead, host-side)
+int launch_scan_slotted(Session& s);
+int launch_repair(Session& s);
+int launch_compact(Session& s);
 int launch_moments(Session& s);
 int launch_solve(Session& s, int with_alpha);
-int launch_update(Session& s, uint32_t stages, int bc_call_base);
+// slotted: write the new state into the slotted layout of the other buffer
+// (FP32 passes that bin the new positions)
+int launch_update(Session& s, uint32_t stages, int bc_call_base, bool slotted = false);
 int launch_esmc(Session& s);
 int launch_long_range(Session& s);
 int launch_init_omega(Session& s);

@@ -17,6 +17,7 @@
 #include <cfloat>
 
 #include <type_traits>
+#include <utility>
 
 #include "mcpm_device.cuh"
 
@@ -97,36 +98,58 @@ __global__ void k_bin(PT<real> p, int64_t n, DevConsts k, int step, int32_t* key
 
 // ================================================ scan + work lists
 // Counts of the new layout -> cnt, exclusive offsets, the two work lists
-// (cells with <= wcap particles / more), max count; resets the accumulation
-// counters and cursors for the next step.  Three passes over blocks of 1024
-// cells: block totals, scan of the totals, block-local scan + writes.
+// (cells with <= wcap particles / more), max count, and -- for sessions
+// with slotted layouts -- the region bases of the next destination layout;
+// resets the accumulation counters and cursors for the next step.  Three
+// passes over blocks of 1024 cells: block totals, scan of the totals,
+// block-local scan + writes.
 constexpr int SCAN_T = 1024;
+constexpr int SCAN_Q = 4;       // scanned quantities: count, small, big, slots
+constexpr int SCAN_STRIDE = 8;  // ints per block in the totals array
 
-__device__ __forceinline__ void block_scan3(int& v0, int& v1, int& v2, int& t0, int& t1, int& t2, int (*sh)[32]) {
-  // inclusive scan of three ints over a 1024-thread block; t* = block totals
+// region capacity of a cell of v particles in a slotted layout: a quarter
+// (at least 16) of slack, rounded to whole 32-byte sectors of floats
+__device__ __forceinline__ int slot_cap(int v) { return (v + max(16, v >> 2) + 7) & ~7; }
+
+__device__ __forceinline__ void block_scan4(int (&v)[SCAN_Q], int (&t)[SCAN_Q], int (*sh)[32]) {
+  // inclusive scan of four ints over a 1024-thread block; t = block totals
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
   for (int d = 1; d < 32; d <<= 1) {
-    int a0 = __shfl_up_sync(FULL, v0, d), a1 = __shfl_up_sync(FULL, v1, d), a2 = __shfl_up_sync(FULL, v2, d);
-    if (lane >= d) { v0 += a0; v1 += a1; v2 += a2; }
+#pragma unroll
+    for (int q = 0; q < SCAN_Q; ++q) {
+      const int a = __shfl_up_sync(FULL, v[q], d);
+      if (lane >= d) v[q] += a;
+    }
   }
-  if (lane == 31) { sh[0][warp] = v0; sh[1][warp] = v1; sh[2][warp] = v2; }
+  if (lane == 31) {
+#pragma unroll
+    for (int q = 0; q < SCAN_Q; ++q) sh[q][warp] = v[q];
+  }
   __syncthreads();
   if (warp == 0) {
-    int w0 = sh[0][lane], w1 = sh[1][lane], w2 = sh[2][lane];
+    int w[SCAN_Q];
+#pragma unroll
+    for (int q = 0; q < SCAN_Q; ++q) w[q] = sh[q][lane];
 #pragma unroll
     for (int d = 1; d < 32; d <<= 1) {
-      int a0 = __shfl_up_sync(FULL, w0, d), a1 = __shfl_up_sync(FULL, w1, d), a2 = __shfl_up_sync(FULL, w2, d);
-      if (lane >= d) { w0 += a0; w1 += a1; w2 += a2; }
+#pragma unroll
+      for (int q = 0; q < SCAN_Q; ++q) {
+        const int a = __shfl_up_sync(FULL, w[q], d);
+        if (lane >= d) w[q] += a;
+      }
     }
-    sh[0][lane] = w0; sh[1][lane] = w1; sh[2][lane] = w2;
+#pragma unroll
+    for (int q = 0; q < SCAN_Q; ++q) sh[q][lane] = w[q];
   }
   __syncthreads();
-  if (warp) { v0 += sh[0][warp - 1]; v1 += sh[1][warp - 1]; v2 += sh[2][warp - 1]; }
-  t0 = sh[0][31]; t1 = sh[1][31]; t2 = sh[2][31];
+#pragma unroll
+  for (int q = 0; q < SCAN_Q; ++q) {
+    if (warp) v[q] += sh[q][warp - 1];
+    t[q] = sh[q][31];
+  }
 }
 
-// pass 1: per-block totals (count, small cells, big cells, max count)
 // particles binned into cell c for the next layout: the counter, or -- when
 // the particle pass counted quadrants -- the sum of the cell's four
 // quadrant counts (then the pass keeps no separate counter)
@@ -138,43 +161,62 @@ __device__ __forceinline__ int next_count(const int32_t* cnt_next, const int32_t
   return cnt_next[c];
 }
 
+__device__ __forceinline__ void scan_values(int (&v)[SCAN_Q], int c, int C, int count, int wcap) {
+  v[0] = c < C ? count : 0;
+  v[1] = (c < C && count <= wcap) ? 1 : 0;
+  v[2] = (c < C && count > wcap) ? 1 : 0;
+  v[3] = c < C ? slot_cap(count) : 0;
+}
+
+// pass 1: per-block totals (count, small cells, big cells, slots, max count)
 __global__ void __launch_bounds__(SCAN_T) k_scan_blocks(const int32_t* cnt_next, const int32_t* qc, int32_t* blk,
                                                         int C, int wcap) {
-  __shared__ int sh[3][32];
+  __shared__ int sh[SCAN_Q][32];
   __shared__ int shm[32];
   const int c = blockIdx.x * SCAN_T + threadIdx.x;
-  const int v = c < C ? next_count(cnt_next, qc, c) : 0;
-  int v0 = v, v1 = (c < C && v <= wcap) ? 1 : 0, v2 = (c < C && v > wcap) ? 1 : 0, t0, t1, t2;
-  int mx = v;
+  const int count = c < C ? next_count(cnt_next, qc, c) : 0;
+  int v[SCAN_Q], t[SCAN_Q];
+  scan_values(v, c, C, count, wcap);
+  int mx = count;
 #pragma unroll
   for (int d = 16; d >= 1; d >>= 1) mx = max(mx, __shfl_xor_sync(FULL, mx, d));
   if ((threadIdx.x & 31) == 0) shm[threadIdx.x >> 5] = mx;
-  block_scan3(v0, v1, v2, t0, t1, t2, sh);
+  block_scan4(v, t, sh);
   if (threadIdx.x == 0) {
     int m = shm[0];
     for (int w = 1; w < 32; ++w) m = max(m, shm[w]);
-    blk[4 * blockIdx.x + 0] = t0; blk[4 * blockIdx.x + 1] = t1; blk[4 * blockIdx.x + 2] = t2;
-    blk[4 * blockIdx.x + 3] = m;
+#pragma unroll
+    for (int q = 0; q < SCAN_Q; ++q) blk[SCAN_STRIDE * blockIdx.x + q] = t[q];
+    blk[SCAN_STRIDE * blockIdx.x + SCAN_Q] = m;
   }
 }
 
-// pass 2: exclusive scan of the block totals (one block), list lengths
-__global__ void __launch_bounds__(SCAN_T) k_scan_totals(int32_t* blk, int nblk, int32_t* wl, int32_t* work) {
-  __shared__ int sh[3][32];
-  int carry0 = 0, carry1 = 0, carry2 = 0, mx = 0;
+// pass 2: exclusive scan of the block totals (one block), list lengths; the
+// overflow counter of the next slotted pass starts from zero
+__global__ void __launch_bounds__(SCAN_T) k_scan_totals(int32_t* blk, int nblk, int32_t* wl, int32_t* work,
+                                                        int32_t* ovf_clear) {
+  __shared__ int sh[SCAN_Q][32];
+  int carry[SCAN_Q] = {0, 0, 0, 0}, mx = 0;
   for (int base = 0; base < nblk; base += SCAN_T) {
     const int b = base + threadIdx.x;
-    int v0 = 0, v1 = 0, v2 = 0, m = 0, t0, t1, t2;
-    if (b < nblk) { v0 = blk[4 * b]; v1 = blk[4 * b + 1]; v2 = blk[4 * b + 2]; m = blk[4 * b + 3]; }
-    const int e0 = v0, e1 = v1, e2 = v2;
-    block_scan3(v0, v1, v2, t0, t1, t2, sh);
+    int v[SCAN_Q] = {0, 0, 0, 0}, e[SCAN_Q], t[SCAN_Q], m = 0;
+    if (b < nblk) {
+#pragma unroll
+      for (int q = 0; q < SCAN_Q; ++q) v[q] = blk[SCAN_STRIDE * b + q];
+      m = blk[SCAN_STRIDE * b + SCAN_Q];
+    }
+#pragma unroll
+    for (int q = 0; q < SCAN_Q; ++q) e[q] = v[q];
+    block_scan4(v, t, sh);
     if (b < nblk) {  // exclusive bases in place of the totals
-      blk[4 * b] = carry0 + v0 - e0; blk[4 * b + 1] = carry1 + v1 - e1; blk[4 * b + 2] = carry2 + v2 - e2;
+#pragma unroll
+      for (int q = 0; q < SCAN_Q; ++q) blk[SCAN_STRIDE * b + q] = carry[q] + v[q] - e[q];
     }
 #pragma unroll
     for (int d = 16; d >= 1; d >>= 1) m = max(m, __shfl_xor_sync(FULL, m, d));
     mx = max(mx, m);
-    carry0 += t0; carry1 += t1; carry2 += t2;
+#pragma unroll
+    for (int q = 0; q < SCAN_Q; ++q) carry[q] += t[q];
     __syncthreads();
   }
   __shared__ int shm[32];
@@ -183,30 +225,49 @@ __global__ void __launch_bounds__(SCAN_T) k_scan_totals(int32_t* blk, int nblk, 
   if (threadIdx.x == 0) {
     int m = shm[0];
     for (int w = 1; w < 32; ++w) m = max(m, shm[w]);
-    wl[WL_N] = carry0; wl[WL_NSMALL] = carry1; wl[WL_NBIG] = carry2; wl[WL_MAXCNT] = m;
+    wl[WL_N] = carry[0]; wl[WL_NSMALL] = carry[1]; wl[WL_NBIG] = carry[2]; wl[WL_MAXCNT] = m;
+    if (ovf_clear) *ovf_clear = 0;
   }
   if (threadIdx.x < WK_COUNT) work[threadIdx.x] = 0;
 }
 
-// pass 3: block-local scan plus the block base; writes the layout
-__global__ void __launch_bounds__(SCAN_T) k_scan_write(int32_t* cnt_next, const int32_t* qc, int32_t* cnt,
-                                                       int32_t* off, int32_t* cursor, int32_t* list_small,
-                                                       int32_t* list_big, const int32_t* blk, int C, int wcap) {
-  __shared__ int sh[3][32];
+// pass 3: block-local scan plus the block base; writes the layout.  off:
+// packed offsets of the counts (null: the layout keeps its region bases);
+// noff: the same packed offsets for the overflow repair; doff: region bases
+// of the next slotted layout
+struct ScanOut {
+  int32_t *cnt_next, *cursor, *dcur;  // reset (dcur: may be null)
+  const int32_t *qc, *src;            // counts: src (cnt_next or dcur), or qc sums
+  int32_t *cnt, *off, *noff, *doff, *list_small, *list_big;
+  const int32_t* blk;
+  int C, wcap;
+};
+__global__ void __launch_bounds__(SCAN_T) k_scan_write(ScanOut a) {
+  __shared__ int sh[SCAN_Q][32];
   const int c = blockIdx.x * SCAN_T + threadIdx.x;
-  const int v = c < C ? next_count(cnt_next, qc, c) : 0;
-  const bool small = c < C && v <= wcap, big = c < C && v > wcap;
-  int v0 = v, v1 = small ? 1 : 0, v2 = big ? 1 : 0, t0, t1, t2;
-  block_scan3(v0, v1, v2, t0, t1, t2, sh);
-  if (c < C) {
-    const int o = blk[4 * blockIdx.x] + v0 - v;
-    cnt[c] = v;
-    off[c] = o;
-    if (small) list_small[blk[4 * blockIdx.x + 1] + v1 - 1] = c;
-    if (big) list_big[blk[4 * blockIdx.x + 2] + v2 - 1] = c;
-    cnt_next[c] = 0;
-    cursor[c] = 0;
-    if (c == C - 1) off[C] = o + v;
+  const int count = c < a.C ? next_count(a.src, a.qc, c) : 0;
+  int v[SCAN_Q], t[SCAN_Q];
+  scan_values(v, c, a.C, count, a.wcap);
+  const bool small = v[1], big = v[2];
+  const int cap = v[3];
+  block_scan4(v, t, sh);
+  if (c < a.C) {
+    const int32_t* bb = a.blk + SCAN_STRIDE * blockIdx.x;
+    const int o = bb[0] + v[0] - count, po = bb[3] + v[3] - cap;
+    a.cnt[c] = count;
+    if (a.off) a.off[c] = o;
+    if (a.noff) a.noff[c] = o;
+    if (a.doff) a.doff[c] = po;
+    if (small) a.list_small[bb[1] + v[1] - 1] = c;
+    if (big) a.list_big[bb[2] + v[2] - 1] = c;
+    a.cnt_next[c] = 0;
+    a.cursor[c] = 0;
+    if (a.dcur) a.dcur[c] = 0;
+    if (c == a.C - 1) {
+      if (a.off) a.off[a.C] = o + count;
+      if (a.noff) a.noff[a.C] = o + count;
+      if (a.doff) a.doff[a.C] = po + cap;
+    }
   }
 }
 
@@ -247,6 +308,53 @@ __global__ void k_scatter(PT<real> src, PT<real> dst, const int32_t* key, const 
       if (src.x2o) dst.x2o[d] = x2o;
     }
   }
+}
+
+// ==================================================== slotted layouts
+template <typename real>
+__device__ __forceinline__ void copy_particle(const PT<real>& src, int64_t i, const PT<real>& dst, int64_t d) {
+  if (src.x1) dst.x1[d] = src.x1[i];
+  dst.x2[d] = src.x2[i];
+  dst.U1[d] = src.U1[i];
+  dst.U2[d] = src.U2[i];
+  dst.U3[d] = src.U3[i];
+  dst.pid[d] = src.pid[i];
+  if (src.x1o) dst.x1o[d] = src.x1o[i];
+  if (src.x2o) dst.x2o[d] = src.x2o[i];
+}
+
+// Packs a slotted layout into dst at the packed offsets noff: each cell's
+// first min(total, capacity) particles from its region of src (bases off),
+// the rest from the overflow arrays.  Without force it returns at once when
+// nothing overflowed (the common case: the layout stays slotted).
+template <typename real>
+__global__ void k_repair_move(PT<real> src, PT<real> dst, PT<real> ovf, const int32_t* ovf_key,
+                              const int32_t* ovf_n, const int32_t* off, const int32_t* cnt, const int32_t* noff,
+                              int32_t* cursor, int C, int force) {
+  const int n_ovf = *ovf_n;
+  if (!force && n_ovf == 0) return;
+  const int lane = threadIdx.x & 31;
+  const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x, nt = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t c = tid >> 5; c < C; c += nt >> 5) {
+    const int s0 = off[c], m = min(cnt[c], off[c + 1] - s0), d0 = noff[c];
+    for (int i = lane; i < m; i += 32) copy_particle(src, (int64_t)s0 + i, dst, (int64_t)d0 + i);
+  }
+  for (int64_t e = tid; e < n_ovf; e += nt) {
+    const int c = ovf_key[e];
+    const int d = noff[c] + (off[c + 1] - off[c]) + atomicAdd(&cursor[c], 1);
+    copy_particle(ovf, e, dst, (int64_t)d);
+  }
+}
+
+// After an overflow: the packed particles back into the buffer the layout
+// belongs to, and the packed offsets in place of the region bases.
+template <typename real>
+__global__ void k_repair_back(PT<real> packed, PT<real> dst, const int32_t* ovf_n, const int32_t* noff, int32_t* off,
+                              int C, int64_t n) {
+  if (*ovf_n == 0) return;
+  const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x, nt = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = tid; i < n; i += nt) copy_particle(packed, i, dst, i);
+  for (int64_t c = tid; c <= C; c += nt) off[c] = noff[c];
 }
 
 // ================================================ cell access helpers
@@ -1037,6 +1145,15 @@ template <typename real> struct UpdArgs {
   // cell-centre thresholds per column / row
   int32_t* qc;
   const float *qtx, *qty;
+  // slotted layouts (FP32 fused steps): the destination buffer, the region
+  // bases of its layout and their slot counters, the overflow arrays and
+  // their counter
+  PT<real> d;
+  const int32_t* doff;
+  int32_t* dcur;
+  PT<real> ovf;
+  int32_t* ovf_key;
+  int32_t* ovf_n;
 };
 
 template <typename real>
@@ -1425,7 +1542,7 @@ __device__ __forceinline__ void tile_sum_f32(float (&v)[K], float* red) {
 // pairwise (tile_sum_f32; the compensated sums stay in the moment pass),
 // fused multiply-adds throughout, and the packed per-cell record read into
 // registers where each pass needs it.
-template <int TILE, uint32_t CST, int PB>
+template <int TILE, uint32_t CST, int PB, bool SL>
 __device__ void update_cell_f32(int c, const UpdArgs<float>& a, int step, float* xs, int xcap, float* red,
                                 float* R) {
   const int t = (TILE == 32) ? (threadIdx.x & 31) : threadIdx.x;
@@ -1541,15 +1658,15 @@ __device__ void update_cell_f32(int c, const UpdArgs<float>& a, int step, float*
   for (int r = 0; r < iters; ++r) {
     const int i = r * TILE + t;
     const bool act = i < n;
-    int key = 0, qkey = 0;
+    int key = 0, quad = 0, pid = 0;
+    PState<float> s;
     if (act) {
       const int64_t p = s0 + i;
-      PState<float> s;
       s.x1 = P.x1 ? P.x1[p] : 0.f;
       s.x2 = P.x2[p];
       s.x1o = P.x1o ? P.x1o[p] : 0.f;
       s.x2o = P.x2o ? P.x2o[p] : 0.f;
-      const int pid = P.pid[p];
+      pid = P.pid[p];
       if (fp) {
         if (n > 1) {
           float m1, m2, m3;
@@ -1612,31 +1729,79 @@ __device__ void update_cell_f32(int c, const UpdArgs<float>& a, int step, float*
       }
       if (st & ST_BC2) bc(1);
       if (st & ST_BC3) bc(2);
-      P.U1[p] = s.u1; P.U2[p] = s.u2; P.U3[p] = s.u3;
-      if (P.x1) P.x1[p] = s.x1;
-      P.x2[p] = s.x2;
-      if (P.x1o) P.x1o[p] = s.x1o;
-      if (P.x2o) P.x2o[p] = s.x2o;
-      if (st & ST_KEY) {
+      if constexpr (!SL) {
+        P.U1[p] = s.u1; P.U2[p] = s.u2; P.U3[p] = s.u3;
+        if (P.x1) P.x1[p] = s.x1;
+        P.x2[p] = s.x2;
+        if (P.x1o) P.x1o[p] = s.x1o;
+        if (P.x2o) P.x2o[p] = s.x2o;
+      }
+      if (SL || (st & ST_KEY)) {
         int jn, kn;
         key = bin_one<float>(s.x1, s.x2, pid, step + 1, k, kc, bad, &jn, &kn);
-        a.key_out[p] = key;
+        if constexpr (!SL) a.key_out[p] = key;
         // its quadrant in the new cell, as the nodal deposit counts it
         // (left of / below the centre: the threshold is the smallest float
         // at or above the centre)
-        if (a.qc) qkey = 4 * key + (s.x1 < a.qtx[jn] ? 0 : 1) + (s.x2 < a.qty[kn] ? 0 : 2);
+        if (a.qc) quad = (s.x1 < a.qtx[jn] ? 0 : 1) + (s.x2 < a.qty[kn] ? 0 : 2);
       }
     }
-    if (st & ST_KEY) {
+    if constexpr (SL) {
+      // the particle's slot in its new cell's region: one atomic per cell
+      // and warp (the lanes bound for the same cell share it), the lane's
+      // rank among them on top
+      const int lane = threadIdx.x & 31;
+      const unsigned am = __ballot_sync(FULL, act);
+      unsigned peers = 0;
+      int leader = 0, slot = 0;
+      if (act) {
+        peers = __match_any_sync(am, key);
+        leader = __ffs(peers) - 1;
+        int base = 0;
+        if (lane == leader) base = atomicAdd(&a.dcur[key], __popc(peers));
+        base = __shfl_sync(peers, base, leader);
+        slot = base + __popc(peers & ((1u << lane) - 1u));
+      }
+      if (a.qc) {
+        // quadrant counts of the same groups, split by ballots
+        const unsigned q1 = __ballot_sync(FULL, act && quad == 1), q2 = __ballot_sync(FULL, act && quad == 2),
+                       q3 = __ballot_sync(FULL, act && quad == 3);
+        if (act && lane == leader) {
+          const int n1 = __popc(peers & q1), n2 = __popc(peers & q2), n3 = __popc(peers & q3);
+          const int n0 = __popc(peers) - n1 - n2 - n3;
+          int32_t* qk = a.qc + 4 * (size_t)key;
+          if (n0) atomicAdd(qk, n0);
+          if (n1) atomicAdd(qk + 1, n1);
+          if (n2) atomicAdd(qk + 2, n2);
+          if (n3) atomicAdd(qk + 3, n3);
+        }
+      }
+      if (act) {
+        const int r0 = a.doff[key], capc = a.doff[key + 1] - r0;
+        const PT<float>* D = &a.d;
+        int64_t d = (int64_t)r0 + slot;
+        if (slot >= capc) {  // the region is full: to the overflow arrays
+          d = atomicAdd(a.ovf_n, 1);
+          a.ovf_key[d] = key;
+          D = &a.ovf;
+        }
+        D->U1[d] = s.u1; D->U2[d] = s.u2; D->U3[d] = s.u3;
+        if (D->x1) D->x1[d] = s.x1;
+        D->x2[d] = s.x2;
+        D->pid[d] = pid;
+        if (D->x1o) D->x1o[d] = s.x1o;
+        if (D->x2o) D->x2o[d] = s.x2o;
+      }
+    } else if (st & ST_KEY) {
       // with quadrant counting the cell's count is their sum (read by the scan)
-      if (a.qc) count_key(a.qc, qkey, act);
+      if (a.qc) count_key(a.qc, 4 * key + quad, act);
       else count_key(a.cnt_next, key, act);
     }
   }
   raise_status(a.status, bad);
 }
 
-template <typename real, uint32_t CST, int PB = 0>
+template <typename real, uint32_t CST, int PB = 0, bool SL = false>
 __global__ void __launch_bounds__(256, sizeof(real) == 4 ? (CST ? MCPM_UPD_MINB : 3) : 1) k_update(UpdArgs<real> a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ Acc<real> red[8 * 8];
@@ -1648,10 +1813,10 @@ __global__ void __launch_bounds__(256, sizeof(real) == 4 ? (CST ? MCPM_UPD_MINB 
     __shared__ __align__(16) float recs[8][PF_STRIDE];
     schedule_cells(
         a.list_big, a.list_small, a.wl, a.work, WK_UPD_BIG, WK_UPD_SMALL,
-        [&](int c) { update_cell_f32<256, CST, PB>(c, a, step, xs, a.bcap, rf, recs[0]); },
+        [&](int c) { update_cell_f32<256, CST, PB, SL>(c, a, step, xs, a.bcap, rf, recs[0]); },
         [&](int c) {
-          update_cell_f32<32, CST, PB>(c, a, step, xs + (size_t)warp * 3 * (a.bcap / 8), a.bcap / 8, rf,
-                                       recs[warp]);
+          update_cell_f32<32, CST, PB, SL>(c, a, step, xs + (size_t)warp * 3 * (a.bcap / 8), a.bcap / 8, rf,
+                                           recs[warp]);
         });
   } else {
     schedule_cells(
@@ -1710,15 +1875,54 @@ template <typename real> static int bin_impl(Session& s, int bin_step) {
 }
 int launch_bin(Session& s, int bin_step) { return s.prec == MCPM_FP32 ? bin_impl<float>(s, bin_step) : bin_impl<double>(s, bin_step); }
 
-int launch_scan(Session& s) {
+static void scan_launch(Session& s, const int32_t* src, const int32_t* qc, int32_t* off, int32_t* noff) {
   const int nblk = (s.C + SCAN_T - 1) / SCAN_T;
+  k_scan_blocks<<<nblk, SCAN_T, 0, s.stream>>>(src, qc, s.scan_blk, s.C, s.tune.wcap);
+  k_scan_totals<<<1, SCAN_T, 0, s.stream>>>(s.scan_blk, nblk, s.wl, s.work,
+                                            s.use_slotted ? s.ovf_n + s.ovf_par : nullptr);
+  ScanOut o;
+  o.cnt_next = s.cnt_next; o.cursor = s.cursor; o.dcur = s.dcur;
+  o.qc = qc; o.src = src;
+  o.cnt = s.cnt; o.off = off; o.noff = noff; o.doff = s.use_slotted ? s.doff : nullptr;
+  o.list_small = s.list_small; o.list_big = s.list_big;
+  o.blk = s.scan_blk; o.C = s.C; o.wcap = s.tune.wcap;
+  k_scan_write<<<nblk, SCAN_T, 0, s.stream>>>(o);
+}
+
+int launch_scan(Session& s) {
   // the particle pass that binned the current keys counted quadrants only
   const int32_t* qc = s.qc_ready ? lr2d_quad_next(s) : nullptr;
-  k_scan_blocks<<<nblk, SCAN_T, 0, s.stream>>>(s.cnt_next, qc, s.scan_blk, s.C, s.tune.wcap);
-  k_scan_totals<<<1, SCAN_T, 0, s.stream>>>(s.scan_blk, nblk, s.wl, s.work);
-  k_scan_write<<<nblk, SCAN_T, 0, s.stream>>>(s.cnt_next, qc, s.cnt, s.off, s.cursor, s.list_small, s.list_big,
-                                               s.scan_blk, s.C, s.tune.wcap);
+  scan_launch(s, s.cnt_next, qc, s.off, nullptr);
   return 3;
+}
+
+// the scan of a slotted layout: counts from the slot counters, the region
+// bases stay (off), the packed offsets go to noff for the repair
+int launch_scan_slotted(Session& s) {
+  scan_launch(s, s.dcur, nullptr, nullptr, s.noff);
+  return 3;
+}
+
+template <typename real> static int repair_impl(Session& s, bool force) {
+  PT<real> src = pt<real>(s.P[s.cur]), oth = pt<real>(s.P[1 - s.cur]), ov = pt<real>(s.ovf);
+  const int32_t* ovn = s.ovf_n + (1 - s.ovf_par);  // the counter of the pass that made the layout
+  const int g = s.num_sms * 4;
+  k_repair_move<real><<<g, 256, 0, s.stream>>>(src, oth, ov, s.ovf_key, ovn, s.off, s.cnt, s.noff, s.cursor, s.C,
+                                               force ? 1 : 0);
+  if (force) return 1;
+  k_repair_back<real><<<g, 256, 0, s.stream>>>(oth, src, ovn, s.noff, s.off, s.C, s.N);
+  return 2;
+}
+int launch_repair(Session& s) { return s.prec == MCPM_FP32 ? repair_impl<float>(s, false) : repair_impl<double>(s, false); }
+
+// a slotted layout packed into the other buffer (host-side: the buffer and
+// the offsets change places)
+int launch_compact(Session& s) {
+  int n = launch_scan_slotted(s);
+  n += s.prec == MCPM_FP32 ? repair_impl<float>(s, true) : repair_impl<double>(s, true);
+  s.cur = 1 - s.cur;
+  std::swap(s.off, s.noff);
+  return n;
 }
 
 template <typename real> static int scatter_impl(Session& s) {
@@ -1754,7 +1958,7 @@ template <typename real> static size_t update_smem(const Session& s) {
   return 3 * sizeof(real) * (size_t)s.tune.bcap;
 }
 
-template <typename real> static int update_impl(Session& s, uint32_t stages, int bc_call_base) {
+template <typename real> static int update_impl(Session& s, uint32_t stages, int bc_call_base, bool slotted) {
   const int n = sync_dstep(s);
   UpdArgs<real> a;
   a.k = s.k;
@@ -1780,12 +1984,33 @@ template <typename real> static int update_impl(Session& s, uint32_t stages, int
   a.qc = nullptr;
   a.qtx = a.qty = nullptr;
   if (sizeof(real) == 4 && s.qc_fuse_now) lr2d_quad_fuse(s, &a.qc, &a.qtx, &a.qty);
+  a.d = pt<real>(s.P[1 - s.cur]);
+  a.doff = s.doff;
+  a.dcur = s.dcur;
+  a.ovf = pt<real>(s.ovf);
+  a.ovf_key = s.ovf_key;
+  a.ovf_n = s.ovf_n ? s.ovf_n + s.ovf_par : nullptr;
   size_t sm = update_smem<real>(s);
   const dim3 g(s.tune.grid_upd), b(256);
   const bool spec = s.k.problem == MCPM_PROBLEM_CLOSED_BOX, per = s.k.problem == MCPM_PROBLEM_PERIODIC;
   constexpr int SPEC = MCPM_PROBLEM_CLOSED_BOX, PER = MCPM_PROBLEM_PERIODIC;
   constexpr uint32_t F = ST_FUSED_FP, FL = ST_FUSED_FP | ST_LR;
   if constexpr (sizeof(real) == 4) {
+    if (slotted) {
+      // the pass writes the slotted layout of the other buffer
+      if (stages == F) {
+        if (spec) k_update<real, F, SPEC, true><<<g, b, sm, s.stream>>>(a);
+        else if (per) k_update<real, F, PER, true><<<g, b, sm, s.stream>>>(a);
+        else k_update<real, F, 0, true><<<g, b, sm, s.stream>>>(a);
+      } else if (stages == FL) {
+        if (spec) k_update<real, FL, SPEC, true><<<g, b, sm, s.stream>>>(a);
+        else if (per) k_update<real, FL, PER, true><<<g, b, sm, s.stream>>>(a);
+        else k_update<real, FL, 0, true><<<g, b, sm, s.stream>>>(a);
+      } else {
+        k_update<real, 0u, 0, true><<<g, b, sm, s.stream>>>(a);
+      }
+      return n + 1;
+    }
     if (stages == F) {
       if (spec) k_update<real, F, SPEC><<<g, b, sm, s.stream>>>(a);
       else if (per) k_update<real, F, PER><<<g, b, sm, s.stream>>>(a);
@@ -1804,8 +2029,9 @@ template <typename real> static int update_impl(Session& s, uint32_t stages, int
   else k_update<real, 0u><<<g, b, sm, s.stream>>>(a);
   return n + 1;
 }
-int launch_update(Session& s, uint32_t stages, int bc_call_base) {
-  return s.prec == MCPM_FP32 ? update_impl<float>(s, stages, bc_call_base) : update_impl<double>(s, stages, bc_call_base);
+int launch_update(Session& s, uint32_t stages, int bc_call_base, bool slotted) {
+  return s.prec == MCPM_FP32 ? update_impl<float>(s, stages, bc_call_base, slotted)
+                             : update_impl<double>(s, stages, bc_call_base, false);
 }
 
 template <typename real> static int conv_in_impl(Session& s, int64_t n) {
@@ -1835,7 +2061,11 @@ cudaError_t update_set_smem_max() {
       (const void*)k_update<float, F>,           (const void*)k_update<double, F>,
       (const void*)k_update<float, FL>,          (const void*)k_update<double, FL>,
       (const void*)k_update<float, F, SPEC>,     (const void*)k_update<float, F, PER>,
-      (const void*)k_update<float, FL, SPEC>,    (const void*)k_update<float, FL, PER>};
+      (const void*)k_update<float, FL, SPEC>,    (const void*)k_update<float, FL, PER>,
+      (const void*)k_update<float, F, 0, true>,  (const void*)k_update<float, F, SPEC, true>,
+      (const void*)k_update<float, F, PER, true>, (const void*)k_update<float, FL, 0, true>,
+      (const void*)k_update<float, FL, SPEC, true>, (const void*)k_update<float, FL, PER, true>,
+      (const void*)k_update<float, 0u, 0, true>};
   cudaError_t e = cudaSuccess;
   for (const void* f : fns)
     if (e == cudaSuccess) e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);

@@ -206,22 +206,34 @@ int mcpm_session_create(const mcpm_config* cfg, mcpm_session** out) {
   s->tune.block = 256;
 
   const size_t cap = (size_t)s->cap, C = (size_t)s->C, rs = s->rsz;
+  // FP32 sessions write slotted layouts (MCPM_SLOTTED=0 keeps the packed
+  // layout and its scatter pass): room for every region's slack -- a
+  // quarter of the count, at least 16, rounded to 8 -- besides the particles
+  const char* sl_env = getenv("MCPM_SLOTTED");
+  s->use_slotted = s->prec == MCPM_FP32 && !(sl_env && sl_env[0] == '0');
+  s->slots = s->use_slotted ? (int64_t)(cap + cap / 4 + 24 * C + 64) : (int64_t)cap;
+  const size_t slots = (size_t)s->slots;
   auto A = [&](void** p, size_t bytes) -> bool { return cudaMalloc(p, bytes ? bytes : 16) == cudaSuccess; };
   bool ok = true;
-  for (int b = 0; b < 2 && ok; ++b) {
-    PBuf& P = s->P[b];
-    if (s->need_x1) ok = ok && A(&P.x1, cap * rs);
-    ok = ok && A(&P.x2, cap * rs) && A(&P.U1, cap * rs) && A(&P.U2, cap * rs) && A(&P.U3, cap * rs) &&
-         A((void**)&P.pid, cap * 4);
+  auto alloc_set = [&](PBuf& P, size_t n) {
+    if (s->need_x1) ok = ok && A(&P.x1, n * rs);
+    ok = ok && A(&P.x2, n * rs) && A(&P.U1, n * rs) && A(&P.U2, n * rs) && A(&P.U3, n * rs) &&
+         A((void**)&P.pid, n * 4);
     if (s->need_old) {
-      if (s->need_x1) ok = ok && A(&P.x1o, cap * rs);
-      ok = ok && A(&P.x2o, cap * rs);
+      if (s->need_x1) ok = ok && A(&P.x1o, n * rs);
+      ok = ok && A(&P.x2o, n * rs);
     }
+  };
+  for (int b = 0; b < 2 && ok; ++b) alloc_set(s->P[b], slots);
+  if (s->use_slotted) {
+    alloc_set(s->ovf, cap);
+    ok = ok && A((void**)&s->ovf_key, cap * 4) && A((void**)&s->ovf_n, 16) && A((void**)&s->doff, (C + 1) * 4) &&
+         A((void**)&s->noff, (C + 1) * 4) && A((void**)&s->dcur, C * 4);
   }
   ok = ok && A((void**)&s->key, cap * 4) && A((void**)&s->cnt, C * 4) && A((void**)&s->cnt_next, C * 4) &&
        A((void**)&s->off, (C + 1) * 4) && A((void**)&s->cursor, C * 4) && A((void**)&s->list_small, C * 4) &&
        A((void**)&s->list_big, C * 4) && A((void**)&s->wl, WL_COUNT * 4) && A((void**)&s->work, WK_COUNT * 4) &&
-       A((void**)&s->scan_blk, 4 * (C / 1024 + 2) * 4) &&
+       A((void**)&s->scan_blk, 8 * (C / 1024 + 2) * 4) &&
        A((void**)&s->cell, (size_t)CF_DEV_COUNT * C * 8) && A((void**)&s->pcell, (size_t)PF_STRIDE * C * 4) && A((void**)&s->xi, 3 * cap * 8) &&
        A((void**)&s->inj, 3 * cap * 8) && A((void**)&s->stage, 5 * cap * 8) &&
        A((void**)&s->faces, ((size_t)k.N1 + 1 + 5000) * 8) && A((void**)&s->status, 16) &&
@@ -232,6 +244,10 @@ int mcpm_session_create(const mcpm_config* cfg, mcpm_session** out) {
     return MCPM_ERR_CUDA;
   }
   cudaMemsetAsync(s->cnt_next, 0, C * 4, s->stream);
+  if (s->use_slotted) {
+    cudaMemsetAsync(s->dcur, 0, C * 4, s->stream);
+    cudaMemsetAsync(s->ovf_n, 0, 16, s->stream);
+  }
   cudaMemsetAsync(s->cell, 0, (size_t)CF_DEV_COUNT * C * 8, s->stream);
   cudaMemsetAsync(s->pcell, 0, (size_t)PF_STRIDE * C * 4, s->stream);
   cudaMemsetAsync(s->status, 0, 16, s->stream);
@@ -265,6 +281,12 @@ int mcpm_session_destroy(mcpm_session* s) {
     cudaFree(P.x1); cudaFree(P.x2); cudaFree(P.U1); cudaFree(P.U2); cudaFree(P.U3); cudaFree(P.pid);
     cudaFree(P.x1o); cudaFree(P.x2o);
   }
+  {
+    PBuf& P = s->ovf;
+    cudaFree(P.x1); cudaFree(P.x2); cudaFree(P.U1); cudaFree(P.U2); cudaFree(P.U3); cudaFree(P.pid);
+    cudaFree(P.x1o); cudaFree(P.x2o);
+  }
+  cudaFree(s->ovf_key); cudaFree(s->ovf_n); cudaFree(s->doff); cudaFree(s->noff); cudaFree(s->dcur);
   cudaFree(s->key); cudaFree(s->cnt); cudaFree(s->cnt_next); cudaFree(s->off); cudaFree(s->cursor);
   cudaFree(s->list_small); cudaFree(s->list_big); cudaFree(s->wl); cudaFree(s->work); cudaFree(s->scan_blk); cudaFree(s->cell); cudaFree(s->pcell);
   cudaFree(s->xi); cudaFree(s->inj); cudaFree(s->stage); cudaFree(s->faces); cudaFree(s->lr_tab); cudaFree(s->status); cudaFree(s->dstep);
@@ -304,7 +326,20 @@ int mcpm_check_status(mcpm_session* s) {
 }
 
 // binning + counting sort into cell order (the front of cell_update)
+// A slotted layout left by the fused step packed into the other buffer:
+// everything but the fused step works on packed layouts [0, N).
+static int leave_slotted(mcpm_session* s) {
+  if (!s->slotted) return MCPM_OK;
+  int n = T_SCAN(launch_compact(*s));
+  s->slotted = false;
+  s->sorted = true;
+  s->keys_current = false;
+  s->qc_ready = false;
+  return after_launch(s, n, "compact");
+}
+
 static int sort_by_cell(mcpm_session* s) {
+  if (s->slotted) return leave_slotted(s);
   int n = 0;
   if (!s->keys_current) n += T_BIN(launch_bin(*s, s->step));
   n += T_SCAN(launch_scan(*s));
@@ -336,6 +371,7 @@ int mcpm_upload_particles(mcpm_session* s, int64_t n, const double* x1, const do
   s->omega_init = false;
   s->keys_current = false;
   s->sorted = false;
+  s->slotted = false;
   s->have_particles = true;
   return sort_by_cell(s);
 }
@@ -344,6 +380,8 @@ int mcpm_download_particles(mcpm_session* s, int64_t n, double* x1, double* x2, 
   if (!s || n != s->N || !x2 || !U1 || !U2 || !U3) return fail(s, MCPM_ERR_ARG, "download: bad arguments");
   const size_t cap = (size_t)s->cap, b = (size_t)n * 8;
   cudaStream_t st = s->stream;
+  int rc0 = leave_slotted(s);  // the staging kernel reads a packed layout [0, N)
+  if (rc0) return rc0;
   int k = launch_convert_out(*s, n);
   int rc = after_launch(s, k, "download");
   if (rc) return rc;
@@ -449,7 +487,14 @@ static int step_once(mcpm_session* s, uint32_t stages) {
   const int m = s->cfg.model;
   int n = 0;
   if (s->needs_rebin) { s->sorted = false; s->needs_rebin = false; }
-  if (!s->sorted) {
+  if (s->slotted) {
+    // the last particle pass wrote a slotted layout: its counts, work lists
+    // and the next destination layout, then the repair of overflowed
+    // regions (two launches that return at once when none overflowed)
+    n += T_SCAN(launch_scan_slotted(*s));
+    n += T_SCAT(launch_repair(*s));
+    s->slotted = false;
+  } else if (!s->sorted) {
     if (!s->keys_current) n += T_BIN(launch_bin(*s, s->step));
     n += T_SCAN(launch_scan(*s));
     n += T_SCAT(launch_scatter(*s));
@@ -467,7 +512,8 @@ static int step_once(mcpm_session* s, uint32_t stages) {
   int32_t* qn = lr2d_quad_next(*s);
   s->qc_fuse_now = qn && (stages & ST_KEY) && (s->lr2d_nodes_needed());
   if (s->qc_fuse_now) cudaMemsetAsync(qn, 0, (size_t)s->C * 4 * sizeof(int32_t), s->stream);
-  n += T_UPD(launch_update(*s, stages, 0));
+  const bool slot = s->use_slotted && (stages & ST_KEY);
+  n += T_UPD(launch_update(*s, stages, 0, slot));
   s->qc_ready = s->qc_fuse_now;
   s->qc_fuse_now = false;
   k_step_advance<<<1, 1, 0, s->stream>>>(s->dstep);
@@ -475,8 +521,17 @@ static int step_once(mcpm_session* s, uint32_t stages) {
   s->step++;
   s->dstep_val = s->step;
   s->bc_calls = 0;
-  s->keys_current = true;
   s->sorted = false;
+  if (slot) {
+    // the new state sits in the other buffer, laid out by doff
+    s->cur = 1 - s->cur;
+    std::swap(s->off, s->doff);
+    s->ovf_par ^= 1;
+    s->slotted = true;
+    s->keys_current = false;
+  } else {
+    s->keys_current = true;
+  }
   return n;
 }
 
@@ -486,6 +541,11 @@ static uint64_t graph_signature(const mcpm_session* s, uint32_t stages) {
   auto mix = [&](uint64_t v) { h = (h ^ v) * 1099511628211ull; };
   mix((uint64_t)(uintptr_t)s->stream);
   mix((uint64_t)s->cur);
+  mix((uint64_t)(uintptr_t)s->off);
+  mix((uint64_t)(uintptr_t)s->doff);
+  mix((uint64_t)(uintptr_t)s->noff);
+  mix((uint64_t)s->ovf_par);
+  mix((uint64_t)s->slotted);
   mix(stages);
   mix((uint64_t)s->tune.wcap);
   mix((uint64_t)s->tune.bcap);
@@ -503,8 +563,10 @@ static int capture_pair(mcpm_session* s, uint32_t stages, uint64_t sig) {
   if (s->graph) { cudaGraphExecDestroy(s->graph); s->graph = nullptr; }
   int rc = after_launch(s, sync_dstep(*s), "step");
   if (rc) return rc;
-  const int step0 = s->step, cur0 = s->cur, dval0 = s->dstep_val;
+  const int step0 = s->step, cur0 = s->cur, dval0 = s->dstep_val, par0 = s->ovf_par;
   const int64_t launches0 = s->launches;
+  const bool keys0 = s->keys_current, sorted0 = s->sorted, slotted0 = s->slotted, qc0 = s->qc_ready;
+  int32_t *off0 = s->off, *doff0 = s->doff, *noff0 = s->noff;
   cudaGraph_t g = nullptr;
   if (cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
     cudaGetLastError();
@@ -514,8 +576,9 @@ static int capture_pair(mcpm_session* s, uint32_t stages, uint64_t sig) {
   int n = step_once(s, stages);
   n += step_once(s, stages);
   cudaError_t e = cudaStreamEndCapture(s->stream, &g);
-  s->step = step0; s->cur = cur0; s->dstep_val = dval0; s->launches = launches0;
-  s->keys_current = true; s->sorted = false; s->needs_rebin = false;
+  s->step = step0; s->cur = cur0; s->dstep_val = dval0; s->launches = launches0; s->ovf_par = par0;
+  s->keys_current = keys0; s->sorted = sorted0; s->needs_rebin = false; s->slotted = slotted0; s->qc_ready = qc0;
+  s->off = off0; s->doff = doff0; s->noff = noff0;
   if (e == cudaSuccess && g) e = cudaGraphInstantiate(&s->graph, g, 0);
   if (g) cudaGraphDestroy(g);
   if (e != cudaSuccess) {
@@ -538,8 +601,10 @@ static int capture_pair(mcpm_session* s, uint32_t stages, uint64_t sig) {
 // graph advances it), then the odd step eagerly
 static int run_steps(mcpm_session* s, int n_steps, uint32_t stages) {
   int it = 0, rc;
-  while (it < n_steps && (s->needs_rebin || s->sorted || !s->keys_current || n_steps - it < 2 || s->prof ||
-                          !s->use_graphs)) {
+  // steady state: the last fused step left a slotted layout, or keys for
+  // the scan and scatter
+  auto steady = [&]() { return !s->needs_rebin && (s->slotted || (s->keys_current && !s->sorted)); };
+  while (it < n_steps && (!steady() || n_steps - it < 2 || s->prof || !s->use_graphs)) {
     if ((rc = after_launch(s, step_once(s, stages), "step"))) return rc;
     ++it;
   }
@@ -747,6 +812,8 @@ int mcpm_get_index(mcpm_session* s, int32_t* index) {
 
 int mcpm_get_normals(mcpm_session* s, double* a, double* b, double* c) {
   if (!s || !a || !b || !c) return MCPM_ERR_ARG;
+  int rc0 = leave_slotted(s);
+  if (rc0) return rc0;
   const size_t cap = (size_t)s->cap;
   k_unpermute3<<<(int)((s->N + 255) / 256 > 4096 ? 4096 : (s->N + 255) / 256 + 1), 256, 0, s->stream>>>(s->xi, s->P[s->cur].pid, s->stage, s->N, s->cap);
   int rc = after_launch(s, 1, "get_normals");
@@ -802,6 +869,8 @@ int32_t mcpm_get_wcap(const mcpm_session* s) { return s ? s->tune.wcap : -1; }
 // keeps the fastest.  The particle state is unchanged on return.
 int mcpm_autotune(mcpm_session* s, int32_t steps, int32_t* chosen) {
   if (!s || !s->have_particles || steps < 1) return MCPM_ERR_STATE;
+  int rc = leave_slotted(s);  // the trials start from a packed layout
+  if (rc) return rc;
   const size_t rs = s->rsz, N = (size_t)s->N, C = (size_t)s->C;
   const PBuf& P = s->P[s->cur];
   void* arrs[7] = {P.x1, P.x2, P.U1, P.U2, P.U3, P.x1o, P.x2o};
@@ -809,7 +878,7 @@ int mcpm_autotune(mcpm_session* s, int32_t steps, int32_t* chosen) {
   for (int i = 0; i < 7; ++i) if (arrs[i]) bytes += N * rs;
   bytes += N * 4 + (size_t)CF_DEV_COUNT * C * 8 + (size_t)PF_STRIDE * C * 4;
   char* save = nullptr;
-  int rc = cuda_check(s, cudaMalloc(&save, bytes), "autotune scratch");
+  rc = cuda_check(s, cudaMalloc(&save, bytes), "autotune scratch");
   if (rc) return rc;
   cudaStream_t st = s->stream;
   auto copy_all = [&](bool to_save) {
@@ -839,6 +908,7 @@ int mcpm_autotune(mcpm_session* s, int32_t steps, int32_t* chosen) {
     if (cands[ci] > s->tune.bcap / 8) continue;
     s->tune.wcap = cands[ci];
     s->cur = cur0; s->step = step0; s->keys_current = false; s->sorted = false; s->needs_rebin = false;
+    s->slotted = false;
     s->omega_init = om0;
     rc = mcpm_step(s, 1);  // warm-up (and a re-scan with this split)
     if (rc) break;
@@ -856,6 +926,7 @@ int mcpm_autotune(mcpm_session* s, int32_t steps, int32_t* chosen) {
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   s->cur = cur0; s->step = step0; s->sorted = sorted0; s->keys_current = keys0; s->needs_rebin = rebin0;
+  s->slotted = false;
   s->omega_init = om0;
   s->tune.wcap = best;
   // the saved layout's work lists were built with the old split: rebuild
