@@ -118,14 +118,15 @@ struct Session {
   // particle straight into its new cell's region of the other buffer, a
   // region of capacity doff[c+1] - doff[c] with slack over the cell's count,
   // slots handed out by dcur; a region that fills up sends the rest to the
-  // overflow arrays, which the next scan's repair pass folds back
+  // overflow arrays, and the repair after the next scan moves such cells,
+  // overflow included, to spare slots past the layout
   int64_t slots = 0;            // slots per particle array (>= cap)
   int32_t* doff = nullptr;      // [C+1] region bases of the destination layout
   int32_t* noff = nullptr;      // [C+1] packed offsets of the totals (repair / compaction)
   int32_t* dcur = nullptr;      // [C] slots taken per destination region (= particles binned there)
   PBuf ovf{};                   // overflow particles (cap each)
   int32_t* ovf_key = nullptr;   // [cap] their cells
-  int32_t* ovf_n = nullptr;     // [2] overflow counts, alternating between steps
+  int32_t* ovf_n = nullptr;     // [4] overflow counts (alternating between steps), spare cursor
   int ovf_par = 0;              // the overflow counter the next slotted pass uses
   bool use_slotted = false;     // the session writes slotted layouts (FP32)
   bool slotted = false;         // P[cur] holds a slotted layout (off = doff of that pass,

@@ -191,10 +191,16 @@ __global__ void __launch_bounds__(SCAN_T) k_scan_blocks(const int32_t* cnt_next,
   }
 }
 
+// overflow bookkeeping of slotted layouts: two overflow counters (the pass
+// that wrote the layout and the next one alternate) and the cursor of the
+// spare slots past the layout
+enum { OVF_SPARE = 2, OVF_WORDS = 4 };
+
 // pass 2: exclusive scan of the block totals (one block), list lengths; the
-// overflow counter of the next slotted pass starts from zero
+// overflow counter of the next slotted pass and the spare cursor start from
+// zero
 __global__ void __launch_bounds__(SCAN_T) k_scan_totals(int32_t* blk, int nblk, int32_t* wl, int32_t* work,
-                                                        int32_t* ovf_clear) {
+                                                        int32_t* ovf_n, int par) {
   __shared__ int sh[SCAN_Q][32];
   int carry[SCAN_Q] = {0, 0, 0, 0}, mx = 0;
   for (int base = 0; base < nblk; base += SCAN_T) {
@@ -226,7 +232,10 @@ __global__ void __launch_bounds__(SCAN_T) k_scan_totals(int32_t* blk, int nblk, 
     int m = shm[0];
     for (int w = 1; w < 32; ++w) m = max(m, shm[w]);
     wl[WL_N] = carry[0]; wl[WL_NSMALL] = carry[1]; wl[WL_NBIG] = carry[2]; wl[WL_MAXCNT] = m;
-    if (ovf_clear) *ovf_clear = 0;
+    if (ovf_n) {
+      ovf_n[par] = 0;
+      ovf_n[OVF_SPARE] = 0;
+    }
   }
   if (threadIdx.x < WK_COUNT) work[threadIdx.x] = 0;
 }
@@ -325,14 +334,11 @@ __device__ __forceinline__ void copy_particle(const PT<real>& src, int64_t i, co
 
 // Packs a slotted layout into dst at the packed offsets noff: each cell's
 // first min(total, capacity) particles from its region of src (bases off),
-// the rest from the overflow arrays.  Without force it returns at once when
-// nothing overflowed (the common case: the layout stays slotted).
+// the rest from the overflow arrays.
 template <typename real>
-__global__ void k_repair_move(PT<real> src, PT<real> dst, PT<real> ovf, const int32_t* ovf_key,
-                              const int32_t* ovf_n, const int32_t* off, const int32_t* cnt, const int32_t* noff,
-                              int32_t* cursor, int C, int force) {
+__global__ void k_pack(PT<real> src, PT<real> dst, PT<real> ovf, const int32_t* ovf_key, const int32_t* ovf_n,
+                       const int32_t* off, const int32_t* cnt, const int32_t* noff, int32_t* cursor, int C) {
   const int n_ovf = *ovf_n;
-  if (!force && n_ovf == 0) return;
   const int lane = threadIdx.x & 31;
   const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x, nt = (int64_t)gridDim.x * blockDim.x;
   for (int64_t c = tid >> 5; c < C; c += nt >> 5) {
@@ -346,15 +352,43 @@ __global__ void k_repair_move(PT<real> src, PT<real> dst, PT<real> ovf, const in
   }
 }
 
-// After an overflow: the packed particles back into the buffer the layout
-// belongs to, and the packed offsets in place of the region bases.
+// Repair of a slotted layout whose regions overflowed, in two launches that
+// return at once when nothing did.  Every cell holding more particles than
+// its region moves to the spare slots past the layout (from off[C] on): its
+// region's particles here, the base of its new place in nbase (-1: the cell
+// stays) and the slot its overflow entries start from in cursor.
 template <typename real>
-__global__ void k_repair_back(PT<real> packed, PT<real> dst, const int32_t* ovf_n, const int32_t* noff, int32_t* off,
-                              int C, int64_t n) {
+__global__ void k_relocate(PT<real> p, const int32_t* ovf_n, const int32_t* off, const int32_t* cnt, int32_t* nbase,
+                           int32_t* cursor, int32_t* spare, int C) {
   if (*ovf_n == 0) return;
+  const int lane = threadIdx.x & 31;
   const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x, nt = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t i = tid; i < n; i += nt) copy_particle(packed, i, dst, i);
-  for (int64_t c = tid; c <= C; c += nt) off[c] = noff[c];
+  const int end = off[C];
+  for (int64_t c = tid >> 5; c < C; c += nt >> 5) {
+    const int s0 = off[c], capc = off[c + 1] - s0, n = cnt[c];
+    int nb = -1;
+    if (n > capc) {
+      if (lane == 0) nb = end + atomicAdd(spare, n);
+      nb = __shfl_sync(FULL, nb, 0);
+      for (int i = lane; i < capc; i += 32) copy_particle(p, (int64_t)s0 + i, p, (int64_t)nb + i);
+      if (lane == 0) cursor[c] = capc;
+    }
+    if (lane == 0) nbase[c] = nb;
+  }
+}
+// ... then the overflow entries after them, and the moved cells' bases
+template <typename real>
+__global__ void k_relocate_tail(PT<real> p, PT<real> ovf, const int32_t* ovf_key, const int32_t* ovf_n,
+                                const int32_t* nbase, int32_t* cursor, int32_t* off, int C) {
+  const int n_ovf = *ovf_n;
+  if (n_ovf == 0) return;
+  const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x, nt = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t e = tid; e < n_ovf; e += nt) {
+    const int c = ovf_key[e];
+    copy_particle(ovf, e, p, (int64_t)nbase[c] + atomicAdd(&cursor[c], 1));
+  }
+  for (int64_t c = tid; c < C; c += nt)
+    if (nbase[c] >= 0) off[c] = nbase[c];
 }
 
 // ================================================ cell access helpers
@@ -1502,6 +1536,9 @@ __device__ void update_cell(int c, const UpdArgs<real>& a, int step, real* xs, i
 #ifndef MCPM_UPD_MINB
 #define MCPM_UPD_MINB 5
 #endif
+#ifndef MCPM_UPD_MINB_SL
+#define MCPM_UPD_MINB_SL 5
+#endif
 #ifndef MCPM_UPD_UNROLL
 #define MCPM_UPD_UNROLL 1
 #endif
@@ -1778,19 +1815,20 @@ __device__ void update_cell_f32(int c, const UpdArgs<float>& a, int step, float*
       }
       if (act) {
         const int r0 = a.doff[key], capc = a.doff[key + 1] - r0;
-        const PT<float>* D = &a.d;
+        const bool ov = slot >= capc;  // the region is full: to the overflow arrays
         int64_t d = (int64_t)r0 + slot;
-        if (slot >= capc) {  // the region is full: to the overflow arrays
+        if (ov) {
           d = atomicAdd(a.ovf_n, 1);
           a.ovf_key[d] = key;
-          D = &a.ovf;
         }
-        D->U1[d] = s.u1; D->U2[d] = s.u2; D->U3[d] = s.u3;
-        if (D->x1) D->x1[d] = s.x1;
-        D->x2[d] = s.x2;
-        D->pid[d] = pid;
-        if (D->x1o) D->x1o[d] = s.x1o;
-        if (D->x2o) D->x2o[d] = s.x2o;
+        (ov ? a.ovf.U1 : a.d.U1)[d] = s.u1;
+        (ov ? a.ovf.U2 : a.d.U2)[d] = s.u2;
+        (ov ? a.ovf.U3 : a.d.U3)[d] = s.u3;
+        if (a.d.x1) (ov ? a.ovf.x1 : a.d.x1)[d] = s.x1;
+        (ov ? a.ovf.x2 : a.d.x2)[d] = s.x2;
+        (ov ? a.ovf.pid : a.d.pid)[d] = pid;
+        if (a.d.x1o) (ov ? a.ovf.x1o : a.d.x1o)[d] = s.x1o;
+        if (a.d.x2o) (ov ? a.ovf.x2o : a.d.x2o)[d] = s.x2o;
       }
     } else if (st & ST_KEY) {
       // with quadrant counting the cell's count is their sum (read by the scan)
@@ -1802,7 +1840,8 @@ __device__ void update_cell_f32(int c, const UpdArgs<float>& a, int step, float*
 }
 
 template <typename real, uint32_t CST, int PB = 0, bool SL = false>
-__global__ void __launch_bounds__(256, sizeof(real) == 4 ? (CST ? MCPM_UPD_MINB : 3) : 1) k_update(UpdArgs<real> a) {
+__global__ void __launch_bounds__(256, sizeof(real) == 4 ? (CST ? (SL ? MCPM_UPD_MINB_SL : MCPM_UPD_MINB) : 3) : 1)
+    k_update(UpdArgs<real> a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ Acc<real> red[8 * 8];
   real* xs = reinterpret_cast<real*>(smem_raw);
@@ -1878,8 +1917,8 @@ int launch_bin(Session& s, int bin_step) { return s.prec == MCPM_FP32 ? bin_impl
 static void scan_launch(Session& s, const int32_t* src, const int32_t* qc, int32_t* off, int32_t* noff) {
   const int nblk = (s.C + SCAN_T - 1) / SCAN_T;
   k_scan_blocks<<<nblk, SCAN_T, 0, s.stream>>>(src, qc, s.scan_blk, s.C, s.tune.wcap);
-  k_scan_totals<<<1, SCAN_T, 0, s.stream>>>(s.scan_blk, nblk, s.wl, s.work,
-                                            s.use_slotted ? s.ovf_n + s.ovf_par : nullptr);
+  k_scan_totals<<<1, SCAN_T, 0, s.stream>>>(s.scan_blk, nblk, s.wl, s.work, s.use_slotted ? s.ovf_n : nullptr,
+                                            s.ovf_par);
   ScanOut o;
   o.cnt_next = s.cnt_next; o.cursor = s.cursor; o.dcur = s.dcur;
   o.qc = qc; o.src = src;
@@ -1907,10 +1946,12 @@ template <typename real> static int repair_impl(Session& s, bool force) {
   PT<real> src = pt<real>(s.P[s.cur]), oth = pt<real>(s.P[1 - s.cur]), ov = pt<real>(s.ovf);
   const int32_t* ovn = s.ovf_n + (1 - s.ovf_par);  // the counter of the pass that made the layout
   const int g = s.num_sms * 4;
-  k_repair_move<real><<<g, 256, 0, s.stream>>>(src, oth, ov, s.ovf_key, ovn, s.off, s.cnt, s.noff, s.cursor, s.C,
-                                               force ? 1 : 0);
-  if (force) return 1;
-  k_repair_back<real><<<g, 256, 0, s.stream>>>(oth, src, ovn, s.noff, s.off, s.C, s.N);
+  if (force) {
+    k_pack<real><<<g, 256, 0, s.stream>>>(src, oth, ov, s.ovf_key, ovn, s.off, s.cnt, s.noff, s.cursor, s.C);
+    return 1;
+  }
+  k_relocate<real><<<g, 256, 0, s.stream>>>(src, ovn, s.off, s.cnt, s.noff, s.cursor, s.ovf_n + OVF_SPARE, s.C);
+  k_relocate_tail<real><<<g, 256, 0, s.stream>>>(src, ov, s.ovf_key, ovn, s.noff, s.cursor, s.off, s.C);
   return 2;
 }
 int launch_repair(Session& s) { return s.prec == MCPM_FP32 ? repair_impl<float>(s, false) : repair_impl<double>(s, false); }
@@ -2076,7 +2117,10 @@ int update_occupancy(const Session& s) {
   size_t sm = update_smem_bytes(s);
   // the fused step's kernel sets the persistent grid (the split-mode
   // variant, with every stage decided at run time, holds fewer blocks)
-  if (s.prec == MCPM_FP32) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_update<float, ST_FUSED_FP>, 256, sm);
+  if (s.prec == MCPM_FP32 && s.use_slotted)
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_update<float, ST_FUSED_FP, 0, true>, 256, sm);
+  else if (s.prec == MCPM_FP32)
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_update<float, ST_FUSED_FP>, 256, sm);
   else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_update<double, 0u>, 256, sm);
   return nb < 1 ? 1 : nb;
 }

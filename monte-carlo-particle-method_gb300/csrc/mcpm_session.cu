@@ -211,7 +211,8 @@ int mcpm_session_create(const mcpm_config* cfg, mcpm_session** out) {
   // quarter of the count, at least 16, rounded to 8 -- besides the particles
   const char* sl_env = getenv("MCPM_SLOTTED");
   s->use_slotted = s->prec == MCPM_FP32 && !(sl_env && sl_env[0] == '0');
-  s->slots = s->use_slotted ? (int64_t)(cap + cap / 4 + 24 * C + 64) : (int64_t)cap;
+  // and, past the layout, spare slots for the cells whose regions overflow
+  s->slots = s->use_slotted ? (int64_t)(2 * cap + cap / 4 + 24 * C + 64) : (int64_t)cap;
   const size_t slots = (size_t)s->slots;
   auto A = [&](void** p, size_t bytes) -> bool { return cudaMalloc(p, bytes ? bytes : 16) == cudaSuccess; };
   bool ok = true;
