@@ -958,6 +958,16 @@ template <typename real> struct PState {
   real x1, x2, x1o, x2o, u1, u2, u3;
 };
 
+// a particle's state into slot d of a set of arrays
+__device__ __forceinline__ void store_state(const PT<float>& D, int64_t d, const PState<float>& s, int pid) {
+  D.U1[d] = s.u1; D.U2[d] = s.u2; D.U3[d] = s.u3;
+  if (D.x1) D.x1[d] = s.x1;
+  D.x2[d] = s.x2;
+  D.pid[d] = pid;
+  if (D.x1o) D.x1o[d] = s.x1o;
+  if (D.x2o) D.x2o[d] = s.x2o;
+}
+
 // BC_specular_reflection, src/Main_Functions.cpp:6399-6525
 template <typename real>
 __device__ __forceinline__ void bc_specular(PState<real>& s, const DevConsts& k, const KC<real>& kc, uint32_t& bad) {
@@ -1815,20 +1825,13 @@ __device__ void update_cell_f32(int c, const UpdArgs<float>& a, int step, float*
       }
       if (act) {
         const int r0 = a.doff[key], capc = a.doff[key + 1] - r0;
-        const bool ov = slot >= capc;  // the region is full: to the overflow arrays
-        int64_t d = (int64_t)r0 + slot;
-        if (ov) {
-          d = atomicAdd(a.ovf_n, 1);
-          a.ovf_key[d] = key;
+        if (slot < capc) {
+          store_state(a.d, (int64_t)r0 + slot, s, pid);
+        } else {  // the region is full: to the overflow arrays
+          const int64_t e = atomicAdd(a.ovf_n, 1);
+          a.ovf_key[e] = key;
+          store_state(a.ovf, e, s, pid);
         }
-        (ov ? a.ovf.U1 : a.d.U1)[d] = s.u1;
-        (ov ? a.ovf.U2 : a.d.U2)[d] = s.u2;
-        (ov ? a.ovf.U3 : a.d.U3)[d] = s.u3;
-        if (a.d.x1) (ov ? a.ovf.x1 : a.d.x1)[d] = s.x1;
-        (ov ? a.ovf.x2 : a.d.x2)[d] = s.x2;
-        (ov ? a.ovf.pid : a.d.pid)[d] = pid;
-        if (a.d.x1o) (ov ? a.ovf.x1o : a.d.x1o)[d] = s.x1o;
-        if (a.d.x2o) (ov ? a.ovf.x2o : a.d.x2o)[d] = s.x2o;
       }
     } else if (st & ST_KEY) {
       // with quadrant counting the cell's count is their sum (read by the scan)

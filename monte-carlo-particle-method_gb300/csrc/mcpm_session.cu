@@ -899,14 +899,15 @@ int mcpm_autotune(mcpm_session* s, int32_t steps, int32_t* chosen) {
   const bool sorted0 = s->sorted, keys0 = s->keys_current, rebin0 = s->needs_rebin, om0 = s->omega_init;
   const int64_t launches0 = s->launches;
   copy_all(true);
-  const int cands[5] = {128, 256, 384, 512, 768};
+  // the fixed splits, and the largest cell a warp can stage (bcap / 8)
+  const int cands[6] = {128, 256, 384, 512, 768, s->tune.bcap / 8};
   int best = s->tune.wcap;
   float best_ms = 1e30f;
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
-  for (int ci = 0; ci < 5 && rc == MCPM_OK; ++ci) {
-    if (cands[ci] > s->tune.bcap / 8) continue;
+  for (int ci = 0; ci < 6 && rc == MCPM_OK; ++ci) {
+    if (cands[ci] > s->tune.bcap / 8 || (ci == 5 && (cands[5] % 128) == 0)) continue;
     s->tune.wcap = cands[ci];
     s->cur = cur0; s->step = step0; s->keys_current = false; s->sorted = false; s->needs_rebin = false;
     s->slotted = false;

@@ -324,7 +324,7 @@ def test_autotune_restores_state(cuda_ok):
     s.step(2)
     before = s.download()
     w = s.autotune(2)
-    assert w in (128, 256, 384) and s.wcap == w
+    assert 128 <= w <= 768 and s.wcap == w
     after = s.download()
     for k in before:
         assert np.array_equal(before[k], after[k]), k
