@@ -154,6 +154,10 @@ struct Session {
   int32_t* dstep = nullptr;     // device copy of the step number the kernels read
   int dstep_val = -1;           // the value it holds once queued work has run (-1: unknown)
   cudaStream_t stream = nullptr;
+  // the learned force's branch of a fused step (nodal deposit + network)
+  // runs on a stream of its own, beside the moment pass and the solves
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   int step = 0;
   int bc_calls = 0;             // apply_BC calls in the current step (split mode)
   int rng_mode = MCPM_RNG_PHILOX;

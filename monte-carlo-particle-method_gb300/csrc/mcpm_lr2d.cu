@@ -131,7 +131,7 @@ __global__ void k_quadrants(DevConsts k, const int32_t* off, const int32_t* cnt,
 // wall (src/Main_Functions.cpp:2268-2364).  exact: the sum of equal terms in
 // sequence, as the reference accumulates it.
 __global__ void k_node_density(DevConsts k, const int32_t* qc, double* nnd, int exact,
-                               __nv_bfloat16* xin = nullptr, const double* ncell = nullptr) {
+                               __nv_bfloat16* xin = nullptr, const int32_t* ccnt = nullptr) {
   const int N0 = k.N0, N1 = k.N1;
   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < 4 * k.C; e += gridDim.x * blockDim.x) {
     const int c = e >> 2, slot = e & 3;
@@ -162,7 +162,10 @@ __global__ void k_node_density(DevConsts k, const int32_t* qc, double* nnd, int 
       __nv_bfloat16* xc = xin + (size_t)c * 16;
       sur_hi_lo(10.0 * (k.b * acc - 0.25), xc[slot], xc[6 + slot]);
       if (slot == 0) {
-        sur_hi_lo(10.0 * (k.b * ncell[c] - 0.25), xc[4], xc[10]);
+        // the cell density n = Fn N / V as the moment finalisation forms
+        // it, from the cell's count (so the deposit needs no moment pass)
+        const double ncv = 1 * k.Fn * (double)ccnt[c] / cell_volume(c, k);
+        sur_hi_lo(10.0 * (k.b * ncv - 0.25), xc[4], xc[10]);
         xc[5] = __float2bfloat16_rn(1.0f);
         for (int q = 11; q < 16; ++q) xc[q] = __float2bfloat16_rn(0.0f);
       }
@@ -635,12 +638,11 @@ int launch_node_density(Session& s) {
   if (!t || (t->mode != MCPM_LR_SCREENED_POISSON && !s.sur)) return 0;
   // with the network attached the deposit also writes the network's input
   __nv_bfloat16* xin = s.sur ? s.sur->xin : nullptr;
-  const double* ncell = s.cell + (size_t)MCPM_CF_N * s.C;
   s.sur_xin_ready = xin != nullptr;
   if (s.qc_ready && t->qc_next) {
     // the previous particle pass counted the quadrants of these positions
     k_node_density<<<blocks_for(4L * s.C, 256, s.num_sms * 16), 256, 0, s.stream>>>(
-        s.k, t->qc_next, t->nnd, s.prec == MCPM_FP64, xin, ncell);
+        s.k, t->qc_next, t->nnd, s.prec == MCPM_FP64, xin, s.cnt);
     return 1;
   }
   const int g = blocks_for((long)s.C * 32, 256, s.num_sms * 16);
@@ -652,7 +654,7 @@ int launch_node_density(Session& s) {
     k_quadrants<double><<<g, 256, 0, s.stream>>>(s.k, s.off, s.cnt, (const double*)P.x1, (const double*)P.x2, t->qc);
   }
   k_node_density<<<blocks_for(4L * s.C, 256, s.num_sms * 16), 256, 0, s.stream>>>(s.k, t->qc, t->nnd,
-                                                                                    s.prec == MCPM_FP64, xin, ncell);
+                                                                                    s.prec == MCPM_FP64, xin, s.cnt);
   return 2;
 }
 

@@ -199,6 +199,9 @@ int mcpm_session_create(const mcpm_config* cfg, mcpm_session** out) {
   cudaDeviceGetAttribute(&s->num_sms, cudaDevAttrMultiProcessorCount, dev);
   if ((rc = cuda_check(s, cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking), "stream"))) { delete s; return rc; }
   s->own_stream = s->stream;
+  if ((rc = cuda_check(s, cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking), "stream"))) { delete s; return rc; }
+  cudaEventCreateWithFlags(&s->ev_fork, cudaEventDisableTiming);
+  cudaEventCreateWithFlags(&s->ev_join, cudaEventDisableTiming);
 
   // tuning defaults (see mcpm_tune in the Python layer for the sweep)
   s->tune.bcap = (s->prec == MCPM_FP32) ? MCPM_UPD_BCAP : 3072;
@@ -298,6 +301,9 @@ int mcpm_session_destroy(mcpm_session* s) {
   for (auto& r : s->prof_recs) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
   for (auto e : s->prof_pool) cudaEventDestroy(e);
   if (s->own_stream) cudaStreamDestroy(s->own_stream);
+  if (s->side) { cudaStreamSynchronize(s->side); cudaStreamDestroy(s->side); }
+  if (s->ev_fork) cudaEventDestroy(s->ev_fork);
+  if (s->ev_join) cudaEventDestroy(s->ev_join);
   delete s;
   return MCPM_OK;
 }
@@ -502,12 +508,29 @@ static int step_once(mcpm_session* s, uint32_t stages) {
   } else {
     cudaMemsetAsync(s->work, 0, WK_COUNT * 4, s->stream);
   }
+  // the network in charge (not judged this step): its branch -- the nodal
+  // deposit from the new layout's counts and quadrants, then the inference
+  // that writes the kick -- needs no moments, so it runs on the side stream
+  // while the moment pass and the solves run here
+  const bool branch = s->sur && s->sur_active && !s->sur_judge_now && !s->prof && s->side &&
+                      s->cfg.long_range != MCPM_LR_NONE;
+  if (branch) {
+    cudaEventRecord(s->ev_fork, s->stream);
+    cudaStreamWaitEvent(s->side, s->ev_fork, 0);
+    cudaStream_t main_stream = s->stream;
+    s->stream = s->side;
+    n += launch_node_density(*s);
+    n += long_range_force(s);
+    s->stream = main_stream;
+    cudaEventRecord(s->ev_join, s->side);
+  }
   n += T_MOM(launch_moments(*s));
   n += T_SOLVE(launch_solve(*s, (m == MCPM_MODEL_FP_DENSE && s->step > 0) ? 1 : 0));
-  n += T_LR(launch_node_density(*s));
+  if (!branch) n += T_LR(launch_node_density(*s));
   s->nodes_valid = s->lr2d != nullptr;
   if (m == MCPM_MODEL_ESMC) n += T_ESMC(launch_esmc(*s));
-  if (s->cfg.long_range != MCPM_LR_NONE) n += long_range_force(s);
+  if (branch) cudaStreamWaitEvent(s->stream, s->ev_join, 0);
+  else if (s->cfg.long_range != MCPM_LR_NONE) n += long_range_force(s);
   // FP32 sessions with nodal densities: the particle pass also counts the
   // quadrants of the new positions, which the next step's deposit reads
   int32_t* qn = lr2d_quad_next(*s);
