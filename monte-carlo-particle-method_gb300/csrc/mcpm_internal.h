@@ -146,10 +146,6 @@ struct Session {
   alignas(16) char lr_host[160];  // the kernel's view of lr_tab
   LR2D* lr2d = nullptr;         // 2-D long range (node grid), when configured
   bool nodes_valid = false;     // nodal densities describe the last cell_update
-  bool qc_fuse_now = false;     // this particle pass also counts cell quadrants
-  // the 2-D force reads nodal densities (screened Poisson or the learned force)
-  bool lr2d_nodes_needed() const { return lr2d && (cfg.long_range == MCPM_LR_SCREENED_POISSON || sur); }
-  bool qc_ready = false;        // those counts describe the positions the keys bin
   uint32_t* status = nullptr;
   int32_t* dstep = nullptr;     // device copy of the step number the kernels read
   int dstep_val = -1;           // the value it holds once queued work has run (-1: unknown)
@@ -227,10 +223,6 @@ int launch_node_density(Session& s);
 int launch_long_range_2d(Session& s);
 int launch_node_density_from(Session& s, const int32_t* qc);
 int32_t* lr2d_quadrants(Session& s);
-// the quadrant-count buffer the FP32 particle pass fills and its cell-centre
-// thresholds; false when the session has none
-bool lr2d_quad_fuse(Session& s, int32_t** qc, const float** qtx, const float** qty);
-int32_t* lr2d_quad_next(Session& s);
 double* lr2d_node_density_mut(Session& s);
 const double* lr2d_potential(const Session& s);
 const double* lr2d_node_density(const Session& s);

@@ -150,17 +150,6 @@ __device__ __forceinline__ void block_scan4(int (&v)[SCAN_Q], int (&t)[SCAN_Q], 
   }
 }
 
-// particles binned into cell c for the next layout: the counter, or -- when
-// the particle pass counted quadrants -- the sum of the cell's four
-// quadrant counts (then the pass keeps no separate counter)
-__device__ __forceinline__ int next_count(const int32_t* cnt_next, const int32_t* qc, int c) {
-  if (qc) {
-    const int4 q = *reinterpret_cast<const int4*>(qc + 4 * (size_t)c);
-    return q.x + q.y + q.z + q.w;
-  }
-  return cnt_next[c];
-}
-
 __device__ __forceinline__ void scan_values(int (&v)[SCAN_Q], int c, int C, int count, int wcap) {
   v[0] = c < C ? count : 0;
   v[1] = (c < C && count <= wcap) ? 1 : 0;
@@ -169,12 +158,11 @@ __device__ __forceinline__ void scan_values(int (&v)[SCAN_Q], int c, int C, int 
 }
 
 // pass 1: per-block totals (count, small cells, big cells, slots, max count)
-__global__ void __launch_bounds__(SCAN_T) k_scan_blocks(const int32_t* cnt_next, const int32_t* qc, int32_t* blk,
-                                                        int C, int wcap) {
+__global__ void __launch_bounds__(SCAN_T) k_scan_blocks(const int32_t* counts, int32_t* blk, int C, int wcap) {
   __shared__ int sh[SCAN_Q][32];
   __shared__ int shm[32];
   const int c = blockIdx.x * SCAN_T + threadIdx.x;
-  const int count = c < C ? next_count(cnt_next, qc, c) : 0;
+  const int count = c < C ? counts[c] : 0;
   int v[SCAN_Q], t[SCAN_Q];
   scan_values(v, c, C, count, wcap);
   int mx = count;
@@ -246,7 +234,7 @@ __global__ void __launch_bounds__(SCAN_T) k_scan_totals(int32_t* blk, int nblk, 
 // of the next slotted layout
 struct ScanOut {
   int32_t *cnt_next, *cursor, *dcur;  // reset (dcur: may be null)
-  const int32_t *qc, *src;            // counts: src (cnt_next or dcur), or qc sums
+  const int32_t* src;                 // the counts: cnt_next or dcur
   int32_t *cnt, *off, *noff, *doff, *list_small, *list_big;
   const int32_t* blk;
   int C, wcap;
@@ -254,7 +242,7 @@ struct ScanOut {
 __global__ void __launch_bounds__(SCAN_T) k_scan_write(ScanOut a) {
   __shared__ int sh[SCAN_Q][32];
   const int c = blockIdx.x * SCAN_T + threadIdx.x;
-  const int count = c < a.C ? next_count(a.src, a.qc, c) : 0;
+  const int count = c < a.C ? a.src[c] : 0;
   int v[SCAN_Q], t[SCAN_Q];
   scan_values(v, c, a.C, count, a.wcap);
   const bool small = v[1], big = v[2];
@@ -337,7 +325,8 @@ __device__ __forceinline__ void copy_particle(const PT<real>& src, int64_t i, co
 // the rest from the overflow arrays.
 template <typename real>
 __global__ void k_pack(PT<real> src, PT<real> dst, PT<real> ovf, const int32_t* ovf_key, const int32_t* ovf_n,
-                       const int32_t* off, const int32_t* cnt, const int32_t* noff, int32_t* cursor, int C) {
+                       const int32_t* off, const int32_t* cnt, const int32_t* noff, int32_t* cursor, int C,
+                       uint32_t* status) {
   const int n_ovf = *ovf_n;
   const int lane = threadIdx.x & 31;
   const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x, nt = (int64_t)gridDim.x * blockDim.x;
@@ -348,7 +337,10 @@ __global__ void k_pack(PT<real> src, PT<real> dst, PT<real> ovf, const int32_t* 
   for (int64_t e = tid; e < n_ovf; e += nt) {
     const int c = ovf_key[e];
     const int d = noff[c] + (off[c + 1] - off[c]) + atomicAdd(&cursor[c], 1);
-    copy_particle(ovf, e, dst, (int64_t)d);
+    // an overflow entry lies within its cell's packed range by construction
+    // (its slot came from the cell's own counter); checked, not assumed
+    if (d < noff[c] + cnt[c]) copy_particle(ovf, e, dst, (int64_t)d);
+    else raise_status(status, MCPM_ERR_CAPACITY);
   }
 }
 
@@ -379,13 +371,18 @@ __global__ void k_relocate(PT<real> p, const int32_t* ovf_n, const int32_t* off,
 // ... then the overflow entries after them, and the moved cells' bases
 template <typename real>
 __global__ void k_relocate_tail(PT<real> p, PT<real> ovf, const int32_t* ovf_key, const int32_t* ovf_n,
-                                const int32_t* nbase, int32_t* cursor, int32_t* off, int C) {
+                                const int32_t* nbase, const int32_t* cnt, int32_t* cursor, int32_t* off, int C,
+                                uint32_t* status) {
   const int n_ovf = *ovf_n;
   if (n_ovf == 0) return;
   const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x, nt = (int64_t)gridDim.x * blockDim.x;
   for (int64_t e = tid; e < n_ovf; e += nt) {
     const int c = ovf_key[e];
-    copy_particle(ovf, e, p, (int64_t)nbase[c] + atomicAdd(&cursor[c], 1));
+    // only cells that outgrew their regions have overflow entries, and they
+    // were moved (nbase >= 0) with room for all cnt[c] particles; checked
+    const int b = nbase[c], q = atomicAdd(&cursor[c], 1);
+    if (b >= 0 && q < cnt[c]) copy_particle(ovf, e, p, (int64_t)b + q);
+    else raise_status(status, MCPM_ERR_CAPACITY);
   }
   for (int64_t c = tid; c < C; c += nt)
     if (nbase[c] >= 0) off[c] = nbase[c];
@@ -1184,11 +1181,6 @@ template <typename real> struct UpdArgs {
   const double* Vn;  // node potential of the 2-D Vlasov force (FP64 path)
   KC<real> kc;       // constants in the state's precision (read from the
                      // parameter bank, so they cost no registers)
-  // quadrant counts of the new positions for the next step's nodal deposit
-  // (FP32 2-D Vlasov sessions; null otherwise): qc[cell][quadrant] and the
-  // cell-centre thresholds per column / row
-  int32_t* qc;
-  const float *qtx, *qty;
   // slotted layouts (FP32 fused steps): the destination buffer, the region
   // bases of its layout and their slot counters, the overflow arrays and
   // their counter
@@ -1705,7 +1697,7 @@ __device__ void update_cell_f32(int c, const UpdArgs<float>& a, int step, float*
   for (int r = 0; r < iters; ++r) {
     const int i = r * TILE + t;
     const bool act = i < n;
-    int key = 0, quad = 0, pid = 0;
+    int key = 0, pid = 0;
     PState<float> s;
     if (act) {
       const int64_t p = s0 + i;
@@ -1784,13 +1776,8 @@ __device__ void update_cell_f32(int c, const UpdArgs<float>& a, int step, float*
         if (P.x2o) P.x2o[p] = s.x2o;
       }
       if (SL || (st & ST_KEY)) {
-        int jn, kn;
-        key = bin_one<float>(s.x1, s.x2, pid, step + 1, k, kc, bad, &jn, &kn);
+        key = bin_one<float>(s.x1, s.x2, pid, step + 1, k, kc, bad);
         if constexpr (!SL) a.key_out[p] = key;
-        // its quadrant in the new cell, as the nodal deposit counts it
-        // (left of / below the centre: the threshold is the smallest float
-        // at or above the centre)
-        if (a.qc) quad = (s.x1 < a.qtx[jn] ? 0 : 1) + (s.x2 < a.qty[kn] ? 0 : 2);
       }
     }
     if constexpr (SL) {
@@ -1799,31 +1786,13 @@ __device__ void update_cell_f32(int c, const UpdArgs<float>& a, int step, float*
       // rank among them on top
       const int lane = threadIdx.x & 31;
       const unsigned am = __ballot_sync(FULL, act);
-      unsigned peers = 0;
-      int leader = 0, slot = 0;
       if (act) {
-        peers = __match_any_sync(am, key);
-        leader = __ffs(peers) - 1;
+        const unsigned peers = __match_any_sync(am, key);
+        const int leader = __ffs(peers) - 1;
         int base = 0;
         if (lane == leader) base = atomicAdd(&a.dcur[key], __popc(peers));
         base = __shfl_sync(peers, base, leader);
-        slot = base + __popc(peers & ((1u << lane) - 1u));
-      }
-      if (a.qc) {
-        // quadrant counts of the same groups, split by ballots
-        const unsigned q1 = __ballot_sync(FULL, act && quad == 1), q2 = __ballot_sync(FULL, act && quad == 2),
-                       q3 = __ballot_sync(FULL, act && quad == 3);
-        if (act && lane == leader) {
-          const int n1 = __popc(peers & q1), n2 = __popc(peers & q2), n3 = __popc(peers & q3);
-          const int n0 = __popc(peers) - n1 - n2 - n3;
-          int32_t* qk = a.qc + 4 * (size_t)key;
-          if (n0) atomicAdd(qk, n0);
-          if (n1) atomicAdd(qk + 1, n1);
-          if (n2) atomicAdd(qk + 2, n2);
-          if (n3) atomicAdd(qk + 3, n3);
-        }
-      }
-      if (act) {
+        const int slot = base + __popc(peers & ((1u << lane) - 1u));
         const int r0 = a.doff[key], capc = a.doff[key + 1] - r0;
         if (slot < capc) {
           store_state(a.d, (int64_t)r0 + slot, s, pid);
@@ -1834,9 +1803,7 @@ __device__ void update_cell_f32(int c, const UpdArgs<float>& a, int step, float*
         }
       }
     } else if (st & ST_KEY) {
-      // with quadrant counting the cell's count is their sum (read by the scan)
-      if (a.qc) count_key(a.qc, 4 * key + quad, act);
-      else count_key(a.cnt_next, key, act);
+      count_key(a.cnt_next, key, act);
     }
   }
   raise_status(a.status, bad);
@@ -1908,7 +1875,6 @@ static inline int grid_for(int64_t n, int block, int max_blocks) {
 
 template <typename real> static int bin_impl(Session& s, int bin_step) {
   PT<real> p = pt<real>(s.P[s.cur]);
-  s.qc_ready = false;  // the quadrant counts follow the particle pass's keys only
   // every key is recomputed: counts start from zero, whatever was pending
   cudaMemsetAsync(s.cnt_next, 0, (size_t)s.C * sizeof(int32_t), s.stream);
   k_bin<real><<<grid_for(s.N, 256, s.num_sms * 8), 256, 0, s.stream>>>(p, s.N, s.k, bin_step, s.key, s.cnt_next,
@@ -1917,14 +1883,14 @@ template <typename real> static int bin_impl(Session& s, int bin_step) {
 }
 int launch_bin(Session& s, int bin_step) { return s.prec == MCPM_FP32 ? bin_impl<float>(s, bin_step) : bin_impl<double>(s, bin_step); }
 
-static void scan_launch(Session& s, const int32_t* src, const int32_t* qc, int32_t* off, int32_t* noff) {
+static void scan_launch(Session& s, const int32_t* src, int32_t* off, int32_t* noff) {
   const int nblk = (s.C + SCAN_T - 1) / SCAN_T;
-  k_scan_blocks<<<nblk, SCAN_T, 0, s.stream>>>(src, qc, s.scan_blk, s.C, s.tune.wcap);
+  k_scan_blocks<<<nblk, SCAN_T, 0, s.stream>>>(src, s.scan_blk, s.C, s.tune.wcap);
   k_scan_totals<<<1, SCAN_T, 0, s.stream>>>(s.scan_blk, nblk, s.wl, s.work, s.use_slotted ? s.ovf_n : nullptr,
                                             s.ovf_par);
   ScanOut o;
   o.cnt_next = s.cnt_next; o.cursor = s.cursor; o.dcur = s.dcur;
-  o.qc = qc; o.src = src;
+  o.src = src;
   o.cnt = s.cnt; o.off = off; o.noff = noff; o.doff = s.use_slotted ? s.doff : nullptr;
   o.list_small = s.list_small; o.list_big = s.list_big;
   o.blk = s.scan_blk; o.C = s.C; o.wcap = s.tune.wcap;
@@ -1932,16 +1898,14 @@ static void scan_launch(Session& s, const int32_t* src, const int32_t* qc, int32
 }
 
 int launch_scan(Session& s) {
-  // the particle pass that binned the current keys counted quadrants only
-  const int32_t* qc = s.qc_ready ? lr2d_quad_next(s) : nullptr;
-  scan_launch(s, s.cnt_next, qc, s.off, nullptr);
+  scan_launch(s, s.cnt_next, s.off, nullptr);
   return 3;
 }
 
 // the scan of a slotted layout: counts from the slot counters, the region
 // bases stay (off), the packed offsets go to noff for the repair
 int launch_scan_slotted(Session& s) {
-  scan_launch(s, s.dcur, nullptr, nullptr, s.noff);
+  scan_launch(s, s.dcur, nullptr, s.noff);
   return 3;
 }
 
@@ -1950,11 +1914,13 @@ template <typename real> static int repair_impl(Session& s, bool force) {
   const int32_t* ovn = s.ovf_n + (1 - s.ovf_par);  // the counter of the pass that made the layout
   const int g = s.num_sms * 4;
   if (force) {
-    k_pack<real><<<g, 256, 0, s.stream>>>(src, oth, ov, s.ovf_key, ovn, s.off, s.cnt, s.noff, s.cursor, s.C);
+    k_pack<real><<<g, 256, 0, s.stream>>>(src, oth, ov, s.ovf_key, ovn, s.off, s.cnt, s.noff, s.cursor, s.C,
+                                          s.status);
     return 1;
   }
   k_relocate<real><<<g, 256, 0, s.stream>>>(src, ovn, s.off, s.cnt, s.noff, s.cursor, s.ovf_n + OVF_SPARE, s.C);
-  k_relocate_tail<real><<<g, 256, 0, s.stream>>>(src, ov, s.ovf_key, ovn, s.noff, s.cursor, s.off, s.C);
+  k_relocate_tail<real><<<g, 256, 0, s.stream>>>(src, ov, s.ovf_key, ovn, s.noff, s.cnt, s.cursor, s.off, s.C,
+                                                 s.status);
   return 2;
 }
 int launch_repair(Session& s) { return s.prec == MCPM_FP32 ? repair_impl<float>(s, false) : repair_impl<double>(s, false); }
@@ -2025,9 +1991,6 @@ template <typename real> static int update_impl(Session& s, uint32_t stages, int
   a.bcap = s.tune.bcap;
   a.Vn = lr2d_potential(s);
   a.kc = make_kc<real>(s.k);
-  a.qc = nullptr;
-  a.qtx = a.qty = nullptr;
-  if (sizeof(real) == 4 && s.qc_fuse_now) lr2d_quad_fuse(s, &a.qc, &a.qtx, &a.qty);
   a.d = pt<real>(s.P[1 - s.cur]);
   a.doff = s.doff;
   a.dcur = s.dcur;

@@ -73,7 +73,6 @@ struct LR2D {
   double lambda2vol;                  // bst^2 vol, the mass coefficient of the operator
   double near1, near2;                // the near-field constants of src/FEM.cpp:491-496
   int iters;                          // refinement passes
-  int32_t* qc_next = nullptr;  // [C][4] quadrant counts accumulated by the FP32 particle pass
   float *qtx = nullptr, *qty = nullptr;  // [N0], [N1] cell-centre thresholds (smallest float >= centre)
   int* wall = nullptr;      // [n_wall] ids of the wall nodes
   int n_wall;
@@ -123,6 +122,41 @@ __global__ void k_quadrants(DevConsts k, const int32_t* off, const int32_t* cnt,
       for (int t = 0; t < 4; ++t) q[t] += __popc(__ballot_sync(FULL, quad == t));
     }
     if (lane < 4) qc[(size_t)c * 4 + lane] = q[lane];
+  }
+}
+
+// The FP32 sessions' quadrant counts: the same comparison against the
+// cell-centre thresholds (the smallest float at or above each centre),
+// four particles per lane in flight and the counts summed by warp
+// reductions.
+__global__ void k_quadrants_f32(DevConsts k, const int32_t* off, const int32_t* cnt, const float* x1, const float* x2,
+                                const float* qtx, const float* qty, int32_t* qc) {
+  const int lane = threadIdx.x & 31;
+  const int warps = (gridDim.x * blockDim.x) >> 5;
+  for (int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < k.C; c += warps) {
+    const float tx = qtx[c % k.N0], ty = qty[c / k.N0];
+    const int64_t s0 = off[c];
+    const int n = cnt[c];
+    int q1 = 0, q2 = 0, q3 = 0, m = 0;
+    for (int i = lane; i < n; i += 128) {
+      float a[4], b[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const bool in = i + 32 * u < n;
+        a[u] = in ? x1[s0 + i + 32 * u] : 0.f;
+        b[u] = in ? x2[s0 + i + 32 * u] : 0.f;
+        if (in) {
+          const int q = (a[u] < tx ? 0 : 1) + (b[u] < ty ? 0 : 2);
+          q1 += q == 1; q2 += q == 2; q3 += q == 3;
+          ++m;
+        }
+      }
+    }
+    q1 = __reduce_add_sync(0xffffffffu, q1);
+    q2 = __reduce_add_sync(0xffffffffu, q2);
+    q3 = __reduce_add_sync(0xffffffffu, q3);
+    m = __reduce_add_sync(0xffffffffu, m);
+    if (lane == 0) *reinterpret_cast<int4*>(qc + (size_t)c * 4) = make_int4(m - q1 - q2 - q3, q1, q2, q3);
   }
 }
 
@@ -535,7 +569,7 @@ int lr2d_setup(Session& s) {
             A((void**)&t->V, (size_t)t->nn * 8) && A((void**)&t->nnd, (size_t)k.C * 4 * 8) &&
             A((void**)&t->qc, (size_t)k.C * 4 * 4);
   if (ok && s.prec == MCPM_FP32) {
-    // the particle pass counts quadrants of the new positions: x < the
+    // the FP32 quadrant pass compares positions with thresholds: x < the
     // centre of the column / row in exact arithmetic <=> x < the smallest
     // float at or above it (the comparison k_quadrants makes)
     std::vector<float> tx(k.N0), ty(k.N1);
@@ -549,7 +583,7 @@ int lr2d_setup(Session& s) {
       const float f = (float)cy;
       ty[j] = (double)f >= cy ? f : nextafterf(f, INFINITY);
     }
-    ok = A((void**)&t->qc_next, (size_t)k.C * 4 * 4) && A((void**)&t->qtx, tx.size() * 4) &&
+    ok = A((void**)&t->qtx, tx.size() * 4) &&
          H(t->qtx, tx.data(), tx.size() * 4) && A((void**)&t->qty, ty.size() * 4) && H(t->qty, ty.data(), ty.size() * 4);
   }
   if (ok && mode == MCPM_LR_SCREENED_POISSON) {
@@ -600,7 +634,7 @@ void lr2d_free(Session& s) {
   if (!t) return;
   cudaFree(t->W); cudaFree(t->exc_off); cudaFree(t->exc_i); cudaFree(t->exc_w); cudaFree(t->V); cudaFree(t->nnd);
   cudaFree(t->qc); cudaFree(t->Sx); cudaFree(t->Sy); cudaFree(t->mu); cudaFree(t->B); cudaFree(t->U); cudaFree(t->Bf); cudaFree(t->Tf);
-  cudaFree(t->wall); cudaFree(t->qc_next); cudaFree(t->qtx); cudaFree(t->qty);
+  cudaFree(t->wall); cudaFree(t->qtx); cudaFree(t->qty);
   delete t;
   s.lr2d = nullptr;
 }
@@ -613,15 +647,6 @@ int lr2d_num_nodes(const Session& s) { return s.lr2d ? s.lr2d->nn : 0; }
 static int blocks_for(long n, int bs, int cap) { return (int)std::max(1L, std::min((n + bs - 1) / bs, (long)cap)); }
 
 int32_t* lr2d_quadrants(Session& s) { return s.lr2d ? s.lr2d->qc : nullptr; }
-bool lr2d_quad_fuse(Session& s, int32_t** qc, const float** qtx, const float** qty) {
-  LR2D* t = s.lr2d;
-  if (!t || !t->qc_next) return false;
-  *qc = t->qc_next;
-  *qtx = t->qtx;
-  *qty = t->qty;
-  return true;
-}
-int32_t* lr2d_quad_next(Session& s) { return s.lr2d ? s.lr2d->qc_next : nullptr; }
 double* lr2d_node_density_mut(Session& s) { return s.lr2d ? s.lr2d->nnd : nullptr; }
 
 // nodal densities from given quadrant counts (training snapshots)
@@ -639,16 +664,11 @@ int launch_node_density(Session& s) {
   // with the network attached the deposit also writes the network's input
   __nv_bfloat16* xin = s.sur ? s.sur->xin : nullptr;
   s.sur_xin_ready = xin != nullptr;
-  if (s.qc_ready && t->qc_next) {
-    // the previous particle pass counted the quadrants of these positions
-    k_node_density<<<blocks_for(4L * s.C, 256, s.num_sms * 16), 256, 0, s.stream>>>(
-        s.k, t->qc_next, t->nnd, s.prec == MCPM_FP64, xin, s.cnt);
-    return 1;
-  }
   const int g = blocks_for((long)s.C * 32, 256, s.num_sms * 16);
   if (s.prec == MCPM_FP32) {
     const PBuf& P = s.P[s.cur];
-    k_quadrants<float><<<g, 256, 0, s.stream>>>(s.k, s.off, s.cnt, (const float*)P.x1, (const float*)P.x2, t->qc);
+    k_quadrants_f32<<<g, 256, 0, s.stream>>>(s.k, s.off, s.cnt, (const float*)P.x1, (const float*)P.x2, t->qtx,
+                                             t->qty, t->qc);
   } else {
     const PBuf& P = s.P[s.cur];
     k_quadrants<double><<<g, 256, 0, s.stream>>>(s.k, s.off, s.cnt, (const double*)P.x1, (const double*)P.x2, t->qc);

@@ -341,7 +341,6 @@ static int leave_slotted(mcpm_session* s) {
   s->slotted = false;
   s->sorted = true;
   s->keys_current = false;
-  s->qc_ready = false;
   return after_launch(s, n, "compact");
 }
 
@@ -531,15 +530,8 @@ static int step_once(mcpm_session* s, uint32_t stages) {
   if (m == MCPM_MODEL_ESMC) n += T_ESMC(launch_esmc(*s));
   if (branch) cudaStreamWaitEvent(s->stream, s->ev_join, 0);
   else if (s->cfg.long_range != MCPM_LR_NONE) n += long_range_force(s);
-  // FP32 sessions with nodal densities: the particle pass also counts the
-  // quadrants of the new positions, which the next step's deposit reads
-  int32_t* qn = lr2d_quad_next(*s);
-  s->qc_fuse_now = qn && (stages & ST_KEY) && (s->lr2d_nodes_needed());
-  if (s->qc_fuse_now) cudaMemsetAsync(qn, 0, (size_t)s->C * 4 * sizeof(int32_t), s->stream);
   const bool slot = s->use_slotted && (stages & ST_KEY);
   n += T_UPD(launch_update(*s, stages, 0, slot));
-  s->qc_ready = s->qc_fuse_now;
-  s->qc_fuse_now = false;
   k_step_advance<<<1, 1, 0, s->stream>>>(s->dstep);
   ++n;
   s->step++;
@@ -589,7 +581,7 @@ static int capture_pair(mcpm_session* s, uint32_t stages, uint64_t sig) {
   if (rc) return rc;
   const int step0 = s->step, cur0 = s->cur, dval0 = s->dstep_val, par0 = s->ovf_par;
   const int64_t launches0 = s->launches;
-  const bool keys0 = s->keys_current, sorted0 = s->sorted, slotted0 = s->slotted, qc0 = s->qc_ready;
+  const bool keys0 = s->keys_current, sorted0 = s->sorted, slotted0 = s->slotted;
   int32_t *off0 = s->off, *doff0 = s->doff, *noff0 = s->noff;
   cudaGraph_t g = nullptr;
   if (cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
@@ -601,7 +593,7 @@ static int capture_pair(mcpm_session* s, uint32_t stages, uint64_t sig) {
   n += step_once(s, stages);
   cudaError_t e = cudaStreamEndCapture(s->stream, &g);
   s->step = step0; s->cur = cur0; s->dstep_val = dval0; s->launches = launches0; s->ovf_par = par0;
-  s->keys_current = keys0; s->sorted = sorted0; s->needs_rebin = false; s->slotted = slotted0; s->qc_ready = qc0;
+  s->keys_current = keys0; s->sorted = sorted0; s->needs_rebin = false; s->slotted = slotted0;
   s->off = off0; s->doff = doff0; s->noff = noff0;
   if (e == cudaSuccess && g) e = cudaGraphInstantiate(&s->graph, g, 0);
   if (g) cudaGraphDestroy(g);

@@ -113,16 +113,24 @@ def test_fused_step_fp_dense_2d_vlasov(cuda_ok, lr):
         assert err <= 1e-9, (k, err)
 
 
-def test_fused_quadrant_counts_equal_the_deposit_pass(cuda_ok):
-    """FP32 sessions count the quadrants of the new positions inside the
-    particle pass; the next deposit must equal the one the separate
-    quadrant pass makes from the same positions (exact: counts x Fn/vol)."""
+def test_fp32_quadrant_counts_after_fused_steps(cuda_ok):
+    """FP32 sessions count cell quadrants against float thresholds (the
+    smallest float at or above each cell centre).  After fused steps (a
+    slotted layout) the deposit must equal a fresh session's from the same
+    positions, and the FP64 session's exact comparison in double (counts x
+    Fn/vol: equal up to the FP64 deposit's sequential sum)."""
     cfg, parts = _box(mcpm.LR_SCREENED_POISSON, prec=mcpm.FP32, n_cells=(24, 20), ppc=60, model=mcpm.MODEL_FP_DENSE)
     s = _session(cfg, parts)
     s.step(3)
-    s.cell_update()  # bins by the particle pass's keys: the fused counts
-    fused = s.get_node_density()
+    s.cell_update()
+    after = s.get_node_density()
     g = s.download()
     r = _session(cfg, g)  # the same positions, binned and counted afresh
     r.cell_update()
-    assert np.array_equal(fused, r.get_node_density())
+    assert np.array_equal(after, r.get_node_density())
+    cfg64 = cfg.copy()
+    cfg64.precision = mcpm.FP64
+    r64 = _session(cfg64, g)
+    r64.cell_update()
+    ref = r64.get_node_density()
+    assert np.max(np.abs(after - ref)) <= 1e-12 * np.max(np.abs(ref))
