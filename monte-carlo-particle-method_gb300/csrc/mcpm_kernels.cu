@@ -568,17 +568,133 @@ __device__ void moments_cell(int c, const MomArgs<real>& a, Acc<real>* red) {
   }
 }
 
+// Sums of K floats over a tile of TILE threads (one warp or the block):
+// per-lane running sums combined by an XOR butterfly (pairwise), every
+// thread gets the totals.  red holds K * TILE / 32 floats.
+template <int K, int TILE>
+__device__ __forceinline__ void tile_sum_f32(float (&v)[K], float* red) {
+#pragma unroll
+  for (int q = 0; q < K; ++q)
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v[q] += __shfl_xor_sync(FULL, v[q], o);
+  if constexpr (TILE > 32) {
+    constexpr int W = TILE / 32;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) {
+#pragma unroll
+      for (int q = 0; q < K; ++q) red[q * W + warp] = v[q];
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < K; ++q) {
+      float t = 0.f;
+#pragma unroll
+      for (int w = 0; w < W; ++w) t += red[q * W + w];
+      v[q] = t;
+    }
+  }
+}
+
+// The FP32 moment pass without compensation: the cell mean from plain
+// per-lane sums (butterfly), then one pass over the cell's velocities (from
+// L1) with the 29 products in plain per-lane float sums -- P from the
+// centred velocities, M3 = P c, M4 = P e, M5 = c e^2 -- and a reduce-scatter
+// across the warp (recursive halving: 31 shuffles leave sum j on lane j),
+// across the block's warps through shared memory for block-sized cells.
+// Each lane sums n / TILE terms; the sums enter the FP64 finalisation as
+// doubles.
+template <int TILE>
+__device__ void moments_cell_f32(int c, const MomArgs<float>& a, float* red) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int t = (TILE == 32) ? lane : threadIdx.x;
+  const int s0 = a.off[c], n = a.cnt[c];
+  const int C = a.k.C;
+  float u[3] = {0.f, 0.f, 0.f};
+  for (int i = t; i < n; i += TILE) {
+    u[0] += a.U1[s0 + i];
+    u[1] += a.U2[s0 + i];
+    u[2] += a.U3[s0 + i];
+  }
+  tile_sum_f32<3, TILE>(u, red);
+  float m0 = 0.f, m1 = 0.f, m2 = 0.f;
+  if (n > 0) {
+    const float w = (float)n;
+    m0 = u[0] / w; m1 = u[1] / w; m2 = u[2] / w;
+  }
+  float v[32];
+#pragma unroll
+  for (int j = 0; j < 32; ++j) v[j] = 0.f;
+  for (int i = t; i < n; i += TILE) {
+    const float c1 = a.U1[s0 + i] - m0, c2 = a.U2[s0 + i] - m1, c3 = a.U3[s0 + i] - m2;
+    const float e = fmaf(c3, c3, fmaf(c2, c2, c1 * c1));
+    const float p11 = c1 * c1, p12 = c1 * c2, p13 = c1 * c3, p22 = c2 * c2, p23 = c2 * c3, p33 = c3 * c3;
+    const float e2 = e * e;
+    v[0] += c1; v[1] += c2; v[2] += c3;
+    v[3] += p11; v[4] += p12; v[5] += p13; v[6] += p22; v[7] += p23; v[8] += p33;
+    v[9] = fmaf(p11, c1, v[9]); v[10] = fmaf(p11, c2, v[10]); v[11] = fmaf(p11, c3, v[11]);
+    v[12] = fmaf(p12, c2, v[12]); v[13] = fmaf(p12, c3, v[13]); v[14] = fmaf(p13, c3, v[14]);
+    v[15] = fmaf(p22, c2, v[15]); v[16] = fmaf(p22, c3, v[16]); v[17] = fmaf(p23, c3, v[17]);
+    v[18] = fmaf(p33, c3, v[18]);
+    v[19] = fmaf(p11, e, v[19]); v[20] = fmaf(p12, e, v[20]); v[21] = fmaf(p13, e, v[21]);
+    v[22] = fmaf(p22, e, v[22]); v[23] = fmaf(p23, e, v[23]); v[24] = fmaf(p33, e, v[24]);
+    v[25] = fmaf(c1, e2, v[25]); v[26] = fmaf(c2, e2, v[26]); v[27] = fmaf(c3, e2, v[27]);
+    v[28] += e;
+  }
+  // reduce-scatter over the warp: after the level of width d a lane keeps
+  // the half of its values whose index bit matches its lane bit
+#pragma unroll
+  for (int d = 16, W = 32; d >= 1; d >>= 1, W >>= 1) {
+    const bool up = lane & d;
+#pragma unroll
+    for (int j = 0; j < W / 2; ++j) {
+      const float send = up ? v[j] : v[W / 2 + j];
+      const float keep = up ? v[W / 2 + j] : v[j];
+      v[j] = keep + __shfl_xor_sync(FULL, send, d);
+    }
+  }
+  float tot = v[0];  // sum number `lane`
+  if constexpr (TILE > 32) {
+    __syncthreads();
+    red[warp * 32 + lane] = tot;
+    __syncthreads();
+    if (warp == 0) {
+      tot = 0.f;
+#pragma unroll
+      for (int w = 0; w < TILE / 32; ++w) tot += red[w * 32 + lane];
+    }
+  }
+  if (TILE == 32 || warp == 0) {
+    double* cl = a.cell;
+    if (lane < 29) cl[(size_t)(CFI_RAW + lane) * C + c] = (double)tot;
+    else if (lane == 29) cl[(size_t)(MCPM_CF_U_SPACE + 0) * C + c] = (double)m0;
+    else if (lane == 30) cl[(size_t)(MCPM_CF_U_SPACE + 1) * C + c] = (double)m1;
+    else cl[(size_t)(MCPM_CF_U_SPACE + 2) * C + c] = (double)m2;
+    if (lane == 0) cl[(size_t)MCPM_CF_NUM_INSIDE * C + c] = (double)n;
+  }
+}
+
 // blocks of 256 threads resident per SM in the FP32 moment pass (4: 64
 // registers, the two-group accumulation fits without spilling)
 #ifndef MCPM_MOM_MINB
 #define MCPM_MOM_MINB 4
 #endif
+#ifndef MCPM_MOM_PLAIN
+#define MCPM_MOM_PLAIN 1
+#endif
 template <typename real>
 __global__ void __launch_bounds__(256, sizeof(real) == 4 ? MCPM_MOM_MINB : 1) k_moments(MomArgs<real> a) {
   __shared__ Acc<real> red[29 * 8];
-  schedule_cells(
-      a.list_big, a.list_small, a.wl, a.work, WK_MOM_BIG, WK_MOM_SMALL,
-      [&](int c) { moments_cell<real, 256>(c, a, red); }, [&](int c) { moments_cell<real, 32>(c, a, red); });
+  if constexpr (sizeof(real) == 4 && MCPM_MOM_PLAIN) {
+    float* rf = reinterpret_cast<float*>(red);
+    schedule_cells(
+        a.list_big, a.list_small, a.wl, a.work, WK_MOM_BIG, WK_MOM_SMALL,
+        [&](int c) { moments_cell_f32<256>(c, a, rf); }, [&](int c) { moments_cell_f32<32>(c, a, rf); });
+  } else {
+    schedule_cells(
+        a.list_big, a.list_small, a.wl, a.work, WK_MOM_BIG, WK_MOM_SMALL,
+        [&](int c) { moments_cell<real, 256>(c, a, red); }, [&](int c) { moments_cell<real, 32>(c, a, red); });
+  }
 }
 
 // ===================================================== per-cell solves
@@ -1548,33 +1664,6 @@ __device__ void update_cell(int c, const UpdArgs<real>& a, int step, real* xs, i
 #define MCPM_STR(x) MCPM_STR2(x)
 #define UPD_UNROLL _Pragma(MCPM_STR(unroll MCPM_UPD_UNROLL))
 
-// Sums of K floats over a tile of TILE threads (one warp or the block):
-// per-lane running sums combined by an XOR butterfly (pairwise), every
-// thread gets the totals.  red holds K * TILE / 32 floats.
-template <int K, int TILE>
-__device__ __forceinline__ void tile_sum_f32(float (&v)[K], float* red) {
-#pragma unroll
-  for (int q = 0; q < K; ++q)
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v[q] += __shfl_xor_sync(FULL, v[q], o);
-  if constexpr (TILE > 32) {
-    constexpr int W = TILE / 32;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    __syncthreads();
-    if (lane == 0) {
-#pragma unroll
-      for (int q = 0; q < K; ++q) red[q * W + warp] = v[q];
-    }
-    __syncthreads();
-#pragma unroll
-    for (int q = 0; q < K; ++q) {
-      float t = 0.f;
-#pragma unroll
-      for (int w = 0; w < W; ++w) t += red[q * W + w];
-      v[q] = t;
-    }
-  }
-}
 
 // The FP32 particle pass: the stages of update_cell for float state, with
 // plain FP32 per-lane sums of the whitening and energy terms combined
