@@ -72,6 +72,9 @@ struct DevConsts {
   // box; its coefficient (phi for the direct path, ast for screened Poisson)
   int lr2d;
   double lr_coef;
+  // quotients of constants for the FP32 sessions' per-cell solve (formed
+  // once on the host): m/(3 kb), m/kb, kb/m, 1/dy, 1/m
+  double q_T, q_m_kb, q_kb_m, q_idy, q_im;
   // float copies for the FP32 kernels
   float f_dx, f_dy, f_L0, f_L1, f_dt, f_sigma, f_m, f_kb, f_Tw[4], f_Uw[4], f_idx, f_idy, f_eps_x, f_eps_y;
 };

@@ -841,8 +841,11 @@ __global__ void __launch_bounds__(128) k_solve(DevConsts k, double* cell, float*
   for (int j = 0; j < 3; ++j) W(MCPM_CF_MP + j, Mp[j]);
   W(MCPM_CF_DM2, DM2);
   W(MCPM_CF_DM4, DM4);
-  const double T = k.m * DM2 / (3.0 * k.kb);
+  // (the FP32 sessions' variant multiplies by quotients formed once, where
+  // the reference divides)
+  const double T = EXACT ? k.m * DM2 / (3.0 * k.kb) : DM2 * k.q_T;
   const double n = 1 * k.Fn * weight / cell_volume(c, k);
+  const double iT = EXACT ? 0.0 : 1.0 / T;
   double Ycell;
   if (EXACT) {
     Ycell = ycoll(n, k.b);
@@ -855,20 +858,30 @@ __global__ void __launch_bounds__(128) k_solve(DevConsts k, double* cell, float*
   W(CFI_Y, Ycell);
   double gst = R(MCPM_CF_GAMMA_ST);
   if (weight > 1e-14) {
-    gst = -0.001 * (n * k.b * Ycell / (k.kb * T / k.m));
+    gst = EXACT ? -0.001 * (n * k.b * Ycell / (k.kb * T / k.m)) : -0.001 * (n * k.b * Ycell) * (k.q_m_kb * iT);
     W(MCPM_CF_GAMMA_ST, gst);
   }
   uint32_t bad = 0;
   double Lam = R(MCPM_CF_LAMBDA);
   if (weight > 1e-14) {
     double mu = scale_mu(T, k);
-    double tau = 2.0 * mu / (n * k.kb * T);
-    double L = (P[0] - DM2 / 3.0) * ((P[3] - DM2 / 3.0) * (P[5] - DM2 / 3.0) - P[4] * P[4]);
-    L = L - P[1] * (P[1] * (P[5] - DM2 / 3.0) - P[4] * P[2]);
-    L = L + P[2] * (P[1] * P[4] - P[2] * (P[3] - DM2 / 3.0));
-    const double dm4 = EXACT ? pow(DM2, 4.0) : (DM2 * DM2) * (DM2 * DM2);
-    L = -L / (tau * dm4);
-    Lam = L;
+    if (EXACT) {
+      double tau = 2.0 * mu / (n * k.kb * T);
+      double L = (P[0] - DM2 / 3.0) * ((P[3] - DM2 / 3.0) * (P[5] - DM2 / 3.0) - P[4] * P[4]);
+      L = L - P[1] * (P[1] * (P[5] - DM2 / 3.0) - P[4] * P[2]);
+      L = L + P[2] * (P[1] * P[4] - P[2] * (P[3] - DM2 / 3.0));
+      L = -L / (tau * pow(DM2, 4.0));
+      Lam = L;
+    } else {
+      // -det(P - DM2/3) / (tau DM2^4), 1/tau = n kb T / (2 mu)
+      const double d3 = DM2 * (1.0 / 3.0);
+      const double a0 = P[0] - d3, a3 = P[3] - d3, a5 = P[5] - d3;
+      double L = a0 * (a3 * a5 - P[4] * P[4]);
+      L = L - P[1] * (P[1] * a5 - P[4] * P[2]);
+      L = L + P[2] * (P[1] * P[4] - P[2] * a3);
+      const double iD = 1.0 / DM2, iD2 = iD * iD;
+      Lam = -L * (n * k.kb * T / (2.0 * mu)) * (iD2 * iD2);
+    }
     W(MCPM_CF_LAMBDA, Lam);
   }
   double al[9], be[3];
@@ -905,20 +918,34 @@ __global__ void __launch_bounds__(128) k_solve(DevConsts k, double* cell, float*
         }
         double div_U;
         const int last = C - 1;
-        if (C == 1) div_U = 0.0;
-        else if (c == 0) div_U = (Rc(MCPM_CF_U_SPACE + 1, c + 1) - Rc(MCPM_CF_U_SPACE + 1, c)) / k.dy;
-        else if (c == k.N1 - 1 || c == last)
-          div_U = (Rc(MCPM_CF_U_SPACE + 1, c) - Rc(MCPM_CF_U_SPACE + 1, c - 1)) / k.dy;
-        else div_U = (Rc(MCPM_CF_U_SPACE + 1, c + 1) - Rc(MCPM_CF_U_SPACE + 1, c - 1)) / k.dy / 2.0;
+        if (EXACT) {
+          if (C == 1) div_U = 0.0;
+          else if (c == 0) div_U = (Rc(MCPM_CF_U_SPACE + 1, c + 1) - Rc(MCPM_CF_U_SPACE + 1, c)) / k.dy;
+          else if (c == k.N1 - 1 || c == last)
+            div_U = (Rc(MCPM_CF_U_SPACE + 1, c) - Rc(MCPM_CF_U_SPACE + 1, c - 1)) / k.dy;
+          else div_U = (Rc(MCPM_CF_U_SPACE + 1, c + 1) - Rc(MCPM_CF_U_SPACE + 1, c - 1)) / k.dy / 2.0;
+        } else {
+          if (C == 1) div_U = 0.0;
+          else if (c == 0) div_U = (Rc(MCPM_CF_U_SPACE + 1, c + 1) - Rc(MCPM_CF_U_SPACE + 1, c)) * k.q_idy;
+          else if (c == k.N1 - 1 || c == last)
+            div_U = (Rc(MCPM_CF_U_SPACE + 1, c) - Rc(MCPM_CF_U_SPACE + 1, c - 1)) * k.q_idy;
+          else div_U = (Rc(MCPM_CF_U_SPACE + 1, c + 1) - Rc(MCPM_CF_U_SPACE + 1, c - 1)) * (0.5 * k.q_idy);
+        }
         W(MCPM_CF_DIVU, div_U);
         double nbY = n * k.b * Y;
-        double coeff_mu = 3.0 * 1.002 / 5.0 * (nbY * nbY) / (1 + 2.0 * n * k.b * Y / 5.0);
-        double coeff_k = 1.002 * (nbY * nbY) / (1 + 3.0 * n * k.b * Y / 5.0) / 5.0;
         double rhs[12];
         if (!EXACT) {
-          // the same terms with the common factors formed once
-          const double pt3 = (p_crr - 1.0) * trace * (1.0 / 3.0) - w * div_U / (k.m * n);
-          const double cm = (mu_crr - 1.0) + coeff_mu, ck = (k_crr - 1.0) + coeff_k;
+          // the same terms with the common factors formed once and one
+          // division for the two transport corrections:
+          // coeff_mu = 0.6012 x^2 / (1 + 0.4 x), coeff_k = 0.2004 x^2 / (1 + 0.6 x)
+          const double x2 = nbY * nbY, dmu = 1.0 + 0.4 * nbY, dk = 1.0 + 0.6 * nbY;
+          const double id = 1.0 / (dmu * dk);
+          const double coeff_mu = (3.0 * 1.002 / 5.0) * x2 * (dk * id), coeff_k = (1.002 / 5.0) * x2 * (dmu * id);
+          // w div_U / (m n) with w's factor n^2 cancelled
+          const double s2 = k.sigma * k.sigma;
+          const double wmn = (4.0 / 9.0) * 1.7724538509055159 * Y * n * (s2 * s2) * sqrt(k.m * k.kb * T) * k.q_im;
+          const double pt3 = nbY * trace * (1.0 / 3.0) - wmn * div_U;
+          const double cm = 0.4 * nbY + coeff_mu, ck = 0.6 * nbY + coeff_k;
           rhs[0] = cm * dev[0] + pt3 - gst * M4[0];
           rhs[1] = cm * dev[1] - gst * M4[1];
           rhs[2] = cm * dev[2] - gst * M4[2];
@@ -932,6 +959,8 @@ __global__ void __launch_bounds__(128) k_solve(DevConsts k, double* cell, float*
           rhs[10] = ck * mb - gst * M5[1] + gst * (DM2 * mb);
           rhs[11] = ck * mc - gst * M5[2] + gst * (DM2 * mc);
         } else {
+        double coeff_mu = 3.0 * 1.002 / 5.0 * (nbY * nbY) / (1 + 2.0 * n * k.b * Y / 5.0);
+        double coeff_k = 1.002 * (nbY * nbY) / (1 + 3.0 * n * k.b * Y / 5.0) / 5.0;
         rhs[0] = (mu_crr - 1.0) * dev[0] + (p_crr - 1.0) * trace / 3.0 - w * div_U / (k.m * n) + coeff_mu * dev[0] - gst * M4[0];
         rhs[1] = (mu_crr - 1.0) * dev[1] + coeff_mu * dev[1] - gst * M4[1];
         rhs[2] = (mu_crr - 1.0) * dev[2] + coeff_mu * dev[2] - gst * M4[2];
@@ -1000,14 +1029,14 @@ __global__ void __launch_bounds__(128) k_solve(DevConsts k, double* cell, float*
       double Pr = 2.0 / 3.0;
       double Y = (k.model == MCPM_MODEL_FP_DENSE) ? Ycell : 1.0;
       double mu = scale_mu(T, k);
-      double tau = 2.0 * mu / (n * k.kb * T);
       for (int j = 0; j < 6; ++j) rhs[j] = -2.0 * Lam * M4[j];
       if (EXACT) {
+        double tau = 2.0 * mu / (n * k.kb * T);
         rhs[6] = Y * (3.0 / tau - 2.0 * Pr / tau) * Q[0];
         rhs[7] = Y * (3.0 / tau - 2.0 * Pr / tau) * Q[1];
         rhs[8] = Y * (3.0 / tau - 2.0 * Pr / tau) * Q[2];
       } else {
-        const double f = Y * (3.0 - 2.0 * Pr) / tau;
+        const double f = Y * (3.0 - 2.0 * Pr) * (n * k.kb * T / (2.0 * mu));  // Y (3 - 2 Pr) / tau
         rhs[6] = f * Q[0]; rhs[7] = f * Q[1]; rhs[8] = f * Q[2];
       }
       rhs[6] += Lam * (-3.0 * M5[0] + DM2 * Q[0] + 2.0 * (P[0] * Q[0] + P[1] * Q[1] + P[2] * Q[2]));
@@ -1021,17 +1050,18 @@ __global__ void __launch_bounds__(128) k_solve(DevConsts k, double* cell, float*
     // ---------------- Velocity_FP_parallel per-cell constants
     if (ncnt > 1) {
       double mu = scale_mu(T, k);
-      double tau = 2.0 * mu / (n * k.kb * T);
       double Y = (k.model == MCPM_MODEL_FP_DENSE) ? Ycell : 1.0;
-      tau = tau / Y;
       if (EXACT) {
+        double tau = 2.0 * mu / (n * k.kb * T);
+        tau = tau / Y;
         W(CFI_A1, exp(-k.dt / tau));
         W(CFI_A3, sqrt((1.0 - exp(-2.0 * k.dt / tau)) * k.kb * T / (1.0 * k.m)));
         W(CFI_A2, (1.0 - exp(-k.dt / tau)) * tau);
       } else {
+        const double tau = 2.0 * mu / (n * k.kb * T * Y);
         const double e1 = exp(-k.dt / tau);  // exp(-2 dt/tau) = e1^2
         W(CFI_A1, e1);
-        W(CFI_A3, sqrt((1.0 - e1 * e1) * k.kb * T / k.m));
+        W(CFI_A3, sqrt((1.0 - e1 * e1) * T * k.q_kb_m));
         W(CFI_A2, (1.0 - e1) * tau);
       }
     }

@@ -178,6 +178,11 @@ int mcpm_session_create(const mcpm_config* cfg, mcpm_session** out) {
   k.seed = c.seed;
   k.lr2d = (c.long_range != MCPM_LR_NONE && c.direction[0] == 1) ? 1 : 0;
   k.lr_coef = c.long_range == MCPM_LR_DIRECT ? c.phi : c.ast;
+  k.q_T = c.m / (3.0 * c.kb);
+  k.q_m_kb = c.m / c.kb;
+  k.q_kb_m = c.kb / c.m;
+  k.q_idy = 1.0 / k.dy;
+  k.q_im = 1.0 / c.m;
   k.f_dx = (float)k.dx; k.f_dy = (float)k.dy; k.f_L0 = (float)k.L0; k.f_L1 = (float)k.L1;
   k.f_dt = (float)k.dt; k.f_sigma = (float)k.sigma; k.f_m = (float)k.m; k.f_kb = (float)k.kb;
   for (int i = 0; i < 4; ++i) { k.f_Tw[i] = (float)k.Tw[i]; k.f_Uw[i] = (float)k.Uw[i]; }
