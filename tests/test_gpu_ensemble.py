@@ -3,9 +3,12 @@ independent Philox streams (GPU seeds 1..R, oracle seeds 1001..1000+R) from
 the same initial particles, compared on the box moments -- mean velocity
 u_i, temperatures T_ii = <c_i^2>, shear stress P_12 = <c_1 c_2> and heat flux
 q_i = <c_i |c|^2> / 2 -- after a few steps.  Each ensemble mean of the GPU
-must lie within 3 standard errors of the oracle's (the combined standard
-error of the two ensemble means); the test prints every difference in units
-of that error.  The seeds are fixed, so the outcome is reproducible."""
+must lie within 4 standard errors of the oracle's (the combined standard
+error of the two ensemble means): with 9 moments in each of 3 tests a 3-error
+bar would fail about one run in 14 by chance, 4 errors one in 600; the test
+prints every difference in units of that error.  The seeds are fixed; the
+GPU's in-cell particle order (atomic slot assignment) is not, so the GPU
+ensemble varies slightly from run to run."""
 import numpy as np
 import pytest
 
@@ -61,16 +64,16 @@ def _compare(gpu, orc, label):
         if se[q] < 1e-9 * max(1.0, abs(orc[:, q].mean())):
             assert abs(d[q]) < 1e-5 * max(1.0, abs(orc[:, q].mean())), (label, NAMES[q], d[q])
         else:
-            assert abs(z[q]) <= 3.0, (label, NAMES[q], z[q])
+            assert abs(z[q]) <= 4.0, (label, NAMES[q], z[q])
     return z
 
 
 @pytest.mark.parametrize("prec", [mcpm.FP64, mcpm.FP32])
 def test_fp_relaxation_ensemble_matches_oracle(cuda_ok, prec):
     """Enskog-FP homogeneous relaxation (T_x = 2, T_y = T_z = 0.5, n b = 0.3):
-    the anisotropy relaxes at the rate of the cubic drift; 24 replicas of
+    the anisotropy relaxes at the rate of the cubic drift; 32 replicas of
     10,000 particles, 8 steps."""
-    R, steps = 24, 8
+    R, steps = 32, 8
     cfg, parts = W.homogeneous_relaxation_1d(n_cells=50, ppc=200, precision=prec)
     gpu = np.array([_gpu_run(cfg, parts, 1 + r, steps) for r in range(R)])
     orc = np.array([_oracle_run(cfg, parts, 1001 + r, steps) for r in range(R)])
@@ -81,8 +84,8 @@ def test_fp_relaxation_ensemble_matches_oracle(cuda_ok, prec):
 
 def test_esmc_ensemble_matches_oracle(cuda_ok):
     """ESMC hard-sphere collisions with a hot diffuse wall (the Couette box of
-    the benchmark's ESMC workload at 8 x 8 cells): 24 replicas, 6 steps."""
-    R, steps = 24, 6
+    the benchmark's ESMC workload at 8 x 8 cells): 48 replicas, 6 steps."""
+    R, steps = 48, 6
     cfg, parts = W.esmc_box_2d(n_cells=(8, 8), precision=mcpm.FP32)
     gpu = np.array([_gpu_run(cfg, parts, 1 + r, steps) for r in range(R)])
     orc = np.array([_oracle_run(cfg, parts, 1001 + r, steps) for r in range(R)])
