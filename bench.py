@@ -50,8 +50,10 @@ sys.path.insert(0, PKG)
 METRIC = "particle-steps/s at 16M particles: plain vs surrogate-Vlasov, moment err <=1%"
 UNIT = "particle-steps/s"
 # algorithmic bytes per particle of one launch (FP32 state, 2-D positions):
-#  update: read x1 x2 U1 U2 U3 pid (24 B), write x1 x2 U1 U2 U3 key (24 B)
-#  moments: read U1 U2 U3 (12 B); scatter (not credited): read 28 B, write 24 B
+#  update: read x1 x2 U1 U2 U3 pid (24 B), write x1 x2 U1 U2 U3 pid into the
+#  new cell's region of the slotted layout (24 B; FP64 sessions write the key)
+#  moments: read U1 U2 U3 (12 B); scatter (FP64 sessions, not credited): read
+#  28 B, write 24 B
 #  esmc: read x1 x2 U1 U2 U3 (20 B), write U1 U2 U3 (12 B)
 ALG_BYTES = {"update": 48, "moments": 12, "scatter": 52, "esmc": 32}
 
@@ -560,7 +562,7 @@ def main():
     if args.impl == "reference":
         # one reference step of a 16M workload is ~0.5-5 s on 16 cores
         args.steps = min(args.steps, 60 if args.workload not in ("surrogate16m", "vlasov16m") else 4)
-        args.warmup = min(args.warmup, 1)
+        args.warmup = min(args.warmup, 3)
         run_reference(args)
     else:
         run_mcpm(args)
