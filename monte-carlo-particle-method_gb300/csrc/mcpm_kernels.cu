@@ -1867,17 +1867,20 @@ __device__ void update_cell_f32(int c, const UpdArgs<float>& a, int step, float*
         }
       }
       // apply_BC: the box's wall type fixed at compile time where the
-      // launch knows it (PB), else the run-time dispatch
-      auto bc = [&](int call) {
+      // launch knows it (PB), else the run-time dispatch; true when the
+      // call may have moved the particle
+      auto bc = [&](int call) -> bool {
         if constexpr (PB == MCPM_PROBLEM_CLOSED_BOX) {
           // the first-pass tests of BC_specular_reflection: a particle that
           // triggers none of them is left as it is
           const bool r1 = k.dir0 == 1 && (s.x1 - kc.L0 > -1e-16f || s.x1 < 1e-16f);
           const bool r2 = k.dir1 == 1 && (s.x2 - kc.L1 > -1e-16f || s.x2 < 1e-16f);
           if (r1 || r2) bc_specular<float>(s, k, kc, bad);
+          return r1 || r2;
         }
         else if constexpr (PB == MCPM_PROBLEM_PERIODIC) bc_periodic<float>(s, k, kc);
         else apply_bc<float>(s, a.bc_call_base + call, pid, step, k, kc, bad);
+        return true;
       };
       if (st & ST_BC1) bc(0);
       if (st & ST_OLD) { s.x1o = s.x1; s.x2o = s.x2; }
@@ -1885,8 +1888,10 @@ __device__ void update_cell_f32(int c, const UpdArgs<float>& a, int step, float*
         if (k.dir0 == 1) s.x1 = fmaf(dtr, s.u1, s.x1);
         if (k.dir1 == 1) s.x2 = fmaf(dtr, s.u2, s.x2);
       }
-      if (st & ST_BC2) bc(1);
-      if (st & ST_BC3) bc(2);
+      // the third call sees the second's position: between specular walls
+      // it can only act where the second reflected the particle
+      const bool moved = (st & ST_BC2) ? bc(1) : true;
+      if ((st & ST_BC3) && (PB != MCPM_PROBLEM_CLOSED_BOX || moved)) bc(2);
       if constexpr (!SL) {
         P.U1[p] = s.u1; P.U2[p] = s.u2; P.U3[p] = s.u3;
         if (P.x1) P.x1[p] = s.x1;
