@@ -235,5 +235,10 @@ int lr2d_num_nodes(const Session& s);
 int sync_dstep(Session& s);
 int launch_convert_in(Session& s, int64_t n);
 int launch_convert_out(Session& s, int64_t n);
+// one staged upload field (0..4: x1 x2 U1 U2 U3; field 2 also sets the ids)
+// on stream st
+int launch_convert_field(Session& s, int field, int64_t n, cudaStream_t st);
+// the staging of a download straight from a slotted layout (FP32 sessions)
+int launch_convert_out_slotted(Session& s);
 
 }  // namespace mcpm

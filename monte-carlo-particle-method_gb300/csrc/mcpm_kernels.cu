@@ -1977,6 +1977,15 @@ __global__ void k_convert_in(PT<real> p, const double* stage, int64_t n, int64_t
     if (p.x2o) p.x2o[i] = p.x2[i];
   }
 }
+// one staged field into the state's precision (uploads: each field's
+// conversion overlaps the copy of the next), and the particle ids
+template <typename real>
+__global__ void k_convert_field(real* dst, const double* src, int32_t* pid, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    dst[i] = (real)src[i];
+    if (pid) pid[i] = (int32_t)i;
+  }
+}
 template <typename real>
 __global__ void k_convert_out(PT<real> p, double* stage, int64_t n, int64_t cap) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
@@ -1987,6 +1996,31 @@ __global__ void k_convert_out(PT<real> p, double* stage, int64_t n, int64_t cap)
     stage[3 * cap + q] = (double)p.U2[i];
     stage[4 * cap + q] = (double)p.U3[i];
   }
+}
+
+// The same from a slotted layout as the particle pass left it: each cell's
+// first min(slots taken, capacity) particles of its region (bases off, the
+// counts still in the slot counters), then the overflow entries; the layout
+// itself stays as it is.
+template <typename real>
+__global__ void k_convert_out_slotted(PT<real> p, PT<real> ovf, const int32_t* ovf_n, const int32_t* off,
+                                      const int32_t* dcur, int C, double* stage, int64_t cap) {
+  const int lane = threadIdx.x & 31;
+  const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x, nt = (int64_t)gridDim.x * blockDim.x;
+  auto put = [&](const PT<real>& src, int64_t i) {
+    const int q = src.pid[i];
+    stage[q] = src.x1 ? (double)src.x1[i] : 0.0;
+    stage[cap + q] = (double)src.x2[i];
+    stage[2 * cap + q] = (double)src.U1[i];
+    stage[3 * cap + q] = (double)src.U2[i];
+    stage[4 * cap + q] = (double)src.U3[i];
+  };
+  for (int64_t c = tid >> 5; c < C; c += nt >> 5) {
+    const int s0 = off[c], m = min(dcur[c], off[c + 1] - s0);
+    for (int i = lane; i < m; i += 32) put(p, (int64_t)s0 + i);
+  }
+  const int n_ovf = *ovf_n;
+  for (int64_t e = tid; e < n_ovf; e += nt) put(ovf, e);
 }
 
 // ============================================================ launchers
@@ -2175,6 +2209,22 @@ template <typename real> static int conv_out_impl(Session& s, int64_t n) {
   return 1;
 }
 int launch_convert_out(Session& s, int64_t n) { return s.prec == MCPM_FP32 ? conv_out_impl<float>(s, n) : conv_out_impl<double>(s, n); }
+template <typename real> static int conv_field_impl(Session& s, int f, int64_t n, cudaStream_t st) {
+  const PBuf& b = s.P[s.cur];
+  void* dsts[5] = {b.x1, b.x2, b.U1, b.U2, b.U3};
+  if (!dsts[f]) return 0;
+  k_convert_field<real><<<grid_for(n, 256, s.num_sms * 8), 256, 0, st>>>(
+      (real*)dsts[f], s.stage + (size_t)f * s.cap, f == 2 ? b.pid : nullptr, n);
+  return 1;
+}
+int launch_convert_field(Session& s, int field, int64_t n, cudaStream_t st) {
+  return s.prec == MCPM_FP32 ? conv_field_impl<float>(s, field, n, st) : conv_field_impl<double>(s, field, n, st);
+}
+int launch_convert_out_slotted(Session& s) {
+  k_convert_out_slotted<float><<<s.num_sms * 8, 256, 0, s.stream>>>(
+      pt<float>(s.P[s.cur]), pt<float>(s.ovf), s.ovf_n + (1 - s.ovf_par), s.off, s.dcur, s.C, s.stage, s.cap);
+  return 1;
+}
 
 // the dynamic shared memory the update kernel needs, for the session setup
 size_t update_smem_bytes(const Session& s) {

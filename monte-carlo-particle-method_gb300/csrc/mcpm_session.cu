@@ -367,14 +367,29 @@ int mcpm_upload_particles(mcpm_session* s, int64_t n, const double* x1, const do
   s->N = n;
   const size_t cap = (size_t)s->cap, b = (size_t)n * 8;
   cudaStream_t st = s->stream;
-  if (x1) cudaMemcpyAsync(s->stage, x1, b, cudaMemcpyHostToDevice, st);
-  else cudaMemsetAsync(s->stage, 0, b, st);
-  cudaMemcpyAsync(s->stage + cap, x2, b, cudaMemcpyHostToDevice, st);
-  cudaMemcpyAsync(s->stage + 2 * cap, U1, b, cudaMemcpyHostToDevice, st);
-  cudaMemcpyAsync(s->stage + 3 * cap, U2, b, cudaMemcpyHostToDevice, st);
-  cudaMemcpyAsync(s->stage + 4 * cap, U3, b, cudaMemcpyHostToDevice, st);
   s->cur = 0;
-  int k = launch_convert_in(*s, n);
+  int k = 0;
+  const double* src[5] = {x1, x2, U1, U2, U3};
+  if (s->need_old || !s->side) {
+    for (int f = 0; f < 5; ++f) {
+      if (src[f]) cudaMemcpyAsync(s->stage + f * cap, src[f], b, cudaMemcpyHostToDevice, st);
+      else cudaMemsetAsync(s->stage + f * cap, 0, b, st);
+    }
+    k = launch_convert_in(*s, n);
+  } else {
+    // each field converted on the side stream while the next one is copied
+    cudaEventRecord(s->ev_fork, st);
+    cudaStreamWaitEvent(s->side, s->ev_fork, 0);
+    for (int f = 0; f < 5; ++f) {
+      if (src[f]) cudaMemcpyAsync(s->stage + f * cap, src[f], b, cudaMemcpyHostToDevice, st);
+      else cudaMemsetAsync(s->stage + f * cap, 0, b, st);
+      cudaEventRecord(s->ev_fork, st);
+      cudaStreamWaitEvent(s->side, s->ev_fork, 0);
+      k += launch_convert_field(*s, f, n, s->side);
+    }
+    cudaEventRecord(s->ev_join, s->side);
+    cudaStreamWaitEvent(st, s->ev_join, 0);
+  }
   int rc = after_launch(s, k, "upload");
   if (rc) return rc;
   s->step = 0;
@@ -391,9 +406,8 @@ int mcpm_download_particles(mcpm_session* s, int64_t n, double* x1, double* x2, 
   if (!s || n != s->N || !x2 || !U1 || !U2 || !U3) return fail(s, MCPM_ERR_ARG, "download: bad arguments");
   const size_t cap = (size_t)s->cap, b = (size_t)n * 8;
   cudaStream_t st = s->stream;
-  int rc0 = leave_slotted(s);  // the staging kernel reads a packed layout [0, N)
-  if (rc0) return rc0;
-  int k = launch_convert_out(*s, n);
+  // a slotted layout is staged as it lies (and stays slotted for the next step)
+  int k = s->slotted ? launch_convert_out_slotted(*s) : launch_convert_out(*s, n);
   int rc = after_launch(s, k, "download");
   if (rc) return rc;
   // x1 is not tracked when it never changes (no x streaming, no ESMC):
