@@ -238,6 +238,9 @@ int launch_convert_out(Session& s, int64_t n);
 // one staged upload field (0..4: x1 x2 U1 U2 U3; field 2 also sets the ids)
 // on stream st
 int launch_convert_field(Session& s, int field, int64_t n, cudaStream_t st);
+// one download field (0..4) into particle-id order in the stage, from the
+// current layout (packed or slotted)
+int launch_convert_out_field(Session& s, int field, int64_t n);
 // the staging of a download straight from a slotted layout (FP32 sessions)
 int launch_convert_out_slotted(Session& s);
 

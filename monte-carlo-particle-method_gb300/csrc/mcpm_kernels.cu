@@ -1998,6 +1998,32 @@ __global__ void k_convert_out(PT<real> p, double* stage, int64_t n, int64_t cap)
   }
 }
 
+// One field of a download (0..4: x1 x2 U1 U2 U3) into particle-id order,
+// from a packed layout or -- with dcur -- from a slotted one (each cell's
+// filled slots, then the overflow entries); downloads convert one field
+// while the previous one is copied to the host.
+template <typename real>
+__global__ void k_convert_out_field(PT<real> p, PT<real> ovf, const int32_t* ovf_n, const int32_t* off,
+                                    const int32_t* dcur, int C, int f, double* dst, int64_t n) {
+  const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x, nt = (int64_t)gridDim.x * blockDim.x;
+  auto field = [&](const PT<real>& src) -> const real* {
+    return f == 0 ? src.x1 : f == 1 ? src.x2 : f == 2 ? src.U1 : f == 3 ? src.U2 : src.U3;
+  };
+  const real* v = field(p);
+  if (!dcur) {
+    for (int64_t i = tid; i < n; i += nt) dst[p.pid[i]] = (double)v[i];
+    return;
+  }
+  const int lane = threadIdx.x & 31;
+  for (int64_t c = tid >> 5; c < C; c += nt >> 5) {
+    const int s0 = off[c], m = min(dcur[c], off[c + 1] - s0);
+    for (int i = lane; i < m; i += 32) dst[p.pid[s0 + i]] = (double)v[s0 + i];
+  }
+  const real* w = field(ovf);
+  const int n_ovf = *ovf_n;
+  for (int64_t e = tid; e < n_ovf; e += nt) dst[ovf.pid[e]] = (double)w[e];
+}
+
 // The same from a slotted layout as the particle pass left it: each cell's
 // first min(slots taken, capacity) particles of its region (bases off, the
 // counts still in the slot counters), then the overflow entries; the layout
@@ -2219,6 +2245,16 @@ template <typename real> static int conv_field_impl(Session& s, int f, int64_t n
 }
 int launch_convert_field(Session& s, int field, int64_t n, cudaStream_t st) {
   return s.prec == MCPM_FP32 ? conv_field_impl<float>(s, field, n, st) : conv_field_impl<double>(s, field, n, st);
+}
+template <typename real> static int conv_out_field_impl(Session& s, int f, int64_t n) {
+  const bool sl = s.slotted;
+  k_convert_out_field<real><<<s.num_sms * 8, 256, 0, s.stream>>>(
+      pt<real>(s.P[s.cur]), pt<real>(s.ovf), sl ? s.ovf_n + (1 - s.ovf_par) : nullptr, s.off, sl ? s.dcur : nullptr,
+      s.C, f, s.stage + (size_t)f * s.cap, n);
+  return 1;
+}
+int launch_convert_out_field(Session& s, int field, int64_t n) {
+  return s.prec == MCPM_FP32 ? conv_out_field_impl<float>(s, field, n) : conv_out_field_impl<double>(s, field, n);
 }
 int launch_convert_out_slotted(Session& s) {
   k_convert_out_slotted<float><<<s.num_sms * 8, 256, 0, s.stream>>>(

@@ -406,17 +406,31 @@ int mcpm_download_particles(mcpm_session* s, int64_t n, double* x1, double* x2, 
   if (!s || n != s->N || !x2 || !U1 || !U2 || !U3) return fail(s, MCPM_ERR_ARG, "download: bad arguments");
   const size_t cap = (size_t)s->cap, b = (size_t)n * 8;
   cudaStream_t st = s->stream;
-  // a slotted layout is staged as it lies (and stays slotted for the next step)
+  // a slotted layout is staged as it lies (and stays slotted for the next
+  // step); each field is converted while the previous one is copied out
+  double* dsts[5] = {(x1 && s->need_x1) ? x1 : nullptr, x2, U1, U2, U3};
+  if (s->side) {
+    int k = 0;
+    for (int f = 0; f < 5; ++f) {
+      if (!dsts[f]) continue;
+      k += launch_convert_out_field(*s, f, n);
+      cudaEventRecord(s->ev_fork, st);
+      cudaStreamWaitEvent(s->side, s->ev_fork, 0);
+      cudaMemcpyAsync(dsts[f], s->stage + (size_t)f * cap, b, cudaMemcpyDeviceToHost, s->side);
+    }
+    int rc = after_launch(s, k, "download");
+    if (rc) return rc;
+    cudaEventRecord(s->ev_join, s->side);
+    cudaStreamWaitEvent(st, s->ev_join, 0);
+    return cuda_check(s, cudaStreamSynchronize(st), "download");
+  }
   int k = s->slotted ? launch_convert_out_slotted(*s) : launch_convert_out(*s, n);
   int rc = after_launch(s, k, "download");
   if (rc) return rc;
   // x1 is not tracked when it never changes (no x streaming, no ESMC):
   // the caller's array is left as it is, like the reference's x1
-  if (x1 && s->need_x1) cudaMemcpyAsync(x1, s->stage, b, cudaMemcpyDeviceToHost, st);
-  cudaMemcpyAsync(x2, s->stage + cap, b, cudaMemcpyDeviceToHost, st);
-  cudaMemcpyAsync(U1, s->stage + 2 * cap, b, cudaMemcpyDeviceToHost, st);
-  cudaMemcpyAsync(U2, s->stage + 3 * cap, b, cudaMemcpyDeviceToHost, st);
-  cudaMemcpyAsync(U3, s->stage + 4 * cap, b, cudaMemcpyDeviceToHost, st);
+  for (int f = 0; f < 5; ++f)
+    if (dsts[f]) cudaMemcpyAsync(dsts[f], s->stage + (size_t)f * cap, b, cudaMemcpyDeviceToHost, st);
   return cuda_check(s, cudaStreamSynchronize(st), "download");
 }
 
