@@ -1688,6 +1688,12 @@ __device__ void update_cell(int c, const UpdArgs<real>& a, int step, real* xs, i
 #ifndef MCPM_UPD_MINB_SL
 #define MCPM_UPD_MINB_SL 5
 #endif
+#ifndef MCPM_UPD_PF_C
+#define MCPM_UPD_PF_C 1
+#endif
+#ifndef MCPM_UPD_PF_D
+#define MCPM_UPD_PF_D 1
+#endif
 #ifndef MCPM_UPD_UNROLL
 #define MCPM_UPD_UNROLL 1
 #endif
@@ -1767,9 +1773,8 @@ __device__ void update_cell_f32(int c, const UpdArgs<float>& a, int step, float*
   }
   // the Ornstein-Uhlenbeck update of M' with the cubic drift
   // (src/Fokker_Planck.cpp:1114-1130), constants from the shared record
-  auto mnew = [&](int i, float& m1, float& m2, float& m3) {
-    const int64_t p = s0 + i;
-    m1 = P.U1[p] - Us0; m2 = P.U2[p] - Us1; m3 = P.U3[p] - Us2;
+  auto mnew_u = [&](int i, float u1, float u2, float u3, float& m1, float& m2, float& m3) {
+    m1 = u1 - Us0; m2 = u2 - Us1; m3 = u3 - Us2;
     if (n > 1) {
       float z0, z1, z2;
       xiw(i, z0, z1, z2);
@@ -1789,14 +1794,32 @@ __device__ void update_cell_f32(int c, const UpdArgs<float>& a, int step, float*
       m1 = 0.f; m2 = 0.f; m3 = 0.f;
     }
   };
+  auto mnew = [&](int i, float& m1, float& m2, float& m3) {
+    const int64_t p = s0 + i;
+    mnew_u(i, P.U1[p], P.U2[p], P.U3[p], m1, m2, m3);
+  };
   // ---- pass C: M'_new, sum |M'_new|^2; M'_new replaces the staged normals
   float scale = 1.f;
   if (fp) {
     float f2[1] = {0.f};
+#if MCPM_UPD_PF_C
+    // the next particle's velocities are loaded while this one is computed
+    float nu1 = 0.f, nu2 = 0.f, nu3 = 0.f;
+    if (t < n) { nu1 = P.U1[s0 + t]; nu2 = P.U2[s0 + t]; nu3 = P.U3[s0 + t]; }
+#endif
     UPD_UNROLL
     for (int i = t; i < n; i += TILE) {
       float m1, m2, m3;
+#if MCPM_UPD_PF_C
+      const float u1 = nu1, u2 = nu2, u3 = nu3;
+      if (i + TILE < n) {
+        const int64_t q = s0 + i + TILE;
+        nu1 = P.U1[q]; nu2 = P.U2[q]; nu3 = P.U3[q];
+      }
+      mnew_u(i, u1, u2, u3, m1, m2, m3);
+#else
       mnew(i, m1, m2, m3);
+#endif
       if (m2 != m2) bad |= MCPM_ERR_NAN;
       f2[0] = fmaf(m3, m3, fmaf(m2, m2, fmaf(m1, m1, f2[0])));
       if (staged) { xs[3 * i] = m1; xs[3 * i + 1] = m2; xs[3 * i + 2] = m3; }
@@ -1813,19 +1836,34 @@ __device__ void update_cell_f32(int c, const UpdArgs<float>& a, int step, float*
   const float dtr = kc.dt;
   const float fj = (float)(c % k.N0), fk = (float)(c / k.N0);
   const int iters = (n + TILE - 1) / TILE;
+  // the next particle's positions and id are loaded while this one is moved
+  // (passes without the long-range kick: with it, the extra registers spill)
+  constexpr bool PFD = MCPM_UPD_PF_D && CST != 0 && !(CST & ST_LR);
+  float nx1 = 0.f, nx2 = 0.f;
+  int npid = 0;
+  if (PFD && t < n) { nx1 = P.x1 ? P.x1[s0 + t] : 0.f; nx2 = P.x2[s0 + t]; npid = P.pid[s0 + t]; }
   UPD_UNROLL
   for (int r = 0; r < iters; ++r) {
     const int i = r * TILE + t;
     const bool act = i < n;
     int key = 0, pid = 0;
     PState<float> s;
+    if constexpr (PFD) {
+      s.x1 = nx1; s.x2 = nx2; pid = npid;
+      if (i + TILE < n) {
+        const int64_t q = s0 + i + TILE;
+        nx1 = P.x1 ? P.x1[q] : 0.f; nx2 = P.x2[q]; npid = P.pid[q];
+      }
+    }
     if (act) {
       const int64_t p = s0 + i;
-      s.x1 = P.x1 ? P.x1[p] : 0.f;
-      s.x2 = P.x2[p];
+      if constexpr (!PFD) {
+        s.x1 = P.x1 ? P.x1[p] : 0.f;
+        s.x2 = P.x2[p];
+        pid = P.pid[p];
+      }
       s.x1o = P.x1o ? P.x1o[p] : 0.f;
       s.x2o = P.x2o ? P.x2o[p] : 0.f;
-      pid = P.pid[p];
       if (fp) {
         if (n > 1) {
           float m1, m2, m3;
