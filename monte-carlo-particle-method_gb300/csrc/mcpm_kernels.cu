@@ -1340,15 +1340,19 @@ template <typename real> struct UpdArgs {
 };
 
 template <typename real>
-__device__ __forceinline__ void raw_normals(const UpdArgs<real>& a, int step, int64_t p, real& z0, real& z1,
-                                            real& z2) {
-  int pid = a.p.pid[p];
+__device__ __forceinline__ void raw_normals_pid(const UpdArgs<real>& a, int step, int pid, real& z0, real& z1,
+                                                real& z2) {
   if (a.rng_mode == MCPM_RNG_INJECTED) {
     z0 = (real)a.inj[pid]; z1 = (real)a.inj[a.cap + pid]; z2 = (real)a.inj[2 * a.cap + pid];
   } else {
     Normals3<real> z = normals3<real>(philox(a.k.seed, (uint32_t)pid, (uint32_t)step, RNG_FP, 0u));
     z0 = z.z0; z1 = z.z1; z2 = z.z2;
   }
+}
+template <typename real>
+__device__ __forceinline__ void raw_normals(const UpdArgs<real>& a, int step, int64_t p, real& z0, real& z1,
+                                            real& z2) {
+  raw_normals_pid(a, step, a.p.pid[p], z0, z1, z2);
 }
 
 // Per-cell constants of the particle pass.  FP64: read from the double cell
@@ -1694,6 +1698,9 @@ __device__ void update_cell(int c, const UpdArgs<real>& a, int step, real* xs, i
 #ifndef MCPM_UPD_PF_D
 #define MCPM_UPD_PF_D 1
 #endif
+#ifndef MCPM_UPD_PF_A
+#define MCPM_UPD_PF_A 1
+#endif
 #ifndef MCPM_UPD_UNROLL
 #define MCPM_UPD_UNROLL 1
 #endif
@@ -1734,11 +1741,20 @@ __device__ void update_cell_f32(int c, const UpdArgs<float>& a, int step, float*
   f1 = R[PF_E2];
   if (rng) {
     float sa[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};  // z0 z1 z2 z0^2 z1^2 z2^2
+#if MCPM_UPD_PF_A
+    // the next particle's id is loaded while this one's draws are made
+    int npid = t < n ? P.pid[s0 + t] : 0;
+#endif
     UPD_UNROLL
     for (int i = t; i < n; i += TILE) {
-      const int64_t p = s0 + i;
       float z0, z1, z2;
-      raw_normals(a, step, p, z0, z1, z2);
+#if MCPM_UPD_PF_A
+      const int pid_i = npid;
+      if (i + TILE < n) npid = P.pid[s0 + i + TILE];
+      raw_normals_pid(a, step, pid_i, z0, z1, z2);
+#else
+      raw_normals(a, step, s0 + i, z0, z1, z2);
+#endif
       if (staged) { xs[3 * i] = z0; xs[3 * i + 1] = z1; xs[3 * i + 2] = z2; }
       sa[0] += z0; sa[1] += z1; sa[2] += z2;
       sa[3] = fmaf(z0, z0, sa[3]); sa[4] = fmaf(z1, z1, sa[4]); sa[5] = fmaf(z2, z2, sa[5]);
