@@ -249,7 +249,9 @@ int mcpm_init_omega_max(mcpm_session* s);
 /* Launch on the caller's CUDA stream (cudaStream_t) instead of the
    session's own; NULL restores the session stream. */
 int mcpm_set_stream(mcpm_session* s, void* stream);
-/* Kernel classes timed by the profiling mode, in mcpm_profile_read order. */
+/* Kernel classes timed by the profiling mode, in mcpm_profile_read order
+   (MCPM_K_SCATTER: the keyed reorder of packed layouts, or the overflow
+   repair of the slotted layouts FP32 sessions keep between fused steps). */
 enum mcpm_kernel_class {
   MCPM_K_BIN = 0, MCPM_K_SCAN, MCPM_K_SCATTER, MCPM_K_MOMENTS, MCPM_K_SOLVE,
   MCPM_K_ESMC, MCPM_K_LONG_RANGE, MCPM_K_UPDATE, MCPM_K_SURROGATE, MCPM_K_COUNT
