@@ -297,32 +297,6 @@ __device__ __forceinline__ void tile_reduce(Acc<real> (&a)[K], Acc<real>* smem) 
   }
 }
 
-// Reduce K <= 16 accumulators over a tile and hand each total to write(f,
-// total) exactly once (one lane per field; lanes of warp 0 when TILE > 32).
-// smem must hold K * (TILE/32) Acc entries when TILE > 32.
-template <typename real, int K, int TILE, typename WR>
-__device__ __forceinline__ void tile_reduce_write(Acc<real> (&a)[K], Acc<real>* smem, WR write) {
-  constexpr int P = K <= 1 ? 1 : K <= 2 ? 2 : K <= 4 ? 4 : K <= 8 ? 8 : K <= 16 ? 16 : 32;
-  static_assert(K <= 16, "at most 16 fields");
-  const int lane = threadIdx.x & 31;
-  int f;
-  Acc<real> r = warp_reduce_halving<real, K>(a, &f);
-  const bool owner = (lane & (32 / P - 1)) == 0 && f < K;
-  if constexpr (TILE == 32) {
-    if (owner) write(f, r);
-  } else {
-    constexpr int W = TILE / 32;
-    const int warp = threadIdx.x >> 5;
-    __syncthreads();
-    if (owner) smem[f * W + warp] = r;
-    __syncthreads();
-    if (warp == 0 && lane < K) {
-      Acc<real> tot = smem[lane * W];
-      for (int w = 1; w < W; ++w) tot.merge(smem[lane * W + w]);
-      write(lane, tot);
-    }
-  }
-}
 
 // floor(t) for -1 < t < 2^23 without a float-to-int conversion instruction:
 // adding 2^23 with rounding toward -inf leaves floor(t) in the mantissa.

@@ -431,8 +431,10 @@ template <typename real> struct MomArgs {
   const real *U1, *U2, *U3;
 };
 
+// FP64 sessions (FP32 sessions take moments_cell_f32)
 template <typename real, int TILE>
 __device__ void moments_cell(int c, const MomArgs<real>& a, Acc<real>* red) {
+  static_assert(sizeof(real) == 8, "the FP32 moment pass is moments_cell_f32");
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int t = (TILE == 32) ? lane : threadIdx.x;
   const int s0 = a.off[c], n = a.cnt[c];
@@ -446,17 +448,11 @@ __device__ void moments_cell(int c, const MomArgs<real>& a, Acc<real>* red) {
     u[2].add(a.U3[s0 + i]);
   }
   tile_reduce<real, 3, TILE>(u, red);
-  // cell mean velocity U_space (src/Main_Functions.cpp:2493-2500); in the
-  // FP32 path the mean is formed in float, and stored widened
+  // cell mean velocity U_space (src/Main_Functions.cpp:2493-2500)
   real m0 = 0, m1 = 0, m2 = 0;
   if (n > 0) {
-    if constexpr (sizeof(real) == 8) {
-      const double weight = (double)n;
-      m0 = u[0].get() / weight; m1 = u[1].get() / weight; m2 = u[2].get() / weight;
-    } else {
-      const float w = (float)n;
-      m0 = u[0].getr() / w; m1 = u[1].getr() / w; m2 = u[2].getr() / w;
-    }
+    const double weight = (double)n;
+    m0 = u[0].get() / weight; m1 = u[1].get() / weight; m2 = u[2].get() / weight;
   }
   Acc<real> q[29];
 #pragma unroll
@@ -477,83 +473,11 @@ __device__ void moments_cell(int c, const MomArgs<real>& a, Acc<real>* red) {
     v[25] = Mp1 * energy * energy; v[26] = Mp2 * energy * energy; v[27] = Mp3 * energy * energy;
     v[28] = energy;
   };
-  if constexpr (sizeof(real) == 4) {
-    // FP32: the 29 sums in two groups (terms 0..14, then 15..28), each a
-    // pass over the cell's velocities (the second pass reads them from
-    // L1): half the accumulators live at a time, so more warps fit per SM.
-    // Within a group: compensated accumulation of partials -- the terms of
-    // up to four of a lane's particles are summed in float, then the partial
-    // enters the lane's compensated sum.
-    auto group = [&](auto J0c, auto Kc) {
-      constexpr int J0 = decltype(J0c)::value, K = decltype(Kc)::value;
-      // Kahan's compensated sum per lane (4 additions per term; the
-      // library is built without contraction, so the compensation holds),
-      // merged across lanes as (sum, -compensation) pairs
-      float ks[K], kc[K];
+  for (int i = t; i < n; i += TILE) {
+    real v[29];
+    terms(i, v);
 #pragma unroll
-      for (int j = 0; j < K; ++j) { ks[j] = 0.f; kc[j] = 0.f; }
-      for (int i = t; i < n; i += 4 * TILE) {
-        real ps[K];
-        {
-          real v[29];
-          terms(i, v);
-#pragma unroll
-          for (int j = 0; j < K; ++j) ps[j] = v[J0 + j];
-        }
-#pragma unroll 1
-        for (int q = 1; q < 4; ++q) {
-          if (i + q * TILE >= n) break;
-          real v[29];
-          terms(i + q * TILE, v);
-#pragma unroll
-          for (int j = 0; j < K; ++j) ps[j] += v[J0 + j];
-        }
-#pragma unroll
-        for (int j = 0; j < K; ++j) {
-          const float y = ps[j] - kc[j], tt = ks[j] + y;
-          kc[j] = (tt - ks[j]) - y;
-          ks[j] = tt;
-        }
-      }
-      Acc<real> g[K];
-#pragma unroll
-      for (int j = 0; j < K; ++j) { g[j].c.hi = ks[j]; g[j].c.lo = -kc[j]; }
-      tile_reduce_write<real, K, TILE>(g, red, [&](int f, const Acc<real>& tot) {
-        a.cell[(size_t)(CFI_RAW + J0 + f) * C + c] = tot.get();
-      });
-    };
-    group(std::integral_constant<int, 0>(), std::integral_constant<int, 15>());
-    group(std::integral_constant<int, 15>(), std::integral_constant<int, 14>());
-    if (TILE == 32 || warp == 0) {
-      double* cl = a.cell;
-      if (lane == 29) cl[(size_t)(MCPM_CF_U_SPACE + 0) * C + c] = (double)m0;
-      else if (lane == 30) cl[(size_t)(MCPM_CF_U_SPACE + 1) * C + c] = (double)m1;
-      else if (lane == 31) cl[(size_t)(MCPM_CF_U_SPACE + 2) * C + c] = (double)m2;
-      if (lane == 0) cl[(size_t)MCPM_CF_NUM_INSIDE * C + c] = (double)n;
-    }
-    return;
-  }
-  if constexpr (sizeof(real) == 8) {
-    for (int i = t; i < n; i += TILE) {
-      real v[29];
-      terms(i, v);
-#pragma unroll
-      for (int j = 0; j < 29; ++j) q[j].add(v[j]);
-    }
-  } else {
-    // compensated pairwise accumulation: the terms of two particles are
-    // added in float, then the pair enters the compensated sum
-    for (int i = t; i < n; i += 2 * TILE) {
-      real v[29], w[29];
-      terms(i, v);
-      if (i + TILE < n) {
-        terms(i + TILE, w);
-#pragma unroll
-        for (int j = 0; j < 29; ++j) v[j] += w[j];
-      }
-#pragma unroll
-      for (int j = 0; j < 29; ++j) q[j].add(v[j]);
-    }
+    for (int j = 0; j < 29; ++j) q[j].add(v[j]);
   }
   // raw sums, one field per lane; the FP64 finalisation (divisions by the
   // weight, T, n, Y, gamma*) runs once per cell in k_solve
@@ -680,13 +604,10 @@ __device__ void moments_cell_f32(int c, const MomArgs<float>& a, float* red) {
 #ifndef MCPM_MOM_MINB
 #define MCPM_MOM_MINB 5
 #endif
-#ifndef MCPM_MOM_PLAIN
-#define MCPM_MOM_PLAIN 1
-#endif
 template <typename real>
 __global__ void __launch_bounds__(256, sizeof(real) == 4 ? MCPM_MOM_MINB : 1) k_moments(MomArgs<real> a) {
   __shared__ Acc<real> red[29 * 8];
-  if constexpr (sizeof(real) == 4 && MCPM_MOM_PLAIN) {
+  if constexpr (sizeof(real) == 4) {
     float* rf = reinterpret_cast<float*>(red);
     schedule_cells(
         a.list_big, a.list_small, a.wl, a.work, WK_MOM_BIG, WK_MOM_SMALL,
