@@ -79,7 +79,10 @@ enum mcpm_model {
   MCPM_MODEL_NONE = 0,          /* "none"                                       */
   MCPM_MODEL_FP_DENSE = 1,      /* "FP_dense"   (Enskog-Fokker-Planck)          */
   MCPM_MODEL_FP_IDEAL_GAS = 2,  /* "FP_ideal_gas"                               */
-  MCPM_MODEL_ESMC = 3           /* "ESMC" (Enskog DSMC, Collision_ESMC_new3)    */
+  MCPM_MODEL_ESMC = 3,          /* "ESMC" (Enskog DSMC, Collision_ESMC_new3)    */
+  MCPM_MODEL_FP_LINEAR = 4      /* "FP_linear" (Velocity_FP_linear: Langevin
+                                   relaxation without the cubic drift,
+                                   src/Fokker_Planck.cpp:1186-1283)             */
 };
 
 /* ---- long-range (Vlasov) force, gas.long_range (src/Main_Functions.cpp:1612) */
@@ -193,10 +196,12 @@ int mcpm_download_particles(mcpm_session* s, int64_t n, double* x1, double* x2,
 int mcpm_cell_update(mcpm_session* s);
 /* random_generator (src/Fokker_Planck.cpp:20-145): 3 normals per particle,
    centred and normalised per cell; kept on the device for the next
-   mcpm_velocity_update. */
+   mcpm_velocity_update.  Draws for the models the routine serves
+   (FP_dense, FP_ideal_gas, FP_linear, :22); a no-op for the others. */
 int mcpm_random_generator(mcpm_session* s);
-/* velocity_update (src/Main_Functions.cpp:1538-1672): FP Langevin update or
-   ESMC collisions, then the long-range force kick. */
+/* velocity_update (src/Main_Functions.cpp:1538-1672): FP Langevin update
+   (Velocity_FP_parallel, or Velocity_FP_linear for FP_linear) or ESMC
+   collisions, then the long-range force kick. */
 int mcpm_velocity_update(mcpm_session* s);
 int mcpm_dfp_extra_streaming(mcpm_session* s);
 int mcpm_apply_bc(mcpm_session* s);
@@ -208,7 +213,10 @@ int mcpm_end_step(mcpm_session* s);
 /* n_steps iterations of the main loop body (src/main.cpp:389-669) for the
    in-scope models: cell_update, random_generator, velocity_update,
    DFP_extra_streaming, apply_BC, store_old_positions, stream_particles,
-   apply_BC.  The particle-side stages run fused in one kernel per step;
+   apply_BC.  FP_linear steps draw their normals with random_generator:
+   the reference's loop calls it for FP_dense and FP_ideal_gas only
+   (src/main.cpp:442), which leaves Velocity_FP_linear reading noise arrays
+   that nothing filled (malloc'd at :129).  The particle-side stages run fused in one kernel per step;
    once the cell layout is in its steady state, pairs of steps are replayed
    as one CUDA graph (not in profiling mode). */
 int mcpm_step(mcpm_session* s, int32_t n_steps);

@@ -1001,11 +1001,18 @@ __global__ void __launch_bounds__(128) k_solve(DevConsts k, double* cell, float*
     pf[PF_US0] = (float)R(MCPM_CF_U_SPACE + 0);
     pf[PF_US1] = (float)R(MCPM_CF_U_SPACE + 1);
     pf[PF_US2] = (float)R(MCPM_CF_U_SPACE + 2);
-    pf[PF_A1] = (float)R(CFI_A1); pf[PF_A2] = (float)R(CFI_A2); pf[PF_A3] = (float)R(CFI_A3);
+    // Velocity_FP_linear (src/Fokker_Planck.cpp:1262-1264) has no drift:
+    // its cells carry zero drift coefficients (c, gamma, Lambda stay in the
+    // cell view, where cell_update computed them)
+    const bool lin = k.model == MCPM_MODEL_FP_LINEAR;
+    pf[PF_A1] = (float)R(CFI_A1); pf[PF_A2] = lin ? 0.f : (float)R(CFI_A2); pf[PF_A3] = (float)R(CFI_A3);
     pf[PF_EQ] = (float)eq3;
-    pf[PF_LAM] = (float)Lam;
-    for (int j = 0; j < 6; ++j) pf[PF_C0 + j] = (float)R(MCPM_CF_C + j);
-    for (int j = 0; j < 3; ++j) { pf[PF_G0 + j] = (float)R(MCPM_CF_GAMMA + j); pf[PF_Q0 + j] = (float)Q[j]; }
+    pf[PF_LAM] = lin ? 0.f : (float)Lam;
+    for (int j = 0; j < 6; ++j) pf[PF_C0 + j] = lin ? 0.f : (float)R(MCPM_CF_C + j);
+    for (int j = 0; j < 3; ++j) {
+      pf[PF_G0 + j] = lin ? 0.f : (float)R(MCPM_CF_GAMMA + j);
+      pf[PF_Q0 + j] = (float)Q[j];
+    }
     for (int j = 0; j < 6; ++j) pf[PF_AL0 + j] = (float)al[j];
     pf[PF_BE0] = (float)be[0]; pf[PF_BE1] = (float)be[1];
     pf[PF_GST] = (float)gst;
@@ -1319,6 +1326,12 @@ __device__ __forceinline__ void load_cellk(CellK<real>& K, int c, const UpdArgs<
     K.m3_1 = R(MCPM_CF_M3 + 1, c); K.m3_6 = R(MCPM_CF_M3 + 6, c); K.m3_8 = R(MCPM_CF_M3 + 8, c);
     K.hq0 = K.hq1 = 0.0;
     K.ph0 = R(MCPM_CF_PHI + 0, c); K.ph1 = R(MCPM_CF_PHI + 1, c);
+    if (a.k.model == MCPM_MODEL_FP_LINEAR) {
+      // Velocity_FP_linear: M' <- A1 M' + A3 xi (src/Fokker_Planck.cpp:1262-1264)
+      K.A2 = 0.0; K.lam = 0.0;
+      for (int j = 0; j < 6; ++j) K.c[j] = 0.0;
+      for (int j = 0; j < 3; ++j) K.g[j] = 0.0;
+    }
     K.f2dt = (st & ST_LR) ? R(MCPM_CF_F2, c) * a.k.dt : 0.0;
     if ((st & ST_LR) && a.k.lr2d) {
       // cells[num].x_n[0], y_n[0], dx, dy as make_cells builds them (src/myIO.cpp:1456-1479)
@@ -2112,7 +2125,9 @@ template <typename real> static int moments_impl(Session& s) {
 int launch_moments(Session& s) { return s.prec == MCPM_FP32 ? moments_impl<float>(s) : moments_impl<double>(s); }
 
 int launch_solve(Session& s, int with_alpha) {
-  int fp = (s.cfg.model == MCPM_MODEL_FP_DENSE || s.cfg.model == MCPM_MODEL_FP_IDEAL_GAS) ? 1 : 0;
+  // c_gamma_calculation and the Langevin constants (src/Main_Functions.cpp:2729)
+  const int m = s.cfg.model;
+  int fp = (m == MCPM_MODEL_FP_DENSE || m == MCPM_MODEL_FP_IDEAL_GAS || m == MCPM_MODEL_FP_LINEAR) ? 1 : 0;
   // the FP64 path reproduces the reference's solve exactly; the FP32 path
   // runs the leaner FP64 variant
   if (s.prec == MCPM_FP32)

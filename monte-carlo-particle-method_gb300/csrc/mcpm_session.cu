@@ -108,7 +108,11 @@ template <typename F> static int timed(mcpm_session* s, int cls, F f) {
 #define T_UPD(x) timed(s, MCPM_K_UPDATE, [&] { return (x); })
 #define T_SUR(x) timed(s, MCPM_K_SURROGATE, [&] { return (x); })
 
-static inline bool is_fp_model(int m) { return m == MCPM_MODEL_FP_DENSE || m == MCPM_MODEL_FP_IDEAL_GAS; }
+// the models random_generator and the FP velocity update serve
+// (src/Fokker_Planck.cpp:22, src/Main_Functions.cpp:1565-1570)
+static inline bool is_fp_model(int m) {
+  return m == MCPM_MODEL_FP_DENSE || m == MCPM_MODEL_FP_IDEAL_GAS || m == MCPM_MODEL_FP_LINEAR;
+}
 
 extern "C" {
 static int long_range_force(mcpm_session* s);
@@ -137,7 +141,7 @@ int mcpm_session_create(const mcpm_config* cfg, mcpm_session** out) {
   if ((int64_t)c.n_cells[0] * c.n_cells[1] > (1 << 24)) return MCPM_ERR_ARG;
   if (c.max_particles > ((int64_t)1 << 31) - 1) return MCPM_ERR_ARG;
   if (c.precision != MCPM_FP64 && c.precision != MCPM_FP32) return MCPM_ERR_ARG;
-  if (c.model < MCPM_MODEL_NONE || c.model > MCPM_MODEL_ESMC) return MCPM_ERR_ARG;
+  if (c.model < MCPM_MODEL_NONE || c.model > MCPM_MODEL_FP_LINEAR) return MCPM_ERR_ARG;
   if (c.problem != MCPM_PROBLEM_CLOSED_BOX && c.problem != MCPM_PROBLEM_COUETTE && c.problem != MCPM_PROBLEM_WALL &&
       c.problem != MCPM_PROBLEM_PERIODIC)
     return MCPM_ERR_ARG;
@@ -450,7 +454,7 @@ int mcpm_cell_update(mcpm_session* s) {
 
 int mcpm_random_generator(mcpm_session* s) {
   if (!s || !s->sorted) return fail(s, MCPM_ERR_STATE, "random_generator: call cell_update first");
-  if (!is_fp_model(s->cfg.model)) return MCPM_OK;  // src/main.cpp:442
+  if (!is_fp_model(s->cfg.model)) return MCPM_OK;  // src/Fokker_Planck.cpp:22
   cudaMemsetAsync(s->work, 0, WK_COUNT * 4, s->stream);
   return after_launch(s, T_UPD(launch_update(*s, ST_RNG | ST_STORE_XI, 0)), "random_generator");
 }

@@ -635,7 +635,7 @@ void orc_cell_update(orc_state* s, const double* x1, const double* x2,
   moments(s, U1, U2, U3);
   lambda_cells(s);
   int m = s->cfg.model;
-  if (m == MCPM_MODEL_FP_DENSE || m == MCPM_MODEL_FP_IDEAL_GAS) {
+  if (m == MCPM_MODEL_FP_DENSE || m == MCPM_MODEL_FP_IDEAL_GAS || m == MCPM_MODEL_FP_LINEAR) {
     if (s->step > 0 && m == MCPM_MODEL_FP_DENSE) alpha_cells(s);
     c_gamma_cells(s);
   }
@@ -697,7 +697,13 @@ void orc_random_generator(orc_state* s, double* x1f, double* x2f, double* x3f) {
 
 /* ------------------------------------------------- Velocity_FP_parallel -- */
 /* src/Fokker_Planck.cpp:1065-1182: Ornstein-Uhlenbeck step with the cubic
-   drift, then per-cell rescaling that restores sum |M'|^2 exactly. */
+   drift, then per-cell rescaling that restores sum |M'|^2 exactly.
+   FP_linear (Velocity_FP_linear, :1186-1283) is the same step without the
+   drift, Y = 1; its face-force term F (:1246-1260) is computed but never
+   used there and is left out.  Velocity_FP_linear has no one-particle
+   guard: such a cell has T = 0 and its tau is 0/0, so the reference stops
+   on its NaN check (:1266-1268); here it takes the guarded branch of
+   Velocity_FP_parallel (U = U_space, the particle keeps its velocity). */
 void orc_velocity_fp(orc_state* s, double* U1, double* U2, double* U3,
                      const double* xi1, const double* xi2, const double* xi3) {
   const mcpm_config* g = &s->cfg;
@@ -725,6 +731,14 @@ void orc_velocity_fp(orc_state* s, double* U1, double* U2, double* U3,
       double A1 = exp(-g->dt / tau);
       double A3 = sqrt((1.0 - exp(-2.0 * g->dt / tau)) * g->kb * T / (1.0 * g->m));
       double A2 = (1.0 - exp(-g->dt / tau)) * tau;
+      if (g->model == MCPM_MODEL_FP_LINEAR) {
+        /* Velocity_FP_linear, src/Fokker_Planck.cpp:1262-1264: no drift */
+        Mp1[id] = A1 * Mp1[id] + A3 * xi1[id];
+        Mp2[id] = A1 * Mp2[id] + A3 * xi2[id];
+        Mp3[id] = A1 * Mp3[id] + A3 * xi3[id];
+        if (Mp2[id] != Mp2[id]) s->status |= MCPM_ERR_NAN;
+        continue;
+      }
       double energy = Mp1[id] * Mp1[id] + Mp2[id] * Mp2[id] + Mp3[id] * Mp3[id];
       const double* c = &CELL(s, num, MCPM_CF_C);
       const double* gm = &CELL(s, num, MCPM_CF_GAMMA);
@@ -1484,7 +1498,9 @@ void orc_step(orc_state* s, double* x1, double* x2, double* x1_old,
   int m = s->cfg.model;
   int64_t N = s->N;
   orc_cell_update(s, x1, x2, U1, U2, U3, index);
-  if (m == MCPM_MODEL_FP_DENSE || m == MCPM_MODEL_FP_IDEAL_GAS) {
+  /* FP_linear draws as well: the reference's loop leaves its noise arrays
+     unfilled for that model (src/main.cpp:442) */
+  if (m == MCPM_MODEL_FP_DENSE || m == MCPM_MODEL_FP_IDEAL_GAS || m == MCPM_MODEL_FP_LINEAR) {
     orc_random_generator(s, s->xi, s->xi + N, s->xi + 2 * N);
     orc_velocity_fp(s, U1, U2, U3, s->xi, s->xi + N, s->xi + 2 * N);
   } else if (m == MCPM_MODEL_ESMC) {

@@ -97,6 +97,7 @@ static const char* model_name(int m) {
     case MCPM_MODEL_FP_DENSE: return "FP_dense";
     case MCPM_MODEL_FP_IDEAL_GAS: return "FP_ideal_gas";
     case MCPM_MODEL_ESMC: return "ESMC";
+    case MCPM_MODEL_FP_LINEAR: return "FP_linear";
     default: return "none";
   }
 }
@@ -172,8 +173,13 @@ void ref_velocity_fp(void* h, double* U1, double* U2, double* U3, int* index, do
                      double* xi3f) {
   Quiet q;
   Ref* r = (Ref*)h;
-  Velocity_FP_parallel(U1, U2, U3, &r->gas, r->cells, &r->box, index, xi1f, xi2f, xi3f, r->Mp1.data(),
+  // the dispatch of velocity_update, src/Main_Functions.cpp:1565-1570
+  if (r->gas.model == "FP_linear")
+    Velocity_FP_linear(U1, U2, U3, &r->gas, r->cells, &r->box, index, xi1f, xi2f, xi3f, r->Mp1.data(),
                        r->Mp2.data(), r->Mp3.data());
+  else
+    Velocity_FP_parallel(U1, U2, U3, &r->gas, r->cells, &r->box, index, xi1f, xi2f, xi3f, r->Mp1.data(),
+                         r->Mp2.data(), r->Mp3.data());
 }
 
 void ref_long_range(void* h, double* x1, double* x2, double* U2, int* index) {

@@ -6,7 +6,7 @@ normals and stores inputs and outputs as .npz.  tests/test_oracle_golden.py
 checks the CPU restatement against these files bit for bit, which pins the
 oracle where the reference tree is not available.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [case ...]     (all cases by default)
 """
 import json
 import os
@@ -83,20 +83,37 @@ def case_specular():
     return cfg, parts, dict(step=1), dict(x2=r.s.x2.copy(), U2=r.s.U2.copy())
 
 
+def case_fp_linear():
+    cfg, parts = W.homogeneous_relaxation_1d(n_cells=10, ppc=50)
+    cfg.model = mcpm.MODEL_FP_LINEAR
+    r = O.Reference(cfg, parts)
+    rng = np.random.default_rng(303)
+    xi = [rng.standard_normal(r.N) for _ in range(3)]
+    r.inject_normals(*xi)
+    r.set_step(2)
+    r.cell_update()
+    out = dict(index=r.s.index.copy(), cells=r.cells())
+    r.random_generator()
+    r.velocity_fp()
+    out.update(U1=r.s.U1.copy(), U2=r.s.U2.copy(), U3=r.s.U3.copy())
+    return cfg, parts, dict(xi1=xi[0], xi2=xi[1], xi3=xi[2], step=2), out
+
+
 CASES = {
     "fp_step_1d": case_fp_step,
     "cells_2d": case_cells_2d,
     "vlasov_direct_1d": lambda: case_vlasov(mcpm.LR_DIRECT),
     "vlasov_gf_1d": lambda: case_vlasov(mcpm.LR_SCREENED_POISSON),
     "specular_bc_1d": case_specular,
+    "fp_linear_1d": case_fp_linear,
 }
 
 
 def main():
     if O.ref_lib() is None:
         raise SystemExit("the reference build (oracle/_ref) is not available")
-    for name, fn in CASES.items():
-        cfg, parts, extra, out = fn()
+    for name in sys.argv[1:] or list(CASES):
+        cfg, parts, extra, out = CASES[name]()
         arrays = {"in_" + k: np.asarray(v) for k, v in parts.items() if k in ("x1", "x2", "U1", "U2", "U3")}
         arrays.update({"in_" + k: np.asarray(v) for k, v in extra.items()})
         arrays.update({"out_" + k: np.asarray(v) for k, v in out.items()})

@@ -56,6 +56,21 @@ def test_golden_fp_step(built):
     assert _same(o.s.x2, z["out_x2"])
 
 
+def test_golden_fp_linear(built):
+    """Velocity_FP_linear (src/Fokker_Planck.cpp:1186-1283) after cell_update
+    and random_generator, model FP_linear, step 2."""
+    cfg, parts, z = _load("fp_linear_1d")
+    assert cfg.model == mcpm.MODEL_FP_LINEAR
+    o = _oracle(cfg, parts, z)
+    o.cell_update()
+    assert _same(o.s.index, z["out_index"])
+    assert _same(o.cells()[:, :65], z["out_cells"][:, :65])
+    o.random_generator()
+    o.velocity_fp()
+    for k in ("U1", "U2", "U3"):
+        assert _same(getattr(o.s, k), z["out_" + k])
+
+
 def test_golden_cells_2d(built):
     cfg, parts, z = _load("cells_2d")
     o = _oracle(cfg, parts, z)

@@ -148,3 +148,33 @@ def test_esmc_reference_statistics(built):
     (mo, so), (mr, sr) = rates["orc"], rates["ref"]
     assert mo > 0 and mr > 0
     assert abs(mo - mr) < 4 * np.hypot(so, sr) + 0.02 * mr
+
+
+@pytest.mark.parametrize("step", [0, 3])
+def test_fp_linear_routines_bit_exact(built, step):
+    """FP_linear: cell_update (c/gamma for this model too, src/Main_Functions.cpp:2729),
+    random_generator (:22 of src/Fokker_Planck.cpp) and Velocity_FP_linear
+    (:1186-1283) against the restatement's drift-free branch."""
+    _ref_or_skip()
+    cfg, parts = W.homogeneous_relaxation_1d(n_cells=10, ppc=50)
+    cfg.model = mcpm.MODEL_FP_LINEAR
+    orc, ref = _pair(cfg, parts, seed=4, step=step)
+    for o in (orc, ref):
+        o.cell_update()
+        o.random_generator()
+    co, cr = orc.cells(), ref.cells()
+    for f in ("C", "GAMMA", "LAMBDA", "T", "N"):
+        assert _same(mcpm.cell_field(co, f, True), mcpm.cell_field(cr, f, True)), f
+    for a, b in zip(orc.xi, ref.xi):
+        assert _same(a, b)
+    for o in (orc, ref):
+        o.velocity_fp()
+    for k in ("U1", "U2", "U3"):
+        assert _same(getattr(orc.s, k), getattr(ref.s, k)), k
+    # the drift-free update differs from Velocity_FP_parallel's on the same draws
+    cfg.model = mcpm.MODEL_FP_IDEAL_GAS
+    o2, _ = _pair(cfg, parts, seed=4, step=step)
+    o2.cell_update()
+    o2.random_generator()
+    o2.velocity_fp()
+    assert not np.array_equal(o2.s.U1, orc.s.U1)
