@@ -15,7 +15,9 @@
  *   random_generator     src/Fokker_Planck.cpp:20           mcpm_random_generator
  *   velocity_update      src/Main_Functions.cpp:1538        mcpm_velocity_update
  *     Velocity_FP_parallel src/Fokker_Planck.cpp:1065         (model FP_dense / FP_ideal_gas)
+ *     Velocity_FP_linear   src/Fokker_Planck.cpp:1186         (model FP_linear)
  *     Collision_ESMC_new3  src/collisions.cpp:583             (model ESMC)
+ *     Collision_DSMC_VHS   src/collisions.cpp:2063            (model DSMC_VHS)
  *     vlasov_taking_the_integral src/Main_Functions.cpp:3582  (long_range 1, 1-D)
  *     poisson_solver       src/Main_Functions.cpp:3285        (long_range 3, 1-D)
  *     compute_Vlasov_2D    src/FEM.cpp:613                    (long_range 1, 2-D)
@@ -49,7 +51,7 @@
 extern "C" {
 #endif
 
-#define MCPM_ABI_VERSION 1
+#define MCPM_ABI_VERSION 2
 
 /* ---- status codes (bit flags may be OR-ed in the device status word) ---- */
 enum mcpm_status {
@@ -80,9 +82,12 @@ enum mcpm_model {
   MCPM_MODEL_FP_DENSE = 1,      /* "FP_dense"   (Enskog-Fokker-Planck)          */
   MCPM_MODEL_FP_IDEAL_GAS = 2,  /* "FP_ideal_gas"                               */
   MCPM_MODEL_ESMC = 3,          /* "ESMC" (Enskog DSMC, Collision_ESMC_new3)    */
-  MCPM_MODEL_FP_LINEAR = 4      /* "FP_linear" (Velocity_FP_linear: Langevin
+  MCPM_MODEL_FP_LINEAR = 4,     /* "FP_linear" (Velocity_FP_linear: Langevin
                                    relaxation without the cubic drift,
                                    src/Fokker_Planck.cpp:1186-1283)             */
+  MCPM_MODEL_DSMC_VHS = 5       /* "DSMC_VHS" (Collision_DSMC_VHS: Bird's
+                                   no-time-counter DSMC with variable hard
+                                   spheres, src/collisions.cpp:2063-2141)       */
 };
 
 /* ---- long-range (Vlasov) force, gas.long_range (src/Main_Functions.cpp:1612) */
@@ -134,6 +139,9 @@ typedef struct mcpm_config {
   double  U_wall[4];      /* box.U_wall_1..4                                    */
   uint64_t seed;          /* Philox key                                         */
   int64_t max_particles;  /* capacity of the device particle arrays             */
+  double  crref;          /* gas.crref  VHS reference speed sqrt(kb T / m) of
+                             the initial temperature (src/myIO.cpp:2242);
+                             DSMC_VHS only, must then be > 0                    */
 } mcpm_config;
 
 /* Per-cell quantities exported by mcpm_get_cells as a [MCPM_CF_COUNT][C]
@@ -160,7 +168,8 @@ enum mcpm_cell_field {
   MCPM_CF_BETA = 59,      /* 3 */
   MCPM_CF_PHI = 62,       /* 3 */
   MCPM_CF_F2 = 65,        /* long-range force per cell (y component)     */
-  MCPM_CF_OMEGA_MAX = 66, /* ESMC majorant                                */
+  MCPM_CF_OMEGA_MAX = 66, /* ESMC majorant omega_max; for DSMC_VHS the
+                             cell's majorant relative speed crm          */
   MCPM_CF_DIVU = 67,
   MCPM_CF_COUNT = 68
 };
@@ -252,7 +261,9 @@ int mcpm_set_cell_field(mcpm_session* s, int32_t field, const double* values);
 /* Slot layout of the device copy: particle id held by every slot and the
    first slot of every cell (C+1 entries); valid after mcpm_cell_update. */
 int mcpm_get_layout(mcpm_session* s, int32_t* pid_by_slot, int32_t* off);
-/* ESMC majorant from the current cell T and n (src/main.cpp:250-269). */
+/* Collision majorants from the current cell T and n (src/main.cpp:250-269):
+   omega_max for ESMC, crm = 10 sqrt(kb T / m) for DSMC_VHS.  mcpm_step calls
+   it before its first step for those two models. */
 int mcpm_init_omega_max(mcpm_session* s);
 /* Launch on the caller's CUDA stream (cudaStream_t) instead of the
    session's own; NULL restores the session stream. */

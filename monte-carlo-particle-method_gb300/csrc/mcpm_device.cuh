@@ -80,6 +80,10 @@ __device__ __forceinline__ float r_log(float x) { return __logf(x); }
 __device__ __forceinline__ double r_log(double x) { return ::log(x); }
 __device__ __forceinline__ void r_sincos(float x, float* s, float* c) { __sincosf(x, s, c); }
 __device__ __forceinline__ void r_sincos(double x, double* s, double* c) { ::sincos(x, s, c); }
+__device__ __forceinline__ float r_pow(float x, float y) { return powf(x, y); }
+__device__ __forceinline__ double r_pow(double x, double y) { return ::pow(x, y); }
+__device__ __forceinline__ float r_acos(float x) { return acosf(x); }
+__device__ __forceinline__ double r_acos(double x) { return ::acos(x); }
 
 // ------------------------------------------------ constants in real type
 // The FP32 kernels read float copies prepared on the host, so that no

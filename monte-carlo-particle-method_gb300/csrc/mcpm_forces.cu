@@ -157,6 +157,113 @@ template <typename real> static int esmc_impl(Session& s) {
 }
 int launch_esmc(Session& s) { return s.prec == MCPM_FP32 ? esmc_impl<float>(s) : esmc_impl<double>(s); }
 
+// ============================================================ DSMC VHS
+// Collision_DSMC_VHS, src/collisions.cpp:2063-2141: Bird's no-time-counter
+// scheme inside each cell, one warp per cell (pairs never leave their cell,
+// so all cells run in one launch).  Cell I with N_I > 1 runs
+// m_I = floor(pi sigma^2 N_I n_I crm_I dt / 2 + u) candidates: two distinct
+// particles of the cell chosen uniformly (the reference redraws the second
+// until it differs, the same distribution), sigma_T = |g|^(2 - 2 visp)
+// crref^(2 visp - 1), accepted when sigma_T / crm_I > u, then an isotropic
+// post-collision relative velocity of the same magnitude (cos theta =
+// 2 a1 - 1, phi = 2 pi a2) about the pair's centre of mass.  As in the ESMC
+// kernel a warp draws 32 candidates and applies the longest prefix with
+// disjoint pairs, which equals processing them one after another.  The
+// majorant then becomes max(1.1 max sigma_T, 0.9 crm_I) (:2135).
+template <typename real>
+__global__ void __launch_bounds__(128) k_dsmc_vhs(DevConsts k, double* cell, const int32_t* off,
+                                                  const int32_t* cnt, PT2<real> p, const int32_t* dstep,
+                                                  uint32_t* status) {
+  const int lane = threadIdx.x & 31;
+  const int I = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (I >= k.C) return;
+  const int NI = cnt[I];
+  if (NI < 2) return;  // warp-uniform
+  const int C = k.C;
+  const int step = *dstep;
+  const double crm = cell[(size_t)MCPM_CF_OMEGA_MAX * C + I];
+  const double nI = cell[(size_t)MCPM_CF_N * C + I];
+  const double pi = 3.14159265358979323846;
+  const double Mc = pi * k.sigma * k.sigma * ((double)NI * nI) * crm * k.dt / 2.0;
+  const double mreal = r_floor(Mc + u01d(philox(k.seed, (uint32_t)I, (uint32_t)step, RNG_DSMC_M, 0u).x));
+  // a non-finite or absurd majorant would make the candidate loop unbounded
+  const double mcap = 64.0 * NI + 4096.0;
+  int mI = 0;
+  if (mreal >= 0.0 && mreal <= mcap) mI = (int)mreal;
+  else if (lane == 0) raise_status(status, MCPM_ERR_ITER_LIMIT);
+  constexpr bool F32 = sizeof(real) == 4;
+  const real e = (real)k.vhs_e, cr = (real)k.vhs_cr, crm_r = (real)crm, half = (real)0.5;
+  const int64_t o = off[I];
+  real seen = 0;
+  int base = 0;
+  while (base < mI) {
+    const int kc = base + lane;
+    const bool valid = kc < mI;
+    int64_t si = -1, sj = -1;
+    uint4 r = make_uint4(0u, 0u, 0u, 0u);
+    if (valid) {
+      r = philox(k.seed, (uint32_t)I, (uint32_t)step, RNG_DSMC, (uint32_t)kc);
+      const int a = pick(r.x, NI);
+      int b = pick(r.y, NI - 1);
+      b += (b >= a) ? 1 : 0;
+      si = o + a;
+      sj = o + b;
+    }
+    // longest prefix of candidates with pairwise disjoint particles
+    bool conflict = false;
+    for (int l = 0; l < 31; ++l) {
+      int64_t oi = __shfl_sync(FULL, si, l), oj = __shfl_sync(FULL, sj, l);
+      if (l < lane && valid && (oi == si || oi == sj || oj == si || oj == sj)) conflict = true;
+    }
+    const unsigned cm = __ballot_sync(FULL, conflict);
+    int take = cm ? (__ffs(cm) - 1) : 32;
+    if (take > mI - base) take = mI - base;
+    if (lane < take) {
+      const real u1i = p.U1[si], u2i = p.U2[si], u3i = p.U3[si];
+      const real u1j = p.U1[sj], u2j = p.U2[sj], u3j = p.U3[sj];
+      const real Vr = r_sqrt((u1i - u1j) * (u1i - u1j) + (u2i - u2j) * (u2i - u2j) + (u3i - u3j) * (u3i - u3j));
+      const real sigmat = r_pow(Vr, e) * cr;
+      if (sigmat - seen > (real)0) seen = sigmat;
+      const real uacc = F32 ? (real)u01f(r.z) : (real)u01d(r.z);
+      if (sigmat / crm_r > uacc) {
+        const uint32_t w2 = philox(k.seed, (uint32_t)I, (uint32_t)step, RNG_DSMC_ACC, (uint32_t)kc).x;
+        const real a1 = F32 ? (real)u01f(r.w) : (real)u01d(r.w);
+        const real a2 = F32 ? (real)u01f(w2) : (real)u01d(w2);
+        const real theta = r_acos((real)2.0 * a1 - (real)1.0);
+        const real ph = (real)2.0 * (real)pi * a2;
+        real st, ct, sp, cp;
+        r_sincos(theta, &st, &ct);
+        r_sincos(ph, &sp, &cp);
+        const real v0 = Vr * ct, v1 = Vr * st * cp, v2 = Vr * st * sp;
+        const real c0 = half * (u1i + u1j), c1 = half * (u2i + u2j), c2 = half * (u3i + u3j);
+        p.U1[si] = c0 + half * v0; p.U2[si] = c1 + half * v1; p.U3[si] = c2 + half * v2;
+        p.U1[sj] = c0 - half * v0; p.U2[sj] = c1 - half * v1; p.U3[sj] = c2 - half * v2;
+      }
+    }
+    __syncwarp();
+    base += take;
+  }
+#pragma unroll
+  for (int m = 16; m >= 1; m >>= 1) {
+    const real t = __shfl_xor_sync(FULL, seen, m);
+    seen = t > seen ? t : seen;
+  }
+  if (lane == 0) {
+    const double a = 1.1 * (double)seen, b = 0.9 * crm;
+    cell[(size_t)MCPM_CF_OMEGA_MAX * C + I] = a < b ? b : a;  // std::max(a, b)
+  }
+}
+
+template <typename real> static int dsmc_impl(Session& s) {
+  int n = sync_dstep(s);
+  const PBuf& b = s.P[s.cur];
+  PT2<real> p{(real*)b.x1, (real*)b.x2, (real*)b.U1, (real*)b.U2, (real*)b.U3};
+  const int blocks = (int)(((int64_t)s.C * 32 + 127) / 128);
+  k_dsmc_vhs<real><<<blocks, 128, 0, s.stream>>>(s.k, s.cell, s.off, s.cnt, p, s.dstep, s.status);
+  return n + 1;
+}
+int launch_dsmc_vhs(Session& s) { return s.prec == MCPM_FP32 ? dsmc_impl<float>(s) : dsmc_impl<double>(s); }
+
 // ESMC majorant initialisation, src/main.cpp:250-269
 __global__ void k_init_omega(DevConsts k, double* cell, double Ygas) {
   const int C = k.C;
@@ -167,7 +274,8 @@ __global__ void k_init_omega(DevConsts k, double* cell, double Ygas) {
   double crm = 10.0 * (thermal);
   double om = 4.0 * pi * k.sigma * k.sigma * crm * cell[(size_t)MCPM_CF_N * C + c] * k.dt;
   if (k.model == MCPM_MODEL_ESMC) om = om * Ygas;
-  cell[(size_t)MCPM_CF_OMEGA_MAX * C + c] = om;
+  // DSMC_VHS keeps cells[].crm, its majorant relative speed, in this field
+  cell[(size_t)MCPM_CF_OMEGA_MAX * C + c] = (k.model == MCPM_MODEL_DSMC_VHS) ? crm : om;
 }
 int launch_init_omega(Session& s) {
   double nb = s.k.n * s.k.b;

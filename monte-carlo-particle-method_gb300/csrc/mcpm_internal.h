@@ -56,7 +56,8 @@ enum : uint32_t {
 };
 
 // Counter-stream ids for the Philox draws (third counter word).
-enum : uint32_t { RNG_FP = 0, RNG_BC = 1, RNG_ESMC = 2, RNG_BIN = 3, RNG_ESMC_ACC = 4, RNG_ESMC_M = 5 };
+enum : uint32_t { RNG_FP = 0, RNG_BC = 1, RNG_ESMC = 2, RNG_BIN = 3, RNG_ESMC_ACC = 4, RNG_ESMC_M = 5,
+                  RNG_DSMC = 6, RNG_DSMC_ACC = 7, RNG_DSMC_M = 8 };
 
 struct DevConsts {
   int N0, N1, C;
@@ -75,6 +76,9 @@ struct DevConsts {
   // quotients of constants for the FP32 sessions' per-cell solve (formed
   // once on the host): m/(3 kb), m/kb, kb/m, 1/dy, 1/m
   double q_T, q_m_kb, q_kb_m, q_idy, q_im;
+  // DSMC_VHS: exponent 2 - 2 visp of the relative speed and the factor
+  // crref^(2 visp - 1) of sigma_T (src/collisions.cpp:2102)
+  double vhs_e, vhs_cr;
   // float copies for the FP32 kernels
   float f_dx, f_dy, f_L0, f_L1, f_dt, f_sigma, f_m, f_kb, f_Tw[4], f_Uw[4], f_idx, f_idy, f_eps_x, f_eps_y;
 };
@@ -164,7 +168,7 @@ struct Session {
   bool sorted = false;          // layout is sorted by key, cnt/off/lists valid
   bool needs_rebin = false;     // positions moved since the last binning
   bool have_particles = false;
-  bool omega_init = false;      // ESMC majorant initialised (src/main.cpp:250-269)
+  bool omega_init = false;      // ESMC / DSMC majorant initialised (src/main.cpp:250-269)
   int num_sms = 0;
   Tuning tune{};
   int64_t launches = 0;
@@ -216,6 +220,7 @@ int launch_solve(Session& s, int with_alpha);
 // (FP32 passes that bin the new positions)
 int launch_update(Session& s, uint32_t stages, int bc_call_base, bool slotted = false);
 int launch_esmc(Session& s);
+int launch_dsmc_vhs(Session& s);
 int launch_long_range(Session& s);
 int launch_init_omega(Session& s);
 // 2-D long range (mcpm_lr2d.cu): set-up / release, the nodal deposit of

@@ -141,7 +141,8 @@ int mcpm_session_create(const mcpm_config* cfg, mcpm_session** out) {
   if ((int64_t)c.n_cells[0] * c.n_cells[1] > (1 << 24)) return MCPM_ERR_ARG;
   if (c.max_particles > ((int64_t)1 << 31) - 1) return MCPM_ERR_ARG;
   if (c.precision != MCPM_FP64 && c.precision != MCPM_FP32) return MCPM_ERR_ARG;
-  if (c.model < MCPM_MODEL_NONE || c.model > MCPM_MODEL_FP_LINEAR) return MCPM_ERR_ARG;
+  if (c.model < MCPM_MODEL_NONE || c.model > MCPM_MODEL_DSMC_VHS) return MCPM_ERR_ARG;
+  if (c.model == MCPM_MODEL_DSMC_VHS && !(c.crref > 0)) return MCPM_ERR_ARG;
   if (c.problem != MCPM_PROBLEM_CLOSED_BOX && c.problem != MCPM_PROBLEM_COUETTE && c.problem != MCPM_PROBLEM_WALL &&
       c.problem != MCPM_PROBLEM_PERIODIC)
     return MCPM_ERR_ARG;
@@ -187,6 +188,8 @@ int mcpm_session_create(const mcpm_config* cfg, mcpm_session** out) {
   k.q_kb_m = c.kb / c.m;
   k.q_idy = 1.0 / k.dy;
   k.q_im = 1.0 / c.m;
+  k.vhs_e = 2.0 - 2.0 * c.visp;
+  k.vhs_cr = pow(c.crref, 2.0 * c.visp - 1.0);
   k.f_dx = (float)k.dx; k.f_dy = (float)k.dy; k.f_L0 = (float)k.L0; k.f_L1 = (float)k.L1;
   k.f_dt = (float)k.dt; k.f_sigma = (float)k.sigma; k.f_m = (float)k.m; k.f_kb = (float)k.kb;
   for (int i = 0; i < 4; ++i) { k.f_Tw[i] = (float)k.Tw[i]; k.f_Uw[i] = (float)k.Uw[i]; }
@@ -464,6 +467,7 @@ int mcpm_velocity_update(mcpm_session* s) {
   int n = 0;
   uint32_t stages = 0;
   if (s->cfg.model == MCPM_MODEL_ESMC) n += T_ESMC(launch_esmc(*s));
+  else if (s->cfg.model == MCPM_MODEL_DSMC_VHS) n += T_ESMC(launch_dsmc_vhs(*s));
   else if (is_fp_model(s->cfg.model)) stages |= ST_LOAD_XI | ST_FP;
   if (s->cfg.long_range != MCPM_LR_NONE) {
     n += long_range_force(s);
@@ -565,6 +569,7 @@ static int step_once(mcpm_session* s, uint32_t stages) {
   if (!branch) n += T_LR(launch_node_density(*s));
   s->nodes_valid = s->lr2d != nullptr;
   if (m == MCPM_MODEL_ESMC) n += T_ESMC(launch_esmc(*s));
+  else if (m == MCPM_MODEL_DSMC_VHS) n += T_ESMC(launch_dsmc_vhs(*s));
   if (branch) cudaStreamWaitEvent(s->stream, s->ev_join, 0);
   else if (s->cfg.long_range != MCPM_LR_NONE) n += long_range_force(s);
   const bool slot = s->use_slotted && (stages & ST_KEY);
@@ -701,7 +706,7 @@ static int read_judge(mcpm_session* s) {
 int mcpm_step(mcpm_session* s, int32_t n_steps) {
   if (!s || !s->have_particles || n_steps < 0) return fail(s, MCPM_ERR_STATE, "step: no particles");
   const int m = s->cfg.model;
-  if (m == MCPM_MODEL_ESMC && !s->omega_init) {
+  if ((m == MCPM_MODEL_ESMC || m == MCPM_MODEL_DSMC_VHS) && !s->omega_init) {
     // src/main.cpp:236-269: cell_update at the current positions, then the majorant
     int rc = mcpm_cell_update(s);
     if (rc) return rc;

@@ -25,7 +25,7 @@ OK = 0
 ERR_ARG, ERR_CUDA, ERR_OUT_OF_BOX, ERR_NAN, ERR_CAPACITY, ERR_BC_LOOP, ERR_ITER_LIMIT, ERR_STATE = (
     1, 2, 4, 8, 16, 32, 64, 128)
 PROBLEM_CLOSED_BOX, PROBLEM_COUETTE, PROBLEM_WALL, PROBLEM_PERIODIC = 1, 2, 11, 100
-MODEL_NONE, MODEL_FP_DENSE, MODEL_FP_IDEAL_GAS, MODEL_ESMC, MODEL_FP_LINEAR = 0, 1, 2, 3, 4
+MODEL_NONE, MODEL_FP_DENSE, MODEL_FP_IDEAL_GAS, MODEL_ESMC, MODEL_FP_LINEAR, MODEL_DSMC_VHS = 0, 1, 2, 3, 4, 5
 LR_NONE, LR_DIRECT, LR_SCREENED_POISSON = 0, 1, 3
 FP64, FP32 = 0, 1
 RNG_PHILOX, RNG_INJECTED = 0, 1
@@ -49,7 +49,7 @@ class Config(C.Structure):
         ("T0", C.c_double), ("mu", C.c_double), ("visp", C.c_double), ("b", C.c_double), ("dt", C.c_double),
         ("phi", C.c_double), ("eqdist", C.c_double), ("ast", C.c_double), ("bst", C.c_double),
         ("T_wall", C.c_double * 4), ("U_wall", C.c_double * 4), ("seed", C.c_uint64),
-        ("max_particles", C.c_int64),
+        ("max_particles", C.c_int64), ("crref", C.c_double),
     ]
 
     def copy(self):

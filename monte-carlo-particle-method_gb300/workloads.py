@@ -16,7 +16,7 @@ import math
 
 import numpy as np
 
-from mcpm import (Config, derive, FP32, FP64, LR_DIRECT, LR_NONE, LR_SCREENED_POISSON, MODEL_ESMC,
+from mcpm import (Config, derive, FP32, FP64, LR_DIRECT, LR_NONE, LR_SCREENED_POISSON, MODEL_DSMC_VHS, MODEL_ESMC,
                   MODEL_FP_DENSE, PROBLEM_CLOSED_BOX, PROBLEM_COUETTE, PROBLEM_PERIODIC)
 
 BASE_SEED = 0x4D43504D
@@ -127,6 +127,15 @@ def esmc_box_2d(n_cells=(256, 256), ppc=100, precision=FP32, seed=BASE_SEED + 2,
     U1, U2, U3 = rng.normal(0, s, N), rng.normal(0, s, N), rng.normal(0, s, N)
     derive(c, N)
     return c, dict(x1=x1, x2=x2, U1=U1, U2=U2, U3=U3)
+
+
+def with_dsmc_vhs(cfg, T=1.0):
+    """The same box with Bird's DSMC (Collision_DSMC_VHS) as the collision
+    model; crref = sqrt(kb T / m) of the initial temperature, as
+    readSettingsFile sets it (src/myIO.cpp:2242)."""
+    cfg.model = MODEL_DSMC_VHS
+    cfg.crref = math.sqrt(cfg.kb * T / cfg.m)
+    return cfg
 
 
 def lognormal_counts(n_cells, seed, median=100, lo=10, hi=5000, target=None, s=None):

@@ -17,7 +17,8 @@
 #define CELL(s, c, f) ((s)->cell[(size_t)(c) * CF + (f)])
 
 enum { RNG_STREAM_FP = 0, RNG_STREAM_BC = 1, RNG_STREAM_ESMC = 2,
-       RNG_STREAM_BIN = 3, RNG_STREAM_ESMC_ACC = 4, RNG_STREAM_ESMC_M = 5 };
+       RNG_STREAM_BIN = 3, RNG_STREAM_ESMC_ACC = 4, RNG_STREAM_ESMC_M = 5,
+       RNG_STREAM_DSMC = 6, RNG_STREAM_DSMC_ACC = 7, RNG_STREAM_DSMC_M = 8 };
 
 struct orc_state {
   mcpm_config cfg;
@@ -852,6 +853,58 @@ void orc_esmc(orc_state* s, const double* x1, const double* x2, double* U1,
         for (int j = cx; j < s->N0; j += Sx) esmc_cell(s, k * s->N0 + j, x1, x2, U1, U2, U3);
 }
 
+/* -------------------------------------------------------------- DSMC VHS -- */
+/* Collision_DSMC_VHS, src/collisions.cpp:2063-2141, restated with
+   counter-based draws.  Per cell I with N_I > 1: the reference loops while
+   cand < floor(M + u) with a fresh u per test (:2090), which stops after
+   floor(M) or floor(M) + 1 candidates with the probabilities of
+   floor(M + u); here one u gives that count.  Each candidate takes two
+   distinct particles of the cell uniformly (the reference redraws the
+   second until it differs, :2092-2096: the same distribution),
+   sigma_T = |g|^(2 - 2 visp) crref^(2 visp - 1) (:2102), the running maximum
+   of sigma_T, acceptance sigma_T / crm > u (:2106) and on acceptance an
+   isotropic relative velocity of the same magnitude about the pair's centre
+   of mass (:2107-2127).  Finally crm = max(1.1 max sigma_T, 0.9 crm) (:2135).
+   The cell's crm lives in the OMEGA_MAX field. */
+static void dsmc_cell(orc_state* s, int I, double* U1, double* U2, double* U3) {
+  const mcpm_config* g = &s->cfg;
+  const double pi = acos(-1.0);
+  int NI = s->cnt[I];
+  if (NI <= 1) return;
+  uint32_t r[4], ra[4];
+  double crm_cell = CELL(s, I, MCPM_CF_OMEGA_MAX);
+  philox(g->seed, (uint32_t)I, (uint32_t)s->step, RNG_STREAM_DSMC_M, 0, r);
+  double M_cand = pi * g->sigma * g->sigma * ((double)NI * CELL(s, I, MCPM_CF_N)) * crm_cell * g->dt / 2.0;
+  int mI = (int)floor(M_cand + u01(r[0]));
+  double crm = 0.0;
+  double crfac = pow(g->crref, 2.0 * g->visp - 1.0);
+  for (int k = 0; k < mI; ++k) {
+    philox(g->seed, (uint32_t)I, (uint32_t)s->step, RNG_STREAM_DSMC, (uint32_t)k, r);
+    int a = pick(r[0], NI), b = pick(r[1], NI - 1);
+    if (b >= a) b += 1;
+    int i = s->list[s->off[I] + a], j = s->list[s->off[I] + b];
+    double Vr = sqrt((U1[i] - U1[j]) * (U1[i] - U1[j]) + (U2[i] - U2[j]) * (U2[i] - U2[j]) +
+                     (U3[i] - U3[j]) * (U3[i] - U3[j]));
+    double sigmat = pow(Vr, (2.0 - 2.0 * g->visp)) * crfac;
+    if (sigmat - crm > 0.0) crm = sigmat;
+    if (sigmat / crm_cell > u01(r[2])) {
+      philox(g->seed, (uint32_t)I, (uint32_t)s->step, RNG_STREAM_DSMC_ACC, (uint32_t)k, ra);
+      double theta = acos(2.0 * u01(r[3]) - 1.0);
+      double phi = 2.0 * pi * u01(ra[0]);
+      double v0 = Vr * cos(theta), v1 = Vr * sin(theta) * cos(phi), v2 = Vr * sin(theta) * sin(phi);
+      double c0 = 0.5 * (U1[i] + U1[j]), c1 = 0.5 * (U2[i] + U2[j]), c2 = 0.5 * (U3[i] + U3[j]);
+      U1[i] = c0 + 0.5 * v0; U2[i] = c1 + 0.5 * v1; U3[i] = c2 + 0.5 * v2;
+      U1[j] = c0 - 0.5 * v0; U2[j] = c1 - 0.5 * v1; U3[j] = c2 - 0.5 * v2;
+    }
+  }
+  double x = 1.1 * crm, y = 0.9 * crm_cell;
+  CELL(s, I, MCPM_CF_OMEGA_MAX) = x < y ? y : x;
+}
+
+void orc_dsmc_vhs(orc_state* s, double* U1, double* U2, double* U3) {
+  for (int I = 0; I < s->C; ++I) dsmc_cell(s, I, U1, U2, U3);
+}
+
 /* ESMC majorant initialisation, src/main.cpp:250-269 */
 void orc_init_omega_max(orc_state* s) {
   const mcpm_config* g = &s->cfg;
@@ -861,7 +914,8 @@ void orc_init_omega_max(orc_state* s) {
     double crm = 10.0 * (thermal);
     double om = 4.0 * pi * g->sigma * g->sigma * crm * CELL(s, num, MCPM_CF_N) * g->dt;
     if (g->model == MCPM_MODEL_ESMC) om = om * Ycoll(s, g->n);
-    CELL(s, num, MCPM_CF_OMEGA_MAX) = om;
+    /* DSMC_VHS keeps cells[].crm in this field */
+    CELL(s, num, MCPM_CF_OMEGA_MAX) = (g->model == MCPM_MODEL_DSMC_VHS) ? crm : om;
   }
 }
 
@@ -1505,6 +1559,8 @@ void orc_step(orc_state* s, double* x1, double* x2, double* x1_old,
     orc_velocity_fp(s, U1, U2, U3, s->xi, s->xi + N, s->xi + 2 * N);
   } else if (m == MCPM_MODEL_ESMC) {
     orc_esmc(s, x1, x2, U1, U2, U3);
+  } else if (m == MCPM_MODEL_DSMC_VHS) {
+    orc_dsmc_vhs(s, U1, U2, U3);
   }
   if (s->cfg.direction[0] == 1) orc_long_range_2d(s, x1, x2, U1, U2, NULL);
   else orc_long_range(s, U2);

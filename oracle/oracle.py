@@ -56,6 +56,7 @@ def _load_oracle():
         "orc_random_generator": (None, [vp, dp, dp, dp]),
         "orc_velocity_fp": (None, [vp, dp, dp, dp, dp, dp, dp]),
         "orc_esmc": (None, [vp, dp, dp, dp, dp, dp]),
+        "orc_dsmc_vhs": (None, [vp, dp, dp, dp]),
         "orc_long_range": (None, [vp, dp]),
         "orc_dfp_extra_streaming": (None, [vp, dp, dp, dp, dp, dp]),
         "orc_apply_bc": (None, [vp, C.c_int, dp, dp, dp, dp, dp, dp, dp]),
@@ -177,6 +178,11 @@ class Oracle:
         s = self.s
         self.L.orc_esmc(self.h, _dp(s.x1), _dp(s.x2), _dp(s.U1), _dp(s.U2), _dp(s.U3))
 
+    def dsmc(self):
+        """Collision_DSMC_VHS (src/collisions.cpp:2063-2141)"""
+        s = self.s
+        self.L.orc_dsmc_vhs(self.h, _dp(s.U1), _dp(s.U2), _dp(s.U3))
+
     def long_range(self):
         """velocity_update's long-range kick: the 1-D face paths, or the 2-D
         node paths when the box is 2-D (returns the node potential then)."""
@@ -275,6 +281,7 @@ def ref_lib(build=True):
         "ref_store_old_positions": (None, [vp, dp, dp, dp, dp]),
         "ref_stream": (None, [vp, dp, dp, dp, dp, dp, dp, dp, ip]),
         "ref_esmc": (None, [vp, dp, dp, dp, dp, dp, ip]),
+        "ref_dsmc_vhs": (None, [vp, dp, dp, dp, dp, dp]),
         "ref_init_omega_max": (None, [vp]),
         "ref_get_cells": (None, [vp, dp]),
         "ref_long_range_2d": (None, [vp, dp, dp, dp, dp, ip]),
@@ -364,6 +371,10 @@ class Reference:
     def esmc(self):
         s = self.s
         self.L.ref_esmc(self.h, _dp(s.U1), _dp(s.U2), _dp(s.U3), _dp(s.x1), _dp(s.x2), _ip(s.index))
+
+    def dsmc(self):
+        s = self.s
+        self.L.ref_dsmc_vhs(self.h, _dp(s.U1), _dp(s.U2), _dp(s.U3), _dp(s.x1), _dp(s.x2))
 
     def init_omega_max(self):
         self.L.ref_init_omega_max(self.h)

@@ -98,6 +98,7 @@ static const char* model_name(int m) {
     case MCPM_MODEL_FP_IDEAL_GAS: return "FP_ideal_gas";
     case MCPM_MODEL_ESMC: return "ESMC";
     case MCPM_MODEL_FP_LINEAR: return "FP_linear";
+    case MCPM_MODEL_DSMC_VHS: return "DSMC_VHS";
     default: return "none";
   }
 }
@@ -113,6 +114,7 @@ void* ref_create(const mcpm_config* c, long N) {
   g.T0 = c->T0; g.mu = c->mu; g.visp = c->visp; g.b = c->b; g.delta_t = c->dt;
   g.phi = c->phi; g.eqdist = c->eqdist; g.ast = c->ast; g.bst = c->bst;
   g.long_range = c->long_range; g.model = model_name(c->model); g.N = N;
+  g.crref = c->crref;
   g.n_ratio = 1; g.times = 1.0;
   for (int i = 0; i < 3; ++i) {
     b.N[i] = c->n_cells[i]; b.Len[i] = c->length[i];
@@ -241,6 +243,14 @@ void ref_esmc(void* h, double* U1, double* U2, double* U3, double* x1, double* x
   Collision_ESMC_new3(U1, U2, U3, x1, x2, &r->gas, &r->box, r->cells, index);
 }
 
+void ref_dsmc_vhs(void* h, double* U1, double* U2, double* U3, double* x1, double* x2) {
+  Quiet q;
+  Ref* r = (Ref*)h;
+  Collision DSMC;
+  std::memset(&DSMC, 0, sizeof(DSMC));
+  Collision_DSMC_VHS(U1, U2, U3, x1, x2, &r->gas, &r->box, r->cells, &DSMC);
+}
+
 void ref_init_omega_max(void* h) {
   // src/main.cpp:250-269
   Ref* r = (Ref*)h;
@@ -279,7 +289,7 @@ void ref_get_cells(void* h, double* out) {
     for (int i = 0; i < 3; ++i) o[MCPM_CF_BETA + i] = k.beta[i];
     for (int i = 0; i < 3; ++i) o[MCPM_CF_PHI + i] = k.phi[i];
     o[MCPM_CF_F2] = k.F2;
-    o[MCPM_CF_OMEGA_MAX] = k.omega_max;
+    o[MCPM_CF_OMEGA_MAX] = (r->gas.model == "DSMC_VHS") ? k.crm : k.omega_max;
     o[MCPM_CF_DIVU] = k.divU;
   }
 }

@@ -44,7 +44,7 @@ def _oracle_run(cfg, parts, seed, steps):
     c.seed = seed
     c.precision = mcpm.FP64
     o = Oracle(c, parts)
-    if c.model == mcpm.MODEL_ESMC:
+    if c.model in (mcpm.MODEL_ESMC, mcpm.MODEL_DSMC_VHS):
         # the majorant from the initial cells (src/main.cpp:236-269), as mcpm_step does
         o.cell_update()
         o.init_omega_max()
@@ -90,3 +90,14 @@ def test_esmc_ensemble_matches_oracle(cuda_ok):
     gpu = np.array([_gpu_run(cfg, parts, 1 + r, steps) for r in range(R)])
     orc = np.array([_oracle_run(cfg, parts, 1001 + r, steps) for r in range(R)])
     _compare(gpu, orc, "ESMC")
+
+
+def test_dsmc_ensemble_matches_oracle(cuda_ok):
+    """Bird's DSMC (Collision_DSMC_VHS) in the same hot-wall box, FP32
+    state: 32 replicas, 6 steps."""
+    R, steps = 32, 6
+    cfg, parts = W.esmc_box_2d(n_cells=(8, 8), precision=mcpm.FP32)
+    W.with_dsmc_vhs(cfg)
+    gpu = np.array([_gpu_run(cfg, parts, 1 + r, steps) for r in range(R)])
+    orc = np.array([_oracle_run(cfg, parts, 1001 + r, steps) for r in range(R)])
+    _compare(gpu, orc, "DSMC")

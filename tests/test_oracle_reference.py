@@ -178,3 +178,43 @@ def test_fp_linear_routines_bit_exact(built, step):
     o2.random_generator()
     o2.velocity_fp()
     assert not np.array_equal(o2.s.U1, orc.s.U1)
+
+
+def _dsmc_cfg(n_cells=8, ppc=400):
+    cfg, parts = W.homogeneous_relaxation_1d(n_cells=n_cells, ppc=ppc)
+    return W.with_dsmc_vhs(cfg), parts
+
+
+def test_dsmc_vhs_reference_statistics(built):
+    """Collision_DSMC_VHS draws from std::random_device; compare the
+    restatement statistically: the anisotropic temperature relaxes at the
+    same rate within 4 sigma, collisions conserve momentum and energy, and
+    the majorant crm follows max(1.1 max sigma_T, 0.9 crm) alike."""
+    _ref_or_skip()
+    cfg, parts = _dsmc_cfg()
+    rates, crms = {}, {}
+    for name, cls in (("orc", O.Oracle), ("ref", O.Reference)):
+        vals, cr = [], []
+        for rep in range(8):
+            cfg.seed = 2000 + rep
+            o = cls(cfg, parts)
+            o.set_step(0)
+            o.cell_update()
+            o.init_omega_max()
+            Tx0 = np.var(o.s.U1)
+            for st in range(1, 4):
+                o.set_step(st)
+                o.cell_update()
+                o.dsmc()
+            vals.append((Tx0 - np.var(o.s.U1)) / Tx0)
+            cr.append(mcpm.cell_field(o.cells(), "OMEGA_MAX", True).mean())
+            assert abs(o.s.U1.sum() - parts["U1"].sum()) < 1e-8
+            e0 = (parts["U1"] ** 2 + parts["U2"] ** 2 + parts["U3"] ** 2).sum()
+            e1 = (o.s.U1 ** 2 + o.s.U2 ** 2 + o.s.U3 ** 2).sum()
+            assert abs(e1 - e0) < 1e-8 * e0
+        rates[name] = (np.mean(vals), np.std(vals) / np.sqrt(len(vals)))
+        crms[name] = np.mean(cr)
+    (mo, so), (mr, sr) = rates["orc"], rates["ref"]
+    assert mo > 0.05 and mr > 0.05
+    assert abs(mo - mr) < 4 * np.hypot(so, sr) + 0.02 * mr
+    assert abs(crms["orc"] - crms["ref"]) < 0.05 * crms["ref"]
