@@ -94,6 +94,8 @@ enum mcpm_model {
 enum mcpm_long_range {
   MCPM_LR_NONE = 0,
   MCPM_LR_DIRECT = 1,           /* 1-D vlasov_taking_the_integral               */
+  MCPM_LR_DENSITY_EXPANSION = 2, /* density-gradient force from the kernel-
+                                   smoothed density (src/Main_Functions.cpp:1632-1653) */
   MCPM_LR_SCREENED_POISSON = 3  /* 1-D poisson_solver (Green's-function BC)     */
 };
 
@@ -167,11 +169,21 @@ enum mcpm_cell_field {
   MCPM_CF_ALPHA = 50,     /* 9 */
   MCPM_CF_BETA = 59,      /* 3 */
   MCPM_CF_PHI = 62,       /* 3 */
-  MCPM_CF_F2 = 65,        /* long-range force per cell (y component)     */
+  MCPM_CF_F2 = 65,        /* long-range force per cell (y component); for
+                             long_range 2 the kick -dummyF of
+                             src/Main_Functions.cpp:1647, 0 in the
+                             first cell and in cell N[1]-1               */
   MCPM_CF_OMEGA_MAX = 66, /* ESMC majorant omega_max; for DSMC_VHS the
                              cell's majorant relative speed crm          */
   MCPM_CF_DIVU = 67,
-  MCPM_CF_COUNT = 68
+  MCPM_CF_N_SMOOTH = 68,  /* kernel-smoothed density and its first and
+                             third y-derivative sums (cell_update,
+                             src/Main_Functions.cpp:2378-2427); computed
+                             when long_range is 2, the only consumer,
+                             else 0                                      */
+  MCPM_CF_DN2 = 69,
+  MCPM_CF_DN3 = 70,
+  MCPM_CF_COUNT = 71
 };
 
 typedef struct mcpm_session mcpm_session;

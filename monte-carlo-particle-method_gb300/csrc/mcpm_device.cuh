@@ -83,6 +83,8 @@ __device__ __forceinline__ void r_sincos(double x, double* s, double* c) { ::sin
 __device__ __forceinline__ float r_pow(float x, float y) { return powf(x, y); }
 __device__ __forceinline__ double r_pow(double x, double y) { return ::pow(x, y); }
 __device__ __forceinline__ float r_acos(float x) { return acosf(x); }
+__device__ __forceinline__ float r_exp(float x) { return expf(x); }
+__device__ __forceinline__ double r_exp(double x) { return ::exp(x); }
 __device__ __forceinline__ double r_acos(double x) { return ::acos(x); }
 
 // ------------------------------------------------ constants in real type

@@ -442,8 +442,85 @@ __global__ void __launch_bounds__(1024) k_long_range_1d(DevConsts k, double* cel
   }
 }
 
+// ============================================ density expansion (long_range 2)
+// The kernel smoothing of cell_update (src/Main_Functions.cpp:2378-2427): at
+// the centre of every cell, a Gaussian of width h = dy/2 cut at r_cut = 2 dy
+// over the particles of rows k-2..k+2 of its column (a row past a wall takes
+// the wall row's particles shifted by whole cells) gives n_smooth and the
+// derivative sums dn2 and dn3.  velocity_update's density-expansion force
+// (:1632-1653) is then dummyF = dn2 4 pi (sigma 2^(1/6))^3 phi / m 2, applied
+// as U2 -= dummyF dt except in cell 0 and cell N[1]-1 (the reference compares
+// the linear cell index with N[1]-1, kept as it is); F2 holds -dummyF, and
+// the particle pass's kick adds F2 dt.  One warp per cell: each lane sums its
+// share of the ~5 cells' particles, the warp reduces in double.
+template <typename real>
+__global__ void __launch_bounds__(128) k_smoothing(DevConsts k, double* cell, float* pcell, const int32_t* off,
+                                                   const int32_t* cnt, const real* x2) {
+  const int lane = threadIdx.x & 31;
+  const int num = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (num >= k.C) return;
+  const int C = k.C;
+  const int j = num % k.N0, kr = num / k.N0;
+  const double dy = k.dy;
+  const double r1 = 0.5 * ((double)kr * dy + (double)(kr + 1) * dy);  // cell_center[1], src/myIO.cpp:1466
+  const double r_cut = 2.0 * dy, h = r_cut / 4.0;
+  const int search = (int)floor(r_cut / dy);
+  // per-term factors, in the order the reference forms them
+  const real a_n = (real)(k.Fn / k.de_s2p / h), a_w = (real)(1.0 / k.de_s2p / h), ih2 = (real)(-1.0 / h / h);
+  const real ih2p = (real)(1.0 / h / h), s2h2 = (real)k.de_s2h2, mb = (real)k.Fn, h_r = (real)h;
+  const real r1_r = (real)r1, rc_r = (real)r_cut;
+  real ns = 0, d2 = 0, d3 = 0;
+  for (int kk = kr - search; kk <= kr + search; ++kk) {
+    const int kkk = kk < 0 ? 0 : (kk > k.N1 - 1 ? k.N1 - 1 : kk);
+    const int num2 = kkk * k.N0 + j;
+    const int64_t o = off[num2];
+    const int n2 = cnt[num2];
+    const real shift = (real)((double)(kk - kkk) * dy);
+    for (int i = lane; i < n2; i += 32) {
+      const real r2 = x2[o + i] + shift;
+      const real r1r2 = r2 - r1_r;
+      const real rr = r2 > r1_r ? r1r2 : -r1r2;
+      if (rr < rc_r) {
+        const real e = r_exp(-rr * rr / h_r / h_r / (real)2.0);
+        ns += a_n * e;
+        const real W = a_w * e;
+        d2 += mb * W * r1r2 * ih2;
+        d3 += mb * W * s2h2 * ((real)3.0 * r1r2 - ih2p * r1r2 * r1r2 * r1r2);
+      }
+    }
+  }
+  double dns = (double)ns, dd2 = (double)d2, dd3 = (double)d3;
+#pragma unroll
+  for (int m = 16; m >= 1; m >>= 1) {
+    dns += __shfl_xor_sync(FULL, dns, m);
+    dd2 += __shfl_xor_sync(FULL, dd2, m);
+    dd3 += __shfl_xor_sync(FULL, dd3, m);
+  }
+  if (lane == 0) {
+    cell[(size_t)MCPM_CF_N_SMOOTH * C + num] = dns;
+    cell[(size_t)MCPM_CF_DN2 * C + num] = dd2;
+    cell[(size_t)MCPM_CF_DN3 * C + num] = dd3;
+    const double pi = 3.14159265358979323846;
+    const double dummyF = dd2 * 4.0 * pi * k.de_p * k.phi / k.m * 2.0;
+    const double F2 = (num != 0 && num != k.N1 - 1) ? -dummyF : 0.0;
+    cell[(size_t)MCPM_CF_F2 * C + num] = F2;
+    if (pcell) pcell[(size_t)num * PF_STRIDE + PF_F2DT] = (float)(F2 * k.dt);
+  }
+}
+
+int launch_smoothing(Session& s) {
+  const PBuf& b = s.P[s.cur];
+  const int blocks = (int)(((int64_t)s.C * 32 + 127) / 128);
+  if (s.prec == MCPM_FP32)
+    k_smoothing<float><<<blocks, 128, 0, s.stream>>>(s.k, s.cell, s.pcell, s.off, s.cnt, (const float*)b.x2);
+  else
+    k_smoothing<double><<<blocks, 128, 0, s.stream>>>(s.k, s.cell, nullptr, s.off, s.cnt, (const double*)b.x2);
+  return 1;
+}
+
 int launch_long_range(Session& s) {
   const int mode = s.cfg.long_range;
+  if (mode == MCPM_LR_DENSITY_EXPANSION) return launch_smoothing(s);
   if (mode != MCPM_LR_DIRECT && mode != MCPM_LR_SCREENED_POISSON) return 0;
   if (s.k.lr2d) return launch_long_range_2d(s);
   const LRTab* t = reinterpret_cast<const LRTab*>(s.lr_host);

@@ -79,6 +79,9 @@ struct DevConsts {
   // DSMC_VHS: exponent 2 - 2 visp of the relative speed and the factor
   // crref^(2 visp - 1) of sigma_T (src/collisions.cpp:2102)
   double vhs_e, vhs_cr;
+  // density expansion: pow(sigma 2^(1/6), 3) (src/Main_Functions.cpp:1647),
+  // sqrt(2 pi) and pow(1/h/h, 2) with h = dy/2 of the kernel smoothing (:2380-2393)
+  double de_p, de_s2p, de_s2h2;
   // float copies for the FP32 kernels
   float f_dx, f_dy, f_L0, f_L1, f_dt, f_sigma, f_m, f_kb, f_Tw[4], f_Uw[4], f_idx, f_idy, f_eps_x, f_eps_y;
 };
@@ -221,6 +224,7 @@ int launch_solve(Session& s, int with_alpha);
 int launch_update(Session& s, uint32_t stages, int bc_call_base, bool slotted = false);
 int launch_esmc(Session& s);
 int launch_dsmc_vhs(Session& s);
+int launch_smoothing(Session& s);
 int launch_long_range(Session& s);
 int launch_init_omega(Session& s);
 // 2-D long range (mcpm_lr2d.cu): set-up / release, the nodal deposit of

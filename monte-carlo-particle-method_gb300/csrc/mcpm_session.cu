@@ -146,9 +146,11 @@ int mcpm_session_create(const mcpm_config* cfg, mcpm_session** out) {
   if (c.problem != MCPM_PROBLEM_CLOSED_BOX && c.problem != MCPM_PROBLEM_COUETTE && c.problem != MCPM_PROBLEM_WALL &&
       c.problem != MCPM_PROBLEM_PERIODIC)
     return MCPM_ERR_ARG;
-  if (c.long_range != MCPM_LR_NONE && c.long_range != MCPM_LR_DIRECT && c.long_range != MCPM_LR_SCREENED_POISSON)
+  if (c.long_range != MCPM_LR_NONE && c.long_range != MCPM_LR_DIRECT && c.long_range != MCPM_LR_SCREENED_POISSON &&
+      c.long_range != MCPM_LR_DENSITY_EXPANSION)
     return MCPM_ERR_ARG;
-  if (c.long_range != MCPM_LR_NONE) {
+  // the density-expansion force works per column of cells in any box
+  if (c.long_range != MCPM_LR_NONE && c.long_range != MCPM_LR_DENSITY_EXPANSION) {
     if (c.direction[0] == 1) {
       // 2-D: the node-grid paths of src/FEM.cpp; the screened-Poisson solve
       // needs interior nodes and keeps two dense DST matrices of order <= 2047
@@ -181,7 +183,15 @@ int mcpm_session_create(const mcpm_config* cfg, mcpm_session** out) {
   k.b = c.b; k.dt = c.dt; k.phi = c.phi; k.eqdist = c.eqdist; k.ast = c.ast; k.bst = c.bst;
   for (int i = 0; i < 4; ++i) { k.Tw[i] = c.T_wall[i]; k.Uw[i] = c.U_wall[i]; }
   k.seed = c.seed;
-  k.lr2d = (c.long_range != MCPM_LR_NONE && c.direction[0] == 1) ? 1 : 0;
+  k.lr2d = (c.long_range != MCPM_LR_NONE && c.long_range != MCPM_LR_DENSITY_EXPANSION && c.direction[0] == 1) ? 1 : 0;
+  // 4 pi (sigma 2^(1/6))^3 of the density-expansion force, the pow factor
+  // formed once as src/Main_Functions.cpp:1647 forms it
+  k.de_p = pow(c.sigma * pow(2.0, 1.0 / 6.0), 3.0);
+  k.de_s2p = sqrt(2.0 * acos(-1.0));
+  {
+    const double h = 2.0 * k.dy / 4.0;
+    k.de_s2h2 = pow(1.0 / h / h, 2.0);
+  }
   k.lr_coef = c.long_range == MCPM_LR_DIRECT ? c.phi : c.ast;
   k.q_T = c.m / (3.0 * c.kb);
   k.q_m_kb = c.m / c.kb;
@@ -452,6 +462,8 @@ int mcpm_cell_update(mcpm_session* s) {
   n += T_SOLVE(launch_solve(*s, (s->cfg.model == MCPM_MODEL_FP_DENSE && s->step > 0) ? 1 : 0));
   n += T_LR(launch_node_density(*s));  // n_n (src/Main_Functions.cpp:2268-2364), 2-D screened Poisson only
   s->nodes_valid = s->lr2d != nullptr;
+  // kernel smoothing (src/Main_Functions.cpp:2378-2427), for long_range 2
+  if (s->cfg.long_range == MCPM_LR_DENSITY_EXPANSION) n += T_LR(launch_smoothing(*s));
   return after_launch(s, n, "cell_update");
 }
 

@@ -26,18 +26,20 @@ ERR_ARG, ERR_CUDA, ERR_OUT_OF_BOX, ERR_NAN, ERR_CAPACITY, ERR_BC_LOOP, ERR_ITER_
     1, 2, 4, 8, 16, 32, 64, 128)
 PROBLEM_CLOSED_BOX, PROBLEM_COUETTE, PROBLEM_WALL, PROBLEM_PERIODIC = 1, 2, 11, 100
 MODEL_NONE, MODEL_FP_DENSE, MODEL_FP_IDEAL_GAS, MODEL_ESMC, MODEL_FP_LINEAR, MODEL_DSMC_VHS = 0, 1, 2, 3, 4, 5
-LR_NONE, LR_DIRECT, LR_SCREENED_POISSON = 0, 1, 3
+LR_NONE, LR_DIRECT, LR_DENSITY_EXPANSION, LR_SCREENED_POISSON = 0, 1, 2, 3
 FP64, FP32 = 0, 1
 RNG_PHILOX, RNG_INJECTED = 0, 1
 
 CF = dict(NUM_INSIDE=0, U_SPACE=1, PIJ=4, M3=10, M4=20, M5=26, Q=29, DM2=32, DM4=33, MP=34, T=37, N=38,
-          GAMMA_ST=39, LAMBDA=40, C=41, GAMMA=47, ALPHA=50, BETA=59, PHI=62, F2=65, OMEGA_MAX=66, DIVU=67)
-CF_COUNT = 68
+          GAMMA_ST=39, LAMBDA=40, C=41, GAMMA=47, ALPHA=50, BETA=59, PHI=62, F2=65, OMEGA_MAX=66, DIVU=67,
+          N_SMOOTH=68, DN2=69, DN3=70)
+CF_COUNT = 71
 K_NAMES = ["bin", "scan", "scatter", "moments", "solve", "esmc", "long_range", "update", "surrogate"]
 K_COUNT = len(K_NAMES)
 # (field, width) of every exported per-cell quantity
 CF_WIDTH = dict(NUM_INSIDE=1, U_SPACE=3, PIJ=6, M3=10, M4=6, M5=3, Q=3, DM2=1, DM4=1, MP=3, T=1, N=1,
-                GAMMA_ST=1, LAMBDA=1, C=6, GAMMA=3, ALPHA=9, BETA=3, PHI=3, F2=1, OMEGA_MAX=1, DIVU=1)
+                GAMMA_ST=1, LAMBDA=1, C=6, GAMMA=3, ALPHA=9, BETA=3, PHI=3, F2=1, OMEGA_MAX=1, DIVU=1,
+                N_SMOOTH=1, DN2=1, DN3=1)
 
 
 class Config(C.Structure):

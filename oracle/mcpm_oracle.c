@@ -624,6 +624,47 @@ static void phi_cells(orc_state* s) {
   }
 }
 
+/* Kernel smoothing of cell_update, src/Main_Functions.cpp:2378-2427: at the
+   centre of every cell a Gaussian of width h = dy/2, cut at r_cut = 2 dy,
+   over the particles of rows k-2..k+2 of its column (a row past a wall
+   takes the wall row's particles shifted by whole cells), summed in the
+   reference's order (column, row, neighbour row, particle id). */
+static void kernel_smoothing(orc_state* s, const double* x2) {
+  const double dy = s->dy;
+  double r_cut = 2.0 * dy, h = r_cut / 4.0;
+  double sqrt_pi = sqrt(2.0 * acos(-1.0));
+  int search = (int)floor(r_cut / dy);
+  double mb = s->cfg.Fn;
+  double s2h2 = pow(1.0 / h / h, 2.0);
+  for (int num = 0; num < s->C; ++num) {
+    CELL(s, num, MCPM_CF_N_SMOOTH) = 0.0;
+    CELL(s, num, MCPM_CF_DN2) = 0.0;
+    CELL(s, num, MCPM_CF_DN3) = 0.0;
+  }
+  for (int j = 0; j < s->N0; ++j)
+    for (int k = 0; k < s->N1; ++k) {
+      int num = k * s->N0 + j;
+      double d2 = (double)k * dy, d3 = (double)(k + 1) * dy;
+      double r1 = 0.5 * (d2 + d3);
+      for (int kk = k - search; kk <= k + search; ++kk) {
+        int kkk = kk < 0 ? 0 : (kk > s->N1 - 1 ? s->N1 - 1 : kk);
+        int num2 = kkk * s->N0 + j;
+        for (int i = 0; i < s->cnt[num2]; ++i) {
+          int64_t id = s->list[s->off[num2] + i];
+          double r2 = x2[id] + (kk - kkk) * dy;
+          double r1r2 = r2 - r1;
+          double rr = fabs(r2 - r1);
+          if (rr < r_cut) {
+            CELL(s, num, MCPM_CF_N_SMOOTH) += mb / sqrt_pi / h * exp(-rr * rr / h / h / 2.0);
+            double W = 1.0 / sqrt_pi / h * exp(-rr * rr / h / h / 2.0);
+            CELL(s, num, MCPM_CF_DN2) += mb * W * r1r2 * (-1.0 / h / h);
+            CELL(s, num, MCPM_CF_DN3) += mb * W * s2h2 * (3.0 * r1r2 - 1.0 / h / h * r1r2 * r1r2 * r1r2);
+          }
+        }
+      }
+    }
+}
+
 /* cell_update, src/Main_Functions.cpp:2138-2749, for the uniform Cartesian
    grid.  The kernel-density smoothing (:2378-2427) feeds only long_range 2,
    which is out of scope, and is not computed. */
@@ -632,6 +673,7 @@ void orc_cell_update(orc_state* s, const double* x1, const double* x2,
                      int32_t* index) {
   bin_particles(s, x1, x2);
   if (x1) node_density(s, x1, x2);
+  if (s->cfg.long_range == MCPM_LR_DENSITY_EXPANSION) kernel_smoothing(s, x2);
   if (index) memcpy(index, s->index, sizeof(int32_t) * (size_t)s->N);
   moments(s, U1, U2, U3);
   lambda_cells(s);
@@ -1018,8 +1060,28 @@ void orc_poisson_faces(orc_state* s, double* x) {
 
 /* long-range dispatch of velocity_update, src/Main_Functions.cpp:1618-1663,
    for the 1-D paths: F2 per cell from the face potential, U2 += F2 dt. */
+/* velocity_update's density-expansion force, src/Main_Functions.cpp:1632-1653:
+   the gradient sum dn2 of the kernel smoothing scaled by
+   4 pi (sigma 2^(1/6))^3 phi / m 2, subtracted (times dt) from U2 except in
+   cell 0 and in cell N[1]-1 (the linear cell index against N[1]-1, as the
+   reference writes it).  F2 records the kick, -dummyF. */
+static void density_expansion(orc_state* s, double* U2) {
+  const mcpm_config* g = &s->cfg;
+  const double pi = acos(-1);
+  for (int num = 0; num < s->C; ++num) {
+    double dummyF = CELL(s, num, MCPM_CF_DN2);
+    dummyF = dummyF * 4.0 * pi * pow(g->sigma * pow(2.0, 1.0 / 6.0), 3.0) * g->phi / g->m * 2.0;
+    CELL(s, num, MCPM_CF_F2) = (num != 0 && num != s->N1 - 1) ? -dummyF : 0.0;
+  }
+  for (int64_t id = 0; id < s->N; ++id) {
+    int num = s->index[id];
+    if (num != 0 && num != s->N1 - 1) U2[id] = U2[id] - (-CELL(s, num, MCPM_CF_F2)) * g->dt;
+  }
+}
+
 void orc_long_range(orc_state* s, double* U2) {
   const mcpm_config* g = &s->cfg;
+  if (g->long_range == MCPM_LR_DENSITY_EXPANSION) { density_expansion(s, U2); return; }
   if (g->long_range != MCPM_LR_DIRECT && g->long_range != MCPM_LR_SCREENED_POISSON) return;
   int nf = s->N1 + 1;
   double* V = (double*)malloc(sizeof(double) * nf);
@@ -1562,7 +1624,8 @@ void orc_step(orc_state* s, double* x1, double* x2, double* x1_old,
   } else if (m == MCPM_MODEL_DSMC_VHS) {
     orc_dsmc_vhs(s, U1, U2, U3);
   }
-  if (s->cfg.direction[0] == 1) orc_long_range_2d(s, x1, x2, U1, U2, NULL);
+  if (s->cfg.direction[0] == 1 && s->cfg.long_range != MCPM_LR_DENSITY_EXPANSION)
+    orc_long_range_2d(s, x1, x2, U1, U2, NULL);
   else orc_long_range(s, U2);
   if (m == MCPM_MODEL_FP_DENSE) orc_dfp_extra_streaming(s, U1, U2, U3, x1, x2);
   orc_apply_bc(s, 0, x1, x2, x1_old, x2_old, U1, U2, U3);

@@ -22,7 +22,7 @@ REPO = os.path.dirname(HERE)
 PKG = os.path.join(REPO, "monte-carlo-particle-method_gb300")
 if PKG not in sys.path:
     sys.path.insert(0, PKG)
-from mcpm import CF_COUNT, Config  # noqa: E402
+from mcpm import CF_COUNT, LR_DENSITY_EXPANSION, Config  # noqa: E402
 
 dp = C.POINTER(C.c_double)
 ip = C.POINTER(C.c_int32)
@@ -187,7 +187,7 @@ class Oracle:
         """velocity_update's long-range kick: the 1-D face paths, or the 2-D
         node paths when the box is 2-D (returns the node potential then)."""
         s = self.s
-        if self.cfg.direction[0] == 1:
+        if self.cfg.direction[0] == 1 and self.cfg.long_range != LR_DENSITY_EXPANSION:
             V = np.empty((self.cfg.n_cells[0] + 1) * (self.cfg.n_cells[1] + 1))
             self.L.orc_long_range_2d(self.h, _dp(s.x1), _dp(s.x2), _dp(s.U1), _dp(s.U2), _dp(V))
             return V
@@ -340,7 +340,7 @@ class Reference:
 
     def long_range(self):
         s = self.s
-        if self.cfg.direction[0] == 1:
+        if self.cfg.direction[0] == 1 and self.cfg.long_range != LR_DENSITY_EXPANSION:
             self.L.ref_long_range_2d(self.h, _dp(s.x1), _dp(s.x2), _dp(s.U1), _dp(s.U2), _ip(s.index))
         else:
             self.L.ref_long_range(self.h, _dp(s.x1), _dp(s.x2), _dp(s.U2), _ip(s.index))

@@ -21,6 +21,7 @@
 
 #include <cstdio>
 #include <cstring>
+#include <string>
 #include <vector>
 
 // ---------------------------------------------------------------- injected
@@ -187,6 +188,21 @@ void ref_velocity_fp(void* h, double* U1, double* U2, double* U3, int* index, do
 void ref_long_range(void* h, double* x1, double* x2, double* U2, int* index) {
   Quiet q;
   Ref* r = (Ref*)h;
+  if (r->gas.long_range == 2) {
+    // the density-expansion force is inline in velocity_update
+    // (src/Main_Functions.cpp:1632-1653): run velocity_update with no
+    // collision model so that only its long-range part acts
+    const std::string model = r->gas.model;
+    r->gas.model = "none";
+    Collision cba;
+    std::memset(&cba, 0, sizeof(cba));
+    std::vector<double> U1(r->N, 0.0), U3(r->N, 0.0), F1(r->N, 0.0), F2(r->N, 0.0), F3(r->N, 0.0);
+    velocity_update(U1.data(), U2, U3.data(), x1, x2, r->x3.data(), &r->gas, &r->box, r->cells, index, &cba,
+                    r->xi1.data(), r->xi2.data(), r->xi3.data(), r->Mp1.data(), r->Mp2.data(), r->Mp3.data(),
+                    F1.data(), F2.data(), F3.data(), r->rho.data(), r->T.data(), r->color.data());
+    r->gas.model = model;
+    return;
+  }
   if (r->gas.long_range == 1) vlasov_taking_the_integral(U2, &r->gas, &r->box, r->cells, index, x1, x2, r->x3.data());
   else if (r->gas.long_range == 3) poisson_solver(U2, x1, x2, r->x3.data(), &r->gas, &r->box, r->cells, index);
 }
@@ -291,6 +307,9 @@ void ref_get_cells(void* h, double* out) {
     o[MCPM_CF_F2] = k.F2;
     o[MCPM_CF_OMEGA_MAX] = (r->gas.model == "DSMC_VHS") ? k.crm : k.omega_max;
     o[MCPM_CF_DIVU] = k.divU;
+    o[MCPM_CF_N_SMOOTH] = k.n_smooth;
+    o[MCPM_CF_DN2] = k.dn2;
+    o[MCPM_CF_DN3] = k.dn3;
   }
 }
 

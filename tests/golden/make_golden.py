@@ -99,6 +99,17 @@ def case_fp_linear():
     return cfg, parts, dict(xi1=xi[0], xi2=xi[1], xi3=xi[2], step=2), out
 
 
+def case_density_expansion():
+    cfg, parts = W.vlasov_slab_1d(n_cells=60, mean_ppc=40, long_range=mcpm.LR_DENSITY_EXPANSION)
+    r = O.Reference(cfg, parts)
+    r.set_step(3)
+    r.cell_update()
+    out = dict(cells=r.cells())
+    r.long_range()
+    out.update(U2=r.s.U2.copy())
+    return cfg, parts, dict(step=3), out
+
+
 CASES = {
     "fp_step_1d": case_fp_step,
     "cells_2d": case_cells_2d,
@@ -106,6 +117,7 @@ CASES = {
     "vlasov_gf_1d": lambda: case_vlasov(mcpm.LR_SCREENED_POISSON),
     "specular_bc_1d": case_specular,
     "fp_linear_1d": case_fp_linear,
+    "density_expansion_1d": case_density_expansion,
 }
 
 

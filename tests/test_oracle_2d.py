@@ -51,7 +51,9 @@ def test_long_range_2d_matches_reference(lr):
     cfg, parts, o, r = _pair(lr)
     o.cell_update()
     r.cell_update()
-    assert np.array_equal(o.cells(), r.cells())
+    # all fields but the kernel-smoothing ones (computed for long_range 2 only)
+    sm = mcpm.CF["N_SMOOTH"]
+    assert np.array_equal(o.cells()[:, :sm], r.cells()[:, :sm])
     o.long_range()
     r.long_range()
     for k in ("U1", "U2"):

@@ -71,6 +71,18 @@ def test_golden_fp_linear(built):
         assert _same(getattr(o.s, k), z["out_" + k])
 
 
+def test_golden_density_expansion(built):
+    """long_range 2 on the 1-D slab: kernel smoothing and the density-expansion kick."""
+    cfg, parts, z = _load("density_expansion_1d")
+    assert cfg.long_range == mcpm.LR_DENSITY_EXPANSION
+    o = _oracle(cfg, parts, z)
+    o.cell_update()
+    for f in ("N_SMOOTH", "DN2", "DN3"):
+        assert _same(mcpm.cell_field(o.cells(), f, True), mcpm.cell_field(z["out_cells"], f, True)), f
+    o.long_range()
+    assert _same(o.s.U2, z["out_U2"])
+
+
 def test_golden_cells_2d(built):
     cfg, parts, z = _load("cells_2d")
     o = _oracle(cfg, parts, z)
@@ -78,7 +90,7 @@ def test_golden_cells_2d(built):
     assert _same(o.s.index, z["out_index"])
     co, cr = o.cells(), z["out_cells"]
     C = co.shape[0]
-    for f in [f for f in mcpm.CF if f not in ("F2", "OMEGA_MAX", "DIVU")]:
+    for f in [f for f in mcpm.CF if f not in ("F2", "OMEGA_MAX", "DIVU", "N_SMOOTH", "DN2", "DN3")]:
         a, b = mcpm.cell_field(co, f, True), mcpm.cell_field(cr, f, True)
         if f in ("ALPHA", "BETA", "PHI"):  # the reference reads past the cells for the last cell
             a, b = a[:C - 1], b[:C - 1]

@@ -40,7 +40,9 @@ def test_cell_update_bit_exact(built, step):
     assert _same(orc.s.index, ref.s.index)
     # every exported CELLS field (moments, Lambda, c, gamma, alpha, beta, phi)
     co, cr = orc.cells(), ref.cells()
-    fields = [f for f in mcpm.CF if f not in ("F2", "OMEGA_MAX", "DIVU")]
+    # the kernel-smoothing fields are computed for long_range 2 only (their
+    # one consumer); tests below compare them there
+    fields = [f for f in mcpm.CF if f not in ("F2", "OMEGA_MAX", "DIVU", "N_SMOOTH", "DN2", "DN3")]
     for f in fields:
         a, b = mcpm.cell_field(co, f, True), mcpm.cell_field(cr, f, True)
         assert _same(a, b), f
@@ -110,7 +112,7 @@ def test_two_dimensional_cell_update_bit_exact(built):
     # the reference reads one past the cell array for the last cell's div U
     # (src/Fokker_Planck.cpp:449); compare all but that cell's alpha/beta
     C = orc.C
-    for f in [f for f in mcpm.CF if f not in ("F2", "OMEGA_MAX", "DIVU")]:
+    for f in [f for f in mcpm.CF if f not in ("F2", "OMEGA_MAX", "DIVU", "N_SMOOTH", "DN2", "DN3")]:
         a, b = mcpm.cell_field(co, f, True), mcpm.cell_field(cr, f, True)
         if f in ("ALPHA", "BETA", "PHI"):
             a, b = a[:C - 1], b[:C - 1]
@@ -218,3 +220,25 @@ def test_dsmc_vhs_reference_statistics(built):
     assert mo > 0.05 and mr > 0.05
     assert abs(mo - mr) < 4 * np.hypot(so, sr) + 0.02 * mr
     assert abs(crms["orc"] - crms["ref"]) < 0.05 * crms["ref"]
+
+
+@pytest.mark.parametrize("shape", ["1d", "2d"])
+def test_density_expansion_bit_exact(built, shape):
+    """long_range 2: the kernel smoothing of cell_update
+    (src/Main_Functions.cpp:2378-2427) and velocity_update's density-expansion
+    kick (:1632-1653, run through the reference's own velocity_update)."""
+    _ref_or_skip()
+    if shape == "1d":
+        cfg, parts = W.vlasov_slab_1d(n_cells=60, mean_ppc=40, long_range=mcpm.LR_DENSITY_EXPANSION)
+    else:
+        cfg, parts = W.uneven_cells_2d(n_cells=(6, 5), hi=60)
+        cfg.long_range, cfg.phi = mcpm.LR_DENSITY_EXPANSION, -1.0
+    orc, ref = _pair(cfg, parts, seed=5, step=3)
+    for o in (orc, ref):
+        o.cell_update()
+    for f in ("N_SMOOTH", "DN2", "DN3"):
+        assert _same(mcpm.cell_field(orc.cells(), f, True), mcpm.cell_field(ref.cells(), f, True)), f
+    for o in (orc, ref):
+        o.long_range()
+    assert _same(orc.s.U2, ref.s.U2)
+    assert not np.array_equal(orc.s.U2, parts["U2"])
