@@ -249,6 +249,28 @@ int mcpm_step(mcpm_session* s, int32_t n_steps);
 int mcpm_inject_normals(mcpm_session* s, int64_t n, const double* xi1,
                         const double* xi2, const double* xi3);
 int mcpm_set_rng(mcpm_session* s, int32_t mode);
+/* Time-sampled raw velocity sums per cell, the CELLS members that
+   cell_poly_velocity accumulates (src/Main_Functions.cpp:1918-1968, called by
+   post_processing once the run passes its averaging start, src/myIO.cpp:968-971):
+   particle count, sum U_i, sum U_i U_j (11 12 13 22 23 33), sum
+   U1^m U2^n U3^(3-m-n) in the order m = 0..3, n = 0..3-m, and
+   sum U_i U_j |U|^2 (11 12 13 22 23 33). */
+enum mcpm_sample_field {
+  MCPM_SF_WEIGHT = 0,
+  MCPM_SF_M = 1,     /* 3  */
+  MCPM_SF_MM = 4,    /* 6  */
+  MCPM_SF_MMM = 10,  /* 10 */
+  MCPM_SF_MMMM = 20, /* 6  */
+  MCPM_SF_COUNT = 26
+};
+/* cell_poly_velocity: adds the current particles' sums to the session's
+   sample accumulators (FP64, zero at creation).  Needs the layout of a
+   preceding mcpm_cell_update, as the reference samples right after it. */
+int mcpm_sample_cells(mcpm_session* s);
+/* [MCPM_SF_COUNT][C] doubles, see enum mcpm_sample_field. */
+int mcpm_get_samples(mcpm_session* s, double* out);
+/* Sets the sample accumulators back to zero. */
+int mcpm_reset_samples(mcpm_session* s);
 /* [MCPM_CF_COUNT][C] doubles, see enum mcpm_cell_field. */
 int mcpm_get_cells(mcpm_session* s, double* out);
 /* Cell index of every particle, in particle-id order (cell_update's index[]). */

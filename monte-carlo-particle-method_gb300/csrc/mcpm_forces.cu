@@ -264,6 +264,65 @@ template <typename real> static int dsmc_impl(Session& s) {
 }
 int launch_dsmc_vhs(Session& s) { return s.prec == MCPM_FP32 ? dsmc_impl<float>(s) : dsmc_impl<double>(s); }
 
+// ============================================================== sampling
+// cell_poly_velocity, src/Main_Functions.cpp:1918-1968: per cell the particle
+// count and the raw sums of U, U U, U1^m U2^n U3^(3-m-n) (m = 0..3,
+// n = 0..3-m) and U U |U|^2, added to the session's accumulators.  One warp
+// per cell; the state is widened to double and summed per lane, the warp
+// reduces and lane 0 adds to the [MCPM_SF_COUNT][C] accumulators.
+template <typename real>
+__global__ void __launch_bounds__(128) k_sample(int C, double* smp, const int32_t* off, const int32_t* cnt,
+                                                const real* U1, const real* U2, const real* U3) {
+  constexpr int NS = MCPM_SF_COUNT - 1;
+  const int lane = threadIdx.x & 31;
+  const int num = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (num >= C) return;
+  const int n = cnt[num];
+  if (n == 0) return;  // warp-uniform: nothing to add
+  const int64_t o = off[num];
+  double a[NS];
+#pragma unroll
+  for (int j = 0; j < NS; ++j) a[j] = 0.0;
+  for (int i = lane; i < n; i += 32) {
+    const double u1 = (double)U1[o + i], u2 = (double)U2[o + i], u3 = (double)U3[o + i];
+    a[0] += u1; a[1] += u2; a[2] += u3;
+    a[3] += u1 * u1; a[4] += u1 * u2; a[5] += u1 * u3;
+    a[6] += u2 * u2; a[7] += u2 * u3; a[8] += u3 * u3;
+    const double p1[4] = {1.0, u1, u1 * u1, u1 * u1 * u1};
+    const double p2[4] = {1.0, u2, u2 * u2, u2 * u2 * u2};
+    const double p3[4] = {1.0, u3, u3 * u3, u3 * u3 * u3};
+    int id = 9;
+#pragma unroll
+    for (int m = 0; m < 4; ++m)
+#pragma unroll
+      for (int q = 0; q < 4 - m; ++q) a[id++] += p1[m] * p2[q] * p3[3 - m - q];
+    const double e = u1 * u1 + u2 * u2 + u3 * u3;
+    a[19] += u1 * u1 * e; a[20] += u1 * u2 * e; a[21] += u1 * u3 * e;
+    a[22] += u2 * u2 * e; a[23] += u2 * u3 * e; a[24] += u3 * u3 * e;
+  }
+#pragma unroll
+  for (int j = 0; j < NS; ++j)
+#pragma unroll
+    for (int m = 16; m >= 1; m >>= 1) a[j] += __shfl_xor_sync(FULL, a[j], m);
+  if (lane == 0) {
+    smp[(size_t)MCPM_SF_WEIGHT * C + num] += (double)n;
+#pragma unroll
+    for (int j = 0; j < NS; ++j) smp[(size_t)(1 + j) * C + num] += a[j];
+  }
+}
+
+int launch_sample(Session& s) {
+  const PBuf& b = s.P[s.cur];
+  const int blocks = (int)(((int64_t)s.C * 32 + 127) / 128);
+  if (s.prec == MCPM_FP32)
+    k_sample<float><<<blocks, 128, 0, s.stream>>>(s.C, s.samples, s.off, s.cnt, (const float*)b.U1,
+                                                  (const float*)b.U2, (const float*)b.U3);
+  else
+    k_sample<double><<<blocks, 128, 0, s.stream>>>(s.C, s.samples, s.off, s.cnt, (const double*)b.U1,
+                                                   (const double*)b.U2, (const double*)b.U3);
+  return 1;
+}
+
 // ESMC majorant initialisation, src/main.cpp:250-269
 __global__ void k_init_omega(DevConsts k, double* cell, double Ygas) {
   const int C = k.C;

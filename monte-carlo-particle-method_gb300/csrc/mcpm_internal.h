@@ -171,6 +171,7 @@ struct Session {
   bool sorted = false;          // layout is sorted by key, cnt/off/lists valid
   bool needs_rebin = false;     // positions moved since the last binning
   bool have_particles = false;
+  double* samples = nullptr;    // [MCPM_SF_COUNT][C] cell_poly_velocity accumulators
   bool omega_init = false;      // ESMC / DSMC majorant initialised (src/main.cpp:250-269)
   int num_sms = 0;
   Tuning tune{};
@@ -225,6 +226,7 @@ int launch_update(Session& s, uint32_t stages, int bc_call_base, bool slotted = 
 int launch_esmc(Session& s);
 int launch_dsmc_vhs(Session& s);
 int launch_smoothing(Session& s);
+int launch_sample(Session& s);
 int launch_long_range(Session& s);
 int launch_init_omega(Session& s);
 // 2-D long range (mcpm_lr2d.cu): set-up / release, the nodal deposit of

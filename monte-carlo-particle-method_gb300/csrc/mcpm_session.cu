@@ -302,6 +302,7 @@ int mcpm_session_destroy(mcpm_session* s) {
   if (!s) return MCPM_ERR_ARG;
   if (s->stream) cudaStreamSynchronize(s->stream);
   if (s->own_stream && s->own_stream != s->stream) cudaStreamSynchronize(s->own_stream);
+  cudaFree(s->samples);
   for (int b = 0; b < 2; ++b) {
     PBuf& P = s->P[b];
     cudaFree(P.x1); cudaFree(P.x2); cudaFree(P.U1); cudaFree(P.U2); cudaFree(P.U3); cudaFree(P.pid);
@@ -842,6 +843,36 @@ int mcpm_inject_normals(mcpm_session* s, int64_t n, const double* a, const doubl
 int mcpm_set_rng(mcpm_session* s, int32_t mode) {
   if (!s || (mode != MCPM_RNG_PHILOX && mode != MCPM_RNG_INJECTED)) return MCPM_ERR_ARG;
   s->rng_mode = mode;
+  return MCPM_OK;
+}
+
+int mcpm_sample_cells(mcpm_session* s) {
+  if (!s || !s->sorted) return fail(s, MCPM_ERR_STATE, "sample_cells: call cell_update first");
+  if (!s->samples) {
+    const size_t b = (size_t)MCPM_SF_COUNT * s->C * 8;
+    if (cudaMalloc(&s->samples, b) != cudaSuccess) {
+      s->samples = nullptr;
+      return fail(s, MCPM_ERR_CUDA, "sample_cells: no device memory for the accumulators");
+    }
+    cudaMemsetAsync(s->samples, 0, b, s->stream);
+  }
+  return after_launch(s, launch_sample(*s), "sample_cells");
+}
+
+int mcpm_get_samples(mcpm_session* s, double* out) {
+  if (!s || !out) return MCPM_ERR_ARG;
+  const size_t b = (size_t)MCPM_SF_COUNT * s->C * 8;
+  if (!s->samples) {
+    memset(out, 0, b);
+    return MCPM_OK;
+  }
+  cudaMemcpyAsync(out, s->samples, b, cudaMemcpyDeviceToHost, s->stream);
+  return cuda_check(s, cudaStreamSynchronize(s->stream), "get_samples");
+}
+
+int mcpm_reset_samples(mcpm_session* s) {
+  if (!s) return MCPM_ERR_ARG;
+  if (s->samples) cudaMemsetAsync(s->samples, 0, (size_t)MCPM_SF_COUNT * s->C * 8, s->stream);
   return MCPM_OK;
 }
 

@@ -34,6 +34,9 @@ CF = dict(NUM_INSIDE=0, U_SPACE=1, PIJ=4, M3=10, M4=20, M5=26, Q=29, DM2=32, DM4
           GAMMA_ST=39, LAMBDA=40, C=41, GAMMA=47, ALPHA=50, BETA=59, PHI=62, F2=65, OMEGA_MAX=66, DIVU=67,
           N_SMOOTH=68, DN2=69, DN3=70)
 CF_COUNT = 71
+# enum mcpm_sample_field: cell_poly_velocity's accumulators
+SF = dict(WEIGHT=0, M=1, MM=4, MMM=10, MMMM=20)
+SF_COUNT = 26
 K_NAMES = ["bin", "scan", "scatter", "moments", "solve", "esmc", "long_range", "update", "surrogate"]
 K_COUNT = len(K_NAMES)
 # (field, width) of every exported per-cell quantity
@@ -138,6 +141,9 @@ def load_library(path: str | None = None):
         "mcpm_inject_normals": (C.c_int, [vp, i64, dp, dp, dp]),
         "mcpm_set_rng": (C.c_int, [vp, i32]),
         "mcpm_get_cells": (C.c_int, [vp, dp]),
+        "mcpm_sample_cells": (C.c_int, [vp]),
+        "mcpm_get_samples": (C.c_int, [vp, dp]),
+        "mcpm_reset_samples": (C.c_int, [vp]),
         "mcpm_get_index": (C.c_int, [vp, ip]),
         "mcpm_get_normals": (C.c_int, [vp, dp, dp, dp]),
         "mcpm_get_node_density": (C.c_int, [vp, dp]),
@@ -317,6 +323,18 @@ class Session:
         out = np.empty((CF_COUNT, self.C))
         self._ck(self.lib.mcpm_get_cells(self.h, _dp(out)), "get_cells")
         return out
+
+    def sample_cells(self):
+        """cell_poly_velocity (src/Main_Functions.cpp:1918-1968) into the session's accumulators."""
+        self._ck(self.lib.mcpm_sample_cells(self.h), "sample_cells")
+
+    def get_samples(self):
+        out = np.empty((SF_COUNT, self.C))
+        self._ck(self.lib.mcpm_get_samples(self.h, _dp(out)), "get_samples")
+        return out
+
+    def reset_samples(self):
+        self._ck(self.lib.mcpm_reset_samples(self.h), "reset_samples")
 
     def get_index(self):
         out = np.empty(self.N, dtype=np.int32)

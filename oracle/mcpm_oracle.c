@@ -947,6 +947,42 @@ void orc_dsmc_vhs(orc_state* s, double* U1, double* U2, double* U3) {
   for (int I = 0; I < s->C; ++I) dsmc_cell(s, I, U1, U2, U3);
 }
 
+/* ---------------------------------------------------------- sampling -- */
+/* cell_poly_velocity, src/Main_Functions.cpp:1918-1968, in particle-id order:
+   adds every particle's raw velocity products to acc, [C][MCPM_SF_COUNT]
+   cell-major (the CELLS members sum_weight, sum_M, sum_MM, sum_MMM,
+   sum_MMMM). */
+void orc_sample_cells(orc_state* s, const double* U1, const double* U2, const double* U3, double* acc) {
+  for (int64_t i = 0; i < s->N; ++i) {
+    int num = s->index[i];
+    double* a = acc + (size_t)num * MCPM_SF_COUNT;
+    a[MCPM_SF_WEIGHT] += 1.0;
+    a[MCPM_SF_M + 0] += U1[i];
+    a[MCPM_SF_M + 1] += U2[i];
+    a[MCPM_SF_M + 2] += U3[i];
+    a[MCPM_SF_MM + 0] += U1[i] * U1[i];
+    a[MCPM_SF_MM + 1] += U1[i] * U2[i];
+    a[MCPM_SF_MM + 2] += U1[i] * U3[i];
+    a[MCPM_SF_MM + 3] += U2[i] * U2[i];
+    a[MCPM_SF_MM + 4] += U2[i] * U3[i];
+    a[MCPM_SF_MM + 5] += U3[i] * U3[i];
+    int id = 0;
+    for (int m = 0; m < 4; ++m)
+      for (int n = 0; n < 4 - m; ++n) {
+        int l = 3 - m - n;
+        a[MCPM_SF_MMM + id] += pow(U1[i], m) * pow(U2[i], n) * pow(U3[i], l);
+        id++;
+      }
+    double energy = U1[i] * U1[i] + U2[i] * U2[i] + U3[i] * U3[i];
+    a[MCPM_SF_MMMM + 0] += U1[i] * U1[i] * energy;
+    a[MCPM_SF_MMMM + 1] += U1[i] * U2[i] * energy;
+    a[MCPM_SF_MMMM + 2] += U1[i] * U3[i] * energy;
+    a[MCPM_SF_MMMM + 3] += U2[i] * U2[i] * energy;
+    a[MCPM_SF_MMMM + 4] += U2[i] * U3[i] * energy;
+    a[MCPM_SF_MMMM + 5] += U3[i] * U3[i] * energy;
+  }
+}
+
 /* ESMC majorant initialisation, src/main.cpp:250-269 */
 void orc_init_omega_max(orc_state* s) {
   const mcpm_config* g = &s->cfg;

@@ -64,6 +64,7 @@ void orc_stream(orc_state* s, double* x1, double* x2, const double* U1,
                 const double* U2, const double* U3);
 void orc_init_omega_max(orc_state* s);
 void orc_dsmc_vhs(orc_state* s, double* U1, double* U2, double* U3);
+void orc_sample_cells(orc_state* s, const double* U1, const double* U2, const double* U3, double* acc);
 void orc_set_layout(orc_state* s, const int32_t* off, const int32_t* list);
 /* one iteration of the main loop body; x_old arrays persist across steps */
 void orc_step(orc_state* s, double* x1, double* x2, double* x1_old,

@@ -57,6 +57,7 @@ def _load_oracle():
         "orc_velocity_fp": (None, [vp, dp, dp, dp, dp, dp, dp]),
         "orc_esmc": (None, [vp, dp, dp, dp, dp, dp]),
         "orc_dsmc_vhs": (None, [vp, dp, dp, dp]),
+        "orc_sample_cells": (None, [vp, dp, dp, dp, dp]),
         "orc_long_range": (None, [vp, dp]),
         "orc_dfp_extra_streaming": (None, [vp, dp, dp, dp, dp, dp]),
         "orc_apply_bc": (None, [vp, C.c_int, dp, dp, dp, dp, dp, dp, dp]),
@@ -178,6 +179,11 @@ class Oracle:
         s = self.s
         self.L.orc_esmc(self.h, _dp(s.x1), _dp(s.x2), _dp(s.U1), _dp(s.U2), _dp(s.U3))
 
+    def sample_cells(self, acc):
+        """cell_poly_velocity into acc, [C][SF_COUNT] (added to)"""
+        s = self.s
+        self.L.orc_sample_cells(self.h, _dp(s.U1), _dp(s.U2), _dp(s.U3), _dp(acc))
+
     def dsmc(self):
         """Collision_DSMC_VHS (src/collisions.cpp:2063-2141)"""
         s = self.s
@@ -282,6 +288,7 @@ def ref_lib(build=True):
         "ref_stream": (None, [vp, dp, dp, dp, dp, dp, dp, dp, ip]),
         "ref_esmc": (None, [vp, dp, dp, dp, dp, dp, ip]),
         "ref_dsmc_vhs": (None, [vp, dp, dp, dp, dp, dp]),
+        "ref_sample_cells": (None, [vp, dp, dp, dp, ip, dp]),
         "ref_init_omega_max": (None, [vp]),
         "ref_get_cells": (None, [vp, dp]),
         "ref_long_range_2d": (None, [vp, dp, dp, dp, dp, ip]),
@@ -371,6 +378,11 @@ class Reference:
     def esmc(self):
         s = self.s
         self.L.ref_esmc(self.h, _dp(s.U1), _dp(s.U2), _dp(s.U3), _dp(s.x1), _dp(s.x2), _ip(s.index))
+
+    def sample_cells(self, acc):
+        """the reference's cell_poly_velocity; acc receives its running sums"""
+        s = self.s
+        self.L.ref_sample_cells(self.h, _dp(s.U1), _dp(s.U2), _dp(s.U3), _ip(s.index), _dp(acc))
 
     def dsmc(self):
         s = self.s

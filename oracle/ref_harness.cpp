@@ -267,6 +267,23 @@ void ref_dsmc_vhs(void* h, double* U1, double* U2, double* U3, double* x1, doubl
   Collision_DSMC_VHS(U1, U2, U3, x1, x2, &r->gas, &r->box, r->cells, &DSMC);
 }
 
+// cell_poly_velocity (src/Main_Functions.cpp:1918), then its running sums
+// into out, [C][MCPM_SF_COUNT]
+void ref_sample_cells(void* h, double* U1, double* U2, double* U3, int* index, double* out) {
+  Quiet q;
+  Ref* r = (Ref*)h;
+  cell_poly_velocity(U1, U2, U3, r->cells, &r->box, r->box.step, &r->gas, index);
+  for (int c = 0; c < r->C; ++c) {
+    const CELLS& k = r->cells[c];
+    double* o = out + (size_t)c * MCPM_SF_COUNT;
+    o[MCPM_SF_WEIGHT] = k.sum_weight;
+    for (int i = 0; i < 3; ++i) o[MCPM_SF_M + i] = k.sum_M[i];
+    for (int i = 0; i < 6; ++i) o[MCPM_SF_MM + i] = k.sum_MM[i];
+    for (int i = 0; i < 10; ++i) o[MCPM_SF_MMM + i] = k.sum_MMM[i];
+    for (int i = 0; i < 6; ++i) o[MCPM_SF_MMMM + i] = k.sum_MMMM[i];
+  }
+}
+
 void ref_init_omega_max(void* h) {
   // src/main.cpp:250-269
   Ref* r = (Ref*)h;

@@ -242,3 +242,23 @@ def test_density_expansion_bit_exact(built, shape):
         o.long_range()
     assert _same(orc.s.U2, ref.s.U2)
     assert not np.array_equal(orc.s.U2, parts["U2"])
+
+
+def test_sample_cells_bit_exact(built):
+    """cell_poly_velocity (src/Main_Functions.cpp:1918-1968): the running
+    per-cell sums after three samples with FP updates between them."""
+    _ref_or_skip()
+    cfg, parts = W.uneven_cells_2d(n_cells=(6, 5), hi=60)
+    orc, ref = _pair(cfg, parts, seed=6, step=2)
+    acc_o = np.zeros((orc.C, mcpm.SF_COUNT))
+    acc_r = np.zeros((orc.C, mcpm.SF_COUNT))
+    for it in range(3):
+        for o in (orc, ref):
+            o.cell_update()
+        orc.sample_cells(acc_o)
+        ref.sample_cells(acc_r)
+        assert _same(acc_o, acc_r), it
+        for o in (orc, ref):
+            o.random_generator()
+            o.velocity_fp()
+    assert acc_o[:, mcpm.SF["WEIGHT"]].sum() == 3 * orc.N
