@@ -193,6 +193,19 @@ typedef struct mcpm_session mcpm_session;
    mu = 5/(16 sigma^2) sqrt(m kb T0/pi), Fn = n*Volume/N, eqdist = sigma. */
 int mcpm_config_derive(mcpm_config* cfg, int64_t n_particles);
 
+/* readSettingsFile (src/myIO.cpp:1756-3016) for the problems the particle
+   step covers, closed_box (1) and couette_flow (2): reads the reference's
+   settings file ("keyword values..." per line, '#' comment lines) and
+   derives the configuration as the reference does (cell sizes, Fn, sigma and
+   crref from mu for hard or variable hard spheres, b, mu(T0), dt from the
+   mean free path and frac_mft, phi from epsilon; SI constants where the
+   reference fixes them).  *n_particles receives gas.N.  Keywords the
+   reference does not know, other problems and models outside the step
+   return MCPM_ERR_ARG; msg (optional, msg_len bytes) receives the reason.
+   The result is an FP64 configuration; change precision before creating
+   the session for an FP32 one. */
+int mcpm_config_from_settings(const char* path, mcpm_config* out, int64_t* n_particles, char* msg,
+                              int32_t msg_len);
 int mcpm_session_create(const mcpm_config* cfg, mcpm_session** out);
 int mcpm_session_destroy(mcpm_session* s);
 const char* mcpm_last_error(const mcpm_session* s);

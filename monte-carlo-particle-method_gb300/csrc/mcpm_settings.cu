@@ -1,0 +1,231 @@
+// mcpm_settings.cu -- the reference's settings file as an mcpm_config.
+//
+// readSettingsFile (src/myIO.cpp:1756-3016) reads one "keyword values..."
+// line at a time ('#' lines are comments) into GAS/BOX and then derives the
+// run's constants: cell sizes, Fn, the hard-sphere or VHS diameter and
+// reference speed from the viscosity, b, mu(T0), the mean free path, dt and
+// the attraction strength.  This restates that reading and the derivation
+// along the path the particle step covers (problems closed_box 1 and
+// couette_flow 2; the step's models), in the reference's order of
+// operations, so that a run configured by the reference's own files gets
+// the constants the reference would use.  Host code only.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <sstream>
+#include <string>
+
+#include "../../include/mcpm.h"
+
+namespace {
+
+// the keywords readSettingsFile accepts (src/myIO.cpp:1880-2122); lines with
+// any other keyword abort the reference's run
+const char* const kKeywords[] = {
+    "N", "gp_nn", "N13", "sigc", "alphac", "sigh", "alphah", "n", "nc", "nh", "nvc", "nvh", "nv1", "nv2", "nv3",
+    "Tc", "Th", "Tv1", "Tv2", "Tv3", "LcN", "LhN", "LvN", "LvN1", "LvN3", "Lv1", "Lv3", "Nh", "Nv1", "Nv2", "Nv3",
+    "long_range", "box_len", "cone_len", "x2_prob", "ghost", "thermc", "thermh", "cone_num_cells", "cone_angles",
+    "flatnose", "flatratio", "box_delta_dim", "direction", "U0", "sigma", "weight", "dcones_n", "mass", "steps",
+    "dt", "init_step", "model", "output", "movie", "every", "num_realizations", "after", "reset_every",
+    "frac_mft", "T", "epsilon", "kb", "num_thr", "mu", "visp", "nualpha", "phi", "phi0", "factor", "n_ratio",
+    "problem", "U_wall_1", "U_wall_2", "U_wall_3", "U_wall_4", "U_wall_5", "U_wall_6", "U_wall_7", "T_wall_1",
+    "T_wall_2", "T_wall_3", "T_wall_4", "T_wall_5", "T_wall_6", "T_wall_7", "n_wall_4", "n_wall_5", "n_wall_6",
+    "n_wall_7", "reset", "drop_dia", "num_cells"};
+
+bool known(const std::string& k) {
+  for (const char* w : kKeywords)
+    if (k == w) return true;
+  return false;
+}
+
+// the values the derivation reads, with readSettingsFile's "unset" markers
+struct Raw {
+  long N = -1;
+  int cells[3] = {-1, -1, -1};
+  int direction[3] = {0, 0, 0};
+  double Len[3] = {-1.0, -1.0, -1.0};
+  double delta_dim[3] = {-1.0, -1.0, -1.0};
+  double kb = -1.0, sigma = -1.0, T = -1.0, n = -1.0, m = -1.0, dt = -1.0, mu = -1.0, frac_mft = -1.0;
+  double epsilon = -1.0, phi = -1.0;
+  bool has_visp = false, has_nualpha = false;
+  double visp = 0.0, nualpha = 0.0;
+  int problem = -1, long_range = 0;
+  std::string model;
+  double U_wall[4] = {-1.0, -1.0, -1.0, -1.0};
+  double T_wall[4] = {-1.0, -1.0, -1.0, -1.0};
+};
+
+int set_msg(char* msg, int32_t len, const char* text, int code) {
+  if (msg && len > 0) {
+    std::strncpy(msg, text, (size_t)len - 1);
+    msg[len - 1] = '\0';
+  }
+  return code;
+}
+
+int model_code(const std::string& m) {
+  if (m == "none") return MCPM_MODEL_NONE;
+  if (m == "FP_dense") return MCPM_MODEL_FP_DENSE;
+  if (m == "FP_ideal_gas") return MCPM_MODEL_FP_IDEAL_GAS;
+  if (m == "ESMC") return MCPM_MODEL_ESMC;
+  if (m == "FP_linear") return MCPM_MODEL_FP_LINEAR;
+  if (m == "DSMC_VHS") return MCPM_MODEL_DSMC_VHS;
+  return -1;
+}
+
+}  // namespace
+
+extern "C" int mcpm_config_from_settings(const char* path, mcpm_config* out, int64_t* n_particles, char* msg,
+                                         int32_t msg_len) {
+  if (!path || !out) return set_msg(msg, msg_len, "settings: null argument", MCPM_ERR_ARG);
+  FILE* f = std::fopen(path, "r");
+  if (!f) return set_msg(msg, msg_len, "settings: cannot open the file", MCPM_ERR_ARG);
+  Raw r;
+  char buf[4096];
+  int rc = MCPM_OK;
+  char err[512] = {0};
+  while (std::fgets(buf, sizeof(buf), f)) {
+    if (buf[0] == '#') continue;
+    std::istringstream iss(buf);
+    std::string key;
+    // a blank line: the reference re-enters the previous keyword's branch
+    // with nothing left to read, which changes nothing
+    if (!(iss >> key)) continue;
+    if (!known(key)) {
+      std::snprintf(err, sizeof(err), "settings: unknown keyword '%s' (src/myIO.cpp:2116-2121)", key.c_str());
+      rc = MCPM_ERR_ARG;
+      break;
+    }
+    if (key == "N") iss >> r.N;
+    else if (key == "n") iss >> r.n;
+    else if (key == "long_range") iss >> r.long_range;
+    else if (key == "box_len") iss >> r.Len[0] >> r.Len[1] >> r.Len[2];
+    else if (key == "box_delta_dim") iss >> r.delta_dim[0] >> r.delta_dim[1] >> r.delta_dim[2];
+    else if (key == "direction") iss >> r.direction[0] >> r.direction[1] >> r.direction[2];
+    else if (key == "sigma") iss >> r.sigma;
+    else if (key == "mass") iss >> r.m;
+    else if (key == "dt") iss >> r.dt;
+    else if (key == "model") iss >> r.model;
+    else if (key == "frac_mft") iss >> r.frac_mft;
+    else if (key == "T") iss >> r.T;
+    else if (key == "epsilon") iss >> r.epsilon;
+    else if (key == "kb") iss >> r.kb;
+    else if (key == "mu") iss >> r.mu;
+    else if (key == "visp") r.has_visp = static_cast<bool>(iss >> r.visp);
+    else if (key == "nualpha") r.has_nualpha = static_cast<bool>(iss >> r.nualpha);
+    else if (key == "phi") iss >> r.phi;
+    else if (key == "problem") iss >> r.problem;
+    else if (key == "num_cells") iss >> r.cells[0] >> r.cells[1] >> r.cells[2];
+    else if (key.rfind("U_wall_", 0) == 0 || key.rfind("T_wall_", 0) == 0) {
+      const int w = key[7] - '1';
+      if (w >= 0 && w < 4) iss >> (key[0] == 'U' ? r.U_wall[w] : r.T_wall[w]);
+    }
+    // every other keyword belongs to problems, outputs or run control the
+    // particle step does not read
+  }
+  std::fclose(f);
+  if (rc) return set_msg(msg, msg_len, err, rc);
+
+  // ---- the derivation, src/myIO.cpp:2122-2900, problems 1 and 2
+  const double pi = std::acos(-1.0);
+  if (r.Len[0] < 0.0) return set_msg(msg, msg_len, "settings: box_len is required", MCPM_ERR_ARG);
+  if (r.cells[0] < 1 || r.cells[1] < 1 || r.cells[2] != 1)
+    return set_msg(msg, msg_len, "settings: num_cells must be N0 N1 1", MCPM_ERR_ARG);
+  if (r.N < 1) return set_msg(msg, msg_len, "settings: N (particles) is required", MCPM_ERR_ARG);
+  if (r.delta_dim[0] < 0.0)
+    for (int i = 0; i < 3; ++i) r.delta_dim[i] = r.Len[i] / r.cells[i];
+  if (r.kb < 0.0) r.kb = 1.38064852 * 1e-23;
+  if (r.T < 0.0) r.T = 1.0 / r.kb;
+  if (r.sigma < 0.0) r.sigma = 1;
+  if (r.n < 0.0) r.n = 1e-3;
+  if (r.m < 0.0) r.m = 1.0;
+  if (r.problem < 0) r.problem = 1;
+  for (int i = 0; i < 4; ++i)
+    if (r.T_wall[i] < 0) r.T_wall[i] = 1.0;
+  if (r.problem != 1 && r.problem != 2)
+    return set_msg(msg, msg_len,
+                   "settings: only problems closed_box (1) and couette_flow (2) configure the particle step",
+                   MCPM_ERR_ARG);
+  const int model = model_code(r.model);
+  if (model < 0) return set_msg(msg, msg_len, "settings: the model is outside the particle step", MCPM_ERR_ARG);
+  if (!r.has_visp) return set_msg(msg, msg_len, "settings: visp is required", MCPM_ERR_ARG);
+  const double volume = r.Len[0] * r.Len[1] * r.Len[2];
+  const double Fn = r.n * volume / r.N;
+  const double thermal = std::sqrt(r.kb * r.T / r.m);
+  const double T0 = 273.0;
+  if (r.epsilon < 0.0) r.epsilon = 119.8 * r.kb;
+  double crref;
+  if (std::fabs(r.sigma - 1.0) < 1e-14) {
+    crref = thermal;
+  } else if (std::fabs(r.visp - 0.5) < 1e-13) {
+    // hard spheres: the diameter that gives the viscosity mu at T0
+    if (!(r.mu > 0.0)) return set_msg(msg, msg_len, "settings: mu is required to derive sigma", MCPM_ERR_ARG);
+    r.sigma = 1.016 * 5.0 * std::sqrt(r.m * r.kb * T0 / pi);
+    r.sigma = r.sigma / (16.0 * r.mu);
+    r.sigma = std::sqrt(r.sigma);
+    crref = thermal;
+  } else {
+    // variable hard spheres (Bird): diameter and reference speed from mu
+    if (!(r.mu > 0.0) || !r.has_nualpha)
+      return set_msg(msg, msg_len, "settings: mu and nualpha are required to derive the VHS sigma", MCPM_ERR_ARG);
+    const double nu = r.nualpha, w = r.visp;
+    r.sigma = 1.016 * 5.0 * (nu + 1.0) * (nu + 2.0) * std::sqrt(r.m * r.kb * T0 / pi);
+    r.sigma = r.sigma / ((4.0 * nu) * (5.0 - 2.0 * w) * (7.0 - 2.0 * w) * r.mu);
+    r.sigma = std::sqrt(r.sigma);
+    const double numer = r.m * std::pow(4.0, w - 1) * 5.0 * (nu + 1.0) * (nu + 2.0) * std::sqrt(pi);
+    const double denom = pi * std::pow(r.sigma, 2.0) * nu * (5.0 - 2.0 * w) * (7.0 - 2.0 * w) * 2.0 *
+                         std::tgamma(5.0 / 2.0 - w);
+    crref = (numer / denom) * std::pow(r.kb * 273.0 / r.m, w) / r.mu;
+    crref = std::pow(crref, 1.0 / (w * 2.0 - 1.0));
+  }
+  const double eqdist = std::pow(2.0, 1.0 / 6.0) * r.sigma;  // :2820-2822
+  const double b = 2 * pi * std::pow(r.sigma, 3) / (3.0);
+  const double mu = 5.0 / (16.0 * r.sigma * r.sigma) * std::sqrt(r.m * r.kb * T0 / std::acos(-1.0));
+  if (r.dt < 0.0) {
+    const double wall_speed = std::fmax(std::sqrt(r.kb * r.T_wall[0] / r.m), std::fmax(r.U_wall[0], r.U_wall[1]));
+    const double dy = r.Len[1] / r.cells[1];
+    if (model == MCPM_MODEL_DSMC_VHS || model == MCPM_MODEL_ESMC || model == MCPM_MODEL_FP_DENSE) {
+      // the mean free path of the VHS/VSS gas, :2836-2839
+      if (!r.has_nualpha)
+        return set_msg(msg, msg_len, "settings: nualpha is required to derive dt", MCPM_ERR_ARG);
+      double lambda = 4.0 * r.nualpha * (5.0 - 2.0 * r.visp) * (7.0 - 2.0 * r.visp);
+      lambda = lambda / (5.0 * (r.nualpha + 1.0) * (r.nualpha + 2.0));
+      lambda = lambda * std::sqrt(r.m / (2.0 * pi * r.kb * r.T)) * mu / (r.m * r.n);
+      const double frac = r.frac_mft < 0.0 ? 0.5 : r.frac_mft;
+      r.dt = frac * std::fmin(lambda, dy) / wall_speed;
+    } else {
+      const double frac = r.frac_mft < 0.0 ? 0.5 : r.frac_mft;
+      r.dt = frac * r.Len[1] / r.cells[1] / wall_speed;
+    }
+  }
+  const double phi = r.phi < 0.0 ? -4.0 * r.epsilon : -r.phi * r.epsilon;  // :2900-2905
+
+  mcpm_config c;
+  std::memset(&c, 0, sizeof(c));
+  for (int i = 0; i < 3; ++i) {
+    c.n_cells[i] = r.cells[i];
+    c.direction[i] = r.direction[i];
+    c.length[i] = r.Len[i];
+  }
+  c.problem = r.problem == 1 ? MCPM_PROBLEM_CLOSED_BOX : MCPM_PROBLEM_COUETTE;
+  c.model = model;
+  // "0 or anything > 3 = no attraction" (src/Main_Functions.cpp:1612-1617)
+  c.long_range = (r.long_range >= 1 && r.long_range <= 3) ? r.long_range : MCPM_LR_NONE;
+  c.precision = MCPM_FP64;
+  c.sigma = r.sigma; c.m = r.m; c.kb = r.kb; c.n = r.n; c.Fn = Fn;
+  c.T0 = T0; c.mu = mu; c.visp = r.visp; c.b = b; c.dt = r.dt;
+  c.phi = phi; c.eqdist = eqdist;
+  // the screened-Poisson constants readSettingsFile sets (SI, :2884-2885)
+  c.ast = -1.64835851e-28;
+  c.bst = 6.91304716e+09;
+  for (int i = 0; i < 4; ++i) {
+    c.T_wall[i] = r.T_wall[i];
+    c.U_wall[i] = r.U_wall[i];
+  }
+  c.seed = 0x4D43504Dull;
+  c.max_particles = r.N;
+  c.crref = crref;
+  *out = c;
+  if (n_particles) *n_particles = r.N;
+  return set_msg(msg, msg_len, "", MCPM_OK);
+}

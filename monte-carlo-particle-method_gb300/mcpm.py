@@ -70,6 +70,18 @@ class Config(C.Structure):
         return out
 
 
+def config_from_settings(path: str):
+    """readSettingsFile (src/myIO.cpp:1756-3016) through the library: the
+    reference's settings file as (Config, N) for problems 1 and 2."""
+    L = load_library()
+    cfg, n = Config(), C.c_int64(0)
+    msg = C.create_string_buffer(512)
+    rc = L.mcpm_config_from_settings(os.fsencode(path), C.byref(cfg), C.byref(n), msg, 512)
+    if rc:
+        raise MCPMError(rc, msg.value.decode())
+    return cfg, n.value
+
+
 def derive(cfg: Config, n_particles: int) -> Config:
     """Derived GAS fields as readSettingsFile fills them (src/myIO.cpp:2217-2233,
     :2828-2830); identical to mcpm_config_derive in the library."""
@@ -122,6 +134,7 @@ def load_library(path: str | None = None):
     vp, i64, i32, dp, ip = C.c_void_p, C.c_int64, C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_int32)
     sig = {
         "mcpm_config_derive": (C.c_int, [C.POINTER(Config), i64]),
+        "mcpm_config_from_settings": (C.c_int, [C.c_char_p, C.POINTER(Config), C.POINTER(i64), C.c_char_p, i32]),
         "mcpm_session_create": (C.c_int, [C.POINTER(Config), C.POINTER(vp)]),
         "mcpm_session_destroy": (C.c_int, [vp]),
         "mcpm_last_error": (C.c_char_p, [vp]),

@@ -275,6 +275,7 @@ def ref_lib(build=True):
     vp = C.c_void_p
     sig = {
         "ref_create": (vp, [C.POINTER(Config), C.c_long]),
+        "ref_read_settings": (None, [C.c_char_p, C.POINTER(C.c_long), C.POINTER(C.c_double)]),
         "ref_destroy": (None, [vp]),
         "ref_set_step": (None, [vp, C.c_int]),
         "ref_inject_normals": (None, [dp, dp, dp, C.c_long]),
@@ -390,3 +391,16 @@ class Reference:
 
     def init_omega_max(self):
         self.L.ref_init_omega_max(self.h)
+
+
+def ref_read_settings(path):
+    """The reference's readSettingsFile on path: (ints, doubles) in the order
+    of ref_read_settings in ref_harness.cpp; None without the reference."""
+    L = ref_lib()
+    if L is None:
+        return None
+    iv = np.zeros(10, dtype=np.int64)
+    dv = np.zeros(28)
+    L.ref_read_settings(os.fsencode(path), iv.ctypes.data_as(C.POINTER(C.c_long)),
+                        dv.ctypes.data_as(C.POINTER(C.c_double)))
+    return iv, dv[:26]

@@ -284,6 +284,33 @@ void ref_sample_cells(void* h, double* U1, double* U2, double* U3, int* index, d
   }
 }
 
+// readSettingsFile (src/myIO.cpp:1756-3016) on the file at path: the derived
+// GAS/BOX values a configuration takes, ints [N0 N1 N2 dir0 dir1 dir2
+// problem long_range model N] and doubles [Len0..2 sigma m kb n Fn T0 mu visp
+// b delta_t phi eqdist ast bst T_wall1..4 U_wall1..4 crref]
+void ref_read_settings(const char* path, long* iv, double* dv) {
+  Quiet q;
+  GAS g{};
+  BOX b{};
+  b.file_name = path;
+  readSettingsFile(&g, &b);
+  int model = -1;
+  if (g.model == "none") model = 0;
+  else if (g.model == "FP_dense") model = MCPM_MODEL_FP_DENSE;
+  else if (g.model == "FP_ideal_gas") model = MCPM_MODEL_FP_IDEAL_GAS;
+  else if (g.model == "ESMC") model = MCPM_MODEL_ESMC;
+  else if (g.model == "FP_linear") model = MCPM_MODEL_FP_LINEAR;
+  else if (g.model == "DSMC_VHS") model = MCPM_MODEL_DSMC_VHS;
+  const long ivals[10] = {b.N[0], b.N[1], b.N[2], b.direction[0], b.direction[1], b.direction[2],
+                          b.problem, g.long_range, model, (long)g.N};
+  for (int i = 0; i < 10; ++i) iv[i] = ivals[i];
+  const double dvals[28] = {b.Len[0], b.Len[1], b.Len[2], g.sigma, g.m, g.kb, g.n, g.Fn, g.T0, g.mu,
+                            g.visp, g.b, g.delta_t, g.phi, g.eqdist, g.ast, g.bst,
+                            b.T_wall_1, b.T_wall_2, b.T_wall_3, b.T_wall_4,
+                            b.U_wall_1, b.U_wall_2, b.U_wall_3, b.U_wall_4, g.crref, 0.0, 0.0};
+  for (int i = 0; i < 26; ++i) dv[i] = dvals[i];
+}
+
 void ref_init_omega_max(void* h) {
   // src/main.cpp:250-269
   Ref* r = (Ref*)h;

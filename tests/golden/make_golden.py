@@ -7,6 +7,7 @@ checks the CPU restatement against these files bit for bit, which pins the
 oracle where the reference tree is not available.
 
     python tests/golden/make_golden.py [case ...]     (all cases by default)
+    python tests/golden/make_golden.py settings       (settings_expected.json)
 """
 import json
 import os
@@ -121,9 +122,26 @@ CASES = {
 }
 
 
+def settings_expected():
+    """readSettingsFile of the reference on every settings/*.in fixture, the
+    derived values as exact hex floats (settings_expected.json)"""
+    out = {}
+    d = os.path.join(HERE, "settings")
+    for f in sorted(os.listdir(d)):
+        if f.endswith(".in"):
+            iv, dv = O.ref_read_settings(os.path.join(d, f))
+            out[f] = dict(ints=[int(v) for v in iv], doubles=[float(v).hex() for v in dv])
+    with open(os.path.join(HERE, "settings_expected.json"), "w") as fh:
+        json.dump(out, fh, indent=1, sort_keys=True)
+    print("settings_expected.json", sorted(out))
+
+
 def main():
     if O.ref_lib() is None:
         raise SystemExit("the reference build (oracle/_ref) is not available")
+    if sys.argv[1:] == ["settings"]:
+        settings_expected()
+        return
     for name in sys.argv[1:] or list(CASES):
         cfg, parts, extra, out = CASES[name]()
         arrays = {"in_" + k: np.asarray(v) for k, v in parts.items() if k in ("x1", "x2", "U1", "U2", "U3")}

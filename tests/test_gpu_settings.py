@@ -1,0 +1,39 @@
+"""A run configured by a settings file in the reference's format
+(mcpm_config_from_settings): seeded particles in the configured box, fused
+FP64 steps on the GPU against the oracle under the same configuration, both
+drawing the same Philox streams (1e-10)."""
+import os
+
+import numpy as np
+import pytest
+
+import mcpm
+from oracle import Oracle
+
+pytestmark = pytest.mark.gpu
+
+SETTINGS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "settings")
+
+
+def test_settings_drive_the_step(cuda_ok):
+    cfg, N = mcpm.config_from_settings(os.path.join(SETTINGS, "reduced_fp_ideal.in"))
+    rng = np.random.default_rng(41)
+    L = cfg.length
+    parts = dict(x1=rng.uniform(0.0, L[0], N), x2=rng.uniform(0.0, L[1], N))
+    s = np.sqrt(cfg.kb * 1.0 / cfg.m)  # the file's T = 1
+    for k in ("U1", "U2", "U3"):
+        parts[k] = rng.normal(0.0, s, N)
+    ses = mcpm.Session(cfg)
+    ses.upload(parts["x1"], parts["x2"], parts["U1"], parts["U2"], parts["U3"])
+    o = Oracle(cfg, parts)
+    ses.set_rng(mcpm.RNG_PHILOX)
+    o.set_rng(mcpm.RNG_PHILOX)
+    ses.set_step(1)
+    o.set_step(1)
+    ses.step(3)
+    o.step(3)
+    g = ses.download()
+    for k in ("x2", "U1", "U2", "U3"):
+        a, b = g[k], getattr(o.s, k)
+        assert np.max(np.abs(a - b)) / max(1.0, np.max(np.abs(b))) <= 1e-10, k
+    assert not np.array_equal(g["U1"], parts["U1"])

@@ -1,0 +1,99 @@
+"""The settings-file front end (mcpm_config_from_settings, a restatement of
+readSettingsFile, src/myIO.cpp:1756-3016, for problems 1 and 2) on the
+fixtures in tests/golden/settings: bit-exact against the reference's own
+reader where the reference tree is present, and against the values it
+produced (tests/golden/settings_expected.json, written by
+tests/golden/make_golden.py) everywhere.  No GPU needed: the reader is host
+code in libmcpm.so."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import mcpm
+import oracle as O
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+SETTINGS = os.path.join(HERE, "golden", "settings")
+FIXTURES = sorted(f for f in os.listdir(SETTINGS) if f.endswith(".in"))
+
+
+def _values(cfg, N):
+    ints = [cfg.n_cells[0], cfg.n_cells[1], cfg.n_cells[2], cfg.direction[0], cfg.direction[1],
+            cfg.direction[2], cfg.problem, cfg.long_range, cfg.model, N]
+    dbl = [cfg.length[0], cfg.length[1], cfg.length[2], cfg.sigma, cfg.m, cfg.kb, cfg.n, cfg.Fn, cfg.T0, cfg.mu,
+           cfg.visp, cfg.b, cfg.dt, cfg.phi, cfg.eqdist, cfg.ast, cfg.bst]
+    dbl += list(cfg.T_wall) + list(cfg.U_wall) + [cfg.crref]
+    return ints, dbl
+
+
+@pytest.mark.parametrize("name", FIXTURES)
+def test_settings_match_golden(built, name):
+    with open(os.path.join(HERE, "golden", "settings_expected.json")) as fh:
+        exp = json.load(fh)[name]
+    cfg, N = mcpm.config_from_settings(os.path.join(SETTINGS, name))
+    ints, dbl = _values(cfg, N)
+    assert ints == exp["ints"]
+    want = [float.fromhex(h) for h in exp["doubles"]]
+    assert dbl == want, [(i, a, b) for i, (a, b) in enumerate(zip(dbl, want)) if a != b]
+    assert cfg.precision == mcpm.FP64 and cfg.max_particles == N
+
+
+@pytest.mark.parametrize("name", FIXTURES)
+def test_settings_match_reference(built, name):
+    if O.ref_lib() is None:
+        pytest.skip("reference sources not available")
+    path = os.path.join(SETTINGS, name)
+    iv, dv = O.ref_read_settings(path)
+    cfg, N = mcpm.config_from_settings(path)
+    ints, dbl = _values(cfg, N)
+    assert ints == [int(v) for v in iv]
+    assert np.array_equal(np.array(dbl), dv)
+
+
+def test_settings_branches(built):
+    """the three diameter branches: sigma kept (reduced units), hard spheres
+    and variable hard spheres from mu; dt from the cell size or the mean free path"""
+    red, _ = mcpm.config_from_settings(os.path.join(SETTINGS, "reduced_fp_ideal.in"))
+    assert red.sigma == 1.0 and red.crref == 1.0 and red.dt == pytest.approx(0.05)
+    hs, _ = mcpm.config_from_settings(os.path.join(SETTINGS, "closed_box_fp_dense.in"))
+    assert hs.sigma != 3.405e-10 and 2e-10 < hs.sigma < 5e-10
+    vhs, _ = mcpm.config_from_settings(os.path.join(SETTINGS, "dsmc_vhs.in"))
+    assert vhs.model == mcpm.MODEL_DSMC_VHS and vhs.crref > 0 and vhs.visp == 0.81
+    es, _ = mcpm.config_from_settings(os.path.join(SETTINGS, "couette_esmc.in"))
+    assert es.problem == mcpm.PROBLEM_COUETTE and es.U_wall[1] == 50.0 and es.phi < 0
+
+
+def _write(dirpath, text):
+    p = os.path.join(dirpath, "case.in")
+    with open(p, "w") as fh:
+        fh.write(text)
+    return p
+
+
+BASE = "model FP_dense\nN 100\nvisp 0.5\nnualpha 1.0\nbox_len 1 10 1\nnum_cells 1 10 1\nsigma 1\nkb 1\nmass 1\nT 1\n"
+
+
+@pytest.mark.parametrize("extra,needle", [
+    ("bogus_key 3\n", "unknown keyword"),
+    ("problem 3\n", "problems"),
+    ("model MD\n", "model"),
+])
+def test_settings_errors(built, extra, needle):
+    """what the reference aborts on, or what lies outside the particle step,
+    returns MCPM_ERR_ARG with a reason"""
+    d = os.path.join(HERE, "_tmp_settings")
+    os.makedirs(d, exist_ok=True)
+    try:
+        p = _write(d, BASE + extra)
+        with pytest.raises(mcpm.MCPMError) as e:
+            mcpm.config_from_settings(p)
+        assert needle in str(e.value)
+        p = _write(d, BASE)
+        cfg, N = mcpm.config_from_settings(p)
+        assert N == 100 and cfg.model == mcpm.MODEL_FP_DENSE
+    finally:
+        for f in os.listdir(d):
+            os.remove(os.path.join(d, f))
+        os.rmdir(d)
