@@ -206,6 +206,13 @@ int mcpm_config_derive(mcpm_config* cfg, int64_t n_particles);
    the session for an FP32 one. */
 int mcpm_config_from_settings(const char* path, mcpm_config* out, int64_t* n_particles, char* msg,
                               int32_t msg_len);
+/* initialization (src/Main_Functions.cpp:4222-4814) for the same problems:
+   fills n_particles (= the file's N) host particles, uniform along the
+   streaming directions and mid-box along the others, velocities Maxwellian
+   about U0 at T = max(gas.T, max(T_wall_1 + T_wall_2, T_wall_3 + T_wall_4)/2).
+   The reference seeds from std::random_device; seed makes a run repeatable. */
+int mcpm_initialize_from_settings(const char* path, uint64_t seed, double* x1, double* x2, double* U1, double* U2,
+                                  double* U3, int64_t n_particles, char* msg, int32_t msg_len);
 int mcpm_session_create(const mcpm_config* cfg, mcpm_session** out);
 int mcpm_session_destroy(mcpm_session* s);
 const char* mcpm_last_error(const mcpm_session* s);

@@ -12,6 +12,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <random>
 #include <sstream>
 #include <string>
 
@@ -53,6 +54,7 @@ struct Raw {
   std::string model;
   double U_wall[4] = {-1.0, -1.0, -1.0, -1.0};
   double T_wall[4] = {-1.0, -1.0, -1.0, -1.0};
+  double U0[3] = {-1.0, -1.0, -1.0};
 };
 
 int set_msg(char* msg, int32_t len, const char* text, int code) {
@@ -73,14 +75,10 @@ int model_code(const std::string& m) {
   return -1;
 }
 
-}  // namespace
-
-extern "C" int mcpm_config_from_settings(const char* path, mcpm_config* out, int64_t* n_particles, char* msg,
-                                         int32_t msg_len) {
-  if (!path || !out) return set_msg(msg, msg_len, "settings: null argument", MCPM_ERR_ARG);
+// reads the file into r, then applies the defaults of src/myIO.cpp:2122-2188
+int read_raw(const char* path, Raw& r, char* msg, int32_t msg_len) {
   FILE* f = std::fopen(path, "r");
   if (!f) return set_msg(msg, msg_len, "settings: cannot open the file", MCPM_ERR_ARG);
-  Raw r;
   char buf[4096];
   int rc = MCPM_OK;
   char err[512] = {0};
@@ -116,6 +114,7 @@ extern "C" int mcpm_config_from_settings(const char* path, mcpm_config* out, int
     else if (key == "phi") iss >> r.phi;
     else if (key == "problem") iss >> r.problem;
     else if (key == "num_cells") iss >> r.cells[0] >> r.cells[1] >> r.cells[2];
+    else if (key == "U0") iss >> r.U0[0] >> r.U0[1] >> r.U0[2];
     else if (key.rfind("U_wall_", 0) == 0 || key.rfind("T_wall_", 0) == 0) {
       const int w = key[7] - '1';
       if (w >= 0 && w < 4) iss >> (key[0] == 'U' ? r.U_wall[w] : r.T_wall[w]);
@@ -125,9 +124,6 @@ extern "C" int mcpm_config_from_settings(const char* path, mcpm_config* out, int
   }
   std::fclose(f);
   if (rc) return set_msg(msg, msg_len, err, rc);
-
-  // ---- the derivation, src/myIO.cpp:2122-2900, problems 1 and 2
-  const double pi = std::acos(-1.0);
   if (r.Len[0] < 0.0) return set_msg(msg, msg_len, "settings: box_len is required", MCPM_ERR_ARG);
   if (r.cells[0] < 1 || r.cells[1] < 1 || r.cells[2] != 1)
     return set_msg(msg, msg_len, "settings: num_cells must be N0 N1 1", MCPM_ERR_ARG);
@@ -139,6 +135,7 @@ extern "C" int mcpm_config_from_settings(const char* path, mcpm_config* out, int
   if (r.sigma < 0.0) r.sigma = 1;
   if (r.n < 0.0) r.n = 1e-3;
   if (r.m < 0.0) r.m = 1.0;
+  if (r.U0[0] < 0.0) r.U0[0] = r.U0[1] = r.U0[2] = 1.0;
   if (r.problem < 0) r.problem = 1;
   for (int i = 0; i < 4; ++i)
     if (r.T_wall[i] < 0) r.T_wall[i] = 1.0;
@@ -146,6 +143,18 @@ extern "C" int mcpm_config_from_settings(const char* path, mcpm_config* out, int
     return set_msg(msg, msg_len,
                    "settings: only problems closed_box (1) and couette_flow (2) configure the particle step",
                    MCPM_ERR_ARG);
+  return MCPM_OK;
+}
+
+}  // namespace
+
+extern "C" int mcpm_config_from_settings(const char* path, mcpm_config* out, int64_t* n_particles, char* msg,
+                                         int32_t msg_len) {
+  if (!path || !out) return set_msg(msg, msg_len, "settings: null argument", MCPM_ERR_ARG);
+  Raw r;
+  if (int rc = read_raw(path, r, msg, msg_len)) return rc;
+  // ---- the derivation, src/myIO.cpp:2213-2900, problems 1 and 2
+  const double pi = std::acos(-1.0);
   const int model = model_code(r.model);
   if (model < 0) return set_msg(msg, msg_len, "settings: the model is outside the particle step", MCPM_ERR_ARG);
   if (!r.has_visp) return set_msg(msg, msg_len, "settings: visp is required", MCPM_ERR_ARG);
@@ -227,5 +236,39 @@ extern "C" int mcpm_config_from_settings(const char* path, mcpm_config* out, int
   c.crref = crref;
   *out = c;
   if (n_particles) *n_particles = r.N;
+  return set_msg(msg, msg_len, "", MCPM_OK);
+}
+
+// initialization (src/Main_Functions.cpp:4222-4814), its branch for the
+// problems above: positions uniform along the streaming directions and at
+// mid-box along the others (:4657-4672); velocities normal about U0 with
+// sqrt(kb T / m), T = max(gas.T, max(T_wall_1 + T_wall_2, T_wall_3 + T_wall_4) / 2)
+// (:4790-4799).  The reference seeds its generator from std::random_device;
+// here a 64-bit Mersenne twister seeded by the caller gives the uniforms and
+// Box-Muller pairs the normals, so a seed repeats a run on any host.
+extern "C" int mcpm_initialize_from_settings(const char* path, uint64_t seed, double* x1, double* x2, double* U1,
+                                             double* U2, double* U3, int64_t n_particles, char* msg,
+                                             int32_t msg_len) {
+  if (!path || !x1 || !x2 || !U1 || !U2 || !U3)
+    return set_msg(msg, msg_len, "initialize: null argument", MCPM_ERR_ARG);
+  Raw r;
+  if (int rc = read_raw(path, r, msg, msg_len)) return rc;
+  if (n_particles != r.N) return set_msg(msg, msg_len, "initialize: n_particles differs from the file's N", MCPM_ERR_ARG);
+  std::mt19937_64 gen(seed);
+  auto uni = [&]() { return ((double)(gen() >> 11) + 0.5) * (1.0 / 9007199254740992.0); };
+  for (int64_t i = 0; i < r.N; ++i) {
+    x1[i] = r.direction[0] == 1 ? uni() * r.Len[0] : 0.5 * r.Len[0];
+    x2[i] = r.direction[1] == 1 ? uni() * r.Len[1] : 0.5 * r.Len[1];
+  }
+  double T = std::fmax(r.T_wall[0] + r.T_wall[1], r.T_wall[2] + r.T_wall[3]) / 2.0;
+  T = std::fmax(r.T, T);
+  const double sd = std::sqrt(r.kb * T / r.m);
+  const double two_pi = 2.0 * std::acos(-1.0);
+  double* U[3] = {U1, U2, U3};
+  for (int64_t i = 0; i < r.N; ++i)
+    for (int d = 0; d < 3; ++d) {
+      const double a = std::sqrt(-2.0 * std::log(uni())), z = a * std::cos(two_pi * uni());
+      U[d][i] = r.U0[d] + sd * z;
+    }
   return set_msg(msg, msg_len, "", MCPM_OK);
 }

@@ -82,6 +82,19 @@ def config_from_settings(path: str):
     return cfg, n.value
 
 
+def initialize_from_settings(path: str, seed: int, n_particles: int):
+    """initialization (src/Main_Functions.cpp:4222-4814) for a settings file's
+    closed-box or Couette run: dict of the N initial particles."""
+    L = load_library()
+    out = {k: np.zeros(n_particles) for k in ("x1", "x2", "U1", "U2", "U3")}
+    msg = C.create_string_buffer(512)
+    rc = L.mcpm_initialize_from_settings(os.fsencode(path), seed, *[_dp(out[k]) for k in ("x1", "x2", "U1", "U2", "U3")],
+                                         n_particles, msg, 512)
+    if rc:
+        raise MCPMError(rc, msg.value.decode())
+    return out
+
+
 def derive(cfg: Config, n_particles: int) -> Config:
     """Derived GAS fields as readSettingsFile fills them (src/myIO.cpp:2217-2233,
     :2828-2830); identical to mcpm_config_derive in the library."""
@@ -135,6 +148,7 @@ def load_library(path: str | None = None):
     sig = {
         "mcpm_config_derive": (C.c_int, [C.POINTER(Config), i64]),
         "mcpm_config_from_settings": (C.c_int, [C.c_char_p, C.POINTER(Config), C.POINTER(i64), C.c_char_p, i32]),
+        "mcpm_initialize_from_settings": (C.c_int, [C.c_char_p, C.c_uint64, dp, dp, dp, dp, dp, i64, C.c_char_p, i32]),
         "mcpm_session_create": (C.c_int, [C.POINTER(Config), C.POINTER(vp)]),
         "mcpm_session_destroy": (C.c_int, [vp]),
         "mcpm_last_error": (C.c_char_p, [vp]),

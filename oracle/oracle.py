@@ -276,6 +276,8 @@ def ref_lib(build=True):
     sig = {
         "ref_create": (vp, [C.POINTER(Config), C.c_long]),
         "ref_read_settings": (None, [C.c_char_p, C.POINTER(C.c_long), C.POINTER(C.c_double)]),
+        "ref_initialize": (None, [C.c_char_p, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                  C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_long]),
         "ref_destroy": (None, [vp]),
         "ref_set_step": (None, [vp, C.c_int]),
         "ref_inject_normals": (None, [dp, dp, dp, C.c_long]),
@@ -404,3 +406,15 @@ def ref_read_settings(path):
     L.ref_read_settings(os.fsencode(path), iv.ctypes.data_as(C.POINTER(C.c_long)),
                         dv.ctypes.data_as(C.POINTER(C.c_double)))
     return iv, dv[:26]
+
+
+def ref_initialize(path, N):
+    """The reference's initialization after readSettingsFile: dict of its N
+    initial particles; None without the reference."""
+    L = ref_lib()
+    if L is None:
+        return None
+    out = {k: np.zeros(N) for k in ("x1", "x2", "U1", "U2", "U3")}
+    dp = C.POINTER(C.c_double)
+    L.ref_initialize(os.fsencode(path), *[out[k].ctypes.data_as(dp) for k in ("x1", "x2", "U1", "U2", "U3")], N)
+    return out

@@ -311,6 +311,23 @@ void ref_read_settings(const char* path, long* iv, double* dv) {
   for (int i = 0; i < 26; ++i) dv[i] = dvals[i];
 }
 
+// readSettingsFile then initialization (src/Main_Functions.cpp:4222) on the
+// file at path: the reference's initial particles (N of them)
+void ref_initialize(const char* path, double* x1, double* x2, double* U1, double* U2, double* U3, long N) {
+  Quiet q;
+  GAS g{};
+  BOX b{};
+  b.file_name = path;
+  readSettingsFile(&g, &b);
+  if ((long)g.N != N) return;
+  const int C = b.N[0] * b.N[1] * b.N[2];
+  CELLS* cells = (CELLS*)calloc(C, sizeof(CELLS));
+  make_cells(&b, cells, &g);
+  std::vector<double> x3(N);
+  initialization(U1, U2, U3, x1, x2, x3.data(), &g, &b, cells);
+  free(cells);
+}
+
 void ref_init_omega_max(void* h) {
   // src/main.cpp:250-269
   Ref* r = (Ref*)h;

@@ -1,7 +1,8 @@
-"""A run configured by a settings file in the reference's format
-(mcpm_config_from_settings): seeded particles in the configured box, fused
-FP64 steps on the GPU against the oracle under the same configuration, both
-drawing the same Philox streams (1e-10)."""
+"""A run set up by a settings file in the reference's format: the
+configuration (mcpm_config_from_settings) and the initial particles
+(mcpm_initialize_from_settings), then fused FP64 steps on the GPU against
+the oracle under the same configuration, both drawing the same Philox
+streams (1e-10)."""
 import os
 
 import numpy as np
@@ -16,13 +17,9 @@ SETTINGS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "s
 
 
 def test_settings_drive_the_step(cuda_ok):
-    cfg, N = mcpm.config_from_settings(os.path.join(SETTINGS, "reduced_fp_ideal.in"))
-    rng = np.random.default_rng(41)
-    L = cfg.length
-    parts = dict(x1=rng.uniform(0.0, L[0], N), x2=rng.uniform(0.0, L[1], N))
-    s = np.sqrt(cfg.kb * 1.0 / cfg.m)  # the file's T = 1
-    for k in ("U1", "U2", "U3"):
-        parts[k] = rng.normal(0.0, s, N)
+    path = os.path.join(SETTINGS, "reduced_fp_ideal.in")
+    cfg, N = mcpm.config_from_settings(path)
+    parts = mcpm.initialize_from_settings(path, 41, N)
     ses = mcpm.Session(cfg)
     ses.upload(parts["x1"], parts["x2"], parts["U1"], parts["U2"], parts["U3"])
     o = Oracle(cfg, parts)

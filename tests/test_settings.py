@@ -97,3 +97,34 @@ def test_settings_errors(built, extra, needle):
         for f in os.listdir(d):
             os.remove(os.path.join(d, f))
         os.rmdir(d)
+
+
+@pytest.mark.parametrize("name", ["closed_box_fp_dense.in", "couette_esmc.in"])
+def test_initialize_from_settings(built, name):
+    """initialization's branch for problems 1 and 2: positions uniform along
+    the streaming directions (mid-box otherwise), velocities normal about U0
+    at T = max(gas.T, max(T_w1 + T_w2, T_w3 + T_w4) / 2).  Repeatable for a
+    seed; against the reference's own initialization (std::random_device)
+    statistically: means within 5 standard errors, variances within 5 %."""
+    path = os.path.join(SETTINGS, name)
+    cfg, N = mcpm.config_from_settings(path)
+    a = mcpm.initialize_from_settings(path, 7, N)
+    b = mcpm.initialize_from_settings(path, 7, N)
+    assert all(np.array_equal(a[k], b[k]) for k in a)
+    for d, k in ((0, "x1"), (1, "x2")):
+        if cfg.direction[d]:
+            assert a[k].min() > 0 and a[k].max() < cfg.length[d]
+            assert abs(a[k].mean() / cfg.length[d] - 0.5) < 5 * np.sqrt(1 / 12 / N)
+        else:
+            assert np.all(a[k] == 0.5 * cfg.length[d])
+    ref = O.ref_initialize(path, N)
+    if ref is None:
+        return
+    for k in ("x1", "x2"):
+        d = 0 if k == "x1" else 1
+        if not cfg.direction[d]:
+            assert np.array_equal(a[k], ref[k])
+    for k in ("U1", "U2", "U3"):
+        se = np.sqrt((a[k].var() + ref[k].var()) / N)
+        assert abs(a[k].mean() - ref[k].mean()) < 5 * se, k
+        assert abs(a[k].var() / ref[k].var() - 1) < 0.05, k
