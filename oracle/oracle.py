@@ -418,3 +418,15 @@ def ref_initialize(path, N):
     dp = C.POINTER(C.c_double)
     L.ref_initialize(os.fsencode(path), *[out[k].ctypes.data_as(dp) for k in ("x1", "x2", "U1", "U2", "U3")], N)
     return out
+
+
+def ref_src_dir():
+    """The reference's source directory when present (the sources oracle/build.py
+    compiles), else None."""
+    sys.path.insert(0, HERE)
+    try:
+        from build import REF_SRC_DEFAULT
+    finally:
+        sys.path.remove(HERE)
+    d = os.environ.get("MCPM_REFERENCE_SRC", REF_SRC_DEFAULT)
+    return d if os.path.isdir(d) else None

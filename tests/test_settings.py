@@ -128,3 +128,15 @@ def test_initialize_from_settings(built, name):
         se = np.sqrt((a[k].var() + ref[k].var()) / N)
         assert abs(a[k].mean() - ref[k].mean()) < 5 * se, k
         assert abs(a[k].var() / ref[k].var() - 1) < 0.05, k
+
+
+def test_reference_settings_file(built):
+    """The reference's own settings file (its injection run, problem 12):
+    every keyword is read, and the problem is refused as outside the step."""
+    src = O.ref_src_dir()
+    path = os.path.join(src, "injection.in") if src else None
+    if not path or not os.path.exists(path):
+        pytest.skip("reference sources not available")
+    with pytest.raises(mcpm.MCPMError) as e:
+        mcpm.config_from_settings(path)
+    assert "problems" in str(e.value)
