@@ -128,8 +128,15 @@ int read_raw(const char* path, Raw& r, char* msg, int32_t msg_len) {
   if (r.cells[0] < 1 || r.cells[1] < 1 || r.cells[2] != 1)
     return set_msg(msg, msg_len, "settings: num_cells must be N0 N1 1", MCPM_ERR_ARG);
   if (r.N < 1) return set_msg(msg, msg_len, "settings: N (particles) is required", MCPM_ERR_ARG);
-  if (r.delta_dim[0] < 0.0)
+  if (r.delta_dim[0] < 0.0) {
     for (int i = 0; i < 3; ++i) r.delta_dim[i] = r.Len[i] / r.cells[i];
+  } else {
+    // the session's cells are Len / N: a box_delta_dim that disagrees would
+    // give the reference other cells than the step's
+    for (int i = 0; i < 2; ++i)
+      if (std::fabs(r.delta_dim[i] - r.Len[i] / r.cells[i]) > 1e-12 * std::fabs(r.Len[i] / r.cells[i]))
+        return set_msg(msg, msg_len, "settings: box_delta_dim differs from box_len / num_cells", MCPM_ERR_ARG);
+  }
   if (r.kb < 0.0) r.kb = 1.38064852 * 1e-23;
   if (r.T < 0.0) r.T = 1.0 / r.kb;
   if (r.sigma < 0.0) r.sigma = 1;

@@ -79,6 +79,7 @@ BASE = "model FP_dense\nN 100\nvisp 0.5\nnualpha 1.0\nbox_len 1 10 1\nnum_cells 
     ("bogus_key 3\n", "unknown keyword"),
     ("problem 3\n", "problems"),
     ("model MD\n", "model"),
+    ("box_delta_dim 1 2 1\n", "box_delta_dim"),
 ])
 def test_settings_errors(built, extra, needle):
     """what the reference aborts on, or what lies outside the particle step,
