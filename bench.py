@@ -4,7 +4,8 @@
 Workload (default, surrogate16m): the 2-D Enskog-Vlasov box -- 256 x 256
 unit cells, 16.0M particles with a sinusoidally perturbed density (n b
 between 0.05 and 0.45), Enskog-Fokker-Planck (FP_dense), FP32 particle state
-with compensated FP32 moment sums and FP64 per-cell drift solves, specular
+with FP32 moment sums (per-lane runs combined pairwise) and FP64 per-cell
+drift solves, specular
 walls, and the Vlasov mean-field force from the learned convolutional
 operator, judged every 10 steps by the plain screened-Poisson FEM path
 (which takes over while the kick error exceeds 1%).  A step is one
@@ -451,6 +452,50 @@ def run_mcpm(args):
     print(json.dumps(line))
 
 
+# ------------------------------------------------- small case for ncu
+def run_profile_case(args):
+    """A small particle-step run for ncu captures: the named workload on an
+    n x n grid (``--cells``; the 1-D slab: n cells), ``--steps`` fused steps
+    (the first launches of each kernel are the warm-up, so a capture takes
+    ``-s 2 -c 1`` of the kernel it names), exits 0.
+
+    uneven     log-normal uneven cells (n = 160: 25,600 cells, ~6.3M particles,
+               175 MB of FP32 state -- above the 129 MB L2, a few hundred MB
+               on the device)
+    esmc       the 2-D ESMC box with diffuse walls (100 particles per cell)
+    slab       the 1-D Enskog-Vlasov slab (1000 particles per cell)
+    vlasov     the 2-D Enskog-Vlasov box with the screened-Poisson force
+               (244 particles per cell on average: 16.0M at n = 256)
+    surrogate  the same box with the trained Vlasov network attached (plain
+               judge every 10 steps; the first step is a judge step)"""
+    import mcpm
+    import workloads as W
+    kind, n = args.profile_case, args.cells
+    prec = mcpm.FP64 if args.fp64 else mcpm.FP32
+    if kind == "uneven":
+        cfg, parts = W.uneven_cells_2d(n_cells=(n, n), precision=prec, streaming=True)
+    elif kind == "esmc":
+        cfg, parts = W.esmc_box_2d(n_cells=(n, n), precision=prec)
+    elif kind in ("vlasov", "surrogate"):
+        cfg, parts = W.vlasov_box_2d(n_cells=(n, n), total=244 * n * n, precision=prec,
+                                     long_range=mcpm.LR_SCREENED_POISSON, model=mcpm.MODEL_FP_DENSE)
+    elif kind == "slab":
+        cfg, parts = W.vlasov_slab_1d(n_cells=n, precision=prec)
+    else:
+        raise SystemExit("unknown profile case %r" % kind)
+    s = mcpm.Session(cfg)
+    s.upload(parts["x1"], parts["x2"], parts["U1"], parts["U2"], parts["U3"])
+    sur = None
+    if kind == "surrogate":
+        import surrogate as SG
+        sur = SG.attach(s, judge_every=10, threshold=0.01)
+    s.step(args.steps)
+    s.sync()
+    s.check_status()
+    print("ok", kind, n, len(parts["x2"]), s.surrogate_stats() if sur else "")
+    s.close()
+
+
 # --------------------------------------------------------- reference arm
 def _ref_worker_init(jobs):
     global _W
@@ -560,7 +605,14 @@ def main():
     ap.add_argument("--workload", default="surrogate16m",
                     choices=["surrogate16m", "uneven16m", "esmc6m", "slab1m", "vlasov16m"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--profile-case", choices=["uneven", "esmc", "slab", "vlasov", "surrogate"],
+                    help="run a small case of a workload for an ncu capture and exit (no JSON line)")
+    ap.add_argument("--cells", type=int, default=160, help="grid size n of --profile-case")
+    ap.add_argument("--fp64", action="store_true", help="FP64 state for --profile-case")
     args = ap.parse_args()
+    if args.profile_case:
+        run_profile_case(args)
+        return
     if args.warmup < 3 and args.impl == "mcpm":
         args.warmup = 3
     if args.impl == "reference":

@@ -101,8 +101,9 @@ enum mcpm_long_range {
 
 enum mcpm_precision {
   MCPM_FP64 = 0,                /* particle state and sums in double            */
-  MCPM_FP32 = 1                 /* particle state float, compensated sums,
-                                   per-cell solves still in double              */
+  MCPM_FP32 = 1                 /* particle state and moment sums float
+                                   (per-lane runs combined pairwise), per-cell
+                                   solves still in double                       */
 };
 
 enum mcpm_rng {
@@ -221,8 +222,10 @@ int mcpm_sync(mcpm_session* s);
 int mcpm_check_status(mcpm_session* s);
 
 /* Copies caller arrays (reference layout, double, indexed by particle id) to
-   the device, bins them (cell_update's binning) and sorts the device copy by
-   cell.  x1 may be NULL when direction[0] == 0.  Resets the step counter. */
+   the device and bins them (cell_update's binning, which also reports
+   particles outside the box); the device copy is sorted by cell at the
+   first cell_update or step.  x1 may be NULL when direction[0] == 0.
+   Resets the step counter to 0. */
 int mcpm_upload_particles(mcpm_session* s, int64_t n, const double* x1,
                           const double* x2, const double* U1, const double* U2,
                           const double* U3);
@@ -308,6 +311,10 @@ int mcpm_get_node_density(mcpm_session* s, double* out);
 int mcpm_get_node_potential(mcpm_session* s, double* out);
 /* Whitened normals last produced by random_generator, per particle id. */
 int mcpm_get_normals(mcpm_session* s, double* xi1, double* xi2, double* xi3);
+/* The step number the draws are keyed by (the reference's loop counter).
+   Setting another number re-draws the binning's face jitter
+   (src/Main_Functions.cpp:2238-2247) at the next cell_update or step, as the
+   reference's cell_update at that step would. */
 int32_t mcpm_get_step(const mcpm_session* s);
 int mcpm_set_step(mcpm_session* s, int32_t step);
 /* Overwrite one cell field (e.g. omega_max) for all cells from host data. */
@@ -356,10 +363,14 @@ int mcpm_autotune(mcpm_session* s, int32_t steps, int32_t* chosen);
    from cfg (length[1], sigma, eqdist, bst, ast, m).  It allocates nothing:
    its scratch is a fixed array of the library that every GPU loading the
    library holds until exit.  n_cells above MCPM_NOALLOC_MAX_CELLS returns
-   MCPM_ERR_CAPACITY.  The first call on a device resolves the scratch's
-   device address (call it once before any stream capture).  All calls share
-   the scratch, so calls that overlap on the GPU race.  stream may be NULL.
-   Synchronises the stream before returning. */
+   MCPM_ERR_CAPACITY.  The first call on a device, with that device current,
+   looks up the scratch's device address and sets the force kernel's
+   shared-memory limit; make that first call before any stream capture on
+   the device begins.  All calls on one device share its scratch, so calls
+   whose work overlaps on that GPU (two streams, or two host threads) race;
+   calls on different devices do not share it, and no host-side buffer is
+   shared.  stream may be NULL.  The work is queued on the stream and the
+   call returns without waiting: F2 is ready once the stream has reached it. */
 #define MCPM_NOALLOC_MAX_CELLS 6999
 int mcpm_poisson_force_1d_noalloc(const double* n_cell, int32_t n_cells,
                                   const mcpm_config* cfg, double* F2,

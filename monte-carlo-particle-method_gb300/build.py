@@ -3,7 +3,7 @@
 Each CUDA translation unit is compiled in parallel with nvcc, then linked into
 one shared library next to this file.  The particle kernels are compiled with
 ``--fmad=false``: the FP64 path then rounds every multiply and add separately,
-as the reference does, and the compensated FP32 sums stay exact.
+as the reference does (the FP32 kernels write their fused multiply-adds out).
 """
 from __future__ import annotations
 

@@ -94,6 +94,8 @@ template <typename real> struct KC {
   real dx, dy, L0, L1, dt, sigma, m, kb, Tw[4], Uw[4];
   real idx, idy;  // 1/dx, 1/dy (FP32 binning)
   real eps_x, eps_y;  // diffuse-wall offsets
+  const float *face_x, *face_y;  // FP32 binning face tables (DevConsts)
+  float wx, wy;
 };
 template <typename real> __host__ __device__ __forceinline__ KC<real> make_kc(const DevConsts& k) {
   KC<real> c;
@@ -102,11 +104,13 @@ template <typename real> __host__ __device__ __forceinline__ KC<real> make_kc(co
     c.sigma = k.f_sigma; c.m = k.f_m; c.kb = k.f_kb;
     for (int i = 0; i < 4; ++i) { c.Tw[i] = k.f_Tw[i]; c.Uw[i] = k.f_Uw[i]; }
     c.idx = k.f_idx; c.idy = k.f_idy; c.eps_x = k.f_eps_x; c.eps_y = k.f_eps_y;
+    c.face_x = k.f_face_x; c.face_y = k.f_face_y; c.wx = k.f_bin_wx; c.wy = k.f_bin_wy;
   } else {
     c.dx = k.dx; c.dy = k.dy; c.L0 = k.L0; c.L1 = k.L1; c.dt = k.dt;
     c.sigma = k.sigma; c.m = k.m; c.kb = k.kb;
     for (int i = 0; i < 4; ++i) { c.Tw[i] = k.Tw[i]; c.Uw[i] = k.Uw[i]; }
     c.idx = 1.0 / k.dx; c.idy = 1.0 / k.dy; c.eps_x = k.eps_x; c.eps_y = k.eps_y;
+    c.face_x = nullptr; c.face_y = nullptr; c.wx = 0.f; c.wy = 0.f;
   }
   return c;
 }
@@ -152,6 +156,8 @@ __device__ __forceinline__ CSum ccombine(CSum a, CSum b) {
 __device__ __forceinline__ double cvalue(CSum a) { return (double)a.hi + (double)a.lo; }
 
 // accumulator abstraction: double sums in FP64 mode, compensated float in FP32
+// (the float form serves only code written for both precisions; the FP32
+// sessions' kernels sum in plain float runs combined pairwise)
 template <typename real> struct Acc;
 template <> struct Acc<double> {
   double v;

@@ -84,6 +84,15 @@ struct DevConsts {
   double de_p, de_s2p, de_s2h2;
   // float copies for the FP32 kernels
   float f_dx, f_dy, f_L0, f_L1, f_dt, f_sigma, f_m, f_kb, f_Tw[4], f_Uw[4], f_idx, f_idy, f_eps_x, f_eps_y;
+  // FP32 binning.  f_face_x[j] (j = 0..N0) is the smallest float x with
+  // floor((double)x / dx) >= j, +inf at j = N0 + 1; f_face_y likewise over
+  // dy.  f_bin_wx / f_bin_wy: where the fraction of x * (1/dx) in float lies
+  // within this distance of an integer, the float quotient may sit on the
+  // wrong side of a face (or within the reference's 1e-15 jitter band), and
+  // the cell is taken from the face table instead.
+  const float* f_face_x;
+  const float* f_face_y;
+  float f_bin_wx, f_bin_wy;
 };
 
 // One set of device particle arrays (SoA).  real is float or double.
@@ -152,6 +161,7 @@ struct Session {
   double* inj = nullptr;        // [3][cap] injected raw normals, particle-id order
   double* stage = nullptr;      // [5][cap] host<->device staging (double)
   double* faces = nullptr;      // [4][N1+1] long-range face scratch
+  float* bin_faces = nullptr;   // [N0+2 + N1+2] FP32 binning face tables (DevConsts f_face_x/y)
   void* lr_tab = nullptr;       // long-range tables (stencil / PCR coefficients)
   alignas(16) char lr_host[160];  // the kernel's view of lr_tab
   LR2D* lr2d = nullptr;         // 2-D long range (node grid), when configured

@@ -12,8 +12,8 @@
 // Cells are processed by persistent blocks fed from two prefix-sum work
 // lists: cells with more than `wcap` particles are handled by a whole block,
 // the rest by one warp each.  Compiled with --fmad=false: every multiply
-// and add rounds separately, as in the reference (x86-64 without FMA) and as
-// the compensated FP32 sums require.
+// and add rounds separately, as in the reference (x86-64 without FMA); the
+// FP32 kernels write their fused multiply-adds out (fmaf).
 #include <cfloat>
 
 #include <type_traits>
@@ -38,38 +38,69 @@ template <typename real> static PT<real> pt(const PBuf& b) {
 // jitter of :2238-2247 drawn from Philox.  Particles outside [0, Len] raise
 // MCPM_ERR_OUT_OF_BOX (the reference exits); a particle on the far wall is
 // binned into the last cell.
+
+// floor((double)x / d) for a float x from its float estimate i = floor(x * (1/d)),
+// which is at most one cell off: face[c] is the smallest float whose
+// quotient reaches c (face[n + 1] = +inf)
+__device__ __forceinline__ int face_fix(float x, int i, int n, const float* face) {
+  const int c = i < 0 ? 0 : (i > n ? n : i);
+  if (x < __ldg(face + c)) return c - 1;
+  if (x >= __ldg(face + c + 1)) return c + 1;
+  return c;
+}
+
 template <typename real>
 __device__ __forceinline__ int bin_one(real x1, real x2, int pid, int step, const DevConsts& k, const KC<real>& kc,
                                        uint32_t& bad, int* jo = nullptr, int* ko = nullptr) {
-  // FP64: r_floor(x / dx) as the reference; FP32: x * (1/dx)
+  // FP64: r_floor(x / dx) as the reference.  FP32: the same cell, floor of
+  // the double quotient of the float position: x * (1/dx) in float, and the
+  // face tables where that quotient lies within rounding of an integer
   constexpr bool F32 = sizeof(real) == 4;
   int j = 0;
-  const real dy = kc.dy;
-  real tk;  // k as a real: dy * k needs no conversion
   int kk;
   if constexpr (F32) {
     if (k.dir0 == 1) {
       float tj;
-      j = floor_to_int(x1 * kc.idx, &tj);
+      const float q = x1 * kc.idx;
+      j = floor_to_int(q, &tj);
+      const float fr = q - tj;
+      if (fr < kc.wx || fr > 1.f - kc.wx) j = face_fix(x1, j, k.N0, kc.face_x);
       if (!(x1 >= 0.f && x1 <= kc.L0)) bad |= MCPM_ERR_OUT_OF_BOX;
     }
-    kk = floor_to_int(x2 * kc.idy, &tk);
+    float tk;
+    const float q = x2 * kc.idy;
+    kk = floor_to_int(q, &tk);
+    const float fr = q - tk;
+    if (fr < kc.wy || fr > 1.f - kc.wy) {
+      kk = face_fix(x2, kk, k.N1, kc.face_y);
+      // the face jitter, tested in double on the float position as the
+      // reference tests its position (the band lies inside the window)
+      if (kk > 0 && kk < k.N1 - 1) {
+        const double xd = (double)x2;
+        if (fabs(xd - k.dy * kk) < 1e-15 || fabs(xd - k.dy * (kk + 1)) < 1e-15) {
+          uint4 r = philox(k.seed, (uint32_t)pid, (uint32_t)step, RNG_BIN, 0u);
+          int sgn = (r.x >= 0x80000000u) ? 1 : -1;  // u01(r.x) > 0.5
+          kk = (int)floor((xd + 1e-14 * sgn) / k.dy);
+        }
+      }
+    }
   } else {
+    const real dy = kc.dy;
     if (k.dir0 == 1) {
       j = (int)r_floor(x1 / kc.dx);
       if (!(x1 >= (real)0 && x1 <= kc.L0)) bad |= MCPM_ERR_OUT_OF_BOX;
     }
-    tk = r_floor(x2 / dy);
+    const real tk = r_floor(x2 / dy);  // k as a real: dy * k needs no conversion
     kk = (int)tk;
-  }
-  if (!(x2 >= (real)0 && x2 <= kc.L1)) bad |= MCPM_ERR_OUT_OF_BOX;
-  if (kk > 0 && kk < k.N1 - 1) {
-    if (r_fabs(x2 - dy * tk) < (real)1e-15 || r_fabs(x2 - dy * (tk + (real)1)) < (real)1e-15) {
-      uint4 r = philox(k.seed, (uint32_t)pid, (uint32_t)step, RNG_BIN, 0u);
-      int sgn = (r.x >= 0x80000000u) ? 1 : -1;  // u01(r.x) > 0.5
-      kk = (int)r_floor((x2 + (real)1e-14 * sgn) / dy);
+    if (kk > 0 && kk < k.N1 - 1) {
+      if (r_fabs(x2 - dy * tk) < (real)1e-15 || r_fabs(x2 - dy * (tk + (real)1)) < (real)1e-15) {
+        uint4 r = philox(k.seed, (uint32_t)pid, (uint32_t)step, RNG_BIN, 0u);
+        int sgn = (r.x >= 0x80000000u) ? 1 : -1;  // u01(r.x) > 0.5
+        kk = (int)r_floor((x2 + (real)1e-14 * sgn) / dy);
+      }
     }
   }
+  if (!(x2 >= (real)0 && x2 <= kc.L1)) bad |= MCPM_ERR_OUT_OF_BOX;
   j = j < 0 ? 0 : (j > k.N0 - 1 ? k.N0 - 1 : j);
   kk = kk < 0 ? 0 : (kk > k.N1 - 1 ? k.N1 - 1 : kk);
   if (jo) *jo = j;
@@ -1365,8 +1396,9 @@ template <typename real> __device__ __forceinline__ real crms(const Acc<real>& s
 // xs stages three values per particle in shared memory when the cell fits:
 // the raw normals, then the new peculiar velocities M'.
 // The FP64 path follows the reference's two-pass centring/normalisation of
-// the normals; the FP32 path takes the per-cell mean and RMS from one pass
-// of compensated sums of z and z^2.
+// the normals.  Instantiated for FP64 sessions only (FP32 sessions run
+// update_cell_f32 below); its float branches are not compiled into the
+// library.
 template <typename real, int TILE, uint32_t CST>
 __device__ void update_cell(int c, const UpdArgs<real>& a, int step, real* xs, int xcap, Acc<real>* red) {
   constexpr bool F32 = sizeof(real) == 4;
@@ -1645,7 +1677,7 @@ __device__ void update_cell(int c, const UpdArgs<real>& a, int step, real* xs, i
 
 // The FP32 particle pass: the stages of update_cell for float state, with
 // plain FP32 per-lane sums of the whitening and energy terms combined
-// pairwise (tile_sum_f32; the compensated sums stay in the moment pass),
+// pairwise (tile_sum_f32),
 // fused multiply-adds throughout, and the packed per-cell record read into
 // registers where each pass needs it.
 template <int TILE, uint32_t CST, int PB, bool SL>

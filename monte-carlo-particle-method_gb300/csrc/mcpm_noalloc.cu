@@ -15,9 +15,11 @@
 // The scratch is the file-scope __device__ array below, of fixed size
 // (MCPM_NOALLOC_MAX_CELLS + 1 = 7000 face values plus the 2 x 2500-entry
 // quadrature table, 96 KB).  Every GPU that loads the library holds it until the
-// process exits.  All calls share it and it keeps the last call's contents;
-// each call rewrites every entry it reads before reading it.  Calls whose
-// work overlaps on the GPU (two streams, or two host threads) race on it.
+// process exits.  All calls on a device share it and it keeps the last call's
+// contents; each call rewrites every entry it reads before reading it (the
+// quadrature table by a kernel of its own, so no host buffer is involved).
+// Calls whose work overlaps on the same GPU (two streams, or two host
+// threads) race on it; calls on different GPUs use different copies.
 #include <cmath>
 #include <cstring>
 
@@ -68,6 +70,25 @@ struct Params {
   int N1;
   double dy, sigma, bst, ast, m;
 };
+
+// GL(50) radial points r_i in [0, 3 eqdist] and polar angles phi_i in
+// [0, pi] with their interval weights (poisson_solver :3362-3397), formed on
+// the host per call and passed by value
+struct QuadNodes {
+  double rr[50], dr[50], ph[50], dph[50];
+  double bst;
+};
+
+// the wall-integral quadrature table into the scratch: points r cos(phi)
+// and weights exp(-bst r) / 2 r dr sin(phi) dphi
+__global__ void k_noalloc_table(QuadNodes q, double* scratch) {
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < kQuad; t += gridDim.x * blockDim.x) {
+    const int i = t / 50, ii = t % 50;
+    const double radial = exp(-q.bst * q.rr[i]) / (2.0) * q.rr[i] * q.dr[i];
+    scratch[kFaces + t] = q.rr[i] * cos(q.ph[ii]);
+    scratch[kFaces + kQuad + t] = radial * sin(q.ph[ii]) * q.dph[ii];
+  }
+}
 
 // density of cell num with the reference's edge clamping
 __device__ __forceinline__ double nclamp(const double* n, int num, int N1) {
@@ -161,26 +182,17 @@ extern "C" int mcpm_poisson_force_1d_noalloc(const double* n_cell, int32_t n_cel
     g_scratch_ptr[dev] = (double*)ptr;
   }
   double* scratch = g_scratch_ptr[dev];
-  // quadrature points r cos(phi) and weights exp(-bst r)/2 r dr sin(phi) dphi
-  // of the wall integrals, r in [0, 3 eqdist], phi in [0, pi] (:3362-3397);
-  // built in static host storage, nothing allocated (shared by all host
-  // threads, like the device scratch)
-  static double qtab[2 * kQuad];
-  double xi[50], wi[50], rr[50], dr[50], ph[50], dph[50];
+  // the quadrature nodes of the wall integrals, r in [0, 3 eqdist] and phi
+  // in [0, pi] (:3362-3397); the table itself is formed on the GPU
+  QuadNodes qn;
+  double xi[50], wi[50];
   gl50(xi, wi);
   const double pi = acos(-1.0);
   const double bb = 3.0 * cfg->eqdist, aa = 0.0 * cfg->eqdist, cc = 0.0, dd = pi;
-  for (int i = 0; i < 50; ++i) { rr[i] = (bb - aa) / 2.0 * xi[i] + (aa + bb) / 2.0; dr[i] = wi[i] * (bb - aa) / 2.0; }
-  for (int i = 0; i < 50; ++i) { ph[i] = (dd - cc) / 2.0 * xi[i] + (cc + dd) / 2.0; dph[i] = wi[i] * (dd - cc) / 2.0; }
-  for (int i = 0; i < 50; ++i) {
-    double radial = exp(-cfg->bst * rr[i]) / (2.0) * rr[i] * dr[i];
-    for (int ii = 0; ii < 50; ++ii) {
-      qtab[i * 50 + ii] = rr[i] * cos(ph[ii]);
-      qtab[kQuad + i * 50 + ii] = radial * sin(ph[ii]) * dph[ii];
-    }
-  }
-  if (cudaMemcpyAsync(scratch + kFaces, qtab, sizeof(qtab), cudaMemcpyHostToDevice, st) != cudaSuccess)
-    return MCPM_ERR_CUDA;
+  for (int i = 0; i < 50; ++i) { qn.rr[i] = (bb - aa) / 2.0 * xi[i] + (aa + bb) / 2.0; qn.dr[i] = wi[i] * (bb - aa) / 2.0; }
+  for (int i = 0; i < 50; ++i) { qn.ph[i] = (dd - cc) / 2.0 * xi[i] + (cc + dd) / 2.0; qn.dph[i] = wi[i] * (dd - cc) / 2.0; }
+  qn.bst = cfg->bst;
+  k_noalloc_table<<<10, 256, 0, st>>>(qn, scratch);
   Params p;
   p.N1 = n_cells;
   p.dy = cfg->length[1] / n_cells;
@@ -191,7 +203,5 @@ extern "C" int mcpm_poisson_force_1d_noalloc(const double* n_cell, int32_t n_cel
   k_noalloc_walls<<<1, 64, 0, st>>>(p, n_cell, scratch);
   k_noalloc_pcr_force<<<1, 1024, 4 * (n_cells + 1) * sizeof(double), st>>>(p, n_cell, scratch, F2);
   if (cudaGetLastError() != cudaSuccess) return MCPM_ERR_CUDA;
-  // the host table must stay unchanged until the copy has read it
-  if (cudaStreamSynchronize(st) != cudaSuccess) return MCPM_ERR_CUDA;
   return MCPM_OK;
 }

@@ -108,6 +108,31 @@ template <typename F> static int timed(mcpm_session* s, int cls, F f) {
 #define T_UPD(x) timed(s, MCPM_K_UPDATE, [&] { return (x); })
 #define T_SUR(x) timed(s, MCPM_K_SURROGATE, [&] { return (x); })
 
+// FP32 binning.  face[c], c = 0..n: the smallest float x whose cell by the
+// reference's rule, floor((double)x / d), is at least c; face[n + 1] = +inf.
+// Division by a positive d is monotone, so the float cell of any x is the
+// number of faces at or below it.
+static void bin_face_table(float* face, int n, double d) {
+  for (int c = 0; c <= n; ++c) {
+    float f = (float)((double)c * d);
+    const float lo = -INFINITY, hi = INFINITY;
+    while (floor((double)nextafterf(f, lo) / d) >= c) f = nextafterf(f, lo);
+    while (floor((double)f / d) < c) f = nextafterf(f, hi);
+    face[c] = f;
+  }
+  face[n + 1] = INFINITY;
+}
+
+// Half-width of the band around an integer in which the fraction of the
+// float quotient x * fl(1/d) is not trusted: its error is below 2^-23 of the
+// quotient (two float roundings), at most n for a particle in the box; the
+// band also covers the reference's face-jitter band of 1e-15 / d, plus a
+// margin for the rounding of 1 - w in float.
+static float bin_window(int n, double d) {
+  const double w = 2.0 * ldexp(1.0, -23) * (n + 1) + 2e-15 / d + ldexp(1.0, -22);
+  return (float)fmin(w, 0.5);
+}
+
 // the models random_generator and the FP velocity update serve
 // (src/Fokker_Planck.cpp:22, src/Main_Functions.cpp:1565-1570)
 static inline bool is_fp_model(int m) {
@@ -263,11 +288,25 @@ int mcpm_session_create(const mcpm_config* cfg, mcpm_session** out) {
        A((void**)&s->cell, (size_t)CF_DEV_COUNT * C * 8) && A((void**)&s->pcell, (size_t)PF_STRIDE * C * 4) && A((void**)&s->xi, 3 * cap * 8) &&
        A((void**)&s->inj, 3 * cap * 8) && A((void**)&s->stage, 5 * cap * 8) &&
        A((void**)&s->faces, ((size_t)k.N1 + 1 + 5000) * 8) && A((void**)&s->status, 16) &&
-       A((void**)&s->dstep, 16);
+       A((void**)&s->dstep, 16) && A((void**)&s->bin_faces, ((size_t)k.N0 + k.N1 + 4) * 4);
   if (!ok) {
     s->err = "out of device memory";
     mcpm_session_destroy(s);
     return MCPM_ERR_CUDA;
+  }
+  {
+    // FP32 binning face tables and windows (DevConsts f_face_x / f_face_y)
+    std::vector<float> ft((size_t)k.N0 + k.N1 + 4);
+    bin_face_table(ft.data(), k.N0, k.dx);
+    bin_face_table(ft.data() + k.N0 + 2, k.N1, k.dy);
+    if ((rc = cuda_check(s, cudaMemcpy(s->bin_faces, ft.data(), ft.size() * 4, cudaMemcpyHostToDevice), "face tables"))) {
+      mcpm_session_destroy(s);
+      return rc;
+    }
+    k.f_face_x = s->bin_faces;
+    k.f_face_y = s->bin_faces + k.N0 + 2;
+    k.f_bin_wx = bin_window(k.N0, k.dx);
+    k.f_bin_wy = bin_window(k.N1, k.dy);
   }
   cudaMemsetAsync(s->cnt_next, 0, C * 4, s->stream);
   if (s->use_slotted) {
@@ -317,6 +356,7 @@ int mcpm_session_destroy(mcpm_session* s) {
   cudaFree(s->key); cudaFree(s->cnt); cudaFree(s->cnt_next); cudaFree(s->off); cudaFree(s->cursor);
   cudaFree(s->list_small); cudaFree(s->list_big); cudaFree(s->wl); cudaFree(s->work); cudaFree(s->scan_blk); cudaFree(s->cell); cudaFree(s->pcell);
   cudaFree(s->xi); cudaFree(s->inj); cudaFree(s->stage); cudaFree(s->faces); cudaFree(s->lr_tab); cudaFree(s->status); cudaFree(s->dstep);
+  cudaFree(s->bin_faces);
   lr2d_free(*s);
   cudaFree(s->sur_err);
   if (s->sur_err_h) cudaFreeHost(s->sur_err_h);
@@ -413,11 +453,15 @@ int mcpm_upload_particles(mcpm_session* s, int64_t n, const double* x1, const do
   s->step = 0;
   s->bc_calls = 0;
   s->omega_init = false;
-  s->keys_current = false;
   s->sorted = false;
   s->slotted = false;
   s->have_particles = true;
-  return sort_by_cell(s);
+  // the cell keys at step 0 (this also checks that every particle is in
+  // the box); the layout follows at the first cell_update or step, which
+  // re-draws the keys if the caller sets another step number first
+  rc = after_launch(s, T_BIN(launch_bin(*s, s->step)), "upload");
+  s->keys_current = rc == MCPM_OK;
+  return rc;
 }
 
 int mcpm_download_particles(mcpm_session* s, int64_t n, double* x1, double* x2, double* U1, double* U2, double* U3) {
@@ -674,7 +718,9 @@ static int run_steps(mcpm_session* s, int n_steps, uint32_t stages) {
   int it = 0, rc;
   // steady state: the last fused step left a slotted layout, or keys for
   // the scan and scatter
-  auto steady = [&]() { return !s->needs_rebin && (s->slotted || (s->keys_current && !s->sorted)); };
+  auto steady = [&]() {
+    return !s->needs_rebin && (s->use_slotted ? s->slotted : (s->keys_current && !s->sorted));
+  };
   while (it < n_steps && (!steady() || n_steps - it < 2 || s->prof || !s->use_graphs)) {
     if ((rc = after_launch(s, step_once(s, stages), "step"))) return rc;
     ++it;
@@ -725,7 +771,11 @@ int mcpm_step(mcpm_session* s, int32_t n_steps) {
     if (rc) return rc;
     if ((rc = mcpm_init_omega_max(s))) return rc;
   }
-  if (s->step == 0) s->step = 1;  // the loop of src/main.cpp starts at step 1 (:389)
+  if (s->step == 0) {
+    // the loop of src/main.cpp starts at step 1 (:389)
+    int rc = mcpm_set_step(s, 1);
+    if (rc) return rc;
+  }
   uint32_t stages = ST_BC1 | ST_OLD | ST_STREAM | ST_BC2 | ST_BC3 | ST_KEY;
   if (is_fp_model(m)) stages |= ST_RNG | ST_FP;
   if (m == MCPM_MODEL_FP_DENSE) stages |= ST_DFP;
@@ -936,6 +986,16 @@ int mcpm_get_layout(mcpm_session* s, int32_t* pid_by_slot, int32_t* off) {
 int32_t mcpm_get_step(const mcpm_session* s) { return s ? s->step : -1; }
 int mcpm_set_step(mcpm_session* s, int32_t step) {
   if (!s || step < 0) return MCPM_ERR_ARG;
+  if (step != s->step && s->have_particles) {
+    // the face jitter of the binning draws by step number: keys drawn at
+    // another step are re-drawn by the next cell_update or step
+    s->keys_current = false;
+    if (s->slotted) {
+      const int rc = leave_slotted(s);
+      if (rc) return rc;
+    }
+    if (s->sorted) s->needs_rebin = true;
+  }
   s->step = step;
   s->bc_calls = 0;
   return MCPM_OK;

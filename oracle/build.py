@@ -19,7 +19,15 @@ from concurrent.futures import ThreadPoolExecutor
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(HERE)
-REF_SRC_DEFAULT = "/root/reference/src"
+
+
+def default_ref_src():
+    """The reference's source folder: $MCPM_REFERENCE_SRC, else the
+    ``reference/src`` folder of a reference checkout beside this repository."""
+    env = os.environ.get("MCPM_REFERENCE_SRC")
+    if env:
+        return env
+    return os.path.join(os.path.dirname(REPO), "reference", "src")
 
 # reference translation units the particle step reaches (main.cpp, the
 # MKL-bound solver_pardiso.cpp, the dead solver.cpp demo and the rand()-based
@@ -55,7 +63,7 @@ def build_oracle(force=False):
 def build_ref(ref_src=None, force=False):
     """Compile the reference into oracle/_ref/libref.so; returns the path or
     None when the reference sources are not available."""
-    ref_src = ref_src or os.environ.get("MCPM_REFERENCE_SRC", REF_SRC_DEFAULT)
+    ref_src = ref_src or default_ref_src()
     if not os.path.isfile(os.path.join(ref_src, "cpp_headers.h")):
         return None
     outdir = os.path.join(HERE, "_ref")

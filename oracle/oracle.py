@@ -425,8 +425,8 @@ def ref_src_dir():
     compiles), else None."""
     sys.path.insert(0, HERE)
     try:
-        from build import REF_SRC_DEFAULT
+        from build import default_ref_src
     finally:
         sys.path.remove(HERE)
-    d = os.environ.get("MCPM_REFERENCE_SRC", REF_SRC_DEFAULT)
+    d = default_ref_src()
     return d if os.path.isdir(d) else None

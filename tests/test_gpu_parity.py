@@ -74,6 +74,60 @@ def test_binning_bit_exact(cuda_ok, maker):
     assert np.array_equal(np.sort(pid), np.arange(o.N))
 
 
+def _face_positions(n, d, L, rng, count):
+    """float32 positions in [0, L]: uniform ones, every face k d rounded to
+    float and its two float neighbours, 0 and L."""
+    f = np.arange(n + 1) * d
+    x = np.concatenate([rng.random(count) * L, f, np.nextafter(f.astype(np.float32), np.float32(np.inf)),
+                        np.nextafter(f.astype(np.float32), np.float32(-np.inf)), [0.0, L]])
+    top = np.float32(L)
+    if float(top) > L:  # the largest float inside the box
+        top = np.nextafter(top, np.float32(-np.inf))
+    x = np.clip(x.astype(np.float32), np.float32(0.0), top).astype(np.float64)
+    return rng.permutation(x)
+
+
+@pytest.mark.parametrize("shape,d", [((1, 37), 0.3), ((1, 40), 1.0), ((19, 23), 0.7)])
+def test_binning_fp32_bit_exact(cuda_ok, shape, d):
+    """FP32 sessions bin the float position by the reference's rule,
+    floor(x / dx) in double (src/Main_Functions.cpp:2232-2266), face jitter
+    included (a float lying on a face of unit cells, :2238-2247): the cell
+    index equals the oracle's on the same float-rounded positions, for
+    positions on every face, one float either side of it, 0 and Len; then
+    again after a fused step, whose particle pass bins the new positions."""
+    rng = np.random.default_rng(17)
+    N0, N1 = shape
+    cfg, _ = W.homogeneous_relaxation_1d(n_cells=N1, ppc=4, precision=mcpm.FP32)
+    cfg.n_cells[0] = N0
+    cfg.length[0] = N0 * d if N0 > 1 else 1.0
+    cfg.length[1] = N1 * d
+    cfg.direction[0] = 1 if N0 > 1 else 0
+    x2 = _face_positions(N1, d, cfg.length[1], rng, 40 * N0 * N1)
+    n = len(x2)
+    x1 = (_face_positions(N0, d, cfg.length[0], rng, n)[:n] if N0 > 1 else rng.random(n))
+    x1 = np.resize(x1, n)
+    U = [rng.normal(0.0, 1.0, n).astype(np.float32).astype(np.float64) for _ in range(3)]
+    parts = dict(x1=x1, x2=x2, U1=U[0], U2=U[1], U3=U[2])
+    mcpm.derive(cfg, n)
+    cfg.max_particles = n
+    s, o = _pair(cfg, parts, step=3)
+    o.cell_update()
+    s.cell_update()
+    idx = s.get_index()
+    assert np.array_equal(idx, o.s.index), np.count_nonzero(idx != o.s.index)
+    # the faces of unit cells are floats: some particles took the jitter branch
+    if d == 1.0:
+        on = (x2 == np.floor(x2)) & (x2 > 1.0) & (x2 < N1 - 1)
+        assert on.sum() > 10
+        assert np.any(o.s.index[on] == x2[on].astype(np.int64) - 1)
+    s.step(1)
+    g = s.download()
+    o2 = Oracle(cfg, g)
+    o2.set_step(s.step_count)
+    o2.cell_update()
+    assert np.array_equal(s.get_index(), o2.s.index)
+
+
 def test_binning_edges_and_out_of_box(cuda_ok):
     """Particles on the far wall bin into the last cell; a particle outside
     the box raises MCPM_ERR_OUT_OF_BOX (the reference exits)."""

@@ -43,6 +43,7 @@ def test_noalloc_matches_session_force(cuda_ok):
         rc = lib.mcpm_poisson_force_1d_noalloc(C.c_void_p(d_n.data_ptr()), cfg.n_cells[1], C.byref(cfg),
                                                C.c_void_p(d_F.data_ptr()), None)
         assert rc == mcpm.OK
+        torch.cuda.synchronize()  # the call queues its work without waiting
         F2 = d_F.cpu().numpy()
         scale = np.max(np.abs(F2_ref))
         assert np.max(np.abs(F2 - F2_ref)) <= 1e-12 * scale, "call %d" % call
