@@ -140,6 +140,29 @@ def aggregate_ranks(ms_local, particles_local, steps, dist=None):
     return ms_max, float(n.item()) * steps / (ms_max / 1e3)
 
 
+def host_link_rates(stream, n_doubles):
+    """The bare host<->device copy rate on this machine for the bytes one e2e
+    step moves each way: copy-engine cudaMemcpyAsync of n_doubles doubles
+    between pinned host memory and the device (GB/s, CUDA events)."""
+    import torch
+    h = torch.empty(n_doubles, dtype=torch.float64, pin_memory=True)
+    d = torch.empty(n_doubles, dtype=torch.float64, device="cuda")
+    out = {}
+    for name, f in (("h2d_GBs", lambda: d.copy_(h, non_blocking=True)),
+                    ("d2h_GBs", lambda: h.copy_(d, non_blocking=True))):
+        f()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(3):
+            f()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        out[name] = round(3 * 8 * n_doubles / (e0.elapsed_time(e1) / 1e3) / 1e9, 1)
+    del h, d
+    return out
+
+
 def build_workload(args):
     import mcpm
     import workloads as W
@@ -218,13 +241,49 @@ def _rel(a, b):
     return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
 
 
+def _field_errors(c, ref, n0, n1, blocks_of=(8, 32)):
+    """Errors of the cell fields c against ref ([CF][C] as mcpm_get_cells
+    returns them): relative L2 over cells of n and T; P_ij as the relative
+    Frobenius norm over cells; the heat flux q_i against its thermal scale
+    (rms over cells of (3 kT/m)^(3/2)); and n, T averaged over blocks of
+    b x b cells (count-weighted T), where the per-cell sampling noise of two
+    runs that no longer share trajectories averages out (about
+    sqrt(2 / particles per block) for two independent runs)."""
+    import numpy as np
+
+    import mcpm
+    F = mcpm.CF
+    n, nr = c[F["N"]], ref[F["N"]]
+    T, Tr = c[F["T"]], ref[F["T"]]
+    P, Pr = c[F["PIJ"]:F["PIJ"] + 6], ref[F["PIJ"]:F["PIJ"] + 6]
+    q, qr = c[F["Q"]:F["Q"] + 3], ref[F["Q"]:F["Q"] + 3]
+    th = np.sqrt(np.mean(np.maximum(ref[F["DM2"]], 0.0) ** 3))
+    cnt, cntr = c[F["NUM_INSIDE"]], ref[F["NUM_INSIDE"]]
+
+    def blocks(v, w, b):
+        s = (v * w).reshape(n1 // b, b, n0 // b, b).sum(axis=(1, 3))
+        return s / np.maximum(w.reshape(n1 // b, b, n0 // b, b).sum(axis=(1, 3)), 1e-300)
+
+    ones = np.ones_like(n)
+    out = {"n_rel_l2": _rel(n, nr), "T_rel_l2": _rel(T, Tr), "P_rel_fro": _rel(P, Pr),
+           "q_rel_thermal": float(np.linalg.norm(q - qr) / (th * np.sqrt(q.size)))}
+    for b in blocks_of:
+        if n0 % b == 0 and n1 % b == 0:
+            out["n_rel_l2_%dx%d" % (b, b)] = _rel(blocks(n, ones, b), blocks(nr, ones, b))
+            out["T_rel_l2_%dx%d" % (b, b)] = _rel(blocks(T, cnt, b), blocks(Tr, cntr, b))
+    return out
+
+
 def surrogate_comparison(args, cfg, parts, s, stream):
     """The plain path on the same workload (FP32 and FP64 particle-steps/s),
-    and the errors of the surrogate run against the FP64 plain run after the
-    same number of steps from the same state: cell density n and temperature
-    T (relative L2 over cells), and the kick field of the last state (network
-    against plain path, relative L2 over the four kick coefficients of every
-    cell)."""
+    and the accuracy of the FP32 + network run against the FP64 plain run
+    (the FP64 GPU step, parity-tested against the FP64 oracle) from the same
+    state with the same draws, at checkpoints up to the workload's 2,000
+    steps: cell density n, temperature T, pressure tensor P_ij and heat flux
+    q_i (_field_errors), and the kick field of the network against the
+    plain path's on the FP32 run's state.  The FP32 plain run is carried
+    beside it, which separates what the network adds from what FP32 state
+    adds."""
     import torch
 
     import mcpm
@@ -252,37 +311,99 @@ def surrogate_comparison(args, cfg, parts, s, stream):
     s64.upload(parts["x1"], parts["x2"], parts["U1"], parts["U2"], parts["U3"])
     s64.set_wcap(min(s.wcap, 384))
     plain64 = timed(s64, max(5, k // 3))
-    # accuracy: the same start, the same number of steps
-    n_acc = 20
-    s64.upload(parts["x1"], parts["x2"], parts["U1"], parts["U2"], parts["U3"])
-    s.upload(parts["x1"], parts["x2"], parts["U1"], parts["U2"], parts["U3"])
+    # accuracy over the horizon: four runs from the same state -- FP64
+    # plain, FP32 + network and FP32 plain with the same draws, and FP32
+    # plain with other draws (another Philox seed): the floor that the
+    # sampling noise of two independent realisations sets
+    sp = mcpm.Session(cfg)
+    sp.set_stream(stream.cuda_stream)
+    sp.set_wcap(s.wcap)
+    cfg_o = cfg.copy()
+    cfg_o.seed = cfg.seed ^ 0x5EED
+    so = mcpm.Session(cfg_o)
+    so.set_stream(stream.cuda_stream)
+    so.set_wcap(s.wcap)
+    for x in (s64, s, sp, so):
+        x.upload(parts["x1"], parts["x2"], parts["U1"], parts["U2"], parts["U3"])
     sur = SG.attach(s, judge_every=10, threshold=0.01)
-    s64.step(n_acc)
-    s.step(n_acc)
-    s64.cell_update()
-    s.cell_update()
-    c64, c32 = s64.get_cells(), s.get_cells()
-    err_n = _rel(c32[mcpm.CF["N"]], c64[mcpm.CF["N"]])
-    err_T = _rel(c32[mcpm.CF["T"]], c64[mcpm.CF["T"]])
-    s.eval_vlasov_2d(0)
-    kp = s.get_kick_2d()
-    s.eval_vlasov_2d(1)
-    kn = s.get_kick_2d()
-    err_F = _rel(kn, kp)
+    n0, n1 = cfg.n_cells[0], cfg.n_cells[1]
+    checkpoints, done, acc = [c for c in (20, 200, 1000, 2000) if c <= args.horizon], 0, []
+    t0 = time.perf_counter()
+    for cp in checkpoints:
+        for x in (s64, s, sp, so):
+            x.step(cp - done)
+        done = cp
+        for x in (s64, s, sp, so):
+            x.cell_update()
+        c64, c32, cp32, co32 = s64.get_cells(), s.get_cells(), sp.get_cells(), so.get_cells()
+        s.eval_vlasov_2d(0)
+        kp = s.get_kick_2d()
+        s.eval_vlasov_2d(1)
+        kn = s.get_kick_2d()
+        e = _field_errors(c32, c64, n0, n1)
+        e["force_rel_l2"] = _rel(kn, kp)
+        acc.append({"step": cp, "surrogate_fp32": e, "plain_fp32": _field_errors(cp32, c64, n0, n1),
+                    "plain_fp32_other_draws": _field_errors(co32, c64, n0, n1)})
+    acc_s = time.perf_counter() - t0
     st2 = s.surrogate_stats()
     s64.close()
+    sp.close()
+    so.close()
     sur_info = SG.load()[2]
     return {
         "plain": {"fp32_value": plain32, "fp64_value": plain64, "unit": UNIT,
                   "steps_timed": [k, max(5, k // 3)],
                   "note": "the same workload with the plain screened-Poisson FEM force every step"},
-        "accuracy": {"steps": n_acc, "against": "FP64 plain GPU step (parity-tested against the FP64 oracle)",
-                     "n_rel_l2": err_n, "T_rel_l2": err_T, "force_rel_l2": err_F,
-                     "judge_last_error": st2["last_error"]},
+        "accuracy": {"against": "FP64 plain GPU step from the same state with the same draws (parity-tested "
+                                "against the FP64 oracle)", "checkpoints": acc,
+                     "judge": {k2: st2[k2] for k2 in ("last_error", "judged", "takeovers")},
+                     "wall_s": round(acc_s, 1)},
         "surrogate": {"judge_every": 10, "threshold": 0.01, "timed_run": stats,
                       "trained_on": {kk: sur_info.get(kk) for kk in ("n_snap", "epochs", "batch", "steps",
                                                                     "val_kick_error", "train_s", "gen_s")}},
     }
+
+
+def side_workloads(args, stream, steps=20):
+    """The survey's other configurations timed the same way (device-resident,
+    CUDA events on the launch stream, after 3 warm-up steps), each in its
+    own session: the uneven 16M box (config 4; threads-per-cell autotuned),
+    the 2-D ESMC box (config 3) and the 1-D Vlasov slab (config 2, FP32 and
+    FP64).  Returns {workload: {value, ms_per_step, particles, ...}}."""
+    import torch
+
+    import mcpm
+    out = {}
+    runs = [("uneven16m", mcpm.FP32), ("esmc6m", mcpm.FP32), ("slab1m", mcpm.FP32), ("slab1m", mcpm.FP64)]
+    for name, prec in runs:
+        a = argparse.Namespace(**vars(args))
+        a.workload = name
+        cfg, parts, desc = build_workload(a)
+        cfg.precision = prec
+        N = len(parts["x2"])
+        s = mcpm.Session(cfg)
+        s.set_stream(stream.cuda_stream)
+        s.upload(parts["x1"], parts["x2"], parts["U1"], parts["U2"], parts["U3"])
+        del parts
+        if cfg.model == mcpm.MODEL_ESMC:
+            s.cell_update()
+            s.init_omega_max()
+        wcap = s.autotune(3) if name == "uneven16m" else s.wcap
+        s.step(3)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        s.step(steps)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+        s.check_status()
+        s.close()
+        key = name + ("_fp64" if prec == mcpm.FP64 else "")
+        out[key] = {"value": N / (ms / 1e3), "unit": UNIT, "ms_per_step": round(ms, 4), "steps": steps,
+                    "particles": N, "precision": "fp64" if prec == mcpm.FP64 else "fp32", "wcap": wcap,
+                    "workload": desc["workload"]}
+    return out
 
 
 def cpu_baseline_sample(args, seconds=12.0):
@@ -423,12 +544,16 @@ def run_mcpm(args):
     torch.cuda.synchronize()
     e2e_ms = (time.perf_counter() - t0) * 1e3 / e2e_steps
     e2e = {"value": N * ws / (e2e_ms / 1e3), "unit": UNIT, "h2d_bytes_per_step": 5 * 8 * N,
-           "d2h_bytes_per_step": 5 * 8 * N, "ms_per_step": round(e2e_ms, 3)}
+           "d2h_bytes_per_step": 5 * 8 * N, "ms_per_step": round(e2e_ms, 3),
+           "host_link": host_link_rates(stream, 5 * N)}
     ok = bool(np.all(np.isfinite(hout["U1"])))
     extra = {}
     if sur is not None:
         extra = surrogate_comparison(args, cfg, parts, s, stream)
     s.close()
+    del parts
+    if ws == 1 and not args.no_side and args.workload == "surrogate16m":
+        extra["side_workloads"] = side_workloads(args, stream)
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -605,6 +730,9 @@ def main():
     ap.add_argument("--workload", default="surrogate16m",
                     choices=["surrogate16m", "uneven16m", "esmc6m", "slab1m", "vlasov16m"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--horizon", type=int, default=2000,
+                    help="last accuracy checkpoint of the learned-force workload (steps)")
+    ap.add_argument("--no-side", action="store_true", help="skip the side workloads (configs 2-4)")
     ap.add_argument("--profile-case", choices=["uneven", "esmc", "slab", "vlasov", "surrogate"],
                     help="run a small case of a workload for an ncu capture and exit (no JSON line)")
     ap.add_argument("--cells", type=int, default=160, help="grid size n of --profile-case")
