@@ -225,15 +225,34 @@ int mcpm_check_status(mcpm_session* s);
    the device and bins them (cell_update's binning, which also reports
    particles outside the box); the device copy is sorted by cell at the
    first cell_update or step.  x1 may be NULL when direction[0] == 0.
-   Resets the step counter to 0. */
+   Resets the step counter to 0.  Returns once the caller's arrays have been
+   read; the copies run on a stream of their own and overlap the copies of
+   a download still in flight (mcpm_download_particles_async). */
 int mcpm_upload_particles(mcpm_session* s, int64_t n, const double* x1,
                           const double* x2, const double* U1, const double* U2,
                           const double* U3);
+/* The same without waiting for the copies: the caller's arrays must stay
+   unchanged until mcpm_sync returns.  With pinned host arrays the copies
+   run while the session's earlier work (steps, a download's copies) is
+   still in flight. */
+int mcpm_upload_particles_async(mcpm_session* s, int64_t n, const double* x1,
+                                const double* x2, const double* U1,
+                                const double* U2, const double* U3);
 /* Copies the device state back into caller arrays, in particle-id order.
    When x1 never changes (direction[0] == 0 and not ESMC) the device does not
    keep it and the caller's x1 is left untouched. */
 int mcpm_download_particles(mcpm_session* s, int64_t n, double* x1, double* x2,
                             double* U1, double* U2, double* U3);
+/* The same without waiting: the conversions are queued on the session's
+   stream and the copies on a stream of their own; the caller's arrays are
+   written once mcpm_sync returns (or a later synchronous download).  The
+   state may be stepped or replaced by an upload meanwhile: the copies read
+   a staging buffer, not the state.  With pinned host arrays the copies of a
+   download overlap those of the next upload (the host link carries both
+   directions at once). */
+int mcpm_download_particles_async(mcpm_session* s, int64_t n, double* x1,
+                                  double* x2, double* U1, double* U2,
+                                  double* U3);
 
 /* cell_update (src/Main_Functions.cpp:2138-2749): binning, per-cell moments,
    Lambda, alpha/beta (FP_dense, step > 0), c/gamma, phi. */

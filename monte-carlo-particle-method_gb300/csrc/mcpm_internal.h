@@ -174,6 +174,13 @@ struct Session {
   // runs on a stream of its own, beside the moment pass and the solves
   cudaStream_t side = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  // host transfers: uploads copy into stage_in on h2d, downloads copy out of
+  // stage on d2h, so that a download's copies overlap the next upload's
+  // (the host link runs both directions at once); the events order the
+  // staging buffers' reuse and each field's conversion against its copy
+  double* stage_in = nullptr;   // [5][cap] upload staging (double)
+  cudaStream_t h2d = nullptr, d2h = nullptr;
+  cudaEvent_t ev_in_free = nullptr, ev_out_free = nullptr, ev_up[5] = {}, ev_dn[5] = {};
   int step = 0;
   int bc_calls = 0;             // apply_BC calls in the current step (split mode)
   int rng_mode = MCPM_RNG_PHILOX;
@@ -254,8 +261,6 @@ int lr2d_num_nodes(const Session& s);
 // the device step number made equal to s.step (a one-thread kernel when it
 // differs); returns the launches it made
 int sync_dstep(Session& s);
-int launch_convert_in(Session& s, int64_t n);
-int launch_convert_out(Session& s, int64_t n);
 // one staged upload field (0..4: x1 x2 U1 U2 U3; field 2 also sets the ids)
 // on stream st
 int launch_convert_field(Session& s, int field, int64_t n, cudaStream_t st);
@@ -263,6 +268,5 @@ int launch_convert_field(Session& s, int field, int64_t n, cudaStream_t st);
 // current layout (packed or slotted)
 int launch_convert_out_field(Session& s, int field, int64_t n);
 // the staging of a download straight from a slotted layout (FP32 sessions)
-int launch_convert_out_slotted(Session& s);
 
 }  // namespace mcpm

@@ -1985,19 +1985,6 @@ __global__ void __launch_bounds__(256, sizeof(real) == 4 ? (CST ? (SL ? MCPM_UPD
 constexpr uint32_t ST_FUSED_FP = ST_RNG | ST_FP | ST_DFP | ST_BC1 | ST_STREAM | ST_BC2 | ST_BC3 | ST_KEY;
 
 // ========================================================= host<->device
-template <typename real>
-__global__ void k_convert_in(PT<real> p, const double* stage, int64_t n, int64_t cap) {
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    if (p.x1) p.x1[i] = (real)stage[i];
-    p.x2[i] = (real)stage[cap + i];
-    p.U1[i] = (real)stage[2 * cap + i];
-    p.U2[i] = (real)stage[3 * cap + i];
-    p.U3[i] = (real)stage[4 * cap + i];
-    p.pid[i] = (int32_t)i;
-    if (p.x1o) p.x1o[i] = p.x1 ? p.x1[i] : (real)0;
-    if (p.x2o) p.x2o[i] = p.x2[i];
-  }
-}
 // one staged field into the state's precision (uploads: each field's
 // conversion overlaps the copy of the next), and the particle ids
 template <typename real>
@@ -2007,22 +1994,6 @@ __global__ void k_convert_field(real* dst, const double* src, int32_t* pid, int6
     if (pid) pid[i] = (int32_t)i;
   }
 }
-template <typename real>
-__global__ void k_convert_out(PT<real> p, double* stage, int64_t n, int64_t cap) {
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    int q = p.pid[i];
-    stage[q] = p.x1 ? (double)p.x1[i] : 0.0;
-    stage[cap + q] = (double)p.x2[i];
-    stage[2 * cap + q] = (double)p.U1[i];
-    stage[3 * cap + q] = (double)p.U2[i];
-    stage[4 * cap + q] = (double)p.U3[i];
-  }
-}
-
-// One field of a download (0..4: x1 x2 U1 U2 U3) into particle-id order,
-// from a packed layout or -- with dcur -- from a slotted one (each cell's
-// filled slots, then the overflow entries); downloads convert one field
-// while the previous one is copied to the host.
 template <typename real>
 __global__ void k_convert_out_field(PT<real> p, PT<real> ovf, const int32_t* ovf_n, const int32_t* off,
                                     const int32_t* dcur, int C, int f, double* dst, int64_t n) {
@@ -2045,30 +2016,6 @@ __global__ void k_convert_out_field(PT<real> p, PT<real> ovf, const int32_t* ovf
   for (int64_t e = tid; e < n_ovf; e += nt) dst[ovf.pid[e]] = (double)w[e];
 }
 
-// The same from a slotted layout as the particle pass left it: each cell's
-// first min(slots taken, capacity) particles of its region (bases off, the
-// counts still in the slot counters), then the overflow entries; the layout
-// itself stays as it is.
-template <typename real>
-__global__ void k_convert_out_slotted(PT<real> p, PT<real> ovf, const int32_t* ovf_n, const int32_t* off,
-                                      const int32_t* dcur, int C, double* stage, int64_t cap) {
-  const int lane = threadIdx.x & 31;
-  const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x, nt = (int64_t)gridDim.x * blockDim.x;
-  auto put = [&](const PT<real>& src, int64_t i) {
-    const int q = src.pid[i];
-    stage[q] = src.x1 ? (double)src.x1[i] : 0.0;
-    stage[cap + q] = (double)src.x2[i];
-    stage[2 * cap + q] = (double)src.U1[i];
-    stage[3 * cap + q] = (double)src.U2[i];
-    stage[4 * cap + q] = (double)src.U3[i];
-  };
-  for (int64_t c = tid >> 5; c < C; c += nt >> 5) {
-    const int s0 = off[c], m = min(dcur[c], off[c + 1] - s0);
-    for (int i = lane; i < m; i += 32) put(p, (int64_t)s0 + i);
-  }
-  const int n_ovf = *ovf_n;
-  for (int64_t e = tid; e < n_ovf; e += nt) put(ovf, e);
-}
 
 // ============================================================ launchers
 static inline int grid_for(int64_t n, int block, int max_blocks) {
@@ -2248,22 +2195,12 @@ int launch_update(Session& s, uint32_t stages, int bc_call_base, bool slotted) {
                              : update_impl<double>(s, stages, bc_call_base, false);
 }
 
-template <typename real> static int conv_in_impl(Session& s, int64_t n) {
-  k_convert_in<real><<<grid_for(n, 256, s.num_sms * 8), 256, 0, s.stream>>>(pt<real>(s.P[s.cur]), s.stage, n, s.cap);
-  return 1;
-}
-int launch_convert_in(Session& s, int64_t n) { return s.prec == MCPM_FP32 ? conv_in_impl<float>(s, n) : conv_in_impl<double>(s, n); }
-template <typename real> static int conv_out_impl(Session& s, int64_t n) {
-  k_convert_out<real><<<grid_for(n, 256, s.num_sms * 8), 256, 0, s.stream>>>(pt<real>(s.P[s.cur]), s.stage, n, s.cap);
-  return 1;
-}
-int launch_convert_out(Session& s, int64_t n) { return s.prec == MCPM_FP32 ? conv_out_impl<float>(s, n) : conv_out_impl<double>(s, n); }
 template <typename real> static int conv_field_impl(Session& s, int f, int64_t n, cudaStream_t st) {
   const PBuf& b = s.P[s.cur];
   void* dsts[5] = {b.x1, b.x2, b.U1, b.U2, b.U3};
   if (!dsts[f]) return 0;
   k_convert_field<real><<<grid_for(n, 256, s.num_sms * 8), 256, 0, st>>>(
-      (real*)dsts[f], s.stage + (size_t)f * s.cap, f == 2 ? b.pid : nullptr, n);
+      (real*)dsts[f], s.stage_in + (size_t)f * s.cap, f == 2 ? b.pid : nullptr, n);
   return 1;
 }
 int launch_convert_field(Session& s, int field, int64_t n, cudaStream_t st) {
@@ -2279,12 +2216,6 @@ template <typename real> static int conv_out_field_impl(Session& s, int f, int64
 int launch_convert_out_field(Session& s, int field, int64_t n) {
   return s.prec == MCPM_FP32 ? conv_out_field_impl<float>(s, field, n) : conv_out_field_impl<double>(s, field, n);
 }
-int launch_convert_out_slotted(Session& s) {
-  k_convert_out_slotted<float><<<s.num_sms * 8, 256, 0, s.stream>>>(
-      pt<float>(s.P[s.cur]), pt<float>(s.ovf), s.ovf_n + (1 - s.ovf_par), s.off, s.dcur, s.C, s.stage, s.cap);
-  return 1;
-}
-
 // the dynamic shared memory the update kernel needs, for the session setup
 size_t update_smem_bytes(const Session& s) {
   return s.prec == MCPM_FP32 ? update_smem<float>(s) : update_smem<double>(s);

@@ -249,6 +249,14 @@ int mcpm_session_create(const mcpm_config* cfg, mcpm_session** out) {
   if ((rc = cuda_check(s, cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking), "stream"))) { delete s; return rc; }
   cudaEventCreateWithFlags(&s->ev_fork, cudaEventDisableTiming);
   cudaEventCreateWithFlags(&s->ev_join, cudaEventDisableTiming);
+  if ((rc = cuda_check(s, cudaStreamCreateWithFlags(&s->h2d, cudaStreamNonBlocking), "stream"))) { mcpm_session_destroy(s); return rc; }
+  if ((rc = cuda_check(s, cudaStreamCreateWithFlags(&s->d2h, cudaStreamNonBlocking), "stream"))) { mcpm_session_destroy(s); return rc; }
+  cudaEventCreateWithFlags(&s->ev_in_free, cudaEventDisableTiming);
+  cudaEventCreateWithFlags(&s->ev_out_free, cudaEventDisableTiming);
+  for (int f = 0; f < 5; ++f) {
+    cudaEventCreateWithFlags(&s->ev_up[f], cudaEventDisableTiming);
+    cudaEventCreateWithFlags(&s->ev_dn[f], cudaEventDisableTiming);
+  }
 
   // tuning defaults (see mcpm_tune in the Python layer for the sweep)
   s->tune.bcap = (s->prec == MCPM_FP32) ? MCPM_UPD_BCAP : 3072;
@@ -286,7 +294,7 @@ int mcpm_session_create(const mcpm_config* cfg, mcpm_session** out) {
        A((void**)&s->list_big, C * 4) && A((void**)&s->wl, WL_COUNT * 4) && A((void**)&s->work, WK_COUNT * 4) &&
        A((void**)&s->scan_blk, 8 * (C / 1024 + 2) * 4) &&
        A((void**)&s->cell, (size_t)CF_DEV_COUNT * C * 8) && A((void**)&s->pcell, (size_t)PF_STRIDE * C * 4) && A((void**)&s->xi, 3 * cap * 8) &&
-       A((void**)&s->inj, 3 * cap * 8) && A((void**)&s->stage, 5 * cap * 8) &&
+       A((void**)&s->inj, 3 * cap * 8) && A((void**)&s->stage, 5 * cap * 8) && A((void**)&s->stage_in, 5 * cap * 8) &&
        A((void**)&s->faces, ((size_t)k.N1 + 1 + 5000) * 8) && A((void**)&s->status, 16) &&
        A((void**)&s->dstep, 16) && A((void**)&s->bin_faces, ((size_t)k.N0 + k.N1 + 4) * 4);
   if (!ok) {
@@ -365,8 +373,17 @@ int mcpm_session_destroy(mcpm_session* s) {
   for (auto e : s->prof_pool) cudaEventDestroy(e);
   if (s->own_stream) cudaStreamDestroy(s->own_stream);
   if (s->side) { cudaStreamSynchronize(s->side); cudaStreamDestroy(s->side); }
+  if (s->h2d) { cudaStreamSynchronize(s->h2d); cudaStreamDestroy(s->h2d); }
+  if (s->d2h) { cudaStreamSynchronize(s->d2h); cudaStreamDestroy(s->d2h); }
   if (s->ev_fork) cudaEventDestroy(s->ev_fork);
   if (s->ev_join) cudaEventDestroy(s->ev_join);
+  if (s->ev_in_free) cudaEventDestroy(s->ev_in_free);
+  if (s->ev_out_free) cudaEventDestroy(s->ev_out_free);
+  for (int f = 0; f < 5; ++f) {
+    if (s->ev_up[f]) cudaEventDestroy(s->ev_up[f]);
+    if (s->ev_dn[f]) cudaEventDestroy(s->ev_dn[f]);
+  }
+  cudaFree(s->stage_in);
   delete s;
   return MCPM_OK;
 }
@@ -375,7 +392,10 @@ const char* mcpm_last_error(const mcpm_session* s) { return s ? s->err.c_str() :
 
 int mcpm_sync(mcpm_session* s) {
   if (!s) return MCPM_ERR_ARG;
-  return cuda_check(s, cudaStreamSynchronize(s->stream), "sync");
+  int rc = cuda_check(s, cudaStreamSynchronize(s->stream), "sync");
+  if (!rc && s->d2h) rc = cuda_check(s, cudaStreamSynchronize(s->d2h), "sync (downloads)");
+  if (!rc && s->h2d) rc = cuda_check(s, cudaStreamSynchronize(s->h2d), "sync (uploads)");
+  return rc;
 }
 
 int mcpm_check_status(mcpm_session* s) {
@@ -418,7 +438,8 @@ static int sort_by_cell(mcpm_session* s) {
   return after_launch(s, n, "sort_by_cell");
 }
 
-int mcpm_upload_particles(mcpm_session* s, int64_t n, const double* x1, const double* x2, const double* U1,
+// the upload's copies, conversions and binning, without waiting for them
+static int upload_enqueue(mcpm_session* s, int64_t n, const double* x1, const double* x2, const double* U1,
                           const double* U2, const double* U3) {
   if (!s || n < 0 || n > s->cap || !x2 || !U1 || !U2 || !U3) return fail(s, MCPM_ERR_ARG, "upload: bad arguments");
   if (!x1 && s->need_x1) return fail(s, MCPM_ERR_ARG, "upload: x1 required for this configuration");
@@ -428,26 +449,22 @@ int mcpm_upload_particles(mcpm_session* s, int64_t n, const double* x1, const do
   s->cur = 0;
   int k = 0;
   const double* src[5] = {x1, x2, U1, U2, U3};
-  if (s->need_old || !s->side) {
-    for (int f = 0; f < 5; ++f) {
-      if (src[f]) cudaMemcpyAsync(s->stage + f * cap, src[f], b, cudaMemcpyHostToDevice, st);
-      else cudaMemsetAsync(s->stage + f * cap, 0, b, st);
-    }
-    k = launch_convert_in(*s, n);
-  } else {
-    // each field converted on the side stream while the next one is copied
-    cudaEventRecord(s->ev_fork, st);
-    cudaStreamWaitEvent(s->side, s->ev_fork, 0);
-    for (int f = 0; f < 5; ++f) {
-      if (src[f]) cudaMemcpyAsync(s->stage + f * cap, src[f], b, cudaMemcpyHostToDevice, st);
-      else cudaMemsetAsync(s->stage + f * cap, 0, b, st);
-      cudaEventRecord(s->ev_fork, st);
-      cudaStreamWaitEvent(s->side, s->ev_fork, 0);
-      k += launch_convert_field(*s, f, n, s->side);
-    }
-    cudaEventRecord(s->ev_join, s->side);
-    cudaStreamWaitEvent(st, s->ev_join, 0);
+  // each field is copied into the upload staging on the h2d stream (after
+  // the previous upload's conversions have read it) and converted on the
+  // session stream while the next one is copied; a pending download's
+  // copies run meanwhile on the d2h stream
+  cudaStreamWaitEvent(s->h2d, s->ev_in_free, 0);
+  for (int f = 0; f < 5; ++f) {
+    if (src[f]) cudaMemcpyAsync(s->stage_in + f * cap, src[f], b, cudaMemcpyHostToDevice, s->h2d);
+    else cudaMemsetAsync(s->stage_in + f * cap, 0, b, s->h2d);
+    cudaEventRecord(s->ev_up[f], s->h2d);
+    cudaStreamWaitEvent(st, s->ev_up[f], 0);
+    k += launch_convert_field(*s, f, n, st);
   }
+  cudaEventRecord(s->ev_in_free, st);
+  const PBuf& P = s->P[0];
+  if (P.x1o && P.x1) cudaMemcpyAsync(P.x1o, P.x1, (size_t)n * s->rsz, cudaMemcpyDeviceToDevice, st);
+  if (P.x2o) cudaMemcpyAsync(P.x2o, P.x2, (size_t)n * s->rsz, cudaMemcpyDeviceToDevice, st);
   int rc = after_launch(s, k, "upload");
   if (rc) return rc;
   s->step = 0;
@@ -464,36 +481,54 @@ int mcpm_upload_particles(mcpm_session* s, int64_t n, const double* x1, const do
   return rc;
 }
 
-int mcpm_download_particles(mcpm_session* s, int64_t n, double* x1, double* x2, double* U1, double* U2, double* U3) {
+int mcpm_upload_particles(mcpm_session* s, int64_t n, const double* x1, const double* x2, const double* U1,
+                          const double* U2, const double* U3) {
+  const int rc = upload_enqueue(s, n, x1, x2, U1, U2, U3);
+  if (rc) return rc;
+  // the caller may reuse its arrays once this returns: wait for the copies
+  // (not for the conversions, nor for a pending download)
+  return cuda_check(s, cudaEventSynchronize(s->ev_up[4]), "upload copies");
+}
+
+int mcpm_upload_particles_async(mcpm_session* s, int64_t n, const double* x1, const double* x2, const double* U1,
+                                const double* U2, const double* U3) {
+  return upload_enqueue(s, n, x1, x2, U1, U2, U3);
+}
+
+// the download's conversions and copies, without waiting for them
+static int download_enqueue(mcpm_session* s, int64_t n, double* x1, double* x2, double* U1, double* U2, double* U3) {
   if (!s || n != s->N || !x2 || !U1 || !U2 || !U3) return fail(s, MCPM_ERR_ARG, "download: bad arguments");
   const size_t cap = (size_t)s->cap, b = (size_t)n * 8;
   cudaStream_t st = s->stream;
   // a slotted layout is staged as it lies (and stays slotted for the next
-  // step); each field is converted while the previous one is copied out
+  // step); each field is converted on the session stream, once the previous
+  // download's copies have left the staging, and copied out on the d2h
+  // stream while the next one is converted.  x1 is not tracked when it never
+  // changes (no x streaming, no ESMC): the caller's array is left as it is,
+  // like the reference's x1
   double* dsts[5] = {(x1 && s->need_x1) ? x1 : nullptr, x2, U1, U2, U3};
-  if (s->side) {
-    int k = 0;
-    for (int f = 0; f < 5; ++f) {
-      if (!dsts[f]) continue;
-      k += launch_convert_out_field(*s, f, n);
-      cudaEventRecord(s->ev_fork, st);
-      cudaStreamWaitEvent(s->side, s->ev_fork, 0);
-      cudaMemcpyAsync(dsts[f], s->stage + (size_t)f * cap, b, cudaMemcpyDeviceToHost, s->side);
-    }
-    int rc = after_launch(s, k, "download");
-    if (rc) return rc;
-    cudaEventRecord(s->ev_join, s->side);
-    cudaStreamWaitEvent(st, s->ev_join, 0);
-    return cuda_check(s, cudaStreamSynchronize(st), "download");
+  cudaStreamWaitEvent(st, s->ev_out_free, 0);
+  int k = 0;
+  for (int f = 0; f < 5; ++f) {
+    if (!dsts[f]) continue;
+    k += launch_convert_out_field(*s, f, n);
+    cudaEventRecord(s->ev_dn[f], st);
+    cudaStreamWaitEvent(s->d2h, s->ev_dn[f], 0);
+    cudaMemcpyAsync(dsts[f], s->stage + (size_t)f * cap, b, cudaMemcpyDeviceToHost, s->d2h);
   }
-  int k = s->slotted ? launch_convert_out_slotted(*s) : launch_convert_out(*s, n);
-  int rc = after_launch(s, k, "download");
+  cudaEventRecord(s->ev_out_free, s->d2h);
+  return after_launch(s, k, "download");
+}
+
+int mcpm_download_particles(mcpm_session* s, int64_t n, double* x1, double* x2, double* U1, double* U2, double* U3) {
+  const int rc = download_enqueue(s, n, x1, x2, U1, U2, U3);
   if (rc) return rc;
-  // x1 is not tracked when it never changes (no x streaming, no ESMC):
-  // the caller's array is left as it is, like the reference's x1
-  for (int f = 0; f < 5; ++f)
-    if (dsts[f]) cudaMemcpyAsync(dsts[f], s->stage + (size_t)f * cap, b, cudaMemcpyDeviceToHost, st);
-  return cuda_check(s, cudaStreamSynchronize(st), "download");
+  return cuda_check(s, cudaEventSynchronize(s->ev_out_free), "download");
+}
+
+int mcpm_download_particles_async(mcpm_session* s, int64_t n, double* x1, double* x2, double* U1, double* U2,
+                                  double* U3) {
+  return download_enqueue(s, n, x1, x2, U1, U2, U3);
 }
 
 int mcpm_cell_update(mcpm_session* s) {
@@ -955,6 +990,7 @@ int mcpm_get_index(mcpm_session* s, int32_t* index) {
     if ((rc = sort_by_cell(s))) return rc;
   }
   int32_t* tmp = (int32_t*)s->stage;
+  cudaStreamWaitEvent(s->stream, s->ev_out_free, 0);  // a pending download's copies read the staging
   k_index<<<(int)((s->N + 255) / 256 > 4096 ? 4096 : (s->N + 255) / 256 + 1), 256, 0, s->stream>>>(s->off, s->C, s->P[s->cur].pid, tmp, s->N);
   if ((rc = after_launch(s, 1, "get_index"))) return rc;
   cudaMemcpyAsync(index, tmp, (size_t)s->N * 4, cudaMemcpyDeviceToHost, s->stream);
@@ -966,6 +1002,7 @@ int mcpm_get_normals(mcpm_session* s, double* a, double* b, double* c) {
   int rc0 = leave_slotted(s);
   if (rc0) return rc0;
   const size_t cap = (size_t)s->cap;
+  cudaStreamWaitEvent(s->stream, s->ev_out_free, 0);  // a pending download's copies read the staging
   k_unpermute3<<<(int)((s->N + 255) / 256 > 4096 ? 4096 : (s->N + 255) / 256 + 1), 256, 0, s->stream>>>(s->xi, s->P[s->cur].pid, s->stage, s->N, s->cap);
   int rc = after_launch(s, 1, "get_normals");
   if (rc) return rc;

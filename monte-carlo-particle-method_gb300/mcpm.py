@@ -156,6 +156,8 @@ def load_library(path: str | None = None):
         "mcpm_check_status": (C.c_int, [vp]),
         "mcpm_upload_particles": (C.c_int, [vp, i64, dp, dp, dp, dp, dp]),
         "mcpm_download_particles": (C.c_int, [vp, i64, dp, dp, dp, dp, dp]),
+        "mcpm_download_particles_async": (C.c_int, [vp, i64, dp, dp, dp, dp, dp]),
+        "mcpm_upload_particles_async": (C.c_int, [vp, i64, dp, dp, dp, dp, dp]),
         "mcpm_cell_update": (C.c_int, [vp]),
         "mcpm_random_generator": (C.c_int, [vp]),
         "mcpm_velocity_update": (C.c_int, [vp]),
@@ -268,12 +270,16 @@ class Session:
         self.close()
 
     # -- particles
-    def upload(self, x1, x2, U1, U2, U3):
+    def upload(self, x1, x2, U1, U2, U3, wait=True):
+        """Copy the caller's arrays to the device; with wait=False the copies
+        are queued (mcpm_upload_particles_async) and the arrays must stay
+        unchanged until sync() returns."""
         n = len(x2)
         self._keep = [_f64(x1, n) if x1 is not None else None, _f64(x2, n), _f64(U1, n), _f64(U2, n), _f64(U3, n)]
         k = self._keep
-        self._ck(self.lib.mcpm_upload_particles(self.h, n, _dp(k[0]) if k[0] is not None else None, _dp(k[1]),
-                                                _dp(k[2]), _dp(k[3]), _dp(k[4])), "upload_particles")
+        fn = self.lib.mcpm_upload_particles if wait else self.lib.mcpm_upload_particles_async
+        self._ck(fn(self.h, n, _dp(k[0]) if k[0] is not None else None, _dp(k[1]), _dp(k[2]), _dp(k[3]), _dp(k[4])),
+                 "upload_particles")
         self.N = n
 
     def download(self):
@@ -433,10 +439,13 @@ class Session:
                  "profile_read")
         return {name: (float(ms[i]), int(n[i])) for i, name in enumerate(K_NAMES)}
 
-    def download_into(self, out):
-        """Download into caller arrays (e.g. pinned host buffers)."""
-        self._ck(self.lib.mcpm_download_particles(self.h, self.N, _dp(out["x1"]), _dp(out["x2"]), _dp(out["U1"]),
-                                                  _dp(out["U2"]), _dp(out["U3"])), "download_particles")
+    def download_into(self, out, wait=True):
+        """Download into caller arrays (e.g. pinned host buffers); with
+        wait=False the copies are queued and the arrays are written once
+        sync() returns (mcpm_download_particles_async)."""
+        fn = self.lib.mcpm_download_particles if wait else self.lib.mcpm_download_particles_async
+        self._ck(fn(self.h, self.N, _dp(out["x1"]), _dp(out["x2"]), _dp(out["U1"]), _dp(out["U2"]), _dp(out["U3"])),
+                 "download_particles")
 
     @property
     def kernel_launches(self):
