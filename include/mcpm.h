@@ -317,6 +317,36 @@ int mcpm_reset_samples(mcpm_session* s);
 int mcpm_get_cells(mcpm_session* s, double* out);
 /* Cell index of every particle, in particle-id order (cell_update's index[]). */
 int mcpm_get_index(mcpm_session* s, int32_t* index);
+
+/* ---- interface problems: thermostat and weighted particles ------------ */
+/* Per-particle weights (the reference's n_ratio[], particle-id order, N
+   values) and per-cell weights (cells[].n_ratio, C values, set by make_cells
+   from the problem's liquid / vapour regions, src/myIO.cpp:1486-1526).  Until
+   set, every particle and cell weighs 1.  The particle weights follow the
+   ids through uploads only by being set again. */
+int mcpm_set_particle_weights(mcpm_session* s, const int32_t* w);
+int mcpm_get_particle_weights(mcpm_session* s, int32_t* w);
+int mcpm_set_cell_weights(mcpm_session* s, const int32_t* w);
+/* thermostat (src/Main_Functions.cpp:1674-1869, the live branch, problem
+   inverted): every cell num < N[1] whose centre lies below thermc is
+   rescaled to temperature Tc and every one above Len[1] - thermh to Th,
+   U <- sqrt(T_target / T) (U - U_space) + U_space, with T and U_space of
+   the last cell_update (cells with T > 0).  Call cell_update first, as the
+   reference's loop does (src/main.cpp:429-436). */
+int mcpm_thermostat(mcpm_session* s, double Tc, double Th, double thermc, double thermh);
+/* inverted_addremove_particles (src/Main_Functions.cpp:1206-1450): against
+   the cells of the last binning, a particle heavier than its cell is split
+   into n_ratio particles (itself and n_ratio - 1 copies with velocities
+   U + h z, z standard normals, h = 1.06 sig (numb_rem + n_ratio)^(-1/5));
+   a lighter one is deleted with probability 1 - 1/n_ratio or takes the
+   cell's weight.  When any particle was split or deleted the state is
+   rebuilt: the kept particles in their id order, then the copies (by the
+   rank of the split particle's id, copy j inner), every weight set to its
+   cell's, N updated (*n_out); the next cell_update or step bins it.  The
+   draws are Philox, keyed by particle id and the session's step number (the
+   reference draws from std::random_device).  MCPM_ERR_CAPACITY when the new
+   N would exceed max_particles (the state is then unchanged). */
+int mcpm_addremove_particles(mcpm_session* s, int32_t n_ratio, int64_t* n_out);
 /* Nodal densities n_n of the last cell_update, [C][4] doubles (cell-major,
    corner 0 lower left, 1 lower right, 2 upper left, 3 upper right), as
    cell_update deposits them (src/Main_Functions.cpp:2268-2364).  Computed

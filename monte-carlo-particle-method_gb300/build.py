@@ -23,7 +23,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "--fmad=false", "-Xcompiler", "-fPIC,-O2",
            "-Xptxas", "-warn-spills", "--expt-relaxed-constexpr"]
 SOURCES = ["mcpm_session.cu", "mcpm_kernels.cu", "mcpm_forces.cu", "mcpm_lr2d.cu", "mcpm_noalloc.cu",
-           "mcpm_surrogate.cu", "mcpm_surrogate_tc.cu", "mcpm_settings.cu"]
+           "mcpm_surrogate.cu", "mcpm_surrogate_tc.cu", "mcpm_settings.cu", "mcpm_dynamic.cu"]
 
 
 def nvcc():

@@ -57,7 +57,7 @@ enum : uint32_t {
 
 // Counter-stream ids for the Philox draws (third counter word).
 enum : uint32_t { RNG_FP = 0, RNG_BC = 1, RNG_ESMC = 2, RNG_BIN = 3, RNG_ESMC_ACC = 4, RNG_ESMC_M = 5,
-                  RNG_DSMC = 6, RNG_DSMC_ACC = 7, RNG_DSMC_M = 8 };
+                  RNG_DSMC = 6, RNG_DSMC_ACC = 7, RNG_DSMC_M = 8, RNG_ADDREM_DEL = 9, RNG_ADDREM_NEW = 10 };
 
 struct DevConsts {
   int N0, N1, C;
@@ -189,6 +189,18 @@ struct Session {
   bool needs_rebin = false;     // positions moved since the last binning
   bool have_particles = false;
   double* samples = nullptr;    // [MCPM_SF_COUNT][C] cell_poly_velocity accumulators
+  // particle weights (the reference's n_ratio[]) in particle-id order, the
+  // cells' weights (cells[].n_ratio), and the split / merge scratch
+  int32_t* pw = nullptr;        // [cap]
+  int32_t* pw_alt = nullptr;    // [cap] the weights in the new id order
+  int32_t* cw = nullptr;        // [C]
+  int8_t* ar_flag = nullptr;    // [cap] per particle id: 1 split, -1 deleted, 2 re-weighted, 0 kept
+  int32_t* ar_ci = nullptr;     // [4][C] split, kept, kept weight, last kept id per cell
+  double* ar_h = nullptr;       // [C] velocity spread of the copies
+  int32_t* ar_newid = nullptr;  // [cap]
+  int32_t* ar_srank = nullptr;  // [cap]
+  int32_t* ar_tiles = nullptr;  // [2][tiles of the scan]
+  unsigned long long* ar_tot = nullptr;  // [2] split, deleted
   bool omega_init = false;      // ESMC / DSMC majorant initialised (src/main.cpp:250-269)
   int num_sms = 0;
   Tuning tune{};
@@ -261,6 +273,15 @@ int lr2d_num_nodes(const Session& s);
 // the device step number made equal to s.step (a one-thread kernel when it
 // differs); returns the launches it made
 int sync_dstep(Session& s);
+// the interface problems (mcpm_dynamic.cu): thermostat, and the split /
+// merge of weighted particles -- flags and counts, then the move into the
+// other buffer in the new id order, or the in-place re-weighting when
+// nothing was split or deleted
+int launch_thermostat(Session& s, double Tc, double Th, double thermc, double thermh);
+int launch_addremove_flags(Session& s, int g, int step);
+int launch_addremove_move(Session& s, int g, int step, int64_t n_kept);
+int launch_addremove_reweight(Session& s);
+int addremove_tiles(int64_t n);
 // one staged upload field (0..4: x1 x2 U1 U2 U3; field 2 also sets the ids)
 // on stream st
 int launch_convert_field(Session& s, int field, int64_t n, cudaStream_t st);

@@ -350,6 +350,8 @@ int mcpm_session_destroy(mcpm_session* s) {
   if (s->stream) cudaStreamSynchronize(s->stream);
   if (s->own_stream && s->own_stream != s->stream) cudaStreamSynchronize(s->own_stream);
   cudaFree(s->samples);
+  cudaFree(s->pw); cudaFree(s->pw_alt); cudaFree(s->cw); cudaFree(s->ar_flag); cudaFree(s->ar_ci); cudaFree(s->ar_h);
+  cudaFree(s->ar_newid); cudaFree(s->ar_srank); cudaFree(s->ar_tiles); cudaFree(s->ar_tot);
   for (int b = 0; b < 2; ++b) {
     PBuf& P = s->P[b];
     cudaFree(P.x1); cudaFree(P.x2); cudaFree(P.U1); cudaFree(P.U2); cudaFree(P.U3); cudaFree(P.pid);
@@ -704,6 +706,7 @@ static uint64_t graph_signature(const mcpm_session* s, uint32_t stages) {
   mix((uint64_t)s->rng_mode);
   mix((uint64_t)(uintptr_t)s->sur);
   mix((uint64_t)s->sur_active);
+  mix((uint64_t)s->N);  // the particle count changes with splits and deletions
   return h;
 }
 
@@ -980,6 +983,101 @@ int mcpm_get_node_potential(mcpm_session* s, double* out) {
   if (!s->lr2d) return fail(s, MCPM_ERR_STATE, "get_node_potential: needs a 2-D long-range session");
   cudaMemcpyAsync(out, lr2d_potential(*s), (size_t)lr2d_num_nodes(*s) * 8, cudaMemcpyDeviceToHost, s->stream);
   return cuda_check(s, cudaStreamSynchronize(s->stream), "get_node_potential");
+}
+
+// ------------------------------------------------ interface problems
+// the weights' arrays and the split / merge scratch, allocated on first use
+static int weights_alloc(mcpm_session* s) {
+  if (s->pw) return MCPM_OK;
+  const size_t cap = (size_t)s->cap, C = (size_t)s->C;
+  auto A = [&](void** p, size_t bytes) { return cudaMalloc(p, bytes ? bytes : 16) == cudaSuccess; };
+  const bool ok = A((void**)&s->pw, cap * 4) && A((void**)&s->pw_alt, cap * 4) && A((void**)&s->cw, C * 4) &&
+                  A((void**)&s->ar_flag, cap) && A((void**)&s->ar_ci, 4 * C * 4) && A((void**)&s->ar_h, C * 8) &&
+                  A((void**)&s->ar_newid, cap * 4) && A((void**)&s->ar_srank, cap * 4) &&
+                  A((void**)&s->ar_tiles, 2 * ((size_t)addremove_tiles(s->cap) + 1) * 4) &&
+                  A((void**)&s->ar_tot, 16);
+  if (!ok) {
+    cudaGetLastError();
+    return fail(s, MCPM_ERR_CUDA, "weights: out of device memory");
+  }
+  // until the caller sets them, every particle and cell weighs 1
+  std::vector<int32_t> one(cap > C ? cap : C, 1);
+  cudaMemcpy(s->pw, one.data(), cap * 4, cudaMemcpyHostToDevice);
+  cudaMemcpy(s->cw, one.data(), C * 4, cudaMemcpyHostToDevice);
+  return cuda_check(s, cudaGetLastError(), "weights");
+}
+
+int mcpm_set_particle_weights(mcpm_session* s, const int32_t* w) {
+  if (!s || !w || !s->have_particles) return fail(s, MCPM_ERR_ARG, "set_particle_weights: no particles");
+  int rc = weights_alloc(s);
+  if (rc) return rc;
+  cudaMemcpyAsync(s->pw, w, (size_t)s->N * 4, cudaMemcpyHostToDevice, s->stream);
+  return cuda_check(s, cudaStreamSynchronize(s->stream), "set_particle_weights");
+}
+
+int mcpm_get_particle_weights(mcpm_session* s, int32_t* w) {
+  if (!s || !w || !s->have_particles) return fail(s, MCPM_ERR_ARG, "get_particle_weights: no particles");
+  int rc = weights_alloc(s);
+  if (rc) return rc;
+  cudaMemcpyAsync(w, s->pw, (size_t)s->N * 4, cudaMemcpyDeviceToHost, s->stream);
+  return cuda_check(s, cudaStreamSynchronize(s->stream), "get_particle_weights");
+}
+
+int mcpm_set_cell_weights(mcpm_session* s, const int32_t* w) {
+  if (!s || !w) return fail(s, MCPM_ERR_ARG, "set_cell_weights: bad arguments");
+  int rc = weights_alloc(s);
+  if (rc) return rc;
+  cudaMemcpyAsync(s->cw, w, (size_t)s->C * 4, cudaMemcpyHostToDevice, s->stream);
+  return cuda_check(s, cudaStreamSynchronize(s->stream), "set_cell_weights");
+}
+
+int mcpm_thermostat(mcpm_session* s, double Tc, double Th, double thermc, double thermh) {
+  if (!s || !s->have_particles) return fail(s, MCPM_ERR_STATE, "thermostat: no particles");
+  int rc;
+  if (s->slotted && (rc = leave_slotted(s))) return rc;
+  if (!s->sorted) return fail(s, MCPM_ERR_STATE, "thermostat: call cell_update first");
+  return after_launch(s, launch_thermostat(*s, Tc, Th, thermc, thermh), "thermostat");
+}
+
+int mcpm_addremove_particles(mcpm_session* s, int32_t n_ratio, int64_t* n_out) {
+  if (!s || !s->have_particles) return fail(s, MCPM_ERR_STATE, "addremove: no particles");
+  if (n_ratio < 1) return fail(s, MCPM_ERR_ARG, "addremove: n_ratio must be >= 1");
+  int rc = weights_alloc(s);
+  if (rc) return rc;
+  // the cells of the last binning (the reference's index[] of its last
+  // cell_update), grouped
+  if (s->slotted) {
+    if ((rc = leave_slotted(s))) return rc;
+  } else if (s->needs_rebin || !s->sorted) {
+    s->needs_rebin = false;
+    s->sorted = false;
+    if ((rc = sort_by_cell(s))) return rc;
+  }
+  if ((rc = after_launch(s, launch_addremove_flags(*s, n_ratio, s->step), "addremove"))) return rc;
+  unsigned long long tot[2] = {0, 0};
+  cudaMemcpyAsync(tot, s->ar_tot, sizeof tot, cudaMemcpyDeviceToHost, s->stream);
+  if ((rc = cuda_check(s, cudaStreamSynchronize(s->stream), "addremove counts"))) return rc;
+  const int64_t n_split = (int64_t)tot[0], n_del = (int64_t)tot[1];
+  if (n_split == 0 && n_del == 0) {
+    // nothing split or deleted: the kept light particles take their cell's weight
+    if ((rc = after_launch(s, launch_addremove_reweight(*s), "addremove"))) return rc;
+    if (n_out) *n_out = s->N;
+    return cuda_check(s, cudaStreamSynchronize(s->stream), "addremove");
+  }
+  const int64_t n_kept = s->N - n_del, n_new = (int64_t)(n_ratio - 1) * n_split;
+  if (n_kept + n_new > s->cap) return fail(s, MCPM_ERR_CAPACITY, "addremove: the new particles exceed max_particles");
+  if ((rc = after_launch(s, launch_addremove_move(*s, n_ratio, s->step, n_kept), "addremove"))) return rc;
+  // the new state sits in the other buffer in the new id order
+  s->cur = 1 - s->cur;
+  s->N = n_kept + n_new;
+  std::swap(s->pw, s->pw_alt);
+  s->sorted = false;
+  s->keys_current = false;
+  s->needs_rebin = false;
+  s->slotted = false;
+  s->rng_mode = MCPM_RNG_PHILOX;  // injected normals were per old particle id
+  if (n_out) *n_out = s->N;
+  return cuda_check(s, cudaStreamSynchronize(s->stream), "addremove");
 }
 
 int mcpm_get_index(mcpm_session* s, int32_t* index) {

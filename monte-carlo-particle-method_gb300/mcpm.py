@@ -174,6 +174,11 @@ def load_library(path: str | None = None):
         "mcpm_get_samples": (C.c_int, [vp, dp]),
         "mcpm_reset_samples": (C.c_int, [vp]),
         "mcpm_get_index": (C.c_int, [vp, ip]),
+        "mcpm_set_particle_weights": (C.c_int, [vp, ip]),
+        "mcpm_get_particle_weights": (C.c_int, [vp, ip]),
+        "mcpm_set_cell_weights": (C.c_int, [vp, ip]),
+        "mcpm_thermostat": (C.c_int, [vp, C.c_double, C.c_double, C.c_double, C.c_double]),
+        "mcpm_addremove_particles": (C.c_int, [vp, i32, C.POINTER(i64)]),
         "mcpm_get_normals": (C.c_int, [vp, dp, dp, dp]),
         "mcpm_get_node_density": (C.c_int, [vp, dp]),
         "mcpm_get_node_potential": (C.c_int, [vp, dp]),
@@ -373,6 +378,38 @@ class Session:
         out = np.empty(self.N, dtype=np.int32)
         self._ck(self.lib.mcpm_get_index(self.h, _ip(out)), "get_index")
         return out
+
+    # -- interface problems (the reference's problem inverted)
+    def set_particle_weights(self, w):
+        """n_ratio[] of the reference, particle-id order."""
+        w = np.ascontiguousarray(w, dtype=np.int32)
+        self._ck(self.lib.mcpm_set_particle_weights(self.h, _ip(w)), "set_particle_weights")
+
+    def get_particle_weights(self):
+        out = np.empty(self.N, dtype=np.int32)
+        self._ck(self.lib.mcpm_get_particle_weights(self.h, _ip(out)), "get_particle_weights")
+        return out
+
+    def set_cell_weights(self, w):
+        """cells[].n_ratio of the reference, cell order."""
+        w = np.ascontiguousarray(w, dtype=np.int32)
+        self._ck(self.lib.mcpm_set_cell_weights(self.h, _ip(w)), "set_cell_weights")
+
+    def thermostat(self, Tc, Th, thermc, thermh):
+        """thermostat (src/Main_Functions.cpp:1674-1869)."""
+        self._ck(self.lib.mcpm_thermostat(self.h, Tc, Th, thermc, thermh), "thermostat")
+
+    def addremove_particles(self, n_ratio):
+        """inverted_addremove_particles (src/Main_Functions.cpp:1206-1450);
+        returns the new particle count."""
+        n = C.c_int64(0)
+        self._ck(self.lib.mcpm_addremove_particles(self.h, int(n_ratio), C.byref(n)), "addremove_particles")
+        if n.value != self.N:
+            self.N = n.value
+            # x1 of the caller no longer lines up with the new ids
+            if self._keep and self._keep[0] is not None and not self.cfg.direction[0]:
+                self._keep[0] = np.zeros(self.N)
+        return self.N
 
     def get_normals(self):
         a, b, c = np.empty(self.N), np.empty(self.N), np.empty(self.N)

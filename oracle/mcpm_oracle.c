@@ -18,7 +18,8 @@
 
 enum { RNG_STREAM_FP = 0, RNG_STREAM_BC = 1, RNG_STREAM_ESMC = 2,
        RNG_STREAM_BIN = 3, RNG_STREAM_ESMC_ACC = 4, RNG_STREAM_ESMC_M = 5,
-       RNG_STREAM_DSMC = 6, RNG_STREAM_DSMC_ACC = 7, RNG_STREAM_DSMC_M = 8 };
+       RNG_STREAM_DSMC = 6, RNG_STREAM_DSMC_ACC = 7, RNG_STREAM_DSMC_M = 8,
+       RNG_STREAM_ADDREM_DEL = 9, RNG_STREAM_ADDREM_NEW = 10 };
 
 struct orc_state {
   mcpm_config cfg;
@@ -1678,4 +1679,163 @@ void orc_set_layout(orc_state* s, const int32_t* off, const int32_t* list) {
   for (int c = 0; c <= s->C; ++c) s->off[c] = off[c];
   for (int c = 0; c < s->C; ++c) s->cnt[c] = off[c + 1] - off[c];
   for (int64_t i = 0; i < s->N; ++i) s->list[i] = list[i];
+}
+
+/* ------------------------------------------------ interface problems -- */
+/* thermostat, src/Main_Functions.cpp:1674-1869: the live branch (problem
+   inverted, :1745-1855).  Cells num < N[1] whose centre (make_cells:
+   0.5 (dim[2] + dim[3]), src/myIO.cpp:1467) lies below thermc are rescaled
+   to Tc, above Len[1] - thermh to Th, for T > 0, over the cell's list. */
+void orc_thermostat(orc_state* s, double* U1, double* U2, double* U3,
+                    double Tc, double Th, double thermc, double thermh) {
+  int ncell = s->N1 < s->C ? s->N1 : s->C;
+  for (int num = 0; num < ncell; ++num) {
+    int k = num / s->N0;
+    double d2 = (double)(k) * s->dy, d3 = (double)(k + 1) * s->dy;
+    double yc = 0.5 * (d2 + d3);
+    double target;
+    if (yc < thermc) target = Tc;
+    else if (yc > s->cfg.length[1] - thermh) target = Th;
+    else continue;
+    double T = CELL(s, num, MCPM_CF_T);
+    if (!(T > 0.0)) continue;
+    double lamb = sqrt(target / T);
+    double us0 = CELL(s, num, MCPM_CF_U_SPACE + 0), us1 = CELL(s, num, MCPM_CF_U_SPACE + 1),
+           us2 = CELL(s, num, MCPM_CF_U_SPACE + 2);
+    for (int id = 0; id < s->cnt[num]; ++id) {
+      int i = s->list[s->off[num] + id];
+      U1[i] = lamb * (U1[i] - us0) + us0;
+      U2[i] = lamb * (U2[i] - us1) + us1;
+      U3[i] = lamb * (U3[i] - us2) + us2;
+    }
+  }
+}
+
+/* inverted_addremove_particles, src/Main_Functions.cpp:1258-1284: the
+   flags, in particle order; deletion draws are Philox keyed by the
+   particle id and step (the reference: std::mt19937 from random_device) */
+void orc_addremove_flags(orc_state* s, const int32_t* w, const int32_t* cw,
+                         int n_ratio, int8_t* flag, int64_t* n_kept,
+                         int64_t* n_new) {
+  double ratio = 1.0 - 1.0 / (n_ratio * 1.0);
+  int64_t kept = s->N, split = 0;
+  for (int64_t id = 0; id < s->N; ++id) {
+    int num = s->index[id];
+    if (w[id] > cw[num]) {
+      flag[id] = 1;
+      split++;
+    } else if (w[id] < cw[num]) {
+      uint32_t r[4];
+      philox(s->cfg.seed, (uint32_t)id, (uint32_t)s->step, RNG_STREAM_ADDREM_DEL, 0, r);
+      if (u01(r[0]) < ratio) { flag[id] = -1; kept--; }
+      else flag[id] = 2;
+    } else {
+      flag[id] = 0;
+    }
+  }
+  *n_kept = kept;
+  *n_new = (int64_t)(n_ratio - 1) * split;
+}
+
+/* the velocity spread of the copies per cell, h = 1.06 sig (numb_rem +
+   n_ratio)^(-1/5) (src/Main_Functions.cpp:1285-1346) for the given flags:
+   the kept weight and counts, the "mean" of the reference's assigning loop
+   (the last kept particle's weighted velocity, :1300-1306) over the kept
+   weight, and sig (:1312-1327); 0 in cells without split particles */
+void orc_addremove_widths(orc_state* s, const double* U1, const double* U2, const double* U3,
+                          const int32_t* w, const int32_t* cw, int n_ratio, const int8_t* flag,
+                          double* h) {
+  int C = s->C;
+  int64_t N = s->N;
+  int* numb_new = (int*)calloc(C, sizeof(int));
+  int* numb_rem = (int*)calloc(C, sizeof(int));
+  int* weight = (int*)calloc(C, sizeof(int));
+  double* Um = (double*)calloc(3 * (size_t)C, sizeof(double));
+  double* sig = (double*)calloc(C, sizeof(double));
+#define WEFF(id) (flag[id] == 2 ? cw[s->index[id]] : w[id])
+  for (int64_t id = 0; id < N; ++id) {
+    int num = s->index[id];
+    if (flag[id] == -1) continue;
+    weight[num] += WEFF(id);
+    if (flag[id] == 1) numb_new[num]++;
+    else numb_rem[num]++;
+  }
+  for (int64_t id = 0; id < N; ++id) {
+    if (flag[id] == -1) continue;
+    int num = s->index[id];
+    Um[num] = U1[id] * WEFF(id);
+    Um[C + num] = U2[id] * WEFF(id);
+    Um[2 * C + num] = U3[id] * WEFF(id);
+  }
+  for (int num = 0; num < C; ++num) {
+    Um[num] = Um[num] / (1.0 * weight[num]);
+    Um[C + num] = Um[C + num] / (1.0 * weight[num]);
+    Um[2 * C + num] = Um[2 * C + num] / (1.0 * weight[num]);
+  }
+  for (int64_t id = 0; id < N; ++id) {
+    if (flag[id] == -1) continue;
+    int num = s->index[id];
+    double energy = (U1[id] - Um[num]) * (U1[id] - Um[num])
+                  + (U2[id] - Um[C + num]) * (U2[id] - Um[C + num])
+                  + (U3[id] - Um[2 * C + num]) * (U3[id] - Um[2 * C + num]);
+    sig[num] = sig[num] + energy * WEFF(id);
+  }
+  for (int num = 0; num < C; ++num) {
+    sig[num] = sqrt(sig[num] / (1.0 * weight[num]));
+    h[num] = numb_new[num] ? 1.06 * sig[num] * pow(1.0 * (numb_rem[num] + n_ratio), -1.0 / 5.0) : 0.0;
+  }
+#undef WEFF
+  free(numb_new); free(numb_rem); free(weight); free(Um); free(sig);
+}
+
+/* the rest of inverted_addremove_particles (:1285-1445): per cell the kept
+   weight and counts, the "mean" of the reference's assigning loop (the last
+   kept particle's weighted velocity, :1300-1306) over the kept weight, the
+   spread sig (:1312-1327), h = 1.06 sig (numb_rem + n_ratio)^(-1/5) and
+   n_ratio - 1 copies per split particle with velocities U + h z; the kept
+   particles first in id order, then the copies by split particle id (the
+   reference: by cell, then by id within the cell), every weight reset to
+   its cell's (:1436-1443, the cell of the last binning). */
+void orc_addremove_apply(orc_state* s, const double* x1, const double* x2,
+                         const double* x1_old, const double* x2_old,
+                         const double* U1, const double* U2, const double* U3,
+                         const int32_t* w, const int32_t* cw, int n_ratio,
+                         const int8_t* flag, double* x1o, double* x2o,
+                         double* x1_oldo, double* x2_oldo, double* U1o,
+                         double* U2o, double* U3o, int32_t* w_out) {
+  int C = s->C;
+  int64_t N = s->N, split = 0, deleted = 0;
+  for (int64_t id = 0; id < N; ++id) {
+    if (flag[id] == 1) split++;
+    if (flag[id] == -1) deleted++;
+  }
+  if (split == 0 && deleted == 0) {
+    for (int64_t id = 0; id < N; ++id) w_out[id] = flag[id] == 2 ? cw[s->index[id]] : w[id];
+    return;
+  }
+  double* h = (double*)calloc(C, sizeof(double));
+  orc_addremove_widths(s, U1, U2, U3, w, cw, n_ratio, flag, h);
+  int64_t j = 0;
+  for (int64_t id = 0; id < N; ++id) {
+    if (flag[id] == -1) continue;
+    x1o[j] = x1[id]; x2o[j] = x2[id]; x1_oldo[j] = x1_old[id]; x2_oldo[j] = x2_old[id];
+    U1o[j] = U1[id]; U2o[j] = U2[id]; U3o[j] = U3[id];
+    w_out[j] = cw[s->index[id]];
+    j++;
+  }
+  for (int64_t id = 0; id < N; ++id) {
+    if (flag[id] != 1) continue;
+    int num = s->index[id];
+    for (int c = 0; c < n_ratio - 1; ++c) {
+      double z[4];
+      orc_normals4(s->cfg.seed, (uint32_t)id, (uint32_t)s->step, RNG_STREAM_ADDREM_NEW, (uint32_t)c, z);
+      U1o[j] = U1[id] + h[num] * z[0];
+      U2o[j] = U2[id] + h[num] * z[1];
+      U3o[j] = U3[id] + h[num] * z[2];
+      x1o[j] = x1[id]; x2o[j] = x2[id]; x1_oldo[j] = x1_old[id]; x2_oldo[j] = x2_old[id];
+      w_out[j] = cw[num];
+      j++;
+    }
+  }
+  free(h);
 }

@@ -66,6 +66,29 @@ void orc_init_omega_max(orc_state* s);
 void orc_dsmc_vhs(orc_state* s, double* U1, double* U2, double* U3);
 void orc_sample_cells(orc_state* s, const double* U1, const double* U2, const double* U3, double* acc);
 void orc_set_layout(orc_state* s, const int32_t* off, const int32_t* list);
+/* thermostat (src/Main_Functions.cpp:1674-1869) on the lists of the last
+   orc_cell_update */
+void orc_thermostat(orc_state* s, double* U1, double* U2, double* U3,
+                    double Tc, double Th, double thermc, double thermh);
+/* inverted_addremove_particles (src/Main_Functions.cpp:1206-1450) in two
+   calls: the flags (1 split, -1 deleted, 2 re-weighted, 0 kept) and the
+   counts against the cells of the last orc_cell_update, then the new state
+   (n_kept + n_new particles: the kept ones in id order, then the copies)
+   and weights; with nothing split or deleted the second call only
+   re-weights (w_out = w with the cell weight where flag is 2). */
+void orc_addremove_flags(orc_state* s, const int32_t* w, const int32_t* cw,
+                         int n_ratio, int8_t* flag, int64_t* n_kept,
+                         int64_t* n_new);
+void orc_addremove_widths(orc_state* s, const double* U1, const double* U2,
+                          const double* U3, const int32_t* w, const int32_t* cw,
+                          int n_ratio, const int8_t* flag, double* h);
+void orc_addremove_apply(orc_state* s, const double* x1, const double* x2,
+                         const double* x1_old, const double* x2_old,
+                         const double* U1, const double* U2, const double* U3,
+                         const int32_t* w, const int32_t* cw, int n_ratio,
+                         const int8_t* flag, double* x1o, double* x2o,
+                         double* x1_oldo, double* x2_oldo, double* U1o,
+                         double* U2o, double* U3o, int32_t* w_out);
 /* one iteration of the main loop body; x_old arrays persist across steps */
 void orc_step(orc_state* s, double* x1, double* x2, double* x1_old,
               double* x2_old, double* U1, double* U2, double* U3,

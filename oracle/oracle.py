@@ -76,6 +76,12 @@ def _load_oracle():
         "orc_vlasov2d_nodes": (None, [vp, dp]),
         "orc_sp2d_nodes": (None, [vp, dp]),
         "orc_long_range_2d": (None, [vp, dp, dp, dp, dp, dp]),
+        "orc_thermostat": (None, [vp, dp, dp, dp, C.c_double, C.c_double, C.c_double, C.c_double]),
+        "orc_addremove_flags": (None, [vp, ip, ip, C.c_int, C.POINTER(C.c_int8), C.POINTER(C.c_int64),
+                                       C.POINTER(C.c_int64)]),
+        "orc_addremove_widths": (None, [vp, dp, dp, dp, ip, ip, C.c_int, C.POINTER(C.c_int8), dp]),
+        "orc_addremove_apply": (None, [vp, dp, dp, dp, dp, dp, dp, dp, ip, ip, C.c_int, C.POINTER(C.c_int8),
+                                       dp, dp, dp, dp, dp, dp, dp, ip]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -230,6 +236,45 @@ class Oracle:
     def init_omega_max(self):
         self.L.orc_init_omega_max(self.h)
 
+    def thermostat(self, Tc, Th, thermc, thermh):
+        """thermostat (src/Main_Functions.cpp:1674-1869) on the lists of the
+        last cell_update"""
+        s = self.s
+        self.L.orc_thermostat(self.h, _dp(s.U1), _dp(s.U2), _dp(s.U3), Tc, Th, thermc, thermh)
+
+    def addremove(self, w, cw, n_ratio):
+        """inverted_addremove_particles (src/Main_Functions.cpp:1206-1450)
+        against the cells of the last cell_update: returns (parts, weights,
+        flags) of the new state; the oracle itself is left as it was (build a
+        new one on the returned particles to go on)."""
+        w = np.ascontiguousarray(w, dtype=np.int32)
+        cw = np.ascontiguousarray(cw, dtype=np.int32)
+        flag = np.zeros(self.N, dtype=np.int8)
+        nk, nn = C.c_int64(0), C.c_int64(0)
+        i8 = lambda a: a.ctypes.data_as(C.POINTER(C.c_int8))  # noqa: E731
+        self.L.orc_addremove_flags(self.h, _ip(w), _ip(cw), int(n_ratio), i8(flag), C.byref(nk), C.byref(nn))
+        n = nk.value + nn.value if (nn.value or nk.value != self.N) else self.N
+        out = {k: np.zeros(n) for k in ("x1", "x2", "x1o", "x2o", "U1", "U2", "U3")}
+        wo = np.zeros(n, dtype=np.int32)
+        s = self.s
+        self.L.orc_addremove_apply(self.h, _dp(s.x1), _dp(s.x2), _dp(s.x1o), _dp(s.x2o), _dp(s.U1), _dp(s.U2),
+                                   _dp(s.U3), _ip(w), _ip(cw), int(n_ratio), i8(flag),
+                                   *[_dp(out[k]) for k in ("x1", "x2", "x1o", "x2o", "U1", "U2", "U3")], _ip(wo))
+        if n == self.N and not nn.value:
+            out = {k: getattr(s, k).copy() for k in ("x1", "x2", "x1o", "x2o", "U1", "U2", "U3")}
+        return out, wo, flag
+
+    def addremove_widths(self, w, cw, n_ratio, flag):
+        """per-cell velocity spread h of the copies for the given flags"""
+        w = np.ascontiguousarray(w, dtype=np.int32)
+        cw = np.ascontiguousarray(cw, dtype=np.int32)
+        flag = np.ascontiguousarray(flag, dtype=np.int8)
+        h = np.zeros(self.C)
+        s = self.s
+        self.L.orc_addremove_widths(self.h, _dp(s.U1), _dp(s.U2), _dp(s.U3), _ip(w), _ip(cw), int(n_ratio),
+                                    flag.ctypes.data_as(C.POINTER(C.c_int8)), _dp(h))
+        return h
+
     def step(self, n=1):
         s = self.s
         for _ in range(n):
@@ -296,6 +341,9 @@ def ref_lib(build=True):
         "ref_get_cells": (None, [vp, dp]),
         "ref_long_range_2d": (None, [vp, dp, dp, dp, dp, ip]),
         "ref_get_node_density": (None, [vp, dp]),
+        "ref_thermostat": (None, [vp, dp, dp, dp, dp, ip, C.c_double, C.c_double, C.c_double, C.c_double]),
+        "ref_addremove": (C.c_long, [vp, dp, dp, dp, dp, dp, dp, dp, ip, ip, ip, C.c_int, C.c_long,
+                                     dp, dp, dp, dp, dp, dp, dp, ip]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -381,6 +429,25 @@ class Reference:
     def esmc(self):
         s = self.s
         self.L.ref_esmc(self.h, _dp(s.U1), _dp(s.U2), _dp(s.U3), _dp(s.x1), _dp(s.x2), _ip(s.index))
+
+    def thermostat(self, Tc, Th, thermc, thermh):
+        s = self.s
+        self.L.ref_thermostat(self.h, _dp(s.U1), _dp(s.U2), _dp(s.U3), _dp(s.x2), _ip(s.index), Tc, Th, thermc, thermh)
+
+    def addremove(self, w, cw, n_ratio, cap):
+        """the reference's inverted_addremove_particles; returns (parts,
+        weights) of its new state (the reference object keeps its own)"""
+        s = self.s
+        w = np.ascontiguousarray(w, dtype=np.int32)
+        cw = np.ascontiguousarray(cw, dtype=np.int32)
+        out = {k: np.zeros(cap) for k in ("x1", "x2", "x1o", "x2o", "U1", "U2", "U3")}
+        wo = np.zeros(cap, dtype=np.int32)
+        m = self.L.ref_addremove(self.h, _dp(s.x1), _dp(s.x2), _dp(s.x1o), _dp(s.x2o), _dp(s.U1), _dp(s.U2),
+                                 _dp(s.U3), _ip(s.index), _ip(w), _ip(cw), int(n_ratio), int(cap),
+                                 *[_dp(out[k]) for k in ("x1", "x2", "x1o", "x2o", "U1", "U2", "U3")], _ip(wo))
+        if m < 0:
+            raise RuntimeError("reference addremove: more than %d particles" % cap)
+        return {k: v[:m] for k, v in out.items()}, wo[:m]
 
     def sample_cells(self, acc):
         """the reference's cell_poly_velocity; acc receives its running sums"""

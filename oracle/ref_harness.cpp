@@ -340,6 +340,70 @@ void ref_init_omega_max(void* h) {
   }
 }
 
+// thermostat (src/Main_Functions.cpp:1674) in its live branch, problem
+// inverted, on the lists of the last ref_cell_update
+void ref_thermostat(void* h, double* U1, double* U2, double* U3, double* x2, int* index, double Tc, double Th,
+                    double thermc, double thermh) {
+  Quiet q;
+  Ref* r = (Ref*)h;
+  const int problem = r->box.problem;
+  r->box.problem = inverted;
+  r->gas.Tc = Tc; r->gas.Th = Th;
+  r->box.thermc = thermc; r->box.thermh = thermh;
+  thermostat(U1, U2, U3, x2, &r->gas, &r->box, r->cells, index);
+  r->box.problem = problem;
+}
+
+// inverted_addremove_particles (src/Main_Functions.cpp:1206) against the
+// lists of the last ref_cell_update: the particle weights w (N), the cell
+// weights cw (C) and n_ratio; the reference frees and re-allocates its
+// arrays, so they are handed over as malloc'd copies and the new state is
+// copied out (room for cap particles).  Returns the new N (-1: no room).
+long ref_addremove(void* h, const double* x1, const double* x2, const double* x1_old, const double* x2_old,
+                   const double* U1, const double* U2, const double* U3, const int* index, const int* w,
+                   const int* cw, int n_ratio, long cap, double* ox1, double* ox2, double* ox1_old,
+                   double* ox2_old, double* oU1, double* oU2, double* oU3, int* ow) {
+  Quiet q;
+  Ref* r = (Ref*)h;
+  const long N = r->gas.N;
+  auto dup = [&](const double* a) {
+    double* p = (double*)malloc(sizeof(double) * (N > 0 ? N : 1));
+    memcpy(p, a, sizeof(double) * N);
+    return p;
+  };
+  auto idup = [&](const int* a) {
+    int* p = (int*)malloc(sizeof(int) * (N > 0 ? N : 1));
+    if (a) memcpy(p, a, sizeof(int) * N);
+    else memset(p, 0, sizeof(int) * N);
+    return p;
+  };
+  double *a1 = dup(x1), *a2 = dup(x2), *a1o = dup(x1_old), *a2o = dup(x2_old);
+  double *u1 = dup(U1), *u2 = dup(U2), *u3 = dup(U3);
+  double *xi1 = dup(U1), *xi2 = dup(U1), *xi3 = dup(U1), *xf1 = dup(U1), *xf2 = dup(U1), *xf3 = dup(U1);
+  double *m1 = dup(U1), *m2 = dup(U1), *m3 = dup(U1);
+  int *ix = idup(index), *fl = idup(nullptr), *nr = idup(w), *col = idup(nullptr);
+  for (int c = 0; c < r->C; ++c) r->cells[c].n_ratio = cw[c];
+  r->gas.n_ratio = n_ratio;
+  const int step = r->box.step;
+  r->box.step = 1;  // the first call frees no earlier split lists (:1289-1290)
+  inverted_addremove_particles(&u1, &u2, &u3, &a1, &a1o, &a2, &a2o, &r->gas, &r->box, r->cells, &ix, &fl, &nr,
+                               &xi1, &xi2, &xi3, &xf1, &xf2, &xf3, &m1, &m2, &m3, &col);
+  r->box.step = step;
+  const long M = (long)r->gas.N;
+  if (M <= cap) {
+    memcpy(ox1, a1, sizeof(double) * M); memcpy(ox2, a2, sizeof(double) * M);
+    memcpy(ox1_old, a1o, sizeof(double) * M); memcpy(ox2_old, a2o, sizeof(double) * M);
+    memcpy(oU1, u1, sizeof(double) * M); memcpy(oU2, u2, sizeof(double) * M); memcpy(oU3, u3, sizeof(double) * M);
+    memcpy(ow, nr, sizeof(int) * M);
+  }
+  for (int c = 0; c < r->C; ++c) { free(r->cells[c].id_split_part); r->cells[c].id_split_part = nullptr; }
+  free(a1); free(a2); free(a1o); free(a2o); free(u1); free(u2); free(u3);
+  free(xi1); free(xi2); free(xi3); free(xf1); free(xf2); free(xf3); free(m1); free(m2); free(m3);
+  free(ix); free(fl); free(nr); free(col);
+  r->gas.N = N;  // the harness's particle count stays (its side arrays are sized by it)
+  return M <= cap ? M : -1;
+}
+
 // the CELLS fields of enum mcpm_cell_field, cell-major [C][MCPM_CF_COUNT]
 void ref_get_cells(void* h, double* out) {
   Ref* r = (Ref*)h;
