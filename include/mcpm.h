@@ -318,6 +318,49 @@ int mcpm_get_cells(mcpm_session* s, double* out);
 /* Cell index of every particle, in particle-id order (cell_update's index[]). */
 int mcpm_get_index(mcpm_session* s, int32_t* index);
 
+/* ---- pressure sampling -------------------------------------------------- */
+/* measure_pressure (src/Main_Functions.cpp:13-34, called src/main.cpp:490-492
+   once step > times * after): every particle whose cell row changed over
+   the step adds Fn m |U2| to p_m of each row index it crossed.  Switching
+   sampling on keeps the positions before the flight (sessions without
+   diffuse walls otherwise do not) and makes every fused step add its
+   crossings after the flight and the walls; mcpm_measure_pressure adds
+   those of the current state once (the routine-by-routine loop, after
+   store_old_positions / stream_particles / apply_BC).  p_m accumulates until
+   reset; mcpm_get_pressure copies its C values (cells[].p_m). */
+int mcpm_set_pressure_sampling(mcpm_session* s, int32_t on);
+int mcpm_measure_pressure(mcpm_session* s);
+int mcpm_get_pressure(mcpm_session* s, double* p_m);
+int mcpm_reset_pressure(mcpm_session* s);
+
+/* ---- post-processing output ------------------------------------------- */
+/* write_post_processing (src/myIO.cpp:597-934): the file
+   <dir>/<output_name>_<lr>_<step>.dat (lr: noatt / direct / denexp /
+   screened-Poisson) in the reference's layout -- a header of 122 names,
+   then per cell (x outer, y inner, a blank line after each column) 121
+   values: geometry, t_post, dt, U_space, T, n, the cell_poly_velocity sums,
+   the interface face sums (0 here), volume, n_smooth, num_inside, the
+   Enskog pressure with attraction, n_ratio Fn, model / xx / UU.. (0 here),
+   P_12 ... the FP coefficients, p_m and the Enskog pressure.  The reference
+   writes it into PostProc/ when step > times * after and step % every == 0
+   or at its first step; the caller decides.  cells: [MCPM_CF_COUNT][C]
+   (mcpm_get_cells); samples [MCPM_SF_COUNT][C], p_m [C], cell_weights [C]
+   may be NULL (0, 0, 1).  path receives the file name. */
+int mcpm_post_processing_write(const mcpm_config* cfg, int32_t step, double t_post,
+                               const char* dir, const char* output_name,
+                               const double* cells, const double* samples,
+                               const double* p_m, const int32_t* cell_weights,
+                               char* path, int32_t path_len);
+/* The same from a session's cell fields, sample sums, p_m and cell weights. */
+int mcpm_write_post_processing(mcpm_session* s, int32_t step, double t_post,
+                               const char* dir, const char* output_name,
+                               char* path, int32_t path_len);
+/* The console summary of post_processing (src/myIO.cpp:945-965: T, N,
+   n sigma^3 and p of cells 0, 1, 2, N[1]/2, N[1]-2, N[1]-1, their mean T,
+   Fn; the 1-D-box form when N[1] == 1) into buf; returns its length. */
+int mcpm_post_processing_text(const mcpm_config* cfg, const double* cells,
+                              char* buf, int32_t len);
+
 /* ---- interface problems: thermostat and weighted particles ------------ */
 /* Per-particle weights (the reference's n_ratio[], particle-id order, N
    values) and per-cell weights (cells[].n_ratio, C values, set by make_cells

@@ -3,7 +3,9 @@
 Each CUDA translation unit is compiled in parallel with nvcc, then linked into
 one shared library next to this file.  The particle kernels are compiled with
 ``--fmad=false``: the FP64 path then rounds every multiply and add separately,
-as the reference does (the FP32 kernels write their fused multiply-adds out).
+as the reference does (the FP32 kernels write their fused multiply-adds out);
+host code is compiled with ``-ffp-contract=off`` for the same reason (aarch64
+compilers contract by default).
 """
 from __future__ import annotations
 
@@ -20,10 +22,10 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libmcpm.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "--fmad=false", "-Xcompiler", "-fPIC,-O2",
+NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "--fmad=false", "-Xcompiler", "-fPIC,-O2,-ffp-contract=off",
            "-Xptxas", "-warn-spills", "--expt-relaxed-constexpr"]
 SOURCES = ["mcpm_session.cu", "mcpm_kernels.cu", "mcpm_forces.cu", "mcpm_lr2d.cu", "mcpm_noalloc.cu",
-           "mcpm_surrogate.cu", "mcpm_surrogate_tc.cu", "mcpm_settings.cu", "mcpm_dynamic.cu"]
+           "mcpm_surrogate.cu", "mcpm_surrogate_tc.cu", "mcpm_settings.cu", "mcpm_dynamic.cu", "mcpm_output.cu"]
 
 
 def nvcc():

@@ -320,6 +320,38 @@ __global__ void k_ar_reweight(DevConsts k, const int32_t* off, const int32_t* cn
   }
 }
 
+// ------------------------------------------------------- measure_pressure
+// src/Main_Functions.cpp:13-34: every particle whose cell row changed over
+// the step (floor(x2_old / dy) -> floor(x2 / dy)) adds Fn m |U2| to p_m of
+// each row index it crossed, num1 <= num < num2 (the reference indexes
+// cells by the row number, as in its 1-D boxes).  The state may be packed
+// (n particles in [0, n)) or slotted (each cell's region, then the overflow
+// entries).
+template <typename real>
+__global__ void k_pressure(DevConsts k, DynP<real> p, DynP<real> ovf, const int32_t* ovf_n, const int32_t* off,
+                           const int32_t* dcur, int64_t n, double coef, double* p_m) {
+  const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x, nt = (int64_t)gridDim.x * blockDim.x;
+  auto one = [&](real x2, real x2o, real u2) {
+    const int numO = (int)floor((double)x2o / k.dy), numN = (int)floor((double)x2 / k.dy);
+    int lo = -1, hi = -1;
+    if (numN > numO) { lo = numO; hi = numN; }
+    else if (numN < numO) { lo = numN; hi = numO; }
+    for (int num = lo; num < hi; ++num)
+      if (num >= 0 && num < k.C) atomicAdd(&p_m[num], coef * fabs((double)u2));
+  };
+  if (!dcur) {
+    for (int64_t i = tid; i < n; i += nt) one(p.x2[i], p.x2o[i], p.U2[i]);
+    return;
+  }
+  const int lane = threadIdx.x & 31;
+  for (int64_t c = tid >> 5; c < k.C; c += nt >> 5) {
+    const int s0 = off[c], m = min(dcur[c], off[c + 1] - s0);
+    for (int i = lane; i < m; i += 32) one(p.x2[s0 + i], p.x2o[s0 + i], p.U2[s0 + i]);
+  }
+  const int n_ovf = *ovf_n;
+  for (int64_t e = tid; e < n_ovf; e += nt) one(ovf.x2[e], ovf.x2o[e], ovf.U2[e]);
+}
+
 static int warp_grid(const Session& s, int cells) {
   const int blocks = (cells + 7) / 8;  // 8 warps of 256 threads
   return blocks < 1 ? 1 : (blocks > s.num_sms * 16 ? s.num_sms * 16 : blocks);
@@ -370,5 +402,14 @@ int launch_addremove_reweight(Session& s) {
 }
 
 int addremove_tiles(int64_t n) { return (int)((n + AR_TILE - 1) / AR_TILE); }
+
+template <typename real> static int pressure_impl(Session& s) {
+  const bool sl = s.slotted;
+  k_pressure<real><<<s.num_sms * 8, 256, 0, s.stream>>>(
+      s.k, ptd<real>(s.P[s.cur]), ptd<real>(s.ovf), sl ? s.ovf_n + (1 - s.ovf_par) : nullptr, s.off,
+      sl ? s.dcur : nullptr, s.N, s.k.Fn * s.k.m, s.p_m);
+  return 1;
+}
+int launch_pressure(Session& s) { return s.prec == MCPM_FP32 ? pressure_impl<float>(s) : pressure_impl<double>(s); }
 
 }  // namespace mcpm

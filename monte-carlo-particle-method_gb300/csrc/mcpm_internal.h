@@ -201,6 +201,8 @@ struct Session {
   int32_t* ar_srank = nullptr;  // [cap]
   int32_t* ar_tiles = nullptr;  // [2][tiles of the scan]
   unsigned long long* ar_tot = nullptr;  // [2] split, deleted
+  double* p_m = nullptr;        // [C] measure_pressure accumulators (cells[].p_m)
+  bool press = false;           // fused steps add their crossings to p_m
   bool omega_init = false;      // ESMC / DSMC majorant initialised (src/main.cpp:250-269)
   int num_sms = 0;
   Tuning tune{};
@@ -282,6 +284,8 @@ int launch_addremove_flags(Session& s, int g, int step);
 int launch_addremove_move(Session& s, int g, int step, int64_t n_kept);
 int launch_addremove_reweight(Session& s);
 int addremove_tiles(int64_t n);
+// measure_pressure on the current state (x2, x2_old, U2) into p_m
+int launch_pressure(Session& s);
 // one staged upload field (0..4: x1 x2 U1 U2 U3; field 2 also sets the ids)
 // on stream st
 int launch_convert_field(Session& s, int field, int64_t n, cudaStream_t st);

@@ -352,6 +352,7 @@ int mcpm_session_destroy(mcpm_session* s) {
   cudaFree(s->samples);
   cudaFree(s->pw); cudaFree(s->pw_alt); cudaFree(s->cw); cudaFree(s->ar_flag); cudaFree(s->ar_ci); cudaFree(s->ar_h);
   cudaFree(s->ar_newid); cudaFree(s->ar_srank); cudaFree(s->ar_tiles); cudaFree(s->ar_tot);
+  cudaFree(s->p_m);
   for (int b = 0; b < 2; ++b) {
     PBuf& P = s->P[b];
     cudaFree(P.x1); cudaFree(P.x2); cudaFree(P.U1); cudaFree(P.U2); cudaFree(P.U3); cudaFree(P.pid);
@@ -671,6 +672,7 @@ static int step_once(mcpm_session* s, uint32_t stages) {
   k_step_advance<<<1, 1, 0, s->stream>>>(s->dstep);
   ++n;
   s->step++;
+  const bool press = s->press;
   s->dstep_val = s->step;
   s->bc_calls = 0;
   s->sorted = false;
@@ -684,6 +686,8 @@ static int step_once(mcpm_session* s, uint32_t stages) {
   } else {
     s->keys_current = true;
   }
+  // measure_pressure after the flight and the walls (src/main.cpp:490-492)
+  if (press) n += launch_pressure(*s);
   return n;
 }
 
@@ -707,6 +711,7 @@ static uint64_t graph_signature(const mcpm_session* s, uint32_t stages) {
   mix((uint64_t)(uintptr_t)s->sur);
   mix((uint64_t)s->sur_active);
   mix((uint64_t)s->N);  // the particle count changes with splits and deletions
+  mix((uint64_t)s->press);
   return h;
 }
 
@@ -983,6 +988,100 @@ int mcpm_get_node_potential(mcpm_session* s, double* out) {
   if (!s->lr2d) return fail(s, MCPM_ERR_STATE, "get_node_potential: needs a 2-D long-range session");
   cudaMemcpyAsync(out, lr2d_potential(*s), (size_t)lr2d_num_nodes(*s) * 8, cudaMemcpyDeviceToHost, s->stream);
   return cuda_check(s, cudaStreamSynchronize(s->stream), "get_node_potential");
+}
+
+// ------------------------------------------------------------ pressure
+// measure_pressure (src/Main_Functions.cpp:13-34) needs the positions before
+// the flight: sessions without diffuse walls do not keep them until
+// sampling is switched on, which adds the old-position arrays (both buffer
+// sets and the overflow) and the p_m accumulators
+int mcpm_set_pressure_sampling(mcpm_session* s, int32_t on) {
+  if (!s) return MCPM_ERR_ARG;
+  if (!on) {
+    s->press = false;
+    return MCPM_OK;
+  }
+  if (!s->p_m) {
+    if (cudaMalloc((void**)&s->p_m, (size_t)s->C * 8) != cudaSuccess) {
+      s->p_m = nullptr;
+      cudaGetLastError();
+      return fail(s, MCPM_ERR_CUDA, "pressure sampling: out of device memory");
+    }
+    cudaMemsetAsync(s->p_m, 0, (size_t)s->C * 8, s->stream);
+  }
+  if (!s->need_old) {
+    const size_t n = (size_t)s->slots;
+    for (int b = 0; b < 2; ++b)
+      if (!s->P[b].x2o && cudaMalloc(&s->P[b].x2o, n * s->rsz) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(s, MCPM_ERR_CUDA, "pressure sampling: out of device memory");
+      }
+    if (s->use_slotted && !s->ovf.x2o && cudaMalloc(&s->ovf.x2o, (size_t)s->cap * s->rsz) != cudaSuccess) {
+      cudaGetLastError();
+      return fail(s, MCPM_ERR_CUDA, "pressure sampling: out of device memory");
+    }
+    // the old positions start as the current ones
+    if (s->have_particles) {
+      if (s->slotted) {
+        int rc = leave_slotted(s);
+        if (rc) return rc;
+      }
+      cudaMemcpyAsync(s->P[s->cur].x2o, s->P[s->cur].x2, (size_t)s->N * s->rsz, cudaMemcpyDeviceToDevice, s->stream);
+    }
+    s->need_old = true;
+  }
+  s->press = true;
+  return cuda_check(s, cudaStreamSynchronize(s->stream), "pressure sampling");
+}
+
+int mcpm_measure_pressure(mcpm_session* s) {
+  if (!s || !s->have_particles) return fail(s, MCPM_ERR_STATE, "measure_pressure: no particles");
+  if (!s->p_m) return fail(s, MCPM_ERR_STATE, "measure_pressure: switch pressure sampling on first");
+  return after_launch(s, launch_pressure(*s), "measure_pressure");
+}
+
+int mcpm_get_pressure(mcpm_session* s, double* p_m) {
+  if (!s || !p_m) return MCPM_ERR_ARG;
+  if (!s->p_m) {
+    memset(p_m, 0, (size_t)s->C * 8);
+    return MCPM_OK;
+  }
+  cudaMemcpyAsync(p_m, s->p_m, (size_t)s->C * 8, cudaMemcpyDeviceToHost, s->stream);
+  return cuda_check(s, cudaStreamSynchronize(s->stream), "get_pressure");
+}
+
+int mcpm_reset_pressure(mcpm_session* s) {
+  if (!s) return MCPM_ERR_ARG;
+  if (s->p_m) cudaMemsetAsync(s->p_m, 0, (size_t)s->C * 8, s->stream);
+  return MCPM_OK;
+}
+
+// ------------------------------------------------------------- output
+int mcpm_write_post_processing(mcpm_session* s, int32_t step, double t_post, const char* dir,
+                               const char* output_name, char* path, int32_t path_len) {
+  if (!s || !dir || !output_name) return MCPM_ERR_ARG;
+  const size_t C = (size_t)s->C;
+  std::vector<double> cells((size_t)MCPM_CF_COUNT * C), samples, pm;
+  std::vector<int32_t> cw;
+  int rc = mcpm_get_cells(s, cells.data());
+  if (rc) return rc;
+  if (s->samples) {
+    samples.resize((size_t)MCPM_SF_COUNT * C);
+    if ((rc = mcpm_get_samples(s, samples.data()))) return rc;
+  }
+  if (s->p_m) {
+    pm.resize(C);
+    if ((rc = mcpm_get_pressure(s, pm.data()))) return rc;
+  }
+  if (s->cw) {
+    cw.resize(C);
+    cudaMemcpyAsync(cw.data(), s->cw, C * 4, cudaMemcpyDeviceToHost, s->stream);
+    if ((rc = cuda_check(s, cudaStreamSynchronize(s->stream), "write_post_processing"))) return rc;
+  }
+  rc = mcpm_post_processing_write(&s->cfg, step, t_post, dir, output_name, cells.data(),
+                                  samples.empty() ? nullptr : samples.data(), pm.empty() ? nullptr : pm.data(),
+                                  cw.empty() ? nullptr : cw.data(), path, path_len);
+  return rc ? fail(s, rc, "write_post_processing: cannot write the file") : MCPM_OK;
 }
 
 // ------------------------------------------------ interface problems

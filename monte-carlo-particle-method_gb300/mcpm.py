@@ -174,6 +174,14 @@ def load_library(path: str | None = None):
         "mcpm_get_samples": (C.c_int, [vp, dp]),
         "mcpm_reset_samples": (C.c_int, [vp]),
         "mcpm_get_index": (C.c_int, [vp, ip]),
+        "mcpm_post_processing_write": (C.c_int, [C.POINTER(Config), i32, C.c_double, C.c_char_p, C.c_char_p, dp, dp,
+                                                 dp, ip, C.c_char_p, i32]),
+        "mcpm_write_post_processing": (C.c_int, [vp, i32, C.c_double, C.c_char_p, C.c_char_p, C.c_char_p, i32]),
+        "mcpm_post_processing_text": (C.c_int, [C.POINTER(Config), dp, C.c_char_p, i32]),
+        "mcpm_set_pressure_sampling": (C.c_int, [vp, i32]),
+        "mcpm_measure_pressure": (C.c_int, [vp]),
+        "mcpm_get_pressure": (C.c_int, [vp, dp]),
+        "mcpm_reset_pressure": (C.c_int, [vp]),
         "mcpm_set_particle_weights": (C.c_int, [vp, ip]),
         "mcpm_get_particle_weights": (C.c_int, [vp, ip]),
         "mcpm_set_cell_weights": (C.c_int, [vp, ip]),
@@ -378,6 +386,29 @@ class Session:
         out = np.empty(self.N, dtype=np.int32)
         self._ck(self.lib.mcpm_get_index(self.h, _ip(out)), "get_index")
         return out
+
+    # -- post-processing output (src/myIO.cpp:597-965)
+    def write_post_processing(self, step, t_post, directory, output_name):
+        """The reference's .dat file of the current cell fields; returns its path."""
+        buf = C.create_string_buffer(4096)
+        self._ck(self.lib.mcpm_write_post_processing(self.h, int(step), float(t_post), os.fsencode(directory),
+                                                     output_name.encode(), buf, 4096), "write_post_processing")
+        return buf.value.decode()
+
+    # -- pressure sampling (measure_pressure, src/Main_Functions.cpp:13-34)
+    def set_pressure_sampling(self, on=True):
+        self._ck(self.lib.mcpm_set_pressure_sampling(self.h, 1 if on else 0), "set_pressure_sampling")
+
+    def measure_pressure(self):
+        self._ck(self.lib.mcpm_measure_pressure(self.h), "measure_pressure")
+
+    def get_pressure(self):
+        out = np.empty(self.C)
+        self._ck(self.lib.mcpm_get_pressure(self.h, _dp(out)), "get_pressure")
+        return out
+
+    def reset_pressure(self):
+        self._ck(self.lib.mcpm_reset_pressure(self.h), "reset_pressure")
 
     # -- interface problems (the reference's problem inverted)
     def set_particle_weights(self, w):
@@ -602,3 +633,33 @@ def cell_field(cells, name, cell_major=False):
         return v[:, 0] if w == 1 else v
     v = cells[o:o + w]
     return v[0] if w == 1 else v.T
+
+
+def post_processing_write(cfg, step, t_post, directory, output_name, cells, samples=None, p_m=None,
+                          cell_weights=None):
+    """write_post_processing (src/myIO.cpp:597-934) of host arrays: cells
+    [CF_COUNT][C], samples [SF_COUNT][C], p_m [C], cell weights [C]; returns
+    the file's path."""
+    L = load_library()
+    buf = C.create_string_buffer(4096)
+
+    def arr(a, dt):
+        return None if a is None else np.ascontiguousarray(a, dtype=dt)
+    cells, samples, p_m, cw = arr(cells, np.float64), arr(samples, np.float64), arr(p_m, np.float64), arr(cell_weights, np.int32)
+    rc = L.mcpm_post_processing_write(C.byref(cfg), int(step), float(t_post), os.fsencode(directory),
+                                      output_name.encode(), _dp(cells), None if samples is None else _dp(samples),
+                                      None if p_m is None else _dp(p_m), None if cw is None else _ip(cw), buf, 4096)
+    if rc:
+        raise MCPMError(rc, "post_processing_write failed")
+    return buf.value.decode()
+
+
+def post_processing_text(cfg, cells):
+    """The console summary of post_processing (src/myIO.cpp:945-965)."""
+    L = load_library()
+    buf = C.create_string_buffer(1 << 14)
+    cells = np.ascontiguousarray(cells, dtype=np.float64)
+    n = L.mcpm_post_processing_text(C.byref(cfg), _dp(cells), buf, 1 << 14)
+    if n < 0:
+        raise MCPMError(-n, "post_processing_text failed")
+    return buf.value.decode()

@@ -1839,3 +1839,19 @@ void orc_addremove_apply(orc_state* s, const double* x1, const double* x2,
   }
   free(h);
 }
+
+/* measure_pressure, src/Main_Functions.cpp:13-34: every particle whose
+   cell row changed over the step adds Fn m |U2| to p_m of each row index it
+   crossed (p_m accumulates, C values) */
+void orc_measure_pressure(orc_state* s, const double* U2, const double* x2,
+                          const double* x2_old, double* p_m) {
+  for (int64_t i = 0; i < s->N; ++i) {
+    int numO = (int)floor(x2_old[i] / s->dy);
+    int numN = (int)floor(x2[i] / s->dy);
+    int num1, num2;
+    if (numN > numO) { num1 = numO; num2 = numN; }
+    else if (numN < numO) { num1 = numN; num2 = numO; }
+    else { num1 = -1; num2 = -1; }
+    for (int num = num1; num < num2; num++) p_m[num] += s->cfg.Fn * s->cfg.m * fabs(U2[i]);
+  }
+}

@@ -89,6 +89,9 @@ void orc_addremove_apply(orc_state* s, const double* x1, const double* x2,
                          const int8_t* flag, double* x1o, double* x2o,
                          double* x1_oldo, double* x2_oldo, double* U1o,
                          double* U2o, double* U3o, int32_t* w_out);
+/* measure_pressure (src/Main_Functions.cpp:13-34) into p_m[C] (added to) */
+void orc_measure_pressure(orc_state* s, const double* U2, const double* x2,
+                          const double* x2_old, double* p_m);
 /* one iteration of the main loop body; x_old arrays persist across steps */
 void orc_step(orc_state* s, double* x1, double* x2, double* x1_old,
               double* x2_old, double* U1, double* U2, double* U3,

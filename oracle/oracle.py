@@ -79,6 +79,7 @@ def _load_oracle():
         "orc_thermostat": (None, [vp, dp, dp, dp, C.c_double, C.c_double, C.c_double, C.c_double]),
         "orc_addremove_flags": (None, [vp, ip, ip, C.c_int, C.POINTER(C.c_int8), C.POINTER(C.c_int64),
                                        C.POINTER(C.c_int64)]),
+        "orc_measure_pressure": (None, [vp, dp, dp, dp, dp]),
         "orc_addremove_widths": (None, [vp, dp, dp, dp, ip, ip, C.c_int, C.POINTER(C.c_int8), dp]),
         "orc_addremove_apply": (None, [vp, dp, dp, dp, dp, dp, dp, dp, ip, ip, C.c_int, C.POINTER(C.c_int8),
                                        dp, dp, dp, dp, dp, dp, dp, ip]),
@@ -236,6 +237,11 @@ class Oracle:
     def init_omega_max(self):
         self.L.orc_init_omega_max(self.h)
 
+    def measure_pressure(self, p_m):
+        """measure_pressure (src/Main_Functions.cpp:13-34) added into p_m [C]"""
+        s = self.s
+        self.L.orc_measure_pressure(self.h, _dp(s.U2), _dp(s.x2), _dp(s.x2o), _dp(p_m))
+
     def thermostat(self, Tc, Th, thermc, thermh):
         """thermostat (src/Main_Functions.cpp:1674-1869) on the lists of the
         last cell_update"""
@@ -341,6 +347,9 @@ def ref_lib(build=True):
         "ref_get_cells": (None, [vp, dp]),
         "ref_long_range_2d": (None, [vp, dp, dp, dp, dp, ip]),
         "ref_get_node_density": (None, [vp, dp]),
+        "ref_measure_pressure": (None, [vp, dp, dp, dp, dp]),
+        "ref_write_post": (None, [vp, C.c_int, C.c_double, C.c_char_p, C.c_char_p, dp, dp, dp, dp, dp, dp, ip]),
+        "ref_post_text": (C.c_long, [vp, C.c_int, dp, dp, dp, dp, dp, dp, ip, C.c_char_p, C.c_long]),
         "ref_thermostat": (None, [vp, dp, dp, dp, dp, ip, C.c_double, C.c_double, C.c_double, C.c_double]),
         "ref_addremove": (C.c_long, [vp, dp, dp, dp, dp, dp, dp, dp, ip, ip, ip, C.c_int, C.c_long,
                                      dp, dp, dp, dp, dp, dp, dp, ip]),
@@ -429,6 +438,27 @@ class Reference:
     def esmc(self):
         s = self.s
         self.L.ref_esmc(self.h, _dp(s.U1), _dp(s.U2), _dp(s.U3), _dp(s.x1), _dp(s.x2), _ip(s.index))
+
+    def measure_pressure(self):
+        """the reference's measure_pressure; returns its cells' p_m (cumulative)"""
+        s = self.s
+        out = np.empty(self.C)
+        self.L.ref_measure_pressure(self.h, _dp(s.U2), _dp(s.x2), _dp(s.x2o), _dp(out))
+        return out
+
+    def write_post(self, step, t_post, directory, name):
+        """the reference's write_post_processing into directory/PostProc"""
+        s = self.s
+        self.L.ref_write_post(self.h, int(step), float(t_post), os.fsencode(directory), name.encode(), _dp(s.U1),
+                              _dp(s.U2), _dp(s.U3), _dp(s.x1), _dp(s.x2), _dp(s.x2o), _ip(s.index))
+
+    def post_text(self, step):
+        """the console lines of the reference's post_processing"""
+        s = self.s
+        buf = C.create_string_buffer(1 << 16)
+        n = self.L.ref_post_text(self.h, int(step), _dp(s.U1), _dp(s.U2), _dp(s.U3), _dp(s.x1), _dp(s.x2),
+                                 _dp(s.x2o), _ip(s.index), buf, 1 << 16)
+        return buf.value.decode() if n >= 0 else None
 
     def thermostat(self, Tc, Th, thermc, thermh):
         s = self.s

@@ -404,6 +404,65 @@ long ref_addremove(void* h, const double* x1, const double* x2, const double* x1
   return M <= cap ? M : -1;
 }
 
+// measure_pressure (src/Main_Functions.cpp:13), then cells[].p_m into out [C]
+void ref_measure_pressure(void* h, double* U2, double* x2, double* x2_old, double* out) {
+  Quiet q;
+  Ref* r = (Ref*)h;
+  measure_pressure(U2, x2, x2_old, &r->gas, &r->box, r->cells);
+  for (int c = 0; c < r->C; ++c) out[c] = r->cells[c].p_m;
+}
+
+// write_post_processing (src/myIO.cpp:597) with the harness's cells: the
+// file PostProc/<name>_<lr>_<step>.dat under dir (which must hold PostProc/)
+void ref_write_post(void* h, int step, double t_post, const char* dir, const char* name, double* U1, double* U2,
+                    double* U3, double* x1, double* x2, double* x2_old, int* index) {
+  Quiet q;
+  Ref* r = (Ref*)h;
+  char cwd[4096];
+  if (!getcwd(cwd, sizeof cwd) || chdir(dir) != 0) return;
+  const int every = r->box.every, after = r->box.after;
+  const double times = r->gas.times;
+  r->box.every = 1; r->box.after = 0; r->gas.times = 0.0;
+  r->gas.output_name = name;
+  r->gas.t_post = t_post;
+  int done = 0;
+  std::vector<int> nratio(r->N, 1);
+  write_post_processing(step, r->cells, &r->box, &done, &r->gas, U1, U2, U3, x1, x2, r->flag.data(), index,
+                        r->color.data(), nratio.data(), x2_old);
+  r->box.every = every; r->box.after = after; r->gas.times = times;
+  if (chdir(cwd) != 0) return;
+}
+
+// the console lines of post_processing (src/myIO.cpp:935) into buf
+long ref_post_text(void* h, int step, double* U1, double* U2, double* U3, double* x1, double* x2, double* x2_old,
+                   int* index, char* buf, long len) {
+  Ref* r = (Ref*)h;
+  char tmpl[] = "/tmp/mcpm_ref_textXXXXXX";
+  const int fd = mkstemp(tmpl);
+  if (fd < 0) return -1;
+  fflush(stdout);
+  const int saved = dup(1);
+  dup2(fd, 1);
+  const int every = r->box.every, st = r->box.step;
+  r->box.every = 1; r->box.step = step;
+  int done = 0;
+  std::vector<int> nratio(r->N, 1);
+  post_processing(step, r->cells, &r->box, &done, &r->gas, U1, U2, U3, x1, x2, r->flag.data(), index,
+                  r->color.data(), nratio.data(), x2_old);
+  r->box.every = every; r->box.step = st;
+  fflush(stdout);
+  dup2(saved, 1);
+  close(saved);
+  const long n = (long)lseek(fd, 0, SEEK_END);
+  lseek(fd, 0, SEEK_SET);
+  long got = 0;
+  if (n > 0 && n < len) got = (long)read(fd, buf, (size_t)n);
+  close(fd);
+  unlink(tmpl);
+  if (got >= 0 && got < len) buf[got] = 0;
+  return got;
+}
+
 // the CELLS fields of enum mcpm_cell_field, cell-major [C][MCPM_CF_COUNT]
 void ref_get_cells(void* h, double* out) {
   Ref* r = (Ref*)h;
