@@ -93,6 +93,9 @@ struct DevConsts {
   const float* f_face_x;
   const float* f_face_y;
   float f_bin_wx, f_bin_wy;
+  // the cells' weights (cells[].n_ratio) once set, else null (weight 1): the
+  // cell density is n_ratio Fn N / V (src/Main_Functions.cpp:2588)
+  const int32_t* cell_w;
 };
 
 // One set of device particle arrays (SoA).  real is float or double.

@@ -797,7 +797,7 @@ __global__ void __launch_bounds__(128) k_solve(DevConsts k, double* cell, float*
   // (the FP32 sessions' variant multiplies by quotients formed once, where
   // the reference divides)
   const double T = EXACT ? k.m * DM2 / (3.0 * k.kb) : DM2 * k.q_T;
-  const double n = 1 * k.Fn * weight / cell_volume(c, k);
+  const double n = (k.cell_w ? k.cell_w[c] : 1) * k.Fn * weight / cell_volume(c, k);
   const double iT = EXACT ? 0.0 : 1.0 / T;
   double Ycell;
   if (EXACT) {

@@ -198,7 +198,7 @@ __global__ void k_node_density(DevConsts k, const int32_t* qc, double* nnd, int 
       if (slot == 0) {
         // the cell density n = Fn N / V as the moment finalisation forms
         // it, from the cell's count (so the deposit needs no moment pass)
-        const double ncv = 1 * k.Fn * (double)ccnt[c] / cell_volume(c, k);
+        const double ncv = (k.cell_w ? k.cell_w[c] : 1) * k.Fn * (double)ccnt[c] / cell_volume(c, k);
         sur_hi_lo(10.0 * (k.b * ncv - 0.25), xc[4], xc[10]);
         xc[5] = __float2bfloat16_rn(1.0f);
         for (int q = 11; q < 16; ++q) xc[q] = __float2bfloat16_rn(0.0f);

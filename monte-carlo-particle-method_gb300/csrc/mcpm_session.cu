@@ -712,6 +712,7 @@ static uint64_t graph_signature(const mcpm_session* s, uint32_t stages) {
   mix((uint64_t)s->sur_active);
   mix((uint64_t)s->N);  // the particle count changes with splits and deletions
   mix((uint64_t)s->press);
+  mix((uint64_t)(uintptr_t)s->k.cell_w);
   return h;
 }
 
@@ -1103,6 +1104,7 @@ static int weights_alloc(mcpm_session* s) {
   std::vector<int32_t> one(cap > C ? cap : C, 1);
   cudaMemcpy(s->pw, one.data(), cap * 4, cudaMemcpyHostToDevice);
   cudaMemcpy(s->cw, one.data(), C * 4, cudaMemcpyHostToDevice);
+  s->k.cell_w = s->cw;
   return cuda_check(s, cudaGetLastError(), "weights");
 }
 

@@ -124,7 +124,7 @@ int read_raw(const char* path, Raw& r, char* msg, int32_t msg_len) {
   }
   std::fclose(f);
   if (rc) return set_msg(msg, msg_len, err, rc);
-  if (r.Len[0] < 0.0) return set_msg(msg, msg_len, "settings: box_len is required", MCPM_ERR_ARG);
+  if (r.Len[0] < 0.0) r.Len[0] = r.Len[1] = r.Len[2] = 1.0;  // src/myIO.cpp:2163-2166
   if (r.cells[0] < 1 || r.cells[1] < 1 || r.cells[2] != 1)
     return set_msg(msg, msg_len, "settings: num_cells must be N0 N1 1", MCPM_ERR_ARG);
   if (r.N < 1) return set_msg(msg, msg_len, "settings: N (particles) is required", MCPM_ERR_ARG);

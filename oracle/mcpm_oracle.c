@@ -37,6 +37,7 @@ struct orc_state {
   double* inj;       /* 3N injected normals */
   double* xi;        /* 3N whitened normals (random_generator output) */
   double* nn;        /* [C][4] nodal densities n_n of the last cell_update */
+  int32_t* cw;       /* [C] cells[].n_ratio once set, else NULL (1) */
 };
 
 /* ------------------------------------------------------------------ RNG -- */
@@ -207,10 +208,14 @@ orc_state* orc_create(const mcpm_config* cfg, int64_t n_particles) {
 void orc_destroy(orc_state* s) {
   if (!s) return;
   free(s->cell); free(s->cnt); free(s->off); free(s->list); free(s->index);
-  free(s->inj); free(s->xi); free(s->nn); free(s);
+  free(s->inj); free(s->xi); free(s->nn); free(s->cw); free(s);
 }
 
 int orc_num_cells(const orc_state* s) { return s->C; }
+void orc_set_cell_weights(orc_state* s, const int32_t* cw) {
+  if (!s->cw) s->cw = (int32_t*)malloc(sizeof(int32_t) * (size_t)s->C);
+  memcpy(s->cw, cw, sizeof(int32_t) * (size_t)s->C);
+}
 void orc_get_cells(const orc_state* s, double* out) {
   memcpy(out, s->cell, sizeof(double) * (size_t)s->C * CF);
 }
@@ -438,7 +443,7 @@ static void moments(orc_state* s, const double* U1, const double* U2,
     CELL(s, num, MCPM_CF_DM2) = DM2;
     CELL(s, num, MCPM_CF_DM4) = DM4;
     double T = g->m * DM2 / (3.0 * g->kb);
-    double n = 1 * g->Fn * weight / cell_volume(s, num);
+    double n = (s->cw ? s->cw[num] : 1) * g->Fn * weight / cell_volume(s, num);
     CELL(s, num, MCPM_CF_T) = T;
     CELL(s, num, MCPM_CF_N) = n;
     double Y = Ycoll(s, n);

@@ -28,6 +28,9 @@ typedef struct orc_state orc_state;
 orc_state* orc_create(const mcpm_config* cfg, int64_t n_particles);
 void orc_destroy(orc_state* s);
 int orc_num_cells(const orc_state* s);
+/* cells[].n_ratio: the weight in the cell density n = n_ratio Fn N / V
+   (src/Main_Functions.cpp:2588); 1 until set */
+void orc_set_cell_weights(orc_state* s, const int32_t* cw);
 /* [C][MCPM_CF_COUNT] cell-major copy of the per-cell fields */
 void orc_get_cells(const orc_state* s, double* out_cell_major);
 void orc_set_cell_field(orc_state* s, int field, const double* values);

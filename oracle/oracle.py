@@ -45,6 +45,7 @@ def _load_oracle():
         "orc_create": (vp, [C.POINTER(Config), C.c_int64]),
         "orc_destroy": (None, [vp]),
         "orc_num_cells": (C.c_int, [vp]),
+        "orc_set_cell_weights": (None, [vp, ip]),
         "orc_get_cells": (None, [vp, dp]),
         "orc_set_cell_field": (None, [vp, C.c_int, dp]),
         "orc_get_step": (C.c_int, [vp]),
@@ -237,6 +238,11 @@ class Oracle:
     def init_omega_max(self):
         self.L.orc_init_omega_max(self.h)
 
+    def set_cell_weights(self, cw):
+        """cells[].n_ratio (the weight in the cell density)"""
+        self._cw = np.ascontiguousarray(cw, dtype=np.int32)
+        self.L.orc_set_cell_weights(self.h, _ip(self._cw))
+
     def measure_pressure(self, p_m):
         """measure_pressure (src/Main_Functions.cpp:13-34) added into p_m [C]"""
         s = self.s
@@ -348,6 +354,7 @@ def ref_lib(build=True):
         "ref_long_range_2d": (None, [vp, dp, dp, dp, dp, ip]),
         "ref_get_node_density": (None, [vp, dp]),
         "ref_measure_pressure": (None, [vp, dp, dp, dp, dp]),
+        "ref_set_cell_weights": (None, [vp, ip]),
         "ref_write_post": (None, [vp, C.c_int, C.c_double, C.c_char_p, C.c_char_p, dp, dp, dp, dp, dp, dp, ip]),
         "ref_post_text": (C.c_long, [vp, C.c_int, dp, dp, dp, dp, dp, dp, ip, C.c_char_p, C.c_long]),
         "ref_thermostat": (None, [vp, dp, dp, dp, dp, ip, C.c_double, C.c_double, C.c_double, C.c_double]),
@@ -438,6 +445,10 @@ class Reference:
     def esmc(self):
         s = self.s
         self.L.ref_esmc(self.h, _dp(s.U1), _dp(s.U2), _dp(s.U3), _dp(s.x1), _dp(s.x2), _ip(s.index))
+
+    def set_cell_weights(self, cw):
+        self._cw = np.ascontiguousarray(cw, dtype=np.int32)
+        self.L.ref_set_cell_weights(self.h, _ip(self._cw))
 
     def measure_pressure(self):
         """the reference's measure_pressure; returns its cells' p_m (cumulative)"""

@@ -340,6 +340,13 @@ void ref_init_omega_max(void* h) {
   }
 }
 
+// cells[].n_ratio of the harness's cells (make_cells sets 1 outside the
+// interface problems)
+void ref_set_cell_weights(void* h, const int* cw) {
+  Ref* r = (Ref*)h;
+  for (int c = 0; c < r->C; ++c) r->cells[c].n_ratio = cw[c];
+}
+
 // thermostat (src/Main_Functions.cpp:1674) in its live branch, problem
 // inverted, on the lists of the last ref_cell_update
 void ref_thermostat(void* h, double* U1, double* U2, double* U3, double* x2, int* index, double Tc, double Th,

@@ -33,6 +33,28 @@ def _need_ref():
         pytest.skip("reference sources not present")
 
 
+def test_weighted_cell_density_bit_exact_against_reference():
+    """cells[].n_ratio enters the cell density, n = n_ratio Fn N / V
+    (src/Main_Functions.cpp:2588), and every quantity built on it"""
+    _need_ref()
+    cfg, parts = _slab()
+    cw = np.where(np.arange(cfg.n_cells[1]) < 10, 3, 1).astype(np.int32)
+    o, r = Oracle(cfg, parts), Reference(cfg, parts)
+    for x in (o, r):
+        x.set_cell_weights(cw)
+        x.set_step(2)
+        x.cell_update()
+    # every field but the kernel smoothing, which the oracle forms for its
+    # one consumer (long_range 2) only
+    ns = mcpm.CF["N_SMOOTH"]
+    assert np.array_equal(o.cells()[:, :ns], r.cells()[:, :ns])
+    o1 = Oracle(cfg, parts)
+    o1.set_step(2)
+    o1.cell_update()
+    n, n1 = mcpm.cell_field(o.cells(), "N", True), mcpm.cell_field(o1.cells(), "N", True)
+    assert np.allclose(n / n1, cw, rtol=1e-15)
+
+
 def test_thermostat_bit_exact_against_reference():
     _need_ref()
     cfg, parts = _slab()

@@ -114,3 +114,30 @@ def test_addremove_refuses_beyond_capacity(cuda_ok):
     s.set_particle_weights(np.ones(N, dtype=np.int32))
     assert s.addremove_particles(g) == N
     s.close()
+
+
+def test_weighted_cell_density_matches_oracle(cuda_ok):
+    """cells[].n_ratio in the cell density n = n_ratio Fn N / V
+    (src/Main_Functions.cpp:2588) and what is built on it (Y, gamma*, the
+    drift coefficients)"""
+    cfg, parts = _slab(mcpm.FP64)
+    C = cfg.n_cells[1]
+    cw = np.where(np.arange(C) < C // 2, 3, 1).astype(np.int32)
+    s = mcpm.Session(cfg)
+    s.upload(parts["x1"], parts["x2"], parts["U1"], parts["U2"], parts["U3"])
+    s.set_cell_weights(cw)
+    o = Oracle(cfg, parts)
+    o.set_cell_weights(cw)
+    for x in (s, o):
+        x.set_step(2)
+        x.cell_update()
+    cg, co = s.get_cells(), o.cells()
+    for f in ("N", "T", "GAMMA_ST"):
+        a, b = mcpm.cell_field(cg, f), mcpm.cell_field(co, f, True)
+        assert np.max(np.abs(a - b)) <= 1e-12 * np.max(np.abs(b)), f
+    for f in ("C", "GAMMA", "ALPHA", "BETA"):
+        a, b = mcpm.cell_field(cg, f), mcpm.cell_field(co, f, True)
+        assert np.max(np.abs(a - b)) <= 1e-9 * max(np.max(np.abs(b)), 1e-300), f
+    n = mcpm.cell_field(cg, "N")
+    assert n[0] > 0 and np.all(n[: C // 2] > 0)
+    s.close()
