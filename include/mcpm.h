@@ -238,6 +238,15 @@ int mcpm_upload_particles(mcpm_session* s, int64_t n, const double* x1,
 int mcpm_upload_particles_async(mcpm_session* s, int64_t n, const double* x1,
                                 const double* x2, const double* U1,
                                 const double* U2, const double* U3);
+/* The positions before the last flight (the reference's x1_old, x2_old,
+   particle-id order), for sessions with diffuse walls, which read them:
+   an upload starts them as the positions themselves.  x1_old may be NULL
+   when direction[0] == 0.  No effect where nothing reads them. */
+int mcpm_set_old_positions(mcpm_session* s, const double* x1_old, const double* x2_old);
+/* The positions before the last flight as the walls left them (diffuse
+   walls move them to the wall crossing), particle-id order; sessions that
+   keep them only (diffuse walls, pressure sampling). */
+int mcpm_get_old_positions(mcpm_session* s, double* x1_old, double* x2_old);
 /* Copies the device state back into caller arrays, in particle-id order.
    When x1 never changes (direction[0] == 0 and not ESMC) the device does not
    keep it and the caller's x1 is left untouched. */

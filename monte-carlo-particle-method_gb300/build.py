@@ -20,6 +20,9 @@ REPO = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libmcpm.so")
+# the reference's own routine signatures over the C-ABI (compat/reference_surface.cpp)
+REF_LIB = os.path.join(HERE, "libmcpm_ref.so")
+REF_SRC = [os.path.join(HERE, "compat", f) for f in ("reference_surface.cpp", "ref_layout.h")]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "--fmad=false", "-Xcompiler", "-fPIC,-O2,-ffp-contract=off",
@@ -73,6 +76,10 @@ def build(force=False, verbose=False):
             logs = list(ex.map(comp, todo))
     if todo or not os.path.exists(LIB):
         _run([cc, *ARCH, "-shared", "-o", LIB, *objs])
+    if (not os.path.exists(REF_LIB) or os.path.getmtime(REF_LIB) <
+            max(os.path.getmtime(LIB), hdr_t, *(os.path.getmtime(f) for f in REF_SRC))):
+        _run([os.environ.get("CXX", "g++"), "-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-Wall", "-shared",
+              "-o", REF_LIB, REF_SRC[0], "-L" + HERE, "-lmcpm", "-Wl,-rpath,$ORIGIN"])
     if verbose:
         for l in logs:
             if l.strip():

@@ -292,7 +292,11 @@ int launch_pressure(Session& s);
 // one staged upload field (0..4: x1 x2 U1 U2 U3; field 2 also sets the ids)
 // on stream st
 int launch_convert_field(Session& s, int field, int64_t n, cudaStream_t st);
-// one download field (0..4) into particle-id order in the stage, from the
+// a staged field in particle-id order (doubles) into dst, a field of the
+// current packed layout's slots
+int launch_gather_field(Session& s, void* dst, const double* src);
+// one download field (0..4: x1 x2 U1 U2 U3, 5..6: x1_old x2_old) into
+// particle-id order in the stage, from the
 // current layout (packed or slotted)
 int launch_convert_out_field(Session& s, int field, int64_t n);
 // the staging of a download straight from a slotted layout (FP32 sessions)

@@ -745,9 +745,17 @@ __device__ void gauss_jordan_fast(double* A, double* R, double* x) {
 // on the 12x12 performs exactly the arithmetic of the three 4x4 solves),
 // c/gamma (src/Fokker_Planck.cpp:590-804, 9x9), phi (:2734-2746) and the
 // Velocity_FP_parallel constants A1..A3 (src/Fokker_Planck.cpp:1099-1112).
+// Launch shape of the per-cell solves: threads per block and blocks resident
+// per SM (the register budget).
+#ifndef MCPM_SOLVE_T
+#define MCPM_SOLVE_T 128
+#endif
+#ifndef MCPM_SOLVE_MINB
+#define MCPM_SOLVE_MINB 1
+#endif
 template <bool EXACT>
-__global__ void __launch_bounds__(128) k_solve(DevConsts k, double* cell, float* pcell, int with_alpha,
-                                               int fp_model, uint32_t* status) {
+__global__ void __launch_bounds__(MCPM_SOLVE_T, MCPM_SOLVE_MINB)
+    k_solve(DevConsts k, double* cell, float* pcell, int with_alpha, int fp_model, uint32_t* status) {
   const int C = k.C;
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= C) return;
@@ -809,6 +817,9 @@ __global__ void __launch_bounds__(128) k_solve(DevConsts k, double* cell, float*
   W(MCPM_CF_T, T);
   W(MCPM_CF_N, n);
   W(CFI_Y, Ycell);
+  // scale_mu(T) (src/Main_Functions.cpp:1970-1973), which the reference
+  // evaluates again for Lambda, the c/gamma rhs and the FP constants: once
+  const double mu_T = scale_mu(T, k);
   double gst = R(MCPM_CF_GAMMA_ST);
   if (weight > 1e-14) {
     gst = EXACT ? -0.001 * (n * k.b * Ycell / (k.kb * T / k.m)) : -0.001 * (n * k.b * Ycell) * (k.q_m_kb * iT);
@@ -817,7 +828,7 @@ __global__ void __launch_bounds__(128) k_solve(DevConsts k, double* cell, float*
   uint32_t bad = 0;
   double Lam = R(MCPM_CF_LAMBDA);
   if (weight > 1e-14) {
-    double mu = scale_mu(T, k);
+    const double mu = mu_T;
     if (EXACT) {
       double tau = 2.0 * mu / (n * k.kb * T);
       double L = (P[0] - DM2 / 3.0) * ((P[3] - DM2 / 3.0) * (P[5] - DM2 / 3.0) - P[4] * P[4]);
@@ -981,7 +992,7 @@ __global__ void __launch_bounds__(128) k_solve(DevConsts k, double* cell, float*
 #undef AA
       double Pr = 2.0 / 3.0;
       double Y = (k.model == MCPM_MODEL_FP_DENSE) ? Ycell : 1.0;
-      double mu = scale_mu(T, k);
+      const double mu = mu_T;
       for (int j = 0; j < 6; ++j) rhs[j] = -2.0 * Lam * M4[j];
       if (EXACT) {
         double tau = 2.0 * mu / (n * k.kb * T);
@@ -1002,7 +1013,7 @@ __global__ void __launch_bounds__(128) k_solve(DevConsts k, double* cell, float*
     for (int j = 0; j < 3; ++j) W(MCPM_CF_GAMMA + j, x[6 + j]);
     // ---------------- Velocity_FP_parallel per-cell constants
     if (ncnt > 1) {
-      double mu = scale_mu(T, k);
+      const double mu = mu_T;
       double Y = (k.model == MCPM_MODEL_FP_DENSE) ? Ycell : 1.0;
       if (EXACT) {
         double tau = 2.0 * mu / (n * k.kb * T);
@@ -1994,12 +2005,19 @@ __global__ void k_convert_field(real* dst, const double* src, int32_t* pid, int6
     if (pid) pid[i] = (int32_t)i;
   }
 }
+// a staged field in particle-id order into the slots of a packed layout
+template <typename real>
+__global__ void k_gather_field(real* dst, const double* src, const int32_t* pid, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    dst[i] = (real)src[pid[i]];
+}
 template <typename real>
 __global__ void k_convert_out_field(PT<real> p, PT<real> ovf, const int32_t* ovf_n, const int32_t* off,
                                     const int32_t* dcur, int C, int f, double* dst, int64_t n) {
   const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x, nt = (int64_t)gridDim.x * blockDim.x;
   auto field = [&](const PT<real>& src) -> const real* {
-    return f == 0 ? src.x1 : f == 1 ? src.x2 : f == 2 ? src.U1 : f == 3 ? src.U2 : src.U3;
+    return f == 0 ? src.x1 : f == 1 ? src.x2 : f == 2 ? src.U1 : f == 3 ? src.U2 : f == 4 ? src.U3
+                                                                        : f == 5 ? src.x1o : src.x2o;
   };
   const real* v = field(p);
   if (!dcur) {
@@ -2109,10 +2127,11 @@ int launch_solve(Session& s, int with_alpha) {
   int fp = (m == MCPM_MODEL_FP_DENSE || m == MCPM_MODEL_FP_IDEAL_GAS || m == MCPM_MODEL_FP_LINEAR) ? 1 : 0;
   // the FP64 path reproduces the reference's solve exactly; the FP32 path
   // runs the leaner FP64 variant
+  const int nb = (s.C + MCPM_SOLVE_T - 1) / MCPM_SOLVE_T;
   if (s.prec == MCPM_FP32)
-    k_solve<false><<<(s.C + 127) / 128, 128, 0, s.stream>>>(s.k, s.cell, s.pcell, with_alpha, fp, s.status);
+    k_solve<false><<<nb, MCPM_SOLVE_T, 0, s.stream>>>(s.k, s.cell, s.pcell, with_alpha, fp, s.status);
   else
-    k_solve<true><<<(s.C + 127) / 128, 128, 0, s.stream>>>(s.k, s.cell, nullptr, with_alpha, fp, s.status);
+    k_solve<true><<<nb, MCPM_SOLVE_T, 0, s.stream>>>(s.k, s.cell, nullptr, with_alpha, fp, s.status);
   return 1;
 }
 
@@ -2206,11 +2225,19 @@ template <typename real> static int conv_field_impl(Session& s, int f, int64_t n
 int launch_convert_field(Session& s, int field, int64_t n, cudaStream_t st) {
   return s.prec == MCPM_FP32 ? conv_field_impl<float>(s, field, n, st) : conv_field_impl<double>(s, field, n, st);
 }
+int launch_gather_field(Session& s, void* dst, const double* src) {
+  const PBuf& b = s.P[s.cur];
+  if (s.prec == MCPM_FP32)
+    k_gather_field<float><<<grid_for(s.N, 256, s.num_sms * 8), 256, 0, s.stream>>>((float*)dst, src, b.pid, s.N);
+  else
+    k_gather_field<double><<<grid_for(s.N, 256, s.num_sms * 8), 256, 0, s.stream>>>((double*)dst, src, b.pid, s.N);
+  return 1;
+}
 template <typename real> static int conv_out_field_impl(Session& s, int f, int64_t n) {
   const bool sl = s.slotted;
   k_convert_out_field<real><<<s.num_sms * 8, 256, 0, s.stream>>>(
       pt<real>(s.P[s.cur]), pt<real>(s.ovf), sl ? s.ovf_n + (1 - s.ovf_par) : nullptr, s.off, sl ? s.dcur : nullptr,
-      s.C, f, s.stage + (size_t)f * s.cap, n);
+      s.C, f, s.stage + (size_t)(f < 5 ? f : f - 5) * s.cap, n);  // old positions: the first two slices
   return 1;
 }
 int launch_convert_out_field(Session& s, int field, int64_t n) {

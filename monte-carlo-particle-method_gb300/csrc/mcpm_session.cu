@@ -498,6 +498,45 @@ int mcpm_upload_particles_async(mcpm_session* s, int64_t n, const double* x1, co
   return upload_enqueue(s, n, x1, x2, U1, U2, U3);
 }
 
+int mcpm_set_old_positions(mcpm_session* s, const double* x1_old, const double* x2_old) {
+  if (!s || !x2_old || !s->have_particles) return fail(s, MCPM_ERR_ARG, "set_old_positions: bad arguments");
+  int rc;
+  if (s->slotted && (rc = leave_slotted(s))) return rc;
+  const PBuf& P = s->P[s->cur];
+  if (!P.x2o) return MCPM_OK;  // the session keeps no old positions (nothing reads them)
+  const size_t b = (size_t)s->N * 8;
+  cudaStreamWaitEvent(s->stream, s->ev_in_free, 0);
+  const double* src[2] = {x1_old, x2_old};
+  void* dst[2] = {P.x1o, P.x2o};
+  int k = 0;
+  for (int f = 0; f < 2; ++f) {
+    if (!src[f] || !dst[f]) continue;
+    cudaMemcpyAsync(s->stage_in + (size_t)f * s->cap, src[f], b, cudaMemcpyHostToDevice, s->stream);
+    k += launch_gather_field(*s, dst[f], s->stage_in + (size_t)f * s->cap);
+  }
+  cudaEventRecord(s->ev_in_free, s->stream);
+  if ((rc = after_launch(s, k, "set_old_positions"))) return rc;
+  return cuda_check(s, cudaStreamSynchronize(s->stream), "set_old_positions");
+}
+
+int mcpm_get_old_positions(mcpm_session* s, double* x1_old, double* x2_old) {
+  if (!s || !x2_old || !s->have_particles) return fail(s, MCPM_ERR_ARG, "get_old_positions: bad arguments");
+  const PBuf& P = s->P[s->cur];
+  if (!P.x2o) return fail(s, MCPM_ERR_STATE, "get_old_positions: the session keeps no old positions");
+  const size_t cap = (size_t)s->cap, b = (size_t)s->N * 8;
+  cudaStreamWaitEvent(s->stream, s->ev_out_free, 0);
+  double* dst[2] = {P.x1o ? x1_old : nullptr, x2_old};
+  int k = 0;
+  for (int f = 0; f < 2; ++f) {
+    if (!dst[f]) continue;
+    k += launch_convert_out_field(*s, 5 + f, s->N);
+    cudaMemcpyAsync(dst[f], s->stage + (5 + f - 5) * cap, b, cudaMemcpyDeviceToHost, s->stream);
+  }
+  int rc = after_launch(s, k, "get_old_positions");
+  if (rc) return rc;
+  return cuda_check(s, cudaStreamSynchronize(s->stream), "get_old_positions");
+}
+
 // the download's conversions and copies, without waiting for them
 static int download_enqueue(mcpm_session* s, int64_t n, double* x1, double* x2, double* U1, double* U2, double* U3) {
   if (!s || n != s->N || !x2 || !U1 || !U2 || !U3) return fail(s, MCPM_ERR_ARG, "download: bad arguments");

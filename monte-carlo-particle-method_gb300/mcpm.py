@@ -158,6 +158,8 @@ def load_library(path: str | None = None):
         "mcpm_download_particles": (C.c_int, [vp, i64, dp, dp, dp, dp, dp]),
         "mcpm_download_particles_async": (C.c_int, [vp, i64, dp, dp, dp, dp, dp]),
         "mcpm_upload_particles_async": (C.c_int, [vp, i64, dp, dp, dp, dp, dp]),
+        "mcpm_set_old_positions": (C.c_int, [vp, dp, dp]),
+        "mcpm_get_old_positions": (C.c_int, [vp, dp, dp]),
         "mcpm_cell_update": (C.c_int, [vp]),
         "mcpm_random_generator": (C.c_int, [vp]),
         "mcpm_velocity_update": (C.c_int, [vp]),
@@ -304,6 +306,22 @@ class Session:
             out["x1"][:] = 0.0
         self._ck(self.lib.mcpm_download_particles(self.h, n, _dp(out["x1"]), _dp(out["x2"]), _dp(out["U1"]),
                                                   _dp(out["U2"]), _dp(out["U3"])), "download_particles")
+        return out
+
+    def set_old_positions(self, x1_old, x2_old):
+        """The reference's x1_old / x2_old into the session (the walls and the
+        pressure count read them)."""
+        n = self.N
+        self._old = [_f64(x1_old, n) if x1_old is not None else None, _f64(x2_old, n)]
+        a, b = self._old
+        self._ck(self.lib.mcpm_set_old_positions(self.h, _dp(a) if a is not None else None, _dp(b)),
+                 "set_old_positions")
+
+    def get_old_positions(self):
+        n = self.N
+        out = {"x1_old": np.zeros(n), "x2_old": np.empty(n)}
+        self._ck(self.lib.mcpm_get_old_positions(self.h, _dp(out["x1_old"]), _dp(out["x2_old"])),
+                 "get_old_positions")
         return out
 
     # -- the reference routines
