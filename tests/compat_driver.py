@@ -206,7 +206,18 @@ class MainLoop:
         p, s = self._p, self.st
         self.r["measure_pressure"](p(self.U2), p(self.x2), p(self.x2o), s.gas, s.box, s.cells)
 
-    def iteration(self, step, pressure=False):
+    def layout(self):
+        """(pid_by_slot, off) of the session behind the routines: the in-cell
+        order of its last cell_update"""
+        lib = mcpm.load_library()
+        pid = np.empty(self.N, dtype=np.int32)
+        off = np.empty(self.st.C + 1, dtype=np.int32)
+        rc = lib.mcpm_get_layout(self.L.mcpm_compat_session(), pid.ctypes.data_as(C.POINTER(C.c_int32)),
+                                 off.ctypes.data_as(C.POINTER(C.c_int32)))
+        assert rc == 0, rc
+        return pid, off
+
+    def iteration(self, step, pressure=False, after_cell_update=None):
         """src/main.cpp:392-514 for the particle step (no shock / hybrid
         branches): cell_update, the FP draws, velocity_update,
         DFP_extra_streaming, apply_BC, store_old_positions,
@@ -214,6 +225,8 @@ class MainLoop:
         m = self.cfg.model
         self.set_step(step)
         self.cell_update()
+        if after_cell_update is not None:
+            after_cell_update()
         if m in (mcpm.MODEL_FP_DENSE, mcpm.MODEL_FP_IDEAL_GAS):
             self.random_generator()
         self.velocity_update()

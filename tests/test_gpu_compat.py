@@ -8,10 +8,9 @@ particles -- positions and velocities within 1e-9 (the moment sums run in
 another order), the index[] and the per-cell lists (cells[].indices_inside,
 ascending ids) exactly, the CELLS moments within 1e-9 and the pressure
 count (cells[].p_m) within 1e-9.  Pair models (ESMC, DSMC_VHS), whose pairs
-follow the in-cell order of the device layout: three iterations against the
-same calls made on a session through the Python API, bit for bit -- every
-array, the old positions, index[], the CELLS fields and the majorant the
-reference keeps in cells[].omega_max / cells[].crm."""
+follow the in-cell order of the device layout (the oracle is handed that
+order after each cell_update): the same, with the majorant the reference
+keeps in cells[].omega_max / cells[].crm within 1e-12."""
 import ctypes
 
 import numpy as np
@@ -112,86 +111,55 @@ def test_reference_loop_fp_vs_oracle(cuda_ok, name):
         ml.close()
 
 
-def _mirror(cfg, parts, om):
-    """The calls the routines make, made on a session through the Python API."""
-    s = mcpm.Session(cfg)
-    h = {k: np.ascontiguousarray(parts[k], dtype=np.float64).copy() for k in ("x1", "x2", "U1", "U2", "U3")}
-    old = {"x1_old": h["x1"].copy(), "x2_old": h["x2"].copy()}
-    need_old = cfg.problem in (mcpm.PROBLEM_COUETTE, mcpm.PROBLEM_WALL)
-    p_m = np.zeros(cfg.n_cells[0] * cfg.n_cells[1])
-    cells = index = None
-
-    def bc():
-        nonlocal h, old
-        if need_old:
-            s.set_old_positions(old["x1_old"], old["x2_old"])
-        s.apply_BC()
-        h = s.download()
-        if need_old:
-            old = s.get_old_positions()
-
-    for step in range(1, K + 1):
-        s.upload(h["x1"], h["x2"], h["U1"], h["U2"], h["U3"])
-        s.set_step(step)
-        s.cell_update()
-        index = s.get_index()
-        cells = s.get_cells()
-        if step == 1:
-            s.set_cell_field(mcpm.CF["OMEGA_MAX"], om)
-        s.velocity_update()
-        h = s.download()
-        bc()
-        s.store_old_positions()
-        old = {"x1_old": h["x1"].copy(), "x2_old": h["x2"].copy()}
-        s.stream_particles()
-        h = s.download()
-        bc()
-        if step == 1:
-            s.set_pressure_sampling(True)
-        s.set_old_positions(None, old["x2_old"])
-        s.reset_pressure()
-        s.measure_pressure()
-        p_m += s.get_pressure()
-        bc()
-    after = s.get_cells()
-    s.close()
-    return h, old, index, cells, after, p_m
-
-
 @pytest.mark.parametrize("name", ["esmc_couette", "dsmc_periodic"])
-def test_reference_loop_pairs_vs_session(cuda_ok, name):
+def test_reference_loop_pairs_vs_oracle(cuda_ok, name):
     cfg, parts = _case(name)
-    # the majorant the reference's main sets before its loop (src/main.cpp:236-269)
-    s0 = mcpm.Session(cfg)
-    s0.upload(parts["x1"], parts["x2"], parts["U1"], parts["U2"], parts["U3"])
-    s0.set_step(0)
-    s0.cell_update()
-    s0.init_omega_max()
-    om = mcpm.cell_field(s0.get_cells(), "OMEGA_MAX").copy()
-    s0.close()
-    h, old, index, cells, after, p_m = _mirror(cfg, parts, om)
-
     ml = MainLoop(cfg, parts)
+    o = Oracle(cfg, parts)
+    # the majorant the reference's main sets before its loop (src/main.cpp:236-269)
+    o.set_step(0)
+    o.cell_update()
+    o.init_omega_max()
+    om = mcpm.cell_field(o.cells(), "OMEGA_MAX", True).copy()
     field = "crm" if cfg.model == mcpm.MODEL_DSMC_VHS else "omega_max"
+    p_o = np.zeros(ml.st.C)
     try:
         for c in range(ml.st.C):
             ml.st.put(ml.st.cell(c), "CELLS." + field, ctypes.c_double, float(om[c]))
+
         for step in range(1, K + 1):
-            ml.iteration(step, pressure=True)
-        for k in ("x1", "x2", "U1", "U2", "U3"):
-            assert np.array_equal(getattr(ml, k), h[k]), k
-        if cfg.problem == mcpm.PROBLEM_COUETTE:
-            assert np.array_equal(ml.x1o, old["x1_old"]) and np.array_equal(ml.x2o, old["x2_old"])
-        assert np.array_equal(ml.index, index)
-        _check_lists(ml)
-        for ref_name, cf, w in CELL_FIELDS:
-            a = ml.st.field(ref_name, w)
-            b = cells[mcpm.CF[cf]:mcpm.CF[cf] + w].T
-            assert np.array_equal(a, b), ref_name
-        assert np.array_equal(ml.st.field(field)[:, 0], mcpm.cell_field(after, "OMEGA_MAX"))
-        assert np.array_equal(ml.st.field("p_m")[:, 0], p_m)
+            def oracle_cell_update():
+                # the oracle's pairs follow the device's in-cell order
+                pid, off = ml.layout()
+                o.set_step(step)
+                o.cell_update()
+                o.set_layout(off, pid)
+                if step == 1:
+                    o.set_cell_field(mcpm.CF["OMEGA_MAX"], om)
+
+            ml.iteration(step, pressure=True, after_cell_update=oracle_cell_update)
+            (o.esmc if cfg.model == mcpm.MODEL_ESMC else o.dsmc)()
+            o.apply_bc(0)
+            o.store_old_positions()
+            o.stream()
+            o.apply_bc(1)
+            o.measure_pressure(p_o)
+            o.apply_bc(2)
+            for k in ("x1", "x2", "U1", "U2", "U3"):
+                if k == "x1" and cfg.direction[0] == 0:
+                    continue
+                assert _rel(getattr(ml, k), getattr(o.s, k)) <= 1e-10, (step, k)
+            if cfg.problem == mcpm.PROBLEM_COUETTE:
+                assert _rel(ml.x1o, o.s.x1o) <= 1e-10 and _rel(ml.x2o, o.s.x2o) <= 1e-10
+            assert np.array_equal(ml.index, o.s.index), step
+            _check_lists(ml)
+            co = o.cells()
+            for ref_name, cf, w in CELL_FIELDS:
+                assert _rel(ml.st.field(ref_name, w), co[:, mcpm.CF[cf]:mcpm.CF[cf] + w]) <= 1e-9, (step, ref_name)
+            om_o = mcpm.cell_field(co, "OMEGA_MAX", True)
+            assert np.max(np.abs(ml.st.field(field)[:, 0] - om_o)) <= 1e-12 * max(1.0, np.max(om_o)), step
+        assert _rel(ml.st.field("p_m")[:, 0], p_o) <= 1e-9
         # the collisions moved velocities
         assert np.count_nonzero(ml.U1 != parts["U1"]) > 0.05 * ml.N
     finally:
         ml.close()
-
