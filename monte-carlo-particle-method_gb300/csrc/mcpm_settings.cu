@@ -5,8 +5,8 @@
 // run's constants: cell sizes, Fn, the hard-sphere or VHS diameter and
 // reference speed from the viscosity, b, mu(T0), the mean free path, dt and
 // the attraction strength.  This restates that reading and the derivation
-// along the path the particle step covers (problems closed_box 1 and
-// couette_flow 2; the step's models), in the reference's order of
+// along the path the particle step covers (problems closed_box 1,
+// couette_flow 2 and wall 11; the step's models), in the reference's order of
 // operations, so that a run configured by the reference's own files gets
 // the constants the reference would use.  Host code only.
 #include <cmath>
@@ -55,7 +55,22 @@ struct Raw {
   double U_wall[4] = {-1.0, -1.0, -1.0, -1.0};
   double T_wall[4] = {-1.0, -1.0, -1.0, -1.0};
   double U0[3] = {-1.0, -1.0, -1.0};
+  // problem wall (11): a liquid slab between vapour layers, in units of sigma
+  double nc = -1.0, nv1 = 0.0, nv2 = -1.0, Tc = -1.0;
+  int LcN = -1, LvN = -1, LvN1 = -1, n_ratio = -1;
 };
+
+// readSettingsFile's branch for problem wall (src/myIO.cpp:2628-2726): argon's
+// diameter, the densities given in sigma^-3, a fixed Fn, the particle counts
+// of the lower vapour layer, the liquid slab and the upper vapour layer, and
+// the box height they fill; the gas temperature becomes the liquid's
+struct WallSetup {
+  double sigma, n, Fn, Lv1, Lc, Lv, Len1, T;
+  int Nv1, Nc2, Nv2;
+  long N;
+};
+
+int wall_setup(const Raw& r, WallSetup& w, char* msg, int32_t msg_len);
 
 int set_msg(char* msg, int32_t len, const char* text, int code) {
   if (msg && len > 0) {
@@ -115,6 +130,14 @@ int read_raw(const char* path, Raw& r, char* msg, int32_t msg_len) {
     else if (key == "problem") iss >> r.problem;
     else if (key == "num_cells") iss >> r.cells[0] >> r.cells[1] >> r.cells[2];
     else if (key == "U0") iss >> r.U0[0] >> r.U0[1] >> r.U0[2];
+    else if (key == "nc") iss >> r.nc;
+    else if (key == "nv1") iss >> r.nv1;
+    else if (key == "nv2") iss >> r.nv2;
+    else if (key == "Tc") iss >> r.Tc;
+    else if (key == "LcN") iss >> r.LcN;
+    else if (key == "LvN") iss >> r.LvN;
+    else if (key == "LvN1") iss >> r.LvN1;
+    else if (key == "n_ratio") iss >> r.n_ratio;
     else if (key.rfind("U_wall_", 0) == 0 || key.rfind("T_wall_", 0) == 0) {
       const int w = key[7] - '1';
       if (w >= 0 && w < 4) iss >> (key[0] == 'U' ? r.U_wall[w] : r.T_wall[w]);
@@ -127,8 +150,10 @@ int read_raw(const char* path, Raw& r, char* msg, int32_t msg_len) {
   if (r.Len[0] < 0.0) r.Len[0] = r.Len[1] = r.Len[2] = 1.0;  // src/myIO.cpp:2163-2166
   if (r.cells[0] < 1 || r.cells[1] < 1 || r.cells[2] != 1)
     return set_msg(msg, msg_len, "settings: num_cells must be N0 N1 1", MCPM_ERR_ARG);
-  if (r.N < 1) return set_msg(msg, msg_len, "settings: N (particles) is required", MCPM_ERR_ARG);
-  if (r.delta_dim[0] < 0.0) {
+  if (r.problem < 0) r.problem = 1;
+  if (r.problem != 11 && r.N < 1) return set_msg(msg, msg_len, "settings: N (particles) is required", MCPM_ERR_ARG);
+  if (r.delta_dim[0] < 0.0 || r.problem == 11) {
+    // (problem wall sets the cells from the box height it derives)
     for (int i = 0; i < 3; ++i) r.delta_dim[i] = r.Len[i] / r.cells[i];
   } else {
     // the session's cells are Len / N: a box_delta_dim that disagrees would
@@ -143,13 +168,43 @@ int read_raw(const char* path, Raw& r, char* msg, int32_t msg_len) {
   if (r.n < 0.0) r.n = 1e-3;
   if (r.m < 0.0) r.m = 1.0;
   if (r.U0[0] < 0.0) r.U0[0] = r.U0[1] = r.U0[2] = 1.0;
-  if (r.problem < 0) r.problem = 1;
   for (int i = 0; i < 4; ++i)
     if (r.T_wall[i] < 0) r.T_wall[i] = 1.0;
-  if (r.problem != 1 && r.problem != 2)
+  if (r.problem != 1 && r.problem != 2 && r.problem != 11)
     return set_msg(msg, msg_len,
-                   "settings: only problems closed_box (1) and couette_flow (2) configure the particle step",
+                   "settings: only problems closed_box (1), couette_flow (2) and wall (11) configure the particle step",
                    MCPM_ERR_ARG);
+  return MCPM_OK;
+}
+
+int wall_setup(const Raw& r, WallSetup& w, char* msg, int32_t msg_len) {
+  if (!(r.nc > 0.0) || !(r.nv2 > 0.0) || !(r.Tc > 0.0) || r.LcN < 0 || r.LvN < 0)
+    return set_msg(msg, msg_len, "settings: problem wall needs nc, nv2, Tc, LcN and LvN", MCPM_ERR_ARG);
+  // LvN1 < 0 (unset) puts the slab below y = 0 in the reference: refused
+  if (r.LvN1 < 0 || (r.LvN1 > 0 && !(r.nv1 > 0.0)))
+    return set_msg(msg, msg_len, "settings: problem wall needs LvN1 >= 0 (and nv1 when LvN1 > 0)", MCPM_ERR_ARG);
+  const double sigma = 3.405e-10;
+  const double nc = r.nc / std::pow(sigma, 3.0);
+  const double nv1 = r.nv1 / std::pow(sigma, 3.0);
+  const double nv2 = r.nv2 / std::pow(sigma, 3.0);
+  w.sigma = sigma;
+  w.n = nc;
+  w.Lc = r.LcN * sigma;
+  w.Lv = r.LvN * sigma;
+  w.Lv1 = r.LvN1 * sigma;
+  const double Lc_ratio = w.Lc;
+  const int n_ratio = r.n_ratio < 0 ? (int)std::floor(nc / nv2) : r.n_ratio;
+  if (n_ratio < 1) return set_msg(msg, msg_len, "settings: problem wall needs n_ratio >= 1 (or nc >= nv2)", MCPM_ERR_ARG);
+  w.Fn = 0.1e+14;
+  const int sg1 = r.LvN1 > 0 ? 1 : 0;
+  w.Nc2 = (int)std::floor(nc * r.Len[0] * r.Len[2] * (Lc_ratio + 0.5 * (w.Lc - Lc_ratio) * (1 - sg1)) /
+                          (1.0 * n_ratio * w.Fn));
+  w.Nv1 = (int)std::floor(nv1 * r.Len[0] * r.Len[2] * w.Lv1 / w.Fn);
+  w.Nv2 = (int)std::floor(nv2 * r.Len[0] * r.Len[2] * w.Lv / w.Fn);
+  w.N = (long)0 + w.Nc2 + 0 + w.Nv1 + w.Nv2;
+  w.Len1 = w.Lv + w.Lc + w.Lv1;
+  w.T = r.Tc;
+  if (w.N < 1) return set_msg(msg, msg_len, "settings: problem wall gives no particles", MCPM_ERR_ARG);
   return MCPM_OK;
 }
 
@@ -160,7 +215,7 @@ extern "C" int mcpm_config_from_settings(const char* path, mcpm_config* out, int
   if (!path || !out) return set_msg(msg, msg_len, "settings: null argument", MCPM_ERR_ARG);
   Raw r;
   if (int rc = read_raw(path, r, msg, msg_len)) return rc;
-  // ---- the derivation, src/myIO.cpp:2213-2900, problems 1 and 2
+  // ---- the derivation, src/myIO.cpp:2213-2900, problems 1, 2 and 11
   const double pi = std::acos(-1.0);
   const int model = model_code(r.model);
   if (model < 0) return set_msg(msg, msg_len, "settings: the model is outside the particle step", MCPM_ERR_ARG);
@@ -194,7 +249,24 @@ extern "C" int mcpm_config_from_settings(const char* path, mcpm_config* out, int
     crref = (numer / denom) * std::pow(r.kb * 273.0 / r.m, w) / r.mu;
     crref = std::pow(crref, 1.0 / (w * 2.0 - 1.0));
   }
-  const double eqdist = std::pow(2.0, 1.0 / 6.0) * r.sigma;  // :2820-2822
+  double eqdist;
+  double Fn_run = Fn;
+  long N_run = r.N;
+  if (r.problem == 11) {
+    // the wall branch replaces the diameter, density, Fn, N, the box height
+    // and the temperature after crref is set (:2628-2726)
+    WallSetup ws;
+    if (int rc = wall_setup(r, ws, msg, msg_len)) return rc;
+    r.sigma = ws.sigma;
+    eqdist = ws.sigma;
+    r.n = ws.n;
+    Fn_run = ws.Fn;
+    N_run = ws.N;
+    r.Len[1] = ws.Len1;
+    r.T = ws.T;
+  } else {
+    eqdist = std::pow(2.0, 1.0 / 6.0) * r.sigma;  // :2820-2822
+  }
   const double b = 2 * pi * std::pow(r.sigma, 3) / (3.0);
   const double mu = 5.0 / (16.0 * r.sigma * r.sigma) * std::sqrt(r.m * r.kb * T0 / std::acos(-1.0));
   if (r.dt < 0.0) {
@@ -223,12 +295,12 @@ extern "C" int mcpm_config_from_settings(const char* path, mcpm_config* out, int
     c.direction[i] = r.direction[i];
     c.length[i] = r.Len[i];
   }
-  c.problem = r.problem == 1 ? MCPM_PROBLEM_CLOSED_BOX : MCPM_PROBLEM_COUETTE;
+  c.problem = r.problem == 1 ? MCPM_PROBLEM_CLOSED_BOX : r.problem == 2 ? MCPM_PROBLEM_COUETTE : MCPM_PROBLEM_WALL;
   c.model = model;
   // "0 or anything > 3 = no attraction" (src/Main_Functions.cpp:1612-1617)
   c.long_range = (r.long_range >= 1 && r.long_range <= 3) ? r.long_range : MCPM_LR_NONE;
   c.precision = MCPM_FP64;
-  c.sigma = r.sigma; c.m = r.m; c.kb = r.kb; c.n = r.n; c.Fn = Fn;
+  c.sigma = r.sigma; c.m = r.m; c.kb = r.kb; c.n = r.n; c.Fn = Fn_run;
   c.T0 = T0; c.mu = mu; c.visp = r.visp; c.b = b; c.dt = r.dt;
   c.phi = phi; c.eqdist = eqdist;
   // the screened-Poisson constants readSettingsFile sets (SI, :2884-2885)
@@ -239,20 +311,24 @@ extern "C" int mcpm_config_from_settings(const char* path, mcpm_config* out, int
     c.U_wall[i] = r.U_wall[i];
   }
   c.seed = 0x4D43504Dull;
-  c.max_particles = r.N;
+  c.max_particles = N_run;
   c.crref = crref;
   *out = c;
-  if (n_particles) *n_particles = r.N;
+  if (n_particles) *n_particles = N_run;
   return set_msg(msg, msg_len, "", MCPM_OK);
 }
 
-// initialization (src/Main_Functions.cpp:4222-4814), its branch for the
-// problems above: positions uniform along the streaming directions and at
-// mid-box along the others (:4657-4672); velocities normal about U0 with
+// initialization (src/Main_Functions.cpp:4222-4814), its branches for the
+// problems above.  Closed box and Couette: positions uniform along the
+// streaming directions and at mid-box along the others (:4657-4672).  Wall
+// (:4493-4530): x1 as before, x2 uniform in the lower vapour layer for the
+// first Nv1 particles, in the liquid slab for the next Nc2, in the upper
+// vapour layer for the rest.  Velocities normal about U0 with
 // sqrt(kb T / m), T = max(gas.T, max(T_wall_1 + T_wall_2, T_wall_3 + T_wall_4) / 2)
-// (:4790-4799).  The reference seeds its generator from std::random_device;
-// here a 64-bit Mersenne twister seeded by the caller gives the uniforms and
-// Box-Muller pairs the normals, so a seed repeats a run on any host.
+// (:4790-4799; gas.T is the liquid's for the wall problem).  The reference
+// seeds its generator from std::random_device; here a 64-bit Mersenne
+// twister seeded by the caller gives the uniforms and Box-Muller pairs the
+// normals, so a seed repeats a run on any host.
 extern "C" int mcpm_initialize_from_settings(const char* path, uint64_t seed, double* x1, double* x2, double* U1,
                                              double* U2, double* U3, int64_t n_particles, char* msg,
                                              int32_t msg_len) {
@@ -260,12 +336,29 @@ extern "C" int mcpm_initialize_from_settings(const char* path, uint64_t seed, do
     return set_msg(msg, msg_len, "initialize: null argument", MCPM_ERR_ARG);
   Raw r;
   if (int rc = read_raw(path, r, msg, msg_len)) return rc;
+  const bool wall = r.problem == 11;
+  WallSetup ws{};
+  if (wall) {
+    if (int rc = wall_setup(r, ws, msg, msg_len)) return rc;
+    r.N = ws.N;
+    r.Len[1] = ws.Len1;
+    r.T = ws.T;
+  }
   if (n_particles != r.N) return set_msg(msg, msg_len, "initialize: n_particles differs from the file's N", MCPM_ERR_ARG);
   std::mt19937_64 gen(seed);
   auto uni = [&]() { return ((double)(gen() >> 11) + 0.5) * (1.0 / 9007199254740992.0); };
   for (int64_t i = 0; i < r.N; ++i) {
     x1[i] = r.direction[0] == 1 ? uni() * r.Len[0] : 0.5 * r.Len[0];
-    x2[i] = r.direction[1] == 1 ? uni() * r.Len[1] : 0.5 * r.Len[1];
+    if (!wall) {
+      x2[i] = r.direction[1] == 1 ? uni() * r.Len[1] : 0.5 * r.Len[1];
+    } else if (i < ws.Nv1) {
+      x2[i] = uni() * ws.Lv1;
+    } else if (i < ws.Nv1 + ws.Nc2) {
+      // the slab: Lc_ratio = Lc, so the reference's offsets (Lc - Lc_ratio) / 2 vanish
+      x2[i] = ws.Lv1 + uni() * ws.Lc;
+    } else {
+      x2[i] = ws.Lv1 + ws.Lc + uni() * ws.Lv;
+    }
   }
   double T = std::fmax(r.T_wall[0] + r.T_wall[1], r.T_wall[2] + r.T_wall[3]) / 2.0;
   T = std::fmax(r.T, T);

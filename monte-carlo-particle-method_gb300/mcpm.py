@@ -72,7 +72,7 @@ class Config(C.Structure):
 
 def config_from_settings(path: str):
     """readSettingsFile (src/myIO.cpp:1756-3016) through the library: the
-    reference's settings file as (Config, N) for problems 1 and 2."""
+    reference's settings file as (Config, N) for problems 1, 2 and 11."""
     L = load_library()
     cfg, n = Config(), C.c_int64(0)
     msg = C.create_string_buffer(512)

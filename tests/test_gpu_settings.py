@@ -16,8 +16,9 @@ pytestmark = pytest.mark.gpu
 SETTINGS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "settings")
 
 
-def test_settings_drive_the_step(cuda_ok):
-    path = os.path.join(SETTINGS, "reduced_fp_ideal.in")
+@pytest.mark.parametrize("name", ["reduced_fp_ideal.in", "wall_fp_dense.in"])
+def test_settings_drive_the_step(cuda_ok, name):
+    path = os.path.join(SETTINGS, name)
     cfg, N = mcpm.config_from_settings(path)
     parts = mcpm.initialize_from_settings(path, 41, N)
     ses = mcpm.Session(cfg)
@@ -32,5 +33,5 @@ def test_settings_drive_the_step(cuda_ok):
     g = ses.download()
     for k in ("x2", "U1", "U2", "U3"):
         a, b = g[k], getattr(o.s, k)
-        assert np.max(np.abs(a - b)) / max(1.0, np.max(np.abs(b))) <= 1e-10, k
+        assert np.max(np.abs(a - b)) / np.max(np.abs(b)) <= 1e-10, k
     assert not np.array_equal(g["U1"], parts["U1"])

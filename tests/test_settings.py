@@ -1,5 +1,5 @@
 """The settings-file front end (mcpm_config_from_settings, a restatement of
-readSettingsFile, src/myIO.cpp:1756-3016, for problems 1 and 2) on the
+readSettingsFile, src/myIO.cpp:1756-3016, for problems 1, 2 and 11) on the
 fixtures in tests/golden/settings: bit-exact against the reference's own
 reader where the reference tree is present, and against the values it
 produced (tests/golden/settings_expected.json, written by
@@ -78,6 +78,9 @@ BASE = "model FP_dense\nN 100\nvisp 0.5\nnualpha 1.0\nbox_len 1 10 1\nnum_cells 
 @pytest.mark.parametrize("extra,needle", [
     ("bogus_key 3\n", "unknown keyword"),
     ("problem 3\n", "problems"),
+    ("problem 11\n", "problem wall needs nc"),
+    ("problem 11\nnc 0.7\nnv2 0.01\nTc 85\nLcN 20\nLvN 40\n", "LvN1"),
+    ("problem 11\nnc 0.7\nnv2 0.01\nTc 85\nLcN 20\nLvN 40\nLvN1 5\n", "nv1"),
     ("model MD\n", "model"),
     ("box_delta_dim 1 2 1\n", "box_delta_dim"),
 ])
@@ -125,6 +128,51 @@ def test_initialize_from_settings(built, name):
         d = 0 if k == "x1" else 1
         if not cfg.direction[d]:
             assert np.array_equal(a[k], ref[k])
+    for k in ("U1", "U2", "U3"):
+        se = np.sqrt((a[k].var() + ref[k].var()) / N)
+        assert abs(a[k].mean() - ref[k].mean()) < 5 * se, k
+        assert abs(a[k].var() / ref[k].var() - 1) < 0.05, k
+
+
+def test_wall_settings(built):
+    """problem wall (src/myIO.cpp:2628-2726): argon's diameter with
+    eqdist = sigma, densities from sigma^-3, Fn fixed at 1e13, N and the box
+    height from the three layers, the liquid's temperature for dt"""
+    path = os.path.join(SETTINGS, "wall_fp_dense.in")
+    cfg, N = mcpm.config_from_settings(path)
+    s = 3.405e-10
+    assert cfg.problem == mcpm.PROBLEM_WALL and cfg.sigma == s and cfg.eqdist == s and cfg.Fn == 1e13
+    assert cfg.length[1] == (40 * s + 20 * s) + 20 * s
+    assert cfg.n == 0.7 / s ** 3
+    nv = int(np.floor(0.01 / s ** 3 * 0.0316 * 0.0316 * 20 * s / 1e13))
+    nc = int(np.floor(0.7 / s ** 3 * 0.0316 * 0.0316 * (20 * s) / 1e13))
+    assert N == nc + nv + int(np.floor(0.01 / s ** 3 * 0.0316 * 0.0316 * 40 * s / 1e13))
+    assert cfg.max_particles == N
+
+
+def test_initialize_wall(built):
+    """initialization for problem wall (src/Main_Functions.cpp:4493-4530):
+    the first Nv1 particles in the lower vapour layer, the next Nc2 in the
+    liquid slab, the rest in the upper vapour layer -- the same layer for
+    every particle id as the reference's own initialization; velocities at
+    the liquid's temperature, statistically equal to the reference's."""
+    path = os.path.join(SETTINGS, "wall_fp_dense.in")
+    cfg, N = mcpm.config_from_settings(path)
+    a = mcpm.initialize_from_settings(path, 3, N)
+    s = 3.405e-10
+    edges = np.array([0.0, 20 * s, 40 * s, 80 * s])
+    layer = np.searchsorted(edges, a["x2"], side="right") - 1
+    assert np.all(np.diff(layer) >= 0) and set(np.unique(layer)) == {0, 1, 2}
+    assert a["x2"].min() > 0 and a["x2"].max() < cfg.length[1]
+    assert np.all(a["x1"] == 0.5 * cfg.length[0])
+    sd = np.sqrt(cfg.kb * 85.0 / cfg.m)
+    for k in ("U1", "U2", "U3"):
+        assert abs(a[k].std() / sd - 1) < 0.05
+    ref = O.ref_initialize(path, N)
+    if ref is None:
+        return
+    assert np.array_equal(np.searchsorted(edges, ref["x2"], side="right") - 1, layer)
+    assert np.array_equal(a["x1"], ref["x1"])
     for k in ("U1", "U2", "U3"):
         se = np.sqrt((a[k].var() + ref[k].var()) / N)
         assert abs(a[k].mean() - ref[k].mean()) < 5 * se, k
