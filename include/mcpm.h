@@ -112,6 +112,30 @@ enum mcpm_rng {
   MCPM_RNG_INJECTED = 1         /* normals from mcpm_inject_normals (tests)     */
 };
 
+/* The draw streams of the particle step (the Philox counter's third word);
+   mcpm_inject_uniforms replaces one stream's draws.  The key of a draw is
+   the particle id for FP, BC, BIN and the ADDREM streams (the parent's id
+   for ADDREM_NEW) and the cell for the collision streams; the counter is 0
+   except for BC ((apply_BC call of the step << 8) | re-flight loop), the
+   candidate number for ESMC / ESMC_ACC / DSMC / DSMC_ACC and the copy
+   number for ADDREM_NEW. */
+enum mcpm_rng_stream {
+  MCPM_RNG_STREAM_FP = 0,          /* random_generator's normals (4 words)     */
+  MCPM_RNG_STREAM_BC = 1,          /* diffuse re-emission (BC_thermal_wall_3D,
+                                      BC_wall): Rayleigh factor, two normals   */
+  MCPM_RNG_STREAM_ESMC = 2,        /* ESMC candidate pair and direction        */
+  MCPM_RNG_STREAM_BIN = 3,         /* cell_update's face jitter (word 0 >= 2^31:
+                                      +1e-14, else -1e-14)                     */
+  MCPM_RNG_STREAM_ESMC_ACC = 4,    /* ESMC acceptance                          */
+  MCPM_RNG_STREAM_ESMC_M = 5,      /* ESMC candidate count rounding            */
+  MCPM_RNG_STREAM_DSMC = 6,        /* DSMC_VHS candidate pair and direction    */
+  MCPM_RNG_STREAM_DSMC_ACC = 7,    /* DSMC_VHS acceptance                      */
+  MCPM_RNG_STREAM_DSMC_M = 8,      /* DSMC_VHS candidate count rounding        */
+  MCPM_RNG_STREAM_ADDREM_DEL = 9,  /* merge: deletion test                     */
+  MCPM_RNG_STREAM_ADDREM_NEW = 10, /* split: the copies' velocity normals      */
+  MCPM_RNG_STREAM_COUNT = 11
+};
+
 /* Plain-data configuration: the subset of GAS/BOX (src/cpp_headers.h:145-269)
    the particle step reads.  Units are whatever the caller uses consistently
    (the reference mixes SI and reduced units; mcpm does no unit conversion). */
@@ -304,6 +328,17 @@ int mcpm_step(mcpm_session* s, int32_t n_steps);
 int mcpm_inject_normals(mcpm_session* s, int64_t n, const double* xi1,
                         const double* xi2, const double* xi3);
 int mcpm_set_rng(mcpm_session* s, int32_t mode);
+/* Uniform draws in place of one stream's Philox words (tests that need a
+   known draw: a wall re-emission, the face jitter of a particle exactly on
+   a face, a chosen collision candidate).  u holds n_rows rows of four
+   uniforms in [0, 1); a draw with key q and counter c reads row
+   (q + c) mod n_rows, at every step, as the four 32-bit words
+   floor(u 2^32) (clamped to [0, 2^32 - 1]).  The FP64 kernels turn a word w
+   into the uniform (w + 1/2) 2^-32, so u = (w + 1/2) 2^-32 comes back
+   exactly; the FP32 kernels take the top 23 bits, (floor(w / 2^9) + 1/2) 2^-23.
+   Integer uses (a candidate picked among n) take floor(w n / 2^32).
+   n_rows = 0 (or u = NULL) restores the Philox stream. */
+int mcpm_inject_uniforms(mcpm_session* s, int32_t stream, int64_t n_rows, const double* u);
 /* Time-sampled raw velocity sums per cell, the CELLS members that
    cell_poly_velocity accumulates (src/Main_Functions.cpp:1918-1968, called by
    post_processing once the run passes its averaging start, src/myIO.cpp:968-971):

@@ -29,6 +29,16 @@ __device__ __forceinline__ uint4 philox(uint64_t seed, uint32_t c0, uint32_t c1,
   return philox(make_uint4(c0, c1, c2, c3), make_uint2((uint32_t)seed, (uint32_t)(seed >> 32)));
 }
 
+// the four words of a draw: the stream's injected row (key + counter) mod
+// rows when the caller injected uniforms for it, else Philox keyed by the
+// seed with counter (key, step, stream, counter)
+__device__ __forceinline__ uint4 rng_draw(const DevConsts& k, uint32_t key, uint32_t step, uint32_t stream,
+                                          uint32_t ctr) {
+  const uint4* inj = k.rng_inj[stream];
+  if (inj) return inj[((uint64_t)key + ctr) % k.rng_inj_rows[stream]];
+  return philox(k.seed, key, step, stream, ctr);
+}
+
 __device__ __forceinline__ double u01d(uint32_t x) { return ((double)x + 0.5) * (1.0 / 4294967296.0); }
 // uniform in (0,1) from the top 23 bits, built in the mantissa of a float in
 // [1,2) (no integer-to-float conversion): k 2^-23 + 2^-24, k = x >> 9

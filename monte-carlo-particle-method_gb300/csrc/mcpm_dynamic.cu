@@ -95,7 +95,7 @@ __global__ void k_ar_flags(DevConsts k, const int32_t* off, const int32_t* cnt, 
       if (w > cwc) {
         f = 1; ++nn; wt += w;
       } else if (w < cwc) {
-        const uint4 r = philox(k.seed, (uint32_t)q, (uint32_t)step, RNG_ADDREM_DEL, 0u);
+        const uint4 r = rng_draw(k, (uint32_t)q, (uint32_t)step, RNG_ADDREM_DEL, 0u);
         if (u01d(r.x) < ratio) { f = -1; ++nd; }
         else { f = 2; ++nr; wt += cwc; }
       } else {
@@ -289,7 +289,7 @@ __global__ void k_ar_move(DevConsts k, const int32_t* off, const int32_t* cnt, D
       if (f != 1) continue;
       for (int j = 0; j < g - 1; ++j) {
         const int64_t e2 = n_kept + (int64_t)srank[q] * (g - 1) + j;
-        const Normals3<double> z = normals3<double>(philox(k.seed, (uint32_t)q, (uint32_t)step, RNG_ADDREM_NEW,
+        const Normals3<double> z = normals3<double>(rng_draw(k, (uint32_t)q, (uint32_t)step, RNG_ADDREM_NEW,
                                                            (uint32_t)j));
         if (d.x1) d.x1[e2] = x1;
         d.x2[e2] = x2;

@@ -35,7 +35,7 @@ __global__ void __launch_bounds__(128) k_esmc(DevConsts k, double* cell, const i
   const int step = *dstep;
   const int NI = cnt[I];
   const double om_max = cell[(size_t)MCPM_CF_OMEGA_MAX * C + I];
-  const double mreal = r_floor(0.5 * om_max * (1.0 * NI) + u01d(philox(k.seed, (uint32_t)I, (uint32_t)step, RNG_ESMC_M, 0u).x));
+  const double mreal = r_floor(0.5 * om_max * (1.0 * NI) + u01d(rng_draw(k, (uint32_t)I, (uint32_t)step, RNG_ESMC_M, 0u).x));
   // a non-finite or absurd majorant would make the candidate loop unbounded
   const double mcap = 64.0 * NI + 4096.0;
   int mI = 0;
@@ -61,7 +61,7 @@ __global__ void __launch_bounds__(128) k_esmc(DevConsts k, double* cell, const i
       double Ymid = 0.0, nJ = 0.0;
       float Ymid_f = 0.f, nJ_f = 0.f;
       if (kc < mI) {
-        uint4 r = philox(k.seed, (uint32_t)I, (uint32_t)step, RNG_ESMC, (uint32_t)kc);
+        uint4 r = rng_draw(k, (uint32_t)I, (uint32_t)step, RNG_ESMC, (uint32_t)kc);
         si = (int64_t)off[I] + pick(r.x, NI);
         const real uy = F32 ? (real)u01f(r.y) : (real)u01d(r.y), uz = F32 ? (real)u01f(r.z) : (real)u01d(r.z);
         real theta = (real)2.0 * pi * uy;
@@ -108,12 +108,12 @@ __global__ void __launch_bounds__(128) k_esmc(DevConsts k, double* cell, const i
         if constexpr (F32) {
           const float dummy = coef_f * (float)gd * Ymid_f * nJ_f;
           omega_f = fmaxf(omega_f, dummy);
-          const float u = u01f(philox(k.seed, (uint32_t)I, (uint32_t)step, RNG_ESMC_ACC, (uint32_t)kc).x);
+          const float u = u01f(rng_draw(k, (uint32_t)I, (uint32_t)step, RNG_ESMC_ACC, (uint32_t)kc).x);
           accept = dummy > u * om_max_f;
         } else {
           double dummy = 4.0 * 3.14159265358979323846 * k.sigma * k.sigma * (double)gd * Ymid * nJ * k.dt;
           if (dummy - omega > 0.0) omega = dummy;
-          double u = u01d(philox(k.seed, (uint32_t)I, (uint32_t)step, RNG_ESMC_ACC, (uint32_t)kc).x);
+          double u = u01d(rng_draw(k, (uint32_t)I, (uint32_t)step, RNG_ESMC_ACC, (uint32_t)kc).x);
           accept = dummy / om_max > u;
         }
         if (accept) {
@@ -185,7 +185,7 @@ __global__ void __launch_bounds__(128) k_dsmc_vhs(DevConsts k, double* cell, con
   const double nI = cell[(size_t)MCPM_CF_N * C + I];
   const double pi = 3.14159265358979323846;
   const double Mc = pi * k.sigma * k.sigma * ((double)NI * nI) * crm * k.dt / 2.0;
-  const double mreal = r_floor(Mc + u01d(philox(k.seed, (uint32_t)I, (uint32_t)step, RNG_DSMC_M, 0u).x));
+  const double mreal = r_floor(Mc + u01d(rng_draw(k, (uint32_t)I, (uint32_t)step, RNG_DSMC_M, 0u).x));
   // a non-finite or absurd majorant would make the candidate loop unbounded
   const double mcap = 64.0 * NI + 4096.0;
   int mI = 0;
@@ -202,7 +202,7 @@ __global__ void __launch_bounds__(128) k_dsmc_vhs(DevConsts k, double* cell, con
     int64_t si = -1, sj = -1;
     uint4 r = make_uint4(0u, 0u, 0u, 0u);
     if (valid) {
-      r = philox(k.seed, (uint32_t)I, (uint32_t)step, RNG_DSMC, (uint32_t)kc);
+      r = rng_draw(k, (uint32_t)I, (uint32_t)step, RNG_DSMC, (uint32_t)kc);
       const int a = pick(r.x, NI);
       int b = pick(r.y, NI - 1);
       b += (b >= a) ? 1 : 0;
@@ -226,7 +226,7 @@ __global__ void __launch_bounds__(128) k_dsmc_vhs(DevConsts k, double* cell, con
       if (sigmat - seen > (real)0) seen = sigmat;
       const real uacc = F32 ? (real)u01f(r.z) : (real)u01d(r.z);
       if (sigmat / crm_r > uacc) {
-        const uint32_t w2 = philox(k.seed, (uint32_t)I, (uint32_t)step, RNG_DSMC_ACC, (uint32_t)kc).x;
+        const uint32_t w2 = rng_draw(k, (uint32_t)I, (uint32_t)step, RNG_DSMC_ACC, (uint32_t)kc).x;
         const real a1 = F32 ? (real)u01f(r.w) : (real)u01d(r.w);
         const real a2 = F32 ? (real)u01f(w2) : (real)u01d(w2);
         const real theta = r_acos((real)2.0 * a1 - (real)1.0);

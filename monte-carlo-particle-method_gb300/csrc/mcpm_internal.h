@@ -56,8 +56,12 @@ enum : uint32_t {
 };
 
 // Counter-stream ids for the Philox draws (third counter word).
-enum : uint32_t { RNG_FP = 0, RNG_BC = 1, RNG_ESMC = 2, RNG_BIN = 3, RNG_ESMC_ACC = 4, RNG_ESMC_M = 5,
-                  RNG_DSMC = 6, RNG_DSMC_ACC = 7, RNG_DSMC_M = 8, RNG_ADDREM_DEL = 9, RNG_ADDREM_NEW = 10 };
+enum : uint32_t { RNG_FP = MCPM_RNG_STREAM_FP, RNG_BC = MCPM_RNG_STREAM_BC, RNG_ESMC = MCPM_RNG_STREAM_ESMC,
+                  RNG_BIN = MCPM_RNG_STREAM_BIN, RNG_ESMC_ACC = MCPM_RNG_STREAM_ESMC_ACC,
+                  RNG_ESMC_M = MCPM_RNG_STREAM_ESMC_M, RNG_DSMC = MCPM_RNG_STREAM_DSMC,
+                  RNG_DSMC_ACC = MCPM_RNG_STREAM_DSMC_ACC, RNG_DSMC_M = MCPM_RNG_STREAM_DSMC_M,
+                  RNG_ADDREM_DEL = MCPM_RNG_STREAM_ADDREM_DEL, RNG_ADDREM_NEW = MCPM_RNG_STREAM_ADDREM_NEW,
+                  RNG_COUNT = MCPM_RNG_STREAM_COUNT };
 
 struct DevConsts {
   int N0, N1, C;
@@ -96,6 +100,10 @@ struct DevConsts {
   // the cells' weights (cells[].n_ratio) once set, else null (weight 1): the
   // cell density is n_ratio Fn N / V (src/Main_Functions.cpp:2588)
   const int32_t* cell_w;
+  // injected draws per stream (mcpm_inject_uniforms): rng_inj_rows[st] rows
+  // of four words in place of the Philox output, null for Philox
+  const uint4* rng_inj[RNG_COUNT];
+  uint32_t rng_inj_rows[RNG_COUNT];
 };
 
 // One set of device particle arrays (SoA).  real is float or double.
@@ -162,6 +170,8 @@ struct Session {
   float* pcell = nullptr;       // [C][PF_STRIDE] packed FP32 record
   double* xi = nullptr;         // [3][cap] whitened normals, slot order
   double* inj = nullptr;        // [3][cap] injected raw normals, particle-id order
+  uint4* rng_inj[RNG_COUNT] = {};  // injected words per stream (k.rng_inj points here)
+  uint32_t rng_inj_gen = 0;        // bumped by every injection (captured steps are re-recorded)
   double* stage = nullptr;      // [5][cap] host<->device staging (double)
   double* faces = nullptr;      // [4][N1+1] long-range face scratch
   float* bin_faces = nullptr;   // [N0+2 + N1+2] FP32 binning face tables (DevConsts f_face_x/y)

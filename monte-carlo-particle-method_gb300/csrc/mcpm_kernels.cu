@@ -78,7 +78,7 @@ __device__ __forceinline__ int bin_one(real x1, real x2, int pid, int step, cons
       if (kk > 0 && kk < k.N1 - 1) {
         const double xd = (double)x2;
         if (fabs(xd - k.dy * kk) < 1e-15 || fabs(xd - k.dy * (kk + 1)) < 1e-15) {
-          uint4 r = philox(k.seed, (uint32_t)pid, (uint32_t)step, RNG_BIN, 0u);
+          uint4 r = rng_draw(k, (uint32_t)pid, (uint32_t)step, RNG_BIN, 0u);
           int sgn = (r.x >= 0x80000000u) ? 1 : -1;  // u01(r.x) > 0.5
           kk = (int)floor((xd + 1e-14 * sgn) / k.dy);
         }
@@ -94,7 +94,7 @@ __device__ __forceinline__ int bin_one(real x1, real x2, int pid, int step, cons
     kk = (int)tk;
     if (kk > 0 && kk < k.N1 - 1) {
       if (r_fabs(x2 - dy * tk) < (real)1e-15 || r_fabs(x2 - dy * (tk + (real)1)) < (real)1e-15) {
-        uint4 r = philox(k.seed, (uint32_t)pid, (uint32_t)step, RNG_BIN, 0u);
+        uint4 r = rng_draw(k, (uint32_t)pid, (uint32_t)step, RNG_BIN, 0u);
         int sgn = (r.x >= 0x80000000u) ? 1 : -1;  // u01(r.x) > 0.5
         kk = (int)r_floor((x2 + (real)1e-14 * sgn) / dy);
       }
@@ -1114,7 +1114,7 @@ __device__ __forceinline__ void bc_periodic(PState<real>& s, const DevConsts& k,
 template <typename real>
 __device__ __forceinline__ void wall_draw(int pid, int step, int call, int it, const DevConsts& k, real& ray,
                                           real& z0, real& z1) {
-  uint4 r = philox(k.seed, (uint32_t)pid, (uint32_t)step, RNG_BC, (uint32_t)((call << 8) | (it & 0xff)));
+  uint4 r = rng_draw(k, (uint32_t)pid, (uint32_t)step, RNG_BC, (uint32_t)((call << 8) | (it & 0xff)));
   if constexpr (sizeof(real) == 8) {
     ray = r_sqrt(-log(u01d(r.x)));
     double a = r_sqrt(-2.0 * log(u01d(r.y)));
@@ -1315,7 +1315,7 @@ __device__ __forceinline__ void raw_normals_pid(const UpdArgs<real>& a, int step
   if (a.rng_mode == MCPM_RNG_INJECTED) {
     z0 = (real)a.inj[pid]; z1 = (real)a.inj[a.cap + pid]; z2 = (real)a.inj[2 * a.cap + pid];
   } else {
-    Normals3<real> z = normals3<real>(philox(a.k.seed, (uint32_t)pid, (uint32_t)step, RNG_FP, 0u));
+    Normals3<real> z = normals3<real>(rng_draw(a.k, (uint32_t)pid, (uint32_t)step, RNG_FP, 0u));
     z0 = z.z0; z1 = z.z1; z2 = z.z2;
   }
 }

@@ -5,6 +5,7 @@
 #include <cstdio>
 #include <cstring>
 #include <new>
+#include <vector>
 
 #include "mcpm_internal.h"
 #include "mcpm_surrogate.h"
@@ -368,6 +369,7 @@ int mcpm_session_destroy(mcpm_session* s) {
   cudaFree(s->list_small); cudaFree(s->list_big); cudaFree(s->wl); cudaFree(s->work); cudaFree(s->scan_blk); cudaFree(s->cell); cudaFree(s->pcell);
   cudaFree(s->xi); cudaFree(s->inj); cudaFree(s->stage); cudaFree(s->faces); cudaFree(s->lr_tab); cudaFree(s->status); cudaFree(s->dstep);
   cudaFree(s->bin_faces);
+  for (uint4* t : s->rng_inj) cudaFree(t);
   lr2d_free(*s);
   cudaFree(s->sur_err);
   if (s->sur_err_h) cudaFreeHost(s->sur_err_h);
@@ -752,6 +754,7 @@ static uint64_t graph_signature(const mcpm_session* s, uint32_t stages) {
   mix((uint64_t)s->N);  // the particle count changes with splits and deletions
   mix((uint64_t)s->press);
   mix((uint64_t)(uintptr_t)s->k.cell_w);
+  mix((uint64_t)s->rng_inj_gen);
   return h;
 }
 
@@ -971,6 +974,36 @@ int mcpm_inject_normals(mcpm_session* s, int64_t n, const double* a, const doubl
   cudaMemcpyAsync(s->inj + 2 * cap, c, n * 8, cudaMemcpyHostToDevice, s->stream);
   s->rng_mode = MCPM_RNG_INJECTED;
   return cuda_check(s, cudaGetLastError(), "inject_normals");
+}
+
+int mcpm_inject_uniforms(mcpm_session* s, int32_t stream, int64_t n_rows, const double* u) {
+  if (!s || stream < 0 || stream >= (int32_t)RNG_COUNT || n_rows < 0 || n_rows > 0xFFFFFFFFll)
+    return fail(s, MCPM_ERR_ARG, "inject_uniforms: bad arguments");
+  int rc = cuda_check(s, cudaStreamSynchronize(s->stream), "inject_uniforms");  // no kernel reads the old table
+  if (rc) return rc;
+  cudaFree(s->rng_inj[stream]);
+  s->rng_inj[stream] = nullptr;
+  s->k.rng_inj[stream] = nullptr;
+  s->k.rng_inj_rows[stream] = 0;
+  ++s->rng_inj_gen;
+  if (n_rows == 0 || !u) return MCPM_OK;
+  std::vector<uint4> w((size_t)n_rows);
+  auto word = [](double v) -> uint32_t {
+    if (!(v > 0.0)) return 0u;  // also NaN
+    const double t = std::floor(v * 4294967296.0);
+    return t >= 4294967295.0 ? 0xFFFFFFFFu : (uint32_t)t;
+  };
+  for (int64_t r = 0; r < n_rows; ++r)
+    w[r] = make_uint4(word(u[4 * r]), word(u[4 * r + 1]), word(u[4 * r + 2]), word(u[4 * r + 3]));
+  if (cudaMalloc((void**)&s->rng_inj[stream], (size_t)n_rows * sizeof(uint4)) != cudaSuccess) {
+    s->rng_inj[stream] = nullptr;
+    cudaGetLastError();
+    return fail(s, MCPM_ERR_CUDA, "inject_uniforms: out of device memory");
+  }
+  cudaMemcpy(s->rng_inj[stream], w.data(), (size_t)n_rows * sizeof(uint4), cudaMemcpyHostToDevice);
+  s->k.rng_inj[stream] = s->rng_inj[stream];
+  s->k.rng_inj_rows[stream] = (uint32_t)n_rows;
+  return cuda_check(s, cudaGetLastError(), "inject_uniforms");
 }
 
 int mcpm_set_rng(mcpm_session* s, int32_t mode) {

@@ -29,6 +29,9 @@ MODEL_NONE, MODEL_FP_DENSE, MODEL_FP_IDEAL_GAS, MODEL_ESMC, MODEL_FP_LINEAR, MOD
 LR_NONE, LR_DIRECT, LR_DENSITY_EXPANSION, LR_SCREENED_POISSON = 0, 1, 2, 3
 FP64, FP32 = 0, 1
 RNG_PHILOX, RNG_INJECTED = 0, 1
+# enum mcpm_rng_stream
+RS = dict(FP=0, BC=1, ESMC=2, BIN=3, ESMC_ACC=4, ESMC_M=5, DSMC=6, DSMC_ACC=7, DSMC_M=8, ADDREM_DEL=9,
+          ADDREM_NEW=10)
 
 CF = dict(NUM_INSIDE=0, U_SPACE=1, PIJ=4, M3=10, M4=20, M5=26, Q=29, DM2=32, DM4=33, MP=34, T=37, N=38,
           GAMMA_ST=39, LAMBDA=40, C=41, GAMMA=47, ALPHA=50, BETA=59, PHI=62, F2=65, OMEGA_MAX=66, DIVU=67,
@@ -171,6 +174,7 @@ def load_library(path: str | None = None):
         "mcpm_step": (C.c_int, [vp, i32]),
         "mcpm_inject_normals": (C.c_int, [vp, i64, dp, dp, dp]),
         "mcpm_set_rng": (C.c_int, [vp, i32]),
+        "mcpm_inject_uniforms": (C.c_int, [vp, i32, i64, dp]),
         "mcpm_get_cells": (C.c_int, [vp, dp]),
         "mcpm_sample_cells": (C.c_int, [vp]),
         "mcpm_get_samples": (C.c_int, [vp, dp]),
@@ -379,6 +383,16 @@ class Session:
         n = self.N
         self._inj = [_f64(xi1, n), _f64(xi2, n), _f64(xi3, n)]
         self._ck(self.lib.mcpm_inject_normals(self.h, n, *[_dp(a) for a in self._inj]), "inject_normals")
+
+    def inject_uniforms(self, stream, u):
+        """u: [rows][4] uniforms in place of the stream's draws (name or
+        number of enum mcpm_rng_stream); None restores Philox."""
+        st = RS[stream] if isinstance(stream, str) else int(stream)
+        if u is None:
+            self._ck(self.lib.mcpm_inject_uniforms(self.h, st, 0, None), "inject_uniforms")
+            return
+        u = np.ascontiguousarray(u, dtype=np.float64).reshape(-1, 4)
+        self._ck(self.lib.mcpm_inject_uniforms(self.h, st, len(u), _dp(u)), "inject_uniforms")
 
     def set_rng(self, mode):
         self._ck(self.lib.mcpm_set_rng(self.h, int(mode)), "set_rng")

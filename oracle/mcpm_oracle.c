@@ -38,6 +38,8 @@ struct orc_state {
   double* xi;        /* 3N whitened normals (random_generator output) */
   double* nn;        /* [C][4] nodal densities n_n of the last cell_update */
   int32_t* cw;       /* [C] cells[].n_ratio once set, else NULL (1) */
+  uint32_t* rinj[RNG_STREAM_ADDREM_NEW + 1];  /* injected words per stream, 4 per row */
+  int64_t rinj_rows[RNG_STREAM_ADDREM_NEW + 1];
 };
 
 /* ------------------------------------------------------------------ RNG -- */
@@ -71,6 +73,18 @@ static void philox(uint64_t seed, uint32_t c0, uint32_t c1, uint32_t c2,
 
 static double u01(uint32_t x) { return ((double)x + 0.5) * (1.0 / 4294967296.0); }
 
+/* the four words of a draw of the session's stream c2 with key c0 and
+   counter c3: the injected row (c0 + c3) mod rows (mcpm_inject_uniforms),
+   else Philox on (c0, c1 = step, c2, c3) */
+static void rng(const orc_state* s, uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t out[4]) {
+  if (c2 <= RNG_STREAM_ADDREM_NEW && s->rinj[c2]) {
+    const uint32_t* w = s->rinj[c2] + 4 * (((uint64_t)c0 + c3) % (uint64_t)s->rinj_rows[c2]);
+    out[0] = w[0]; out[1] = w[1]; out[2] = w[2]; out[3] = w[3];
+    return;
+  }
+  philox(s->cfg.seed, c0, c1, c2, c3, out);
+}
+
 static const double TWO_PI = 6.283185307179586476925286766559;
 
 /* four standard normals by two Box-Muller pairs on the four Philox words */
@@ -78,6 +92,18 @@ void orc_normals4(uint64_t seed, uint32_t c0, uint32_t c1, uint32_t c2,
                   uint32_t c3, double z[4]) {
   uint32_t r[4];
   philox(seed, c0, c1, c2, c3, r);
+  double a = sqrt(-2.0 * log(u01(r[0])));
+  double b = sqrt(-2.0 * log(u01(r[2])));
+  z[0] = a * cos(TWO_PI * u01(r[1]));
+  z[1] = a * sin(TWO_PI * u01(r[1]));
+  z[2] = b * cos(TWO_PI * u01(r[3]));
+  z[3] = b * sin(TWO_PI * u01(r[3]));
+}
+
+/* orc_normals4 on the session's draw (injected or Philox) */
+static void normals4_s(const orc_state* s, uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, double z[4]) {
+  uint32_t r[4];
+  rng(s, c0, c1, c2, c3, r);
   double a = sqrt(-2.0 * log(u01(r[0])));
   double b = sqrt(-2.0 * log(u01(r[2])));
   z[0] = a * cos(TWO_PI * u01(r[1]));
@@ -208,7 +234,9 @@ orc_state* orc_create(const mcpm_config* cfg, int64_t n_particles) {
 void orc_destroy(orc_state* s) {
   if (!s) return;
   free(s->cell); free(s->cnt); free(s->off); free(s->list); free(s->index);
-  free(s->inj); free(s->xi); free(s->nn); free(s->cw); free(s);
+  free(s->inj); free(s->xi); free(s->nn); free(s->cw);
+  for (int i = 0; i <= RNG_STREAM_ADDREM_NEW; ++i) free(s->rinj[i]);
+  free(s);
 }
 
 int orc_num_cells(const orc_state* s) { return s->C; }
@@ -226,6 +254,26 @@ int orc_get_step(const orc_state* s) { return s->step; }
 void orc_set_step(orc_state* s, int step) { s->step = step; }
 int orc_status(orc_state* s) { int st = s->status; s->status = 0; return st; }
 void orc_set_rng(orc_state* s, int mode) { s->rng_mode = mode; }
+/* mcpm_inject_uniforms: n_rows rows of four uniforms as the words
+   floor(u 2^32), clamped to [0, 2^32 - 1]; n_rows = 0 restores Philox */
+void orc_inject_uniforms(orc_state* s, int stream, int64_t n_rows, const double* u) {
+  if (stream < 0 || stream > RNG_STREAM_ADDREM_NEW) return;
+  free(s->rinj[stream]);
+  s->rinj[stream] = NULL;
+  s->rinj_rows[stream] = 0;
+  if (n_rows <= 0 || !u) return;
+  s->rinj[stream] = (uint32_t*)malloc(sizeof(uint32_t) * 4 * (size_t)n_rows);
+  for (int64_t i = 0; i < 4 * n_rows; ++i) {
+    const double v = u[i];
+    uint32_t w = 0;
+    if (v > 0.0) {
+      const double t = floor(v * 4294967296.0);
+      w = t >= 4294967295.0 ? 0xFFFFFFFFu : (uint32_t)t;
+    }
+    s->rinj[stream][i] = w;
+  }
+  s->rinj_rows[stream] = n_rows;
+}
 void orc_inject_normals(orc_state* s, const double* a, const double* b,
                         const double* c) {
   for (int64_t i = 0; i < s->N; ++i) {
@@ -337,7 +385,7 @@ static void bin_particles(orc_state* s, const double* x1, const double* x2) {
     if (k > 0 && k < s->N1 - 1) {
       if (fabs(x2[i] - s->dy * k) < 1e-15 || fabs(x2[i] - s->dy * (k + 1)) < 1e-15) {
         uint32_t r[4];
-        philox(g->seed, (uint32_t)i, (uint32_t)s->step, RNG_STREAM_BIN, 0, r);
+        rng(s, (uint32_t)i, (uint32_t)s->step, RNG_STREAM_BIN, 0, r);
         int sgn = (u01(r[0]) > 0.5) ? 1 : -1;
         k = (int)floor((x2[i] + 1e-14 * sgn) / s->dy);
       }
@@ -702,7 +750,7 @@ void orc_random_generator(orc_state* s, double* x1f, double* x2f, double* x3f) {
       x1f[i] = s->inj[i]; x2f[i] = s->inj[N + i]; x3f[i] = s->inj[2 * N + i];
     } else {
       double z[4];
-      orc_normals4(s->cfg.seed, (uint32_t)i, (uint32_t)s->step, RNG_STREAM_FP, 0, z);
+      normals4_s(s, (uint32_t)i, (uint32_t)s->step, RNG_STREAM_FP, 0, z);
       x1f[i] = z[0]; x2f[i] = z[1]; x3f[i] = z[2];
     }
   }
@@ -848,13 +896,13 @@ static void esmc_cell(orc_state* s, int I, const double* x1, const double* x2,
   const double pi = acos(-1.0);
   int NI = s->cnt[I];
   uint32_t r[4];
-  philox(g->seed, (uint32_t)I, (uint32_t)s->step, RNG_STREAM_ESMC_M, 0, r);
+  rng(s, (uint32_t)I, (uint32_t)s->step, RNG_STREAM_ESMC_M, 0, r);
   double om_max = CELL(s, I, MCPM_CF_OMEGA_MAX);
   int mI = (int)floor(0.5 * om_max * (1.0 * NI) + u01(r[0]));
   double omega = 0.0;
   if (NI > 0) {
     for (int k = 0; k < mI; ++k) {
-      philox(g->seed, (uint32_t)I, (uint32_t)s->step, RNG_STREAM_ESMC, (uint32_t)k, r);
+      rng(s, (uint32_t)I, (uint32_t)s->step, RNG_STREAM_ESMC, (uint32_t)k, r);
       int i = s->list[s->off[I] + pick(r[0], NI)];
       double theta = 2.0 * pi * u01(r[1]);
       double cph = 2.0 * u01(r[2]) - 1.0;
@@ -879,7 +927,7 @@ static void esmc_cell(orc_state* s, int I, const double* x1, const double* x2,
       double dummy = 4.0 * pi * g->sigma * g->sigma * gd * Ymid * CELL(s, J, MCPM_CF_N) * g->dt;
       if (dummy - omega > 0.0) omega = dummy;
       uint32_t ra[4];
-      philox(g->seed, (uint32_t)I, (uint32_t)s->step, RNG_STREAM_ESMC_ACC, (uint32_t)k, ra);
+      rng(s, (uint32_t)I, (uint32_t)s->step, RNG_STREAM_ESMC_ACC, (uint32_t)k, ra);
       if (dummy / om_max > u01(ra[0])) {
         U1[i] = U1[i] - gd * dir0; U2[i] = U2[i] - gd * dir1; U3[i] = U3[i] - gd * dir2;
         U1[j] = U1[j] + gd * dir0; U2[j] = U2[j] + gd * dir1; U3[j] = U3[j] + gd * dir2;
@@ -921,13 +969,13 @@ static void dsmc_cell(orc_state* s, int I, double* U1, double* U2, double* U3) {
   if (NI <= 1) return;
   uint32_t r[4], ra[4];
   double crm_cell = CELL(s, I, MCPM_CF_OMEGA_MAX);
-  philox(g->seed, (uint32_t)I, (uint32_t)s->step, RNG_STREAM_DSMC_M, 0, r);
+  rng(s, (uint32_t)I, (uint32_t)s->step, RNG_STREAM_DSMC_M, 0, r);
   double M_cand = pi * g->sigma * g->sigma * ((double)NI * CELL(s, I, MCPM_CF_N)) * crm_cell * g->dt / 2.0;
   int mI = (int)floor(M_cand + u01(r[0]));
   double crm = 0.0;
   double crfac = pow(g->crref, 2.0 * g->visp - 1.0);
   for (int k = 0; k < mI; ++k) {
-    philox(g->seed, (uint32_t)I, (uint32_t)s->step, RNG_STREAM_DSMC, (uint32_t)k, r);
+    rng(s, (uint32_t)I, (uint32_t)s->step, RNG_STREAM_DSMC, (uint32_t)k, r);
     int a = pick(r[0], NI), b = pick(r[1], NI - 1);
     if (b >= a) b += 1;
     int i = s->list[s->off[I] + a], j = s->list[s->off[I] + b];
@@ -936,7 +984,7 @@ static void dsmc_cell(orc_state* s, int I, double* U1, double* U2, double* U3) {
     double sigmat = pow(Vr, (2.0 - 2.0 * g->visp)) * crfac;
     if (sigmat - crm > 0.0) crm = sigmat;
     if (sigmat / crm_cell > u01(r[2])) {
-      philox(g->seed, (uint32_t)I, (uint32_t)s->step, RNG_STREAM_DSMC_ACC, (uint32_t)k, ra);
+      rng(s, (uint32_t)I, (uint32_t)s->step, RNG_STREAM_DSMC_ACC, (uint32_t)k, ra);
       double theta = acos(2.0 * u01(r[3]) - 1.0);
       double phi = 2.0 * pi * u01(ra[0]);
       double v0 = Vr * cos(theta), v1 = Vr * sin(theta) * cos(phi), v2 = Vr * sin(theta) * sin(phi);
@@ -1485,7 +1533,7 @@ static void intersect_y(double* x, double y, double xo, double yo, double xn, do
 /* one diffuse re-emission: tangential Maxwellian, normal Rayleigh */
 static void wall_draw(const orc_state* s, int64_t i, int call_no, int it, double z[2], double* ray) {
   uint32_t r[4];
-  philox(s->cfg.seed, (uint32_t)i, (uint32_t)s->step, RNG_STREAM_BC,
+  rng(s, (uint32_t)i, (uint32_t)s->step, RNG_STREAM_BC,
          (uint32_t)((call_no << 8) | (it & 0xff)), r);
   *ray = sqrt(-log(u01(r[0])));
   double a = sqrt(-2.0 * log(u01(r[1])));
@@ -1731,7 +1779,7 @@ void orc_addremove_flags(orc_state* s, const int32_t* w, const int32_t* cw,
       split++;
     } else if (w[id] < cw[num]) {
       uint32_t r[4];
-      philox(s->cfg.seed, (uint32_t)id, (uint32_t)s->step, RNG_STREAM_ADDREM_DEL, 0, r);
+      rng(s, (uint32_t)id, (uint32_t)s->step, RNG_STREAM_ADDREM_DEL, 0, r);
       if (u01(r[0]) < ratio) { flag[id] = -1; kept--; }
       else flag[id] = 2;
     } else {
@@ -1833,7 +1881,7 @@ void orc_addremove_apply(orc_state* s, const double* x1, const double* x2,
     int num = s->index[id];
     for (int c = 0; c < n_ratio - 1; ++c) {
       double z[4];
-      orc_normals4(s->cfg.seed, (uint32_t)id, (uint32_t)s->step, RNG_STREAM_ADDREM_NEW, (uint32_t)c, z);
+      normals4_s(s, (uint32_t)id, (uint32_t)s->step, RNG_STREAM_ADDREM_NEW, (uint32_t)c, z);
       U1o[j] = U1[id] + h[num] * z[0];
       U2o[j] = U2[id] + h[num] * z[1];
       U3o[j] = U3[id] + h[num] * z[2];

@@ -53,6 +53,7 @@ def _load_oracle():
         "orc_status": (C.c_int, [vp]),
         "orc_inject_normals": (None, [vp, dp, dp, dp]),
         "orc_set_rng": (None, [vp, C.c_int]),
+        "orc_inject_uniforms": (None, [vp, C.c_int, C.c_int64, dp]),
         "orc_cell_update": (None, [vp, dp, dp, dp, dp, dp, ip]),
         "orc_random_generator": (None, [vp, dp, dp, dp]),
         "orc_velocity_fp": (None, [vp, dp, dp, dp, dp, dp, dp]),
@@ -157,6 +158,14 @@ class Oracle:
 
     def set_rng(self, mode):
         self.L.orc_set_rng(self.h, mode)
+
+    def inject_uniforms(self, stream, u):
+        """u: [rows][4] uniforms for the stream (None restores Philox)"""
+        if u is None:
+            self.L.orc_inject_uniforms(self.h, int(stream), 0, None)
+            return
+        u = np.ascontiguousarray(u, dtype=np.float64).reshape(-1, 4)
+        self.L.orc_inject_uniforms(self.h, int(stream), len(u), _dp(u))
 
     def cells(self):
         out = np.empty((self.C, CF_COUNT))

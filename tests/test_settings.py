@@ -144,9 +144,9 @@ def test_wall_settings(built):
     assert cfg.problem == mcpm.PROBLEM_WALL and cfg.sigma == s and cfg.eqdist == s and cfg.Fn == 1e13
     assert cfg.length[1] == (40 * s + 20 * s) + 20 * s
     assert cfg.n == 0.7 / s ** 3
-    nv = int(np.floor(0.01 / s ** 3 * 0.0316 * 0.0316 * 20 * s / 1e13))
+    nv = int(np.floor(0.05 / s ** 3 * 0.0316 * 0.0316 * 20 * s / 1e13))
     nc = int(np.floor(0.7 / s ** 3 * 0.0316 * 0.0316 * (20 * s) / 1e13))
-    assert N == nc + nv + int(np.floor(0.01 / s ** 3 * 0.0316 * 0.0316 * 40 * s / 1e13))
+    assert N == nc + nv + int(np.floor(0.05 / s ** 3 * 0.0316 * 0.0316 * 40 * s / 1e13))
     assert cfg.max_particles == N
 
 
