@@ -3,7 +3,9 @@
 Each CUDA translation unit is compiled in parallel with nvcc, then linked into
 one shared library next to this file.  The particle kernels are compiled with
 ``--fmad=false``: the FP64 path then rounds every multiply and add separately,
-as the reference does (the FP32 kernels write their fused multiply-adds out);
+as the reference does (the FP32 kernels write their fused multiply-adds out;
+the FP32 sessions' per-cell solve, ``mcpm_solve_fast.cu``, is the one unit
+compiled with ``--fmad=true``);
 host code is compiled with ``-ffp-contract=off`` for the same reason (aarch64
 compilers contract by default).
 """
@@ -28,7 +30,11 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "--fmad=false", "-Xcompiler", "-fPIC,-O2,-ffp-contract=off",
            "-Xptxas", "-warn-spills", "--expt-relaxed-constexpr"]
 SOURCES = ["mcpm_session.cu", "mcpm_kernels.cu", "mcpm_forces.cu", "mcpm_lr2d.cu", "mcpm_noalloc.cu",
-           "mcpm_surrogate.cu", "mcpm_surrogate_tc.cu", "mcpm_settings.cu", "mcpm_dynamic.cu", "mcpm_output.cu"]
+           "mcpm_surrogate.cu", "mcpm_surrogate_tc.cu", "mcpm_settings.cu", "mcpm_dynamic.cu", "mcpm_output.cu",
+           "mcpm_solve_fast.cu"]
+# translation units whose FP64 multiply-adds may fuse (results of FP32
+# sessions only); every other unit rounds each operation separately
+FMAD_TRUE = {"mcpm_solve_fast.cu"}
 
 
 def nvcc():
@@ -69,7 +75,9 @@ def build(force=False, verbose=False):
 
     def comp(so):
         s, o = so
-        return _run([cc, *ARCH, *NVFLAGS, "-c", s, "-o", o])
+        flags = [f.replace("--fmad=false", "--fmad=true") for f in NVFLAGS] \
+            if os.path.basename(s) in FMAD_TRUE else NVFLAGS
+        return _run([cc, *ARCH, *flags, "-c", s, "-o", o])
 
     if todo:
         with ThreadPoolExecutor(max_workers=len(todo)) as ex:

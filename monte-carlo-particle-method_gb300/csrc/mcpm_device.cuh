@@ -29,6 +29,18 @@ __device__ __forceinline__ uint4 philox(uint64_t seed, uint32_t c0, uint32_t c1,
   return philox(make_uint4(c0, c1, c2, c3), make_uint2((uint32_t)seed, (uint32_t)(seed >> 32)));
 }
 
+// Philox4x32-10 with the round keys given (rk[2r], rk[2r + 1]: the key
+// after r bumps), so that no key arithmetic runs per draw
+__device__ __forceinline__ uint4 philox_rk(uint4 c, const uint32_t (&rk)[20]) {
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    uint32_t hi0 = __umulhi(0xD2511F53u, c.x), lo0 = 0xD2511F53u * c.x;
+    uint32_t hi1 = __umulhi(0xCD9E8D57u, c.z), lo1 = 0xCD9E8D57u * c.z;
+    c = make_uint4(hi1 ^ c.y ^ rk[2 * r], lo1, hi0 ^ c.w ^ rk[2 * r + 1], lo0);
+  }
+  return c;
+}
+
 // the four words of a draw: the stream's injected row (key + counter) mod
 // rows when the caller injected uniforms for it, else Philox keyed by the
 // seed with counter (key, step, stream, counter)
@@ -36,7 +48,7 @@ __device__ __forceinline__ uint4 rng_draw(const DevConsts& k, uint32_t key, uint
                                           uint32_t ctr) {
   const uint4* inj = k.rng_inj[stream];
   if (inj) return inj[((uint64_t)key + ctr) % k.rng_inj_rows[stream]];
-  return philox(k.seed, key, step, stream, ctr);
+  return philox_rk(make_uint4(key, step, stream, ctr), k.rk);
 }
 
 __device__ __forceinline__ double u01d(uint32_t x) { return ((double)x + 0.5) * (1.0 / 4294967296.0); }

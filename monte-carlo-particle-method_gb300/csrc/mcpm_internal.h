@@ -71,6 +71,9 @@ struct DevConsts {
   double sigma, m, kb, n, Fn, T0, mu, visp, b, dt, phi, eqdist, ast, bst;
   double Tw[4], Uw[4];
   uint64_t seed;
+  // the Philox key of each of the ten rounds for this seed (formed once on
+  // the host: the draws then read the round keys from the parameter bank)
+  uint32_t rk[20];
   // wall offset of the diffuse walls, max(1e-15, 4 ulp(Len)) per direction
   double eps_x, eps_y;
   // 2-D long range: 1 when the Vlasov force acts on the node grid of a 2-D
@@ -264,6 +267,8 @@ int launch_repair(Session& s);
 int launch_compact(Session& s);
 int launch_moments(Session& s);
 int launch_solve(Session& s, int with_alpha);
+// the FP32 sessions' variant (mcpm_solve_fast.cu, FP64 multiply-adds fused)
+int launch_solve_fast(Session& s, int with_alpha, int fp_model);
 // slotted: write the new state into the slotted layout of the other buffer
 // (FP32 passes that bin the new positions)
 int launch_update(Session& s, uint32_t stages, int bc_call_base, bool slotted = false);

@@ -209,6 +209,10 @@ int mcpm_session_create(const mcpm_config* cfg, mcpm_session** out) {
   k.b = c.b; k.dt = c.dt; k.phi = c.phi; k.eqdist = c.eqdist; k.ast = c.ast; k.bst = c.bst;
   for (int i = 0; i < 4; ++i) { k.Tw[i] = c.T_wall[i]; k.Uw[i] = c.U_wall[i]; }
   k.seed = c.seed;
+  for (int r = 0; r < 10; ++r) {
+    k.rk[2 * r] = (uint32_t)c.seed + (uint32_t)r * 0x9E3779B9u;
+    k.rk[2 * r + 1] = (uint32_t)(c.seed >> 32) + (uint32_t)r * 0xBB67AE85u;
+  }
   k.lr2d = (c.long_range != MCPM_LR_NONE && c.long_range != MCPM_LR_DENSITY_EXPANSION && c.direction[0] == 1) ? 1 : 0;
   // 4 pi (sigma 2^(1/6))^3 of the density-expansion force, the pow factor
   // formed once as src/Main_Functions.cpp:1647 forms it
@@ -261,7 +265,10 @@ int mcpm_session_create(const mcpm_config* cfg, mcpm_session** out) {
 
   // tuning defaults (see mcpm_tune in the Python layer for the sweep)
   s->tune.bcap = (s->prec == MCPM_FP32) ? MCPM_UPD_BCAP : 3072;
-  s->tune.wcap = 256;  // <= bcap / 8 (a warp's staging capacity); mcpm_autotune picks it
+  // cells up to a warp's staging capacity (bcap / 8) go to one warp each: the
+  // split mcpm_autotune picked on every benchmark workload; it can still
+  // choose another
+  s->tune.wcap = s->tune.bcap / 8;
   s->tune.block = 256;
 
   const size_t cap = (size_t)s->cap, C = (size_t)s->C, rs = s->rsz;

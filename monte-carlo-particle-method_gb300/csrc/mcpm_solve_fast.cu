@@ -1,0 +1,20 @@
+// mcpm_solve_fast.cu -- the FP32 sessions' per-cell solve (k_solve<false>).
+//
+// The same kernel source as the exact FP64 path (mcpm_solve.cuh), compiled
+// with --fmad=true: its multiply-adds contract into DFMA instructions.  The
+// kernel runs on GB300's FP64 pipe (one DFMA, DADD or DMUL per pipe slot),
+// so every contracted pair is a pipe slot saved.  The FP32 sessions' results
+// are rounded to float for the particle pass, and the contraction only makes
+// their FP64 intermediates more accurate; the FP64 sessions keep the
+// reference's separate roundings (mcpm_kernels.cu, --fmad=false).
+#include "mcpm_solve.cuh"
+
+namespace mcpm {
+
+int launch_solve_fast(Session& s, int with_alpha, int fp_model) {
+  const int nb = (s.C + MCPM_SOLVE_T - 1) / MCPM_SOLVE_T;
+  k_solve<false><<<nb, MCPM_SOLVE_T, 0, s.stream>>>(s.k, s.cell, s.pcell, with_alpha, fp_model, s.status);
+  return 1;
+}
+
+}  // namespace mcpm
