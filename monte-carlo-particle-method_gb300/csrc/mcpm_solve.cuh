@@ -101,6 +101,154 @@ __device__ void gauss_jordan_fast(double* A, double* R, double* x) {
   }
 }
 
+// The FP32 sessions' alpha/beta: the three 4x4 systems [P v_b; u^T d]
+// (v_b = m3_b (1, 1, 1), u = (m3_a, m3_b, m3_c)) share the 3x3 block P, so
+// they are solved by block elimination with one inverse of P (the pressure
+// tensor, symmetric positive definite: its adjugate over its determinant):
+// be_b = (s_b - u.P^-1 r_b) / (d - m3_b u.P^-1 e), al_b = P^-1 r_b - m3_b be_b P^-1 e.
+// False (the caller then runs the pivoting solve) when P or a Schur
+// complement is degenerate.
+__device__ __forceinline__ bool ab_blocks(const double* P, const double* m3, double d, const double* rhs,
+                                          double* al, double* be) {
+  const double c00 = P[3] * P[5] - P[4] * P[4], c01 = P[2] * P[4] - P[1] * P[5], c02 = P[1] * P[4] - P[2] * P[3];
+  const double c11 = P[0] * P[5] - P[2] * P[2], c12 = P[1] * P[2] - P[0] * P[4], c22 = P[0] * P[3] - P[1] * P[1];
+  const double det = P[0] * c00 + P[1] * c01 + P[2] * c02;
+  if (!(det > 0.0) || !isfinite(det)) return false;
+  const double id = 1.0 / det;
+  const double i00 = c00 * id, i01 = c01 * id, i02 = c02 * id, i11 = c11 * id, i12 = c12 * id, i22 = c22 * id;
+  const double ye0 = i00 + i01 + i02, ye1 = i01 + i11 + i12, ye2 = i02 + i12 + i22;
+  const double ue = m3[0] * ye0 + m3[1] * ye1 + m3[2] * ye2;
+  for (int b = 0; b < 3; ++b) {
+    const double r0 = rhs[3 * b], r1 = rhs[3 * b + 1], r2 = rhs[3 * b + 2];
+    const double y0 = i00 * r0 + i01 * r1 + i02 * r2;
+    const double y1 = i01 * r0 + i11 * r1 + i12 * r2;
+    const double y2 = i02 * r0 + i12 * r1 + i22 * r2;
+    const double den = d - m3[b] * ue;
+    if (!(fabs(den) > 1e-12 * (fabs(d) + fabs(m3[b] * ue)))) return false;
+    const double bb = (rhs[9 + b] - (m3[0] * y0 + m3[1] * y1 + m3[2] * y2)) / den;
+    const double f = m3[b] * bb;
+    al[3 * b] = y0 - f * ye0;
+    al[3 * b + 1] = y1 - f * ye1;
+    al[3 * b + 2] = y2 - f * ye2;
+    be[b] = bb;
+  }
+  for (int j = 0; j < 9; ++j) if (!isfinite(al[j])) return false;
+  for (int j = 0; j < 3; ++j) if (!isfinite(be[j])) return false;
+  return true;
+}
+
+// The FP32 sessions' c/gamma (the 9x9 system of src/Fokker_Planck.cpp:590-804)
+// by mixed-precision iterative refinement: an LU factorisation of the
+// matrix in FP32 (no pivoting: rows 0..5 are the operator c -> P c + c P of
+// the positive definite P, rows 6..8 are dominated by their diagonal), then
+// residuals b - A x in FP64 with FP32 corrections until the last correction
+// is below 1e-13 of the solution -- the FP64 solution, at a fraction of the
+// FP64 operations of an FP64 elimination (GB300's FP64 pipe bounds this
+// kernel).  False after three corrections without convergence, or on a zero
+// or non-finite pivot: the caller then runs the FP64 elimination.
+static __device__ __noinline__ bool cg_refined(const double* P, const double* Q, const double* M3, const double* M4,
+                                        double DM2, double DM4, const double* b, double* x) {
+  const double E = DM4 - DM2 * DM2;
+  // rows 6..8 of the matrix in FP64 (rows 0..5 are entries of P and Q)
+  double G[27];
+  G[0] = Q[0] + 2.0 * M3[0]; G[1] = Q[1] + 4.0 * M3[1]; G[2] = Q[2] + 4.0 * M3[2];
+  G[3] = 2.0 * M3[3]; G[4] = 4.0 * M3[4]; G[5] = 2.0 * M3[5];
+  G[6] = 2.0 * M4[0] - 2.0 * P[0] * DM2 + E; G[7] = 2.0 * M4[1] - 2.0 * P[1] * DM2;
+  G[8] = 2.0 * M4[2] - 2.0 * P[2] * DM2;
+  G[9] = 2.0 * M3[1]; G[10] = Q[0] + 4.0 * M3[3]; G[11] = 4.0 * M3[4];
+  G[12] = Q[1] + 2.0 * M3[6]; G[13] = Q[2] + 4.0 * M3[7]; G[14] = 2.0 * M3[8];
+  G[15] = G[7]; G[16] = 2.0 * M4[3] - 2.0 * P[3] * DM2 + E; G[17] = 2.0 * M4[4] - 2.0 * P[4] * DM2;
+  G[18] = 2.0 * M3[2]; G[19] = 4.0 * M3[4]; G[20] = Q[0] + 4.0 * M3[5];
+  G[21] = 2.0 * M3[7]; G[22] = Q[1] + 4.0 * M3[8]; G[23] = Q[2] + 2.0 * M3[9];
+  G[24] = G[8]; G[25] = G[17]; G[26] = 2.0 * M4[5] - 2.0 * P[5] * DM2 + E;
+  const double s03 = P[0] + P[3], s05 = P[0] + P[5], s35 = P[3] + P[5];
+  // y = A v in FP64, the rows' nonzeros only
+  auto mul = [&](const double* v, double* y) {
+    y[0] = 2.0 * (P[0] * v[0] + P[1] * v[1] + P[2] * v[2] + Q[0] * v[6]);
+    y[1] = P[1] * v[0] + s03 * v[1] + P[4] * v[2] + P[1] * v[3] + P[2] * v[4] + Q[1] * v[6] + Q[0] * v[7];
+    y[2] = P[2] * v[0] + P[4] * v[1] + s05 * v[2] + P[1] * v[4] + P[2] * v[5] + Q[2] * v[6] + Q[0] * v[8];
+    y[3] = 2.0 * (P[1] * v[1] + P[3] * v[3] + P[4] * v[4] + Q[1] * v[7]);
+    y[4] = P[2] * v[1] + P[1] * v[2] + P[4] * v[3] + s35 * v[4] + P[4] * v[5] + Q[2] * v[7] + Q[1] * v[8];
+    y[5] = 2.0 * (P[2] * v[2] + P[4] * v[4] + P[5] * v[5] + Q[2] * v[8]);
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+      double a = 0.0;
+#pragma unroll
+      for (int q = 0; q < 9; ++q) a += G[9 * r + q] * v[q];
+      y[6 + r] = a;
+    }
+  };
+  // the FP32 matrix, factorised in place (unit lower L below the diagonal,
+  // U on and above it, the diagonal holding 1 / U_ii)
+  float L[81];
+#pragma unroll
+  for (int j = 0; j < 81; ++j) L[j] = 0.f;
+  const float p0 = (float)P[0], p1 = (float)P[1], p2 = (float)P[2], p3 = (float)P[3], p4 = (float)P[4],
+              p5 = (float)P[5], q0 = (float)Q[0], q1 = (float)Q[1], q2 = (float)Q[2];
+  L[0] = 2.f * p0; L[1] = 2.f * p1; L[2] = 2.f * p2; L[6] = 2.f * q0;
+  L[9] = p1; L[10] = p0 + p3; L[11] = p4; L[12] = p1; L[13] = p2; L[15] = q1; L[16] = q0;
+  L[18] = p2; L[19] = p4; L[20] = p0 + p5; L[22] = p1; L[23] = p2; L[24] = q2; L[26] = q0;
+  L[28] = 2.f * p1; L[30] = 2.f * p3; L[31] = 2.f * p4; L[34] = 2.f * q1;
+  L[37] = p2; L[38] = p1; L[39] = p4; L[40] = p3 + p5; L[41] = p4; L[43] = q2; L[44] = q1;
+  L[47] = 2.f * p2; L[49] = 2.f * p4; L[50] = 2.f * p5; L[53] = 2.f * q2;
+#pragma unroll
+  for (int j = 0; j < 27; ++j) L[54 + j] = (float)G[j];
+#pragma unroll
+  for (int i = 0; i < 9; ++i) {
+    const float piv = L[i * 9 + i];
+    if (!(fabsf(piv) > 0.f) || !isfinite(piv)) return false;
+    const float inv = 1.0f / piv;
+    L[i * 9 + i] = inv;
+#pragma unroll
+    for (int j = i + 1; j < 9; ++j) {
+      const float f = L[j * 9 + i] * inv;
+      L[j * 9 + i] = f;
+#pragma unroll
+      for (int q = i + 1; q < 9; ++q) L[j * 9 + q] = fmaf(-f, L[i * 9 + q], L[j * 9 + q]);
+    }
+  }
+  auto lusolve = [&](float* v) {
+#pragma unroll
+    for (int i = 1; i < 9; ++i) {
+      float a = v[i];
+#pragma unroll
+      for (int j = 0; j < i; ++j) a = fmaf(-L[i * 9 + j], v[j], a);
+      v[i] = a;
+    }
+#pragma unroll
+    for (int i = 8; i >= 0; --i) {
+      float a = v[i];
+#pragma unroll
+      for (int j = i + 1; j < 9; ++j) a = fmaf(-L[i * 9 + j], v[j], a);
+      v[i] = a * L[i * 9 + i];
+    }
+  };
+  float v[9];
+#pragma unroll
+  for (int i = 0; i < 9; ++i) v[i] = (float)b[i];
+  lusolve(v);
+#pragma unroll
+  for (int i = 0; i < 9; ++i) x[i] = (double)v[i];
+  for (int it = 0; it < 3; ++it) {
+    double ax[9];
+    mul(x, ax);
+#pragma unroll
+    for (int i = 0; i < 9; ++i) v[i] = (float)(b[i] - ax[i]);
+    lusolve(v);
+    float dmax = 0.f;
+    double xmax = 0.0;
+#pragma unroll
+    for (int i = 0; i < 9; ++i) {
+      x[i] += (double)v[i];
+      dmax = fmaxf(dmax, fabsf(v[i]));
+      xmax = fmax(xmax, fabs(x[i]));
+    }
+    if (!isfinite(xmax)) return false;
+    if ((double)dmax <= 1e-13 * xmax) return true;
+  }
+  return false;
+}
+
 // One thread per cell: Lambda (src/Main_Functions.cpp:2718-2728),
 // alpha/beta (src/Fokker_Planck.cpp:200-587; its 12x12 system is three
 // uncoupled 4x4 blocks -- unknowns (alpha_3b..3b+2, beta_b) -- and Gauss_Jordan
@@ -301,7 +449,8 @@ __global__ void __launch_bounds__(MCPM_SOLVE_T, MCPM_SOLVE_MINB)
         rhs[11] = (k_crr - 1.0) * mc + coeff_k * mc - gst * (M5[2]) + gst * (DM2 * (M3[2] + M3[7] + M3[9]));
         }
         const double m3b[3] = {ma, mb, mc};
-        for (int blk = 0; blk < 3; ++blk) {
+        const bool blocks = !EXACT && ab_blocks(P, m3b, d, rhs, al, be);
+        for (int blk = 0; blk < 3 && !blocks; ++blk) {
           double A[16], r4[4], x4[4];
           A[0] = P[0]; A[1] = P[1]; A[2] = P[2]; A[3] = m3b[blk];
           A[4] = P[1]; A[5] = P[3]; A[6] = P[4]; A[7] = m3b[blk];
@@ -323,35 +472,8 @@ __global__ void __launch_bounds__(MCPM_SOLVE_T, MCPM_SOLVE_MINB)
     if (ncnt < 2) {
       for (int j = 0; j < 9; ++j) x[j] = 0.0;
     } else {
-      double A[81], rhs[9];
-      for (int j = 0; j < 81; ++j) A[j] = 0.0;
+      double rhs[9];
       for (int j = 0; j < 9; ++j) { rhs[j] = 0.0; x[j] = 0.0; }
-#define AA(r, q) A[(r) * 9 + (q)]
-      AA(0, 0) = 2.0 * P[0]; AA(0, 1) = 2.0 * P[1]; AA(0, 2) = 2.0 * P[2]; AA(0, 6) = 2.0 * Q[0];
-      AA(1, 0) = P[1]; AA(1, 1) = P[0] + P[3]; AA(1, 2) = P[4]; AA(1, 3) = P[1]; AA(1, 4) = P[2];
-      AA(1, 6) = Q[1]; AA(1, 7) = Q[0];
-      AA(2, 0) = P[2]; AA(2, 1) = P[4]; AA(2, 2) = P[0] + P[5]; AA(2, 4) = P[1]; AA(2, 5) = P[2];
-      AA(2, 6) = Q[2]; AA(2, 8) = Q[0];
-      AA(3, 1) = 2.0 * P[1]; AA(3, 3) = 2.0 * P[3]; AA(3, 4) = 2.0 * P[4]; AA(3, 7) = 2.0 * Q[1];
-      AA(4, 1) = P[2]; AA(4, 2) = P[1]; AA(4, 3) = P[4]; AA(4, 4) = P[3] + P[5]; AA(4, 5) = P[4];
-      AA(4, 7) = Q[2]; AA(4, 8) = Q[1];
-      AA(5, 2) = 2.0 * P[2]; AA(5, 4) = 2.0 * P[4]; AA(5, 5) = 2.0 * P[5]; AA(5, 8) = 2.0 * Q[2];
-      AA(6, 0) = Q[0] + 2.0 * M3[0]; AA(6, 1) = Q[1] + 4.0 * M3[1]; AA(6, 2) = Q[2] + 4.0 * M3[2];
-      AA(6, 3) = 2.0 * M3[3]; AA(6, 4) = 4.0 * M3[4]; AA(6, 5) = 2.0 * M3[5];
-      AA(6, 6) = 2.0 * M4[0] - 2.0 * P[0] * DM2; AA(6, 7) = 2.0 * M4[1] - 2.0 * P[1] * DM2;
-      AA(6, 8) = 2.0 * M4[2] - 2.0 * P[2] * DM2;
-      AA(7, 0) = 2.0 * M3[1]; AA(7, 1) = Q[0] + 4.0 * M3[3]; AA(7, 2) = 4.0 * M3[4];
-      AA(7, 3) = Q[1] + 2.0 * M3[6]; AA(7, 4) = Q[2] + 4.0 * M3[7]; AA(7, 5) = 2.0 * M3[8];
-      AA(7, 6) = 2.0 * M4[1] - 2.0 * P[1] * DM2; AA(7, 7) = 2.0 * M4[3] - 2.0 * P[3] * DM2;
-      AA(7, 8) = 2.0 * M4[4] - 2.0 * P[4] * DM2;
-      AA(8, 0) = 2.0 * M3[2]; AA(8, 1) = 4.0 * M3[4]; AA(8, 2) = Q[0] + 4.0 * M3[5];
-      AA(8, 3) = 2.0 * M3[7]; AA(8, 4) = Q[1] + 4.0 * M3[8]; AA(8, 5) = Q[2] + 2.0 * M3[9];
-      AA(8, 6) = 2.0 * M4[2] - 2.0 * P[2] * DM2; AA(8, 7) = 2.0 * M4[4] - 2.0 * P[4] * DM2;
-      AA(8, 8) = 2.0 * M4[5] - 2.0 * P[5] * DM2;
-      AA(6, 6) += DM4 - (DM2) * (DM2);
-      AA(7, 7) += DM4 - (DM2) * (DM2);
-      AA(8, 8) += DM4 - (DM2) * (DM2);
-#undef AA
       double Pr = 2.0 / 3.0;
       double Y = (k.model == MCPM_MODEL_FP_DENSE) ? Ycell : 1.0;
       const double mu = mu_T;
@@ -368,8 +490,38 @@ __global__ void __launch_bounds__(MCPM_SOLVE_T, MCPM_SOLVE_MINB)
       rhs[6] += Lam * (-3.0 * M5[0] + DM2 * Q[0] + 2.0 * (P[0] * Q[0] + P[1] * Q[1] + P[2] * Q[2]));
       rhs[7] += Lam * (-3.0 * M5[1] + DM2 * Q[1] + 2.0 * (P[1] * Q[0] + P[3] * Q[1] + P[4] * Q[2]));
       rhs[8] += Lam * (-3.0 * M5[2] + DM2 * Q[2] + 2.0 * (P[2] * Q[0] + P[4] * Q[1] + P[5] * Q[2]));
-      if (EXACT) gauss_jordan<9>(A, rhs, x);
-      else gauss_jordan_fast<9>(A, rhs, x);
+      if (EXACT || !cg_refined(P, Q, M3, M4, DM2, DM4, rhs, x)) {
+        double A[81];
+        for (int j = 0; j < 81; ++j) A[j] = 0.0;
+#define AA(r, q) A[(r) * 9 + (q)]
+        AA(0, 0) = 2.0 * P[0]; AA(0, 1) = 2.0 * P[1]; AA(0, 2) = 2.0 * P[2]; AA(0, 6) = 2.0 * Q[0];
+        AA(1, 0) = P[1]; AA(1, 1) = P[0] + P[3]; AA(1, 2) = P[4]; AA(1, 3) = P[1]; AA(1, 4) = P[2];
+        AA(1, 6) = Q[1]; AA(1, 7) = Q[0];
+        AA(2, 0) = P[2]; AA(2, 1) = P[4]; AA(2, 2) = P[0] + P[5]; AA(2, 4) = P[1]; AA(2, 5) = P[2];
+        AA(2, 6) = Q[2]; AA(2, 8) = Q[0];
+        AA(3, 1) = 2.0 * P[1]; AA(3, 3) = 2.0 * P[3]; AA(3, 4) = 2.0 * P[4]; AA(3, 7) = 2.0 * Q[1];
+        AA(4, 1) = P[2]; AA(4, 2) = P[1]; AA(4, 3) = P[4]; AA(4, 4) = P[3] + P[5]; AA(4, 5) = P[4];
+        AA(4, 7) = Q[2]; AA(4, 8) = Q[1];
+        AA(5, 2) = 2.0 * P[2]; AA(5, 4) = 2.0 * P[4]; AA(5, 5) = 2.0 * P[5]; AA(5, 8) = 2.0 * Q[2];
+        AA(6, 0) = Q[0] + 2.0 * M3[0]; AA(6, 1) = Q[1] + 4.0 * M3[1]; AA(6, 2) = Q[2] + 4.0 * M3[2];
+        AA(6, 3) = 2.0 * M3[3]; AA(6, 4) = 4.0 * M3[4]; AA(6, 5) = 2.0 * M3[5];
+        AA(6, 6) = 2.0 * M4[0] - 2.0 * P[0] * DM2; AA(6, 7) = 2.0 * M4[1] - 2.0 * P[1] * DM2;
+        AA(6, 8) = 2.0 * M4[2] - 2.0 * P[2] * DM2;
+        AA(7, 0) = 2.0 * M3[1]; AA(7, 1) = Q[0] + 4.0 * M3[3]; AA(7, 2) = 4.0 * M3[4];
+        AA(7, 3) = Q[1] + 2.0 * M3[6]; AA(7, 4) = Q[2] + 4.0 * M3[7]; AA(7, 5) = 2.0 * M3[8];
+        AA(7, 6) = 2.0 * M4[1] - 2.0 * P[1] * DM2; AA(7, 7) = 2.0 * M4[3] - 2.0 * P[3] * DM2;
+        AA(7, 8) = 2.0 * M4[4] - 2.0 * P[4] * DM2;
+        AA(8, 0) = 2.0 * M3[2]; AA(8, 1) = 4.0 * M3[4]; AA(8, 2) = Q[0] + 4.0 * M3[5];
+        AA(8, 3) = 2.0 * M3[7]; AA(8, 4) = Q[1] + 4.0 * M3[8]; AA(8, 5) = Q[2] + 2.0 * M3[9];
+        AA(8, 6) = 2.0 * M4[2] - 2.0 * P[2] * DM2; AA(8, 7) = 2.0 * M4[4] - 2.0 * P[4] * DM2;
+        AA(8, 8) = 2.0 * M4[5] - 2.0 * P[5] * DM2;
+        AA(6, 6) += DM4 - (DM2) * (DM2);
+        AA(7, 7) += DM4 - (DM2) * (DM2);
+        AA(8, 8) += DM4 - (DM2) * (DM2);
+#undef AA
+        if (EXACT) gauss_jordan<9>(A, rhs, x);
+        else gauss_jordan_fast<9>(A, rhs, x);
+      }
     }
     for (int j = 0; j < 6; ++j) W(MCPM_CF_C + j, x[j]);
     for (int j = 0; j < 3; ++j) W(MCPM_CF_GAMMA + j, x[6 + j]);
