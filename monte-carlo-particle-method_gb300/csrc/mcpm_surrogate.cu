@@ -28,7 +28,7 @@
 // fp32 accumulate).  The same kernel computes the data gradient of the
 // backward pass (weights transposed and flipped, times the ReLU mask), and a
 // second kernel the weight gradient (the reduction over cells, ldmatrix
-// .trans operands).  The 64->64 forward layers of inference run on the
+// .trans operands).  Every forward layer of inference runs on the
 // fifth-generation tensor cores (tcgen05, mcpm_surrogate_tc.cu).
 //
 // Parameters: one fp32 array (layout SP_OFF_* below, [co][tap][ci] with
@@ -234,118 +234,6 @@ __global__ void __launch_bounds__(NT) k_conv(ConvArgs a) {
           if (ni == 0 && wn == 0) {
             const float w2 = __shfl_down_sync(0xffffffffu, v0, 1), w3 = __shfl_down_sync(0xffffffffu, v1, 1);
             if ((lane & 3) == 0 && p < a.P) {
-              const float d0 = (v0 + a.bias[0]) * a.oscale, d1 = (v1 + a.bias[1]) * a.oscale;
-              const float d2 = (w2 + a.bias[2]) * a.oscale, d3 = (w3 + a.bias[3]) * a.oscale;
-              *reinterpret_cast<float4*>(a.pcell + (size_t)p * PF_STRIDE + PF_LA1) =
-                  make_float4(d0 * a.g1, (d1 - d0) * a.g1, d2 * a.g2, (d3 - d2) * a.g2);
-            }
-          }
-        }
-      }
-    }
-}
-
-// Inference variant for the narrow layers (16 -> 64 and 64 -> 16): one
-// block per 128-cell row segment stages the whole 3-row halo of its input
-// (3 x 130 cells, zero outside the grid) and all nine weight taps once, then
-// runs the nine taps from shared memory -- a third of the per-tap tiles'
-// L2 traffic and one wait instead of nine.  Tiles never cross a grid row.
-template <int CIN, int COUT> constexpr int halo_a_bytes() { return 3 * (TM + 2) * CIN * 2; }
-template <int CIN, int COUT> constexpr int halo_smem() {
-  return ((halo_a_bytes<CIN, COUT>() + 127) / 128) * 128 + COUT * (9 * CIN + 8) * 2;
-}
-
-template <int CIN, int COUT, int EPI>
-__global__ void __launch_bounds__(NT) k_conv_halo(ConvArgs a, int tiles_per_row) {
-  constexpr int CH = CIN / 8, HW = TM + 2, HROWS = 3 * HW;
-  constexpr int KW = 9 * CIN, KWP = KW + 8;  // weight row, padded to an odd number of 16-byte chunks
-  constexpr int WN = COUT >= 64 ? 2 : 1, WM = 8 / WN, WTM = TM / WM, WTN = COUT / WN;
-  constexpr int MI = WTM / 16, NI = WTN / 8;
-  static_assert(NI % 2 == 0 && MI >= 1, "warp tile");
-  extern __shared__ __align__(128) unsigned char smem[];
-  unsigned char* As = smem;
-  unsigned char* Bs = smem + ((halo_a_bytes<CIN, COUT>() + 127) / 128) * 128;
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int wm = warp % WM, wn = warp / WM;
-  const int row = blockIdx.x / tiles_per_row, x0 = (blockIdx.x - row * tiles_per_row) * TM;
-  const int N0 = a.N0, N1 = a.N1;
-  const int b = row / N1, y = row - b * N1;
-  for (int e = tid; e < HROWS * CH; e += NT) {
-    const int hr = e / CH, ch = e - hr * CH, r3 = hr / HW, px = hr - r3 * HW;
-    const int yy = y + r3 - 1, xx = x0 + px - 1;
-    const bool v = yy >= 0 && yy < N1 && xx >= 0 && xx < N0;
-    const bf16* src = v ? a.x + ((size_t)(b * a.C + yy * N0 + xx) * CIN + ch * 8) : a.x;
-    cp_async16(smem_u32(As + swz<CH>(hr, ch)), src, v);
-  }
-  for (int e = tid; e < COUT * (KW / 8); e += NT) {
-    const int co = e / (KW / 8), kc = e - co * (KW / 8);
-    cp_async16(smem_u32(Bs + ((size_t)co * KWP + kc * 8) * 2), a.w + (size_t)co * KW + kc * 8, true);
-  }
-  cp_async_commit();
-  cp_async_wait<0>();
-  __syncthreads();
-
-  float acc[MI][NI][4];
-#pragma unroll
-  for (int i = 0; i < MI; ++i)
-#pragma unroll
-    for (int j = 0; j < NI; ++j)
-#pragma unroll
-      for (int q = 0; q < 4; ++q) acc[i][j][q] = 0.f;
-#pragma unroll 1
-  for (int tap = 0; tap < 9; ++tap) {
-    const int dy = tap / 3 - 1, dx = tap % 3 - 1;
-#pragma unroll
-    for (int kk = 0; kk < CIN / 16; ++kk) {
-      uint32_t af[MI][4], bfr[NI][2];
-#pragma unroll
-      for (int mi = 0; mi < MI; ++mi) {
-        const int hr = (dy + 1) * HW + wm * WTM + mi * 16 + (lane & 15) + dx + 1;
-        ldsm_x4(af[mi], smem_u32(As + swz<CH>(hr, kk * 2 + (lane >> 4))));
-      }
-#pragma unroll
-      for (int ni = 0; ni < NI; ni += 2) {
-        const int co = wn * WTN + ni * 8 + (lane & 7) + ((lane >> 4) << 3);
-        const int kq = tap * CIN + kk * 16 + ((lane >> 3) & 1) * 8;
-        uint32_t r[4];
-        ldsm_x4(r, smem_u32(Bs + ((size_t)co * KWP + kq) * 2));
-        bfr[ni][0] = r[0]; bfr[ni][1] = r[1]; bfr[ni + 1][0] = r[2]; bfr[ni + 1][1] = r[3];
-      }
-#pragma unroll
-      for (int mi = 0; mi < MI; ++mi)
-#pragma unroll
-        for (int ni = 0; ni < NI; ++ni) mma16816(acc[mi][ni], af[mi], bfr[ni][0], bfr[ni][1]);
-    }
-  }
-
-#pragma unroll
-  for (int mi = 0; mi < MI; ++mi)
-#pragma unroll
-    for (int h = 0; h < 2; ++h) {
-      const int xi = x0 + wm * WTM + mi * 16 + (lane >> 2) + h * 8;
-      const bool ok = xi < N0;
-      const int p = row * N0 + xi;
-#pragma unroll
-      for (int ni = 0; ni < NI; ++ni) {
-        const int col = wn * WTN + ni * 8 + 2 * (lane & 3);
-        float v0 = acc[mi][ni][2 * h], v1 = acc[mi][ni][2 * h + 1];
-        if constexpr (EPI == EPI_RELU) {
-          v0 = fmaxf(v0 + a.bias[col], 0.f);
-          v1 = fmaxf(v1 + a.bias[col + 1], 0.f);
-          if (ok)
-            *reinterpret_cast<__nv_bfloat162*>(static_cast<bf16*>(a.out) + (size_t)p * COUT + col) =
-                __floats2bfloat162_rn(v0, v1);
-        } else if constexpr (EPI == EPI_OUT) {
-          if (col < 4 && ok) {
-            float* o = static_cast<float*>(a.out) + (size_t)p * 4 + col;
-            o[0] = v0 + a.bias[col];
-            o[1] = v1 + a.bias[col + 1];
-          }
-        } else {  // EPI_KICK: lanes 4q hold outputs 0, 1 of a cell, lanes 4q + 1 outputs 2, 3
-          static_assert(EPI == EPI_KICK, "inference epilogues");
-          if (ni == 0 && wn == 0) {
-            const float w2 = __shfl_down_sync(0xffffffffu, v0, 1), w3 = __shfl_down_sync(0xffffffffu, v1, 1);
-            if ((lane & 3) == 0 && ok) {
               const float d0 = (v0 + a.bias[0]) * a.oscale, d1 = (v1 + a.bias[1]) * a.oscale;
               const float d2 = (w2 + a.bias[2]) * a.oscale, d3 = (w3 + a.bias[3]) * a.oscale;
               *reinterpret_cast<float4*>(a.pcell + (size_t)p * PF_STRIDE + PF_LA1) =
@@ -655,9 +543,6 @@ static bool set_smem_attrs() {
   set((const void*)k_conv<64, 16, EPI_KICK>, conv_smem<64, 16>());
   set((const void*)k_conv<16, 64, EPI_MASK>, conv_smem<16, 64>());
   set((const void*)k_conv<64, 64, EPI_MASK>, conv_smem<64, 64>());
-  set((const void*)k_conv_halo<16, 64, EPI_RELU>, halo_smem<16, 64>());
-  set((const void*)k_conv_halo<64, 16, EPI_KICK>, halo_smem<64, 16>());
-  set((const void*)k_conv_halo<64, 16, EPI_OUT>, halo_smem<64, 16>());
   set((const void*)k_wgrad<16, 64>, wgrad_smem<16, 64>());
   set((const void*)k_wgrad<64, 64>, wgrad_smem<64, 64>());
   set((const void*)k_wgrad<64, 16>, wgrad_smem<64, 16>());
@@ -681,20 +566,32 @@ static int forward(SurrogateNet& n, const bf16* x, int B, float* y, float* pcell
                    cudaStream_t st, bool allow_tc, uint32_t* status) {
   const int P = B * n.C;
   int launches = 0;
-  // the inference path (allow_tc): halo-tiled narrow layers, tcgen05 wide
-  // ones; the training path: the per-tap kernels the backward pass mirrors
-  const bool infer = allow_tc && n.tc;
-  const int tpr = (n.N0 + TM - 1) / TM, htiles = B * n.N1 * tpr;
+  // the inference path (allow_tc): every layer on tcgen05 (the per-tap
+  // mma.sync kernels if a tensor map is refused); the training path: the
+  // per-tap kernels the backward pass mirrors
+  bool infer = allow_tc && n.tc;
+  auto refused = [&]() {
+    n.tc = false;
+    n.err = "tensor map rejected; the tcgen05 path is off for this network";
+  };
   ConvArgs a = cargs(n, P);
   a.x = x; a.w = n.w16 + SP_OFF_W1; a.bias = n.p32 + SP_OFF_B1; a.out = n.a1;
-  if (infer) k_conv_halo<16, 64, EPI_RELU><<<htiles, NT, halo_smem<16, 64>(), st>>>(a, tpr);
-  else conv<16, 64, EPI_RELU>(n, a, st);
-  ++launches;
+  int r1 = infer ? tc_conv16_relu(x, n.w16 + SP_OFF_W1, n.p32 + SP_OFF_B1, n.a1, n.N0, n.N1, P, n.num_sms, status, st)
+                 : 0;
+  if (r1 > 0) {
+    launches += r1;
+    n.tc_launches += r1;
+  } else {
+    if (infer) refused();
+    infer = false;
+    conv<16, 64, EPI_RELU>(n, a, st);
+    ++launches;
+  }
   for (int l = 0; l < 2; ++l) {
     const bf16* in = l == 0 ? n.a1 : n.a2;
     bf16* out = l == 0 ? n.a2 : n.a3;
     const int wo = l == 0 ? SP_OFF_W2 : SP_OFF_W3, bo = l == 0 ? SP_OFF_B2 : SP_OFF_B3;
-    if (allow_tc && n.tc) {
+    if (infer) {
       const int r = tc_conv64_relu(in, n.w16 + wo, n.p32 + bo, out, n.N0, n.N1, P, n.num_sms, status, st);
       if (r > 0) {
         launches += r;
@@ -702,8 +599,8 @@ static int forward(SurrogateNet& n, const bf16* x, int B, float* y, float* pcell
         continue;
       }
       // the TMA descriptor was refused: this network stays on mma.sync
-      n.tc = false;
-      n.err = "tensor map rejected; the tcgen05 path is off for this network";
+      refused();
+      infer = false;
     }
     a = cargs(n, P);
     a.x = in; a.w = n.w16 + wo; a.bias = n.p32 + bo; a.out = out;
@@ -712,14 +609,21 @@ static int forward(SurrogateNet& n, const bf16* x, int B, float* y, float* pcell
   }
   a = cargs(n, P);
   a.x = n.a3; a.w = n.w16 + SP_OFF_W4; a.bias = n.p32 + SP_OFF_B4;
+  if (infer) {
+    const int r = tc_conv_out(n.a3, n.w16 + SP_OFF_W4, n.p32 + SP_OFF_B4, y, pcell, g1, g2, (float)n.oscale, n.N0,
+                              n.N1, P, n.num_sms, status, st);
+    if (r > 0) {
+      n.tc_launches += r;
+      return launches + r;
+    }
+    refused();
+  }
   if (pcell) {
     a.pcell = pcell; a.g1 = g1; a.g2 = g2; a.oscale = (float)n.oscale;
-    if (infer) k_conv_halo<64, 16, EPI_KICK><<<htiles, NT, halo_smem<64, 16>(), st>>>(a, tpr);
-    else conv<64, 16, EPI_KICK>(n, a, st);
+    conv<64, 16, EPI_KICK>(n, a, st);
   } else {
     a.out = y;
-    if (infer) k_conv_halo<64, 16, EPI_OUT><<<htiles, NT, halo_smem<64, 16>(), st>>>(a, tpr);
-    else conv<64, 16, EPI_OUT>(n, a, st);
+    conv<64, 16, EPI_OUT>(n, a, st);
   }
   return launches + 1;
 }

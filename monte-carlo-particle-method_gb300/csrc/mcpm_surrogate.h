@@ -64,11 +64,17 @@ __device__ __forceinline__ void sur_hi_lo(double v, __nv_bfloat16& hi, __nv_bflo
   lo = __float2bfloat16_rn((float)(v - (double)__bfloat162float(hi)));
 }
 
-// tcgen05 implicit-GEMM 3x3 convolution 64 -> 64 channels with bias and
-// ReLU (mcpm_surrogate_tc.cu); returns the launches
+// tcgen05 implicit-GEMM 3x3 convolutions of inference (mcpm_surrogate_tc.cu):
+// 64 -> 64 and 16 -> 64 with bias and ReLU, and the 64 -> 16 output layer
+// (its four used outputs into pcell's kick coefficients, or as y [P][4]);
+// each returns its launches, -1 when a tensor map was refused
 int tc_setup();
 int tc_conv64_relu(const __nv_bfloat16* x, const __nv_bfloat16* w, const float* bias, __nv_bfloat16* out, int N0,
                    int N1, int P, int num_sms, uint32_t* status, cudaStream_t st);
+int tc_conv16_relu(const __nv_bfloat16* x, const __nv_bfloat16* w, const float* bias, __nv_bfloat16* out, int N0,
+                   int N1, int P, int num_sms, uint32_t* status, cudaStream_t st);
+int tc_conv_out(const __nv_bfloat16* x, const __nv_bfloat16* w, const float* bias, float* y, float* pcell, float g1,
+                float g2, float oscale, int N0, int N1, int P, int num_sms, uint32_t* status, cudaStream_t st);
 
 // session-side launchers (mcpm_surrogate.cu); each returns its launches
 int sur_forward_kick(Session& s, const double* nnd, const double* ncell);

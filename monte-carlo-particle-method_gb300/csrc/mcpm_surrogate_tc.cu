@@ -1,21 +1,25 @@
-// mcpm_surrogate_tc.cu -- the 64 -> 64 channel 3x3 convolutions of the
-// learned Vlasov force on the fifth-generation tensor cores (tcgen05).
+// mcpm_surrogate_tc.cu -- the 3x3 convolutions of the learned Vlasov force's
+// inference on the fifth-generation tensor cores (tcgen05): the 16 -> 64
+// input layer, the two 64 -> 64 layers and the 64 -> 16 output layer.
 //
 // Implicit GEMM per output tile of 128 consecutive cells of one grid row
-// (M = 128) and all 64 output channels (N = 64), reduced over 9 taps x 64
-// input channels (K = 576):
-//   * the activations are an NHWC bf16 tensor [B][N1][N0][64]; the tile of
-//     tap (dy, dx) is one TMA box {64 ch, 128 cells, 1, 1} at (0, x0 + dx,
+// (M = 128) and all COUT output channels (N = COUT), reduced over 9 taps x
+// CIN input channels (K = 9 CIN):
+//   * the activations are an NHWC bf16 tensor [B][N1][N0][CIN]; the tile of
+//     tap (dy, dx) is one TMA box {CIN ch, 128 cells, 1, 1} at (0, x0 + dx,
 //     y + dy, b) -- boxes reaching past the grid are zero-filled by the TMA
 //     unit, which is the convolution's zero padding;
-//   * the 9 weight tiles [64 co][64 ci] stay in shared memory for the life
-//     of the persistent block (72 KB);
-//   * both operands land with the 128-byte swizzle that the K-major UMMA
-//     shared-memory descriptor reads; each tap issues 4 tcgen05.mma of
-//     K = 16 into an fp32 accumulator of 64 TMEM columns;
+//   * the 9 weight tiles [COUT co][CIN ci] stay in shared memory for the
+//     life of the persistent block;
+//   * both operands land with the swizzle that the K-major UMMA
+//     shared-memory descriptor reads (rows of 2 CIN bytes: the 128-byte
+//     swizzle for CIN = 64, the 32-byte one for CIN = 16); each tap issues
+//     CIN / 16 tcgen05.mma of K = 16 into an fp32 accumulator of COUT TMEM
+//     columns;
 //   * two accumulators alternate so that the epilogue of one tile (TMEM ->
-//     registers, + bias, ReLU, bf16, global store) overlaps the MMAs of the
-//     next.
+//     registers, + bias, then ReLU to bf16, or the output layer's kick
+//     coefficients into the packed cell record, or its four outputs)
+//     overlaps the MMAs of the next.
 // Warp roles (6 warps): warp 0 issues the TMA loads, warp 1 allocates TMEM
 // and issues the MMAs, warps 2-5 drain the accumulators (warp w reads TMEM
 // lanes 32 (w % 4) .. 32 (w % 4) + 31).  Every mbarrier wait is bounded
@@ -29,20 +33,38 @@
 #include <cstring>
 
 #include "../../include/mcpm.h"
+#include "mcpm_internal.h"
 #include "mcpm_surrogate.h"
 
 namespace mcpm {
 namespace tc {
 
-constexpr int TM = 128, TN = 64, NSTAGE = 4, NTHREADS = 192;
-constexpr int A_BYTES = TM * 128;              // one tap of the activation tile
-constexpr int B_BYTES = TN * 128;              // one tap of the weights
-constexpr int SMEM_B = 0;                      // 9 weight taps
-constexpr int SMEM_A = SMEM_B + 9 * B_BYTES;   // NSTAGE activation stages
-constexpr int SMEM_BAR = SMEM_A + NSTAGE * A_BYTES;
-constexpr int SMEM_BYTES = SMEM_BAR + 256 + 1024;  // barriers + alignment slack
-constexpr uint32_t TMEM_COLS = 128;            // two accumulators of 64 columns
+constexpr int TM = 128, NSTAGE = 4, NTHREADS = 192;
 constexpr uint64_t WAIT_NS = 1000000000ull;    // bound of every wait
+// epilogues: bias + ReLU to bf16 activations; the output layer's kick
+// coefficients into the packed cell record; its four outputs as fp32
+enum { TEPI_RELU = 0, TEPI_KICK = 1, TEPI_OUT = 2 };
+
+// the shape of one layer: rows of RB = 2 CIN bytes
+template <int CIN, int COUT> struct Cfg {
+  static_assert(CIN == 16 || CIN == 64, "input rows of 32 or 128 bytes");
+  static_assert(COUT % 16 == 0 && COUT >= 16 && COUT <= 256, "UMMA N for M = 128");
+  static constexpr int RB = 2 * CIN;
+  static constexpr int A_BYTES = TM * RB;              // one tap of the activation tile
+  static constexpr int B_BYTES = COUT * RB;            // one tap of the weights
+  static constexpr int SMEM_B = 0;                     // 9 weight taps
+  static constexpr int SMEM_A = SMEM_B + 9 * B_BYTES;  // NSTAGE activation stages
+  static constexpr int SMEM_BAR = SMEM_A + NSTAGE * A_BYTES;
+  static constexpr int SMEM_BYTES = SMEM_BAR + 256 + 1024;  // barriers + alignment slack
+  static constexpr uint32_t TMEM_COLS = 2 * COUT < 32 ? 32u : (uint32_t)(2 * COUT);  // two accumulators
+  static constexpr int KSTEPS = CIN / 16;
+  // descriptor layout type: SWIZZLE_128B (2) or SWIZZLE_32B (6); the stride
+  // between 8-row groups is 8 rows
+  static constexpr uint64_t LAYOUT = CIN == 64 ? 2 : 6;
+  static constexpr uint32_t SBO = 8 * RB;
+  static_assert(SMEM_A % 1024 == 0 && A_BYTES % 1024 == 0 && B_BYTES % 256 == 0, "swizzle atoms aligned");
+  static_assert(CIN == 16 || B_BYTES % 1024 == 0, "128-byte swizzle atoms aligned");
+};
 
 struct Bars {
   uint64_t full[NSTAGE], empty[NSTAGE], acc_full[2], acc_empty[2], wbar, done;
@@ -105,22 +127,22 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, i
       "l"((uint64_t)map), "r"(c0), "r"(c1), "r"(su32(bar))
       : "memory");
 }
-// K-major operand with 128-byte rows, 128-byte swizzle, 8-row groups 1024
-// bytes apart (stride byte offset), descriptor version 1, layout code 2
-__device__ __forceinline__ uint64_t sdesc(uint32_t saddr) {
+// K-major operand: rows of 2 CIN bytes swizzled at that width, 8-row
+// groups SBO bytes apart (stride byte offset), descriptor version 1
+template <int CIN, int COUT> __device__ __forceinline__ uint64_t sdesc(uint32_t saddr) {
   uint64_t d = 0;
   d |= (uint64_t)((saddr & 0x3FFFF) >> 4);
-  d |= (uint64_t)1 << 16;             // leading byte offset (unused for swizzled K-major)
-  d |= (uint64_t)(1024 >> 4) << 32;   // stride byte offset
-  d |= (uint64_t)1 << 46;             // version
-  d |= (uint64_t)2 << 61;             // SWIZZLE_128B
+  d |= (uint64_t)1 << 16;                               // leading byte offset (unused for swizzled K-major)
+  d |= (uint64_t)(Cfg<CIN, COUT>::SBO >> 4) << 32;      // stride byte offset
+  d |= (uint64_t)1 << 46;                               // version
+  d |= Cfg<CIN, COUT>::LAYOUT << 61;                    // swizzle mode
   return d;
 }
 // kind::f16 instruction descriptor: fp32 accumulator, bf16 A and B, both
-// K-major, N = 64, M = 128
-constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(TN >> 3) << 17) | ((uint32_t)(TM >> 4) << 24);
-
-__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t acc) {
+// K-major, N = COUT, M = 128
+template <int COUT> __device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t acc) {
+  constexpr uint32_t IDESC =
+      (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(COUT >> 3) << 17) | ((uint32_t)(TM >> 4) << 24);
   asm volatile(
       "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
           d_tmem),
@@ -143,14 +165,22 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
 struct Args {
-  const float* bias;        // [64]
-  __nv_bfloat16* out;       // [P][64]
+  const float* bias;        // [COUT]
+  void* out;                // bf16 [P][COUT] (TEPI_RELU), fp32 [P][4] (TEPI_OUT)
+  float* pcell;             // packed per-cell record (TEPI_KICK)
   uint32_t* status;
   int N0, N1, rows, tiles_per_row, ntiles;  // rows = B N1
+  float g1, g2, oscale;                     // TEPI_KICK
 };
 
+template <int CIN, int COUT, int EPI>
 __global__ void __launch_bounds__(NTHREADS, 1)
-    k_conv64_tc(const __grid_constant__ CUtensorMap tmx, const __grid_constant__ CUtensorMap tmw, Args a) {
+    k_conv_tc(const __grid_constant__ CUtensorMap tmx, const __grid_constant__ CUtensorMap tmw, Args a) {
+  using L = Cfg<CIN, COUT>;
+  constexpr int A_BYTES = L::A_BYTES, B_BYTES = L::B_BYTES, SMEM_A = L::SMEM_A, SMEM_B = L::SMEM_B,
+                SMEM_BAR = L::SMEM_BAR;
+  constexpr uint32_t TMEM_COLS = L::TMEM_COLS;
+  static_assert(EPI == TEPI_RELU ? COUT == 64 : COUT == 16, "epilogue shapes");
   extern __shared__ unsigned char smem_raw[];
   unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   Bars* bars = reinterpret_cast<Bars*>(smem + SMEM_BAR);
@@ -181,7 +211,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       // producer: the weights once, then one activation box per tap
       asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&tmx) : "memory");
       bar_expect_tx(&bars->wbar, 9 * B_BYTES);
-      for (int t = 0; t < 9; ++t) tma_load_2d(smem + SMEM_B + t * B_BYTES, &tmw, t * 64, 0, &bars->wbar);
+      for (int t = 0; t < 9; ++t) tma_load_2d(smem + SMEM_B + t * B_BYTES, &tmw, t * CIN, 0, &bars->wbar);
       int last_par[NSTAGE];
       for (int s = 0; s < NSTAGE; ++s) last_par[s] = -1;
       uint32_t i = 0;
@@ -214,15 +244,15 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         const uint32_t buf = j & 1, aph = (j >> 1) & 1;
         if (!(ok = bar_wait(&bars->acc_empty[buf], aph ^ 1, abort, a.status))) break;
         fence_after();
-        const uint32_t d = tmem + buf * TN;
+        const uint32_t d = tmem + buf * COUT;
         for (int tap = 0; tap < 9; ++tap, ++i) {
           const int s = i % NSTAGE;
           if (!(ok = bar_wait(&bars->full[s], (i / NSTAGE) & 1, abort, a.status))) break;
           fence_after();
 #pragma unroll
-          for (int kk = 0; kk < 4; ++kk)
-            mma_bf16(d, sdesc(sa + s * A_BYTES + kk * 32), sdesc(sb + tap * B_BYTES + kk * 32),
-                     (tap | kk) != 0 ? 1u : 0u);
+          for (int kk = 0; kk < L::KSTEPS; ++kk)
+            mma_bf16<COUT>(d, sdesc<CIN, COUT>(sa + s * A_BYTES + kk * 32),
+                           sdesc<CIN, COUT>(sb + tap * B_BYTES + kk * 32), (tap | kk) != 0 ? 1u : 0u);
           mma_commit(&bars->empty[s]);  // the stage is free once these MMAs have read it
         }
         if (!ok) break;
@@ -241,10 +271,11 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       if (!bar_wait(&bars->acc_full[buf], aph, abort, a.status)) break;
       __syncwarp();
       fence_after();
-      uint32_t r[4][16];
-      const uint32_t taddr = tmem + ((uint32_t)(32 * q) << 16) + buf * TN;
+      constexpr int NC = COUT / 16;
+      uint32_t r[NC][16];
+      const uint32_t taddr = tmem + ((uint32_t)(32 * q) << 16) + buf * COUT;
 #pragma unroll
-      for (int c = 0; c < 4; ++c) tmem_ld16(taddr + c * 16, r[c]);
+      for (int c = 0; c < NC; ++c) tmem_ld16(taddr + c * 16, r[c]);
       tmem_wait_ld();
       fence_before();
       __syncwarp();
@@ -253,18 +284,31 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       const int x = x0 + 32 * q + lane;
       if (x < a.N0) {
         const size_t p = (size_t)row * a.N0 + x;
-        uint4* o = reinterpret_cast<uint4*>(a.out + p * 64);
+        if constexpr (EPI == TEPI_RELU) {
+          uint4* o = reinterpret_cast<uint4*>(static_cast<__nv_bfloat16*>(a.out) + p * COUT);
 #pragma unroll
-        for (int c = 0; c < 4; ++c) {
-          __nv_bfloat162 h[8];
+          for (int c = 0; c < NC; ++c) {
+            __nv_bfloat162 h[8];
 #pragma unroll
-          for (int e = 0; e < 8; ++e) {
-            const float v0 = fmaxf(__uint_as_float(r[c][2 * e]) + a.bias[c * 16 + 2 * e], 0.f);
-            const float v1 = fmaxf(__uint_as_float(r[c][2 * e + 1]) + a.bias[c * 16 + 2 * e + 1], 0.f);
-            h[e] = __floats2bfloat162_rn(v0, v1);
+            for (int e = 0; e < 8; ++e) {
+              const float v0 = fmaxf(__uint_as_float(r[c][2 * e]) + a.bias[c * 16 + 2 * e], 0.f);
+              const float v1 = fmaxf(__uint_as_float(r[c][2 * e + 1]) + a.bias[c * 16 + 2 * e + 1], 0.f);
+              h[e] = __floats2bfloat162_rn(v0, v1);
+            }
+            o[2 * c] = *reinterpret_cast<uint4*>(&h[0]);
+            o[2 * c + 1] = *reinterpret_cast<uint4*>(&h[4]);
           }
-          o[2 * c] = *reinterpret_cast<uint4*>(&h[0]);
-          o[2 * c + 1] = *reinterpret_cast<uint4*>(&h[4]);
+        } else {
+          // outputs 0..3: the differences of the cell's corner potentials
+          const float o0 = __uint_as_float(r[0][0]) + a.bias[0], o1 = __uint_as_float(r[0][1]) + a.bias[1];
+          const float o2 = __uint_as_float(r[0][2]) + a.bias[2], o3 = __uint_as_float(r[0][3]) + a.bias[3];
+          if constexpr (EPI == TEPI_KICK) {
+            const float d0 = o0 * a.oscale, d1 = o1 * a.oscale, d2 = o2 * a.oscale, d3 = o3 * a.oscale;
+            *reinterpret_cast<float4*>(a.pcell + p * PF_STRIDE + PF_LA1) =
+                make_float4(d0 * a.g1, (d1 - d0) * a.g1, d2 * a.g2, (d3 - d2) * a.g2);
+          } else {
+            *reinterpret_cast<float4*>(static_cast<float*>(a.out) + p * 4) = make_float4(o0, o1, o2, o3);
+          }
         }
       }
     }
@@ -283,6 +327,53 @@ static EncodeTiled g_encode = nullptr;
 
 }  // namespace tc
 
+namespace tc {
+template <int CIN, int COUT, int EPI> static int set_smem() {
+  return cudaFuncSetAttribute(k_conv_tc<CIN, COUT, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              Cfg<CIN, COUT>::SMEM_BYTES) == cudaSuccess
+             ? 0
+             : 1;
+}
+
+// the activation map [B][N1][N0][CIN] read as boxes {CIN, 128, 1, 1}, and the
+// weights [COUT][9 CIN] as boxes {CIN, COUT} (one tap), both swizzled as the
+// UMMA descriptors read them
+template <int CIN, int COUT>
+static bool maps(const void* x, const void* w, int N0, int N1, int B, CUtensorMap& mx, CUtensorMap& mw) {
+  const CUtensorMapSwizzle sw = CIN == 64 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_32B;
+  const cuuint64_t rb = 2 * CIN;
+  cuuint64_t dims[4] = {(cuuint64_t)CIN, (cuuint64_t)N0, (cuuint64_t)N1, (cuuint64_t)B};
+  cuuint64_t strides[3] = {rb, (cuuint64_t)N0 * rb, (cuuint64_t)N0 * N1 * rb};
+  cuuint32_t box[4] = {(cuuint32_t)CIN, TM, 1, 1}, es[4] = {1, 1, 1, 1};
+  if (g_encode(&mx, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void*>(x), dims, strides, box, es,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, sw, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+    return false;
+  cuuint64_t wd[2] = {(cuuint64_t)(9 * CIN), (cuuint64_t)COUT};
+  cuuint64_t ws[1] = {(cuuint64_t)(9 * CIN * 2)};
+  cuuint32_t wb[2] = {(cuuint32_t)CIN, (cuuint32_t)COUT}, we[2] = {1, 1};
+  return g_encode(&mw, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(w), wd, ws, wb, we,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, sw, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// one layer over P cells (whole grid rows of N0 cells); returns the launches,
+// -1 if a tensor map was refused
+template <int CIN, int COUT, int EPI>
+static int launch(const __nv_bfloat16* x, const __nv_bfloat16* w, Args a, int P, int num_sms, cudaStream_t st) {
+  if (!g_encode || P <= 0) return 0;
+  const int rows = P / a.N0, B = rows / a.N1;
+  CUtensorMap mx, mw;
+  if (!maps<CIN, COUT>(x, w, a.N0, a.N1, B, mx, mw)) return -1;
+  a.rows = rows;
+  a.tiles_per_row = (a.N0 + TM - 1) / TM;
+  a.ntiles = rows * a.tiles_per_row;
+  const int grid = a.ntiles < num_sms ? a.ntiles : num_sms;
+  k_conv_tc<CIN, COUT, EPI><<<grid, NTHREADS, Cfg<CIN, COUT>::SMEM_BYTES, st>>>(mx, mw, a);
+  return 1;
+}
+}  // namespace tc
+
 int tc_setup() {
   using namespace tc;
   if (!g_encode) {
@@ -295,49 +386,50 @@ int tc_setup() {
     }
     g_encode = (EncodeTiled)fn;
   }
-  if (cudaFuncSetAttribute(k_conv64_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES) != cudaSuccess) {
+  if (set_smem<64, 64, TEPI_RELU>() | set_smem<16, 64, TEPI_RELU>() | set_smem<64, 16, TEPI_KICK>() |
+      set_smem<64, 16, TEPI_OUT>()) {
     cudaGetLastError();
     return 1;
   }
   return 0;
 }
 
-int tc_conv64_relu(const __nv_bfloat16* x, const __nv_bfloat16* w, const float* bias, __nv_bfloat16* out, int N0,
-                   int N1, int P, int num_sms, uint32_t* status, cudaStream_t st) {
-  using namespace tc;
-  if (!g_encode || P <= 0) return 0;
-  const int rows = P / N0, B = rows / N1;
-  CUtensorMap mx, mw;
-  {
-    cuuint64_t dims[4] = {64, (cuuint64_t)N0, (cuuint64_t)N1, (cuuint64_t)B};
-    cuuint64_t strides[3] = {128, (cuuint64_t)N0 * 128, (cuuint64_t)N0 * N1 * 128};
-    cuuint32_t box[4] = {64, TM, 1, 1}, es[4] = {1, 1, 1, 1};
-    if (g_encode(&mx, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, (void*)x, dims, strides, box, es,
-                 CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                 CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
-      return -1;
-  }
-  {
-    cuuint64_t dims[2] = {576, 64};
-    cuuint64_t strides[1] = {576 * 2};
-    cuuint32_t box[2] = {64, 64}, es[2] = {1, 1};
-    if (g_encode(&mw, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (void*)w, dims, strides, box, es,
-                 CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                 CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
-      return -1;
-  }
-  Args a;
+static tc::Args base_args(const float* bias, int N0, int N1, uint32_t* status) {
+  tc::Args a;
+  std::memset(&a, 0, sizeof a);
   a.bias = bias;
-  a.out = out;
   a.status = status;
   a.N0 = N0;
   a.N1 = N1;
-  a.rows = rows;
-  a.tiles_per_row = (N0 + TM - 1) / TM;
-  a.ntiles = rows * a.tiles_per_row;
-  const int grid = a.ntiles < num_sms ? a.ntiles : num_sms;
-  k_conv64_tc<<<grid, NTHREADS, SMEM_BYTES, st>>>(mx, mw, a);
-  return 1;
+  return a;
+}
+
+int tc_conv64_relu(const __nv_bfloat16* x, const __nv_bfloat16* w, const float* bias, __nv_bfloat16* out, int N0,
+                   int N1, int P, int num_sms, uint32_t* status, cudaStream_t st) {
+  tc::Args a = base_args(bias, N0, N1, status);
+  a.out = out;
+  return tc::launch<64, 64, tc::TEPI_RELU>(x, w, a, P, num_sms, st);
+}
+
+int tc_conv16_relu(const __nv_bfloat16* x, const __nv_bfloat16* w, const float* bias, __nv_bfloat16* out, int N0,
+                   int N1, int P, int num_sms, uint32_t* status, cudaStream_t st) {
+  tc::Args a = base_args(bias, N0, N1, status);
+  a.out = out;
+  return tc::launch<16, 64, tc::TEPI_RELU>(x, w, a, P, num_sms, st);
+}
+
+int tc_conv_out(const __nv_bfloat16* x, const __nv_bfloat16* w, const float* bias, float* y, float* pcell, float g1,
+                float g2, float oscale, int N0, int N1, int P, int num_sms, uint32_t* status, cudaStream_t st) {
+  tc::Args a = base_args(bias, N0, N1, status);
+  if (pcell) {
+    a.pcell = pcell;
+    a.g1 = g1;
+    a.g2 = g2;
+    a.oscale = oscale;
+    return tc::launch<64, 16, tc::TEPI_KICK>(x, w, a, P, num_sms, st);
+  }
+  a.out = y;
+  return tc::launch<64, 16, tc::TEPI_OUT>(x, w, a, P, num_sms, st);
 }
 
 }  // namespace mcpm
