@@ -520,7 +520,7 @@ def run_mcpm(args):
         plain_ms = force_eval_ms(s, stream, 0)
         fl = SURROGATE_FLOP_PER_CELL * cfg.n_cells[0] * cfg.n_cells[1]
         tf, tf_kind = _bf16_peak()
-        roofline["surrogate"] = {"bound": "tensor", "kernels": "k_input + 4 conv (2 x k_conv64_tc)",
+        roofline["surrogate"] = {"bound": "tensor", "kernels": "k_input + 4 tcgen05 convolutions (k_conv_tc)",
                                  "achieved": round(fl / (sur_ms / 1e3) / 1e12, 2), "peak": tf, "unit": "TFLOP/s",
                                  "frac": round(fl / (sur_ms / 1e3) / 1e12 / tf, 4), "peak_kind": tf_kind,
                                  "flop_per_inference": fl, "ms_per_inference": round(sur_ms, 4),

@@ -41,13 +41,18 @@ __device__ __forceinline__ uint4 philox_rk(uint4 c, const uint32_t (&rk)[20]) {
   return c;
 }
 
-// the four words of a draw: the stream's injected row (key + counter) mod
-// rows when the caller injected uniforms for it, else Philox keyed by the
-// seed with counter (key, step, stream, counter)
+// an injected draw: row (key + counter) mod rows of the caller's table (a
+// call out of line, so that the Philox path keeps its registers)
+static __device__ __noinline__ uint4 rng_injected(const uint4* inj, uint32_t rows, uint32_t key, uint32_t ctr) {
+  return inj[((uint64_t)key + ctr) % rows];
+}
+// the four words of a draw: the stream's injected row when the caller
+// injected uniforms for it, else Philox keyed by the seed with counter
+// (key, step, stream, counter)
 __device__ __forceinline__ uint4 rng_draw(const DevConsts& k, uint32_t key, uint32_t step, uint32_t stream,
                                           uint32_t ctr) {
   const uint4* inj = k.rng_inj[stream];
-  if (inj) return inj[((uint64_t)key + ctr) % k.rng_inj_rows[stream]];
+  if (__builtin_expect(inj != nullptr, 0)) return rng_injected(inj, k.rng_inj_rows[stream], key, ctr);
   return philox_rk(make_uint4(key, step, stream, ctr), k.rk);
 }
 

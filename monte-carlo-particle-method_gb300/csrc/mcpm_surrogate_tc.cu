@@ -39,7 +39,7 @@
 namespace mcpm {
 namespace tc {
 
-constexpr int TM = 128, NSTAGE = 4, NTHREADS = 192;
+constexpr int TM = 128, NTHREADS = 192, MAXSTAGE = 16;
 constexpr uint64_t WAIT_NS = 1000000000ull;    // bound of every wait
 // epilogues: bias + ReLU to bf16 activations; the output layer's kick
 // coefficients into the packed cell record; its four outputs as fp32
@@ -50,12 +50,21 @@ template <int CIN, int COUT> struct Cfg {
   static_assert(CIN == 16 || CIN == 64, "input rows of 32 or 128 bytes");
   static_assert(COUT % 16 == 0 && COUT >= 16 && COUT <= 256, "UMMA N for M = 128");
   static constexpr int RB = 2 * CIN;
+  // activation stages in flight (the 4 KB taps of the input layer need a
+  // deeper queue to cover the TMA latency than the 16 KB ones), and the
+  // persistent blocks per SM: the narrow layers' MMAs are short, so several
+  // blocks per SM overlap their load latencies (shared memory and TMEM allow
+  // it: 3 x 68 KB and 3 x 128 columns, 2 x 84 KB and 2 x 32 columns)
+  static constexpr int NSTAGE = CIN == 16 ? 12 : (COUT == 16 ? 4 : 8);
+  static constexpr int CTAS_PER_SM = CIN == 16 ? 3 : (COUT == 16 ? 2 : 1);
+  static_assert(NSTAGE <= MAXSTAGE, "barrier slots");
   static constexpr int A_BYTES = TM * RB;              // one tap of the activation tile
   static constexpr int B_BYTES = COUT * RB;            // one tap of the weights
   static constexpr int SMEM_B = 0;                     // 9 weight taps
   static constexpr int SMEM_A = SMEM_B + 9 * B_BYTES;  // NSTAGE activation stages
   static constexpr int SMEM_BAR = SMEM_A + NSTAGE * A_BYTES;
-  static constexpr int SMEM_BYTES = SMEM_BAR + 256 + 1024;  // barriers + alignment slack
+  static constexpr int SMEM_BYTES = SMEM_BAR + 512 + 1024;  // barriers + alignment slack
+  static_assert(SMEM_BYTES <= 227 * 1024, "shared memory per block");
   static constexpr uint32_t TMEM_COLS = 2 * COUT < 32 ? 32u : (uint32_t)(2 * COUT);  // two accumulators
   static constexpr int KSTEPS = CIN / 16;
   // descriptor layout type: SWIZZLE_128B (2) or SWIZZLE_32B (6); the stride
@@ -67,7 +76,7 @@ template <int CIN, int COUT> struct Cfg {
 };
 
 struct Bars {
-  uint64_t full[NSTAGE], empty[NSTAGE], acc_full[2], acc_empty[2], wbar, done;
+  uint64_t full[MAXSTAGE], empty[MAXSTAGE], acc_full[2], acc_empty[2], wbar, done;
   uint32_t tmem_base;
   int abort;
 };
@@ -180,6 +189,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   constexpr int A_BYTES = L::A_BYTES, B_BYTES = L::B_BYTES, SMEM_A = L::SMEM_A, SMEM_B = L::SMEM_B,
                 SMEM_BAR = L::SMEM_BAR;
   constexpr uint32_t TMEM_COLS = L::TMEM_COLS;
+  constexpr int NSTAGE = L::NSTAGE;
+  static_assert(sizeof(Bars) <= 512, "barrier block");
   static_assert(EPI == TEPI_RELU ? COUT == 64 : COUT == 16, "epilogue shapes");
   extern __shared__ unsigned char smem_raw[];
   unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -368,7 +379,8 @@ static int launch(const __nv_bfloat16* x, const __nv_bfloat16* w, Args a, int P,
   a.rows = rows;
   a.tiles_per_row = (a.N0 + TM - 1) / TM;
   a.ntiles = rows * a.tiles_per_row;
-  const int grid = a.ntiles < num_sms ? a.ntiles : num_sms;
+  const int slots = num_sms * Cfg<CIN, COUT>::CTAS_PER_SM;
+  const int grid = a.ntiles < slots ? a.ntiles : slots;
   k_conv_tc<CIN, COUT, EPI><<<grid, NTHREADS, Cfg<CIN, COUT>::SMEM_BYTES, st>>>(mx, mw, a);
   return 1;
 }
