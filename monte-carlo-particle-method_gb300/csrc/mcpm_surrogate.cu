@@ -639,29 +639,40 @@ static void wgrad(SurrogateNet& n, const bf16* x, const bf16* dz, int P, float* 
   k_bias_reduce<<<1, 64, 0, st>>>(n.partb, Gb, COUT, grad_b);
 }
 
-// loss and gradients of all parameters for one batch (forward on the
-// mma.sync path, the one the backward pass differentiates)
+// loss and gradients of all parameters for one batch: the forward and the
+// data gradients on tcgen05 when the network's tensor path is on (the
+// per-tap mma.sync kernels otherwise), the weight gradients on mma.sync
 static void backward(SurrogateNet& n, const bf16* x, const float* t, int B, float ts, cudaStream_t st) {
   const int P = B * n.C;
-  forward(n, x, B, n.y, nullptr, 0.f, 0.f, st, false, n.status);
+  forward(n, x, B, n.y, nullptr, 0.f, 0.f, st, true, n.status);
+  // dz_out = conv^T(dz_in) gated by the forward activation: tcgen05, else mma.sync
+  auto dgrad = [&](int cin, const bf16* dz_in, const bf16* wf, const bf16* act, bf16* dz_out) {
+    if (n.tc) {
+      const int r = tc_conv_mask(cin, dz_in, wf, act, dz_out, n.N0, n.N1, P, n.num_sms, n.status, st);
+      if (r > 0) {
+        n.tc_launches += r;
+        return;
+      }
+      n.tc = false;
+      n.err = "tensor map rejected; the tcgen05 path is off for this network";
+    }
+    ConvArgs a = cargs(n, P);
+    a.x = dz_in; a.w = wf; a.mask = act; a.out = dz_out;
+    if (cin == 16) conv<16, 64, EPI_MASK>(n, a, st);
+    else conv<64, 64, EPI_MASK>(n, a, st);
+  };
   const int Gl = gblocks(P, NT, RED_G);
   k_loss<<<Gl, NT, 0, st>>>(n.y, t, ts, P, n.dz4, n.lpart);
   k_pair_reduce<<<1, 32, 0, st>>>(n.lpart, Gl, n.loss);
   // layer 4: dz4 -> dW4, db4; dz3 = (dz4 * W4^T) masked by a3
   wgrad<64, 16>(n, n.a3, n.dz4, P, n.grad + SP_OFF_W4, n.grad + SP_OFF_B4, st);
-  ConvArgs a = cargs(n, P);
-  a.x = n.dz4; a.w = n.f16 + SF_OFF_F4; a.mask = n.a3; a.out = n.dzA;
-  conv<16, 64, EPI_MASK>(n, a, st);
+  dgrad(16, n.dz4, n.f16 + SF_OFF_F4, n.a3, n.dzA);
   // layer 3
   wgrad<64, 64>(n, n.a2, n.dzA, P, n.grad + SP_OFF_W3, n.grad + SP_OFF_B3, st);
-  a = cargs(n, P);
-  a.x = n.dzA; a.w = n.f16 + SF_OFF_F3; a.mask = n.a2; a.out = n.dzB;
-  conv<64, 64, EPI_MASK>(n, a, st);
+  dgrad(64, n.dzA, n.f16 + SF_OFF_F3, n.a2, n.dzB);
   // layer 2
   wgrad<64, 64>(n, n.a1, n.dzB, P, n.grad + SP_OFF_W2, n.grad + SP_OFF_B2, st);
-  a = cargs(n, P);
-  a.x = n.dzB; a.w = n.f16 + SF_OFF_F2; a.mask = n.a1; a.out = n.dzA;
-  conv<64, 64, EPI_MASK>(n, a, st);
+  dgrad(64, n.dzB, n.f16 + SF_OFF_F2, n.a1, n.dzA);
   // layer 1
   wgrad<16, 64>(n, x, n.dzA, P, n.grad + SP_OFF_W1, n.grad + SP_OFF_B1, st);
 }

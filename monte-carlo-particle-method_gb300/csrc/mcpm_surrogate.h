@@ -75,6 +75,10 @@ int tc_conv16_relu(const __nv_bfloat16* x, const __nv_bfloat16* w, const float* 
                    int N1, int P, int num_sms, uint32_t* status, cudaStream_t st);
 int tc_conv_out(const __nv_bfloat16* x, const __nv_bfloat16* w, const float* bias, float* y, float* pcell, float g1,
                 float g2, float oscale, int N0, int N1, int P, int num_sms, uint32_t* status, cudaStream_t st);
+// the backward data gradient cin -> 64 (cin = 16 or 64; the transposed and
+// flipped weights), gated by the forward activation's sign (training)
+int tc_conv_mask(int cin, const __nv_bfloat16* x, const __nv_bfloat16* w, const __nv_bfloat16* mask,
+                 __nv_bfloat16* out, int N0, int N1, int P, int num_sms, uint32_t* status, cudaStream_t st);
 
 // session-side launchers (mcpm_surrogate.cu); each returns its launches
 int sur_forward_kick(Session& s, const double* nnd, const double* ncell);

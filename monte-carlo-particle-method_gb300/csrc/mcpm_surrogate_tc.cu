@@ -43,7 +43,9 @@ constexpr int TM = 128, NTHREADS = 192, MAXSTAGE = 16;
 constexpr uint64_t WAIT_NS = 1000000000ull;    // bound of every wait
 // epilogues: bias + ReLU to bf16 activations; the output layer's kick
 // coefficients into the packed cell record; its four outputs as fp32
-enum { TEPI_RELU = 0, TEPI_KICK = 1, TEPI_OUT = 2 };
+// (inference); and, for training, the data gradient of a layer input: the
+// accumulator gated by the sign of the layer's forward activation
+enum { TEPI_RELU = 0, TEPI_KICK = 1, TEPI_OUT = 2, TEPI_MASK = 3 };
 
 // the shape of one layer: rows of RB = 2 CIN bytes
 template <int CIN, int COUT> struct Cfg {
@@ -175,7 +177,8 @@ __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.
 
 struct Args {
   const float* bias;        // [COUT]
-  void* out;                // bf16 [P][COUT] (TEPI_RELU), fp32 [P][4] (TEPI_OUT)
+  void* out;                // bf16 [P][COUT] (TEPI_RELU, TEPI_MASK), fp32 [P][4] (TEPI_OUT)
+  const __nv_bfloat16* mask;  // [P][COUT] forward activations gating the gradient (TEPI_MASK)
   float* pcell;             // packed per-cell record (TEPI_KICK)
   uint32_t* status;
   int N0, N1, rows, tiles_per_row, ntiles;  // rows = B N1
@@ -191,7 +194,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   constexpr uint32_t TMEM_COLS = L::TMEM_COLS;
   constexpr int NSTAGE = L::NSTAGE;
   static_assert(sizeof(Bars) <= 512, "barrier block");
-  static_assert(EPI == TEPI_RELU ? COUT == 64 : COUT == 16, "epilogue shapes");
+  static_assert((EPI == TEPI_RELU || EPI == TEPI_MASK) ? COUT == 64 : COUT == 16, "epilogue shapes");
   extern __shared__ unsigned char smem_raw[];
   unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   Bars* bars = reinterpret_cast<Bars*>(smem + SMEM_BAR);
@@ -295,7 +298,27 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       const int x = x0 + 32 * q + lane;
       if (x < a.N0) {
         const size_t p = (size_t)row * a.N0 + x;
-        if constexpr (EPI == TEPI_RELU) {
+        if constexpr (EPI == TEPI_MASK) {
+          uint4* o = reinterpret_cast<uint4*>(static_cast<__nv_bfloat16*>(a.out) + p * COUT);
+          const uint4* mk = reinterpret_cast<const uint4*>(a.mask + p * COUT);
+#pragma unroll
+          for (int c = 0; c < NC; ++c) {
+#pragma unroll
+            for (int hq = 0; hq < 2; ++hq) {
+              const uint4 m4 = mk[2 * c + hq];
+              const __nv_bfloat162* m2 = reinterpret_cast<const __nv_bfloat162*>(&m4);
+              __nv_bfloat162 h[4];
+#pragma unroll
+              for (int e = 0; e < 4; ++e) {
+                const int k = 8 * hq + 2 * e;
+                const float v0 = __bfloat162float(m2[e].x) > 0.f ? __uint_as_float(r[c][k]) : 0.f;
+                const float v1 = __bfloat162float(m2[e].y) > 0.f ? __uint_as_float(r[c][k + 1]) : 0.f;
+                h[e] = __floats2bfloat162_rn(v0, v1);
+              }
+              o[2 * c + hq] = *reinterpret_cast<uint4*>(&h[0]);
+            }
+          }
+        } else if constexpr (EPI == TEPI_RELU) {
           uint4* o = reinterpret_cast<uint4*>(static_cast<__nv_bfloat16*>(a.out) + p * COUT);
 #pragma unroll
           for (int c = 0; c < NC; ++c) {
@@ -399,7 +422,7 @@ int tc_setup() {
     g_encode = (EncodeTiled)fn;
   }
   if (set_smem<64, 64, TEPI_RELU>() | set_smem<16, 64, TEPI_RELU>() | set_smem<64, 16, TEPI_KICK>() |
-      set_smem<64, 16, TEPI_OUT>()) {
+      set_smem<64, 16, TEPI_OUT>() | set_smem<64, 64, TEPI_MASK>() | set_smem<16, 64, TEPI_MASK>()) {
     cudaGetLastError();
     return 1;
   }
@@ -428,6 +451,16 @@ int tc_conv16_relu(const __nv_bfloat16* x, const __nv_bfloat16* w, const float* 
   tc::Args a = base_args(bias, N0, N1, status);
   a.out = out;
   return tc::launch<16, 64, tc::TEPI_RELU>(x, w, a, P, num_sms, st);
+}
+
+int tc_conv_mask(int cin, const __nv_bfloat16* x, const __nv_bfloat16* w, const __nv_bfloat16* mask,
+                 __nv_bfloat16* out, int N0, int N1, int P, int num_sms, uint32_t* status, cudaStream_t st) {
+  tc::Args a = base_args(nullptr, N0, N1, status);
+  a.out = out;
+  a.mask = mask;
+  if (cin == 16) return tc::launch<16, 64, tc::TEPI_MASK>(x, w, a, P, num_sms, st);
+  if (cin == 64) return tc::launch<64, 64, tc::TEPI_MASK>(x, w, a, P, num_sms, st);
+  return -1;
 }
 
 int tc_conv_out(const __nv_bfloat16* x, const __nv_bfloat16* w, const float* bias, float* y, float* pcell, float g1,

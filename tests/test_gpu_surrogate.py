@@ -90,7 +90,11 @@ def test_forward_tcgen05_matches_mma(cuda_ok, shape):
     assert _rel(out[1].reshape(yo.shape), yo) < 5e-3
 
 
-def test_gradients_match_oracle(cuda_ok):
+@pytest.mark.parametrize("tc", [True, False])
+def test_gradients_match_oracle(cuda_ok, tc):
+    """Loss and all parameter gradients against the oracle's FP64 backward
+    pass, on the tcgen05 path (forward and the three data-gradient
+    convolutions: 7 tcgen05 launches per batch) and on mma.sync."""
     torch = _torch()
     B, n1, n0 = 2, 9, 14
     p = _params(5)
@@ -99,9 +103,12 @@ def test_gradients_match_oracle(cuda_ok):
     ts = 0.5
     sur = mcpm.Surrogate(n0, n1, B)
     sur.set_params(p, 1.0)
+    sur.set_tensor_path(tc)
     xd = _dev_bf16(torch, x)
     td = torch.from_numpy(t.reshape(B, -1, 4)).cuda()
+    n0_tc = sur.tensor_path()[0]
     g, loss = sur.gradients(xd.data_ptr(), td.data_ptr(), B, ts)
+    assert sur.tensor_path() == ((n0_tc + 7, True) if tc else (n0_tc, False))
     lo, se, st, go = SO.loss_and_grad(p, x, t, ts)
     assert abs(loss[0] - se) <= 2e-3 * se and abs(loss[1] - st) <= 1e-6 * st
     dg, do = SO.unpack(g), SO.unpack(go)
