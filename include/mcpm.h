@@ -219,14 +219,17 @@ typedef struct mcpm_session mcpm_session;
 int mcpm_config_derive(mcpm_config* cfg, int64_t n_particles);
 
 /* readSettingsFile (src/myIO.cpp:1756-3016) for the problems the particle
-   step covers, closed_box (1), couette_flow (2) and wall (11): reads the reference's
+   step covers, closed_box (1), couette_flow (2), wall (11) and injection
+   (12, run between the closed box's specular walls): reads the reference's
    settings file ("keyword values..." per line, '#' comment lines) and
    derives the configuration as the reference does (cell sizes, Fn, sigma and
    crref from mu for hard or variable hard spheres, b, mu(T0), dt from the
    mean free path and frac_mft, phi from epsilon; SI constants where the
    reference fixes them; for wall the liquid slab between vapour layers:
    sigma of argon, densities in sigma^-3, Fn = 1e13, N and the box height
-   from the layers, the liquid's temperature).  *n_particles receives gas.N.  Keywords the
+   from the layers, the liquid's temperature; for injection a droplet of
+   extra particles in a gas at rest, box and densities in units of argon's
+   sigma).  *n_particles receives gas.N.  Keywords the
    reference does not know, other problems and models outside the step
    return MCPM_ERR_ARG; msg (optional, msg_len bytes) receives the reason.
    The result is an FP64 configuration; change precision before creating
@@ -237,7 +240,8 @@ int mcpm_config_from_settings(const char* path, mcpm_config* out, int64_t* n_par
    fills n_particles (= gas.N as derived) host particles, uniform along the
    streaming directions and mid-box along the others (wall: x2 uniform
    within the lower vapour layer, the liquid slab and the upper vapour layer
-   in id order, as the reference places them), velocities Maxwellian
+   in id order, as the reference places them; injection: the gas over the
+   box, then the droplet's particles over the central disc), velocities Maxwellian
    about U0 at T = max(gas.T, max(T_wall_1 + T_wall_2, T_wall_3 + T_wall_4)/2).
    The reference seeds from std::random_device; seed makes a run repeatable. */
 int mcpm_initialize_from_settings(const char* path, uint64_t seed, double* x1, double* x2, double* U1, double* U2,

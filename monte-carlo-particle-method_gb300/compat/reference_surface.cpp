@@ -104,6 +104,9 @@ mcpm_config config_of(const GAS* gas, const BOX* box) {
     c.length[i] = at<double>(box, OFF(BOX_Len) + i * sizeof(double));
   }
   c.problem = at<int>(box, OFF(BOX_problem));
+  // injection (12) runs between the closed box's specular walls (apply_BC,
+  // src/Main_Functions.cpp:1487-1489)
+  if (c.problem == 12) c.problem = MCPM_PROBLEM_CLOSED_BOX;
   c.model = model_id(at<std::string>(gas, OFF(GAS_model)));
   const int lr = at<int>(gas, OFF(GAS_long_range));
   c.long_range = (lr >= 1 && lr <= 3) ? lr : MCPM_LR_NONE;  // src/Main_Functions.cpp:1612-1617

@@ -6,7 +6,8 @@
 // reference speed from the viscosity, b, mu(T0), the mean free path, dt and
 // the attraction strength.  This restates that reading and the derivation
 // along the path the particle step covers (problems closed_box 1,
-// couette_flow 2 and wall 11; the step's models), in the reference's order of
+// couette_flow 2, wall 11 and injection 12; the step's models), in the
+// reference's order of
 // operations, so that a run configured by the reference's own files gets
 // the constants the reference would use.  Host code only.
 #include <cmath>
@@ -58,6 +59,8 @@ struct Raw {
   // problem wall (11): a liquid slab between vapour layers, in units of sigma
   double nc = -1.0, nv1 = 0.0, nv2 = -1.0, Tc = -1.0;
   int LcN = -1, LvN = -1, LvN1 = -1, n_ratio = -1;
+  // problem injection (12): a denser disc (the droplet) in a gas at rest
+  double nh = -1.0, drop_dia = -1.0;
 };
 
 // readSettingsFile's branch for problem wall (src/myIO.cpp:2628-2726): argon's
@@ -71,6 +74,19 @@ struct WallSetup {
 };
 
 int wall_setup(const Raw& r, WallSetup& w, char* msg, int32_t msg_len);
+
+// readSettingsFile's branch for problem injection (src/myIO.cpp:2727-2760):
+// argon's diameter, the densities in sigma^-3, N per cell times the cells,
+// the box's x and y lengths in sigma, Fn of the gas density over the box,
+// and the droplet's extra particles Nh = floor((nh - nc) pi d^2 / 4 / Fn)
+// for a disc of diameter d = drop_dia sigma; the gas temperature becomes Tc
+struct InjSetup {
+  double sigma, n, Fn, Len0, Len1, drop_dia, T;
+  int Nh;
+  long N;
+};
+
+int inj_setup(const Raw& r, InjSetup& j, char* msg, int32_t msg_len);
 
 int set_msg(char* msg, int32_t len, const char* text, int code) {
   if (msg && len > 0) {
@@ -138,6 +154,8 @@ int read_raw(const char* path, Raw& r, char* msg, int32_t msg_len) {
     else if (key == "LvN") iss >> r.LvN;
     else if (key == "LvN1") iss >> r.LvN1;
     else if (key == "n_ratio") iss >> r.n_ratio;
+    else if (key == "nh") iss >> r.nh;
+    else if (key == "drop_dia") iss >> r.drop_dia;
     else if (key.rfind("U_wall_", 0) == 0 || key.rfind("T_wall_", 0) == 0) {
       const int w = key[7] - '1';
       if (w >= 0 && w < 4) iss >> (key[0] == 'U' ? r.U_wall[w] : r.T_wall[w]);
@@ -152,8 +170,8 @@ int read_raw(const char* path, Raw& r, char* msg, int32_t msg_len) {
     return set_msg(msg, msg_len, "settings: num_cells must be N0 N1 1", MCPM_ERR_ARG);
   if (r.problem < 0) r.problem = 1;
   if (r.problem != 11 && r.N < 1) return set_msg(msg, msg_len, "settings: N (particles) is required", MCPM_ERR_ARG);
-  if (r.delta_dim[0] < 0.0 || r.problem == 11) {
-    // (problem wall sets the cells from the box height it derives)
+  if (r.delta_dim[0] < 0.0 || r.problem == 11 || r.problem == 12) {
+    // (problems wall and injection set the cells from the box they derive)
     for (int i = 0; i < 3; ++i) r.delta_dim[i] = r.Len[i] / r.cells[i];
   } else {
     // the session's cells are Len / N: a box_delta_dim that disagrees would
@@ -170,10 +188,30 @@ int read_raw(const char* path, Raw& r, char* msg, int32_t msg_len) {
   if (r.U0[0] < 0.0) r.U0[0] = r.U0[1] = r.U0[2] = 1.0;
   for (int i = 0; i < 4; ++i)
     if (r.T_wall[i] < 0) r.T_wall[i] = 1.0;
-  if (r.problem != 1 && r.problem != 2 && r.problem != 11)
+  if (r.problem != 1 && r.problem != 2 && r.problem != 11 && r.problem != 12)
     return set_msg(msg, msg_len,
-                   "settings: only problems closed_box (1), couette_flow (2) and wall (11) configure the particle step",
+                   "settings: only problems closed_box (1), couette_flow (2), wall (11) and injection (12) "
+                   "configure the particle step",
                    MCPM_ERR_ARG);
+  return MCPM_OK;
+}
+
+int inj_setup(const Raw& r, InjSetup& j, char* msg, int32_t msg_len) {
+  if (!(r.nc > 0.0) || !(r.nh >= r.nc) || !(r.Tc > 0.0) || !(r.drop_dia >= 0.0))
+    return set_msg(msg, msg_len, "settings: problem injection needs nc > 0, nh >= nc, Tc and drop_dia", MCPM_ERR_ARG);
+  const double pi = std::acos(-1.0);
+  j.sigma = 3.405e-10;
+  const double nc = r.nc / std::pow(j.sigma, 3.0);
+  const double nh = r.nh / std::pow(j.sigma, 3.0);
+  const long N = r.N * r.cells[0] * r.cells[1];
+  j.Len0 = r.Len[0] * j.sigma;
+  j.Len1 = r.Len[1] * j.sigma;
+  j.T = r.Tc;
+  j.n = nc;
+  j.Fn = j.n * j.Len0 * j.Len1 * r.Len[2] / (1.0 * N);
+  j.drop_dia = r.drop_dia * j.sigma;
+  j.Nh = (int)std::floor((nh - nc) * pi * j.drop_dia * j.drop_dia / 4.0 / j.Fn);
+  j.N = N + j.Nh;
   return MCPM_OK;
 }
 
@@ -252,7 +290,19 @@ extern "C" int mcpm_config_from_settings(const char* path, mcpm_config* out, int
   double eqdist;
   double Fn_run = Fn;
   long N_run = r.N;
-  if (r.problem == 11) {
+  if (r.problem == 12) {
+    // the injection branch, after crref as well (:2727-2760)
+    InjSetup js;
+    if (int rc = inj_setup(r, js, msg, msg_len)) return rc;
+    r.sigma = js.sigma;
+    eqdist = js.sigma;
+    r.n = js.n;
+    Fn_run = js.Fn;
+    N_run = js.N;
+    r.Len[0] = js.Len0;
+    r.Len[1] = js.Len1;
+    r.T = js.T;
+  } else if (r.problem == 11) {
     // the wall branch replaces the diameter, density, Fn, N, the box height
     // and the temperature after crref is set (:2628-2726)
     WallSetup ws;
@@ -295,7 +345,11 @@ extern "C" int mcpm_config_from_settings(const char* path, mcpm_config* out, int
     c.direction[i] = r.direction[i];
     c.length[i] = r.Len[i];
   }
-  c.problem = r.problem == 1 ? MCPM_PROBLEM_CLOSED_BOX : r.problem == 2 ? MCPM_PROBLEM_COUETTE : MCPM_PROBLEM_WALL;
+  // injection's walls are the closed box's specular ones (apply_BC,
+  // src/Main_Functions.cpp:1487-1489)
+  c.problem = (r.problem == 1 || r.problem == 12) ? MCPM_PROBLEM_CLOSED_BOX
+              : r.problem == 2                    ? MCPM_PROBLEM_COUETTE
+                                                  : MCPM_PROBLEM_WALL;
   c.model = model;
   // "0 or anything > 3 = no attraction" (src/Main_Functions.cpp:1612-1617)
   c.long_range = (r.long_range >= 1 && r.long_range <= 3) ? r.long_range : MCPM_LR_NONE;
@@ -323,9 +377,11 @@ extern "C" int mcpm_config_from_settings(const char* path, mcpm_config* out, int
 // streaming directions and at mid-box along the others (:4657-4672).  Wall
 // (:4493-4530): x1 as before, x2 uniform in the lower vapour layer for the
 // first Nv1 particles, in the liquid slab for the next Nc2, in the upper
-// vapour layer for the rest.  Velocities normal about U0 with
-// sqrt(kb T / m), T = max(gas.T, max(T_wall_1 + T_wall_2, T_wall_3 + T_wall_4) / 2)
-// (:4790-4799; gas.T is the liquid's for the wall problem).  The reference
+// vapour layer for the rest.  Injection (:4627-4643): the gas uniform over
+// the box, then the droplet's Nh particles uniform over the central disc.
+// Velocities normal about U0 with sqrt(kb T / m),
+// T = max(gas.T, max(T_wall_1 + T_wall_2, T_wall_3 + T_wall_4) / 2)
+// (:4790-4799; gas.T is Tc for the wall and injection problems).  The reference
 // seeds its generator from std::random_device; here a 64-bit Mersenne
 // twister seeded by the caller gives the uniforms and Box-Muller pairs the
 // normals, so a seed repeats a run on any host.
@@ -336,18 +392,39 @@ extern "C" int mcpm_initialize_from_settings(const char* path, uint64_t seed, do
     return set_msg(msg, msg_len, "initialize: null argument", MCPM_ERR_ARG);
   Raw r;
   if (int rc = read_raw(path, r, msg, msg_len)) return rc;
-  const bool wall = r.problem == 11;
+  const bool wall = r.problem == 11, inj = r.problem == 12;
   WallSetup ws{};
+  InjSetup js{};
   if (wall) {
     if (int rc = wall_setup(r, ws, msg, msg_len)) return rc;
     r.N = ws.N;
     r.Len[1] = ws.Len1;
     r.T = ws.T;
+  } else if (inj) {
+    if (int rc = inj_setup(r, js, msg, msg_len)) return rc;
+    r.N = js.N;
+    r.Len[0] = js.Len0;
+    r.Len[1] = js.Len1;
+    r.T = js.T;
   }
   if (n_particles != r.N) return set_msg(msg, msg_len, "initialize: n_particles differs from the file's N", MCPM_ERR_ARG);
   std::mt19937_64 gen(seed);
   auto uni = [&]() { return ((double)(gen() >> 11) + 0.5) * (1.0 / 9007199254740992.0); };
+  const double two_pi = 2.0 * std::acos(-1.0);
   for (int64_t i = 0; i < r.N; ++i) {
+    if (inj) {
+      // the gas uniform over the box, then the droplet's Nh particles
+      // uniform over the disc at the centre (src/Main_Functions.cpp:4627-4643)
+      if (i < r.N - js.Nh) {
+        x1[i] = uni() * r.Len[0];
+        x2[i] = uni() * r.Len[1];
+      } else {
+        const double rr = (js.drop_dia / 2.0) * std::sqrt(uni()), th = uni() * two_pi;
+        x1[i] = 0.5 * r.Len[0] + rr * std::cos(th);
+        x2[i] = 0.5 * r.Len[1] + rr * std::sin(th);
+      }
+      continue;
+    }
     x1[i] = r.direction[0] == 1 ? uni() * r.Len[0] : 0.5 * r.Len[0];
     if (!wall) {
       x2[i] = r.direction[1] == 1 ? uni() * r.Len[1] : 0.5 * r.Len[1];
@@ -363,7 +440,6 @@ extern "C" int mcpm_initialize_from_settings(const char* path, uint64_t seed, do
   double T = std::fmax(r.T_wall[0] + r.T_wall[1], r.T_wall[2] + r.T_wall[3]) / 2.0;
   T = std::fmax(r.T, T);
   const double sd = std::sqrt(r.kb * T / r.m);
-  const double two_pi = 2.0 * std::acos(-1.0);
   double* U[3] = {U1, U2, U3};
   for (int64_t i = 0; i < r.N; ++i)
     for (int d = 0; d < 3; ++d) {

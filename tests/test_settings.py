@@ -1,5 +1,5 @@
 """The settings-file front end (mcpm_config_from_settings, a restatement of
-readSettingsFile, src/myIO.cpp:1756-3016, for problems 1, 2 and 11) on the
+readSettingsFile, src/myIO.cpp:1756-3016, for problems 1, 2, 11 and 12) on the
 fixtures in tests/golden/settings: bit-exact against the reference's own
 reader where the reference tree is present, and against the values it
 produced (tests/golden/settings_expected.json, written by
@@ -19,6 +19,16 @@ SETTINGS = os.path.join(HERE, "golden", "settings")
 FIXTURES = sorted(f for f in os.listdir(SETTINGS) if f.endswith(".in"))
 
 
+def _ref_ints(iv):
+    """the reference's ints with its problem id as the session's: injection
+    (12) runs between the closed box's specular walls (apply_BC,
+    src/Main_Functions.cpp:1487-1489)"""
+    out = [int(v) for v in iv]
+    if out[6] == 12:
+        out[6] = mcpm.PROBLEM_CLOSED_BOX
+    return out
+
+
 def _values(cfg, N):
     ints = [cfg.n_cells[0], cfg.n_cells[1], cfg.n_cells[2], cfg.direction[0], cfg.direction[1],
             cfg.direction[2], cfg.problem, cfg.long_range, cfg.model, N]
@@ -34,7 +44,7 @@ def test_settings_match_golden(built, name):
         exp = json.load(fh)[name]
     cfg, N = mcpm.config_from_settings(os.path.join(SETTINGS, name))
     ints, dbl = _values(cfg, N)
-    assert ints == exp["ints"]
+    assert ints == _ref_ints(exp["ints"])
     want = [float.fromhex(h) for h in exp["doubles"]]
     assert dbl == want, [(i, a, b) for i, (a, b) in enumerate(zip(dbl, want)) if a != b]
     assert cfg.precision == mcpm.FP64 and cfg.max_particles == N
@@ -48,7 +58,7 @@ def test_settings_match_reference(built, name):
     iv, dv = O.ref_read_settings(path)
     cfg, N = mcpm.config_from_settings(path)
     ints, dbl = _values(cfg, N)
-    assert ints == [int(v) for v in iv]
+    assert ints == _ref_ints(iv)
     assert np.array_equal(np.array(dbl), dv)
 
 
@@ -179,13 +189,65 @@ def test_initialize_wall(built):
         assert abs(a[k].var() / ref[k].var() - 1) < 0.05, k
 
 
+def _injection_layout(path, parts, cfg, N):
+    """(gas particles inside the box, droplet particles inside the disc)"""
+    s = 3.405e-10
+    raw = {}
+    with open(path) as fh:
+        for line in fh:
+            f = line.split()
+            if f and f[0] in ("nc", "nh", "drop_dia"):
+                raw[f[0]] = float(f[1])
+    d = raw["drop_dia"] * s
+    nh = int(np.floor((raw["nh"] - raw["nc"]) / s ** 3 * np.pi * d * d / 4.0 / cfg.Fn))
+    x, y = parts["x1"], parts["x2"]
+    gas = (x[:N - nh] > 0) & (x[:N - nh] < cfg.length[0]) & (y[:N - nh] > 0) & (y[:N - nh] < cfg.length[1])
+    r2 = (x[N - nh:] - 0.5 * cfg.length[0]) ** 2 + (y[N - nh:] - 0.5 * cfg.length[1]) ** 2
+    return nh, gas.all(), bool(np.all(r2 <= (0.5 * d) ** 2 * (1 + 1e-12)))
+
+
+def test_initialize_injection(built):
+    """initialization for problem injection (src/Main_Functions.cpp:4627-4643):
+    the gas uniform over the box, the droplet's Nh particles uniform over the
+    disc at the centre; velocities at Tc.  Against the reference's own
+    initialization where present: the same droplet particles, the same
+    velocity statistics."""
+    path = os.path.join(SETTINGS, "injection_esmc.in")
+    cfg, N = mcpm.config_from_settings(path)
+    a = mcpm.initialize_from_settings(path, 5, N)
+    nh, gas_ok, disc_ok = _injection_layout(path, a, cfg, N)
+    assert nh > 1000 and gas_ok and disc_ok
+    # the disc is uniform: half its particles within radius d / (2 sqrt 2)
+    s = 3.405e-10
+    r = np.hypot(a["x1"][N - nh:] - 0.5 * cfg.length[0], a["x2"][N - nh:] - 0.5 * cfg.length[1])
+    assert abs(np.mean(r < 12.0 * s / 2 / np.sqrt(2)) - 0.5) < 5 * np.sqrt(0.25 / nh)
+    sd = np.sqrt(cfg.kb * 100.0 / cfg.m)
+    for k in ("U1", "U2", "U3"):
+        assert abs(a[k].std() / sd - 1) < 0.02
+    ref = O.ref_initialize(path, N)
+    if ref is None:
+        return
+    nh_r, gas_r, disc_r = _injection_layout(path, ref, cfg, N)
+    assert nh_r == nh and gas_r and disc_r
+    for k in ("U1", "U2", "U3"):
+        se = np.sqrt((a[k].var() + ref[k].var()) / N)
+        assert abs(a[k].mean() - ref[k].mean()) < 5 * se, k
+        assert abs(a[k].var() / ref[k].var() - 1) < 0.02, k
+
+
 def test_reference_settings_file(built):
     """The reference's own settings file (its injection run, problem 12):
-    every keyword is read, and the problem is refused as outside the step."""
+    read and derived as the reference does, every derived value to the last
+    bit, and its initial particles laid out as the reference's."""
     src = O.ref_src_dir()
     path = os.path.join(src, "injection.in") if src else None
     if not path or not os.path.exists(path):
         pytest.skip("reference sources not available")
-    with pytest.raises(mcpm.MCPMError) as e:
-        mcpm.config_from_settings(path)
-    assert "problems" in str(e.value)
+    cfg, N = mcpm.config_from_settings(path)
+    iv, dv = O.ref_read_settings(path)
+    ints, dbl = _values(cfg, N)
+    assert ints == _ref_ints(iv) and np.array_equal(np.array(dbl), dv)
+    assert cfg.problem == mcpm.PROBLEM_CLOSED_BOX and cfg.model == mcpm.MODEL_ESMC
+    a = mcpm.initialize_from_settings(path, 9, N)
+    nh, gas_ok, disc_ok = _injection_layout(path, a, cfg, N)
+    assert gas_ok and disc_ok and nh > 0
