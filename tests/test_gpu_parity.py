@@ -151,6 +151,26 @@ def test_binning_edges_and_out_of_box(cuda_ok):
     assert e.value.code & mcpm.ERR_OUT_OF_BOX
 
 
+@pytest.mark.parametrize("prec", [mcpm.FP64, mcpm.FP32])
+def test_nan_velocity_raises(cuda_ok, prec):
+    """A NaN velocity spreads through its cell's moments into the FP update,
+    which raises MCPM_ERR_NAN (the reference prints the cell and exits,
+    src/Fokker_Planck.cpp:1137-1148); the other cells step on."""
+    cfg, parts = W.homogeneous_relaxation_1d(n_cells=8, ppc=16, precision=prec)
+    bad = {k: v.copy() for k, v in parts.items()}
+    bad["U2"][3] = np.nan
+    s = mcpm.Session(cfg)
+    s.upload(bad["x1"], bad["x2"], bad["U1"], bad["U2"], bad["U3"])
+    s.check_status()
+    with pytest.raises(mcpm.MCPMError) as e:
+        s.step(1)
+        s.check_status()
+    assert e.value.code & mcpm.ERR_NAN
+    g = s.download()
+    # only the NaN particle's cell (16 of 128 particles) is lost
+    assert np.count_nonzero(np.isfinite(g["U1"])) >= len(g["U1"]) - 16
+
+
 # -------------------------------------------------------- cell update
 @pytest.mark.parametrize("step", [0, 1])
 def test_cell_update_fp64(cuda_ok, step):
