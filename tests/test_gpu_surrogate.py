@@ -218,3 +218,34 @@ def test_trained_network_gains_over_the_plain_path(cuda_ok):
     s.profile(False)
     assert prof["surrogate"][0] < prof["long_range"][0], prof
     sur.close()
+
+
+@pytest.mark.skipif(not os.path.exists(S.WEIGHTS), reason="no trained weights")
+def test_network_branch_reads_this_steps_densities(cuda_ok):
+    """Between judge steps the network's branch (nodal deposit and network on
+    a second stream) runs beside the moment pass and the per-cell solve,
+    which writes the cell densities; the branch takes them from the layout's
+    counts by the solve's own operations.  A profiled run executes every
+    kernel in order on one stream and feeds the network the solve's
+    densities: the two runs' kicks agree wherever the runs' particles bin
+    alike (the in-cell order of the slotted passes reorders FP32 sums).  The
+    branch's result no longer depends on whether the solve has written the
+    densities when the network reads them."""
+    cfg, parts = W.vlasov_box_2d(n_cells=(64, 64), total=244 * 64 * 64, precision=mcpm.FP32,
+                                 long_range=mcpm.LR_SCREENED_POISSON, model=mcpm.MODEL_FP_DENSE)
+    runs = []
+    for profiled in (False, True):
+        s = mcpm.Session(cfg)
+        s.upload(parts["x1"], parts["x2"], parts["U1"], parts["U2"], parts["U3"])
+        S.attach(s, judge_every=1000, threshold=1e9)  # in charge after the first (judge) step
+        if profiled:
+            s.profile(True)
+        s.step(6)
+        runs.append((s.get_kick_2d(), s.download()))
+    (ka, ga), (kb, gb) = runs
+    for k in ("x1", "x2", "U1", "U2", "U3"):
+        err = np.max(np.abs(ga[k] - gb[k])) / max(1.0, np.max(np.abs(gb[k])))
+        assert err <= 1e-4, (k, err)
+    differ = np.any(ka != kb, axis=1)
+    assert differ.mean() <= 0.02, differ.mean()
+    assert np.linalg.norm(ka - kb) <= 1e-3 * np.linalg.norm(kb)
