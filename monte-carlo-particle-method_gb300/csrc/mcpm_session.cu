@@ -141,7 +141,7 @@ static inline bool is_fp_model(int m) {
 }
 
 extern "C" {
-static int long_range_force(mcpm_session* s, bool branch = false);
+static int long_range_force(mcpm_session* s);
 
 int mcpm_config_derive(mcpm_config* c, int64_t n_particles) {
   if (!c) return MCPM_ERR_ARG;
@@ -662,13 +662,11 @@ int mcpm_end_step(mcpm_session* s) {
 
 // the long-range force of a step: the attached network while it is in
 // charge, else the plain path -- and on a judge step the plain path (whose
-// kick is kept) followed by the network and the comparison of the two.
-// branch: the network runs beside the per-cell solve, so its cell densities
-// come from the layout's counts
-static int long_range_force(mcpm_session* s, bool branch) {
+// kick is kept) followed by the network and the comparison of the two
+static int long_range_force(mcpm_session* s) {
   const double* ncell = s->cell + (size_t)MCPM_CF_N * s->C;
   if (s->sur && s->sur_active && !s->sur_judge_now)
-    return T_SUR(sur_forward_kick(*s, lr2d_node_density(*s), branch ? nullptr : ncell));
+    return T_SUR(sur_forward_kick(*s, lr2d_node_density(*s), ncell));
   int n = T_LR(launch_long_range(*s));
   if (s->sur && s->sur_judge_now) n += T_SUR(sur_judge(*s, lr2d_node_density(*s), ncell));
   return n;
@@ -705,7 +703,7 @@ static int step_once(mcpm_session* s, uint32_t stages) {
     cudaStream_t main_stream = s->stream;
     s->stream = s->side;
     n += launch_node_density(*s);
-    n += long_range_force(s, true);
+    n += long_range_force(s);
     s->stream = main_stream;
     cudaEventRecord(s->ev_join, s->side);
   }

@@ -439,20 +439,14 @@ __global__ void k_flip(const bf16* W, int cout, int cin, bf16* F) {
 // each value v = 10 (b n - 0.25) as a bf16 pair hi = bf16(v), lo = bf16(v -
 // hi) (channels 0..4 and 6..10), so the input keeps ~16 significant bits --
 // the kick follows from density differences between neighbouring nodes,
-// a few percent of the density, below a single bf16's resolution.  The cell
-// density comes from the cell array (n) or, where the per-cell solve that
-// writes it may still be running on another stream, from the layout's
-// counts (cnt) by the solve's own operations
-__global__ void k_input(const double* nnd, const double* n, const int32_t* cnt, DevConsts kc, bf16* x) {
-  const double b = kc.b;
-  const int C = kc.C;
+// a few percent of the density, below a single bf16's resolution
+__global__ void k_input(const double* nnd, const double* n, double b, int C, bf16* x) {
   for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < C; c += gridDim.x * blockDim.x) {
     __align__(16) bf16 q[16];
     const double* nn = nnd + (size_t)c * 4;
 #pragma unroll
     for (int k = 0; k < 4; ++k) sur_hi_lo(10.0 * (b * nn[k] - 0.25), q[k], q[6 + k]);
-    const double nc = cnt ? (kc.cell_w ? kc.cell_w[c] : 1) * kc.Fn * (double)cnt[c] / cell_volume(c, kc) : n[c];
-    sur_hi_lo(10.0 * (b * nc - 0.25), q[4], q[10]);
+    sur_hi_lo(10.0 * (b * n[c] - 0.25), q[4], q[10]);
     q[5] = __float2bfloat16_rn(1.0f);
 #pragma unroll
     for (int k = 11; k < 16; ++k) q[k] = __float2bfloat16_rn(0.0f);
@@ -695,8 +689,7 @@ static void refresh_weights(SurrogateNet& n, cudaStream_t st, bool from_p32) {
 // deposit when it ran with the network attached, else packed here
 static int sur_input(Session& s, const double* nnd, const double* ncell) {
   if (s.sur_xin_ready) return 0;
-  k_input<<<gblocks(s.C, 256, s.num_sms * 8), 256, 0, s.stream>>>(nnd, ncell, ncell ? nullptr : s.cnt, s.k,
-                                                                   s.sur->xin);
+  k_input<<<gblocks(s.C, 256, s.num_sms * 8), 256, 0, s.stream>>>(nnd, ncell, s.k.b, s.C, s.sur->xin);
   return 1;
 }
 
@@ -725,7 +718,7 @@ int sur_snapshot(Session& s, const double* fld_dev, int K, uint64_t seed, uint32
   k_cell_density<<<gblocks(s.C, 256, cap), 256, 0, s.stream>>>(qc, s.k, ncell);
   int launches = 2 + launch_node_density_from(s, qc);
   launches += launch_long_range_2d(s);
-  k_input<<<gblocks(s.C, 256, cap), 256, 0, s.stream>>>(nnd, ncell, nullptr, s.k, reinterpret_cast<bf16*>(x));
+  k_input<<<gblocks(s.C, 256, cap), 256, 0, s.stream>>>(nnd, ncell, s.k.b, s.C, reinterpret_cast<bf16*>(x));
   k_target<<<gblocks(s.C, 256, cap), 256, 0, s.stream>>>(lr2d_potential(s), s.k.N0, s.C, y);
   return launches + 2;
 }

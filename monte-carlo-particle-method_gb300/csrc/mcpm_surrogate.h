@@ -80,9 +80,7 @@ int tc_conv_out(const __nv_bfloat16* x, const __nv_bfloat16* w, const float* bia
 int tc_conv_mask(int cin, const __nv_bfloat16* x, const __nv_bfloat16* w, const __nv_bfloat16* mask,
                  __nv_bfloat16* out, int N0, int N1, int P, int num_sms, uint32_t* status, cudaStream_t st);
 
-// session-side launchers (mcpm_surrogate.cu); each returns its launches.
-// ncell: the cell densities of the cell array, or null to take them from
-// the layout's counts (the per-cell solve has not written them yet)
+// session-side launchers (mcpm_surrogate.cu); each returns its launches
 int sur_forward_kick(Session& s, const double* nnd, const double* ncell);
 int sur_judge(Session& s, const double* nnd, const double* ncell);
 int sur_snapshot(Session& s, const double* fld_dev, int K, uint64_t seed, uint32_t snap, int32_t* qc, double* nnd,

@@ -224,13 +224,14 @@ def test_trained_network_gains_over_the_plain_path(cuda_ok):
 def test_network_branch_reads_this_steps_densities(cuda_ok):
     """Between judge steps the network's branch (nodal deposit and network on
     a second stream) runs beside the moment pass and the per-cell solve,
-    which writes the cell densities; the branch takes them from the layout's
-    counts by the solve's own operations.  A profiled run executes every
+    which writes the cell densities; the deposit kernel writes the network's
+    input, the cell density from the layout's counts by the solve's own
+    operations.  A profiled run executes every
     kernel in order on one stream and feeds the network the solve's
     densities: the two runs' kicks agree wherever the runs' particles bin
-    alike (the in-cell order of the slotted passes reorders FP32 sums).  The
-    branch's result no longer depends on whether the solve has written the
-    densities when the network reads them."""
+    alike (the in-cell order of the slotted passes reorders FP32 sums), so
+    the branch's result does not depend on whether the solve has written the
+    densities when the network reads its input."""
     cfg, parts = W.vlasov_box_2d(n_cells=(64, 64), total=244 * 64 * 64, precision=mcpm.FP32,
                                  long_range=mcpm.LR_SCREENED_POISSON, model=mcpm.MODEL_FP_DENSE)
     runs = []
