@@ -282,8 +282,15 @@ int launch_init_omega(Session& s);
 // cell_update, the node potential + kick coefficients, device views
 int lr2d_setup(Session& s);
 void lr2d_free(Session& s);
-int launch_node_density(Session& s);
-int launch_long_range_2d(Session& s);
+// count_density: also the cell densities from the layout's counts
+// (lr2d_count_density), for a force that runs beside the per-cell solve
+int launch_node_density(Session& s, bool count_density = false);
+// n: the cell densities the force reads (null: the cell array's, which the
+// per-cell solve writes)
+int launch_long_range_2d(Session& s, const double* n = nullptr);
+// the cell densities the last nodal deposit with count_density formed from
+// the layout's counts (the per-cell solve's values)
+const double* lr2d_count_density(const Session& s);
 int launch_node_density_from(Session& s, const int32_t* qc);
 int32_t* lr2d_quadrants(Session& s);
 double* lr2d_node_density_mut(Session& s);

@@ -67,6 +67,7 @@ struct LR2D {
   double* exc_w = nullptr;  // [n_exc]
   double* V = nullptr;      // [nn] node potential
   double* nnd = nullptr;    // [C][4] nodal densities n_n
+  double* ncell = nullptr;  // [C] cell densities from the layout's counts (the per-cell solve's values)
   int32_t* qc = nullptr;    // [C][4] particles per cell quadrant
   float *Sx = nullptr, *Sy = nullptr, *mu = nullptr, *Bf = nullptr, *Tf = nullptr;  // FP32 transforms
   double *B = nullptr, *U = nullptr;  // FP64 right-hand side and solution (interior, rows y)
@@ -165,7 +166,8 @@ __global__ void k_quadrants_f32(DevConsts k, const int32_t* off, const int32_t* 
 // wall (src/Main_Functions.cpp:2268-2364).  exact: the sum of equal terms in
 // sequence, as the reference accumulates it.
 __global__ void k_node_density(DevConsts k, const int32_t* qc, double* nnd, int exact,
-                               __nv_bfloat16* xin = nullptr, const int32_t* ccnt = nullptr) {
+                               __nv_bfloat16* xin = nullptr, const int32_t* ccnt = nullptr,
+                               double* ncell = nullptr) {
   const int N0 = k.N0, N1 = k.N1;
   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < 4 * k.C; e += gridDim.x * blockDim.x) {
     const int c = e >> 2, slot = e & 3;
@@ -189,6 +191,14 @@ __global__ void k_node_density(DevConsts k, const int32_t* qc, double* nnd, int 
     if (j == 0 && (slot & 1) == 0) acc = acc * 2.0;
     if (j == N0 - 1 && (slot & 1) == 1) acc = acc * 2.0;
     nnd[e] = acc;
+    // the cell density n = Fn N / V as the moment finalisation forms it,
+    // from the cell's count (so that the deposit and what reads it need no
+    // moment pass)
+    double ncv = 0.0;
+    if ((xin || ncell) && slot == 0) {
+      ncv = (k.cell_w ? k.cell_w[c] : 1) * k.Fn * (double)ccnt[c] / cell_volume(c, k);
+      if (ncell) ncell[c] = ncv;
+    }
     if (xin) {
       // the learned force's input for this cell: the nodal density of the
       // slot as a bf16 pair in channels slot and 6 + slot; slot 0 adds the
@@ -196,9 +206,6 @@ __global__ void k_node_density(DevConsts k, const int32_t* qc, double* nnd, int 
       __nv_bfloat16* xc = xin + (size_t)c * 16;
       sur_hi_lo(10.0 * (k.b * acc - 0.25), xc[slot], xc[6 + slot]);
       if (slot == 0) {
-        // the cell density n = Fn N / V as the moment finalisation forms
-        // it, from the cell's count (so the deposit needs no moment pass)
-        const double ncv = (k.cell_w ? k.cell_w[c] : 1) * k.Fn * (double)ccnt[c] / cell_volume(c, k);
         sur_hi_lo(10.0 * (k.b * ncv - 0.25), xc[4], xc[10]);
         xc[5] = __float2bfloat16_rn(1.0f);
         for (int q = 11; q < 16; ++q) xc[q] = __float2bfloat16_rn(0.0f);
@@ -567,6 +574,7 @@ int lr2d_setup(Session& s) {
             A((void**)&t->exc_i, st.exc_i.size() * 4) && H(t->exc_i, st.exc_i.data(), st.exc_i.size() * 4) &&
             A((void**)&t->exc_w, st.exc_w.size() * 8) && H(t->exc_w, st.exc_w.data(), st.exc_w.size() * 8) &&
             A((void**)&t->V, (size_t)t->nn * 8) && A((void**)&t->nnd, (size_t)k.C * 4 * 8) &&
+            A((void**)&t->ncell, (size_t)k.C * 8) &&
             A((void**)&t->qc, (size_t)k.C * 4 * 4);
   if (ok && s.prec == MCPM_FP32) {
     // the FP32 quadrant pass compares positions with thresholds: x < the
@@ -632,7 +640,7 @@ int lr2d_setup(Session& s) {
 void lr2d_free(Session& s) {
   LR2D* t = s.lr2d;
   if (!t) return;
-  cudaFree(t->W); cudaFree(t->exc_off); cudaFree(t->exc_i); cudaFree(t->exc_w); cudaFree(t->V); cudaFree(t->nnd);
+  cudaFree(t->W); cudaFree(t->exc_off); cudaFree(t->exc_i); cudaFree(t->exc_w); cudaFree(t->V); cudaFree(t->nnd); cudaFree(t->ncell);
   cudaFree(t->qc); cudaFree(t->Sx); cudaFree(t->Sy); cudaFree(t->mu); cudaFree(t->B); cudaFree(t->U); cudaFree(t->Bf); cudaFree(t->Tf);
   cudaFree(t->wall); cudaFree(t->qtx); cudaFree(t->qty);
   delete t;
@@ -657,7 +665,7 @@ int launch_node_density_from(Session& s, const int32_t* qc) {
   return 1;
 }
 
-int launch_node_density(Session& s) {
+int launch_node_density(Session& s, bool count_density) {
   LR2D* t = s.lr2d;
   // the screened-Poisson force and the learned force read them
   if (!t || (t->mode != MCPM_LR_SCREENED_POISSON && !s.sur)) return 0;
@@ -673,15 +681,17 @@ int launch_node_density(Session& s) {
     const PBuf& P = s.P[s.cur];
     k_quadrants<double><<<g, 256, 0, s.stream>>>(s.k, s.off, s.cnt, (const double*)P.x1, (const double*)P.x2, t->qc);
   }
-  k_node_density<<<blocks_for(4L * s.C, 256, s.num_sms * 16), 256, 0, s.stream>>>(s.k, t->qc, t->nnd,
-                                                                                    s.prec == MCPM_FP64, xin, s.cnt);
+  k_node_density<<<blocks_for(4L * s.C, 256, s.num_sms * 16), 256, 0, s.stream>>>(
+      s.k, t->qc, t->nnd, s.prec == MCPM_FP64, xin, s.cnt, count_density ? t->ncell : nullptr);
   return 2;
 }
 
-int launch_long_range_2d(Session& s) {
+const double* lr2d_count_density(const Session& s) { return s.lr2d ? s.lr2d->ncell : nullptr; }
+
+int launch_long_range_2d(Session& s, const double* n) {
   LR2D* t = s.lr2d;
   if (!t) return 0;
-  const double* n = s.cell + (size_t)MCPM_CF_N * s.C;
+  if (!n) n = s.cell + (size_t)MCPM_CF_N * s.C;
   int launches = 0;
   const int cap = s.num_sms * 16;
   if (t->mode == MCPM_LR_DIRECT) {

@@ -141,7 +141,7 @@ static inline bool is_fp_model(int m) {
 }
 
 extern "C" {
-static int long_range_force(mcpm_session* s);
+static int long_range_force(mcpm_session* s, bool branch = false);
 
 int mcpm_config_derive(mcpm_config* c, int64_t n_particles) {
   if (!c) return MCPM_ERR_ARG;
@@ -662,12 +662,14 @@ int mcpm_end_step(mcpm_session* s) {
 
 // the long-range force of a step: the attached network while it is in
 // charge, else the plain path -- and on a judge step the plain path (whose
-// kick is kept) followed by the network and the comparison of the two
-static int long_range_force(mcpm_session* s) {
+// kick is kept) followed by the network and the comparison of the two.
+// branch: it runs beside the per-cell solve, the plain path on the cell
+// densities the nodal deposit formed from the layout's counts
+static int long_range_force(mcpm_session* s, bool branch) {
   const double* ncell = s->cell + (size_t)MCPM_CF_N * s->C;
   if (s->sur && s->sur_active && !s->sur_judge_now)
     return T_SUR(sur_forward_kick(*s, lr2d_node_density(*s), ncell));
-  int n = T_LR(launch_long_range(*s));
+  int n = T_LR(branch ? launch_long_range_2d(*s, lr2d_count_density(*s)) : launch_long_range(*s));
   if (s->sur && s->sur_judge_now) n += T_SUR(sur_judge(*s, lr2d_node_density(*s), ncell));
   return n;
 }
@@ -691,19 +693,22 @@ static int step_once(mcpm_session* s, uint32_t stages) {
   } else {
     cudaMemsetAsync(s->work, 0, WK_COUNT * 4, s->stream);
   }
-  // the network in charge (not judged this step): its branch -- the nodal
-  // deposit from the new layout's counts and quadrants, then the inference
-  // that writes the kick -- needs no moments, so it runs on the side stream
-  // while the moment pass and the solves run here
-  const bool branch = s->sur && s->sur_active && !s->sur_judge_now && !s->prof && s->side &&
-                      s->cfg.long_range != MCPM_LR_NONE;
+  // the 2-D long-range force's branch -- the nodal deposit from the new
+  // layout's counts and quadrants, then the network's inference or the
+  // plain screened-Poisson path (on the judge steps both and the judge),
+  // each writing the kick -- needs no moments: its cell densities are the
+  // deposit's, formed from the counts as the per-cell solve forms them.  So
+  // it runs on the side stream while the moment pass and the solves run here
+  const bool net = s->sur && s->sur_active && !s->sur_judge_now;
+  const bool branch = !s->prof && s->side && s->lr2d && s->cfg.long_range != MCPM_LR_NONE &&
+                      (net || s->cfg.long_range == MCPM_LR_SCREENED_POISSON);
   if (branch) {
     cudaEventRecord(s->ev_fork, s->stream);
     cudaStreamWaitEvent(s->side, s->ev_fork, 0);
     cudaStream_t main_stream = s->stream;
     s->stream = s->side;
-    n += launch_node_density(*s);
-    n += long_range_force(s);
+    n += launch_node_density(*s, true);
+    n += long_range_force(s, true);
     s->stream = main_stream;
     cudaEventRecord(s->ev_join, s->side);
   }
