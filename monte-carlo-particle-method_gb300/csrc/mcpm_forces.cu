@@ -1,6 +1,7 @@
 // mcpm_forces.cu -- ESMC collisions and the 1-D Vlasov long-range force.
 #include <algorithm>
 #include <cstring>
+#include <type_traits>
 #include <vector>
 
 #include "mcpm_device.cuh"
@@ -19,14 +20,66 @@ template <typename real> struct PT2 {
 // slot sampling without replacement gives every cell exactly its m_I).
 // Cells whose partner neighbourhoods overlap are never processed together
 // (colour classes of stride 2R+1, R = ceil(sigma/dx)); inside a cell a warp
-// draws 32 candidates at once and applies the longest prefix whose particle
-// pairs are disjoint, so the result equals processing the candidates one
-// after another in order.
-template <typename real>
-__global__ void __launch_bounds__(128) k_esmc(DevConsts k, double* cell, const int32_t* off, const int32_t* cnt,
-                                              PT2<real> p, const int32_t* dstep, int cx, int cy, int Sx, int Sy,
-                                              uint32_t* status) {
+// holds 32 consecutive candidates and applies the longest prefix whose
+// particle pairs are disjoint, so the result equals processing the
+// candidates one after another in order.  The candidates past the prefix
+// move down the warp to the next round (their draws, directions, partners
+// and cell lookups depend on positions only, which collisions do not
+// change); only the lanes that empty draw new ones.
+
+// slots of the collision cell a warp's conflict table covers; larger cells
+// test their candidates pairwise over the warp
+constexpr int ESMC_TAB = 256;
+// FP32 blocks of 4 warps resident per SM: 12 (40 registers) holds a whole
+// colour class of a 256 x 256 box at once -- one wave of cells instead of
+// a full wave and a partial one; measured 0.85 -> 0.45 ms of collisions per
+// step at 6.5M particles (8 blocks 0.49, 16 blocks 0.55 ms)
+#ifndef MCPM_ESMC_MINB
+#define MCPM_ESMC_MINB 12
+#endif
+
+// Whether a lower lane's valid candidate shares a particle with this lane's
+// (si: a slot of the collision cell [o, o + n); sj: the partner, in the cell
+// or a neighbour).  Slots of the collision cell go through the warp's table
+// (each valid lane marks its slots with its lane by atomicMin; a slot whose
+// mark is below the lane was claimed by a lower lane); partners outside the
+// cell can only meet other such partners: __match_any_sync.  tab holds
+// ESMC_TAB entries of 32 on entry and on return.
+__device__ __forceinline__ bool esmc_conflict(int* tab, int o, int n, bool valid, int si, int sj) {
   const int lane = threadIdx.x & 31;
+  const unsigned lower = (1u << lane) - 1u;
+  bool conflict = false;
+  if (n <= ESMC_TAB) {
+    const bool jin = valid && sj >= o && sj < o + n;
+    if (valid) atomicMin(&tab[si - o], lane);
+    if (jin) atomicMin(&tab[sj - o], lane);
+    __syncwarp();
+    if (valid) conflict = tab[si - o] < lane || (jin && tab[sj - o] < lane);
+    const unsigned mj = __match_any_sync(FULL, (valid && !jin) ? sj : -1 - lane);
+    if (valid && !jin && (mj & lower)) conflict = true;
+    __syncwarp();
+    if (valid) tab[si - o] = 32;
+    if (jin) tab[sj - o] = 32;
+    __syncwarp();
+  } else {
+    for (int l = 0; l < 31; ++l) {
+      const int oi = __shfl_sync(FULL, si, l), oj = __shfl_sync(FULL, sj, l);
+      const int ov = __shfl_sync(FULL, (int)valid, l);
+      if (l < lane && ov && valid && (oi == si || oi == sj || oj == si || oj == sj)) conflict = true;
+    }
+  }
+  return conflict;
+}
+
+template <typename real>
+__global__ void __launch_bounds__(128, sizeof(real) == 4 ? MCPM_ESMC_MINB : 1)
+    k_esmc(DevConsts k, double* cell, const int32_t* off, const int32_t* cnt, PT2<real> p, const int32_t* dstep,
+           int cx, int cy, int Sx, int Sy, uint32_t* status) {
+  __shared__ int tabs[4][ESMC_TAB];
+  const int lane = threadIdx.x & 31;
+  int* tab = tabs[threadIdx.x >> 5];
+  for (int e = lane; e < ESMC_TAB; e += 32) tab[e] = 32;
+  __syncwarp();
   const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int nA = (k.N0 - cx + Sx - 1) / Sx, nB = (k.N1 - cy + Sy - 1) / Sy;
   if (gw >= nA * nB) return;
@@ -34,6 +87,7 @@ __global__ void __launch_bounds__(128) k_esmc(DevConsts k, double* cell, const i
   const int C = k.C;
   const int step = *dstep;
   const int NI = cnt[I];
+  const int oI = off[I];
   const double om_max = cell[(size_t)MCPM_CF_OMEGA_MAX * C + I];
   const double mreal = r_floor(0.5 * om_max * (1.0 * NI) + u01d(rng_draw(k, (uint32_t)I, (uint32_t)step, RNG_ESMC_M, 0u).x));
   // a non-finite or absurd majorant would make the candidate loop unbounded
@@ -45,6 +99,7 @@ __global__ void __launch_bounds__(128) k_esmc(DevConsts k, double* cell, const i
   // top 23 bits, the acceptance test as dummy > u om_max); FP64 sessions
   // keep the reference's double arithmetic
   constexpr bool F32 = sizeof(real) == 4;
+  typedef typename std::conditional<F32, float, double>::type cr;  // Y and n_J as the test uses them
   double omega = 0.0;
   float omega_f = 0.f;
   const float om_max_f = (float)om_max;
@@ -53,51 +108,53 @@ __global__ void __launch_bounds__(128) k_esmc(DevConsts k, double* cell, const i
   const real sg = (real)k.sigma;
   if (NI > 0) {
     int base = 0;
+    // this lane's candidate (number base + lane): its slots, direction and
+    // the Y and n_J of its test; `have` once it holds them
+    bool have = false, valid = false;
+    int si = -1, sj = -1;
+    real d0 = 0, d1 = 0, d2 = 0;
+    cr Ymid = 0, nJ = 0;
     while (base < mI) {
       const int kc = base + lane;
-      bool valid = false;
-      int64_t si = -1, sj = -1;
-      real d0 = 0, d1 = 0, d2 = 0;
-      double Ymid = 0.0, nJ = 0.0;
-      float Ymid_f = 0.f, nJ_f = 0.f;
-      if (kc < mI) {
-        uint4 r = rng_draw(k, (uint32_t)I, (uint32_t)step, RNG_ESMC, (uint32_t)kc);
-        si = (int64_t)off[I] + pick(r.x, NI);
-        const real uy = F32 ? (real)u01f(r.y) : (real)u01d(r.y), uz = F32 ? (real)u01f(r.z) : (real)u01d(r.z);
-        real theta = (real)2.0 * pi * uy;
-        real cph = (real)2.0 * uz - (real)1.0;
-        real sph = r_sqrt((real)1.0 - cph * cph);
-        real sn, cs;
-        r_sincos(theta, &sn, &cs);
-        d0 = cs * sph; d1 = sn * sph; d2 = cph;
-        real xi1 = p.x1[si], xi2 = p.x2[si];
-        real xx = xi1 + sg * d0, yy = xi2 + sg * d1;
-        int i0 = (int)r_floor(xx / (real)k.dx), i1 = (int)r_floor(yy / (real)k.dy);
-        if (i0 >= 0 && i0 < k.N0 && i1 >= 0 && i1 < k.N1) {
-          int J = i1 * k.N0 + i0;
-          int NJ = cnt[J];
-          if (NJ > 0) {
-            sj = (int64_t)off[J] + pick(r.w, NJ);
-            if (sj != si) {
-              real xm0 = (xi1 + p.x1[sj]) / (real)2.0, xm1 = (xi2 + p.x2[sj]) / (real)2.0;
-              int m0 = (int)r_floor(xm0 / (real)k.dx), m1 = (int)r_floor(xm1 / (real)k.dy);
-              m0 = m0 < 0 ? 0 : (m0 > k.N0 - 1 ? k.N0 - 1 : m0);
-              m1 = m1 < 0 ? 0 : (m1 > k.N1 - 1 ? k.N1 - 1 : m1);
-              Ymid = cell[(size_t)CFI_Y * C + m1 * k.N0 + m0];
-              nJ = cell[(size_t)MCPM_CF_N * C + J];
-              if constexpr (F32) { Ymid_f = (float)Ymid; nJ_f = (float)nJ; }
-              valid = true;
+      if (!have) {
+        valid = false;
+        si = -1;
+        sj = -1;
+        d0 = d1 = d2 = 0;
+        Ymid = nJ = 0;
+        if (kc < mI) {
+          uint4 r = rng_draw(k, (uint32_t)I, (uint32_t)step, RNG_ESMC, (uint32_t)kc);
+          si = oI + pick(r.x, NI);
+          const real uy = F32 ? (real)u01f(r.y) : (real)u01d(r.y), uz = F32 ? (real)u01f(r.z) : (real)u01d(r.z);
+          real theta = (real)2.0 * pi * uy;
+          real cph = (real)2.0 * uz - (real)1.0;
+          real sph = r_sqrt((real)1.0 - cph * cph);
+          real sn, cs;
+          r_sincos(theta, &sn, &cs);
+          d0 = cs * sph; d1 = sn * sph; d2 = cph;
+          real xi1 = p.x1[si], xi2 = p.x2[si];
+          real xx = xi1 + sg * d0, yy = xi2 + sg * d1;
+          int i0 = (int)r_floor(xx / (real)k.dx), i1 = (int)r_floor(yy / (real)k.dy);
+          if (i0 >= 0 && i0 < k.N0 && i1 >= 0 && i1 < k.N1) {
+            int J = i1 * k.N0 + i0;
+            int NJ = cnt[J];
+            if (NJ > 0) {
+              sj = off[J] + pick(r.w, NJ);
+              if (sj != si) {
+                real xm0 = (xi1 + p.x1[sj]) / (real)2.0, xm1 = (xi2 + p.x2[sj]) / (real)2.0;
+                int m0 = (int)r_floor(xm0 / (real)k.dx), m1 = (int)r_floor(xm1 / (real)k.dy);
+                m0 = m0 < 0 ? 0 : (m0 > k.N0 - 1 ? k.N0 - 1 : m0);
+                m1 = m1 < 0 ? 0 : (m1 > k.N1 - 1 ? k.N1 - 1 : m1);
+                Ymid = (cr)cell[(size_t)CFI_Y * C + m1 * k.N0 + m0];
+                nJ = (cr)cell[(size_t)MCPM_CF_N * C + J];
+                valid = true;
+              }
             }
           }
         }
       }
       // longest prefix of candidates with pairwise disjoint particles
-      bool conflict = false;
-      for (int l = 0; l < 31; ++l) {
-        int64_t oi = __shfl_sync(FULL, si, l), oj = __shfl_sync(FULL, sj, l);
-        int ov = __shfl_sync(FULL, (int)valid, l);
-        if (l < lane && ov && valid && (oi == si || oi == sj || oj == si || oj == sj)) conflict = true;
-      }
+      const bool conflict = esmc_conflict(tab, oI, NI, valid, si, sj);
       unsigned cm = __ballot_sync(FULL, conflict);
       int take = cm ? (__ffs(cm) - 1) : 32;
       if (take > mI - base) take = mI - base;
@@ -106,7 +163,7 @@ __global__ void __launch_bounds__(128) k_esmc(DevConsts k, double* cell, const i
         real gd = g0 * d0 + g1 * d1 + g2 * d2;
         bool accept;
         if constexpr (F32) {
-          const float dummy = coef_f * (float)gd * Ymid_f * nJ_f;
+          const float dummy = coef_f * (float)gd * Ymid * nJ;
           omega_f = fmaxf(omega_f, dummy);
           const float u = u01f(rng_draw(k, (uint32_t)I, (uint32_t)step, RNG_ESMC_ACC, (uint32_t)kc).x);
           accept = dummy > u * om_max_f;
@@ -122,6 +179,17 @@ __global__ void __launch_bounds__(128) k_esmc(DevConsts k, double* cell, const i
         }
       }
       __syncwarp();
+      // the candidates past the prefix move down by `take` lanes
+      const int src = (lane + take) & 31;
+      have = lane + take < 32;
+      valid = __shfl_sync(FULL, valid, src);
+      si = __shfl_sync(FULL, si, src);
+      sj = __shfl_sync(FULL, sj, src);
+      d0 = __shfl_sync(FULL, d0, src);
+      d1 = __shfl_sync(FULL, d1, src);
+      d2 = __shfl_sync(FULL, d2, src);
+      Ymid = __shfl_sync(FULL, Ymid, src);
+      nJ = __shfl_sync(FULL, nJ, src);
       base += take;
     }
   }
