@@ -1605,6 +1605,11 @@ __global__ void __launch_bounds__(256, sizeof(real) == 4 ? (CST ? (SL ? MCPM_UPD
 // the fused FP_dense step with specular or periodic walls and no long-range
 // force: every stage fixed at compile time
 constexpr uint32_t ST_FUSED_FP = ST_RNG | ST_FP | ST_DFP | ST_BC1 | ST_STREAM | ST_BC2 | ST_BC3 | ST_KEY;
+// the fused step of the collision models (ESMC, DSMC): walls, flight and
+// re-binning, with the old positions the diffuse walls and Couette flow
+// keep (ST_FUSED_COLL_OLD) or without them
+constexpr uint32_t ST_FUSED_COLL = ST_BC1 | ST_STREAM | ST_BC2 | ST_BC3 | ST_KEY;
+constexpr uint32_t ST_FUSED_COLL_OLD = ST_FUSED_COLL | ST_OLD;
 
 // ========================================================= host<->device
 // one staged field into the state's precision (uploads: each field's
@@ -1795,6 +1800,10 @@ template <typename real> static int update_impl(Session& s, uint32_t stages, int
         if (spec) k_update<real, FL, SPEC, true><<<g, b, sm, s.stream>>>(a);
         else if (per) k_update<real, FL, PER, true><<<g, b, sm, s.stream>>>(a);
         else k_update<real, FL, 0, true><<<g, b, sm, s.stream>>>(a);
+      } else if (stages == ST_FUSED_COLL_OLD) {
+        k_update<real, ST_FUSED_COLL_OLD, 0, true><<<g, b, sm, s.stream>>>(a);
+      } else if (stages == ST_FUSED_COLL) {
+        k_update<real, ST_FUSED_COLL, 0, true><<<g, b, sm, s.stream>>>(a);
       } else {
         k_update<real, 0u, 0, true><<<g, b, sm, s.stream>>>(a);
       }
@@ -1872,7 +1881,8 @@ cudaError_t update_set_smem_max() {
       (const void*)k_update<float, F, 0, true>,  (const void*)k_update<float, F, SPEC, true>,
       (const void*)k_update<float, F, PER, true>, (const void*)k_update<float, FL, 0, true>,
       (const void*)k_update<float, FL, SPEC, true>, (const void*)k_update<float, FL, PER, true>,
-      (const void*)k_update<float, 0u, 0, true>};
+      (const void*)k_update<float, 0u, 0, true>,  (const void*)k_update<float, ST_FUSED_COLL_OLD, 0, true>,
+      (const void*)k_update<float, ST_FUSED_COLL, 0, true>};
   cudaError_t e = cudaSuccess;
   for (const void* f : fns)
     if (e == cudaSuccess) e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
