@@ -73,8 +73,8 @@ __device__ __forceinline__ bool esmc_conflict(int* tab, int o, int n, bool valid
 
 template <typename real>
 __global__ void __launch_bounds__(128, sizeof(real) == 4 ? MCPM_ESMC_MINB : 1)
-    k_esmc(DevConsts k, double* cell, const int32_t* off, const int32_t* cnt, PT2<real> p, const int32_t* dstep,
-           int cx, int cy, int Sx, int Sy, uint32_t* status) {
+    k_esmc(DevConsts k, double* cell, const float* yn, const int32_t* off, const int32_t* cnt, PT2<real> p,
+           const int32_t* dstep, int cx, int cy, int Sx, int Sy, uint32_t* status) {
   __shared__ int tabs[4][ESMC_TAB];
   const int lane = threadIdx.x & 31;
   int* tab = tabs[threadIdx.x >> 5];
@@ -137,6 +137,11 @@ __global__ void __launch_bounds__(128, sizeof(real) == 4 ? MCPM_ESMC_MINB : 1)
           int i0 = (int)r_floor(xx / (real)k.dx), i1 = (int)r_floor(yy / (real)k.dy);
           if (i0 >= 0 && i0 < k.N0 && i1 >= 0 && i1 < k.N1) {
             int J = i1 * k.N0 + i0;
+            // n_J is loaded beside the partner cell's count and offset
+            // (FP32 sessions: the solve's float copy, no conversion here)
+            cr nJc;
+            if constexpr (F32) nJc = yn[C + J];
+            else nJc = cell[(size_t)MCPM_CF_N * C + J];
             int NJ = cnt[J];
             if (NJ > 0) {
               sj = off[J] + pick(r.w, NJ);
@@ -145,8 +150,9 @@ __global__ void __launch_bounds__(128, sizeof(real) == 4 ? MCPM_ESMC_MINB : 1)
                 int m0 = (int)r_floor(xm0 / (real)k.dx), m1 = (int)r_floor(xm1 / (real)k.dy);
                 m0 = m0 < 0 ? 0 : (m0 > k.N0 - 1 ? k.N0 - 1 : m0);
                 m1 = m1 < 0 ? 0 : (m1 > k.N1 - 1 ? k.N1 - 1 : m1);
-                Ymid = (cr)cell[(size_t)CFI_Y * C + m1 * k.N0 + m0];
-                nJ = (cr)cell[(size_t)MCPM_CF_N * C + J];
+                if constexpr (F32) Ymid = yn[m1 * k.N0 + m0];
+                else Ymid = cell[(size_t)CFI_Y * C + m1 * k.N0 + m0];
+                nJ = nJc;
                 valid = true;
               }
             }
@@ -218,7 +224,9 @@ template <typename real> static int esmc_impl(Session& s) {
       int warps = nA * nB;
       if (warps <= 0) continue;
       int blocks = (warps * 32 + 127) / 128;
-      k_esmc<real><<<blocks, 128, 0, s.stream>>>(s.k, s.cell, s.off, s.cnt, p, s.dstep, cx, cy, Sx, Sy, s.status);
+      k_esmc<real><<<blocks, 128, 0, s.stream>>>(s.k, s.cell,
+                                                 s.prec == MCPM_FP32 ? s.pcell + (size_t)PF_STRIDE * s.C : nullptr,
+                                                 s.off, s.cnt, p, s.dstep, cx, cy, Sx, Sy, s.status);
       ++n;
     }
   return n;

@@ -170,7 +170,8 @@ struct Session {
   int32_t* work = nullptr;      // [WK_COUNT]
   int32_t* scan_blk = nullptr;  // [4][C/1024 + 1] block totals / bases of the scan
   double* cell = nullptr;       // [CF_DEV_COUNT][C]
-  float* pcell = nullptr;       // [C][PF_STRIDE] packed FP32 record
+  float* pcell = nullptr;       // [C][PF_STRIDE] packed FP32 record, then [2][C]: the cells'
+                                // Y(n) and n as floats (the FP32 ESMC acceptance test)
   double* xi = nullptr;         // [3][cap] whitened normals, slot order
   double* inj = nullptr;        // [3][cap] injected raw normals, particle-id order
   uint4* rng_inj[RNG_COUNT] = {};  // injected words per stream (k.rng_inj points here)

@@ -301,7 +301,7 @@ int mcpm_session_create(const mcpm_config* cfg, mcpm_session** out) {
        A((void**)&s->off, (C + 1) * 4) && A((void**)&s->cursor, C * 4) && A((void**)&s->list_small, C * 4) &&
        A((void**)&s->list_big, C * 4) && A((void**)&s->wl, WL_COUNT * 4) && A((void**)&s->work, WK_COUNT * 4) &&
        A((void**)&s->scan_blk, 8 * (C / 1024 + 2) * 4) &&
-       A((void**)&s->cell, (size_t)CF_DEV_COUNT * C * 8) && A((void**)&s->pcell, (size_t)PF_STRIDE * C * 4) && A((void**)&s->xi, 3 * cap * 8) &&
+       A((void**)&s->cell, (size_t)CF_DEV_COUNT * C * 8) && A((void**)&s->pcell, (size_t)(PF_STRIDE + 2) * C * 4) && A((void**)&s->xi, 3 * cap * 8) &&
        A((void**)&s->inj, 3 * cap * 8) && A((void**)&s->stage, 5 * cap * 8) && A((void**)&s->stage_in, 5 * cap * 8) &&
        A((void**)&s->faces, ((size_t)k.N1 + 1 + 5000) * 8) && A((void**)&s->status, 16) &&
        A((void**)&s->dstep, 16) && A((void**)&s->bin_faces, ((size_t)k.N0 + k.N1 + 4) * 4);
@@ -330,7 +330,7 @@ int mcpm_session_create(const mcpm_config* cfg, mcpm_session** out) {
     cudaMemsetAsync(s->ovf_n, 0, 16, s->stream);
   }
   cudaMemsetAsync(s->cell, 0, (size_t)CF_DEV_COUNT * C * 8, s->stream);
-  cudaMemsetAsync(s->pcell, 0, (size_t)PF_STRIDE * C * 4, s->stream);
+  cudaMemsetAsync(s->pcell, 0, (size_t)(PF_STRIDE + 2) * C * 4, s->stream);
   cudaMemsetAsync(s->status, 0, 16, s->stream);
   cudaMemsetAsync(s->work, 0, WK_COUNT * 4, s->stream);
   cudaMemsetAsync(s->inj, 0, 3 * cap * 8, s->stream);

@@ -577,6 +577,11 @@ __global__ void __launch_bounds__(MCPM_SOLVE_T, MCPM_SOLVE_MINB)
     pf[PF_PH0] = (float)ph0; pf[PF_PH1] = (float)ph1;
     pf[PF_N] = (float)ncnt;
     pf[PF_E2] = (float)R(CFI_RAW + 28);
+    // Y(n) and n as floats after the records (the FP32 ESMC test reads
+    // them for every candidate)
+    float* yn = pcell + (size_t)PF_STRIDE * C;
+    yn[c] = (float)Ycell;
+    yn[C + c] = (float)n;
   }
   raise_status(status, bad);
 }
