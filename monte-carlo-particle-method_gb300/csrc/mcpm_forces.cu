@@ -493,6 +493,7 @@ struct LRTab {
   const double* pa;      // PCR coefficients [levels][nf]
   const double* pg;
   const double* dfin;    // final diagonal
+  double corr;           // the analytic r < sigma part's factor (formed on the host, as the reference forms it)
 };
 
 // One block: the whole 1-D long-range force.  direct (long_range 1,
@@ -525,15 +526,29 @@ __global__ void __launch_bounds__(1024) k_long_range_1d(DevConsts k, double* cel
       }
     __syncthreads();
   } else {
-    // wall values: warp 0 -> face 0, warp 1 -> face N1, lane-strided sums
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    if (warp < 2) {
-      const int* idx = warp == 0 ? t.idx0 : t.idxN;
-      double acc = 0.0;
-      for (int q = lane; q < 2500; q += 32) acc += t.wq[q] * n[idx[q]];
+    // wall values at face 0 and face N1: every thread sums its share of
+    // both walls' 2,500 points (independent gathers), the warps' partial
+    // sums are added in a fixed order
+    __shared__ double wpart[2][32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    double a0 = 0.0, aN = 0.0;
+    for (int q = threadIdx.x; q < 2500; q += blockDim.x) {
+      const double w = t.wq[q];
+      a0 += w * n[t.idx0[q]];
+      aN += w * n[t.idxN[q]];
+    }
 #pragma unroll
-      for (int m = 16; m >= 1; m >>= 1) acc += __shfl_xor_sync(FULL, acc, m);
-      if (lane == 0) V[warp == 0 ? 0 : nf - 1] = acc;
+    for (int m = 16; m >= 1; m >>= 1) {
+      a0 += __shfl_xor_sync(FULL, a0, m);
+      aN += __shfl_xor_sync(FULL, aN, m);
+    }
+    if (lane == 0) { wpart[0][warp] = a0; wpart[1][warp] = aN; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double s0 = 0.0, sN = 0.0;
+      for (int w = 0; w < nw; ++w) { s0 += wpart[0][w]; sN += wpart[1][w]; }
+      V[0] = s0;
+      V[nf - 1] = sN;
     }
     __syncthreads();
     const double dy2 = k.dy * k.dy;
@@ -544,20 +559,27 @@ __global__ void __launch_bounds__(1024) k_long_range_1d(DevConsts k, double* cel
     __syncthreads();
     double* src = r2;
     double* dst = V;
+    // the first face of this thread: its coefficients are loaded one level
+    // ahead, so that their latency overlaps the level before
+    const int i0 = threadIdx.x;
+    double an = 0.0, gn = 0.0;
+    if (i0 < nf && t.levels > 0) { an = t.pa[i0]; gn = t.pg[i0]; }
     for (int lv = 0, s = 1; lv < t.levels; ++lv, s <<= 1) {
       const double* pa = t.pa + (size_t)lv * nf;
       const double* pg = t.pg + (size_t)lv * nf;
-      for (int i = threadIdx.x; i < nf; i += blockDim.x) {
+      const double a_i0 = an, g_i0 = gn;
+      if (i0 < nf && lv + 1 < t.levels) { an = pa[nf + i0]; gn = pg[nf + i0]; }
+      for (int i = i0; i < nf; i += blockDim.x) {
+        const double ai = i == i0 ? a_i0 : pa[i], gi = i == i0 ? g_i0 : pg[i];
         double v = src[i];
-        if (i - s >= 0) v += pa[i] * src[i - s];
-        if (i + s < nf) v += pg[i] * src[i + s];
+        if (i - s >= 0) v += ai * src[i - s];
+        if (i + s < nf) v += gi * src[i + s];
         dst[i] = v;
       }
       __syncthreads();
       double* tmp = src; src = dst; dst = tmp;
     }
-    double corr = 1.0 - (k.sigma * k.bst + 1.0) * exp(-k.bst * k.sigma);
-    corr = corr / k.bst / k.bst;
+    const double corr = t.corr;
     for (int i = threadIdx.x; i < nf; i += blockDim.x) {
       double nj = i == 0 ? n[0] : (i == N1 ? n[N1 - 1] : (n[i] + n[i - 1]) / 2.0);
       dst[i] = src[i] / t.dfin[i] - nj * corr;
@@ -749,6 +771,11 @@ int long_range_setup(Session& s) {
       l.swap(nl); d.swap(nd); u.swap(nu);
     }
     t.levels = levels;
+    {
+      const double sg = s.cfg.sigma, b = s.cfg.bst;
+      double corr = 1.0 - (sg * b + 1.0) * exp(-b * sg);
+      t.corr = corr / b / b;
+    }
     oPa = put(pa.data(), pa.size() * 8);
     oPg = put(pg.data(), pg.size() * 8);
     oDf = put(d.data(), nf * 8);

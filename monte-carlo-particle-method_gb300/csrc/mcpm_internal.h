@@ -270,6 +270,8 @@ int launch_moments(Session& s);
 int launch_solve(Session& s, int with_alpha);
 // the FP32 sessions' variant (mcpm_solve_fast.cu, FP64 multiply-adds fused)
 int launch_solve_fast(Session& s, int with_alpha, int fp_model);
+// threads per block of the solves (fewer for grids with few cells)
+int solve_block(const Session& s);
 // slotted: write the new state into the slotted layout of the other buffer
 // (FP32 passes that bin the new positions)
 int launch_update(Session& s, uint32_t stages, int bc_call_base, bool slotted = false);

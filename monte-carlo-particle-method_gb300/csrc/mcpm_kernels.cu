@@ -1737,6 +1737,15 @@ template <typename real> static int moments_impl(Session& s) {
 }
 int launch_moments(Session& s) { return s.prec == MCPM_FP32 ? moments_impl<float>(s) : moments_impl<double>(s); }
 
+// threads per block of the per-cell solves: MCPM_SOLVE_T, halved (down to
+// 8) while the grid would have fewer blocks than SMs -- a small grid's cells
+// then spread over the SMs' FP64 pipes instead of queueing on a few
+int solve_block(const Session& s) {
+  int t = MCPM_SOLVE_T;
+  while (t > 8 && (s.C + t - 1) / t < s.num_sms) t >>= 1;
+  return t;
+}
+
 int launch_solve(Session& s, int with_alpha) {
   // c_gamma_calculation and the Langevin constants (src/Main_Functions.cpp:2729)
   const int m = s.cfg.model;
@@ -1744,8 +1753,8 @@ int launch_solve(Session& s, int with_alpha) {
   // the FP64 path reproduces the reference's solve exactly; the FP32 path
   // runs the leaner FP64 variant
   if (s.prec == MCPM_FP32) return launch_solve_fast(s, with_alpha, fp);
-  const int nb = (s.C + MCPM_SOLVE_T - 1) / MCPM_SOLVE_T;
-  k_solve<true><<<nb, MCPM_SOLVE_T, 0, s.stream>>>(s.k, s.cell, nullptr, with_alpha, fp, s.status);
+  const int bt = solve_block(s), nb = (s.C + bt - 1) / bt;
+  k_solve<true><<<nb, bt, 0, s.stream>>>(s.k, s.cell, nullptr, with_alpha, fp, s.status);
   return 1;
 }
 

@@ -15,8 +15,8 @@
 namespace mcpm {
 
 int launch_solve_fast(Session& s, int with_alpha, int fp_model) {
-  const int nb = (s.C + MCPM_SOLVE_T - 1) / MCPM_SOLVE_T;
-  k_solve<false><<<nb, MCPM_SOLVE_T, 0, s.stream>>>(s.k, s.cell, s.pcell, with_alpha, fp_model, s.status);
+  const int bt = solve_block(s), nb = (s.C + bt - 1) / bt;
+  k_solve<false><<<nb, bt, 0, s.stream>>>(s.k, s.cell, s.pcell, with_alpha, fp_model, s.status);
   return 1;
 }
 
