@@ -168,6 +168,9 @@ __global__ void k_quadrants_f32(DevConsts k, const int32_t* off, const int32_t* 
 __global__ void k_node_density(DevConsts k, const int32_t* qc, double* nnd, int exact,
                                __nv_bfloat16* xin = nullptr, const int32_t* ccnt = nullptr,
                                double* ncell = nullptr) {
+  // the network's first layer (launched as a programmatic dependent) may
+  // begin its set-up; it reads the input after this grid completes
+  if (threadIdx.x == 0) asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
   const int N0 = k.N0, N1 = k.N1;
   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < 4 * k.C; e += gridDim.x * blockDim.x) {
     const int c = e >> 2, slot = e & 3;

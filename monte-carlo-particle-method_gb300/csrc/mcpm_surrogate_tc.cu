@@ -219,6 +219,11 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   __syncthreads();
   fence_after();
   const uint32_t tmem = bars->tmem_base;
+  // programmatic dependent launch: the next layer's blocks may start their
+  // set-up (barriers, TMEM, weights) while this layer finishes; each block
+  // reads the previous kernel's output only after griddepcontrol.wait (a
+  // kernel launched without the attribute passes it at once)
+  if (threadIdx.x == 0) asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 
   if (warp == 0) {
     if (lane == 0) {
@@ -226,6 +231,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&tmx) : "memory");
       bar_expect_tx(&bars->wbar, 9 * B_BYTES);
       for (int t = 0; t < 9; ++t) tma_load_2d(smem + SMEM_B + t * B_BYTES, &tmw, t * CIN, 0, &bars->wbar);
+      asm volatile("griddepcontrol.wait;" ::: "memory");  // the activations are the previous kernel's output
       int last_par[NSTAGE];
       for (int s = 0; s < NSTAGE; ++s) last_par[s] = -1;
       uint32_t i = 0;
@@ -280,6 +286,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     // epilogue: warp w drains TMEM lanes 32 (w % 4) .. + 31 = tile rows
     const int q = warp & 3;
     uint32_t j = 0;
+    asm volatile("griddepcontrol.wait;" ::: "memory");  // the outputs may be what the previous kernel reads
     for (int tile = blockIdx.x; tile < a.ntiles; tile += gridDim.x, ++j) {
       const uint32_t buf = j & 1, aph = (j >> 1) & 1;
       if (!bar_wait(&bars->acc_full[buf], aph, abort, a.status)) break;
@@ -404,7 +411,20 @@ static int launch(const __nv_bfloat16* x, const __nv_bfloat16* w, Args a, int P,
   a.ntiles = rows * a.tiles_per_row;
   const int slots = num_sms * Cfg<CIN, COUT>::CTAS_PER_SM;
   const int grid = a.ntiles < slots ? a.ntiles : slots;
-  k_conv_tc<CIN, COUT, EPI><<<grid, NTHREADS, Cfg<CIN, COUT>::SMEM_BYTES, st>>>(mx, mw, a);
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(NTHREADS);
+  cfg.dynamicSmemBytes = Cfg<CIN, COUT>::SMEM_BYTES;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  if (cudaLaunchKernelEx(&cfg, k_conv_tc<CIN, COUT, EPI>, mx, mw, a) != cudaSuccess) {
+    cudaGetLastError();
+    return -1;
+  }
   return 1;
 }
 }  // namespace tc
