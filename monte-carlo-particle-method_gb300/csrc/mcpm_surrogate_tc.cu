@@ -52,20 +52,18 @@ template <int CIN, int COUT> struct Cfg {
   static_assert(CIN == 16 || CIN == 64, "input rows of 32 or 128 bytes");
   static_assert(COUT % 16 == 0 && COUT >= 16 && COUT <= 256, "UMMA N for M = 128");
   static constexpr int RB = 2 * CIN;
-  // activation stages in flight (the 4 KB taps of the input layer need a
-  // deeper queue to cover the TMA latency than the 16 KB ones), and the
-  // persistent blocks per SM: the narrow layers' MMAs are short, so several
-  // blocks per SM overlap their load latencies (shared memory and TMEM allow
-  // it: 3 x 68 KB and 3 x 128 columns, 2 x 84 KB and 2 x 32 columns)
-  // ROW3 (64-channel inputs): a stage holds one grid row of the tile with
-  // its left and right halo cells (TM + 2 rows of RB bytes), and the MMAs
-  // read its three column shifts at one-row offsets, so a tile takes three
-  // boxes instead of nine; 16-channel inputs keep one box per tap
-  static constexpr bool ROW3 = CIN == 64;
-  static constexpr int NSTAGE = CIN == 16 ? 12 : (COUT == 16 ? 4 : 6);
+  // a stage holds one grid row of the tile with its left and right halo
+  // cells (TM + 2 rows of RB bytes), and the MMAs read its three column
+  // shifts at one-row offsets: a tile takes three boxes, one per grid row.
+  // Stages in flight (three tiles of the input layer's 4 KB boxes, two of
+  // the 17 KB ones) and persistent blocks per SM: the narrow layers' MMAs
+  // are short, so several blocks per SM overlap their load latencies
+  // (shared memory and TMEM allow it: 3 x 65 KB and 3 x 128 columns,
+  // 2 x 88 KB and 2 x 32 columns; the 64 -> 64 layer 1 x 176 KB)
+  static constexpr int NSTAGE = CIN == 16 ? 9 : (COUT == 16 ? 4 : 6);
   static constexpr int CTAS_PER_SM = CIN == 16 ? 3 : (COUT == 16 ? 2 : 1);
   static_assert(NSTAGE <= MAXSTAGE, "barrier slots");
-  static constexpr int BOX_ROWS = ROW3 ? TM + 2 : TM;  // cells per activation box
+  static constexpr int BOX_ROWS = TM + 2;              // cells per activation box
   static constexpr int A_BYTES = BOX_ROWS * RB;        // one activation box
   static constexpr int A_STRIDE = (A_BYTES + 1023) / 1024 * 1024;  // stages on swizzle-pattern boundaries
   static constexpr int B_BYTES = COUT * RB;            // one tap of the weights
@@ -148,9 +146,9 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, i
 // K-major operand: rows of 2 CIN bytes swizzled at that width, 8-row
 // groups SBO bytes apart (stride byte offset), descriptor version 1
 // (an operand may start a whole number of rows into a stage: the swizzle
-// follows the shared-memory address, so the one-row shifts of a ROW3 box
-// read with the matrix base offset left at 0 -- measured: bit-identical to
-// the mma.sync path, while the base offset set to the row gives garbage)
+// follows the shared-memory address, so the one-row shifts of a box read
+// with the matrix base offset left at 0 -- measured: bit-identical to the
+// mma.sync path, while the base offset set to the row gives garbage)
 template <int CIN, int COUT> __device__ __forceinline__ uint64_t sdesc(uint32_t saddr) {
   uint64_t d = 0;
   d |= (uint64_t)((saddr & 0x3FFFF) >> 4);
@@ -247,18 +245,16 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       for (int s = 0; s < NSTAGE; ++s) last_par[s] = -1;
       uint32_t i = 0;
       bool ok = true;
-      constexpr int NLOAD = L::ROW3 ? 3 : 9;  // boxes per tile: grid rows y-1..y+1, or taps
       for (int tile = blockIdx.x; tile < a.ntiles && ok; tile += gridDim.x) {
         const int row = tile / a.tiles_per_row, x0 = (tile - row * a.tiles_per_row) * TM;
         const int b = row / a.N1, y = row - b * a.N1;
-        for (int ld = 0; ld < NLOAD; ++ld, ++i) {
+        for (int dy = 0; dy < 3; ++dy, ++i) {
           const int s = i % NSTAGE;
           const uint32_t ph = (i / NSTAGE) & 1;
           if (!(ok = bar_wait(&bars->empty[s], ph ^ 1, abort, a.status))) break;
           bar_expect_tx(&bars->full[s], A_BYTES);
-          // ROW3: cells x0-1 .. x0+128 of row y+ld-1; else the tap's shifted 128 cells
-          const int cx = L::ROW3 ? x0 - 1 : x0 + ld % 3 - 1, cy = L::ROW3 ? y + ld - 1 : y + ld / 3 - 1;
-          tma_load_4d(smem + SMEM_A + s * L::A_STRIDE, &tmx, 0, cx, cy, b, &bars->full[s]);
+          // cells x0-1 .. x0+128 of grid row y+dy-1 (outside the grid: zeros)
+          tma_load_4d(smem + SMEM_A + s * L::A_STRIDE, &tmx, 0, x0 - 1, y + dy - 1, b, &bars->full[s]);
           last_par[s] = (int)ph;
         }
       }
@@ -279,26 +275,17 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         if (!(ok = bar_wait(&bars->acc_empty[buf], aph ^ 1, abort, a.status))) break;
         fence_after();
         const uint32_t d = tmem + buf * COUT;
-        constexpr int NLOAD = L::ROW3 ? 3 : 9;
-        for (int ld = 0; ld < NLOAD; ++ld, ++i) {
+        for (int dy = 0; dy < 3; ++dy, ++i) {
           const int s = i % NSTAGE;
           if (!(ok = bar_wait(&bars->full[s], (i / NSTAGE) & 1, abort, a.status))) break;
           fence_after();
-          if constexpr (L::ROW3) {
-            // taps 3 ld + dx: the box's rows dx .. dx + 127 (the cells x0+dx-1 ..)
+          // taps 3 dy + dx: the box's rows dx .. dx + 127 (the cells x0+dx-1 ..)
 #pragma unroll
-            for (int dx = 0; dx < 3; ++dx) {
-              const int tap = 3 * ld + dx;
-#pragma unroll
-              for (int kk = 0; kk < L::KSTEPS; ++kk)
-                mma_bf16<COUT>(d, sdesc<CIN, COUT>(sa + s * L::A_STRIDE + dx * L::RB + kk * 32),
-                               sdesc<CIN, COUT>(sb + tap * B_BYTES + kk * 32), (tap | kk) != 0 ? 1u : 0u);
-            }
-          } else {
-            const int tap = ld;
+          for (int dx = 0; dx < 3; ++dx) {
+            const int tap = 3 * dy + dx;
 #pragma unroll
             for (int kk = 0; kk < L::KSTEPS; ++kk)
-              mma_bf16<COUT>(d, sdesc<CIN, COUT>(sa + s * L::A_STRIDE + kk * 32),
+              mma_bf16<COUT>(d, sdesc<CIN, COUT>(sa + s * L::A_STRIDE + dx * L::RB + kk * 32),
                              sdesc<CIN, COUT>(sb + tap * B_BYTES + kk * 32), (tap | kk) != 0 ? 1u : 0u);
           }
           mma_commit(&bars->empty[s]);  // the stage is free once these MMAs have read it
@@ -404,8 +391,8 @@ template <int CIN, int COUT, int EPI> static int set_smem() {
              : 1;
 }
 
-// the activation map [B][N1][N0][CIN] read as boxes {CIN, 128, 1, 1} (64
-// channels: {CIN, 130, 1, 1}, a grid row of the tile with its halo), and the
+// the activation map [B][N1][N0][CIN] read as boxes {CIN, 130, 1, 1} (a
+// grid row of the tile with its halo cells), and the
 // weights [COUT][9 CIN] as boxes {CIN, COUT} (one tap), both swizzled as the
 // UMMA descriptors read them
 template <int CIN, int COUT>
