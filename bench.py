@@ -15,7 +15,8 @@ store_old_positions, stream_particles, apply_BC.  The line also carries the
 plain path on the same workload (FP32 and FP64 particle-steps/s) and the
 errors of the surrogate run against the FP64 plain run in n, T and the
 force field.  Other workloads (--workload): uneven16m (65,536 cells with
-log-normal occupancy), esmc6m, slab1m, vlasov16m (the plain 2-D force).
+log-normal occupancy), esmc6m, dsmc6m (the same box with Bird's DSMC), slab1m,
+vlasov16m (the plain 2-D force).
 
   value  particle-steps/s with the state resident in HBM (CUDA events on the
          launch stream, max over ranks).  The particle state (16M x 20 B +
@@ -175,6 +176,11 @@ def build_workload(args):
     elif args.workload == "esmc6m":
         cfg, parts = W.esmc_box_2d(precision=mcpm.FP32)
         desc = {"workload": "ESMC 256x256 100/cell nb=0.2 diffuse walls fp32", "cells": 65536,
+                "particles": int(len(parts["x2"]))}
+    elif args.workload == "dsmc6m":
+        cfg, parts = W.esmc_box_2d(precision=mcpm.FP32)
+        cfg = W.with_dsmc_vhs(cfg)
+        desc = {"workload": "DSMC_VHS 256x256 100/cell diffuse walls fp32", "cells": 65536,
                 "particles": int(len(parts["x2"]))}
     elif args.workload == "surrogate16m":
         cfg, parts = W.vlasov_box_2d(n_cells=(256, 256), total=16_000_000, precision=mcpm.FP32,
@@ -368,13 +374,15 @@ def side_workloads(args, stream, steps=20):
     """The survey's other configurations timed the same way (device-resident,
     CUDA events on the launch stream, after 3 warm-up steps), each in its
     own session: the uneven 16M box (config 4; threads-per-cell autotuned),
-    the 2-D ESMC box (config 3) and the 1-D Vlasov slab (config 2, FP32 and
-    FP64).  Returns {workload: {value, ms_per_step, particles, ...}}."""
+    the 2-D ESMC box (config 3), the same box with Bird's DSMC (the sibling
+    collision operator) and the 1-D Vlasov slab (config 2, FP32 and FP64).
+    Returns {workload: {value, ms_per_step, particles, ...}}."""
     import torch
 
     import mcpm
     out = {}
-    runs = [("uneven16m", mcpm.FP32), ("esmc6m", mcpm.FP32), ("slab1m", mcpm.FP32), ("slab1m", mcpm.FP64)]
+    runs = [("uneven16m", mcpm.FP32), ("esmc6m", mcpm.FP32), ("dsmc6m", mcpm.FP32), ("slab1m", mcpm.FP32),
+            ("slab1m", mcpm.FP64)]
     for name, prec in runs:
         a = argparse.Namespace(**vars(args))
         a.workload = name
@@ -736,7 +744,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="mcpm", choices=["mcpm", "reference"])
     ap.add_argument("--workload", default="surrogate16m",
-                    choices=["surrogate16m", "uneven16m", "esmc6m", "slab1m", "vlasov16m"])
+                    choices=["surrogate16m", "uneven16m", "esmc6m", "dsmc6m", "slab1m", "vlasov16m"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--horizon", type=int, default=2000,
                     help="last accuracy checkpoint of the learned-force workload (steps)")

@@ -244,13 +244,19 @@ int launch_esmc(Session& s) { return s.prec == MCPM_FP32 ? esmc_impl<float>(s) :
 // post-collision relative velocity of the same magnitude (cos theta =
 // 2 a1 - 1, phi = 2 pi a2) about the pair's centre of mass.  As in the ESMC
 // kernel a warp draws 32 candidates and applies the longest prefix with
-// disjoint pairs, which equals processing them one after another.  The
-// majorant then becomes max(1.1 max sigma_T, 0.9 crm_I) (:2135).
+// disjoint pairs, which equals processing them one after another (both
+// particles of a pair lie in the cell: the warp's slot table of the ESMC
+// kernel finds every conflict).  The majorant then becomes
+// max(1.1 max sigma_T, 0.9 crm_I) (:2135).
 template <typename real>
 __global__ void __launch_bounds__(128) k_dsmc_vhs(DevConsts k, double* cell, const int32_t* off,
                                                   const int32_t* cnt, PT2<real> p, const int32_t* dstep,
                                                   uint32_t* status) {
+  __shared__ int tabs[4][ESMC_TAB];
   const int lane = threadIdx.x & 31;
+  int* tab = tabs[threadIdx.x >> 5];
+  for (int e = lane; e < ESMC_TAB; e += 32) tab[e] = 32;
+  __syncwarp();
   const int I = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (I >= k.C) return;
   const int NI = cnt[I];
@@ -269,13 +275,13 @@ __global__ void __launch_bounds__(128) k_dsmc_vhs(DevConsts k, double* cell, con
   else if (lane == 0) raise_status(status, MCPM_ERR_ITER_LIMIT);
   constexpr bool F32 = sizeof(real) == 4;
   const real e = (real)k.vhs_e, cr = (real)k.vhs_cr, crm_r = (real)crm, half = (real)0.5;
-  const int64_t o = off[I];
+  const int o = off[I];
   real seen = 0;
   int base = 0;
   while (base < mI) {
     const int kc = base + lane;
     const bool valid = kc < mI;
-    int64_t si = -1, sj = -1;
+    int si = -1, sj = -1;
     uint4 r = make_uint4(0u, 0u, 0u, 0u);
     if (valid) {
       r = rng_draw(k, (uint32_t)I, (uint32_t)step, RNG_DSMC, (uint32_t)kc);
@@ -286,11 +292,7 @@ __global__ void __launch_bounds__(128) k_dsmc_vhs(DevConsts k, double* cell, con
       sj = o + b;
     }
     // longest prefix of candidates with pairwise disjoint particles
-    bool conflict = false;
-    for (int l = 0; l < 31; ++l) {
-      int64_t oi = __shfl_sync(FULL, si, l), oj = __shfl_sync(FULL, sj, l);
-      if (l < lane && valid && (oi == si || oi == sj || oj == si || oj == sj)) conflict = true;
-    }
+    const bool conflict = esmc_conflict(tab, o, NI, valid, si, sj);
     const unsigned cm = __ballot_sync(FULL, conflict);
     int take = cm ? (__ffs(cm) - 1) : 32;
     if (take > mI - base) take = mI - base;
