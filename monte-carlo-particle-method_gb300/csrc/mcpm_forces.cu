@@ -248,10 +248,16 @@ int launch_esmc(Session& s) { return s.prec == MCPM_FP32 ? esmc_impl<float>(s) :
 // particles of a pair lie in the cell: the warp's slot table of the ESMC
 // kernel finds every conflict).  The majorant then becomes
 // max(1.1 max sigma_T, 0.9 crm_I) (:2135).
+// FP32 blocks of 4 warps declared resident per SM: 8 (measured 0.116 ms of
+// collisions per step on the 6.5M-particle box against 0.128 ms unbounded
+// and 0.126 ms at 12 blocks, whose 40 registers spill)
+#ifndef MCPM_DSMC_MINB
+#define MCPM_DSMC_MINB 8
+#endif
 template <typename real>
-__global__ void __launch_bounds__(128) k_dsmc_vhs(DevConsts k, double* cell, const int32_t* off,
-                                                  const int32_t* cnt, PT2<real> p, const int32_t* dstep,
-                                                  uint32_t* status) {
+__global__ void __launch_bounds__(128, sizeof(real) == 4 ? MCPM_DSMC_MINB : 1)
+    k_dsmc_vhs(DevConsts k, double* cell, const int32_t* off, const int32_t* cnt, PT2<real> p, const int32_t* dstep,
+               uint32_t* status) {
   __shared__ int tabs[4][ESMC_TAB];
   const int lane = threadIdx.x & 31;
   int* tab = tabs[threadIdx.x >> 5];
