@@ -333,6 +333,60 @@ __global__ void __launch_bounds__(256) k_sgemm(int M, int N, int K, const float*
     }
 }
 
+// The same product for K <= SGEMM_KMAX: the block's 32 rows of A and 32
+// columns of B over the whole of K are staged into shared memory at once
+// (one round of independent loads instead of one round trip per 32-wide
+// slice, which bounds these small transforms), then each output sums over
+// k = 0 .. K-1 in the same order as k_sgemm (the same results bit for bit).
+constexpr int SGEMM_KMAX = 256;
+constexpr size_t sgemm_fullk_smem(int K) { return (size_t)(32 * (K + 1) + K * 33) * sizeof(float); }
+__global__ void __launch_bounds__(256) k_sgemm_fullk(int M, int N, int K, const float* A, const float* B, float* C,
+                                                     const float* D, double* U, int mode) {
+  extern __shared__ float sg[];
+  float* As = sg;                    // [32][K + 1]
+  float* Bs = sg + 32 * (K + 1);     // [K][33]
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  const int r0 = blockIdx.y * 32, c0 = blockIdx.x * 32;
+  for (int e = threadIdx.x; e < 32 * K; e += 256) {
+    const int r = e / K, q = e - r * K;
+    As[r * (K + 1) + q] = r0 + r < M ? A[(size_t)(r0 + r) * K + q] : 0.f;
+  }
+  for (int e = threadIdx.x; e < K * 32; e += 256) {
+    const int q = e >> 5, c = e & 31;
+    Bs[q * 33 + c] = c0 + c < N ? B[(size_t)q * N + c0 + c] : 0.f;
+  }
+  __syncthreads();
+  float acc[2][2] = {{0.f, 0.f}, {0.f, 0.f}};
+  const float* a0p = As + (2 * ty) * (K + 1);
+  const float* a1p = a0p + (K + 1);
+#pragma unroll 8
+  for (int q = 0; q < K; ++q) {
+    const float a0 = a0p[q], a1 = a1p[q];
+    const float b0 = Bs[q * 33 + 2 * tx], b1 = Bs[q * 33 + 2 * tx + 1];
+    acc[0][0] = fmaf(a0, b0, acc[0][0]); acc[0][1] = fmaf(a0, b1, acc[0][1]);
+    acc[1][0] = fmaf(a1, b0, acc[1][0]); acc[1][1] = fmaf(a1, b1, acc[1][1]);
+  }
+#pragma unroll
+  for (int i = 0; i < 2; ++i)
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+      const int row = r0 + 2 * ty + i, col = c0 + 2 * tx + j;
+      if (row >= M || col >= N) continue;
+      const size_t o = (size_t)row * N + col;
+      if (mode == 0) C[o] = acc[i][j];
+      else if (mode == 1) C[o] = acc[i][j] / D[o];
+      else if (mode == 2) U[o] = (double)acc[i][j];
+      else U[o] += (double)acc[i][j];
+    }
+}
+
+// C = A B on the session's stream: the whole-K kernel where K allows
+static void sgemm(dim3 g, int M, int N, int K, const float* A, const float* B, float* C, const float* D, double* U,
+                  int mode, cudaStream_t st) {
+  if (K <= SGEMM_KMAX) k_sgemm_fullk<<<g, 256, sgemm_fullk_smem(K), st>>>(M, N, K, A, B, C, D, U, mode);
+  else k_sgemm<<<g, 256, 0, st>>>(M, N, K, A, B, C, D, U, mode);
+}
+
 // the right-hand side in FP32 for the first pass
 __global__ void k_to_f32(const double* a, float* b, int n) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) b[i] = (float)a[i];
@@ -635,6 +689,11 @@ int lr2d_setup(Session& s) {
     s.err = "2-D long-range stencil: shared memory";
     return 1;
   }
+  if (cudaFuncSetAttribute(k_sgemm_fullk, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)sgemm_fullk_smem(SGEMM_KMAX)) != cudaSuccess) {
+    s.err = "2-D long-range transforms: shared memory";
+    return 1;
+  }
   cudaMemset(t->V, 0, (size_t)t->nn * 8);
   cudaMemset(t->nnd, 0, (size_t)k.C * 4 * 8);
   return 0;
@@ -714,10 +773,10 @@ int launch_long_range_2d(Session& s, const double* n) {
         ++launches;
       }
       // delta = S_y ((S_y r S_x) / mu) S_x  (rows y, columns x); U (+)= delta
-      k_sgemm<<<g, 256, 0, s.stream>>>(ny, nx, ny, t->Sy, t->Bf, t->Tf, nullptr, nullptr, 0);
-      k_sgemm<<<g, 256, 0, s.stream>>>(ny, nx, nx, t->Tf, t->Sx, t->Bf, t->mu, nullptr, 1);
-      k_sgemm<<<g, 256, 0, s.stream>>>(ny, nx, ny, t->Sy, t->Bf, t->Tf, nullptr, nullptr, 0);
-      k_sgemm<<<g, 256, 0, s.stream>>>(ny, nx, nx, t->Tf, t->Sx, nullptr, nullptr, t->U, it == 0 ? 2 : 3);
+      sgemm(g, ny, nx, ny, t->Sy, t->Bf, t->Tf, nullptr, nullptr, 0, s.stream);
+      sgemm(g, ny, nx, nx, t->Tf, t->Sx, t->Bf, t->mu, nullptr, 1, s.stream);
+      sgemm(g, ny, nx, ny, t->Sy, t->Bf, t->Tf, nullptr, nullptr, 0, s.stream);
+      sgemm(g, ny, nx, nx, t->Tf, t->Sx, nullptr, nullptr, t->U, it == 0 ? 2 : 3, s.stream);
       launches += 4;
     }
     k_sp_finish<<<blocks_for(t->nn, 256, cap), 256, 0, s.stream>>>(*t, t->near1, t->near2);
