@@ -19,7 +19,10 @@ pytestmark = pytest.mark.gpu
 
 def _make(shape, prec):
     if shape[0] == 1:
-        cfg, parts = W.homogeneous_relaxation_1d(n_cells=shape[1], ppc=80, precision=prec)
+        # (1, 8): 400 particles a cell, past the warp's 256-slot conflict
+        # table (the candidates are then compared pairwise over the warp)
+        ppc = 400 if shape[1] == 8 else 80
+        cfg, parts = W.homogeneous_relaxation_1d(n_cells=shape[1], ppc=ppc, precision=prec)
     else:
         cfg, parts = W.esmc_box_2d(n_cells=shape, ppc=60, precision=prec)
     return W.with_dsmc_vhs(cfg), parts
@@ -48,7 +51,7 @@ def _same_layout_pass(cfg, parts):
     return s, o, om0
 
 
-@pytest.mark.parametrize("shape", [(1, 30), (14, 12)])
+@pytest.mark.parametrize("shape", [(1, 30), (14, 12), (1, 8)])
 def test_dsmc_fp64_same_layout(cuda_ok, shape):
     cfg, parts = _make(shape, mcpm.FP64)
     s, o, om0 = _same_layout_pass(cfg, parts)

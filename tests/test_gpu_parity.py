@@ -337,12 +337,14 @@ def test_diffuse_walls_fp64(cuda_ok, problem):
 
 
 # ---------------------------------------------------------------- ESMC
-@pytest.mark.parametrize("shape", [(1, 30), (14, 12)])
+@pytest.mark.parametrize("shape", [(1, 30), (14, 12), (1, 8)])
 def test_esmc_fp64_same_layout(cuda_ok, shape):
     """ESMC with the GPU's in-cell order given to the oracle: candidate picks,
-    directions, partners and acceptances then coincide."""
+    directions, partners and acceptances then coincide.  (1, 8): 400
+    particles a cell, past the warp's 256-slot conflict table (the candidates
+    are then compared pairwise over the warp)."""
     if shape[0] == 1:
-        cfg, parts = W.homogeneous_relaxation_1d(n_cells=shape[1], ppc=80)
+        cfg, parts = W.homogeneous_relaxation_1d(n_cells=shape[1], ppc=400 if shape[1] == 8 else 80)
         cfg.model = mcpm.MODEL_ESMC
     else:
         cfg, parts = W.esmc_box_2d(n_cells=shape, ppc=60, precision=mcpm.FP64)
