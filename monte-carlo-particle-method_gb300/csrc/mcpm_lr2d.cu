@@ -68,6 +68,7 @@ struct LR2D {
   double* V = nullptr;      // [nn] node potential
   double* nnd = nullptr;    // [C][4] nodal densities n_n
   double* ncell = nullptr;  // [C] cell densities from the layout's counts (the per-cell solve's values)
+  double* vol = nullptr;    // [C] cell volumes, cell_volume() formed once at set-up
   int32_t* qc = nullptr;    // [C][4] particles per cell quadrant
   float *Sx = nullptr, *Sy = nullptr, *mu = nullptr, *Bf = nullptr, *Tf = nullptr;  // FP32 transforms
   double *B = nullptr, *U = nullptr;  // FP64 right-hand side and solution (interior, rows y)
@@ -165,7 +166,11 @@ __global__ void k_quadrants_f32(DevConsts k, const int32_t* off, const int32_t* 
 // cell sharing the node, each adding Fn/volume(c); wall nodes doubled per
 // wall (src/Main_Functions.cpp:2268-2364).  exact: the sum of equal terms in
 // sequence, as the reference accumulates it.
-__global__ void k_node_density(DevConsts k, const int32_t* qc, double* nnd, int exact,
+__global__ void k_cell_volumes(DevConsts k, double* vol) {
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < k.C; c += gridDim.x * blockDim.x) vol[c] = cell_volume(c, k);
+}
+
+__global__ void k_node_density(DevConsts k, const double* vol, const int32_t* qc, double* nnd, int exact,
                                __nv_bfloat16* xin = nullptr, const int32_t* ccnt = nullptr,
                                double* ncell = nullptr) {
   // the network's first layer (launched as a programmatic dependent) may
@@ -182,7 +187,7 @@ __global__ void k_node_density(DevConsts k, const int32_t* qc, double* nnd, int 
     if (ni > 0 && nj < N1) count += qc[(size_t)(nj * N0 + ni - 1) * 4 + 1];
     if (ni < N0 && nj > 0) count += qc[(size_t)((nj - 1) * N0 + ni) * 4 + 2];
     if (ni > 0 && nj > 0) count += qc[(size_t)((nj - 1) * N0 + ni - 1) * 4 + 3];
-    const double v = k.Fn / cell_volume(c, k);
+    const double v = k.Fn / vol[c];
     double acc = 0.0;
     if (exact) {
       for (int t = 0; t < count; ++t) acc += v;
@@ -199,7 +204,7 @@ __global__ void k_node_density(DevConsts k, const int32_t* qc, double* nnd, int 
     // moment pass)
     double ncv = 0.0;
     if ((xin || ncell) && slot == 0) {
-      ncv = (k.cell_w ? k.cell_w[c] : 1) * k.Fn * (double)ccnt[c] / cell_volume(c, k);
+      ncv = (k.cell_w ? k.cell_w[c] : 1) * k.Fn * (double)ccnt[c] / vol[c];
       if (ncell) ncell[c] = ncv;
     }
     if (xin) {
@@ -276,7 +281,7 @@ __global__ void k_sp_rhs(LR2D t, DevConsts k) {
     for (int q = 0; q < 4; ++q) {
       const int ci = i - 1 + (q & 1), cj = j - 1 + (q >> 1), slot = 3 - q;
       const int c = cj * N0 + ci;
-      const double vol = cell_volume(c, k);
+      const double vol = t.vol[c];
       const double* nn = t.nnd + (size_t)c * 4;
       double v = 0.0;
       for (int l = 0; l < 4; ++l) v += nn[l] * c_uv[slot][l];
@@ -631,7 +636,7 @@ int lr2d_setup(Session& s) {
             A((void**)&t->exc_i, st.exc_i.size() * 4) && H(t->exc_i, st.exc_i.data(), st.exc_i.size() * 4) &&
             A((void**)&t->exc_w, st.exc_w.size() * 8) && H(t->exc_w, st.exc_w.data(), st.exc_w.size() * 8) &&
             A((void**)&t->V, (size_t)t->nn * 8) && A((void**)&t->nnd, (size_t)k.C * 4 * 8) &&
-            A((void**)&t->ncell, (size_t)k.C * 8) &&
+            A((void**)&t->ncell, (size_t)k.C * 8) && A((void**)&t->vol, (size_t)k.C * 8) &&
             A((void**)&t->qc, (size_t)k.C * 4 * 4);
   if (ok && s.prec == MCPM_FP32) {
     // the FP32 quadrant pass compares positions with thresholds: x < the
@@ -696,13 +701,19 @@ int lr2d_setup(Session& s) {
   }
   cudaMemset(t->V, 0, (size_t)t->nn * 8);
   cudaMemset(t->nnd, 0, (size_t)k.C * 4 * 8);
+  // on the default stream, finished before any session stream reads them
+  k_cell_volumes<<<std::max(1, std::min((k.C + 255) / 256, s.num_sms * 8)), 256>>>(k, t->vol);
+  if (cudaStreamSynchronize(0) != cudaSuccess || cudaGetLastError() != cudaSuccess) {
+    s.err = "2-D long-range tables: cell volumes";
+    return 1;
+  }
   return 0;
 }
 
 void lr2d_free(Session& s) {
   LR2D* t = s.lr2d;
   if (!t) return;
-  cudaFree(t->W); cudaFree(t->exc_off); cudaFree(t->exc_i); cudaFree(t->exc_w); cudaFree(t->V); cudaFree(t->nnd); cudaFree(t->ncell);
+  cudaFree(t->W); cudaFree(t->exc_off); cudaFree(t->exc_i); cudaFree(t->exc_w); cudaFree(t->V); cudaFree(t->nnd); cudaFree(t->ncell); cudaFree(t->vol);
   cudaFree(t->qc); cudaFree(t->Sx); cudaFree(t->Sy); cudaFree(t->mu); cudaFree(t->B); cudaFree(t->U); cudaFree(t->Bf); cudaFree(t->Tf);
   cudaFree(t->wall); cudaFree(t->qtx); cudaFree(t->qty);
   delete t;
@@ -723,7 +734,7 @@ double* lr2d_node_density_mut(Session& s) { return s.lr2d ? s.lr2d->nnd : nullpt
 int launch_node_density_from(Session& s, const int32_t* qc) {
   LR2D* t = s.lr2d;
   if (!t) return 0;
-  k_node_density<<<blocks_for(4L * s.C, 256, s.num_sms * 16), 256, 0, s.stream>>>(s.k, qc, t->nnd, 0);
+  k_node_density<<<blocks_for(4L * s.C, 256, s.num_sms * 16), 256, 0, s.stream>>>(s.k, t->vol, qc, t->nnd, 0);
   return 1;
 }
 
@@ -744,7 +755,7 @@ int launch_node_density(Session& s, bool count_density) {
     k_quadrants<double><<<g, 256, 0, s.stream>>>(s.k, s.off, s.cnt, (const double*)P.x1, (const double*)P.x2, t->qc);
   }
   k_node_density<<<blocks_for(4L * s.C, 256, s.num_sms * 16), 256, 0, s.stream>>>(
-      s.k, t->qc, t->nnd, s.prec == MCPM_FP64, xin, s.cnt, count_density ? t->ncell : nullptr);
+      s.k, t->vol, t->qc, t->nnd, s.prec == MCPM_FP64, xin, s.cnt, count_density ? t->ncell : nullptr);
   return 2;
 }
 
