@@ -371,11 +371,12 @@ def surrogate_comparison(args, cfg, parts, s, stream):
 
 
 def side_workloads(args, stream, steps=20):
-    """The survey's other configurations timed the same way (device-resident,
+    """The other benchmark workloads timed the same way (device-resident,
     CUDA events on the launch stream, after 3 warm-up steps), each in its
-    own session: the uneven 16M box (config 4; threads-per-cell autotuned),
-    the 2-D ESMC box (config 3), the same box with Bird's DSMC (the sibling
-    collision operator) and the 1-D Vlasov slab (config 2, FP32 and FP64).
+    own session: the uneven 16M box (65,536 cells of 10 to 5,000 particles;
+    threads-per-cell autotuned), the 2-D ESMC box (256 x 256 cells of 100),
+    the same box with Bird's DSMC (the sibling collision operator) and the
+    1-D Vlasov slab (1,000 cells of 1,000 particles, FP32 and FP64).
     Returns {workload: {value, ms_per_step, particles, ...}}."""
     import torch
 
