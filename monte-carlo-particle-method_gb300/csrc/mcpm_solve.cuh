@@ -536,15 +536,19 @@ __global__ void __launch_bounds__(MCPM_SOLVE_T, MCPM_SOLVE_MINB)
         W(CFI_A3, sqrt((1.0 - exp(-2.0 * k.dt / tau)) * k.kb * T / (1.0 * k.m)));
         W(CFI_A2, (1.0 - exp(-k.dt / tau)) * tau);
       } else {
-        const double tau = 2.0 * mu / (n * k.kb * T * Y);
-        const double e1 = exp(-k.dt / tau);  // exp(-2 dt/tau) = e1^2
-        W(CFI_A1, e1);
-        W(CFI_A3, sqrt((1.0 - e1 * e1) * T * k.q_kb_m));
-        W(CFI_A2, (1.0 - e1) * tau);
+        // the FP32 sessions' record holds these as floats: formed in float
+        // (off GB300's FP64 pipe, which bounds this kernel), 1 - e^-x by
+        // expm1f so that a small dt / tau keeps its digits
+        const float tau = 2.0f * (float)mu / ((float)n * (float)k.kb * (float)T * (float)Y);
+        const float x = (float)k.dt / tau;
+        W(CFI_A1, (double)expf(-x));
+        W(CFI_A3, (double)sqrtf(-expm1f(-2.0f * x) * ((float)T * (float)k.q_kb_m)));
+        W(CFI_A2, (double)(-expm1f(-x) * tau));
       }
     }
   }
-  const double eq3 = 3.0 * k.kb * T / k.m;
+  // 3 kT / m (the FP32 sessions' record holds it as a float: formed in float)
+  const double eq3 = EXACT ? 3.0 * k.kb * T / k.m : (double)(3.0f * (float)T * (float)k.q_kb_m);
   W(CFI_3KT, eq3);
   const double ph0 = al[0] * Mp[0] + al[1] * Mp[1] + al[2] * Mp[2];
   const double ph1 = al[3] * Mp[0] + al[4] * Mp[1] + al[5] * Mp[2];
