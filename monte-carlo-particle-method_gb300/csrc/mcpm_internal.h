@@ -191,6 +191,10 @@ struct Session {
   // runs on a stream of its own, beside the moment pass and the solves
   cudaStream_t side = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  // on a judge step the branch runs the network on a stream of its own
+  // beside the plain path (side2), joined before the comparison
+  cudaStream_t side2 = nullptr;
+  cudaEvent_t ev_fork2 = nullptr, ev_net = nullptr;
   // host transfers: uploads copy into stage_in on h2d, downloads copy out of
   // stage on d2h, so that a download's copies overlap the next upload's
   // (the host link runs both directions at once); the events order the

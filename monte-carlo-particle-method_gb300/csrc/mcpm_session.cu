@@ -254,6 +254,9 @@ int mcpm_session_create(const mcpm_config* cfg, mcpm_session** out) {
   if ((rc = cuda_check(s, cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking), "stream"))) { delete s; return rc; }
   cudaEventCreateWithFlags(&s->ev_fork, cudaEventDisableTiming);
   cudaEventCreateWithFlags(&s->ev_join, cudaEventDisableTiming);
+  if ((rc = cuda_check(s, cudaStreamCreateWithFlags(&s->side2, cudaStreamNonBlocking), "stream"))) { mcpm_session_destroy(s); return rc; }
+  cudaEventCreateWithFlags(&s->ev_fork2, cudaEventDisableTiming);
+  cudaEventCreateWithFlags(&s->ev_net, cudaEventDisableTiming);
   if ((rc = cuda_check(s, cudaStreamCreateWithFlags(&s->h2d, cudaStreamNonBlocking), "stream"))) { mcpm_session_destroy(s); return rc; }
   if ((rc = cuda_check(s, cudaStreamCreateWithFlags(&s->d2h, cudaStreamNonBlocking), "stream"))) { mcpm_session_destroy(s); return rc; }
   cudaEventCreateWithFlags(&s->ev_in_free, cudaEventDisableTiming);
@@ -385,6 +388,9 @@ int mcpm_session_destroy(mcpm_session* s) {
   for (auto e : s->prof_pool) cudaEventDestroy(e);
   if (s->own_stream) cudaStreamDestroy(s->own_stream);
   if (s->side) { cudaStreamSynchronize(s->side); cudaStreamDestroy(s->side); }
+  if (s->side2) { cudaStreamSynchronize(s->side2); cudaStreamDestroy(s->side2); }
+  if (s->ev_fork2) cudaEventDestroy(s->ev_fork2);
+  if (s->ev_net) cudaEventDestroy(s->ev_net);
   if (s->h2d) { cudaStreamSynchronize(s->h2d); cudaStreamDestroy(s->h2d); }
   if (s->d2h) { cudaStreamSynchronize(s->d2h); cudaStreamDestroy(s->d2h); }
   if (s->ev_fork) cudaEventDestroy(s->ev_fork);
@@ -669,6 +675,22 @@ static int long_range_force(mcpm_session* s, bool branch) {
   const double* ncell = s->cell + (size_t)MCPM_CF_N * s->C;
   if (s->sur && s->sur_active && !s->sur_judge_now)
     return T_SUR(sur_forward_kick(*s, lr2d_node_density(*s), ncell));
+  if (branch && s->sur && s->sur_judge_now && s->side2) {
+    // a judge step in the branch: the network's forward on a stream of its
+    // own beside the plain path (their inputs are the deposit's, their
+    // outputs apart), the comparison once both are done
+    int n = 0;
+    cudaEventRecord(s->ev_fork2, s->stream);
+    cudaStreamWaitEvent(s->side2, s->ev_fork2, 0);
+    cudaStream_t branch_stream = s->stream;
+    s->stream = s->side2;
+    n += T_SUR(sur_judge_forward(*s, lr2d_node_density(*s), ncell));
+    cudaEventRecord(s->ev_net, s->side2);
+    s->stream = branch_stream;
+    n += T_LR(launch_long_range_2d(*s, lr2d_count_density(*s)));
+    cudaStreamWaitEvent(s->stream, s->ev_net, 0);
+    return n + T_SUR(sur_judge_compare(*s));
+  }
   int n = T_LR(branch ? launch_long_range_2d(*s, lr2d_count_density(*s)) : launch_long_range(*s));
   if (s->sur && s->sur_judge_now) n += T_SUR(sur_judge(*s, lr2d_node_density(*s), ncell));
   return n;

@@ -713,15 +713,24 @@ int sur_forward_kick(Session& s, const double* nnd, const double* ncell) {
   return in + forward(n, n.xin, 1, nullptr, s.pcell, (float)g1, (float)g2, s.stream, true, s.status);
 }
 
-int sur_judge(Session& s, const double* nnd, const double* ncell) {
+int sur_judge_forward(Session& s, const double* nnd, const double* ncell) {
+  SurrogateNet& n = *s.sur;
+  const int launches = sur_input(s, nnd, ncell);
+  return launches + forward(n, n.xin, 1, n.y, nullptr, 0.f, 0.f, s.stream, true, s.status);
+}
+
+int sur_judge_compare(Session& s) {
   SurrogateNet& n = *s.sur;
   const double g1 = s.k.lr_coef / s.k.m / s.k.dx * s.k.dt, g2 = s.k.lr_coef / s.k.m / s.k.dy * s.k.dt;
-  int launches = sur_input(s, nnd, ncell);
-  launches += forward(n, n.xin, 1, n.y, nullptr, 0.f, 0.f, s.stream, true, s.status);
   const int Gj = gblocks(s.C, NT, RED_G);
   k_judge<<<Gj, NT, 0, s.stream>>>(n.y, (float)n.oscale, (float)g1, (float)g2, s.pcell, s.C, n.lpart);
   k_pair_reduce<<<1, 32, 0, s.stream>>>(n.lpart, Gj, s.sur_err);
-  return launches + 2;
+  return 2;
+}
+
+int sur_judge(Session& s, const double* nnd, const double* ncell) {
+  const int launches = sur_judge_forward(s, nnd, ncell);
+  return launches + sur_judge_compare(s);
 }
 
 int sur_snapshot(Session& s, const double* fld_dev, int K, uint64_t seed, uint32_t snap, int32_t* qc, double* nnd,

@@ -83,6 +83,11 @@ int tc_conv_mask(int cin, const __nv_bfloat16* x, const __nv_bfloat16* w, const 
 // session-side launchers (mcpm_surrogate.cu); each returns its launches
 int sur_forward_kick(Session& s, const double* nnd, const double* ncell);
 int sur_judge(Session& s, const double* nnd, const double* ncell);
+// the judge in two parts: the network's output for the comparison, then the
+// comparison with the plain path's kick in the record (the plain path may
+// run on another stream in between)
+int sur_judge_forward(Session& s, const double* nnd, const double* ncell);
+int sur_judge_compare(Session& s);
 int sur_snapshot(Session& s, const double* fld_dev, int K, uint64_t seed, uint32_t snap, int32_t* qc, double* nnd,
                  double* ncell, uint16_t* x, float* y);
 
