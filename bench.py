@@ -549,15 +549,17 @@ def run_mcpm(args):
     t0 = time.perf_counter()
     step0 = s.step_count
     # every step uploads its inputs and reads its result back; the copies
-    # are queued (mcpm_upload_particles_async, mcpm_download_particles_async:
-    # the host arrays stay untouched until the final sync), so that one
-    # step's result copies overlap the next step's input copies and compute
+    # and the step are queued (mcpm_upload_particles_async, mcpm_step_async,
+    # mcpm_download_particles_async: the host arrays stay untouched until the
+    # final sync), so that one step's result copies overlap the next step's
+    # input copies and compute; the device status is read once at the end
     for i in range(e2e_steps):
         s.upload(hin["x1"], hin["x2"], hin["U1"], hin["U2"], hin["U3"], wait=False)
         s.set_step(step0 + i)  # the caller's simulation continues (upload restarts the counter)
-        s.step(1)
+        s.step(1, wait=False)
         s.download_into(hout, wait=False)
     s.sync()
+    s.check_status()
     torch.cuda.synchronize()
     e2e_ms = (time.perf_counter() - t0) * 1e3 / e2e_steps
     e2e = {"value": N * ws / (e2e_ms / 1e3), "unit": UNIT, "h2d_bytes_per_step": 5 * 8 * N,

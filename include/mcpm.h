@@ -322,8 +322,15 @@ int mcpm_end_step(mcpm_session* s);
    (src/main.cpp:442), which leaves Velocity_FP_linear reading noise arrays
    that nothing filled (malloc'd at :129).  The particle-side stages run fused in one kernel per step;
    once the cell layout is in its steady state, pairs of steps are replayed
-   as one CUDA graph (not in profiling mode). */
+   as one CUDA graph (not in profiling mode).  Returns once the steps have
+   run, with the device status bits (mcpm_check_status). */
 int mcpm_step(mcpm_session* s, int32_t n_steps);
+/* The same steps, returning once they are queued: the host goes on (an
+   upload or download of the next batch, mcpm_*_async) while the device
+   steps.  The status bits stay on the device until mcpm_check_status or a
+   synchronous step reads them.  A judge step of an attached learned force
+   still waits for its verdict before the steps after it are queued. */
+int mcpm_step_async(mcpm_session* s, int32_t n_steps);
 
 /* ---- test and diagnostic hooks ---------------------------------------- */
 /* Raw (un-whitened) normals for the next random_generator, per particle id

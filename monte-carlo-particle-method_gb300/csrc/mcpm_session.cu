@@ -882,7 +882,9 @@ static int read_judge(mcpm_session* s) {
   return MCPM_OK;
 }
 
-int mcpm_step(mcpm_session* s, int32_t n_steps) {
+// queues n_steps iterations; a judge step of an attached learned force
+// reads its verdict on the host before the steps after it are queued
+static int step_enqueue(mcpm_session* s, int32_t n_steps) {
   if (!s || !s->have_particles || n_steps < 0) return fail(s, MCPM_ERR_STATE, "step: no particles");
   const int m = s->cfg.model;
   if ((m == MCPM_MODEL_ESMC || m == MCPM_MODEL_DSMC_VHS) && !s->omega_init) {
@@ -919,8 +921,15 @@ int mcpm_step(mcpm_session* s, int32_t n_steps) {
     if ((rc = run_steps(s, run, stages))) return rc;
     it += run;
   }
-  return mcpm_check_status(s);
+  return MCPM_OK;
 }
+
+int mcpm_step(mcpm_session* s, int32_t n_steps) {
+  const int rc = step_enqueue(s, n_steps);
+  return rc ? rc : mcpm_check_status(s);
+}
+
+int mcpm_step_async(mcpm_session* s, int32_t n_steps) { return step_enqueue(s, n_steps); }
 
 // ------------------------------------------------- learned Vlasov force
 int mcpm_attach_surrogate(mcpm_session* s, mcpm_surrogate* m, int32_t judge_every, double threshold) {

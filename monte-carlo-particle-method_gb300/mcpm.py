@@ -172,6 +172,7 @@ def load_library(path: str | None = None):
         "mcpm_stream_particles": (C.c_int, [vp]),
         "mcpm_end_step": (C.c_int, [vp]),
         "mcpm_step": (C.c_int, [vp, i32]),
+        "mcpm_step_async": (C.c_int, [vp, i32]),
         "mcpm_inject_normals": (C.c_int, [vp, i64, dp, dp, dp]),
         "mcpm_set_rng": (C.c_int, [vp, i32]),
         "mcpm_inject_uniforms": (C.c_int, [vp, i32, i64, dp]),
@@ -367,8 +368,11 @@ class Session:
         self.end_step()
         self.check_status()
 
-    def step(self, n=1):
-        self._ck(self.lib.mcpm_step(self.h, int(n)), "step")
+    def step(self, n=1, wait=True):
+        """n fused steps; with wait=False they are only queued, and the
+        device status is read by check_status (or the next waiting step)."""
+        fn = self.lib.mcpm_step if wait else self.lib.mcpm_step_async
+        self._ck(fn(self.h, int(n)), "step")
 
     # -- hooks
     def check_status(self):

@@ -445,6 +445,42 @@ def test_graph_replay_matches_eager_steps(cuda_ok, maker):
     assert a.kernel_launches - l0 >= 7 * 6
 
 
+@pytest.mark.parametrize("prec", [mcpm.FP64, mcpm.FP32])
+def test_queued_steps_match_and_report_status(cuda_ok, prec):
+    """mcpm_step_async queues the same steps as mcpm_step: a loop of queued
+    uploads, steps and downloads (the host never waiting) gives the arrays
+    of the same loop run call by call, and a NaN raised on the device is
+    reported by the next check_status, not by the queued step."""
+    cfg, parts = W.homogeneous_relaxation_1d(n_cells=20, ppc=60, precision=prec)
+    a, b = mcpm.Session(cfg), mcpm.Session(cfg)
+    outs = {}
+    for s, wait in ((a, True), (b, False)):
+        res = []
+        for i in range(3):
+            out = {k: np.zeros(len(parts["x2"])) for k in ("x1", "x2", "U1", "U2", "U3")}
+            s.upload(parts["x1"], parts["x2"], parts["U1"], parts["U2"], parts["U3"], wait=wait)
+            s.set_step(1 + 2 * i)
+            s.step(2, wait=wait)
+            s.download_into(out, wait=wait)
+            res.append(out)
+        s.sync()
+        s.check_status()
+        outs[wait] = res
+    tol = 1e-9 if prec == mcpm.FP64 else 1e-5
+    for ra, rb in zip(outs[True], outs[False]):
+        for k in ("x2", "U1", "U2", "U3"):
+            err = np.max(np.abs(ra[k] - rb[k])) / max(1.0, np.max(np.abs(ra[k])))
+            assert err <= tol, (k, err)
+    bad = {k: v.copy() for k, v in parts.items()}
+    bad["U2"][3] = np.nan
+    b.upload(bad["x1"], bad["x2"], bad["U1"], bad["U2"], bad["U3"])
+    b.check_status()
+    b.step(1, wait=False)
+    with pytest.raises(mcpm.MCPMError) as e:
+        b.check_status()
+    assert e.value.code & mcpm.ERR_NAN
+
+
 def _ragged_box(prec):
     """12 cells with very uneven occupancy -- an empty cell, small, warp-,
     block- and beyond-staging-sized cells (20 to 4,000) -- Maxwellian T = 1.
