@@ -160,7 +160,28 @@ def host_link_rates(stream, n_doubles):
         e1.record(stream)
         torch.cuda.synchronize()
         out[name] = round(3 * 8 * n_doubles / (e0.elapsed_time(e1) / 1e3) / 1e9, 1)
-    del h, d
+    # both directions at once (a second pair of buffers, a second stream):
+    # the floor of an e2e step whose upload and download overlap
+    h2 = torch.empty(n_doubles, dtype=torch.float64, pin_memory=True)
+    d2 = torch.empty(n_doubles, dtype=torch.float64, device="cuda")
+    side = torch.cuda.Stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    best = None
+    for _ in range(4):
+        torch.cuda.synchronize()
+        e0.record(stream)
+        side.wait_event(e0)
+        d.copy_(h, non_blocking=True)
+        with torch.cuda.stream(side):
+            h2.copy_(d2, non_blocking=True)
+        stream.wait_stream(side)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        best = ms if best is None else min(best, ms)
+    out["both_ms"] = round(best, 3)
+    out["both_GBs"] = round(2 * 8 * n_doubles / (best / 1e3) / 1e9, 1)
+    del h, d, h2, d2
     return out
 
 

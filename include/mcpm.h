@@ -328,8 +328,9 @@ int mcpm_step(mcpm_session* s, int32_t n_steps);
 /* The same steps, returning once they are queued: the host goes on (an
    upload or download of the next batch, mcpm_*_async) while the device
    steps.  The status bits stay on the device until mcpm_check_status or a
-   synchronous step reads them.  A judge step of an attached learned force
-   still waits for its verdict before the steps after it are queued. */
+   synchronous step reads them.  After a judge step of an attached learned
+   force the verdict is read (the host waits for the judge step) when the
+   next step is queued, or by mcpm_sync or mcpm_get_surrogate_stats. */
 int mcpm_step_async(mcpm_session* s, int32_t n_steps);
 
 /* ---- test and diagnostic hooks ---------------------------------------- */

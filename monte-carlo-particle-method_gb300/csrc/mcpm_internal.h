@@ -252,6 +252,8 @@ struct Session {
   bool sur_xin_ready = false;   // the nodal deposit also wrote the network input
   double* sur_err = nullptr;    // device [2]: sum |kick_net - kick_plain|^2, sum |kick_plain|^2
   double* sur_err_h = nullptr;  // pinned host copy
+  cudaEvent_t ev_judge = nullptr;  // recorded after the verdict's copy to sur_err_h
+  bool judge_pending = false;      // a judge step's verdict not yet read on the host
   double sur_last_err = -1.0;
   int64_t sur_judged = 0, sur_takeovers = 0, sur_steps = 0, sur_plain_steps = 0;
   std::string err;

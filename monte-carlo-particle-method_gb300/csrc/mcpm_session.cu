@@ -142,6 +142,7 @@ static inline bool is_fp_model(int m) {
 
 extern "C" {
 static int long_range_force(mcpm_session* s, bool branch = false);
+static int read_judge(mcpm_session* s);
 
 int mcpm_config_derive(mcpm_config* c, int64_t n_particles) {
   if (!c) return MCPM_ERR_ARG;
@@ -383,6 +384,7 @@ int mcpm_session_destroy(mcpm_session* s) {
   lr2d_free(*s);
   cudaFree(s->sur_err);
   if (s->sur_err_h) cudaFreeHost(s->sur_err_h);
+  if (s->ev_judge) cudaEventDestroy(s->ev_judge);
   if (s->graph) cudaGraphExecDestroy(s->graph);
   for (auto& r : s->prof_recs) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
   for (auto e : s->prof_pool) cudaEventDestroy(e);
@@ -413,6 +415,7 @@ int mcpm_sync(mcpm_session* s) {
   int rc = cuda_check(s, cudaStreamSynchronize(s->stream), "sync");
   if (!rc && s->d2h) rc = cuda_check(s, cudaStreamSynchronize(s->d2h), "sync (downloads)");
   if (!rc && s->h2d) rc = cuda_check(s, cudaStreamSynchronize(s->h2d), "sync (uploads)");
+  if (!rc) rc = read_judge(s);
   return rc;
 }
 
@@ -613,6 +616,7 @@ int mcpm_random_generator(mcpm_session* s) {
 
 int mcpm_velocity_update(mcpm_session* s) {
   if (!s || !s->sorted) return fail(s, MCPM_ERR_STATE, "velocity_update: call cell_update first");
+  if (int rc = read_judge(s)) return rc;  // a queued step's verdict picks the force
   int n = 0;
   uint32_t stages = 0;
   if (s->cfg.model == MCPM_MODEL_ESMC) n += T_ESMC(launch_esmc(*s));
@@ -869,9 +873,24 @@ static int run_steps(mcpm_session* s, int n_steps, uint32_t stages) {
 
 // the judge's verdict: relative L2 error of the network's kick against the
 // plain path's on the step just run
-static int read_judge(mcpm_session* s) {
+// the judge step's error sums go to the host behind the step; the verdict
+// is read when the next step (or a query) needs it, so that an end-to-end
+// loop queues the next batch's transfers before the host waits
+static int queue_judge(mcpm_session* s) {
+  if (!s->ev_judge) {
+    int rc = cuda_check(s, cudaEventCreateWithFlags(&s->ev_judge, cudaEventDisableTiming), "judge event");
+    if (rc) return rc;
+  }
   cudaMemcpyAsync(s->sur_err_h, s->sur_err, 16, cudaMemcpyDeviceToHost, s->stream);
-  int rc = cuda_check(s, cudaStreamSynchronize(s->stream), "judge");
+  int rc = cuda_check(s, cudaEventRecord(s->ev_judge, s->stream), "judge");
+  s->judge_pending = rc == MCPM_OK;
+  return rc;
+}
+
+static int read_judge(mcpm_session* s) {
+  if (!s->judge_pending) return MCPM_OK;
+  s->judge_pending = false;
+  int rc = cuda_check(s, cudaEventSynchronize(s->ev_judge), "judge");
   if (rc) return rc;
   const double se = s->sur_err_h[0], sp = s->sur_err_h[1];
   const double e = sp > 0.0 ? sqrt(se / sp) : (se > 0.0 ? INFINITY : 0.0);
@@ -882,8 +901,8 @@ static int read_judge(mcpm_session* s) {
   return MCPM_OK;
 }
 
-// queues n_steps iterations; a judge step of an attached learned force
-// reads its verdict on the host before the steps after it are queued
+// queues n_steps iterations; after a judge step of an attached learned
+// force the host reads the verdict before it queues the next step
 static int step_enqueue(mcpm_session* s, int32_t n_steps) {
   if (!s || !s->have_particles || n_steps < 0) return fail(s, MCPM_ERR_STATE, "step: no particles");
   const int m = s->cfg.model;
@@ -905,12 +924,13 @@ static int step_enqueue(mcpm_session* s, int32_t n_steps) {
   if (!s->need_old) stages &= ~ST_OLD;
   int it = 0, rc;
   while (it < n_steps) {
+    if ((rc = read_judge(s))) return rc;  // the last judge step's verdict picks this step's force
     if (s->sur && (s->step - 1) % s->sur_every == 0) {
       // judge step: both paths, the plain kick applied, eagerly
       s->sur_judge_now = true;
       rc = after_launch(s, step_once(s, stages), "step");
       s->sur_judge_now = false;
-      if (rc || (rc = read_judge(s))) return rc;
+      if (rc || (rc = queue_judge(s))) return rc;
       ++s->sur_plain_steps;
       ++it;
       continue;
@@ -925,7 +945,8 @@ static int step_enqueue(mcpm_session* s, int32_t n_steps) {
 }
 
 int mcpm_step(mcpm_session* s, int32_t n_steps) {
-  const int rc = step_enqueue(s, n_steps);
+  int rc = step_enqueue(s, n_steps);
+  if (!rc) rc = read_judge(s);
   return rc ? rc : mcpm_check_status(s);
 }
 
@@ -934,6 +955,7 @@ int mcpm_step_async(mcpm_session* s, int32_t n_steps) { return step_enqueue(s, n
 // ------------------------------------------------- learned Vlasov force
 int mcpm_attach_surrogate(mcpm_session* s, mcpm_surrogate* m, int32_t judge_every, double threshold) {
   if (!s) return MCPM_ERR_ARG;
+  if (int rc = read_judge(s)) return rc;
   if (!m) {
     s->sur = nullptr;
     s->sur_xin_ready = false;
@@ -962,6 +984,7 @@ int mcpm_attach_surrogate(mcpm_session* s, mcpm_surrogate* m, int32_t judge_ever
 
 int mcpm_get_surrogate_stats(mcpm_session* s, mcpm_surrogate_stats* out) {
   if (!s || !out) return MCPM_ERR_ARG;
+  if (int rc = read_judge(s)) return rc;
   out->last_error = s->sur_last_err;
   out->judged = s->sur_judged;
   out->takeovers = s->sur_takeovers;
